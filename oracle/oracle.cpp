@@ -1,0 +1,1051 @@
+// qed3 CPU ORACLE — test infrastructure only.
+//
+// This file is the FP64 CPU restatement of the reference's fermion hot path.
+// It is the checker the CUDA product is compared against; it is never linked
+// into, called by, or shipped with the product library.  Only tests/,
+// __graft_entry__.smoke() and bench.py's cpu_baseline / reference leg load it.
+//
+// Parity status: the reference cannot be built here
+// (Eigen, GSL, the QFE lattice library and its .dat geometry tables are all
+// absent), so geometry parity against the reference's own tables is UNPINNED.
+// The oracle is pinned instead by every invariant the reference asserts
+// (spin-structure consistency, face deficits, total area 4*pi, ell_A == ell_B),
+// by gamma5-hermiticity, by the free-spectrum known answers of
+// analysis/ev_dual.ipynb, and by the reference's own Zolotarev code, which
+// does compile and is checked against this restatement bit for bit.
+//
+// Each block cites the reference file:line it restates.
+
+#include <algorithm>
+#include <array>
+#include <cassert>
+#include <cmath>
+#include <complex>
+#include <cstdint>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <random>
+#include <stdexcept>
+#include <string>
+#include <vector>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+using Idx = std::int32_t;
+using cplx = std::complex<double>;
+
+namespace {
+
+struct V3 {
+  double x, y, z;
+};
+inline V3 operator+(V3 a, V3 b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
+inline V3 operator-(V3 a, V3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+inline V3 operator*(double s, V3 a) { return {s * a.x, s * a.y, s * a.z}; }
+inline double dot(V3 a, V3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+inline V3 cross(V3 a, V3 b) {
+  return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
+}
+inline double norm(V3 a) { return std::sqrt(dot(a, a)); }
+
+// _acos with clamping, integrator/geodesic.h:119-127
+inline double acos_c(double a) {
+  if (a < -1.0) return M_PI;
+  if (a > 1.0) return 0.0;
+  return std::acos(a);
+}
+
+// Mod with floor, integrator/geodesic.h:38-43 (result in [0,b))
+inline double mod_floor(double a, double b = 2.0 * M_PI) {
+  const double p = std::floor(a / b);
+  return a - p * b;
+}
+// Mod with round, src/both_3d/dirac_dual.h:7-11 (result in [-b/2,b/2])
+inline double mod_round(double a, double b = 2.0 * M_PI) {
+  const double p = std::round(a / b);
+  return a - p * b;
+}
+
+// ---------------------------------------------------------------------------
+// Icosahedral refinement.  The reference takes vertex coordinates from the
+// absent QFE library (integrator/get_geometry.cc:43-59).  This build fixes its
+// own convention, shared with the product builder: a vertex at each pole, two
+// rings of five at z=+-1/sqrt(5) (the lower ring rotated by pi/5), each face
+// split into n^2 triangles on the flat barycentric grid, points projected
+// radially.  Vertex numbering: 12 icosahedron vertices, then edge interiors
+// (edges sorted by (min,max) vertex id, points from min toward max), then face
+// interiors (face order, i-major).  Triangle numbering: face-major, then
+// i-major, an "up" triangle followed by its "down" partner.
+// ---------------------------------------------------------------------------
+struct Icosa {
+  std::array<V3, 12> v;
+  std::array<std::array<int, 3>, 20> f;
+};
+
+Icosa make_icosa() {
+  Icosa ic;
+  const double zr = 1.0 / std::sqrt(5.0);
+  const double rr = 2.0 / std::sqrt(5.0);
+  ic.v[0] = {0.0, 0.0, 1.0};
+  for (int k = 0; k < 5; k++) {
+    const double p1 = 2.0 * M_PI * k / 5.0;
+    const double p2 = p1 + M_PI / 5.0;
+    ic.v[1 + k] = {rr * std::cos(p1), rr * std::sin(p1), zr};
+    ic.v[6 + k] = {rr * std::cos(p2), rr * std::sin(p2), -zr};
+  }
+  ic.v[11] = {0.0, 0.0, -1.0};
+  int nf = 0;
+  for (int k = 0; k < 5; k++) ic.f[nf++] = {0, 1 + k, 1 + (k + 1) % 5};
+  for (int k = 0; k < 5; k++) ic.f[nf++] = {1 + k, 6 + k, 1 + (k + 1) % 5};
+  for (int k = 0; k < 5; k++) ic.f[nf++] = {1 + (k + 1) % 5, 6 + k, 6 + (k + 1) % 5};
+  for (int k = 0; k < 5; k++) ic.f[nf++] = {11, 6 + (k + 1) % 5, 6 + k};
+  for (auto& t : ic.f) {
+    const V3 a = ic.v[t[0]], b = ic.v[t[1]], c = ic.v[t[2]];
+    if (dot(cross(b - a, c - a), a + b + c) < 0.0) std::swap(t[1], t[2]);
+  }
+  return ic;
+}
+
+inline V3 normalized(V3 p) {
+  const double r = std::sqrt(dot(p, p));
+  return (1.0 / r) * p;
+}
+
+// circumcenter, integrator/geodesic.h:72-83
+V3 circumcenter(V3 r0, V3 r1, V3 r2) {
+  const V3 r10 = r1 - r0;
+  const V3 r20 = r2 - r0;
+  const V3 tmp1 = dot(r10, r10) * r20 - dot(r20, r20) * r10;
+  const V3 cr = cross(r10, r20);
+  const V3 numer = cross(tmp1, cr);
+  const double denom = 2.0 * dot(cr, cr);
+  return (1.0 / denom) * numer + r0;
+}
+
+// spherical triangle area by L'Huilier, src/both_3d/s2n_dual.h:124-131
+double lhuilier(V3 x, V3 y, V3 p) {
+  const double a = std::acos(dot(x, p) / (norm(x) * norm(p)));
+  const double b = std::acos(dot(y, p) / (norm(y) * norm(p)));
+  const double c = std::acos(dot(x, y) / (norm(x) * norm(y)));
+  const double s = 0.5 * (a + b + c);
+  const double t = std::tan(0.5 * s) * std::tan(0.5 * (s - a)) * std::tan(0.5 * (s - b)) *
+                   std::tan(0.5 * (s - c));
+  return 4.0 * std::atan(std::sqrt(t));
+}
+
+// Spatial hash used only to accelerate the reference's all-pairs threshold
+// scans (integrator/get_geometry.cc:130-146, 190-201, 222-232); the
+// acceptance criterion is unchanged.
+struct Grid {
+  double h;
+  int nc;
+  std::vector<std::vector<Idx>> cells;
+  explicit Grid(const std::vector<V3>& pts, double h_) : h(h_) {
+    nc = std::max(1, int(std::ceil(2.0 / h)) + 1);
+    cells.assign(size_t(nc) * nc * nc, {});
+    for (Idx i = 0; i < Idx(pts.size()); i++) cells[cell(pts[i])].push_back(i);
+  }
+  int ci(double c) const { return std::min(nc - 1, std::max(0, int(std::floor((c + 1.0) / h)))); }
+  size_t cell(V3 p) const { return (size_t(ci(p.x)) * nc + ci(p.y)) * nc + ci(p.z); }
+  template <class F>
+  void near(V3 p, F&& f) const {
+    const int cx = ci(p.x), cy = ci(p.y), cz = ci(p.z);
+    for (int a = std::max(0, cx - 1); a <= std::min(nc - 1, cx + 1); a++)
+      for (int b = std::max(0, cy - 1); b <= std::min(nc - 1, cy + 1); b++)
+        for (int c = std::max(0, cz - 1); c <= std::min(nc - 1, cz + 1); c++)
+          for (Idx j : cells[(size_t(a) * nc + b) * nc + c]) f(j);
+  }
+};
+
+// Gauss-Legendre nodes/weights on [-1,1] by Newton iteration.
+void gauss_legendre(int n, std::vector<double>& x, std::vector<double>& w) {
+  x.resize(n);
+  w.resize(n);
+  for (int i = 0; i < n; i++) {
+    double z = std::cos(M_PI * (i + 0.75) / (n + 0.5));
+    for (int it = 0; it < 100; it++) {
+      double p0 = 1.0, p1 = z;
+      for (int k = 2; k <= n; k++) {
+        const double p2 = ((2.0 * k - 1.0) * z * p1 - (k - 1.0) * p0) / k;
+        p0 = p1;
+        p1 = p2;
+      }
+      const double dp = n * (z * p1 - p0) / (z * z - 1.0);
+      const double dz = p1 / dp;
+      z -= dz;
+      if (std::abs(dz) < 1e-16) break;
+    }
+    double p0 = 1.0, p1 = z;
+    for (int k = 2; k <= n; k++) {
+      const double p2 = ((2.0 * k - 1.0) * z * p1 - (k - 1.0) * p0) / k;
+      p0 = p1;
+      p1 = p2;
+    }
+    const double dp = n * (z * p1 - p0) / (z * z - 1.0);
+    x[i] = z;
+    w[i] = 2.0 / ((1.0 - z * z) * dp * dp);
+  }
+}
+
+// polar angles of a point, integrator/geodesic.h:135-176 (atan2 form; the
+// reference's acos form loses ~1e-8 near phi = 0, pi)
+inline void polar(V3 p, double& th, double& ph) {
+  th = std::atan2(std::sqrt(p.x * p.x + p.y * p.y), p.z);
+  ph = std::atan2(p.y, p.x);
+}
+// local frame e_theta, e_phi, integrator/geodesic.h:221-258
+inline V3 e_theta(double th, double ph) {
+  return {std::cos(th) * std::cos(ph), std::cos(th) * std::sin(ph), -std::sin(th)};
+}
+inline V3 e_phi(double /*th*/, double ph) { return {-std::sin(ph), std::cos(ph), 0.0}; }
+
+// tangent angle of direction t at point p (alpha in [-pi,pi]),
+// integrator/test_sorting.cc:260-272
+double tangent_angle(V3 p, V3 t) {
+  double th, ph;
+  polar(p, th, ph);
+  const double c0 = dot(t, e_theta(th, ph));
+  const double c1 = dot(t, e_phi(th, ph));
+  // the reference's acos(e0)*sign(e1) of the unit tangent, evaluated as
+  // atan2 so that angles near 0 and pi keep full precision
+  return std::atan2(c1, c0);
+}
+
+}  // namespace
+
+// ===========================================================================
+// Geometry: S2Simp + S2Trivalent (src/both_3d/s2n_simp.h:43-402,
+// src/both_3d/s2n_dual.h:49-166) generated as integrator/get_geometry.cc and
+// integrator/test_sorting.cc do.
+// ===========================================================================
+struct OracleGeom {
+  int n = 0;
+  std::vector<V3> simp_sites;                 // 10n^2+2
+  std::vector<std::array<Idx, 3>> simp_faces;  // 20n^2 triangles
+  std::vector<V3> sites;                      // dual sites = triangles, 20n^2
+  std::vector<std::array<Idx, 3>> nns;        // sorted ascending
+  std::vector<std::array<Idx, 2>> links;      // dual links (i<j), lexicographic
+  std::vector<std::array<Idx, 2>> simp_links; // dual of each link (min,max)
+  std::vector<std::vector<Idx>> faces;        // dual faces, one per simp vertex
+  std::vector<double> ell, link_volume, vols;
+  double mean_ell = 0, mean_link_volume = 0, mean_vol = 0;
+  std::vector<double> omega;                  // per link (i<j): omega(i,j)
+  std::vector<std::array<double, 3>> alpha;   // alpha(x, nns[x][k])
+  std::vector<std::array<Idx, 3>> hop_link;   // link id of hop (x, nns[x][k])
+  std::vector<std::array<int, 3>> hop_sign;   // +1 if x<y
+  std::map<std::pair<Idx, Idx>, Idx> map2il;
+};
+
+static void build_vertices(OracleGeom& g, const Icosa& ic) {
+  const int n = g.n;
+  g.simp_sites.clear();
+  for (int i = 0; i < 12; i++) g.simp_sites.push_back(ic.v[i]);
+  // edges sorted (min,max)
+  std::vector<std::array<int, 2>> edges;
+  for (auto& t : ic.f)
+    for (int e = 0; e < 3; e++) {
+      int a = t[e], b = t[(e + 1) % 3];
+      if (a > b) std::swap(a, b);
+      edges.push_back({a, b});
+    }
+  std::sort(edges.begin(), edges.end());
+  edges.erase(std::unique(edges.begin(), edges.end()), edges.end());
+  std::map<std::pair<int, int>, Idx> edge_base;
+  for (auto& e : edges) {
+    edge_base[{e[0], e[1]}] = Idx(g.simp_sites.size());
+    for (int t = 1; t < n; t++) {
+      const V3 p = double(n - t) * ic.v[e[0]] + double(t) * ic.v[e[1]];
+      g.simp_sites.push_back(normalized(p));
+    }
+  }
+  // per-face lookup of (i,j) -> vertex id
+  g.simp_faces.clear();
+  for (int f = 0; f < 20; f++) {
+    const int A = ic.f[f][0], B = ic.f[f][1], C = ic.f[f][2];
+    const V3 a = ic.v[A], b = ic.v[B], c = ic.v[C];
+    std::vector<Idx> interior_base;
+    std::map<std::pair<int, int>, Idx> loc;
+    for (int i = 1; i <= n - 2; i++)
+      for (int j = 1; j <= n - 1 - i; j++) {
+        const V3 p = double(n - i - j) * a + double(i) * b + double(j) * c;
+        loc[{i, j}] = Idx(g.simp_sites.size());
+        g.simp_sites.push_back(normalized(p));
+      }
+    auto edge_pt = [&](int u, int v, int t) -> Idx {  // point t steps from u toward v
+      if (t == 0) return u;
+      if (t == n) return v;
+      if (u < v) return edge_base.at({u, v}) + (t - 1);
+      return edge_base.at({v, u}) + (n - t - 1);
+    };
+    auto P = [&](int i, int j) -> Idx {
+      if (i == 0 && j == 0) return A;
+      if (j == 0) return edge_pt(A, B, i);
+      if (i == 0) return edge_pt(A, C, j);
+      if (i + j == n) return edge_pt(B, C, j);
+      return loc.at({i, j});
+    };
+    for (int i = 0; i < n; i++)
+      for (int j = 0; j < n - i; j++) {
+        g.simp_faces.push_back({P(i, j), P(i + 1, j), P(i, j + 1)});
+        if (i + j <= n - 2) g.simp_faces.push_back({P(i + 1, j), P(i + 1, j + 1), P(i, j + 1)});
+      }
+  }
+}
+
+extern "C" {
+
+// Build the lattice for refinement n.  Returns nullptr on a failed check.
+OracleGeom* orc_geom_create(int n) {
+  if (n < 1) return nullptr;
+  auto* g = new OracleGeom;
+  g->n = n;
+  const Icosa ic = make_icosa();
+  build_vertices(*g, ic);
+  const Idx Nv = Idx(g->simp_sites.size());
+  const Idx Ns = Idx(g->simp_faces.size());
+  if (Nv != 10 * n * n + 2 || Ns != 20 * n * n) {
+    delete g;
+    return nullptr;
+  }
+  // dual sites: normalised circumcentres, integrator/get_geometry.cc:86-112
+  std::vector<std::vector<Idx>> ring_unsorted(Nv);
+  g->sites.resize(Ns);
+  for (Idx t = 0; t < Ns; t++) {
+    const auto& fc = g->simp_faces[t];
+    ring_unsorted[fc[0]].push_back(t);
+    ring_unsorted[fc[1]].push_back(t);
+    ring_unsorted[fc[2]].push_back(t);
+    const V3 p = circumcenter(g->simp_sites[fc[0]], g->simp_sites[fc[1]], g->simp_sites[fc[2]]);
+    g->sites[t] = (1.0 / norm(p)) * p;
+  }
+  // dual links and neighbours by the geodesic threshold,
+  // integrator/get_geometry.cc:127-146, 206-220
+  const double thr = 0.42188 * 2.0 / n;
+  {
+    Grid grid(g->sites, thr * 1.01);
+    std::vector<std::vector<Idx>> nb(Ns);
+    for (Idx i = 0; i < Ns; i++) {
+      grid.near(g->sites[i], [&](Idx j) {
+        if (j == i) return;
+        if (acos_c(dot(g->sites[i], g->sites[j])) < thr) nb[i].push_back(j);
+      });
+    }
+    g->nns.resize(Ns);
+    for (Idx i = 0; i < Ns; i++) {
+      std::sort(nb[i].begin(), nb[i].end());
+      if (nb[i].size() != 3) {
+        std::fprintf(stderr, "oracle: site %d has %zu neighbours\n", i, nb[i].size());
+        delete g;
+        return nullptr;
+      }
+      g->nns[i] = {nb[i][0], nb[i][1], nb[i][2]};
+      for (Idx j : nb[i])
+        if (j > i) g->links.push_back({i, j});
+    }
+  }
+  const Idx Nl = Idx(g->links.size());
+  for (Idx l = 0; l < Nl; l++) {
+    g->map2il[{g->links[l][0], g->links[l][1]}] = l;
+    g->map2il[{g->links[l][1], g->links[l][0]}] = l;
+  }
+  // simplicial link dual to each dual link (Euclidean threshold),
+  // integrator/get_geometry.cc:179-202
+  {
+    Grid grid(g->simp_sites, thr * 1.01);
+    g->simp_links.resize(Nl);
+    for (Idx l = 0; l < Nl; l++) {
+      const V3 x1 = g->sites[g->links[l][0]], x2 = g->sites[g->links[l][1]];
+      std::vector<Idx> tmp;
+      grid.near(x1, [&](Idx ip) {
+        const V3 x0 = g->simp_sites[ip];
+        if (norm(x0 - x1) < thr && norm(x0 - x2) < thr) tmp.push_back(ip);
+      });
+      if (tmp.size() != 2) {
+        delete g;
+        return nullptr;
+      }
+      g->simp_links[l] = {std::min(tmp[0], tmp[1]), std::max(tmp[0], tmp[1])};
+    }
+  }
+  // dual faces by the oriented ring walk, integrator/get_geometry.cc:252-339
+  g->faces.resize(Nv);
+  for (Idx v = 0; v < Nv; v++) {
+    const auto& ru = ring_unsorted[v];
+    std::vector<std::array<Idx, 2>> facelink;
+    for (size_t i = 0; i < ru.size(); i++)
+      for (size_t j = i + 1; j < ru.size(); j++) {
+        if (g->map2il.count({ru[i], ru[j]})) facelink.push_back({ru[i], ru[j]});
+      }
+    std::vector<Idx> face;
+    size_t il = 0;
+    while (true) {
+      const auto fl = facelink[il];
+      facelink.erase(facelink.begin() + il);
+      const V3 x0 = g->simp_sites[v], x1 = g->sites[fl[0]], x2 = g->sites[fl[1]];
+      const int sign = dot(cross(x1 - x0, x2 - x1), x0) < 0.0 ? -1 : 1;
+      const std::array<Idx, 2> sg = sign < 0 ? std::array<Idx, 2>{fl[1], fl[0]} : fl;
+      face.push_back(sg[0]);
+      if (facelink.empty()) break;
+      const Idx next = sg[1];
+      for (size_t jl = 0; jl < facelink.size(); jl++)
+        if (facelink[jl][0] == next || facelink[jl][1] == next) il = jl;
+    }
+    g->faces[v] = face;
+  }
+  // ell and link volumes, src/both_3d/s2n_dual.h:109-166
+  g->ell.resize(Nl);
+  g->link_volume.resize(Nl);
+  for (Idx l = 0; l < Nl; l++) {
+    const V3 x = g->sites[g->links[l][0]], y = g->sites[g->links[l][1]];
+    const V3 pA = g->simp_sites[g->simp_links[l][0]], pB = g->simp_sites[g->simp_links[l][1]];
+    const double ellA = std::acos(dot(x, y) / (norm(x) * norm(y)));
+    g->ell[l] = ellA;
+    g->link_volume[l] = lhuilier(x, y, pA) + lhuilier(x, y, pB);
+  }
+  double s = 0;
+  for (double e : g->link_volume) s += e;
+  g->mean_link_volume = s / Nl;
+  s = 0;
+  for (double e : g->ell) s += e;
+  g->mean_ell = s / Nl;
+  // dual face areas, src/both_3d/s2n_simp.h:366-402
+  g->vols.resize(Nv);
+  for (Idx v = 0; v < Nv; v++) {
+    double area = 0;
+    const auto& f = g->faces[v];
+    for (size_t i = 0; i < f.size(); i++)
+      area += lhuilier(g->sites[f[i]], g->sites[f[(i + 1) % f.size()]], g->simp_sites[v]);
+    g->vols[v] = area;
+  }
+  s = 0;
+  for (double e : g->vols) s += e;
+  g->mean_vol = s / Nv;
+
+  // spin connection: omega = int cos(theta) dphi along the geodesic,
+  // integrator/test_sorting.cc:139-235 (own Gauss-Legendre quadrature in
+  // place of GSL QAG), section cut at phi0 = pi/48 (:203-235);
+  // alpha from the geodesic tangents (:240-289).
+  std::vector<double> glx, glw;
+  gauss_legendre(48, glx, glw);
+  g->omega.resize(Nl);
+  std::vector<double> alpha0(Nl), alpha1(Nl);
+  for (Idx l = 0; l < Nl; l++) {
+    const V3 x = g->sites[g->links[l][0]], y = g->sites[g->links[l][1]];
+    const double c = dot(x, y);
+    V3 t = y - c * x;
+    t = (1.0 / norm(t)) * t;
+    // arc length to integrate over: atan2 form (acos(x.y) loses ~1e-13 at
+    // n=64 on links near the poles, where dphi/ds is large)
+    const double L = std::atan2(norm(cross(x, y)), c);
+    double acc = 0;
+    for (size_t q = 0; q < glx.size(); q++) {
+      const double sq = 0.5 * L * (glx[q] + 1.0);
+      const V3 gm = std::cos(sq) * x + std::sin(sq) * t;
+      const V3 gd = (-std::sin(sq)) * x + std::cos(sq) * t;
+      const double rho2 = gm.x * gm.x + gm.y * gm.y;
+      const double dphi = (gm.x * gd.y - gm.y * gd.x) / rho2;
+      acc += glw[q] * gm.z * dphi;
+    }
+    g->omega[l] = 0.5 * L * acc;
+    alpha0[l] = tangent_angle(x, t);
+    const V3 tend = (-std::sin(L)) * x + std::cos(L) * t;
+    alpha1[l] = mod_floor(tangent_angle(y, tend) + M_PI);
+  }
+  {
+    const double phi0 = M_PI / 48.0;
+    for (const V3& p : g->sites) {
+      double th, ph;
+      polar(p, th, ph);
+      if (!(std::abs(mod_floor(ph) - phi0) > 1e-6)) {
+        delete g;
+        return nullptr;
+      }
+    }
+    for (Idx l = 0; l < Nl; l++) {
+      double th1, ph1, th2, ph2;
+      polar(g->sites[g->links[l][0]], th1, ph1);
+      polar(g->sites[g->links[l][1]], th2, ph2);
+      double d1 = ph1 - phi0, d2 = ph2 - phi0, d = ph1 - ph2;
+      auto wrap = [](double& a) {
+        if (a >= M_PI) a -= 2.0 * M_PI;
+        else if (a < -M_PI) a += 2.0 * M_PI;
+      };
+      wrap(d1);
+      wrap(d2);
+      wrap(d);
+      if (std::abs(d1) + std::abs(d2) - std::abs(d) < 1e-6) g->omega[l] -= 2.0 * M_PI;
+    }
+  }
+  g->alpha.resize(Ns);
+  g->hop_link.resize(Ns);
+  g->hop_sign.resize(Ns);
+  for (Idx x = 0; x < Ns; x++)
+    for (int k = 0; k < 3; k++) {
+      const Idx y = g->nns[x][k];
+      const Idx l = g->map2il.at({x, y});
+      g->hop_link[x][k] = l;
+      g->hop_sign[x][k] = x < y ? 1 : -1;
+      g->alpha[x][k] = x < y ? alpha0[l] : alpha1[l];
+    }
+  return g;
+}
+
+void orc_geom_destroy(OracleGeom* g) { delete g; }
+
+void orc_geom_sizes(const OracleGeom* g, int* n_sites, int* n_links, int* n_faces, int* n_simp_sites,
+                    int* face_total) {
+  *n_sites = int(g->sites.size());
+  *n_links = int(g->links.size());
+  *n_faces = int(g->faces.size());
+  *n_simp_sites = int(g->simp_sites.size());
+  int t = 0;
+  for (auto& f : g->faces) t += int(f.size());
+  *face_total = t;
+}
+
+void orc_geom_get(const OracleGeom* g, double* sites, int* nns, int* links, int* simp_links,
+                  double* simp_sites, int* face_offsets, int* face_sites, double* ell,
+                  double* link_volume, double* vols, double* omega, double* alpha, double* means) {
+  const size_t Ns = g->sites.size(), Nl = g->links.size(), Nv = g->simp_sites.size();
+  for (size_t i = 0; i < Ns; i++) {
+    sites[3 * i] = g->sites[i].x;
+    sites[3 * i + 1] = g->sites[i].y;
+    sites[3 * i + 2] = g->sites[i].z;
+    for (int k = 0; k < 3; k++) {
+      nns[3 * i + k] = g->nns[i][k];
+      alpha[3 * i + k] = g->alpha[i][k];
+    }
+  }
+  for (size_t l = 0; l < Nl; l++) {
+    links[2 * l] = g->links[l][0];
+    links[2 * l + 1] = g->links[l][1];
+    simp_links[2 * l] = g->simp_links[l][0];
+    simp_links[2 * l + 1] = g->simp_links[l][1];
+    ell[l] = g->ell[l];
+    link_volume[l] = g->link_volume[l];
+    omega[l] = g->omega[l];
+  }
+  int off = 0;
+  for (size_t v = 0; v < Nv; v++) {
+    simp_sites[3 * v] = g->simp_sites[v].x;
+    simp_sites[3 * v + 1] = g->simp_sites[v].y;
+    simp_sites[3 * v + 2] = g->simp_sites[v].z;
+    face_offsets[v] = off;
+    for (Idx s : g->faces[v]) face_sites[off++] = s;
+    vols[v] = g->vols[v];
+  }
+  face_offsets[Nv] = off;
+  means[0] = g->mean_ell;
+  means[1] = g->mean_link_volume;
+  means[2] = g->mean_vol;
+}
+
+// Spin-structure check, src/both_3d/dirac_dual.h:90-102; returns max |Mod(diff)|.
+double orc_check_spin_structure(const OracleGeom* g) {
+  double worst = 0;
+  const Idx Ns = Idx(g->sites.size());
+  for (Idx x = 0; x < Ns; x++)
+    for (int k = 0; k < 3; k++) {
+      const Idx y = g->nns[x][k];
+      int ky = 0;
+      while (g->nns[y][ky] != x) ky++;
+      const double a1 = g->alpha[x][k], a2 = g->alpha[y][ky];
+      const Idx l = g->hop_link[x][k];
+      const double om = g->hop_sign[x][k] * g->omega[l];
+      worst = std::max(worst, std::abs(mod_round(a2 + M_PI + om - a1)));
+    }
+  return worst;
+}
+
+// Deficit check, integrator/test_sorting.cc:392-426: returns the number of
+// faces violating -1.5*4pi/|face| < Mod(sum omega, 4pi) < 0, and writes each
+// face's representative sum.
+int orc_check_deficits(const OracleGeom* g, double* sums) {
+  int bad = 0;
+  for (size_t v = 0; v < g->faces.size(); v++) {
+    const auto& f = g->faces[v];
+    const V3 x0 = g->simp_sites[v], x1 = g->sites[f[0]], x2 = g->sites[f[1]];
+    const int sign = dot(cross(x1 - x0, x2 - x1), x0) < 0 ? -1 : 1;
+    double sum = 0;
+    for (size_t i = 0; i < f.size(); i++) {
+      const Idx a = f[i], b = f[(i + 1) % f.size()];
+      const Idx l = g->map2il.at({a, b});
+      sum += (a < b ? 1.0 : -1.0) * g->omega[l];
+    }
+    sum *= sign;
+    double m = mod_floor(sum, 4.0 * M_PI);
+    if (m > 2.0 * M_PI) m -= 4.0 * M_PI;
+    if (sums) sums[v] = m;
+    if (!(-1.5 * 4.0 * M_PI / f.size() < m && m < 0.0)) bad++;
+  }
+  return bad;
+}
+
+// ===========================================================================
+// Wilson-Dirac operator: DiracS2Dual + DiracExt at Nt=1
+// (src/both_3d/dirac_dual.h:108-116,208-214, src/both_3d/dirac_ext.h:49-155)
+// assembled as the reference's COO list and permuted into CSR of D and of
+// D^dagger as DWDevice does (src/both_3d/sparse_dirac.h:52-151).  The CSR
+// build is O(nnz) instead of the reference's O(N*nnz) scan; entry order per
+// row is the reference's.
+// ===========================================================================
+struct OracleDirac {
+  Idx N = 0;  // 2*Ns
+  std::vector<Idx> rows, cols, rowsT, colsT;
+  std::vector<cplx> val, valH;
+  std::vector<Idx> is, js;
+  std::vector<Idx> ell2em, ell2emT;
+  std::vector<cplx> coo;
+  double r = 1.0, M5 = 0.0;
+  std::vector<double> kappa;
+};
+
+static void hop_matrix(const OracleGeom* g, const OracleDirac* d, Idx x, int k, double A_xy,
+                       cplx H[4]) {
+  const Idx l = g->hop_link[x][k];
+  const double om = g->hop_sign[x][k] * g->omega[l];
+  const double al = g->alpha[x][k];
+  const double kap = d->kappa[l];
+  const cplx I(0.0, 1.0);
+  // (-r sigma0 + cos(al) sigma1 + sin(al) sigma2)
+  const cplx G[4] = {-d->r, cplx(std::cos(al), -std::sin(al)), cplx(std::cos(al), std::sin(al)), -d->r};
+  const cplx ph = std::exp(I * A_xy);
+  // Omega = cos(om/2) - i sin(om/2) sigma3 = diag(e^{-i om/2}, e^{+i om/2})
+  const cplx O0(std::cos(0.5 * om), -std::sin(0.5 * om)), O1(std::cos(0.5 * om), std::sin(0.5 * om));
+  H[0] = 0.5 * kap * G[0] * ph * O0;
+  H[1] = 0.5 * kap * G[1] * ph * O1;
+  H[2] = 0.5 * kap * G[2] * ph * O0;
+  H[3] = 0.5 * kap * G[3] * ph * O1;
+}
+
+OracleDirac* orc_dirac_create(const OracleGeom* g, double r, double M5) {
+  auto* d = new OracleDirac;
+  d->r = r;
+  d->M5 = M5;
+  const Idx Ns = Idx(g->sites.size()), Nl = Idx(g->links.size());
+  d->N = 2 * Ns;
+  d->kappa.resize(Nl);
+  for (Idx l = 0; l < Nl; l++) d->kappa[l] = 2.0 * g->link_volume[l] / g->ell[l] / g->mean_ell;
+  // coo_structure, src/both_3d/dirac_ext.h:49-116 with Nt=1 (N == Nx)
+  const Idx len = 12 * Ns + 8 * Ns + 4 * Ns;
+  d->is.resize(len);
+  d->js.resize(len);
+  const Idx N = d->N;
+  for (Idx x = 0; x < Ns; x++) {
+    Idx c = 12 * x;
+    for (int k = 0; k < 3; k++) {
+      const Idx y = g->nns[x][k];
+      d->is[c] = 2 * x; d->js[c++] = 2 * y;
+      d->is[c] = 2 * x; d->js[c++] = 2 * y + 1;
+      d->is[c] = 2 * x + 1; d->js[c++] = 2 * y;
+      d->is[c] = 2 * x + 1; d->js[c++] = 2 * y + 1;
+    }
+  }
+  for (Idx x = 0; x < Ns; x++) {
+    Idx c = 12 * Ns + 8 * x;
+    const Idx a = (N + 2 * x) % N, b = (2 * x - N + N) % N;
+    d->is[c] = a; d->js[c++] = 2 * x;
+    d->is[c] = a; d->js[c++] = 2 * x + 1;
+    d->is[c] = b; d->js[c++] = 2 * x;
+    d->is[c] = b; d->js[c++] = 2 * x + 1;
+    d->is[c] = a + 1; d->js[c++] = 2 * x;
+    d->is[c] = a + 1; d->js[c++] = 2 * x + 1;
+    d->is[c] = b + 1; d->js[c++] = 2 * x;
+    d->is[c] = b + 1; d->js[c++] = 2 * x + 1;
+  }
+  for (Idx x = 0; x < Ns; x++) {
+    Idx c = 20 * Ns + 4 * x;
+    d->is[c] = 2 * x; d->js[c++] = 2 * x;
+    d->is[c] = 2 * x; d->js[c++] = 2 * x + 1;
+    d->is[c] = 2 * x + 1; d->js[c++] = 2 * x;
+    d->is[c] = 2 * x + 1; d->js[c++] = 2 * x + 1;
+  }
+  // CSR of D and D^T, entries of a row in COO order
+  std::vector<Idx> cnt(N + 1, 0), cntT(N + 1, 0);
+  for (Idx e = 0; e < len; e++) {
+    cnt[d->is[e] + 1]++;
+    cntT[d->js[e] + 1]++;
+  }
+  for (Idx i = 0; i < N; i++) {
+    cnt[i + 1] += cnt[i];
+    cntT[i + 1] += cntT[i];
+  }
+  d->rows = cnt;
+  d->rowsT = cntT;
+  d->cols.resize(len);
+  d->colsT.resize(len);
+  d->ell2em.resize(len);
+  d->ell2emT.resize(len);
+  std::vector<Idx> pos(cnt.begin(), cnt.end() - 1), posT(cntT.begin(), cntT.end() - 1);
+  for (Idx e = 0; e < len; e++) {
+    const Idx em = pos[d->is[e]]++;
+    d->ell2em[e] = em;
+    d->cols[em] = d->js[e];
+    const Idx emT = posT[d->js[e]]++;
+    d->ell2emT[e] = emT;
+    d->colsT[emT] = d->is[e];
+  }
+  d->val.assign(len, 0.0);
+  d->valH.assign(len, 0.0);
+  d->coo.assign(len, 0.0);
+  return d;
+}
+
+void orc_dirac_destroy(OracleDirac* d) { delete d; }
+
+// coo_format (src/both_3d/dirac_ext.h:122-213, Nt=1) + coo2csr_csrH
+// (src/both_3d/sparse_dirac.h:132-151).  A[l] is the link angle of links[l]
+// oriented (min,max); hop (x,y) uses +A if x<y (GaugeExt::sp,
+// src/both_3d/gauge_ext.h:45-49).
+void orc_dirac_update(OracleDirac* d, const OracleGeom* g, const double* A) {
+  const Idx Ns = Idx(g->sites.size());
+  for (Idx x = 0; x < Ns; x++) {
+    Idx c = 12 * x;
+    for (int k = 0; k < 3; k++) {
+      const Idx l = g->hop_link[x][k];
+      cplx H[4];
+      hop_matrix(g, d, x, k, g->hop_sign[x][k] * A[l], H);
+      for (int e = 0; e < 4; e++) d->coo[c++] = H[e];
+    }
+  }
+  for (Idx x = 0; x < Ns; x++)
+    for (int e = 0; e < 8; e++) d->coo[12 * Ns + 8 * x + e] = 0.0;  // kappa_t = 0 at Nt=1
+  for (Idx x = 0; x < Ns; x++) {
+    double coeff = 0.0;
+    for (int k = 0; k < 3; k++) coeff += 0.5 * d->r * d->kappa[g->hop_link[x][k]];
+    coeff += d->M5;
+    Idx c = 20 * Ns + 4 * x;
+    d->coo[c++] = coeff;
+    d->coo[c++] = 0.0;
+    d->coo[c++] = 0.0;
+    d->coo[c++] = coeff;
+  }
+  const Idx len = Idx(d->coo.size());
+  for (Idx e = 0; e < len; e++) {
+    d->val[d->ell2em[e]] = d->coo[e];
+    d->valH[d->ell2emT[e]] = std::conj(d->coo[e]);
+  }
+}
+
+// Host CSR SpMV, src/dual/sparse_matrix.h:233-245 (OpenMP over rows).
+static void csr_mult(const OracleDirac* d, bool dag, cplx* res, const cplx* v) {
+  const std::vector<Idx>& rows = dag ? d->rowsT : d->rows;
+  const std::vector<Idx>& cols = dag ? d->colsT : d->cols;
+  const std::vector<cplx>& val = dag ? d->valH : d->val;
+  const Idx N = d->N;
+#pragma omp parallel for schedule(static)
+  for (Idx i = 0; i < N; i++) {
+    cplx acc = 0.0;
+    for (Idx jj = rows[i]; jj < rows[i + 1]; jj++) acc = acc + val[jj] * v[cols[jj]];
+    res[i] = acc;
+  }
+}
+
+// op: 0 = D, 1 = D^dagger, 2 = D^dagger D (D first, then D^dagger, as
+// DiracPf::DHD_deviceAsyncLaunch, src/both_3d/dirac_pf.h:66-71)
+void orc_dirac_apply(const OracleDirac* d, int op, double* out, const double* in) {
+  const cplx* v = reinterpret_cast<const cplx*>(in);
+  cplx* res = reinterpret_cast<cplx*>(out);
+  if (op == 0) csr_mult(d, false, res, v);
+  else if (op == 1) csr_mult(d, true, res, v);
+  else {
+    std::vector<cplx> t(d->N);
+    csr_mult(d, false, t.data(), v);
+    csr_mult(d, true, res, t.data());
+  }
+}
+
+void orc_dirac_get_csr(const OracleDirac* d, int* rows, int* cols, double* val) {
+  std::memcpy(rows, d->rows.data(), sizeof(Idx) * d->rows.size());
+  std::memcpy(cols, d->cols.data(), sizeof(Idx) * d->cols.size());
+  std::memcpy(val, d->val.data(), sizeof(cplx) * d->val.size());
+}
+int orc_dirac_nnz(const OracleDirac* d) { return int(d->val.size()); }
+void orc_dirac_get_kappa(const OracleDirac* d, double* kappa) {
+  std::memcpy(kappa, d->kappa.data(), sizeof(double) * d->kappa.size());
+}
+
+static cplx zdotc(const cplx* x, const cplx* y, Idx n) {
+  double re = 0, im = 0;
+#pragma omp parallel for reduction(+ : re, im) schedule(static)
+  for (Idx i = 0; i < n; i++) {
+    const cplx t = std::conj(x[i]) * y[i];
+    re += t.real();
+    im += t.imag();
+  }
+  return {re, im};
+}
+
+// CG on (D^dagger D + shift) x = b, restating MatPoly::solve
+// (src/dual/matpoly.h:204-267): x0 = 0, complex alpha = mu/<p,q>,
+// stop when |r|^2 < tol^2 |b|^2 on the recursive residual.
+// Returns iterations; writes the final mu and |b|^2.
+int orc_cg(const OracleDirac* d, double shift, double* x_out, const double* b_in, double tol,
+           int maxiter, double* mu_out) {
+  const Idx N = d->N;
+  const cplx* b = reinterpret_cast<const cplx*>(b_in);
+  cplx* x = reinterpret_cast<cplx*>(x_out);
+  std::vector<cplx> p(b, b + N), r(b, b + N), q(N), t(N);
+  for (Idx i = 0; i < N; i++) x[i] = 0.0;
+  double mu = zdotc(r.data(), r.data(), N).real();
+  double mu_old = mu;
+  const double mu_crit = tol * tol * mu;
+  int k = 0;
+  if (!(mu < mu_crit)) {
+    for (; k < maxiter; ++k) {
+      csr_mult(d, false, t.data(), p.data());
+      csr_mult(d, true, q.data(), t.data());
+      if (shift != 0.0)
+        for (Idx i = 0; i < N; i++) q[i] += shift * p[i];
+      const cplx gam = zdotc(p.data(), q.data(), N);
+      const cplx al = mu / gam;
+#pragma omp parallel for schedule(static)
+      for (Idx i = 0; i < N; i++) {
+        x[i] = al * p[i] + x[i];
+        r[i] = -al * q[i] + r[i];
+      }
+      mu = zdotc(r.data(), r.data(), N).real();
+      if (mu < mu_crit || std::isnan(mu)) break;
+      const double bet = mu / mu_old;
+      mu_old = mu;
+#pragma omp parallel for schedule(static)
+      for (Idx i = 0; i < N; i++) p[i] = bet * p[i] + r[i];
+    }
+  }
+  if (mu_out) *mu_out = mu;
+  return k + 1;
+}
+
+// ===========================================================================
+// Zolotarev rational approximation of sign(x) on [k,1], restating
+// src/both_3d/overlap.h:7-134 (A.D. Kennedy, hep-lat/0402038).
+// ===========================================================================
+static double orc_arithgeom(double z, double a, double b, double* agm, double& pb) {
+  if (b <= pb) {
+    pb = -1.0;
+    *agm = a;
+    return std::sin(z * a);
+  }
+  pb = b;
+  const double xi = orc_arithgeom(z, 0.5 * (a + b), std::sqrt(a * b), agm, pb);
+  return 2 * a * xi / ((a + b) + (a - b) * xi * xi);
+}
+
+static void orc_sncndnK(double z, double k, double& sn, double& cn, double& dn, double& K) {
+  double agm;
+  double pb = -1.0;
+  sn = orc_arithgeom(z, 1.0, std::sqrt(1.0 - k * k), &agm, pb);
+  K = M_PI / (2.0 * agm);
+  int sgn = ((int)(std::abs(z) / K)) % 4;
+  sgn ^= sgn >> 1;
+  sgn = 1 - ((sgn & 1) << 1);
+  cn = ((double)sgn) * std::sqrt(1.0 - sn * sn);
+  dn = std::sqrt(1.0 - k * k * sn * sn);
+}
+
+// out: c[size], cp[size], A[size], scal[4] = {M, lambda_inv, E, C}
+int orc_zolotarev(double k, int n, double* c, double* cp, double* A, double* scal) {
+  const int size = n / 2 + 1;
+  const double kp = std::sqrt(1.0 - k * k);
+  for (int m = 0; m < size; m++) c[m] = cp[m] = A[m] = 0.0;
+  double Kp = 1.0, xibar = 0.0;
+  for (int m = 0; m < size; m++) {
+    double sn, cn, dn;
+    double z = 2.0 * Kp * m / n;
+    orc_sncndnK(z, kp, sn, cn, dn, Kp);
+    if (m == 0) continue;
+    c[m] = -std::pow(cn / sn, 2);
+    z = 2.0 * Kp * (m - 0.5) / n;
+    orc_sncndnK(z, kp, sn, cn, dn, Kp);
+    cp[m] = -std::pow(cn / sn, 2);
+    if (m == 1) xibar = 1.0 / dn;
+  }
+  double M = 1.0;
+  for (int m = 1; m < size; m++) M *= (1.0 - c[m]) / (1.0 - cp[m]);
+  double lambda_inv = xibar / M;
+  for (int m = 1; m < size; m++)
+    lambda_inv *= (1.0 - c[m] * xibar * xibar) / (1.0 - cp[m] * xibar * xibar);
+  double E = 1.0;
+  for (int m = 1; m < size; m++) {
+    double numer = 1.0, denom = 1.0;
+    for (int l = 1; l < size; l++) {
+      numer *= k * k / cp[m] - k * k / c[l];
+      if (m != l) denom *= k * k / cp[m] - k * k / cp[l];
+    }
+    A[m] = numer / denom;
+    E *= c[m] / cp[m];
+  }
+  const double C = E * 2.0 / (1.0 + lambda_inv) / (k * M);
+  scal[0] = M;
+  scal[1] = lambda_inv;
+  scal[2] = E;
+  scal[3] = C;
+  return size;
+}
+
+// ===========================================================================
+// Gauge side: plaquette, Wilson action and force on the dual faces
+// (src/dual/gauge.h:90-110, src/both/action.h:21-48: weights mean_vol/vols).
+// compact: S = -beta sum w_p cos(theta_p); force_mode 0 = the reference's
+// (theta_p, src/dual/action.h:37), 1 = exact (sin theta_p).
+// ===========================================================================
+void orc_plaquettes(const OracleGeom* g, const double* A, double* theta) {
+  for (size_t v = 0; v < g->faces.size(); v++) {
+    const auto& f = g->faces[v];
+    double s = 0;
+    for (size_t i = 0; i < f.size(); i++) {
+      const Idx a = f[i], b = f[(i + 1) % f.size()];
+      const Idx l = g->map2il.at({a, b});
+      s += (a < b ? 1.0 : -1.0) * A[l];
+    }
+    theta[v] = s;
+  }
+}
+
+double orc_gauge_action(const OracleGeom* g, const double* A, double beta, int compact) {
+  std::vector<double> th(g->faces.size());
+  orc_plaquettes(g, A, th.data());
+  double res = 0;
+  for (size_t v = 0; v < th.size(); v++) {
+    const double w = g->mean_vol / g->vols[v];
+    if (compact) res += -w * std::cos(th[v]);
+    else res += 0.5 * w * th[v] * th[v];
+  }
+  return res * beta;
+}
+
+void orc_gauge_force(const OracleGeom* g, const double* A, double beta, int compact, int force_mode,
+                     double* F) {
+  const size_t Nl = g->links.size();
+  for (size_t l = 0; l < Nl; l++) F[l] = 0.0;
+  std::vector<double> th(g->faces.size());
+  orc_plaquettes(g, A, th.data());
+  for (size_t v = 0; v < g->faces.size(); v++) {
+    const auto& f = g->faces[v];
+    const double w = g->mean_vol / g->vols[v];
+    const double gr = w * ((compact && force_mode == 1) ? std::sin(th[v]) : th[v]);
+    for (size_t i = 0; i < f.size(); i++) {
+      const Idx a = f[i], b = f[(i + 1) % f.size()];
+      F[g->map2il.at({a, b})] += gr * (a < b ? 1.0 : -1.0);
+    }
+  }
+  for (size_t l = 0; l < Nl; l++) F[l] *= beta;
+}
+
+// ===========================================================================
+// RNG: ParallelRng2 (src/both/rng.h:76-125; ParallelRngExt at Nt=1,
+// src/both_3d/rng.h:90-129): master mt19937_64(seed) seeds one engine per link
+// then one per site; each engine owns its normal/uniform distributions.
+// ===========================================================================
+struct SingleRng {
+  std::mt19937_64 mt;
+  std::normal_distribution<double> g;
+  std::uniform_real_distribution<double> u;
+};
+struct OracleRng {
+  SingleRng master;
+  std::vector<SingleRng> links, sites;
+};
+
+OracleRng* orc_rng_create(int n_links, int n_sites, int seed) {
+  auto* r = new OracleRng;
+  r->links.resize(n_links);
+  r->sites.resize(n_sites);
+  r->master.mt.seed(seed);
+  for (auto& e : r->links) e.mt.seed(r->master.mt());
+  for (auto& e : r->sites) e.mt.seed(r->master.mt());
+  return r;
+}
+void orc_rng_destroy(OracleRng* r) { delete r; }
+void orc_rng_gaussian_links(OracleRng* r, double width, double* out) {
+  for (size_t l = 0; l < r->links.size(); l++) out[l] = width * r->links[l].g(r->links[l].mt);
+}
+// fill_gaussian, src/both_3d/rng.h:122-129: (g + i g)/sqrt(2) per spin
+void orc_rng_gaussian_spinor(OracleRng* r, double* out) {
+  for (size_t x = 0; x < r->sites.size(); x++)
+    for (int a = 0; a < 2; a++) {
+      auto& e = r->sites[x];
+      const double re = e.g(e.mt);
+      const double im = e.g(e.mt);
+      out[4 * x + 2 * a] = re / std::sqrt(2.0);
+      out[4 * x + 2 * a + 1] = im / std::sqrt(2.0);
+    }
+}
+double orc_rng_uniform(OracleRng* r) { return r->master.u(r->master.mt); }
+
+// HMCPureGauge::run, src/both_3d/hmc.h:212-296: leapfrog (half kick, drift,
+// half kick) nsteps times over tmax; Metropolis with the master uniform.
+// Returns 1 if accepted; writes dH.
+int orc_hmc_pure_gauge(const OracleGeom* g, OracleRng* rng, double* A, double beta, int compact,
+                       int force_mode, double tmax, int nsteps, int no_reject, double* dH_out) {
+  const size_t Nl = g->links.size();
+  std::vector<double> pi(Nl), F(Nl), A0(A, A + Nl);
+  orc_rng_gaussian_links(rng, 1.0, pi.data());
+  auto H = [&]() {
+    double s = 0;
+    for (double p : pi) s += p * p;
+    return 0.5 * s + orc_gauge_action(g, A, beta, compact);
+  };
+  const double h0 = H();
+  const double tau = tmax / nsteps;
+  for (int n = 0; n < nsteps; n++) {
+    orc_gauge_force(g, A, beta, compact, force_mode, F.data());
+    for (size_t l = 0; l < Nl; l++) pi[l] += -0.5 * tau * F[l];
+    for (size_t l = 0; l < Nl; l++) A[l] += tau * pi[l];
+    orc_gauge_force(g, A, beta, compact, force_mode, F.data());
+    for (size_t l = 0; l < Nl; l++) pi[l] += -0.5 * tau * F[l];
+  }
+  const double h1 = H();
+  const double dH = h1 - h0;
+  *dH_out = dH;
+  const double r = std::min(1.0, std::exp(-dH));
+  const double a = orc_rng_uniform(rng);
+  if (a < r || no_reject) return 1;
+  std::memcpy(A, A0.data(), sizeof(double) * Nl);
+  return 0;
+}
+
+// ===========================================================================
+// Wilson fermion force per link, restating DiracPf::grad_deviceAsyncLaunch
+// (src/both_3d/dirac_pf.h:107-122) with d_coo_format
+// (src/both_3d/dirac_ext.h:234-269): F_l = -2 Re <D eta, (dD/dA_l) eta>,
+// dD/dA_l = i H_xy at (x,y) and -i H_yx at (y,x) for links[l] = (x,y).
+// ===========================================================================
+void orc_fermion_force(const OracleDirac* d, const OracleGeom* g, const double* A, const double* eta_in,
+                       double* F) {
+  const Idx N = d->N;
+  const cplx* eta = reinterpret_cast<const cplx*>(eta_in);
+  std::vector<cplx> Deta(N);
+  csr_mult(d, false, Deta.data(), eta);
+  const cplx I(0.0, 1.0);
+  const Idx Nl = Idx(g->links.size());
+#pragma omp parallel for schedule(static)
+  for (Idx l = 0; l < Nl; l++) {
+    const Idx x = g->links[l][0], y = g->links[l][1];
+    int kx = 0, ky = 0;
+    while (g->nns[x][kx] != y) kx++;
+    while (g->nns[y][ky] != x) ky++;
+    cplx Hxy[4], Hyx[4];
+    hop_matrix(g, d, x, kx, A[l], Hxy);
+    hop_matrix(g, d, y, ky, -A[l], Hyx);
+    cplx dx0 = I * (Hxy[0] * eta[2 * y] + Hxy[1] * eta[2 * y + 1]);
+    cplx dx1 = I * (Hxy[2] * eta[2 * y] + Hxy[3] * eta[2 * y + 1]);
+    cplx dy0 = -I * (Hyx[0] * eta[2 * x] + Hyx[1] * eta[2 * x + 1]);
+    cplx dy1 = -I * (Hyx[2] * eta[2 * x] + Hyx[3] * eta[2 * x + 1]);
+    const cplx inner = std::conj(Deta[2 * x]) * dx0 + std::conj(Deta[2 * x + 1]) * dx1 +
+                       std::conj(Deta[2 * y]) * dy0 + std::conj(Deta[2 * y + 1]) * dy1;
+    F[l] = -2.0 * inner.real();
+  }
+}
+
+int orc_num_threads() {
+#ifdef _OPENMP
+  return omp_get_max_threads();
+#else
+  return 1;
+#endif
+}
+
+}  // extern "C"

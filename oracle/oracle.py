@@ -1,0 +1,313 @@
+"""ctypes binding of the CPU oracle (test infrastructure only).
+
+The oracle is the FP64 CPU restatement of the reference's fermion hot path
+(see oracle.cpp for the reference file:line of every routine).  Only tests,
+``__graft_entry__.smoke()`` and ``bench.py``'s CPU-baseline / reference legs
+may import this module; the product library never does.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+from dataclasses import dataclass
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB_PATH = os.path.join(_HERE, "_build", "liboracle.so")
+_lib = None
+
+c_double_p = ctypes.POINTER(ctypes.c_double)
+c_int_p = ctypes.POINTER(ctypes.c_int)
+
+
+def build(force: bool = False) -> str:
+    """Compile the oracle with its Makefile (a second or two)."""
+    if force or not os.path.exists(_LIB_PATH) or os.path.getmtime(_LIB_PATH) < os.path.getmtime(
+        os.path.join(_HERE, "oracle.cpp")
+    ):
+        subprocess.check_call(["make", "-s", "-C", _HERE])
+    return _LIB_PATH
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = ctypes.CDLL(_LIB_PATH)
+        vp = ctypes.c_void_p
+        L.orc_geom_create.restype = vp
+        L.orc_geom_create.argtypes = [ctypes.c_int]
+        L.orc_geom_destroy.argtypes = [vp]
+        L.orc_geom_sizes.argtypes = [vp] + [c_int_p] * 5
+        L.orc_geom_get.argtypes = [vp] + [ctypes.c_void_p] * 13
+        L.orc_check_spin_structure.restype = ctypes.c_double
+        L.orc_check_spin_structure.argtypes = [vp]
+        L.orc_check_deficits.restype = ctypes.c_int
+        L.orc_check_deficits.argtypes = [vp, c_double_p]
+        L.orc_dirac_create.restype = vp
+        L.orc_dirac_create.argtypes = [vp, ctypes.c_double, ctypes.c_double]
+        L.orc_dirac_destroy.argtypes = [vp]
+        L.orc_dirac_update.argtypes = [vp, vp, c_double_p]
+        L.orc_dirac_apply.argtypes = [vp, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]
+        L.orc_dirac_nnz.restype = ctypes.c_int
+        L.orc_dirac_nnz.argtypes = [vp]
+        L.orc_dirac_get_csr.argtypes = [vp, c_int_p, c_int_p, ctypes.c_void_p]
+        L.orc_dirac_get_kappa.argtypes = [vp, c_double_p]
+        L.orc_cg.restype = ctypes.c_int
+        L.orc_cg.argtypes = [vp, ctypes.c_double, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_double,
+                             ctypes.c_int, c_double_p]
+        L.orc_zolotarev.restype = ctypes.c_int
+        L.orc_zolotarev.argtypes = [ctypes.c_double, ctypes.c_int] + [c_double_p] * 4
+        L.orc_plaquettes.argtypes = [vp, c_double_p, c_double_p]
+        L.orc_gauge_action.restype = ctypes.c_double
+        L.orc_gauge_action.argtypes = [vp, c_double_p, ctypes.c_double, ctypes.c_int]
+        L.orc_gauge_force.argtypes = [vp, c_double_p, ctypes.c_double, ctypes.c_int, ctypes.c_int, c_double_p]
+        L.orc_rng_create.restype = vp
+        L.orc_rng_create.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int]
+        L.orc_rng_destroy.argtypes = [vp]
+        L.orc_rng_gaussian_links.argtypes = [vp, ctypes.c_double, c_double_p]
+        L.orc_rng_gaussian_spinor.argtypes = [vp, ctypes.c_void_p]
+        L.orc_rng_uniform.restype = ctypes.c_double
+        L.orc_rng_uniform.argtypes = [vp]
+        L.orc_hmc_pure_gauge.restype = ctypes.c_int
+        L.orc_hmc_pure_gauge.argtypes = [vp, vp, c_double_p, ctypes.c_double, ctypes.c_int, ctypes.c_int,
+                                         ctypes.c_double, ctypes.c_int, ctypes.c_int, c_double_p]
+        L.orc_fermion_force.argtypes = [vp, vp, c_double_p, ctypes.c_void_p, c_double_p]
+        L.orc_num_threads.restype = ctypes.c_int
+        _lib = L
+    return _lib
+
+
+def _p(a):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+def _dp(a):
+    return a.ctypes.data_as(c_double_p)
+
+
+@dataclass
+class Geometry:
+    n: int
+    sites: np.ndarray
+    nns: np.ndarray
+    links: np.ndarray
+    simp_links: np.ndarray
+    simp_sites: np.ndarray
+    face_offsets: np.ndarray
+    face_sites: np.ndarray
+    ell: np.ndarray
+    link_volume: np.ndarray
+    vols: np.ndarray
+    omega: np.ndarray
+    alpha: np.ndarray
+    mean_ell: float
+    mean_link_volume: float
+    mean_vol: float
+    handle: int = 0
+
+    @property
+    def n_sites(self):
+        return self.sites.shape[0]
+
+    @property
+    def n_links(self):
+        return self.links.shape[0]
+
+    @property
+    def n_faces(self):
+        return self.vols.shape[0]
+
+    def faces(self):
+        return [self.face_sites[self.face_offsets[i]:self.face_offsets[i + 1]] for i in range(self.n_faces)]
+
+    def spin_structure_residual(self) -> float:
+        return lib().orc_check_spin_structure(self.handle)
+
+    def deficits(self):
+        sums = np.zeros(self.n_faces)
+        bad = lib().orc_check_deficits(self.handle, _dp(sums))
+        return bad, sums
+
+    def __del__(self):
+        if self.handle and _lib is not None:
+            _lib.orc_geom_destroy(self.handle)
+            self.handle = 0
+
+
+def geometry(n: int) -> Geometry:
+    L = lib()
+    h = L.orc_geom_create(n)
+    if not h:
+        raise RuntimeError(f"oracle geometry failed for n={n}")
+    ns, nl, nf, nv, ft = (ctypes.c_int() for _ in range(5))
+    L.orc_geom_sizes(h, ctypes.byref(ns), ctypes.byref(nl), ctypes.byref(nf), ctypes.byref(nv), ctypes.byref(ft))
+    Ns, Nl, Nv, Ft = ns.value, nl.value, nv.value, ft.value
+    sites = np.zeros((Ns, 3))
+    nns = np.zeros((Ns, 3), np.int32)
+    links = np.zeros((Nl, 2), np.int32)
+    simp_links = np.zeros((Nl, 2), np.int32)
+    simp_sites = np.zeros((Nv, 3))
+    face_off = np.zeros(Nv + 1, np.int32)
+    face_sites = np.zeros(Ft, np.int32)
+    ell = np.zeros(Nl)
+    lv = np.zeros(Nl)
+    vols = np.zeros(Nv)
+    omega = np.zeros(Nl)
+    alpha = np.zeros((Ns, 3))
+    means = np.zeros(3)
+    L.orc_geom_get(h, *[_p(a) for a in (sites, nns, links, simp_links, simp_sites, face_off, face_sites, ell, lv,
+                                         vols, omega, alpha, means)])
+    return Geometry(n, sites, nns, links, simp_links, simp_sites, face_off, face_sites, ell, lv, vols, omega, alpha,
+                    float(means[0]), float(means[1]), float(means[2]), h)
+
+
+class Dirac:
+    """Reference CSR operator D (and D^dagger) on the dual lattice, Nt=1."""
+
+    def __init__(self, geom: Geometry, r: float = 1.0, M5: float = 0.0):
+        self.geom = geom
+        self.N = 2 * geom.n_sites
+        self.h = lib().orc_dirac_create(geom.handle, r, M5)
+
+    def update(self, A: np.ndarray):
+        A = np.ascontiguousarray(A, dtype=np.float64)
+        lib().orc_dirac_update(self.h, self.geom.handle, _dp(A))
+
+    def apply(self, v: np.ndarray, op: int = 0) -> np.ndarray:
+        v = np.ascontiguousarray(v, dtype=np.complex128)
+        out = np.zeros_like(v)
+        lib().orc_dirac_apply(self.h, op, _p(out), _p(v))
+        return out
+
+    def kappa(self):
+        k = np.zeros(self.geom.n_links)
+        lib().orc_dirac_get_kappa(self.h, _dp(k))
+        return k
+
+    def dense(self) -> np.ndarray:
+        nnz = lib().orc_dirac_nnz(self.h)
+        rows = np.zeros(self.N + 1, np.int32)
+        cols = np.zeros(nnz, np.int32)
+        val = np.zeros(nnz, np.complex128)
+        lib().orc_dirac_get_csr(self.h, rows.ctypes.data_as(c_int_p), cols.ctypes.data_as(c_int_p), _p(val))
+        M = np.zeros((self.N, self.N), np.complex128)
+        for i in range(self.N):
+            for jj in range(rows[i], rows[i + 1]):
+                M[i, cols[jj]] += val[jj]
+        return M
+
+    def cg(self, b: np.ndarray, tol: float = 1e-10, maxiter: int = 100000, shift: float = 0.0):
+        b = np.ascontiguousarray(b, dtype=np.complex128)
+        x = np.zeros_like(b)
+        mu = ctypes.c_double()
+        it = lib().orc_cg(self.h, shift, _p(x), _p(b), tol, maxiter, ctypes.byref(mu))
+        return x, it, mu.value
+
+    def fermion_force(self, A: np.ndarray, eta: np.ndarray) -> np.ndarray:
+        A = np.ascontiguousarray(A, dtype=np.float64)
+        eta = np.ascontiguousarray(eta, dtype=np.complex128)
+        F = np.zeros(self.geom.n_links)
+        lib().orc_fermion_force(self.h, self.geom.handle, _dp(A), _p(eta), _dp(F))
+        return F
+
+    def __del__(self):
+        if getattr(self, "h", 0) and _lib is not None:
+            _lib.orc_dirac_destroy(self.h)
+            self.h = 0
+
+
+def zolotarev(k: float, n: int):
+    size = n // 2 + 1
+    c, cp, A, sc = np.zeros(size), np.zeros(size), np.zeros(size), np.zeros(4)
+    lib().orc_zolotarev(k, n, _dp(c), _dp(cp), _dp(A), _dp(sc))
+    return dict(c=c, cp=cp, A=A, M=sc[0], lambda_inv=sc[1], E=sc[2], C=sc[3], size=size, k=k, n=n)
+
+
+def zolotarev_eval(z: dict, x):
+    """r(x) = C x (1 + sum_m A_m / (x^2 - k^2/cp_m)), src/both_3d/overlap.h:123-128."""
+    x = np.asarray(x, dtype=np.float64)
+    res = np.ones_like(x)
+    for m in range(1, z["size"]):
+        res = res + z["A"][m] / (x * x - z["k"] ** 2 / z["cp"][m])
+    return res * z["C"] * x
+
+
+def plaquettes(geom: Geometry, A):
+    A = np.ascontiguousarray(A, dtype=np.float64)
+    th = np.zeros(geom.n_faces)
+    lib().orc_plaquettes(geom.handle, _dp(A), _dp(th))
+    return th
+
+
+def gauge_action(geom: Geometry, A, beta: float, compact: bool = True) -> float:
+    A = np.ascontiguousarray(A, dtype=np.float64)
+    return lib().orc_gauge_action(geom.handle, _dp(A), beta, int(compact))
+
+
+def gauge_force(geom: Geometry, A, beta: float, compact: bool = True, exact: bool = True):
+    A = np.ascontiguousarray(A, dtype=np.float64)
+    F = np.zeros(geom.n_links)
+    lib().orc_gauge_force(geom.handle, _dp(A), beta, int(compact), int(exact), _dp(F))
+    return F
+
+
+class Rng:
+    """ParallelRng2 restated: master mt19937_64 seeds per-link then per-site engines."""
+
+    def __init__(self, geom: Geometry, seed: int):
+        self.geom = geom
+        self.h = lib().orc_rng_create(geom.n_links, geom.n_sites, seed)
+
+    def gaussian_links(self, width=1.0):
+        out = np.zeros(self.geom.n_links)
+        lib().orc_rng_gaussian_links(self.h, width, _dp(out))
+        return out
+
+    def gaussian_spinor(self):
+        out = np.zeros(2 * self.geom.n_sites, np.complex128)
+        lib().orc_rng_gaussian_spinor(self.h, _p(out))
+        return out
+
+    def uniform(self):
+        return lib().orc_rng_uniform(self.h)
+
+    def __del__(self):
+        if getattr(self, "h", 0) and _lib is not None:
+            _lib.orc_rng_destroy(self.h)
+            self.h = 0
+
+
+def hmc_pure_gauge(geom: Geometry, rng: Rng, A: np.ndarray, beta: float, compact=True, exact=True, tmax=1.0,
+                   nsteps=40, no_reject=False):
+    """One HMCPureGauge trajectory in place on A; returns (accepted, dH)."""
+    assert A.dtype == np.float64 and A.flags.c_contiguous
+    dH = ctypes.c_double()
+    acc = lib().orc_hmc_pure_gauge(geom.handle, rng.h, _dp(A), beta, int(compact), int(exact), tmax, nsteps,
+                                   int(no_reject), ctypes.byref(dH))
+    return bool(acc), dH.value
+
+
+def thermalized_links(geom: Geometry, beta: float, seed: int, ntraj: int, init: str = "gaussian",
+                      compact: bool = True, exact: bool = True, nsteps: int = 40):
+    """Seeded pure-gauge configuration (src/both/gauge.cu:157-200 recipe)."""
+    rng = Rng(geom, seed)
+    if init == "gaussian":
+        A = rng.gaussian_links(0.2)
+    elif init == "uniform":
+        r = np.random.default_rng(seed)
+        A = r.uniform(-np.pi, np.pi, geom.n_links)
+    else:
+        A = np.zeros(geom.n_links)
+    A = np.ascontiguousarray(A)
+    acc = 0
+    for _ in range(ntraj):
+        a, _ = hmc_pure_gauge(geom, rng, A, beta, compact, exact, 1.0, nsteps)
+        acc += a
+    return A, acc
+
+
+def num_threads() -> int:
+    return lib().orc_num_threads()
