@@ -1,0 +1,172 @@
+/* qed3-gb300: C ABI of the GB300-native fermion hot path of qed3.
+ *
+ * Every entry point is extern "C", takes plain pointers and sizes, returns an
+ * int status and never throws.  Device vectors are complex128 interleaved
+ * (re, im) with index 2*x + s (site-major, spin-minor) in the REFERENCE site
+ * order -- the layout of the reference's CuC* vectors
+ * (src/dual/valence.h:44-45).  Link fields are float64 per link in the
+ * reference link order (links sorted (i<j), angle oriented i -> j,
+ * src/both_3d/gauge_ext.h:45-49).  `stream` is a cudaStream_t passed as
+ * void* (NULL = legacy default stream).
+ *
+ * Threading: a handle is not safe for concurrent use from several threads;
+ * distinct handles are independent.  Entry points that return a report
+ * synchronise their stream; the others are stream-ordered and asynchronous.
+ */
+#ifndef QED3_GB300_H
+#define QED3_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes (replace CUDA_CHECK/CUBLAS_CHECK exceptions and asserts,
+ *      src/dual/gpu_header.h:52-88) ---------------------------------------- */
+#define QED3_OK 0
+#define QED3_ERR_ARG 1      /* invalid argument or size */
+#define QED3_ERR_CUDA 2     /* a CUDA runtime call failed */
+#define QED3_ERR_NOCONV 3   /* solver hit maxiter / stagnated / NaN */
+#define QED3_ERR_TIMEOUT 4  /* a device-side grid barrier gave up waiting */
+#define QED3_ERR_STATE 5    /* handle used in the wrong state */
+#define QED3_ERR_NOMEM 6    /* device allocation failed */
+
+/* operators (replace LinOp compositions, src/dual/sparse_matrix.h:4-39,
+ * src/both_3d/dirac_pf.h:66-92) */
+#define QED3_OP_D 0
+#define QED3_OP_DDAG 1
+#define QED3_OP_DDAGD 2 /* D^dagger D: D first, then D^dagger */
+#define QED3_OP_DDDAG 3 /* D D^dagger */
+
+/* storage precisions of the device-internal fields */
+#define QED3_PREC_F64 0
+#define QED3_PREC_F32 1
+#define QED3_PREC_BF16 2 /* bf16-stored spinors, fp32 links and arithmetic */
+
+typedef struct qed3_lattice_s qed3_lattice;
+typedef struct qed3_dirac_s qed3_dirac;
+typedef struct qed3_overlap_s qed3_overlap;
+
+/* Message of the last failure on the calling thread ("" if none). */
+const char* qed3_last_error_string(void);
+int qed3_version(void);
+
+/* ======================================================================
+ * Lattice  --  replaces S2Trivalent(n_refine) (src/both_3d/s2n_dual.h:49-106)
+ * and SpinStructureDual (src/both_3d/dirac_dual.h:15-60), which read the
+ * offline generator's .dat tables (integrator/get_geometry.cc:383-465,
+ * integrator/test_sorting.cc:430-594).  Built in O(N) on the host; tables are
+ * uploaded to the current device in a space-filling-curve order.
+ * ====================================================================== */
+int qed3_lattice_create(int n_refine, qed3_lattice** out);
+int qed3_lattice_destroy(qed3_lattice* lat);
+/* n_sites = 20n^2, n_links = 30n^2, n_faces = 10n^2+2, face_total = sum |face| */
+int qed3_lattice_sizes(const qed3_lattice* lat, int* n_sites, int* n_links, int* n_faces, int* face_total);
+/* Host copies of the tables in reference order; any pointer may be NULL.
+ * sites[Ns*3], nns[Ns*3], links[Nl*2], simp_links[Nl*2] (S2Trivalent::dual_links),
+ * face_offsets[Nf+1], face_sites[face_total], ell[Nl], link_volume[Nl],
+ * vols[Nf] (dual-face areas), omega[Nl] (omega(links[l][0], links[l][1])),
+ * alpha[Ns*3] (alpha(x, nns[x][k])), means[3] = {mean_ell, mean_link_volume, mean_vol}. */
+int qed3_lattice_tables(const qed3_lattice* lat, double* sites, int* nns, int* links, int* simp_links,
+                        int* face_offsets, int* face_sites, double* ell, double* link_volume, double* vols,
+                        double* omega, double* alpha, double* means);
+/* Internal (device) order: perm[i] = reference index of internal site i. */
+int qed3_lattice_permutation(const qed3_lattice* lat, int* perm);
+
+/* ======================================================================
+ * Wilson-Dirac operator  --  replaces DiracS2Dual / DiracExt<.., DiracS2Dual>
+ * at Nt=1 (src/both_3d/dirac_dual.h:63-215, src/both_3d/dirac_ext.h:6-334)
+ * together with its device form DWDevice + CSR (src/both_3d/sparse_dirac.h:5-166).
+ * (D psi)_x = [M5 + sum_y r kappa_l/2] psi_x
+ *           + sum_y kappa_l/2 (-r + gamma_xy) e^{i A_xy} Omega_xy psi_y
+ * ====================================================================== */
+int qed3_dirac_create(qed3_lattice* lat, double r, double M5, qed3_dirac** out);
+int qed3_dirac_destroy(qed3_dirac* d);
+/* DWDevice::update(U) (src/both_3d/sparse_dirac.h:144-151): rebuild every hop
+ * matrix on the device from link angles A[n_links] (host or device pointer). */
+int qed3_dirac_set_links(qed3_dirac* d, const double* A, int A_on_device, void* stream);
+/* Load arbitrary coefficients of the same sparsity (any builder, e.g.
+ * Dirac1fonS2::coo_format, src/dual/dirac.h:187-220): host hop[Ns*3*8] =
+ * 2x2 complex row-major block of D at (x, nns[x][k]); host diag[Ns] = real
+ * scalar of the diagonal block. */
+int qed3_dirac_set_coefficients(qed3_dirac* d, const double* hop, const double* diag);
+/* LinOp::operator()/Async (src/dual/sparse_matrix.h:4-39): out = op(in) on
+ * device complex128 vectors of length 2*n_sites in reference order. */
+int qed3_dirac_apply(qed3_dirac* d, int op, double* out, const double* in, void* stream);
+
+/* Device-internal fields (space-filling-curve order, precision `prec`):
+ * F64 = 32 B/site, F32 = 16 B/site, BF16 = 8 B/site, nrhs fields back to back.
+ * These are what the solvers use; the reference-order calls above convert. */
+size_t qed3_field_bytes(const qed3_dirac* d, int prec, int nrhs);
+int qed3_field_import(qed3_dirac* d, int prec, void* field, const double* in_ref, int nrhs, void* stream);
+int qed3_field_export(qed3_dirac* d, int prec, double* out_ref, const void* field, int nrhs, void* stream);
+int qed3_dirac_apply_field(qed3_dirac* d, int op, int prec, void* out, const void* in, int nrhs, void* stream);
+
+/* ======================================================================
+ * Solvers  --  replace MatPoly::solve<N> (src/dual/matpoly.h:204-267):
+ * CG on (D^dagger D + shift) x = b from x0 = 0.
+ * ====================================================================== */
+#define QED3_SOLVE_RECURSIVE_STOP 1 /* stop on the recursive residual alone, as MatPoly::solve */
+
+typedef struct {
+  double tol;     /* target ||b - A x|| / ||b|| of the FP64 true residual */
+  int maxiter;    /* iteration cap (0 => 100000) */
+  int precision;  /* QED3_PREC_F64: plain FP64 CG; F32/BF16: mixed precision with FP64 reliable updates */
+  double delta;   /* reliable-update trigger: update when |r| < delta * max|r| since the last one (0 => 0.1) */
+  double shift;   /* solve (D^dagger D + shift) x = b */
+  int flags;
+} qed3_solve_params;
+
+typedef struct {
+  int status;          /* QED3_OK or QED3_ERR_NOCONV / _TIMEOUT */
+  int iters;           /* CG iterations */
+  int reliable_updates;
+  double true_rel_res; /* ||b - A x|| / ||b|| recomputed in FP64 on the device */
+  double ms;           /* device time of the solve */
+} qed3_solve_report;
+
+/* x, b: device complex128, reference order.  report may be NULL (then the
+ * call is asynchronous and the outcome is read with qed3_solver_last_report). */
+int qed3_cg_solve(qed3_dirac* d, double* x, const double* b, const qed3_solve_params* params,
+                  qed3_solve_report* report, void* stream);
+int qed3_solver_last_report(qed3_dirac* d, qed3_solve_report* report);
+
+/* ======================================================================
+ * Gauge side  --  replaces U1onS2::plaquette_angle/average_plaquette
+ * (src/dual/gauge.h:90-110) and U1Wilson::operator()/get_force
+ * (src/both/action.h:21-48, weights mean_vol/vol_f) on the dual faces.
+ * A, theta, F are device float64 arrays (links / faces in reference order).
+ * compact: 1 = -beta sum w cos(theta), 0 = beta/2 sum w theta^2.
+ * exact: 1 = compact force with sin(theta); 0 = the reference's theta
+ * (src/dual/action.h:37).
+ * ====================================================================== */
+int qed3_plaquette(qed3_lattice* lat, const double* A, double* theta, double* avg, void* stream);
+int qed3_gauge_action(qed3_lattice* lat, const double* A, double beta, int compact, double* S, void* stream);
+int qed3_gauge_force(qed3_lattice* lat, const double* A, double beta, int compact, int exact, double* F, void* stream);
+
+/* Wilson fermion force of every link at once: F[l] = -2 Re <D eta, dD/dA_l eta>
+ * (DiracPf::grad_deviceAsyncLaunch, src/both_3d/dirac_pf.h:107-122, which is
+ * called once per link).  eta: device complex128, reference order; F: device [n_links]. */
+int qed3_fermion_force(qed3_dirac* d, const double* eta, double* F, void* stream);
+
+/* ======================================================================
+ * RNG and pure-gauge HMC  --  ParallelRng2 (src/both/rng.h:76-125) driven by
+ * libstdc++ mt19937_64 + normal_distribution, and HMCPureGauge::run
+ * (src/both_3d/hmc.h:212-296).  dH is accumulated from per-term differences.
+ * ====================================================================== */
+typedef struct qed3_rng_s qed3_rng;
+int qed3_rng_create(int n_links, int n_sites, int seed, qed3_rng** out);
+int qed3_rng_destroy(qed3_rng* r);
+/* host outputs: links[n_links] = width * N(0,1); spinor[2*n_sites] complex
+ * (ParallelRngExt::fill_gaussian, src/both_3d/rng.h:122-129) */
+int qed3_rng_gaussian_links(qed3_rng* r, double width, double* links);
+int qed3_rng_gaussian_spinor(qed3_rng* r, double* spinor);
+int qed3_hmc_pure_gauge(qed3_lattice* lat, qed3_rng* rng, double* A, double beta, int compact, int exact,
+                        double tmax, int nsteps, int no_reject, int* accepted, double* dH, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* QED3_GB300_H */

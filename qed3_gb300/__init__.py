@@ -1,0 +1,337 @@
+"""qed3-gb300: GB300-native fermion hot path of qed3 behind a C ABI.
+
+The compute path is the in-tree CUDA library ``libqed3.so`` (sm_103a); this
+module only binds its C entry points (``include/qed3.h``) with ctypes and
+mirrors the reference's object names:
+
+* :class:`S2Trivalent`   -- the dual lattice (src/both_3d/s2n_dual.h:15)
+* :class:`DiracS2Dual`   -- Wilson-Dirac operator + its device form
+  (src/both_3d/dirac_dual.h:63, src/both_3d/sparse_dirac.h:5)
+* :meth:`DiracS2Dual.solve` -- CG on D^dagger D (MatPoly::solve,
+  src/dual/matpoly.h:204)
+
+Device vectors are torch CUDA tensors (complex128, reference site order,
+index 2*x+s) passed by pointer; torch is only used for device memory and
+streams.  There is no CPU fallback: if the library or a GPU is missing,
+the calls raise.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import build as _build
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libqed3.so")
+
+OK, ERR_ARG, ERR_CUDA, ERR_NOCONV, ERR_TIMEOUT, ERR_STATE, ERR_NOMEM = range(7)
+OP_D, OP_DDAG, OP_DDAGD, OP_DDDAG = range(4)
+PREC_F64, PREC_F32, PREC_BF16 = range(3)
+PREC_NAMES = {"f64": PREC_F64, "f32": PREC_F32, "bf16": PREC_BF16}
+BYTES_PER_SITE = {PREC_F64: 32, PREC_F32: 16, PREC_BF16: 8}
+
+_lib = None
+vp = ctypes.c_void_p
+c_int_p = ctypes.POINTER(ctypes.c_int)
+c_double_p = ctypes.POINTER(ctypes.c_double)
+
+
+class SolveParams(ctypes.Structure):
+    _fields_ = [("tol", ctypes.c_double), ("maxiter", ctypes.c_int), ("precision", ctypes.c_int),
+                ("delta", ctypes.c_double), ("shift", ctypes.c_double), ("flags", ctypes.c_int)]
+
+
+class SolveReport(ctypes.Structure):
+    _fields_ = [("status", ctypes.c_int), ("iters", ctypes.c_int), ("reliable_updates", ctypes.c_int),
+                ("true_rel_res", ctypes.c_double), ("ms", ctypes.c_double)]
+
+
+class Qed3Error(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__(f"qed3 status {status}: {msg}")
+        self.status = status
+
+
+# (name, restype, argtypes) of every entry point of include/qed3.h
+SIGNATURES = [
+    ("qed3_last_error_string", ctypes.c_char_p, []),
+    ("qed3_version", ctypes.c_int, []),
+    ("qed3_lattice_create", ctypes.c_int, [ctypes.c_int, ctypes.POINTER(vp)]),
+    ("qed3_lattice_destroy", ctypes.c_int, [vp]),
+    ("qed3_lattice_sizes", ctypes.c_int, [vp, c_int_p, c_int_p, c_int_p, c_int_p]),
+    ("qed3_lattice_tables", ctypes.c_int, [vp] + [vp] * 12),
+    ("qed3_lattice_permutation", ctypes.c_int, [vp, vp]),
+    ("qed3_dirac_create", ctypes.c_int, [vp, ctypes.c_double, ctypes.c_double, ctypes.POINTER(vp)]),
+    ("qed3_dirac_destroy", ctypes.c_int, [vp]),
+    ("qed3_dirac_set_links", ctypes.c_int, [vp, vp, ctypes.c_int, vp]),
+    ("qed3_dirac_set_coefficients", ctypes.c_int, [vp, vp, vp]),
+    ("qed3_dirac_apply", ctypes.c_int, [vp, ctypes.c_int, vp, vp, vp]),
+    ("qed3_field_bytes", ctypes.c_size_t, [vp, ctypes.c_int, ctypes.c_int]),
+    ("qed3_field_import", ctypes.c_int, [vp, ctypes.c_int, vp, vp, ctypes.c_int, vp]),
+    ("qed3_field_export", ctypes.c_int, [vp, ctypes.c_int, vp, vp, ctypes.c_int, vp]),
+    ("qed3_dirac_apply_field", ctypes.c_int, [vp, ctypes.c_int, ctypes.c_int, vp, vp, ctypes.c_int, vp]),
+    ("qed3_cg_solve", ctypes.c_int, [vp, vp, vp, ctypes.POINTER(SolveParams), ctypes.POINTER(SolveReport), vp]),
+    ("qed3_solver_last_report", ctypes.c_int, [vp, ctypes.POINTER(SolveReport)]),
+    ("qed3_plaquette", ctypes.c_int, [vp, vp, vp, c_double_p, vp]),
+    ("qed3_gauge_action", ctypes.c_int, [vp, vp, ctypes.c_double, ctypes.c_int, c_double_p, vp]),
+    ("qed3_gauge_force", ctypes.c_int, [vp, vp, ctypes.c_double, ctypes.c_int, ctypes.c_int, vp, vp]),
+    ("qed3_fermion_force", ctypes.c_int, [vp, vp, vp, vp]),
+    ("qed3_rng_create", ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.POINTER(vp)]),
+    ("qed3_rng_destroy", ctypes.c_int, [vp]),
+    ("qed3_rng_gaussian_links", ctypes.c_int, [vp, ctypes.c_double, vp]),
+    ("qed3_rng_gaussian_spinor", ctypes.c_int, [vp, vp]),
+    ("qed3_hmc_pure_gauge", ctypes.c_int, [vp, vp, vp, ctypes.c_double, ctypes.c_int, ctypes.c_int, ctypes.c_double,
+                                           ctypes.c_int, ctypes.c_int, c_int_p, c_double_p, vp]),
+]
+
+
+def lib(build: bool = True):
+    """Load (building first if needed) the in-tree CUDA library."""
+    global _lib
+    if _lib is None:
+        if build:
+            _build.build()
+        if not os.path.exists(LIB_PATH):
+            raise Qed3Error(ERR_STATE, f"{LIB_PATH} is missing; run qed3_gb300.build.build()")
+        L = ctypes.CDLL(LIB_PATH)
+        for name, res, args in SIGNATURES:
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = L
+    return _lib
+
+
+def _check(rc):
+    if rc != OK:
+        msg = lib().qed3_last_error_string().decode()
+        raise Qed3Error(rc, msg)
+
+
+def _ptr(t):
+    """Device pointer of a torch tensor, or data pointer of a numpy array."""
+    if isinstance(t, np.ndarray):
+        return t.ctypes.data_as(vp)
+    if t is None:
+        return None
+    return vp(t.data_ptr())
+
+
+def _stream(stream):
+    if stream is None:
+        return None
+    return vp(getattr(stream, "cuda_stream", stream))
+
+
+class S2Trivalent:
+    """Dual trivalent lattice of refinement n (S2Trivalent, src/both_3d/s2n_dual.h:49)."""
+
+    def __init__(self, n_refine: int):
+        self.n_refine = n_refine
+        h = vp()
+        _check(lib().qed3_lattice_create(n_refine, ctypes.byref(h)))
+        self._h = h
+        ns, nl, nf, ft = (ctypes.c_int() for _ in range(4))
+        _check(lib().qed3_lattice_sizes(h, *(ctypes.byref(v) for v in (ns, nl, nf, ft))))
+        self.n_sites, self.n_links, self.n_faces, self.face_total = ns.value, nl.value, nf.value, ft.value
+        self._tables = None
+
+    @property
+    def handle(self):
+        return self._h
+
+    def tables(self) -> dict:
+        if self._tables is None:
+            Ns, Nl, Nf, Ft = self.n_sites, self.n_links, self.n_faces, self.face_total
+            t = dict(sites=np.zeros((Ns, 3)), nns=np.zeros((Ns, 3), np.int32), links=np.zeros((Nl, 2), np.int32),
+                     simp_links=np.zeros((Nl, 2), np.int32), face_offsets=np.zeros(Nf + 1, np.int32),
+                     face_sites=np.zeros(Ft, np.int32), ell=np.zeros(Nl), link_volume=np.zeros(Nl),
+                     vols=np.zeros(Nf), omega=np.zeros(Nl), alpha=np.zeros((Ns, 3)), means=np.zeros(3))
+            order = ["sites", "nns", "links", "simp_links", "face_offsets", "face_sites", "ell", "link_volume",
+                     "vols", "omega", "alpha", "means"]
+            _check(lib().qed3_lattice_tables(self._h, *(_ptr(t[k]) for k in order)))
+            self._tables = t
+        return self._tables
+
+    def permutation(self) -> np.ndarray:
+        p = np.zeros(self.n_sites, np.int32)
+        _check(lib().qed3_lattice_permutation(self._h, _ptr(p)))
+        return p
+
+    def __del__(self):
+        if getattr(self, "_h", None) and _lib is not None:
+            _lib.qed3_lattice_destroy(self._h)
+            self._h = None
+
+
+@dataclass
+class Report:
+    status: int
+    iters: int
+    reliable_updates: int
+    true_rel_res: float
+    ms: float
+
+
+class DiracS2Dual:
+    """Wilson-Dirac operator on the dual lattice with its device coefficients.
+
+    Mirrors DiracS2Dual(lattice, m, r, M5) + DiracPf/DWDevice
+    (src/both_3d/dirac_dual.h:63-106, src/both_3d/dirac_pf.h:4-125): the mass
+    enters as M5, as in the reference where DiracS2Dual::m is unused.
+    """
+
+    def __init__(self, lattice: S2Trivalent, r: float = 1.0, M5: float = 0.0):
+        self.lattice = lattice
+        self.r, self.M5 = r, M5
+        self.N = 2 * lattice.n_sites
+        h = vp()
+        _check(lib().qed3_dirac_create(lattice.handle, r, M5, ctypes.byref(h)))
+        self._h = h
+
+    @property
+    def handle(self):
+        return self._h
+
+    def update(self, A, stream=None):
+        """DWDevice::update(U): rebuild the hop blocks from link angles A[n_links]."""
+        if isinstance(A, np.ndarray):
+            A = np.ascontiguousarray(A, dtype=np.float64)
+            _check(lib().qed3_dirac_set_links(self._h, _ptr(A), 0, _stream(stream)))
+            self._sync(stream)
+        else:
+            _check(lib().qed3_dirac_set_links(self._h, _ptr(A), 1, _stream(stream)))
+
+    def set_coefficients(self, hop: np.ndarray, diag: np.ndarray):
+        hop = np.ascontiguousarray(hop, dtype=np.complex128).reshape(-1)
+        diag = np.ascontiguousarray(diag, dtype=np.float64)
+        _check(lib().qed3_dirac_set_coefficients(self._h, _ptr(hop), _ptr(diag)))
+
+    def apply(self, out, inp, op: int = OP_D, stream=None):
+        """LinOp::operator(): out = op(inp) on device complex128 tensors."""
+        _check(lib().qed3_dirac_apply(self._h, op, _ptr(out), _ptr(inp), _stream(stream)))
+        return out
+
+    # -- device-internal fields ---------------------------------------------------
+    def field_bytes(self, prec: int, nrhs: int = 1) -> int:
+        return lib().qed3_field_bytes(self._h, prec, nrhs)
+
+    def field_import(self, field, inp, prec: int, nrhs: int = 1, stream=None):
+        _check(lib().qed3_field_import(self._h, prec, _ptr(field), _ptr(inp), nrhs, _stream(stream)))
+
+    def field_export(self, out, field, prec: int, nrhs: int = 1, stream=None):
+        _check(lib().qed3_field_export(self._h, prec, _ptr(out), _ptr(field), nrhs, _stream(stream)))
+
+    def apply_field(self, out, inp, op: int, prec: int, nrhs: int = 1, stream=None):
+        _check(lib().qed3_dirac_apply_field(self._h, op, prec, _ptr(out), _ptr(inp), nrhs, _stream(stream)))
+
+    # -- solver ----------------------------------------------------------------------
+    def solve(self, x, b, tol: float = 1e-10, maxiter: int = 100000, precision: int = PREC_F64,
+              delta: float = 0.1, shift: float = 0.0, stream=None) -> Report:
+        """CG on (D^dagger D + shift) x = b (MatPoly::solve); certified by the FP64 true residual."""
+        p = SolveParams(tol, maxiter, precision, delta, shift, 0)
+        r = SolveReport()
+        rc = lib().qed3_cg_solve(self._h, _ptr(x), _ptr(b), ctypes.byref(p), ctypes.byref(r), _stream(stream))
+        if rc not in (OK, ERR_NOCONV):
+            _check(rc)
+        return Report(r.status, r.iters, r.reliable_updates, r.true_rel_res, r.ms)
+
+    @staticmethod
+    def _sync(stream):
+        import torch
+        if torch.cuda.is_available():
+            (stream or torch.cuda.current_stream()).synchronize()
+
+    def __del__(self):
+        if getattr(self, "_h", None) and _lib is not None:
+            _lib.qed3_dirac_destroy(self._h)
+            self._h = None
+
+
+# ---------------------------------------------------------------------------
+# gauge side
+# ---------------------------------------------------------------------------
+def plaquette(lattice: S2Trivalent, A, theta=None, stream=None) -> float:
+    """Plaquette angles into `theta` (device, optional); returns mean cos(theta)."""
+    avg = ctypes.c_double()
+    _check(lib().qed3_plaquette(lattice.handle, _ptr(A), _ptr(theta), ctypes.byref(avg), _stream(stream)))
+    return avg.value
+
+
+def gauge_action(lattice: S2Trivalent, A, beta: float, compact: bool = True, stream=None) -> float:
+    S = ctypes.c_double()
+    _check(lib().qed3_gauge_action(lattice.handle, _ptr(A), beta, int(compact), ctypes.byref(S), _stream(stream)))
+    return S.value
+
+
+def gauge_force(lattice: S2Trivalent, A, F, beta: float, compact: bool = True, exact: bool = True, stream=None):
+    _check(lib().qed3_gauge_force(lattice.handle, _ptr(A), beta, int(compact), int(exact), _ptr(F), _stream(stream)))
+    return F
+
+
+def fermion_force(dirac: DiracS2Dual, eta, F, stream=None):
+    _check(lib().qed3_fermion_force(dirac.handle, _ptr(eta), _ptr(F), _stream(stream)))
+    return F
+
+
+class ParallelRng:
+    """ParallelRng2 (src/both/rng.h:76-125): seeded per-link and per-site engines."""
+
+    def __init__(self, lattice: S2Trivalent, seed: int = 0):
+        self.lattice = lattice
+        h = vp()
+        _check(lib().qed3_rng_create(lattice.n_links, lattice.n_sites, seed, ctypes.byref(h)))
+        self._h = h
+
+    @property
+    def handle(self):
+        return self._h
+
+    def gaussian_links(self, width: float = 1.0) -> np.ndarray:
+        out = np.zeros(self.lattice.n_links)
+        _check(lib().qed3_rng_gaussian_links(self._h, width, _ptr(out)))
+        return out
+
+    def gaussian_spinor(self) -> np.ndarray:
+        out = np.zeros(2 * self.lattice.n_sites, np.complex128)
+        _check(lib().qed3_rng_gaussian_spinor(self._h, _ptr(out)))
+        return out
+
+    def __del__(self):
+        if getattr(self, "_h", None) and _lib is not None:
+            _lib.qed3_rng_destroy(self._h)
+            self._h = None
+
+
+def hmc_pure_gauge(lattice: S2Trivalent, rng: ParallelRng, A, beta: float, compact: bool = True,
+                   exact: bool = True, tmax: float = 1.0, nsteps: int = 40, no_reject: bool = False, stream=None):
+    """One HMCPureGauge trajectory in place on the device links A; returns (accepted, dH)."""
+    acc = ctypes.c_int()
+    dH = ctypes.c_double()
+    _check(lib().qed3_hmc_pure_gauge(lattice.handle, rng.handle, _ptr(A), beta, int(compact), int(exact), tmax,
+                                     nsteps, int(no_reject), ctypes.byref(acc), ctypes.byref(dH), _stream(stream)))
+    return bool(acc.value), dH.value
+
+
+def thermalized_links(lattice: S2Trivalent, beta: float, seed: int, ntraj: int, init: str = "uniform",
+                      device="cuda", compact: bool = True, nsteps: int = 40):
+    """Seeded configuration: A ~ U[-pi, pi) (init="uniform") or 0.2 N(0,1)
+    (init="gaussian", src/both/gauge.cu:157), then `ntraj` pure-gauge HMC
+    trajectories (tmax=1, nsteps) at `beta`.  Returns (device links, acceptance)."""
+    import torch
+
+    rng = ParallelRng(lattice, seed)
+    if init == "uniform":
+        A0 = np.random.default_rng(seed).uniform(-np.pi, np.pi, lattice.n_links)
+    else:
+        A0 = rng.gaussian_links(0.2)
+    A = torch.from_numpy(A0).to(device)
+    acc = 0
+    for _ in range(ntraj):
+        a, _ = hmc_pure_gauge(lattice, rng, A, beta, compact, True, 1.0, nsteps)
+        acc += a
+    return A, acc / max(1, ntraj)

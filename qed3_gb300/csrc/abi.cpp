@@ -1,0 +1,345 @@
+// extern "C" entry points of include/qed3.h.  No exception crosses this
+// boundary: every call returns a status and records a message for
+// qed3_last_error_string().
+
+#include <cuda_runtime.h>
+
+#include <cstring>
+#include <exception>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "dirac_impl.h"
+#include "gauge_impl.h"
+#include "handles.h"
+#include "qed3_internal.h"
+
+namespace qed3 {
+
+static thread_local std::string g_last_error;
+
+void set_error(const std::string& msg) { g_last_error = msg; }
+int fail(int status, const std::string& msg) {
+  g_last_error = msg;
+  return status;
+}
+
+template <class T>
+static int upload(T** dst, const std::vector<T>& src) {
+  QED3_CUDA_TRY(cudaMalloc(dst, src.size() * sizeof(T) + 16));
+  QED3_CUDA_TRY(cudaMemcpy(*dst, src.data(), src.size() * sizeof(T), cudaMemcpyHostToDevice));
+  return QED3_OK;
+}
+
+int lattice_upload(qed3_lattice_s* lat) {
+  const HostLattice& L = lat->host;
+  DeviceLattice& D = lat->dev;
+  const int Ns = L.n_sites, Nl = L.n_links, Nf = L.n_faces;
+  D.Ns = Ns;
+  D.Nl = Nl;
+  D.Nf = Nf;
+  D.face_total = int(L.face_sites.size());
+  std::vector<int32_t> nbr(size_t(3) * Ns), nbr_ref(size_t(3) * Ns), hop_link(size_t(3) * Ns);
+  std::vector<int8_t> hop_sign(size_t(3) * Ns);
+  for (int i = 0; i < Ns; i++) {
+    const int x = L.perm[i];
+    for (int k = 0; k < 3; k++) {
+      const int y = L.nns[3 * x + k];
+      nbr[size_t(k) * Ns + i] = L.iperm[y];
+      nbr_ref[size_t(k) * Ns + i] = y;
+      hop_link[size_t(k) * Ns + i] = L.hop_link[3 * x + k];
+      hop_sign[size_t(k) * Ns + i] = L.hop_sign[3 * x + k];
+    }
+  }
+  std::vector<int32_t> link_x(Nl), link_y(Nl);
+  std::vector<int8_t> link_kx(Nl), link_ky(Nl);
+  for (int l = 0; l < Nl; l++) {
+    const int x = L.links[2 * l], y = L.links[2 * l + 1];
+    link_x[l] = L.iperm[x];
+    link_y[l] = L.iperm[y];
+    int kx = 0, ky = 0;
+    while (L.nns[3 * x + kx] != y) kx++;
+    while (L.nns[3 * y + ky] != x) ky++;
+    link_kx[l] = int8_t(kx);
+    link_ky[l] = int8_t(ky);
+  }
+  std::vector<double> fw(Nf);
+  for (int f = 0; f < Nf; f++) fw[f] = L.mean_vol / L.vols[f];
+  int rc;
+  if ((rc = upload(&D.nbr, nbr)) || (rc = upload(&D.nbr_ref, nbr_ref)) || (rc = upload(&D.perm, L.perm)) ||
+      (rc = upload(&D.iperm, L.iperm)) || (rc = upload(&D.hop_link, hop_link)) || (rc = upload(&D.hop_sign, hop_sign)) ||
+      (rc = upload(&D.face_off, L.face_offsets)) || (rc = upload(&D.face_link, L.face_links)) ||
+      (rc = upload(&D.face_sign, L.face_link_sign)) || (rc = upload(&D.face_weight, fw)) ||
+      (rc = upload(&D.link_x, link_x)) || (rc = upload(&D.link_y, link_y)) || (rc = upload(&D.link_kx, link_kx)) ||
+      (rc = upload(&D.link_ky, link_ky)))
+    return rc;
+  return QED3_OK;
+}
+
+int lattice_free(qed3_lattice_s* lat) {
+  DeviceLattice& D = lat->dev;
+  void* ptrs[] = {D.nbr, D.nbr_ref, D.perm, D.iperm, D.hop_link, D.hop_sign, D.face_off, D.face_link,
+                  D.face_sign, D.face_weight, D.link_x, D.link_y, D.link_kx, D.link_ky};
+  for (void* p : ptrs)
+    if (p) cudaFree(p);
+  D = DeviceLattice{};
+  return QED3_OK;
+}
+
+}  // namespace qed3
+
+using namespace qed3;
+
+#define QED3_GUARD_BEGIN try {
+#define QED3_GUARD_END                                                   \
+  }                                                                      \
+  catch (const std::bad_alloc&) {                                        \
+    return fail(QED3_ERR_NOMEM, "host allocation failed");               \
+  }                                                                      \
+  catch (const std::exception& e) {                                      \
+    return fail(QED3_ERR_STATE, std::string("internal error: ") + e.what()); \
+  }                                                                      \
+  catch (...) {                                                          \
+    return fail(QED3_ERR_STATE, "internal error");                       \
+  }
+
+extern "C" {
+
+const char* qed3_last_error_string(void) { return g_last_error.c_str(); }
+int qed3_version(void) { return 100; }
+
+int qed3_lattice_create(int n_refine, qed3_lattice** out) {
+  QED3_GUARD_BEGIN
+  if (!out) return fail(QED3_ERR_ARG, "out is NULL");
+  *out = nullptr;
+  auto* lat = new qed3_lattice_s;
+  int rc = build_lattice(n_refine, true, lat->host);
+  if (rc) {
+    delete lat;
+    return rc;
+  }
+  // device tables are uploaded on first device use (qed3_dirac_create, gauge
+  // kernels), so host-only queries need no GPU
+  *out = lat;
+  return QED3_OK;
+  QED3_GUARD_END
+}
+
+int qed3_lattice_destroy(qed3_lattice* lat) {
+  if (!lat) return QED3_OK;
+  gauge_free(lat);
+  lattice_free(lat);
+  delete lat;
+  return QED3_OK;
+}
+
+int qed3_lattice_sizes(const qed3_lattice* lat, int* n_sites, int* n_links, int* n_faces, int* face_total) {
+  if (!lat) return fail(QED3_ERR_ARG, "lattice is NULL");
+  if (n_sites) *n_sites = lat->host.n_sites;
+  if (n_links) *n_links = lat->host.n_links;
+  if (n_faces) *n_faces = lat->host.n_faces;
+  if (face_total) *face_total = int(lat->host.face_sites.size());
+  return QED3_OK;
+}
+
+int qed3_lattice_tables(const qed3_lattice* lat, double* sites, int* nns, int* links, int* simp_links,
+                        int* face_offsets, int* face_sites, double* ell, double* link_volume, double* vols,
+                        double* omega, double* alpha, double* means) {
+  if (!lat) return fail(QED3_ERR_ARG, "lattice is NULL");
+  const HostLattice& L = lat->host;
+  auto cp = [](auto* dst, const auto& v) {
+    if (dst) std::memcpy(dst, v.data(), v.size() * sizeof(v[0]));
+  };
+  cp(sites, L.sites);
+  cp(nns, L.nns);
+  cp(links, L.links);
+  cp(simp_links, L.simp_links);
+  cp(face_offsets, L.face_offsets);
+  cp(face_sites, L.face_sites);
+  cp(ell, L.ell);
+  cp(link_volume, L.link_volume);
+  cp(vols, L.vols);
+  cp(omega, L.omega);
+  cp(alpha, L.alpha);
+  if (means) {
+    means[0] = L.mean_ell;
+    means[1] = L.mean_link_volume;
+    means[2] = L.mean_vol;
+  }
+  return QED3_OK;
+}
+
+int qed3_lattice_permutation(const qed3_lattice* lat, int* perm) {
+  if (!lat || !perm) return fail(QED3_ERR_ARG, "NULL argument");
+  std::memcpy(perm, lat->host.perm.data(), lat->host.perm.size() * sizeof(int32_t));
+  return QED3_OK;
+}
+
+int qed3_dirac_create(qed3_lattice* lat, double r, double M5, qed3_dirac** out) {
+  QED3_GUARD_BEGIN
+  if (!lat || !out) return fail(QED3_ERR_ARG, "NULL argument");
+  *out = nullptr;
+  if (!lat->dev.nbr) {
+    cudaGetDevice(&lat->device);
+    int rc0 = lattice_upload(lat);
+    if (rc0) {
+      lattice_free(lat);
+      return rc0;
+    }
+  }
+  auto* d = new qed3_dirac_s;
+  d->lat = lat;
+  d->r = r;
+  d->M5 = M5;
+  int rc = dirac_init_device(d);
+  if (rc) {
+    dirac_free_device(d);
+    delete d;
+    return rc;
+  }
+  *out = d;
+  return QED3_OK;
+  QED3_GUARD_END
+}
+
+int qed3_dirac_destroy(qed3_dirac* d) {
+  if (!d) return QED3_OK;
+  solver_free(d);
+  dirac_free_device(d);
+  delete d;
+  return QED3_OK;
+}
+
+int qed3_dirac_set_links(qed3_dirac* d, const double* A, int A_on_device, void* stream) {
+  QED3_GUARD_BEGIN
+  if (!d || !A) return fail(QED3_ERR_ARG, "NULL argument");
+  return dirac_set_links(d, A, A_on_device, (cudaStream_t)stream);
+  QED3_GUARD_END
+}
+
+int qed3_dirac_set_coefficients(qed3_dirac* d, const double* hop, const double* diag) {
+  QED3_GUARD_BEGIN
+  if (!d || !hop || !diag) return fail(QED3_ERR_ARG, "NULL argument");
+  return dirac_set_coefficients(d, hop, diag);
+  QED3_GUARD_END
+}
+
+int qed3_dirac_apply(qed3_dirac* d, int op, double* out, const double* in, void* stream) {
+  QED3_GUARD_BEGIN
+  if (!d || !out || !in) return fail(QED3_ERR_ARG, "NULL argument");
+  if (op < QED3_OP_D || op > QED3_OP_DDDAG) return fail(QED3_ERR_ARG, "unknown operator");
+  if (!d->coeffs_set) return fail(QED3_ERR_STATE, "operator coefficients not set");
+  return dirac_apply_ref(d, op, out, in, (cudaStream_t)stream);
+  QED3_GUARD_END
+}
+
+size_t qed3_field_bytes(const qed3_dirac* d, int prec, int nrhs) {
+  if (!d || nrhs < 1) return 0;
+  const size_t per = prec == QED3_PREC_F64 ? 32 : prec == QED3_PREC_F32 ? 16 : 8;
+  return per * size_t(d->Ns) * size_t(nrhs);
+}
+
+int qed3_field_import(qed3_dirac* d, int prec, void* field, const double* in_ref, int nrhs, void* stream) {
+  QED3_GUARD_BEGIN
+  if (!d || !field || !in_ref || nrhs < 1) return fail(QED3_ERR_ARG, "bad argument");
+  if (prec < 0 || prec > 2) return fail(QED3_ERR_ARG, "unknown precision");
+  return field_import(d, prec, field, in_ref, nrhs, (cudaStream_t)stream);
+  QED3_GUARD_END
+}
+
+int qed3_field_export(qed3_dirac* d, int prec, double* out_ref, const void* field, int nrhs, void* stream) {
+  QED3_GUARD_BEGIN
+  if (!d || !field || !out_ref || nrhs < 1) return fail(QED3_ERR_ARG, "bad argument");
+  if (prec < 0 || prec > 2) return fail(QED3_ERR_ARG, "unknown precision");
+  return field_export(d, prec, out_ref, field, nrhs, (cudaStream_t)stream);
+  QED3_GUARD_END
+}
+
+int qed3_dirac_apply_field(qed3_dirac* d, int op, int prec, void* out, const void* in, int nrhs, void* stream) {
+  QED3_GUARD_BEGIN
+  if (!d || !out || !in || nrhs < 1) return fail(QED3_ERR_ARG, "bad argument");
+  if (prec < 0 || prec > 2) return fail(QED3_ERR_ARG, "unknown precision");
+  if (!d->coeffs_set) return fail(QED3_ERR_STATE, "operator coefficients not set");
+  if (out == in) return fail(QED3_ERR_ARG, "the stencil gathers: out must not alias in");
+  return dirac_apply_field(d, op, prec, out, in, nrhs, (cudaStream_t)stream);
+  QED3_GUARD_END
+}
+
+int qed3_cg_solve(qed3_dirac* d, double* x, const double* b, const qed3_solve_params* params,
+                  qed3_solve_report* report, void* stream) {
+  QED3_GUARD_BEGIN
+  if (!d || !x || !b) return fail(QED3_ERR_ARG, "NULL argument");
+  return cg_solve(d, x, b, params, report, (cudaStream_t)stream);
+  QED3_GUARD_END
+}
+
+int qed3_solver_last_report(qed3_dirac* d, qed3_solve_report* report) {
+  if (!d || !report) return fail(QED3_ERR_ARG, "NULL argument");
+  *report = d->last;
+  return QED3_OK;
+}
+
+int qed3_plaquette(qed3_lattice* lat, const double* A, double* theta, double* avg, void* stream) {
+  QED3_GUARD_BEGIN
+  if (!lat || !A) return fail(QED3_ERR_ARG, "NULL argument");
+  return gauge_plaquette_avg(lat, A, theta, avg, (cudaStream_t)stream);
+  QED3_GUARD_END
+}
+
+int qed3_gauge_action(qed3_lattice* lat, const double* A, double beta, int compact, double* S, void* stream) {
+  QED3_GUARD_BEGIN
+  if (!lat || !A || !S) return fail(QED3_ERR_ARG, "NULL argument");
+  return gauge_action(lat, A, beta, compact, S, (cudaStream_t)stream);
+  QED3_GUARD_END
+}
+
+int qed3_gauge_force(qed3_lattice* lat, const double* A, double beta, int compact, int exact, double* F, void* stream) {
+  QED3_GUARD_BEGIN
+  if (!lat || !A || !F) return fail(QED3_ERR_ARG, "NULL argument");
+  return gauge_force(lat, A, beta, compact, exact, F, (cudaStream_t)stream);
+  QED3_GUARD_END
+}
+
+int qed3_fermion_force(qed3_dirac* d, const double* eta, double* F, void* stream) {
+  QED3_GUARD_BEGIN
+  if (!d || !eta || !F) return fail(QED3_ERR_ARG, "NULL argument");
+  return fermion_force(d, eta, F, (cudaStream_t)stream);
+  QED3_GUARD_END
+}
+
+int qed3_rng_create(int n_links, int n_sites, int seed, qed3_rng** out) {
+  QED3_GUARD_BEGIN
+  if (!out || n_links < 0 || n_sites < 0) return fail(QED3_ERR_ARG, "bad argument");
+  *out = rng_create(n_links, n_sites, seed);
+  return QED3_OK;
+  QED3_GUARD_END
+}
+
+int qed3_rng_destroy(qed3_rng* r) {
+  rng_destroy(r);
+  return QED3_OK;
+}
+
+int qed3_rng_gaussian_links(qed3_rng* r, double width, double* links) {
+  if (!r || !links) return fail(QED3_ERR_ARG, "NULL argument");
+  rng_gaussian_links(r, width, links);
+  return QED3_OK;
+}
+
+int qed3_rng_gaussian_spinor(qed3_rng* r, double* spinor) {
+  if (!r || !spinor) return fail(QED3_ERR_ARG, "NULL argument");
+  rng_gaussian_spinor(r, spinor);
+  return QED3_OK;
+}
+
+int qed3_hmc_pure_gauge(qed3_lattice* lat, qed3_rng* rng, double* A, double beta, int compact, int exact,
+                        double tmax, int nsteps, int no_reject, int* accepted, double* dH, void* stream) {
+  QED3_GUARD_BEGIN
+  if (!lat || !rng || !A || !accepted || !dH || nsteps < 1) return fail(QED3_ERR_ARG, "bad argument");
+  return hmc_pure_gauge(lat, rng, A, beta, compact, exact, tmax, nsteps, no_reject, accepted, dH,
+                        (cudaStream_t)stream);
+  QED3_GUARD_END
+}
+
+}  // extern "C"

@@ -1,0 +1,26 @@
+// Host-side functions implemented in the .cu translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "handles.h"
+
+namespace qed3 {
+
+int lattice_upload(qed3_lattice_s* lat);
+int lattice_free(qed3_lattice_s* lat);
+
+int dirac_init_device(qed3_dirac_s* d);
+int dirac_free_device(qed3_dirac_s* d);
+int dirac_set_links(qed3_dirac_s* d, const double* A, int on_device, cudaStream_t st);
+int dirac_set_coefficients(qed3_dirac_s* d, const double* hop, const double* diag);
+int dirac_apply_ref(qed3_dirac_s* d, int op, double* out, const double* in, cudaStream_t st);
+int dirac_apply_field(qed3_dirac_s* d, int op, int prec, void* out, const void* in, int nrhs, cudaStream_t st);
+int field_import(qed3_dirac_s* d, int prec, void* field, const double* in_ref, int nrhs, cudaStream_t st);
+int field_export(qed3_dirac_s* d, int prec, double* out_ref, const void* field, int nrhs, cudaStream_t st);
+
+int cg_solve(qed3_dirac_s* d, double* x, const double* b, const qed3_solve_params* prm, qed3_solve_report* rep,
+             cudaStream_t st);
+int solver_free(qed3_dirac_s* d);
+
+}  // namespace qed3

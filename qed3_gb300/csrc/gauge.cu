@@ -1,0 +1,329 @@
+// Gauge side and forces on the device (sm_103a).
+//
+//  * plaquette angles theta_f = sum of oriented link angles around each dual
+//    face (U1onS2::plaquette_angle, src/dual/gauge.h:90-102)
+//  * Wilson action with area weights w_f = mean_vol / vol_f
+//    (src/both/action.h:21-30): compact -beta sum w cos(theta),
+//    non-compact beta/2 sum w theta^2
+//  * gauge force per link from its two faces (src/both/action.h:32-48);
+//    compact force exact (sin theta) or the reference's (theta,
+//    src/dual/action.h:37)
+//  * Wilson fermion force for ALL links in one kernel, F_l = -2 Re <D eta,
+//    dD/dA_l eta> (DiracPf::grad_deviceAsyncLaunch, src/both_3d/dirac_pf.h:107-122,
+//    which launched a full-lattice SpMV per link: O(N_l N) -> O(N_l) here)
+//  * pure-gauge HMC leapfrog (HMCPureGauge, src/both_3d/hmc.h:212-296) with
+//    dH accumulated as per-term differences in FP64.
+
+#include <cmath>
+#include <random>
+#include <vector>
+
+#include "device.cuh"
+#include "dirac_impl.h"
+#include "gauge_impl.h"
+#include "handles.h"
+
+namespace qed3 {
+
+static inline int nblk(long long n, int t = 256) { return int((n + t - 1) / t); }
+
+__global__ void k_plaquettes(int Nf, const int32_t* __restrict__ off, const int32_t* __restrict__ flink,
+                             const int8_t* __restrict__ fsign, const double* __restrict__ A, double* __restrict__ th) {
+  const int f = blockIdx.x * blockDim.x + threadIdx.x;
+  if (f >= Nf) return;
+  double s = 0.0;
+  for (int e = off[f]; e < off[f + 1]; e++) s += double(fsign[e]) * A[flink[e]];
+  th[f] = s;
+}
+
+__device__ __forceinline__ double face_energy(double th, int compact) {
+  return compact ? -cos(th) : 0.5 * th * th;
+}
+__device__ __forceinline__ double face_grad(double th, int compact, int exact) {
+  return (compact && exact) ? sin(th) : th;
+}
+
+// Block partial sums of one or two per-element quantities (deterministic:
+// the host adds the block partials in order).
+template <class F>
+__global__ void k_sum(int n, F f, double* __restrict__ part) {
+  __shared__ double sh[32];
+  double v[1] = {0.0};
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) v[0] += f(i);
+  block_sum<1>(v, sh);
+  if (threadIdx.x == 0) part[blockIdx.x] = v[0];
+}
+
+struct ActionTerm {
+  const double* th;
+  const double* w;
+  int compact;
+  __device__ double operator()(int f) const { return w[f] * face_energy(th[f], compact); }
+};
+struct ActionDiff {  // w (e(theta1) - e(theta0))
+  const double* th1;
+  const double* th0;
+  const double* w;
+  int compact;
+  __device__ double operator()(int f) const {
+    if (compact) {
+      // -cos a + cos b = 2 sin((a+b)/2) sin((a-b)/2): no cancellation
+      const double a = th1[f], b = th0[f];
+      return w[f] * 2.0 * sin(0.5 * (a + b)) * sin(0.5 * (a - b));
+    }
+    return w[f] * 0.5 * (th1[f] - th0[f]) * (th1[f] + th0[f]);
+  }
+};
+struct KinDiff {  // (pi1^2 - pi0^2)/2
+  const double* p1;
+  const double* p0;
+  __device__ double operator()(int l) const { return 0.5 * (p1[l] - p0[l]) * (p1[l] + p0[l]); }
+};
+struct Kin {
+  const double* p;
+  __device__ double operator()(int l) const { return 0.5 * p[l] * p[l]; }
+};
+struct CosTerm {
+  const double* th;
+  __device__ double operator()(int f) const { return cos(th[f]); }
+};
+
+// Each dual link borders exactly two dual faces.
+__global__ void k_gauge_force(int Nl, const int32_t* __restrict__ lf, const int8_t* __restrict__ ls,
+                              const double* __restrict__ th, const double* __restrict__ w, double beta, int compact,
+                              int exact, double* __restrict__ F) {
+  const int l = blockIdx.x * blockDim.x + threadIdx.x;
+  if (l >= Nl) return;
+  const int f0 = lf[2 * l], f1 = lf[2 * l + 1];
+  F[l] = beta * (w[f0] * face_grad(th[f0], compact, exact) * double(ls[2 * l]) +
+                 w[f1] * face_grad(th[f1], compact, exact) * double(ls[2 * l + 1]));
+}
+
+__global__ void k_axpy(int n, double a, const double* __restrict__ x, double* __restrict__ y) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) y[i] += a * x[i];
+}
+
+// F_l = -2 Re[ (D eta)_x^dag (i H_xy eta_y) + (D eta)_y^dag (-i H_yx eta_x) ]
+// with D eta and eta in internal order.
+__global__ void k_fermion_force(int Nl, int Ns, const int32_t* __restrict__ lx, const int32_t* __restrict__ ly,
+                                const int8_t* __restrict__ kx, const int8_t* __restrict__ ky, const M64* __restrict__ H,
+                                const S64* __restrict__ eta, const S64* __restrict__ deta, double* __restrict__ F) {
+  const int l = blockIdx.x * blockDim.x + threadIdx.x;
+  if (l >= Nl) return;
+  const int x = lx[l], y = ly[l];
+  const M64 hxy = H[size_t(kx[l]) * Ns + x], hyx = H[size_t(ky[l]) * Ns + y];
+  const Sp64 ex = ld64(eta, x), ey = ld64(eta, y), dx = ld64(deta, x), dy = ld64(deta, y);
+  // u = H_xy eta_y, v = H_yx eta_x
+  const double2 u0 = cfma(hxy.h01, ey.s1, cmul(hxy.h00, ey.s0));
+  const double2 u1 = cfma(hxy.h11, ey.s1, cmul(hxy.h10, ey.s0));
+  const double2 v0 = cfma(hyx.h01, ex.s1, cmul(hyx.h00, ex.s0));
+  const double2 v1 = cfma(hyx.h11, ex.s1, cmul(hyx.h10, ex.s0));
+  // Re[conj(a) * (i b)] = -(a.x b.y - a.y b.x) = a.y b.x - a.x b.y
+  auto re_ci = [](double2 a, double2 b) { return a.y * b.x - a.x * b.y; };
+  const double inner = re_ci(dx.s0, u0) + re_ci(dx.s1, u1) - re_ci(dy.s0, v0) - re_ci(dy.s1, v1);
+  F[l] = -2.0 * inner;
+}
+
+// ---------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------
+int gauge_prepare(qed3_lattice_s* lat) {
+  GaugeDev& G = lat->gauge;
+  if (G.ready) return QED3_OK;
+  if (!lat->dev.nbr) {
+    int rc = lattice_upload(lat);
+    if (rc) return rc;
+  }
+  const HostLattice& L = lat->host;
+  const int Nl = L.n_links, Nf = L.n_faces;
+  std::vector<int32_t> lf(size_t(2) * Nl, -1);
+  std::vector<int8_t> ls(size_t(2) * Nl, 0);
+  std::vector<int> cnt(Nl, 0);
+  for (int f = 0; f < Nf; f++)
+    for (int e = L.face_offsets[f]; e < L.face_offsets[f + 1]; e++) {
+      const int l = L.face_links[e];
+      if (cnt[l] >= 2) return fail(QED3_ERR_STATE, "link in more than two faces");
+      lf[2 * l + cnt[l]] = f;
+      ls[2 * l + cnt[l]] = L.face_link_sign[e];
+      cnt[l]++;
+    }
+  for (int l = 0; l < Nl; l++)
+    if (cnt[l] != 2) return fail(QED3_ERR_STATE, "link not in two faces");
+  QED3_CUDA_TRY(cudaMalloc(&G.link_face, lf.size() * sizeof(int32_t)));
+  QED3_CUDA_TRY(cudaMalloc(&G.link_fsign, ls.size() * sizeof(int8_t)));
+  QED3_CUDA_TRY(cudaMemcpy(G.link_face, lf.data(), lf.size() * sizeof(int32_t), cudaMemcpyHostToDevice));
+  QED3_CUDA_TRY(cudaMemcpy(G.link_fsign, ls.data(), ls.size() * sizeof(int8_t), cudaMemcpyHostToDevice));
+  QED3_CUDA_TRY(cudaMalloc(&G.th0, size_t(Nf) * sizeof(double)));
+  QED3_CUDA_TRY(cudaMalloc(&G.th1, size_t(Nf) * sizeof(double)));
+  QED3_CUDA_TRY(cudaMalloc(&G.pi, size_t(Nl) * sizeof(double)));
+  QED3_CUDA_TRY(cudaMalloc(&G.pi0, size_t(Nl) * sizeof(double)));
+  QED3_CUDA_TRY(cudaMalloc(&G.F, size_t(Nl) * sizeof(double)));
+  QED3_CUDA_TRY(cudaMalloc(&G.A0, size_t(Nl) * sizeof(double)));
+  QED3_CUDA_TRY(cudaMalloc(&G.part, 1024 * sizeof(double)));
+  G.ready = true;
+  return QED3_OK;
+}
+
+void gauge_free(qed3_lattice_s* lat) {
+  GaugeDev& G = lat->gauge;
+  void* ptrs[] = {G.link_face, G.link_fsign, G.th0, G.th1, G.pi, G.pi0, G.F, G.A0, G.part};
+  for (void* p : ptrs)
+    if (p) cudaFree(p);
+  G = GaugeDev{};
+}
+
+template <class F>
+static int reduce(int n, F f, double* part, double* out, cudaStream_t st) {
+  const int g = std::min(1024, std::max(1, nblk(n)));
+  k_sum<<<g, 256, 0, st>>>(n, f, part);
+  QED3_CUDA_TRY(cudaGetLastError());
+  std::vector<double> h(g);
+  QED3_CUDA_TRY(cudaMemcpyAsync(h.data(), part, size_t(g) * sizeof(double), cudaMemcpyDeviceToHost, st));
+  QED3_CUDA_TRY(cudaStreamSynchronize(st));
+  double s = 0.0;
+  for (double v : h) s += v;
+  *out = s;
+  return QED3_OK;
+}
+
+int gauge_plaquettes(qed3_lattice_s* lat, const double* A, double* th, cudaStream_t st) {
+  const DeviceLattice& D = lat->dev;
+  k_plaquettes<<<nblk(D.Nf), 256, 0, st>>>(D.Nf, D.face_off, D.face_link, D.face_sign, A, th);
+  QED3_CUDA_TRY(cudaGetLastError());
+  return QED3_OK;
+}
+
+int gauge_plaquette_avg(qed3_lattice_s* lat, const double* A, double* theta, double* avg, cudaStream_t st) {
+  int rc = gauge_prepare(lat);
+  if (rc) return rc;
+  double* th = theta ? theta : lat->gauge.th0;
+  if ((rc = gauge_plaquettes(lat, A, th, st))) return rc;
+  if (avg) {
+    double s;
+    if ((rc = reduce(lat->dev.Nf, CosTerm{th}, lat->gauge.part, &s, st))) return rc;
+    *avg = s / lat->dev.Nf;  // U1onS2::average_plaquette, src/dual/gauge.h:104-110
+  }
+  return QED3_OK;
+}
+
+int gauge_action(qed3_lattice_s* lat, const double* A, double beta, int compact, double* S, cudaStream_t st) {
+  int rc = gauge_prepare(lat);
+  if (rc) return rc;
+  if ((rc = gauge_plaquettes(lat, A, lat->gauge.th0, st))) return rc;
+  double s;
+  if ((rc = reduce(lat->dev.Nf, ActionTerm{lat->gauge.th0, lat->dev.face_weight, compact}, lat->gauge.part, &s, st)))
+    return rc;
+  *S = beta * s;
+  return QED3_OK;
+}
+
+int gauge_force(qed3_lattice_s* lat, const double* A, double beta, int compact, int exact, double* F, cudaStream_t st) {
+  int rc = gauge_prepare(lat);
+  if (rc) return rc;
+  const DeviceLattice& D = lat->dev;
+  if ((rc = gauge_plaquettes(lat, A, lat->gauge.th1, st))) return rc;
+  k_gauge_force<<<nblk(D.Nl), 256, 0, st>>>(D.Nl, lat->gauge.link_face, lat->gauge.link_fsign, lat->gauge.th1,
+                                            D.face_weight, beta, compact, exact, F);
+  QED3_CUDA_TRY(cudaGetLastError());
+  return QED3_OK;
+}
+
+int fermion_force(qed3_dirac_s* d, const double* eta_ref, double* F, cudaStream_t st) {
+  if (!d->coeffs_set) return fail(QED3_ERR_STATE, "operator coefficients not set");
+  const DeviceLattice& D = d->lat->dev;
+  int rc = field_import(d, QED3_PREC_F64, d->tmp_in, eta_ref, 1, st);
+  if (rc) return rc;
+  if ((rc = dirac_apply_field(d, QED3_OP_D, QED3_PREC_F64, d->tmp_out, d->tmp_in, 1, st))) return rc;
+  k_fermion_force<<<nblk(D.Nl), 256, 0, st>>>(D.Nl, d->Ns, D.link_x, D.link_y, D.link_kx, D.link_ky, d->H, d->tmp_in,
+                                              d->tmp_out, F);
+  QED3_CUDA_TRY(cudaGetLastError());
+  return QED3_OK;
+}
+
+// ---- RNG: ParallelRng2 (src/both/rng.h:76-125) ------------------------------------
+struct RngEngine {
+  std::mt19937_64 mt;
+  std::normal_distribution<double> g;
+  std::uniform_real_distribution<double> u;
+};
+struct HostRng {
+  RngEngine master;
+  std::vector<RngEngine> links, sites;
+};
+
+}  // namespace qed3
+
+struct qed3_rng_s {
+  qed3::HostRng r;
+};
+
+namespace qed3 {
+
+qed3_rng_s* rng_create(int n_links, int n_sites, int seed) {
+  auto* r = new qed3_rng_s;
+  r->r.links.resize(n_links);
+  r->r.sites.resize(n_sites);
+  r->r.master.mt.seed(seed);
+  for (auto& e : r->r.links) e.mt.seed(r->r.master.mt());
+  for (auto& e : r->r.sites) e.mt.seed(r->r.master.mt());
+  return r;
+}
+void rng_destroy(qed3_rng_s* r) { delete r; }
+void rng_gaussian_links(qed3_rng_s* r, double width, double* out) {
+  for (size_t l = 0; l < r->r.links.size(); l++) out[l] = width * r->r.links[l].g(r->r.links[l].mt);
+}
+void rng_gaussian_spinor(qed3_rng_s* r, double* out) {
+  // ParallelRngExt::fill_gaussian, src/both_3d/rng.h:122-129
+  for (size_t x = 0; x < r->r.sites.size(); x++)
+    for (int a = 0; a < 2; a++) {
+      auto& e = r->r.sites[x];
+      const double re = e.g(e.mt);
+      const double im = e.g(e.mt);
+      out[4 * x + 2 * a] = re / std::sqrt(2.0);
+      out[4 * x + 2 * a + 1] = im / std::sqrt(2.0);
+    }
+}
+double rng_uniform(qed3_rng_s* r) { return r->r.master.u(r->r.master.mt); }
+
+int hmc_pure_gauge(qed3_lattice_s* lat, qed3_rng_s* rng, double* A, double beta, int compact, int exact, double tmax,
+                   int nsteps, int no_reject, int* accepted, double* dH_out, cudaStream_t st) {
+  int rc = gauge_prepare(lat);
+  if (rc) return rc;
+  GaugeDev& G = lat->gauge;
+  const DeviceLattice& D = lat->dev;
+  const int Nl = D.Nl, Nf = D.Nf;
+  std::vector<double> pi(Nl);
+  rng_gaussian_links(rng, 1.0, pi.data());
+  QED3_CUDA_TRY(cudaMemcpyAsync(G.pi, pi.data(), size_t(Nl) * sizeof(double), cudaMemcpyHostToDevice, st));
+  QED3_CUDA_TRY(cudaMemcpyAsync(G.pi0, G.pi, size_t(Nl) * sizeof(double), cudaMemcpyDeviceToDevice, st));
+  QED3_CUDA_TRY(cudaMemcpyAsync(G.A0, A, size_t(Nl) * sizeof(double), cudaMemcpyDeviceToDevice, st));
+  if ((rc = gauge_plaquettes(lat, A, G.th0, st))) return rc;  // theta at the start
+  const double tau = tmax / nsteps;
+  for (int n = 0; n < nsteps; n++) {
+    if ((rc = gauge_force(lat, A, beta, compact, exact, G.F, st))) return rc;
+    k_axpy<<<nblk(Nl), 256, 0, st>>>(Nl, -0.5 * tau, G.F, G.pi);
+    k_axpy<<<nblk(Nl), 256, 0, st>>>(Nl, tau, G.pi, A);
+    if ((rc = gauge_force(lat, A, beta, compact, exact, G.F, st))) return rc;
+    k_axpy<<<nblk(Nl), 256, 0, st>>>(Nl, -0.5 * tau, G.F, G.pi);
+  }
+  QED3_CUDA_TRY(cudaGetLastError());
+  if ((rc = gauge_plaquettes(lat, A, G.th1, st))) return rc;
+  double dk, ds;
+  if ((rc = reduce(Nl, KinDiff{G.pi, G.pi0}, G.part, &dk, st))) return rc;
+  if ((rc = reduce(Nf, ActionDiff{G.th1, G.th0, D.face_weight, compact}, G.part, &ds, st))) return rc;
+  const double dH = dk + beta * ds;
+  *dH_out = dH;
+  const double r = std::min(1.0, std::exp(-dH));
+  const double a = rng_uniform(rng);
+  if (a < r || no_reject) {
+    *accepted = 1;
+  } else {
+    *accepted = 0;
+    QED3_CUDA_TRY(cudaMemcpyAsync(A, G.A0, size_t(Nl) * sizeof(double), cudaMemcpyDeviceToDevice, st));
+  }
+  QED3_CUDA_TRY(cudaStreamSynchronize(st));
+  return QED3_OK;
+}
+
+}  // namespace qed3

@@ -1,0 +1,23 @@
+// Host-side functions of gauge.cu.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "handles.h"
+
+namespace qed3 {
+int gauge_prepare(qed3_lattice_s* lat);
+void gauge_free(qed3_lattice_s* lat);
+int gauge_plaquettes(qed3_lattice_s* lat, const double* A, double* th, cudaStream_t st);
+int gauge_plaquette_avg(qed3_lattice_s* lat, const double* A, double* theta, double* avg, cudaStream_t st);
+int gauge_action(qed3_lattice_s* lat, const double* A, double beta, int compact, double* S, cudaStream_t st);
+int gauge_force(qed3_lattice_s* lat, const double* A, double beta, int compact, int exact, double* F, cudaStream_t st);
+int fermion_force(qed3_dirac_s* d, const double* eta_ref, double* F, cudaStream_t st);
+qed3_rng_s* rng_create(int n_links, int n_sites, int seed);
+void rng_destroy(qed3_rng_s* r);
+void rng_gaussian_links(qed3_rng_s* r, double width, double* out);
+void rng_gaussian_spinor(qed3_rng_s* r, double* out);
+double rng_uniform(qed3_rng_s* r);
+int hmc_pure_gauge(qed3_lattice_s* lat, qed3_rng_s* rng, double* A, double beta, int compact, int exact, double tmax,
+                   int nsteps, int no_reject, int* accepted, double* dH, cudaStream_t st);
+}  // namespace qed3

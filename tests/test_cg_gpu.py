@@ -1,0 +1,89 @@
+"""GPU CG solves (plain FP64 and mixed precision with FP64 reliable updates)
+against the oracle's restatement of MatPoly::solve.
+
+Every solve must be certified by the FP64 true residual
+||b - D^dag D x|| / ||b|| <= tol (recomputed independently here through the
+apply entry point); solutions agree with the oracle's within tol * cond."""
+import numpy as np
+import pytest
+
+import qed3_gb300 as Q
+from oracle import oracle as O
+from tests.gpu_util import from_dev, rand_spinor, to_dev
+
+pytestmark = pytest.mark.gpu
+
+
+def _setup(n, M5, seed, cuda):
+    rng = np.random.default_rng(seed)
+    g = O.geometry(n)
+    lat = Q.S2Trivalent(n)
+    A = rng.uniform(-np.pi, np.pi, g.n_links)
+    Do = O.Dirac(g, 1.0, M5)
+    Do.update(A)
+    Dq = Q.DiracS2Dual(lat, 1.0, M5)
+    Dq.update(A)
+    b = rand_spinor(rng, g.n_sites)
+    return g, lat, Do, Dq, b
+
+
+def _true_res(Dq, x_t, b_t, shift=0.0):
+    q = b_t.clone()
+    Dq.apply(q, x_t, Q.OP_DDAGD)
+    q = q + shift * x_t
+    return float((b_t - q).norm() / b_t.norm())
+
+
+@pytest.mark.parametrize("prec", [Q.PREC_F64, Q.PREC_F32, Q.PREC_BF16])
+def test_cg_matches_oracle_n8(cuda, prec):
+    g, lat, Do, Dq, b = _setup(8, 0.1, 21, cuda)
+    x_ref, it_ref, _ = Do.cg(b, tol=1e-10)
+    bt = to_dev(b, cuda)
+    xt = bt.clone() * 0
+    rep = Dq.solve(xt, bt, tol=1e-10, precision=prec)
+    assert rep.status == Q.OK
+    assert rep.true_rel_res <= 1e-10
+    assert _true_res(Dq, xt, bt) <= 1.05e-10
+    x = from_dev(xt)
+    assert np.linalg.norm(x - x_ref) / np.linalg.norm(x_ref) < 1e-7
+    if prec == Q.PREC_F64:
+        assert abs(rep.iters - it_ref) <= max(5, it_ref // 20)
+    else:
+        assert rep.reliable_updates >= 2
+
+
+@pytest.mark.parametrize("prec", [Q.PREC_F64, Q.PREC_F32])
+def test_cg_n64_certified(cuda, prec):
+    g, lat, Do, Dq, b = _setup(64, 0.05, 22, cuda)
+    bt = to_dev(b, cuda)
+    xt = bt.clone() * 0
+    rep = Dq.solve(xt, bt, tol=1e-10, precision=prec)
+    assert rep.status == Q.OK and rep.true_rel_res <= 1e-10
+    assert _true_res(Dq, xt, bt) <= 1.05e-10
+    # the oracle's residual of the GPU solution (FP64 CSR operator)
+    x = from_dev(xt)
+    r = b - Do.apply(x, 2)
+    assert np.linalg.norm(r) / np.linalg.norm(b) <= 1.05e-10
+
+
+def test_cg_shifted(cuda):
+    g, lat, Do, Dq, b = _setup(8, 0.0, 23, cuda)
+    bt = to_dev(b, cuda)
+    xt = bt.clone() * 0
+    rep = Dq.solve(xt, bt, tol=1e-11, precision=Q.PREC_F32, shift=0.37)
+    assert rep.status == Q.OK
+    x_ref, _, _ = Do.cg(b, tol=1e-12, shift=0.37)
+    assert np.linalg.norm(from_dev(xt) - x_ref) / np.linalg.norm(x_ref) < 1e-9
+    assert _true_res(Dq, xt, bt, 0.37) <= 1.1e-11
+
+
+def test_cg_zero_rhs_and_noconv(cuda):
+    g, lat, Do, Dq, b = _setup(4, 0.1, 24, cuda)
+    import torch
+    z = torch.zeros(2 * g.n_sites, dtype=torch.complex128, device=cuda)
+    x = torch.ones_like(z)
+    rep = Dq.solve(x, z)
+    assert rep.status == Q.OK and rep.iters == 0 and float(x.abs().max()) == 0.0
+    bt = to_dev(b, cuda)
+    rep = Dq.solve(x, bt, tol=1e-14, maxiter=3)
+    assert rep.status == Q.ERR_NOCONV and rep.iters == 3

@@ -1,0 +1,176 @@
+"""The CPU oracle pinned against the reference's own checks and known answers.
+
+Every test here runs without a GPU.  The reference ships no golden vectors for
+this path (its .dat tables are absent), so the oracle is pinned by:
+  * the invariants the reference asserts (spin structure
+    src/both_3d/dirac_dual.h:90-102, face deficits
+    integrator/test_sorting.cc:392-426, total areas src/both_3d/s2n_dual.h:158-160),
+  * gamma5-hermiticity (the condition those invariants guarantee),
+  * the free-spectrum known answers of analysis/ev_dual.ipynb,
+  * the reference's own Zolotarev code (golden fixture),
+  * CG against a dense solve, and finite-difference forces.
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+@pytest.mark.parametrize("n", [1, 2, 3, 4, 8, 16])
+def test_geometry_invariants(n):
+    g = O.geometry(n)
+    assert g.n_sites == 20 * n * n and g.n_links == 30 * n * n and g.n_faces == 10 * n * n + 2
+    assert g.spin_structure_residual() < 1e-12  # reference asserts < 1e-6
+    bad, sums = g.deficits()
+    assert bad == 0
+    assert abs(g.link_volume.sum() - 4 * np.pi) < 1e-10
+    assert abs(g.vols.sum() - 4 * np.pi) < 1e-10
+    sizes = np.diff(g.face_offsets)
+    assert (sizes == 5).sum() == 12 and set(np.unique(sizes)) <= {5, 6}
+    # every site trivalent, links symmetric
+    for x in range(g.n_sites):
+        for y in g.nns[x]:
+            assert x in g.nns[y]
+
+
+def test_gamma5_hermiticity_and_spectrum_known_answers():
+    ref = json.load(open(os.path.join(HERE, "golden", "free_spectrum.json")))["rows"]
+    for n, im2, im1 in ref:
+        g = O.geometry(n)
+        D = O.Dirac(g, 1.0, 0.0)
+        D.update(np.zeros(g.n_links))
+        M = D.dense()
+        g5 = np.diag(np.tile([1.0, -1.0], g.n_sites))
+        assert np.abs(M.conj().T - g5 @ M @ g5).max() < 1e-14
+        ev = np.linalg.eigvals(M)
+        e = ev[np.argsort(ev.real)]
+        lo = np.abs(e[::2].imag)
+        ratio = lo[2] / lo[0]
+        # geometry conventions differ (QFE vs this build), so the j=3/2 : j=1/2
+        # level ratio is compared at the per-mille level (0.3% at n=2)
+        assert abs(ratio - im2 / im1) < (5e-3 if n == 2 else 1e-3), (n, ratio, im2 / im1)
+
+
+def test_zolotarev_matches_reference_build():
+    data = json.load(open(os.path.join(HERE, "golden", "zolotarev_ref.json")))
+    for c in data["cases"]:
+        z = O.zolotarev(c["k"], c["n"])
+        h = lambda v: [float.fromhex(s) for s in v]
+        assert np.array_equal(z["c"], h(c["c"]))
+        assert np.array_equal(z["cp"], h(c["cp"]))
+        assert np.array_equal(z["A"], h(c["A"]))
+        for key in ("M", "lambda_inv", "E", "C"):
+            assert z[key] == float.fromhex(c[key])
+
+
+@pytest.mark.parametrize("k,n", [(0.01, 21), (0.003, 31), (0.2, 11)])
+def test_zolotarev_error_bound(k, n):
+    z = O.zolotarev(k, n)
+    x = np.geomspace(k, 1.0, 20001)
+    err = np.abs(O.zolotarev_eval(z, x) - 1.0).max()
+    delta = (z["lambda_inv"] - 1) / (z["lambda_inv"] + 1)
+    # equioscillation: the max error on [k,1] is Delta (to the accuracy of the
+    # FP64 coefficients)
+    assert abs(err / delta - 1.0) < 1e-2, (err, delta)
+
+
+def test_cg_matches_dense_solve():
+    g = O.geometry(4)
+    rng = np.random.default_rng(3)
+    A = rng.uniform(-np.pi, np.pi, g.n_links)
+    D = O.Dirac(g, 1.0, 0.1)
+    D.update(A)
+    b = rng.normal(size=2 * g.n_sites) + 1j * rng.normal(size=2 * g.n_sites)
+    x, it, mu = D.cg(b, tol=1e-12)
+    M = D.dense()
+    xd = np.linalg.solve(M.conj().T @ M, b)
+    assert np.linalg.norm(x - xd) / np.linalg.norm(xd) < 1e-9
+    assert np.sqrt(mu) / np.linalg.norm(b) < 1e-12
+
+
+def test_dirac_dagger_is_adjoint():
+    g = O.geometry(3)
+    rng = np.random.default_rng(0)
+    D = O.Dirac(g, 1.0, -0.3)
+    D.update(rng.normal(size=g.n_links))
+    u = rng.normal(size=2 * g.n_sites) + 1j * rng.normal(size=2 * g.n_sites)
+    v = rng.normal(size=2 * g.n_sites) + 1j * rng.normal(size=2 * g.n_sites)
+    assert abs(np.vdot(u, D.apply(v, 0)) - np.vdot(D.apply(u, 1), v)) < 1e-12 * np.linalg.norm(u) * np.linalg.norm(v)
+
+
+def test_fermion_force_finite_difference():
+    # src/dual/grad.cu:143-172 (central difference, eps = 1e-5): F_l = dS_f/dA_l
+    # with S_f = |D eta|^2 at fixed eta (the pseudofermion action at fixed eta)
+    g = O.geometry(2)
+    rng = np.random.default_rng(1)
+    A = rng.normal(size=g.n_links) * 0.5
+    D = O.Dirac(g, 1.0, 0.2)
+    D.update(A)
+    eta = rng.normal(size=2 * g.n_sites) + 1j * rng.normal(size=2 * g.n_sites)
+    F = D.fermion_force(A, eta)
+    eps = 1e-5
+    for l in range(0, g.n_links, 7):
+        Ap, Am = A.copy(), A.copy()
+        Ap[l] += eps
+        Am[l] -= eps
+        D.update(Ap)
+        sp = np.linalg.norm(D.apply(eta, 0)) ** 2
+        D.update(Am)
+        sm = np.linalg.norm(D.apply(eta, 0)) ** 2
+        fd = (sp - sm) / (2 * eps)
+        # F = -2 Re<D eta, dD eta> is -dS/dA for S = |D eta|^2 ... sign convention of
+        # DiracPf::grad_deviceAsyncLaunch: the returned value is -(d/dA)|D eta|^2
+        assert abs(F[l] + fd) < 1e-6 * max(1.0, abs(fd)), (l, F[l], fd)
+
+
+@pytest.mark.parametrize("compact", [True, False])
+def test_gauge_force_finite_difference(compact):
+    g = O.geometry(2)
+    rng = np.random.default_rng(2)
+    A = rng.normal(size=g.n_links)
+    beta = 1.4
+    F = O.gauge_force(g, A, beta, compact=compact, exact=True)
+    eps = 1e-5
+    for l in range(0, g.n_links, 5):
+        Ap, Am = A.copy(), A.copy()
+        Ap[l] += eps
+        Am[l] -= eps
+        fd = (O.gauge_action(g, Ap, beta, compact) - O.gauge_action(g, Am, beta, compact)) / (2 * eps)
+        assert abs(F[l] - fd) < 1e-6 * max(1.0, abs(fd))
+
+
+def test_compact_force_reference_mode_uses_theta():
+    # src/dual/action.h:37 differentiates the compact action as if it were
+    # non-compact; the oracle's force_mode 0 reproduces that.
+    g = O.geometry(2)
+    A = np.random.default_rng(4).normal(size=g.n_links)
+    f_ref = O.gauge_force(g, A, 1.0, compact=True, exact=False)
+    f_nc = O.gauge_force(g, A, 1.0, compact=False, exact=True)
+    assert np.allclose(f_ref, f_nc, rtol=0, atol=1e-14)
+
+
+def test_hmc_pure_gauge_reversible_and_deltaH_scaling():
+    # HMC dH ~ tau^2 (src/both_3d/grad.cu:353-369, guide 100 tau^2)
+    g = O.geometry(2)
+    dHs = []
+    for nsteps in (10, 20, 40):
+        rng = O.Rng(g, 5)
+        A = np.ascontiguousarray(rng.gaussian_links(0.3))
+        _, dH = O.hmc_pure_gauge(g, rng, A, 1.4, compact=True, exact=True, tmax=1.0, nsteps=nsteps, no_reject=True)
+        dHs.append(abs(dH))
+    r1, r2 = dHs[0] / dHs[1], dHs[1] / dHs[2]
+    assert 2.5 < r1 < 6 and 2.5 < r2 < 6, dHs
+
+
+def test_rng_streams_are_deterministic():
+    g = O.geometry(1)
+    a = O.Rng(g, 7).gaussian_spinor()
+    b = O.Rng(g, 7).gaussian_spinor()
+    c = O.Rng(g, 8).gaussian_spinor()
+    assert np.array_equal(a, b) and not np.array_equal(a, c)
+    assert abs(np.mean(np.abs(a) ** 2) - 1.0) < 0.5
