@@ -156,6 +156,25 @@ def cpu_reference_solve(b, A, threads=None):
     return dt, it, float(np.linalg.norm(r) / np.linalg.norm(b)), O.num_threads()
 
 
+def profile_case(torch, which):
+    """Small cases for ncu captures (a few hundred MB on the device)."""
+    import qed3_gb300 as Q
+    if which == "apply":
+        for prec in (Q.PREC_F32, Q.PREC_BF16, Q.PREC_F64):
+            r = apply_bandwidth(torch, Q, 512, prec, reps=3)
+            print(json.dumps(r))
+    else:
+        lat = Q.S2Trivalent(N_REFINE)
+        D = Q.DiracS2Dual(lat, 1.0, M5)
+        A = torch.from_numpy(np.random.default_rng(2).uniform(-np.pi, np.pi, lat.n_links)).cuda()
+        D.update(A)
+        b = torch.from_numpy(Q.ParallelRng(lat, 7).gaussian_spinor()).cuda()
+        x = torch.zeros_like(b)
+        rep = D.solve(x, b, tol=TOL, precision=Q.PREC_F32)
+        print(json.dumps(rep.__dict__))
+    torch.cuda.synchronize()
+
+
 def peaks():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -171,11 +190,16 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile", choices=["apply", "cg"], default=None,
+                    help="small self-contained case for ncu: 'apply' = D apply at n=512 (f32, bf16, f64; "
+                         "HBM-resident), 'cg' = one n=64 mixed-precision solve")
     args = ap.parse_args()
     rank, world, local = env_rank()
     warmup = max(3, args.warmup)
 
     import torch
+    if args.profile:
+        return profile_case(torch, args.profile)
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
@@ -269,10 +293,13 @@ def main():
     alg_bytes = per_site_iter * lat.n_sites * iters
     achieved = alg_bytes / (results[best]["ms"] * 1e-3) / 1e9
     peak, peak_kind = peaks()
-    sweep = [apply_bandwidth(torch, Q, n, p) for n, p in ((256, Q.PREC_F32), (512, Q.PREC_F32),
-                                                          (512, Q.PREC_BF16), (256, Q.PREC_F64))]
-    for s in sweep:
+    sweep = []
+    for n, p in ((64, Q.PREC_F32), (256, Q.PREC_F32), (512, Q.PREC_F32), (512, Q.PREC_BF16), (256, Q.PREC_F64),
+                 (512, Q.PREC_F64)):
+        s = apply_bandwidth(torch, Q, n, p)
         s["frac_of_" + peak_kind] = s["GB/s"] / peak
+        s["resident"] = "L2" if s["bytes_per_site"] * 20 * n * n < 100e6 else "HBM"
+        sweep.append(s)
 
     line = {"metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps,
             "warmup": warmup, "ms_per_step": ms_best, "higher_is_better": True, "scaling": "weak",

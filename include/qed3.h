@@ -166,6 +166,14 @@ int qed3_rng_gaussian_spinor(qed3_rng* r, double* spinor);
 int qed3_hmc_pure_gauge(qed3_lattice* lat, qed3_rng* rng, double* A, double beta, int compact, int exact,
                         double tmax, int nsteps, int no_reject, int* accepted, double* dH, void* stream);
 
+/* ======================================================================
+ * Zolotarev coefficients  --  replaces Zolotarev(k, n) / Zolotarev::update
+ * (src/both_3d/overlap.h:7-116): r(x) = C x (1 + sum_m A[m]/(x^2 - k^2/cp[m])).
+ * Host arrays of length n/2+1 (index 0 unused); scal = {M, lambda_inv, E, C}.
+ * Returns the size n/2+1 through *size.
+ * ====================================================================== */
+int qed3_zolotarev(double k, int n, double* c, double* cp, double* A, double* scal, int* size);
+
 #ifdef __cplusplus
 }
 #endif

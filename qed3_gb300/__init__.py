@@ -86,6 +86,7 @@ SIGNATURES = [
     ("qed3_rng_gaussian_spinor", ctypes.c_int, [vp, vp]),
     ("qed3_hmc_pure_gauge", ctypes.c_int, [vp, vp, vp, ctypes.c_double, ctypes.c_int, ctypes.c_int, ctypes.c_double,
                                            ctypes.c_int, ctypes.c_int, c_int_p, c_double_p, vp]),
+    ("qed3_zolotarev", ctypes.c_int, [ctypes.c_double, ctypes.c_int, vp, vp, vp, vp, c_int_p]),
 ]
 
 
@@ -335,3 +336,12 @@ def thermalized_links(lattice: S2Trivalent, beta: float, seed: int, ntraj: int, 
         a, _ = hmc_pure_gauge(lattice, rng, A, beta, compact, True, 1.0, nsteps)
         acc += a
     return A, acc / max(1, ntraj)
+
+
+def zolotarev(k: float, n: int) -> dict:
+    """Zolotarev coefficients of sign(x) on [k, 1] (Zolotarev, src/both_3d/overlap.h:7-116)."""
+    size = n // 2 + 1
+    c, cp, A, sc = np.zeros(size), np.zeros(size), np.zeros(size), np.zeros(4)
+    sz = ctypes.c_int()
+    _check(lib().qed3_zolotarev(k, n, _ptr(c), _ptr(cp), _ptr(A), _ptr(sc), ctypes.byref(sz)))
+    return dict(c=c, cp=cp, A=A, M=sc[0], lambda_inv=sc[1], E=sc[2], C=sc[3], size=size, k=k, n=n)

@@ -342,4 +342,25 @@ int qed3_hmc_pure_gauge(qed3_lattice* lat, qed3_rng* rng, double* A, double beta
   QED3_GUARD_END
 }
 
+int qed3_zolotarev(double k, int n, double* c, double* cp, double* A, double* scal, int* size) {
+  QED3_GUARD_BEGIN
+  ZoloCoeffs z;
+  const int rc = zolotarev_coeffs(k, n, z);
+  if (rc) return rc;
+  for (int m = 0; m < z.size; m++) {
+    if (c) c[m] = z.c[m];
+    if (cp) cp[m] = z.cp[m];
+    if (A) A[m] = z.A[m];
+  }
+  if (scal) {
+    scal[0] = z.M;
+    scal[1] = z.lambda_inv;
+    scal[2] = z.E;
+    scal[3] = z.C;
+  }
+  if (size) *size = z.size;
+  return QED3_OK;
+  QED3_GUARD_END
+}
+
 }  // extern "C"

@@ -351,12 +351,13 @@ int build_lattice(int n, bool sfc_order, HostLattice& L) {
   // (integrator/test_sorting.cc:203-235); alpha(x,y) = angle of the geodesic
   // x -> y at x in (-pi, pi] for x<y and in [0, 2pi) for x>y, the ranges the
   // reference's tables carry (integrator/test_sorting.cc:240-289).
+  // The reference's test |d1| + |d2| - |d| < 1e-6 (and its refusal of sites
+  // within 1e-6 of the cut) is replaced by the exact side test: a link crosses
+  // the cut when its endpoints lie on opposite sides of the half-meridian phi0
+  // and its short arc passes through phi0 (not phi0 + pi).  Both agree when
+  // no site is within 1e-6 of the cut; for n >= 256 some are, and the exact
+  // test keeps every face consistent.
   const double phi0 = M_PI / 48.0;
-  for (int64_t t = 0; t < Ns; t++) {
-    double ph = std::atan2(site[t].y, site[t].x);
-    if (ph < 0) ph += 2.0 * M_PI;
-    if (std::abs(ph - phi0) <= 1e-6) return fail(QED3_ERR_STATE, "a dual site lies on the section cut");
-  }
   L.omega.resize(size_t(Nl));
   for (int64_t l = 0; l < Nl; l++) {
     const V3 x = site[L.links[2 * l]], y = site[L.links[2 * l + 1]];
@@ -367,8 +368,9 @@ int build_lattice(int n, bool sfc_order, HostLattice& L) {
       return a;
     };
     const double p1 = std::atan2(x.y, x.x), p2 = std::atan2(y.y, y.x);
-    const double d1 = wrap(p1 - phi0), d2 = wrap(p2 - phi0), d = wrap(p1 - p2);
-    if (std::abs(d1) + std::abs(d2) - std::abs(d) < 1e-6) om -= 2.0 * M_PI;
+    const double d1 = wrap(p1 - phi0), d2 = wrap(p2 - phi0);
+    const bool opposite = (d1 >= 0.0) != (d2 >= 0.0);
+    if (opposite && std::abs(d1) + std::abs(d2) < M_PI) om -= 2.0 * M_PI;
     L.omega[l] = om;
   }
   L.alpha.resize(size_t(Ns) * 3);
