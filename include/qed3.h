@@ -134,6 +134,27 @@ int qed3_cg_solve(qed3_dirac* d, double* x, const double* b, const qed3_solve_pa
 int qed3_solver_last_report(qed3_dirac* d, qed3_solve_report* report);
 
 /* ======================================================================
+ * Batched solves in ONE persistent launch  --  replaces the reference's
+ * loops of MatPoly::solve over pseudofermions and Zolotarev poles on OpenMP
+ * threads and CUDA streams (src/both_3d/overlap.h:309-332,
+ * src/both_3d/hmc.h:172-200).  System u solves (D_u^dag D_u + shift) x = b
+ * for nrhs[u] right-hand sides; systems may live on different lattices.
+ * rhs_tile (1, 2, 4, 8: right-hand sides sharing each stencil read) and
+ * threads (128, 256) are chosen by the built-in autotuner when passed as 0.
+ * ====================================================================== */
+typedef struct qed3_batch_s qed3_batch;
+int qed3_batch_create(int nsys, qed3_dirac* const* ops, const int* nrhs, int precision, int rhs_tile, int threads,
+                      qed3_batch** out);
+int qed3_batch_destroy(qed3_batch* bt);
+/* tile and threads the batch runs with */
+int qed3_batch_config(const qed3_batch* bt, int* rhs_tile, int* threads, int* blocks);
+/* x[u], b[u]: device complex128, nrhs[u] vectors back to back (reference order);
+ * shifts[u]: host [nrhs[u]] or NULL (then params->shift); reports: host
+ * [sum nrhs] in system order, may be NULL; ms: device time of the launch. */
+int qed3_batch_solve(qed3_batch* bt, double* const* x, const double* const* b, const double* const* shifts,
+                     const qed3_solve_params* params, qed3_solve_report* reports, float* ms, void* stream);
+
+/* ======================================================================
  * Gauge side  --  replaces U1onS2::plaquette_angle/average_plaquette
  * (src/dual/gauge.h:90-110) and U1Wilson::operator()/get_force
  * (src/both/action.h:21-48, weights mean_vol/vol_f) on the dual faces.

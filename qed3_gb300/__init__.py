@@ -87,6 +87,12 @@ SIGNATURES = [
     ("qed3_hmc_pure_gauge", ctypes.c_int, [vp, vp, vp, ctypes.c_double, ctypes.c_int, ctypes.c_int, ctypes.c_double,
                                            ctypes.c_int, ctypes.c_int, c_int_p, c_double_p, vp]),
     ("qed3_zolotarev", ctypes.c_int, [ctypes.c_double, ctypes.c_int, vp, vp, vp, vp, c_int_p]),
+    ("qed3_batch_create", ctypes.c_int, [ctypes.c_int, vp, vp, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                         ctypes.POINTER(vp)]),
+    ("qed3_batch_destroy", ctypes.c_int, [vp]),
+    ("qed3_batch_config", ctypes.c_int, [vp, c_int_p, c_int_p, c_int_p]),
+    ("qed3_batch_solve", ctypes.c_int, [vp, vp, vp, vp, ctypes.POINTER(SolveParams), vp,
+                                        ctypes.POINTER(ctypes.c_float), vp]),
 ]
 
 
@@ -345,3 +351,53 @@ def zolotarev(k: float, n: int) -> dict:
     sz = ctypes.c_int()
     _check(lib().qed3_zolotarev(k, n, _ptr(c), _ptr(cp), _ptr(A), _ptr(sc), ctypes.byref(sz)))
     return dict(c=c, cp=cp, A=A, M=sc[0], lambda_inv=sc[1], E=sc[2], C=sc[3], size=size, k=k, n=n)
+
+
+# ---------------------------------------------------------------------------
+# batched persistent solver
+# ---------------------------------------------------------------------------
+class Batch:
+    """Several CG systems (lattices, right-hand sides, shifts) in one persistent launch.
+
+    systems: list of (DiracS2Dual, nrhs).  rhs_tile / threads = 0 lets the
+    built-in autotuner choose."""
+
+    def __init__(self, systems, precision: int = PREC_F32, rhs_tile: int = 0, threads: int = 0):
+        self.systems = list(systems)
+        n = len(self.systems)
+        ops = (vp * n)(*[s[0].handle for s in self.systems])
+        nr = (ctypes.c_int * n)(*[int(s[1]) for s in self.systems])
+        h = vp()
+        _check(lib().qed3_batch_create(n, ops, nr, precision, rhs_tile, threads, ctypes.byref(h)))
+        self._h = h
+        R, T, B = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        _check(lib().qed3_batch_config(h, ctypes.byref(R), ctypes.byref(T), ctypes.byref(B)))
+        self.rhs_tile, self.threads, self.blocks = R.value, T.value, B.value
+
+    def solve(self, xs, bs, shifts=None, tol: float = 1e-10, maxiter: int = 100000, precision: int = PREC_F32,
+              delta: float = 0.1, stream=None):
+        """xs[u], bs[u]: device complex128 tensors of shape (nrhs_u, 2*n_sites) (or flat)."""
+        n = len(self.systems)
+        X = (vp * n)(*[x.data_ptr() for x in xs])
+        B = (vp * n)(*[b.data_ptr() for b in bs])
+        keep = []
+        if shifts is not None:
+            arrs = [np.ascontiguousarray(s, dtype=np.float64) if s is not None else None for s in shifts]
+            keep = arrs
+            S = (vp * n)(*[(a.ctypes.data if a is not None else None) for a in arrs])
+        else:
+            S = None
+        total = sum(int(s[1]) for s in self.systems)
+        reps = (SolveReport * total)()
+        p = SolveParams(tol, maxiter, precision, delta, 0.0, 0)
+        ms = ctypes.c_float()
+        rc = lib().qed3_batch_solve(self._h, X, B, S, ctypes.byref(p), reps, ctypes.byref(ms), _stream(stream))
+        del keep
+        if rc not in (OK, ERR_NOCONV):
+            _check(rc)
+        return [Report(r.status, r.iters, r.reliable_updates, r.true_rel_res, r.ms) for r in reps], ms.value
+
+    def __del__(self):
+        if getattr(self, "_h", None) and _lib is not None:
+            _lib.qed3_batch_destroy(self._h)
+            self._h = None

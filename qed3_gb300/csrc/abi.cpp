@@ -10,6 +10,7 @@
 #include <string>
 #include <vector>
 
+#include "batched_impl.h"
 #include "dirac_impl.h"
 #include "gauge_impl.h"
 #include "handles.h"
@@ -339,6 +340,41 @@ int qed3_hmc_pure_gauge(qed3_lattice* lat, qed3_rng* rng, double* A, double beta
   if (!lat || !rng || !A || !accepted || !dH || nsteps < 1) return fail(QED3_ERR_ARG, "bad argument");
   return hmc_pure_gauge(lat, rng, A, beta, compact, exact, tmax, nsteps, no_reject, accepted, dH,
                         (cudaStream_t)stream);
+  QED3_GUARD_END
+}
+
+int qed3_batch_create(int nsys, qed3_dirac* const* ops, const int* nrhs, int precision, int rhs_tile, int threads,
+                      qed3_batch** out) {
+  QED3_GUARD_BEGIN
+  if (!out || !ops || !nrhs || nsys < 1) return fail(QED3_ERR_ARG, "bad argument");
+  if (precision < 0 || precision > 2) return fail(QED3_ERR_ARG, "unknown precision");
+  for (int u = 0; u < nsys; u++)
+    if (!ops[u] || nrhs[u] < 1) return fail(QED3_ERR_ARG, "each system needs an operator and >= 1 rhs");
+  *out = nullptr;
+  return batch_create(nsys, ops, nrhs, precision, rhs_tile, threads, out);
+  QED3_GUARD_END
+}
+
+int qed3_batch_destroy(qed3_batch* bt) {
+  batch_destroy(bt);
+  return QED3_OK;
+}
+
+int qed3_batch_config(const qed3_batch* bt, int* rhs_tile, int* threads, int* blocks) {
+  if (!bt) return fail(QED3_ERR_ARG, "NULL batch");
+  if (rhs_tile) *rhs_tile = bt->R;
+  if (threads) *threads = bt->threads;
+  if (blocks) *blocks = bt->grid;
+  return QED3_OK;
+}
+
+int qed3_batch_solve(qed3_batch* bt, double* const* x, const double* const* b, const double* const* shifts,
+                     const qed3_solve_params* params, qed3_solve_report* reports, float* ms, void* stream) {
+  QED3_GUARD_BEGIN
+  if (!bt || !x || !b) return fail(QED3_ERR_ARG, "NULL argument");
+  for (size_t u = 0; u < bt->user_ops.size(); u++)
+    if (!x[u] || !b[u]) return fail(QED3_ERR_ARG, "NULL vector");
+  return batch_solve(bt, x, b, shifts, params, reports, ms, (cudaStream_t)stream);
   QED3_GUARD_END
 }
 

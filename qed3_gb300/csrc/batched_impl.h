@@ -1,0 +1,81 @@
+// Batched persistent solver: device descriptors and host entry points.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <vector>
+
+#include "handles.h"
+
+namespace qed3 {
+
+constexpr int kMaxTile = 8;  // right-hand sides per system (compile-time tile)
+
+struct BatchSys {
+  int Ns, nrhs, blk0, blk1;
+  const int* nbr;
+  const M64* H;
+  const M64* Hd;
+  const double* diag;
+  const M32* H32;
+  const M32* Hd32;
+  const float* diag32;
+  double shift[kMaxTile];
+  const S64* b;
+  S64* xhi;
+  S64* xhi2;
+  S64* t64;
+  void* r;
+  void* p;
+  void* t;
+  void* xlo;
+  double* scal;  // [nrhs][6]: mu_true, bnorm2, iters, reliable updates, status, x buffer
+};
+
+struct BatchArgs {
+  const BatchSys* sys;
+  const int* sys_of_block;
+  int nsys;
+  double* partials;
+  GridBar* bar;
+  int* status;
+  double tol2, delta2;
+  int maxiter;
+  long long spin_limit;
+};
+
+int batch_occupancy(int prec, int R, int threads, int* per_sm);
+int batch_launch(int prec, int R, BatchArgs& args, int grid, int threads, cudaStream_t st);
+int batch_import(const BatchSys& s, const qed3_dirac_s* d, const double* b_ref, int R, cudaStream_t st);
+int batch_export(const BatchSys& s, const qed3_dirac_s* d, double* x_ref, int R, cudaStream_t st);
+
+}  // namespace qed3
+
+// A batch: user systems split into internal systems of at most R right-hand
+// sides, with their workspaces and the block partition of the launch.
+struct qed3_batch_s {
+  int prec = 0, R = 1, threads = 256, grid = 0;
+  std::vector<qed3_dirac_s*> user_ops;
+  std::vector<int> user_nrhs;
+  // internal systems
+  std::vector<int> owner, first_rhs;  // user system and its first rhs
+  std::vector<qed3::BatchSys> sys;
+  qed3::BatchSys* d_sys = nullptr;
+  int* d_sys_of_block = nullptr;
+  double* partials = nullptr;
+  qed3::GridBar* bar = nullptr;
+  int* d_status = nullptr;
+  double* d_scal = nullptr;
+  std::vector<void*> buffers;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+};
+
+namespace qed3 {
+int batch_create(int nsys, qed3_dirac_s* const* ops, const int* nrhs, int prec, int rhs_tile, int threads,
+                 qed3_batch_s** out);
+void batch_destroy(qed3_batch_s* bt);
+int batch_solve(qed3_batch_s* bt, double* const* x, const double* const* b, const double* const* shifts,
+                const qed3_solve_params* prm, qed3_solve_report* reports, float* ms_out, cudaStream_t st);
+int batch_autotune(qed3_batch_s* proto, int* best_R, int* best_threads,
+                   std::vector<std::pair<std::pair<int, int>, float>>* log);
+}  // namespace qed3

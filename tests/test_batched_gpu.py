@@ -1,0 +1,82 @@
+"""Batched persistent solver: several lattices, right-hand sides and shifts in
+one cooperative launch, each solution certified by its FP64 true residual and
+compared with the oracle's CG (src/dual/matpoly.h:204-267 restated)."""
+import numpy as np
+import pytest
+
+import qed3_gb300 as Q
+from oracle import oracle as O
+from tests.gpu_util import from_dev, to_dev
+
+pytestmark = pytest.mark.gpu
+
+
+def _systems(cuda, ns=(2, 4, 8), nrhs=(3, 2, 5), seed=50):
+    rng = np.random.default_rng(seed)
+    out = []
+    for n, k in zip(ns, nrhs):
+        g = O.geometry(n)
+        lat = Q.S2Trivalent(n)
+        A = rng.uniform(-np.pi, np.pi, g.n_links)
+        M5 = float(rng.uniform(0.02, 0.2))
+        Do = O.Dirac(g, 1.0, M5)
+        Do.update(A)
+        Dq = Q.DiracS2Dual(lat, 1.0, M5)
+        Dq.update(A)
+        b = rng.normal(size=(k, 2 * g.n_sites)) + 1j * rng.normal(size=(k, 2 * g.n_sites))
+        out.append((g, lat, Do, Dq, b))
+    return out
+
+
+@pytest.mark.parametrize("prec", [Q.PREC_F64, Q.PREC_F32, Q.PREC_BF16])
+@pytest.mark.parametrize("tile,threads", [(1, 256), (2, 128), (4, 256), (8, 128)])
+def test_batched_multi_lattice(cuda, prec, tile, threads):
+    sy = _systems(cuda)
+    batch = Q.Batch([(s[3], s[4].shape[0]) for s in sy], precision=prec, rhs_tile=tile, threads=threads)
+    assert batch.rhs_tile == tile and batch.threads == threads
+    bs = [to_dev(s[4], cuda) for s in sy]
+    xs = [b.clone() * 0 for b in bs]
+    reps, ms = batch.solve(xs, bs, tol=1e-10, precision=prec)
+    k = 0
+    for (g, lat, Do, Dq, b), xt in zip(sy, xs):
+        x = from_dev(xt)
+        for r in range(b.shape[0]):
+            rep = reps[k]
+            k += 1
+            assert rep.status == Q.OK, rep
+            assert rep.true_rel_res <= 1e-10
+            res = np.linalg.norm(b[r] - Do.apply(x[r], 2)) / np.linalg.norm(b[r])
+            assert res <= 1.05e-10, (r, res)
+            xr, _, _ = Do.cg(b[r], tol=1e-10)
+            assert np.linalg.norm(x[r] - xr) / np.linalg.norm(xr) < 1e-7
+
+
+def test_batched_shifts_and_autotune(cuda):
+    sy = _systems(cuda, ns=(4, 8), nrhs=(4, 3), seed=51)
+    batch = Q.Batch([(s[3], s[4].shape[0]) for s in sy], precision=Q.PREC_F32)  # autotuned
+    assert batch.rhs_tile in (1, 2, 4, 8) and batch.threads in (128, 256)
+    shifts = [np.array([0.0, 0.1, 0.5, 2.0]), np.array([0.03, 0.3, 1.0])]
+    bs = [to_dev(s[4], cuda) for s in sy]
+    xs = [b.clone() * 0 for b in bs]
+    reps, ms = batch.solve(xs, bs, shifts=shifts, tol=1e-11, precision=Q.PREC_F32)
+    k = 0
+    for (g, lat, Do, Dq, b), xt, sh in zip(sy, xs, shifts):
+        x = from_dev(xt)
+        for r in range(b.shape[0]):
+            assert reps[k].status == Q.OK
+            k += 1
+            res = np.linalg.norm(b[r] - Do.apply(x[r], 2) - sh[r] * x[r]) / np.linalg.norm(b[r])
+            assert res <= 1.1e-11
+
+
+def test_batched_zero_rhs_and_noconv(cuda):
+    sy = _systems(cuda, ns=(2, 4), nrhs=(2, 1), seed=52)
+    batch = Q.Batch([(s[3], s[4].shape[0]) for s in sy], precision=Q.PREC_F32, rhs_tile=2, threads=128)
+    bs = [to_dev(s[4], cuda) for s in sy]
+    bs[0][1].zero_()
+    xs = [b.clone() + 1 for b in bs]
+    reps, _ = batch.solve(xs, bs, tol=1e-10, precision=Q.PREC_F32)
+    assert reps[1].status == Q.OK and reps[1].iters == 0 and float(xs[0][1].abs().max()) == 0.0
+    assert reps[0].status == Q.OK and reps[2].status == Q.OK
+    reps, _ = batch.solve(xs, bs, tol=1e-14, maxiter=4, precision=Q.PREC_F32)
+    assert reps[0].status == Q.ERR_NOCONV and reps[0].iters == 4
