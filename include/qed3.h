@@ -108,7 +108,7 @@ int qed3_dirac_apply_field(qed3_dirac* d, int op, int prec, void* out, const voi
  * Solvers  --  replace MatPoly::solve<N> (src/dual/matpoly.h:204-267):
  * CG on (D^dagger D + shift) x = b from x0 = 0.
  * ====================================================================== */
-#define QED3_SOLVE_RECURSIVE_STOP 1 /* stop on the recursive residual alone, as MatPoly::solve */
+#define QED3_SOLVE_STREAMING 2 /* force the memory-streaming persistent kernel (default: register-resident when it fits) */
 
 typedef struct {
   double tol;     /* target ||b - A x|| / ||b|| of the FP64 true residual */
@@ -132,6 +132,7 @@ typedef struct {
 int qed3_cg_solve(qed3_dirac* d, double* x, const double* b, const qed3_solve_params* params,
                   qed3_solve_report* report, void* stream);
 int qed3_solver_last_report(qed3_dirac* d, qed3_solve_report* report);
+
 
 /* ======================================================================
  * Batched solves in ONE persistent launch  --  replaces the reference's

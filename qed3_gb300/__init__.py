@@ -31,6 +31,7 @@ LIB_PATH = os.path.join(_HERE, "libqed3.so")
 OK, ERR_ARG, ERR_CUDA, ERR_NOCONV, ERR_TIMEOUT, ERR_STATE, ERR_NOMEM = range(7)
 OP_D, OP_DDAG, OP_DDAGD, OP_DDDAG = range(4)
 PREC_F64, PREC_F32, PREC_BF16 = range(3)
+SOLVE_STREAMING = 2
 PREC_NAMES = {"f64": PREC_F64, "f32": PREC_F32, "bf16": PREC_BF16}
 BYTES_PER_SITE = {PREC_F64: 32, PREC_F32: 16, PREC_BF16: 8}
 
@@ -238,9 +239,9 @@ class DiracS2Dual:
 
     # -- solver ----------------------------------------------------------------------
     def solve(self, x, b, tol: float = 1e-10, maxiter: int = 100000, precision: int = PREC_F64,
-              delta: float = 0.1, shift: float = 0.0, stream=None) -> Report:
+              delta: float = 0.1, shift: float = 0.0, flags: int = 0, stream=None) -> Report:
         """CG on (D^dagger D + shift) x = b (MatPoly::solve); certified by the FP64 true residual."""
-        p = SolveParams(tol, maxiter, precision, delta, shift, 0)
+        p = SolveParams(tol, maxiter, precision, delta, shift, flags)
         r = SolveReport()
         rc = lib().qed3_cg_solve(self._h, _ptr(x), _ptr(b), ctypes.byref(p), ctypes.byref(r), _stream(stream))
         if rc not in (OK, ERR_NOCONV):

@@ -110,8 +110,12 @@ __global__ void __launch_bounds__(256) k_batched_cg(BatchArgs a) {
   S64* r64 = reinterpret_cast<S64*>(S.r);
   S64* p64 = reinterpret_cast<S64*>(S.p);
   S64* t64w = reinterpret_cast<S64*>(S.t);
-  Lo* rlo = reinterpret_cast<Lo*>(S.r);
-  Lo* tlo = reinterpret_cast<Lo*>(S.t);
+  // mixed modes: r, t are fp32 state; neighbours are read from rh / th, which
+  // alias r / t in fp32 mode and are bf16 copies in bf16 mode
+  float4* r32 = reinterpret_cast<float4*>(S.r);
+  float4* t32 = reinterpret_cast<float4*>(S.t);
+  Lo* rh = reinterpret_cast<Lo*>(P == PBF16 ? S.rh : S.r);
+  Lo* th = reinterpret_cast<Lo*>(P == PBF16 ? S.th : S.t);
   float4* p32 = reinterpret_cast<float4*>(S.p);
   float4* xlo = reinterpret_cast<float4*>(S.xlo);
   S64* xa = S.xhi;
@@ -158,8 +162,12 @@ __global__ void __launch_bounds__(256) k_batched_cg(BatchArgs a) {
           } else {
             const Sp32 bl{make_float2(float(bi.s0.x), float(bi.s0.y)), make_float2(float(bi.s1.x), float(bi.s1.y))};
             const Sp32 zl{make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
-            LoField<P>::st(rlo, int(e), bl);
-            LoField<P>::st(tlo, int(e), zl);
+            st32(r32, int(e), bl);
+            st32(t32, int(e), zl);
+            if constexpr (P == PBF16) {
+              stbf(reinterpret_cast<uint2*>(rh), int(e), bl);
+              stbf(reinterpret_cast<uint2*>(th), int(e), zl);
+            }
             st32(p32, int(e), zl);
             st32(xlo, int(e), zl);
           }
@@ -208,17 +216,17 @@ __global__ void __launch_bounds__(256) k_batched_cg(BatchArgs a) {
           for (int r = 0; r < R; r++) {
             if (r >= nr || !sc.active[r]) continue;
             const int e = i * R + r;
-            const Sp32 self = LoField<P>::ld(rlo, e);
+            const Sp32 self = ld32(r32, e);
             Sp32 o{make_float2(dg * self.s0.x, dg * self.s0.y), make_float2(dg * self.s1.x, dg * self.s1.y)};
 #pragma unroll
             for (int k = 0; k < 3; k++) {
-              const Sp32 bk = LoField<P>::ld(rlo, jj[k] * R + r);
+              const Sp32 bk = LoField<P>::ld(rh, jj[k] * R + r);
               o.s0 = cfmaf(make_float2(m[k].r0.x, m[k].r0.y), bk.s0, o.s0);
               o.s0 = cfmaf(make_float2(m[k].r0.z, m[k].r0.w), bk.s1, o.s0);
               o.s1 = cfmaf(make_float2(m[k].r1.x, m[k].r1.y), bk.s0, o.s1);
               o.s1 = cfmaf(make_float2(m[k].r1.z, m[k].r1.w), bk.s1, o.s1);
             }
-            const Sp32 ti = LoField<P>::ld(tlo, e), pi = ld32(p32, e);
+            const Sp32 ti = ld32(t32, e), pi = ld32(p32, e);
             const float2 ar = make_float2(float(sc.a_r[r].x), float(sc.a_r[r].y));
             const float bt = float(sc.beta[r]);
             Sp32 tn, pn;
@@ -226,7 +234,8 @@ __global__ void __launch_bounds__(256) k_batched_cg(BatchArgs a) {
             tn.s1 = cfmaf(ar, o.s1, make_float2(bt * ti.s1.x, bt * ti.s1.y));
             pn.s0 = cfmaf(ar, self.s0, make_float2(bt * pi.s0.x, bt * pi.s0.y));
             pn.s1 = cfmaf(ar, self.s1, make_float2(bt * pi.s1.x, bt * pi.s1.y));
-            LoField<P>::st(tlo, e, tn);
+            st32(t32, e, tn);
+            if constexpr (P == PBF16) stbf(reinterpret_cast<uint2*>(th), e, tn);
             st32(p32, e, pn);
             const float tt = tn.s0.x * tn.s0.x + tn.s0.y * tn.s0.y + tn.s1.x * tn.s1.x + tn.s1.y * tn.s1.y;
             const float pp = pn.s0.x * pn.s0.x + pn.s0.y * pn.s0.y + pn.s1.x * pn.s1.x + pn.s1.y * pn.s1.y;
@@ -275,27 +284,27 @@ __global__ void __launch_bounds__(256) k_batched_cg(BatchArgs a) {
           for (int r = 0; r < R; r++) {
             if (r >= nr || !sc.active[r]) continue;
             const int e = i * R + r;
-            const Sp32 self = LoField<P>::ld(tlo, e);
+            const Sp32 self = ld32(t32, e);
             Sp32 q{make_float2(dg * self.s0.x, dg * self.s0.y), make_float2(dg * self.s1.x, dg * self.s1.y)};
 #pragma unroll
             for (int k = 0; k < 3; k++) {
-              const Sp32 bk = LoField<P>::ld(tlo, jj[k] * R + r);
+              const Sp32 bk = LoField<P>::ld(th, jj[k] * R + r);
               q.s0 = cfmaf(make_float2(m[k].r0.x, m[k].r0.y), bk.s0, q.s0);
               q.s0 = cfmaf(make_float2(m[k].r0.z, m[k].r0.w), bk.s1, q.s0);
               q.s1 = cfmaf(make_float2(m[k].r1.x, m[k].r1.y), bk.s0, q.s1);
               q.s1 = cfmaf(make_float2(m[k].r1.z, m[k].r1.w), bk.s1, q.s1);
             }
-            const Sp32 pi = ld32(p32, e), ri = LoField<P>::ld(rlo, e), xi = ld32(xlo, e);
+            const Sp32 pi = ld32(p32, e), ri = ld32(r32, e), xi = ld32(xlo, e);
             const float al = float(sc.alpha[r]), sf = float(S.shift[r]);
             Sp32 rn, xn;
             rn.s0 = make_float2(ri.s0.x - al * (q.s0.x + sf * pi.s0.x), ri.s0.y - al * (q.s0.y + sf * pi.s0.y));
             rn.s1 = make_float2(ri.s1.x - al * (q.s1.x + sf * pi.s1.x), ri.s1.y - al * (q.s1.y + sf * pi.s1.y));
             xn.s0 = make_float2(xi.s0.x + al * pi.s0.x, xi.s0.y + al * pi.s0.y);
             xn.s1 = make_float2(xi.s1.x + al * pi.s1.x, xi.s1.y + al * pi.s1.y);
-            LoField<P>::st(rlo, e, rn);
+            st32(r32, e, rn);
+            if constexpr (P == PBF16) stbf(reinterpret_cast<uint2*>(rh), e, rn);
             st32(xlo, e, xn);
-            const Sp32 rs = LoField<P>::ld(rlo, e);
-            v[3 * r] += double(rs.s0.x * rs.s0.x + rs.s0.y * rs.s0.y + rs.s1.x * rs.s1.x + rs.s1.y * rs.s1.y);
+            v[3 * r] += double(rn.s0.x * rn.s0.x + rn.s0.y * rn.s0.y + rn.s1.x * rn.s1.x + rn.s1.y * rn.s1.y);
           }
         }
       }
@@ -307,7 +316,13 @@ __global__ void __launch_bounds__(256) k_batched_cg(BatchArgs a) {
         const double dg = __ldg(S.diag + i);
 #pragma unroll
         for (int r = 0; r < R; r++) {
-          if (r >= nr || !sc.active[r]) continue;
+          if (r >= nr) continue;
+          if (!sc.active[r]) {
+            // a finished right-hand side keeps its solution across the
+            // buffer swap that follows this phase
+            if constexpr (mixed) st64(xb, i * R + r, ld64(xa, i * R + r));
+            continue;
+          }
           auto xs = [&](int site) {
             const int e = site * R + r;
             const Sp64 h = ld64(xa, e);
@@ -368,7 +383,8 @@ __global__ void __launch_bounds__(256) k_batched_cg(BatchArgs a) {
             pv0 = make_double2(pi.s0.x, pi.s0.y);
             pv1 = make_double2(pi.s1.x, pi.s1.y);
             const Sp32 rl{make_float2(float(rt.s0.x), float(rt.s0.y)), make_float2(float(rt.s1.x), float(rt.s1.y))};
-            LoField<P>::st(rlo, e, rl);
+            st32(r32, e, rl);
+            if constexpr (P == PBF16) stbf(reinterpret_cast<uint2*>(rh), e, rl);
             st32(xlo, e, Sp32{make_float2(0.f, 0.f), make_float2(0.f, 0.f)});
           }
           v[3 * r + 1] += rt.s0.x * pv0.x + rt.s0.y * pv0.y + rt.s1.x * pv1.x + rt.s1.y * pv1.y;
@@ -661,8 +677,8 @@ static int batch_build(qed3_batch_s* bt) {
   // workspaces
   for (auto& s : bt->sys) {
     const size_t bytes = size_t(s.Ns) * R * sizeof(S64);
-    void* p[8];
-    for (int k = 0; k < 8; k++) {
+    void* p[10];
+    for (int k = 0; k < 10; k++) {
       QED3_CUDA_TRY(cudaMalloc(&p[k], bytes));
       bt->buffers.push_back(p[k]);
     }
@@ -674,6 +690,8 @@ static int batch_build(qed3_batch_s* bt) {
     s.p = p[5];
     s.t = p[6];
     s.xlo = p[7];
+    s.rh = p[8];
+    s.th = p[9];
   }
   QED3_CUDA_TRY(cudaMalloc(&bt->d_scal, sizeof(double) * 6 * R * nsys));
   for (int i = 0; i < nsys; i++) bt->sys[i].scal = bt->d_scal + size_t(6) * R * i;

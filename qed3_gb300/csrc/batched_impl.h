@@ -29,6 +29,8 @@ struct BatchSys {
   void* p;
   void* t;
   void* xlo;
+  void* rh;      // bf16 copies of r and t for the neighbour gathers (bf16 mode)
+  void* th;
   double* scal;  // [nrhs][6]: mu_true, bnorm2, iters, reliable updates, status, x buffer
 };
 

@@ -146,6 +146,27 @@ __device__ __forceinline__ Sp32 hop32(int i, int Ns, const int* __restrict__ nbr
   return o;
 }
 
+// diag * self + sum_k H[k][i] halo[nbr[k][i]]: the own value comes from the
+// fp32 state, the neighbours from the gathered copy (fp32 or bf16).
+template <int P>
+__device__ __forceinline__ Sp32 hop32_self(int i, int Ns, const int* __restrict__ nbr, const M32* __restrict__ H,
+                                           const float* __restrict__ diag, const Sp32& self,
+                                           const typename LoField<P>::T* halo) {
+  const int j0 = __ldg(nbr + i), j1 = __ldg(nbr + Ns + i), j2 = __ldg(nbr + 2 * Ns + i);
+  const Sp32 bs[3] = {LoField<P>::ld(halo, j0), LoField<P>::ld(halo, j1), LoField<P>::ld(halo, j2)};
+  const float d = __ldg(diag + i);
+  Sp32 o{make_float2(d * self.s0.x, d * self.s0.y), make_float2(d * self.s1.x, d * self.s1.y)};
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    const M32 m = H[k * Ns + i];
+    o.s0 = cfmaf(make_float2(m.r0.x, m.r0.y), bs[k].s0, o.s0);
+    o.s0 = cfmaf(make_float2(m.r0.z, m.r0.w), bs[k].s1, o.s0);
+    o.s1 = cfmaf(make_float2(m.r1.x, m.r1.y), bs[k].s0, o.s1);
+    o.s1 = cfmaf(make_float2(m.r1.z, m.r1.w), bs[k].s1, o.s1);
+  }
+  return o;
+}
+
 // ---- reductions ----------------------------------------------------------------
 __device__ __forceinline__ double warp_sum(double v) {
 #pragma unroll
@@ -229,6 +250,57 @@ __device__ __forceinline__ bool grid_sync(GridBar* bar, unsigned int& gen, long 
   }
   __syncthreads();
   return s_ok != 0;
+}
+
+// ---- grid barrier, monotonic form -------------------------------------------
+// The arrival counter and the generation only grow within a launch (both are
+// zeroed before it), so no reset sits on the critical path: the block whose
+// acq_rel increment completes epoch * gridDim.x arrivals releases the new
+// generation; the others acquire-poll it.  Counter, generation and abort flag
+// sit on separate 128-byte lines.  Every wait is capped as in grid_sync.
+struct __align__(128) GridBar2 {
+  unsigned int count;
+  unsigned int pad0[31];
+  unsigned int gen;
+  unsigned int pad1[31];
+  int abort;
+  int pad2[31];
+};
+
+__device__ __forceinline__ unsigned int atom_add_acq_rel(unsigned int* p, unsigned int v) {
+  unsigned int old;
+  asm volatile("atom.acq_rel.gpu.global.add.u32 %0, [%1], %2;" : "=r"(old) : "l"(p), "r"(v) : "memory");
+  return old;
+}
+
+__device__ __forceinline__ bool grid_sync2(GridBar2* bar, unsigned int& epoch, long long spin_limit) {
+  __syncthreads();
+  __shared__ int s_ok2;
+  if (threadIdx.x == 0) {
+    int ok = 1;
+    epoch += 1u;
+    const unsigned int target = epoch * gridDim.x;
+    const unsigned int prev = atom_add_acq_rel(&bar->count, 1u);
+    if (prev == target - 1u) {
+      st_release(&bar->gen, epoch);
+    } else {
+      long long spins = 0;
+      while (int(ld_acquire(&bar->gen) - epoch) < 0) {
+        if ((spins & 63) == 63 && ld_volatile_int(&bar->abort)) {
+          ok = 0;
+          break;
+        }
+        if (++spins > spin_limit) {
+          atomicExch(&bar->abort, 1);
+          ok = 0;
+          break;
+        }
+      }
+    }
+    s_ok2 = ok;
+  }
+  __syncthreads();
+  return s_ok2 != 0;
 }
 
 }  // namespace qed3

@@ -13,6 +13,7 @@ struct S64;
 struct M64;
 struct M32;
 struct GridBar;
+struct GridBar2;
 
 #define QED3_CUDA_TRY(call)                                                                        \
   do {                                                                                             \
@@ -46,9 +47,10 @@ struct SolverWork {
   // FP64 internal fields
   S64 *b = nullptr, *xhi = nullptr, *xhi2 = nullptr, *rhi = nullptr, *t64 = nullptr;
   // FP32 fields (also used as FP64 scratch when the solve is plain FP64)
-  void *r = nullptr, *p = nullptr, *t = nullptr, *xlo = nullptr, *rg = nullptr;
+  void *r = nullptr, *p = nullptr, *t = nullptr, *xlo = nullptr, *rg = nullptr, *tg = nullptr;
   double* partials = nullptr;  // [2][maxblocks][4]
   GridBar* bar = nullptr;
+  GridBar2* bar2 = nullptr;
   double* scal = nullptr;      // device scalars for the report
   cudaEvent_t e0 = nullptr, e1 = nullptr;
 };

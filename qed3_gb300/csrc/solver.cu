@@ -27,6 +27,7 @@
 #include "device.cuh"
 #include "dirac_impl.h"
 #include "handles.h"
+#include "solver_v2.h"
 
 namespace qed3 {
 
@@ -47,6 +48,8 @@ struct CgArgs {
   void* p;
   void* t;
   void* xlo;
+  void* rh;          // gathered copy of r (== r for fp32; bf16 copy for bf16)
+  void* th;          // gathered copy of t
   double* partials;  // [2][gridDim][4]
   GridBar* bar;
   double* scal;      // [0] mu_true [1] bnorm2 [2] iters [3] reliable updates [4] status [5] x buffer (0/1)
@@ -108,8 +111,12 @@ __global__ void __launch_bounds__(256) k_cg_persistent(CgArgs a) {
   S64* r64 = reinterpret_cast<S64*>(a.r);
   S64* p64 = reinterpret_cast<S64*>(a.p);
   S64* t64w = reinterpret_cast<S64*>(a.t);
-  Lo* rlo = reinterpret_cast<Lo*>(a.r);
-  Lo* tlo = reinterpret_cast<Lo*>(a.t);
+  // mixed modes keep r and t in fp32; neighbours are read from rh / th,
+  // which alias r / t in fp32 mode and are bf16 copies in bf16 mode
+  float4* r32 = reinterpret_cast<float4*>(a.r);
+  float4* t32 = reinterpret_cast<float4*>(a.t);
+  Lo* rh = reinterpret_cast<Lo*>(a.rh);
+  Lo* th = reinterpret_cast<Lo*>(a.th);
   float4* p32 = reinterpret_cast<float4*>(a.p);
   float4* xlo = reinterpret_cast<float4*>(a.xlo);
   S64* xa = a.xhi;
@@ -130,8 +137,12 @@ __global__ void __launch_bounds__(256) k_cg_persistent(CgArgs a) {
       } else {
         const Sp32 bl{make_float2(float(bi.s0.x), float(bi.s0.y)), make_float2(float(bi.s1.x), float(bi.s1.y))};
         const Sp32 zl{make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
-        LoField<P>::st(rlo, i, bl);
-        LoField<P>::st(tlo, i, zl);
+        st32(r32, i, bl);
+        st32(t32, i, zl);
+        if constexpr (P == PBF16) {
+          stbf(reinterpret_cast<uint2*>(rh), i, bl);
+          stbf(reinterpret_cast<uint2*>(th), i, zl);
+        }
         st32(p32, i, zl);
         st32(xlo, i, zl);
       }
@@ -173,8 +184,9 @@ __global__ void __launch_bounds__(256) k_cg_persistent(CgArgs a) {
             v[0] += tn.s0.x * tn.s0.x + tn.s0.y * tn.s0.y + tn.s1.x * tn.s1.x + tn.s1.y * tn.s1.y +
                     s * (pn.s0.x * pn.s0.x + pn.s0.y * pn.s0.y + pn.s1.x * pn.s1.x + pn.s1.y * pn.s1.y);
           } else {
-            const Sp32 dr = hop32<P>(i, Ns, a.nbr, a.H32, a.diag32, rlo);
-            const Sp32 ti = LoField<P>::ld(tlo, i), pi = ld32(p32, i), ri = LoField<P>::ld(rlo, i);
+            const Sp32 ri = ld32(r32, i);
+            const Sp32 dr = hop32_self<P>(i, Ns, a.nbr, a.H32, a.diag32, ri, rh);
+            const Sp32 ti = ld32(t32, i), pi = ld32(p32, i);
             const float2 ar = make_float2(float(a_r.x), float(a_r.y));
             const float bt = float(beta);
             Sp32 tn, pn;
@@ -182,7 +194,8 @@ __global__ void __launch_bounds__(256) k_cg_persistent(CgArgs a) {
             tn.s1 = cfmaf(ar, dr.s1, make_float2(bt * ti.s1.x, bt * ti.s1.y));
             pn.s0 = cfmaf(ar, ri.s0, make_float2(bt * pi.s0.x, bt * pi.s0.y));
             pn.s1 = cfmaf(ar, ri.s1, make_float2(bt * pi.s1.x, bt * pi.s1.y));
-            LoField<P>::st(tlo, i, tn);
+            st32(t32, i, tn);
+            if constexpr (P == PBF16) stbf(reinterpret_cast<uint2*>(th), i, tn);
             st32(p32, i, pn);
             const float tt = tn.s0.x * tn.s0.x + tn.s0.y * tn.s0.y + tn.s1.x * tn.s1.x + tn.s1.y * tn.s1.y;
             const float pp = pn.s0.x * pn.s0.x + pn.s0.y * pn.s0.y + pn.s1.x * pn.s1.x + pn.s1.y * pn.s1.y;
@@ -213,19 +226,19 @@ __global__ void __launch_bounds__(256) k_cg_persistent(CgArgs a) {
             st64(xa, i, xn);
             v[0] += rn.s0.x * rn.s0.x + rn.s0.y * rn.s0.y + rn.s1.x * rn.s1.x + rn.s1.y * rn.s1.y;
           } else {
-            const Sp32 q = hop32<P>(i, Ns, a.nbr, a.Hd32, a.diag32, tlo);
-            const Sp32 pi = ld32(p32, i), ri = LoField<P>::ld(rlo, i), xi = ld32(xlo, i);
+            const Sp32 ti = ld32(t32, i);
+            const Sp32 q = hop32_self<P>(i, Ns, a.nbr, a.Hd32, a.diag32, ti, th);
+            const Sp32 pi = ld32(p32, i), ri = ld32(r32, i), xi = ld32(xlo, i);
             const float al = float(alpha), sf = float(s);
             Sp32 rn, xn;
             rn.s0 = make_float2(ri.s0.x - al * (q.s0.x + sf * pi.s0.x), ri.s0.y - al * (q.s0.y + sf * pi.s0.y));
             rn.s1 = make_float2(ri.s1.x - al * (q.s1.x + sf * pi.s1.x), ri.s1.y - al * (q.s1.y + sf * pi.s1.y));
             xn.s0 = make_float2(xi.s0.x + al * pi.s0.x, xi.s0.y + al * pi.s0.y);
             xn.s1 = make_float2(xi.s1.x + al * pi.s1.x, xi.s1.y + al * pi.s1.y);
-            LoField<P>::st(rlo, i, rn);
+            st32(r32, i, rn);
+            if constexpr (P == PBF16) stbf(reinterpret_cast<uint2*>(rh), i, rn);
             st32(xlo, i, xn);
-            // accumulate the norm of the STORED residual
-            const Sp32 rs = LoField<P>::ld(rlo, i);
-            v[0] += double(rs.s0.x * rs.s0.x + rs.s0.y * rs.s0.y + rs.s1.x * rs.s1.x + rs.s1.y * rs.s1.y);
+            v[0] += double(rn.s0.x * rn.s0.x + rn.s0.y * rn.s0.y + rn.s1.x * rn.s1.x + rn.s1.y * rn.s1.y);
           }
         }
         publish<1>(v, part(), sh);
@@ -302,7 +315,8 @@ __global__ void __launch_bounds__(256) k_cg_persistent(CgArgs a) {
             pv0 = make_double2(pi.s0.x, pi.s0.y);
             pv1 = make_double2(pi.s1.x, pi.s1.y);
             const Sp32 rl{make_float2(float(rt.s0.x), float(rt.s0.y)), make_float2(float(rt.s1.x), float(rt.s1.y))};
-            LoField<P>::st(rlo, i, rl);
+            st32(r32, i, rl);
+            if constexpr (P == PBF16) stbf(reinterpret_cast<uint2*>(rh), i, rl);
             st32(xlo, i, Sp32{make_float2(0.f, 0.f), make_float2(0.f, 0.f)});
           }
           // <r, p> = sum conj(r) p
@@ -352,6 +366,8 @@ timeout:
 // ---------------------------------------------------------------------------
 // Host driver
 // ---------------------------------------------------------------------------
+int cg_finish(qed3_dirac_s* d, double* x, qed3_solve_report* rep, cudaStream_t st);
+
 static int ensure_work(qed3_dirac_s* d) {
   SolverWork& w = d->work;
   const size_t Ns = size_t(d->Ns);
@@ -367,12 +383,15 @@ static int ensure_work(qed3_dirac_s* d) {
   QED3_CUDA_TRY(cudaMalloc(&w.p, b64));
   QED3_CUDA_TRY(cudaMalloc(&w.t, b64));
   QED3_CUDA_TRY(cudaMalloc(&w.xlo, b64));
+  QED3_CUDA_TRY(cudaMalloc(&w.rg, b64));
+  QED3_CUDA_TRY(cudaMalloc(&w.tg, b64));
   int dev = 0;
   QED3_CUDA_TRY(cudaGetDevice(&dev));
   QED3_CUDA_TRY(cudaDeviceGetAttribute(&d->sm_count, cudaDevAttrMultiProcessorCount, dev));
   const size_t maxblocks = size_t(d->sm_count) * 32;
   QED3_CUDA_TRY(cudaMalloc(&w.partials, 2 * maxblocks * 4 * sizeof(double)));
   QED3_CUDA_TRY(cudaMalloc(&w.bar, sizeof(GridBar)));
+  QED3_CUDA_TRY(cudaMalloc(&w.bar2, sizeof(GridBar2)));
   QED3_CUDA_TRY(cudaMalloc(&w.scal, 8 * sizeof(double)));
   QED3_CUDA_TRY(cudaEventCreate(&w.e0));
   QED3_CUDA_TRY(cudaEventCreate(&w.e1));
@@ -382,7 +401,7 @@ static int ensure_work(qed3_dirac_s* d) {
 
 int solver_free(qed3_dirac_s* d) {
   SolverWork& w = d->work;
-  void* ptrs[] = {w.b, w.xhi, w.xhi2, w.rhi, w.t64, w.r, w.p, w.t, w.xlo, w.partials, w.bar, w.scal};
+  void* ptrs[] = {w.b, w.xhi, w.xhi2, w.rhi, w.t64, w.r, w.p, w.t, w.xlo, w.rg, w.tg, w.partials, w.bar, w.bar2, w.scal};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (w.e0) cudaEventDestroy(w.e0);
@@ -420,6 +439,38 @@ int cg_solve(qed3_dirac_s* d, double* x, const double* b, const qed3_solve_param
 
   rc = field_import(d, QED3_PREC_F64, w.b, b, 1, st);
   if (rc) return rc;
+  // register-resident kernel when every site can own a thread
+  int vgrid = 0, vthreads = 0, vspt = 0;
+  const bool streaming = prm && (prm->flags & QED3_SOLVE_STREAMING);
+  if (!streaming && cg_v2_plan(prec, d->Ns, d->sm_count, &vgrid, &vthreads, &vspt)) {
+    QED3_CUDA_TRY(cudaMemsetAsync(w.bar2, 0, sizeof(GridBar2), st));
+    CgV2Args v{};
+    v.Ns = d->Ns;
+    v.nbr = d->lat->dev.nbr;
+    v.H = d->H;
+    v.Hd = d->Hd;
+    v.diag = d->diag;
+    v.H32 = d->H32;
+    v.Hd32 = d->Hd32;
+    v.diag32 = d->diag32;
+    v.b = w.b;
+    v.x = w.xhi;
+    v.t64 = w.t64;
+    v.halo_r = w.r;
+    v.halo_t = w.t;
+    v.partials = w.partials;
+    v.bar = w.bar2;
+    v.scal = w.scal;
+    v.tol2 = tol * tol;
+    v.delta2 = delta * delta;
+    v.shift = shift;
+    v.maxiter = maxiter;
+    v.spin_limit = 4000000LL;  // ~2-4 s of acquire polling before a barrier gives up
+    QED3_CUDA_TRY(cudaEventRecord(w.e0, st));
+    if ((rc = cg_v2_launch(prec, vspt, vgrid, vthreads, v, st))) return rc;
+    QED3_CUDA_TRY(cudaEventRecord(w.e1, st));
+    return cg_finish(d, x, rep, st);
+  }
   QED3_CUDA_TRY(cudaMemsetAsync(w.bar, 0, sizeof(GridBar), st));
   CgArgs a{};
   a.Ns = d->Ns;
@@ -438,6 +489,8 @@ int cg_solve(qed3_dirac_s* d, double* x, const double* b, const qed3_solve_param
   a.p = w.p;
   a.t = w.t;
   a.xlo = w.xlo;
+  a.rh = prec == QED3_PREC_BF16 ? w.rg : w.r;
+  a.th = prec == QED3_PREC_BF16 ? w.tg : w.t;
   a.partials = w.partials;
   a.bar = w.bar;
   a.scal = w.scal;
@@ -452,6 +505,14 @@ int cg_solve(qed3_dirac_s* d, double* x, const double* b, const qed3_solve_param
   else rc = launch_cg<PBF16>(d, a, st);
   if (rc) return rc;
   QED3_CUDA_TRY(cudaEventRecord(w.e1, st));
+  return cg_finish(d, x, rep, st);
+}
+
+// Reads the device scalars, exports the solution buffer the kernel chose and
+// fills the report.
+int cg_finish(qed3_dirac_s* d, double* x, qed3_solve_report* rep, cudaStream_t st) {
+  SolverWork& w = d->work;
+  int rc;
   // export whichever x buffer holds the result (decided on the device)
   double sc[8];
   QED3_CUDA_TRY(cudaMemcpyAsync(sc, w.scal, 6 * sizeof(double), cudaMemcpyDeviceToHost, st));

@@ -34,13 +34,14 @@ def _true_res(Dq, x_t, b_t, shift=0.0):
     return float((b_t - q).norm() / b_t.norm())
 
 
+@pytest.mark.parametrize("flags", [0, Q.SOLVE_STREAMING])
 @pytest.mark.parametrize("prec", [Q.PREC_F64, Q.PREC_F32, Q.PREC_BF16])
-def test_cg_matches_oracle_n8(cuda, prec):
+def test_cg_matches_oracle_n8(cuda, prec, flags):
     g, lat, Do, Dq, b = _setup(8, 0.1, 21, cuda)
     x_ref, it_ref, _ = Do.cg(b, tol=1e-10)
     bt = to_dev(b, cuda)
     xt = bt.clone() * 0
-    rep = Dq.solve(xt, bt, tol=1e-10, precision=prec)
+    rep = Dq.solve(xt, bt, tol=1e-10, precision=prec, flags=flags)
     assert rep.status == Q.OK
     assert rep.true_rel_res <= 1e-10
     assert _true_res(Dq, xt, bt) <= 1.05e-10
@@ -52,12 +53,13 @@ def test_cg_matches_oracle_n8(cuda, prec):
         assert rep.reliable_updates >= 2
 
 
-@pytest.mark.parametrize("prec", [Q.PREC_F64, Q.PREC_F32])
-def test_cg_n64_certified(cuda, prec):
+@pytest.mark.parametrize("flags", [0, Q.SOLVE_STREAMING])
+@pytest.mark.parametrize("prec", [Q.PREC_F64, Q.PREC_F32, Q.PREC_BF16])
+def test_cg_n64_certified(cuda, prec, flags):
     g, lat, Do, Dq, b = _setup(64, 0.05, 22, cuda)
     bt = to_dev(b, cuda)
     xt = bt.clone() * 0
-    rep = Dq.solve(xt, bt, tol=1e-10, precision=prec)
+    rep = Dq.solve(xt, bt, tol=1e-10, precision=prec, flags=flags)
     assert rep.status == Q.OK and rep.true_rel_res <= 1e-10
     assert _true_res(Dq, xt, bt) <= 1.05e-10
     # the oracle's residual of the GPU solution (FP64 CSR operator)
@@ -66,24 +68,26 @@ def test_cg_n64_certified(cuda, prec):
     assert np.linalg.norm(r) / np.linalg.norm(b) <= 1.05e-10
 
 
-def test_cg_shifted(cuda):
+@pytest.mark.parametrize("flags", [0, Q.SOLVE_STREAMING])
+def test_cg_shifted(cuda, flags):
     g, lat, Do, Dq, b = _setup(8, 0.0, 23, cuda)
     bt = to_dev(b, cuda)
     xt = bt.clone() * 0
-    rep = Dq.solve(xt, bt, tol=1e-11, precision=Q.PREC_F32, shift=0.37)
+    rep = Dq.solve(xt, bt, tol=1e-11, precision=Q.PREC_F32, shift=0.37, flags=flags)
     assert rep.status == Q.OK
     x_ref, _, _ = Do.cg(b, tol=1e-12, shift=0.37)
     assert np.linalg.norm(from_dev(xt) - x_ref) / np.linalg.norm(x_ref) < 1e-9
     assert _true_res(Dq, xt, bt, 0.37) <= 1.1e-11
 
 
-def test_cg_zero_rhs_and_noconv(cuda):
+@pytest.mark.parametrize("flags", [0, Q.SOLVE_STREAMING])
+def test_cg_zero_rhs_and_noconv(cuda, flags):
     g, lat, Do, Dq, b = _setup(4, 0.1, 24, cuda)
     import torch
     z = torch.zeros(2 * g.n_sites, dtype=torch.complex128, device=cuda)
     x = torch.ones_like(z)
-    rep = Dq.solve(x, z)
+    rep = Dq.solve(x, z, flags=flags)
     assert rep.status == Q.OK and rep.iters == 0 and float(x.abs().max()) == 0.0
     bt = to_dev(b, cuda)
-    rep = Dq.solve(x, bt, tol=1e-14, maxiter=3)
+    rep = Dq.solve(x, bt, tol=1e-14, maxiter=3, flags=flags)
     assert rep.status == Q.ERR_NOCONV and rep.iters == 3
