@@ -133,6 +133,20 @@ int qed3_cg_solve(qed3_dirac* d, double* x, const double* b, const qed3_solve_pa
                   qed3_solve_report* report, void* stream);
 int qed3_solver_last_report(qed3_dirac* d, qed3_solve_report* report);
 
+/* Allocation-free CG solve.  No counterpart in the reference: it exists for
+ * callers that cannot allocate device memory at solve time -- code inside
+ * CUDA stream capture, hosts whose device memory is owned by another
+ * allocator or pool, multi-stream drivers that must avoid cudaFree's
+ * device-wide synchronisation.  Same algorithm, arguments and report as
+ * qed3_cg_solve, but its scratch is a static device array of the library
+ * (about 6.6 MB, held by every GPU that loads the library until exit), so
+ * lattices are limited to QED3_NOALLOC_MAX_SITES sites (n_refine <= 32);
+ * larger ones return QED3_ERR_ARG.  The first call on a device looks up the
+ * array's address and should precede any stream capture.  All calls share
+ * the array: calls that overlap on the GPU race and must be serialised. */
+#define QED3_NOALLOC_MAX_SITES 20480
+int qed3_cg_solve_noalloc(qed3_dirac* d, double* x, const double* b, const qed3_solve_params* params,
+                          qed3_solve_report* report, void* stream);
 
 /* ======================================================================
  * Batched solves in ONE persistent launch  --  replaces the reference's

@@ -77,6 +77,8 @@ SIGNATURES = [
     ("qed3_dirac_apply_field", ctypes.c_int, [vp, ctypes.c_int, ctypes.c_int, vp, vp, ctypes.c_int, vp]),
     ("qed3_cg_solve", ctypes.c_int, [vp, vp, vp, ctypes.POINTER(SolveParams), ctypes.POINTER(SolveReport), vp]),
     ("qed3_solver_last_report", ctypes.c_int, [vp, ctypes.POINTER(SolveReport)]),
+    ("qed3_cg_solve_noalloc", ctypes.c_int, [vp, vp, vp, ctypes.POINTER(SolveParams), ctypes.POINTER(SolveReport),
+                                             vp]),
     ("qed3_plaquette", ctypes.c_int, [vp, vp, vp, c_double_p, vp]),
     ("qed3_gauge_action", ctypes.c_int, [vp, vp, ctypes.c_double, ctypes.c_int, c_double_p, vp]),
     ("qed3_gauge_force", ctypes.c_int, [vp, vp, ctypes.c_double, ctypes.c_int, ctypes.c_int, vp, vp]),

@@ -22,5 +22,7 @@ int field_export(qed3_dirac_s* d, int prec, double* out_ref, const void* field, 
 int cg_solve(qed3_dirac_s* d, double* x, const double* b, const qed3_solve_params* prm, qed3_solve_report* rep,
              cudaStream_t st);
 int solver_free(qed3_dirac_s* d);
+int cg_solve_noalloc(qed3_dirac_s* d, double* x, const double* b, const qed3_solve_params* prm,
+                     qed3_solve_report* rep, cudaStream_t st);
 
 }  // namespace qed3

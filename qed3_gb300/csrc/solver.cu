@@ -424,6 +424,57 @@ static int launch_cg(qed3_dirac_s* d, CgArgs& args, cudaStream_t st) {
   return QED3_OK;
 }
 
+// Launches the persistent CG kernel on caller-provided scratch (used by the
+// allocation-free entry point); returns the grid size through *grid_out.
+int cg_launch_on_scratch(int prec, qed3_dirac_s* d, S64* b, S64* xhi, S64* xhi2, S64* t64, void* r, void* p, void* t,
+                         void* xlo, void* rh, void* th, double* partials, int max_blocks, GridBar* bar, double* scal,
+                         double tol, double delta, int maxiter, double shift, cudaStream_t st) {
+  int per_sm = 0, smc = 0, dev = 0;
+  QED3_CUDA_TRY(cudaGetDevice(&dev));
+  QED3_CUDA_TRY(cudaDeviceGetAttribute(&smc, cudaDevAttrMultiProcessorCount, dev));
+  if (prec == QED3_PREC_F64)
+    QED3_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cg_persistent<P64>, 256, 0));
+  else if (prec == QED3_PREC_F32)
+    QED3_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cg_persistent<P32>, 256, 0));
+  else
+    QED3_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cg_persistent<PBF16>, 256, 0));
+  long long grid = std::min<long long>((d->Ns + 255) / 256, (long long)per_sm * smc);
+  grid = std::max<long long>(1, std::min<long long>(grid, max_blocks));
+  CgArgs a{};
+  a.Ns = d->Ns;
+  a.nbr = d->lat->dev.nbr;
+  a.H = d->H;
+  a.Hd = d->Hd;
+  a.diag = d->diag;
+  a.H32 = d->H32;
+  a.Hd32 = d->Hd32;
+  a.diag32 = d->diag32;
+  a.b = b;
+  a.xhi = xhi;
+  a.xhi2 = xhi2;
+  a.t64 = t64;
+  a.r = r;
+  a.p = p;
+  a.t = t;
+  a.xlo = xlo;
+  a.rh = prec == QED3_PREC_BF16 ? rh : r;
+  a.th = prec == QED3_PREC_BF16 ? th : t;
+  a.partials = partials;
+  a.bar = bar;
+  a.scal = scal;
+  a.tol2 = tol * tol;
+  a.delta2 = delta * delta;
+  a.shift = shift;
+  a.maxiter = maxiter;
+  a.spin_limit = 20000000LL;
+  void* kargs[] = {&a};
+  const void* fn = prec == QED3_PREC_F64   ? (const void*)k_cg_persistent<P64>
+                   : prec == QED3_PREC_F32 ? (const void*)k_cg_persistent<P32>
+                                           : (const void*)k_cg_persistent<PBF16>;
+  QED3_CUDA_TRY(cudaLaunchCooperativeKernel(fn, dim3(unsigned(grid)), dim3(256), kargs, 0, st));
+  return QED3_OK;
+}
+
 int cg_solve(qed3_dirac_s* d, double* x, const double* b, const qed3_solve_params* prm, qed3_solve_report* rep,
              cudaStream_t st) {
   if (!d->coeffs_set) return fail(QED3_ERR_STATE, "operator coefficients not set (call qed3_dirac_set_links)");
