@@ -109,6 +109,7 @@ int qed3_dirac_apply_field(qed3_dirac* d, int op, int prec, void* out, const voi
  * CG on (D^dagger D + shift) x = b from x0 = 0.
  * ====================================================================== */
 #define QED3_SOLVE_STREAMING 2 /* force the memory-streaming persistent kernel (default: register-resident when it fits) */
+#define QED3_SOLVE_BCAST_B 4   /* batched: every right-hand side of system u is b[u]'s first vector */
 
 typedef struct {
   double tol;     /* target ||b - A x|| / ||b|| of the FP64 true residual */
@@ -201,6 +202,28 @@ int qed3_rng_gaussian_links(qed3_rng* r, double width, double* links);
 int qed3_rng_gaussian_spinor(qed3_rng* r, double* spinor);
 int qed3_hmc_pure_gauge(qed3_lattice* lat, qed3_rng* rng, double* A, double beta, int compact, int exact,
                         double tmax, int nsteps, int no_reject, int* accepted, double* dH, void* stream);
+
+/* ======================================================================
+ * Overlap operator  --  replaces Overlap<WilsonDirac> (src/both_3d/overlap.h:137-390):
+ * D_ov = 1 + X r(X^dag X), X = D_W / lambda_max, r = Zolotarev approximation of
+ * (.)^{-1/2} of order zolo_order (n/2 poles).  All poles are solved in ONE
+ * batched persistent launch (mixed precision, FP64 true residuals).
+ * ====================================================================== */
+int qed3_overlap_create(qed3_dirac* dw, int zolo_order, int precision, qed3_overlap** out);
+int qed3_overlap_destroy(qed3_overlap* ov);
+/* Overlap::update -> compute_lambda_max + Zolotarev::update (:207-306).  Pass
+ * lambda_min, lambda_max > 0 to set the spectral bounds of D_W directly, or
+ * <= 0 to estimate them with the reference's power / inverse power iterations
+ * (inner CG tolerance tol_outer). */
+int qed3_overlap_update(qed3_overlap* ov, double lambda_min, double lambda_max, double tol_outer, void* stream);
+int qed3_overlap_info(const qed3_overlap* ov, double* lambda_min, double* lambda_max, double* k, double* delta,
+                      int* npoles);
+/* mult / adj / DHD / DDH_deviceAsyncLaunch (:309-390): op = QED3_OP_D (D_ov),
+ * QED3_OP_DDAG (D_ov^dag), QED3_OP_DDAGD or QED3_OP_DDDAG (D_ov + D_ov^dag,
+ * which equals D_ov^dag D_ov for the exact overlap).  tol_inner: pole solves'
+ * relative residual.  report: the worst pole (iterations, true residual). */
+int qed3_overlap_apply(qed3_overlap* ov, int op, double* out, const double* in, double tol_inner,
+                       qed3_solve_report* report, void* stream);
 
 /* ======================================================================
  * Zolotarev coefficients  --  replaces Zolotarev(k, n) / Zolotarev::update

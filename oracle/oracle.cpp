@@ -1049,3 +1049,91 @@ int orc_num_threads() {
 }
 
 }  // extern "C"
+
+// ===========================================================================
+// Overlap operator, restating Overlap (src/both_3d/overlap.h:137-390):
+//   X = D/lambda_max, Z_m = (X^dag X - k^2/cp_m)^{-1} xi by CG per pole,
+//   D_ov xi = xi + C X (xi + sum_m A_m Z_m)                  (mult, :309-332)
+//   D_ov^dag xi = xi + C (Y0 + sum_m A_m Y_m), Y0 = X^dag xi,
+//   Y_m = (X^dag X - k^2/cp_m)^{-1} Y0                      (adj, :334-361)
+// The pole solves use CG on (D^dag D + lambda_max^2 sigma_m) with the
+// solution scaled by lambda_max^2 (the same linear system).
+// ===========================================================================
+extern "C" {
+
+// op: 0 = D_ov, 1 = D_ov^dag, 2 = D_ov + D_ov^dag (Overlap::DHD, :363-375)
+int orc_overlap_apply(const OracleDirac* d, double lmin, double lmax, int order, int op, double* out_d,
+                      const double* in_d, double tol_inner) {
+  const Idx N = d->N;
+  const cplx* xi = reinterpret_cast<const cplx*>(in_d);
+  cplx* out = reinterpret_cast<cplx*>(out_d);
+  const double k = lmin / lmax;
+  const int size = order / 2 + 1;
+  std::vector<double> c(size), cp(size), A(size), sc(4);
+  orc_zolotarev(k, order, c.data(), cp.data(), A.data(), sc.data());
+  const double C = sc[3];
+  int total_it = 0;
+  auto pole_sum = [&](const std::vector<cplx>& rhs, std::vector<cplx>& acc) {
+    acc = rhs;
+    std::vector<cplx> z(N);
+    for (int m = 1; m < size; m++) {
+      const double sigma = -k * k / cp[m];
+      total_it += orc_cg(d, lmax * lmax * sigma, reinterpret_cast<double*>(z.data()),
+                         reinterpret_cast<const double*>(rhs.data()), tol_inner, 1000000, nullptr);
+      for (Idx i = 0; i < N; i++) acc[i] += A[m] * (lmax * lmax) * z[i];
+    }
+  };
+  std::vector<cplx> res_mult(N, 0.0), res_adj(N, 0.0);
+  if (op == 0 || op == 2) {
+    std::vector<cplx> acc, w(N);
+    pole_sum(std::vector<cplx>(xi, xi + N), acc);
+    csr_mult(d, false, w.data(), acc.data());
+    for (Idx i = 0; i < N; i++) res_mult[i] = xi[i] + (C / lmax) * w[i];
+  }
+  if (op == 1 || op == 2) {
+    std::vector<cplx> y0(N), acc;
+    csr_mult(d, true, y0.data(), xi);
+    for (Idx i = 0; i < N; i++) y0[i] /= lmax;
+    pole_sum(y0, acc);
+    for (Idx i = 0; i < N; i++) res_adj[i] = xi[i] + C * acc[i];
+  }
+  for (Idx i = 0; i < N; i++)
+    out[i] = (op == 0) ? res_mult[i] : (op == 1) ? res_adj[i] : res_mult[i] + res_adj[i];
+  return total_it;
+}
+
+// Overlap::compute_lambda_max (src/both_3d/overlap.h:217-306): power iteration
+// on D^dag D from q = (1/sqrt2, 1/sqrt2, 0, ...) with the reference's
+// geometric extrapolation, then inverse power iteration with CG at tol_outer.
+void orc_lambda_bounds(const OracleDirac* d, double TOL, int MAXITER, double tol_outer, double* lmin, double* lmax) {
+  const Idx N = d->N;
+  auto run = [&](bool inverse) {
+    std::vector<cplx> q(N, 0.0), x(N);
+    q[0] = std::sqrt(0.5);
+    q[1] = std::sqrt(0.5);
+    double mu_0 = 1.0, mu_m1 = 1.0, mu_m2 = 1.0, lambda = 100.0, lambda_old = 1000.0;
+    for (int i = 0; i < MAXITER; i++) {
+      if (!inverse) orc_dirac_apply(d, 2, reinterpret_cast<double*>(x.data()), reinterpret_cast<const double*>(q.data()));
+      else orc_cg(d, 0.0, reinterpret_cast<double*>(x.data()), reinterpret_cast<const double*>(q.data()), tol_outer,
+                  1000000, nullptr);
+      const double norm = zdotc(x.data(), x.data(), N).real();
+      for (Idx j = 0; j < N; j++) q[j] = x[j] / std::sqrt(norm);
+      const cplx dot = zdotc(x.data(), q.data(), N);
+      mu_m2 = mu_m1;
+      mu_m1 = mu_0;
+      mu_0 = dot.real();
+      const double r = (mu_0 - mu_m1) / (mu_m1 - mu_m2);
+      const double a = (mu_0 - mu_m1) / std::pow(r, i - 1) / (r - 1);
+      lambda_old = lambda;
+      lambda = mu_0 - a * std::pow(r, i);
+      if (std::abs(lambda_old - lambda) / std::abs(lambda) < TOL) break;
+    }
+    return lambda;
+  };
+  const double lam = run(false);
+  const double lam2 = run(true);
+  *lmin = std::sqrt((1.0 - 100 * TOL) / lam2);
+  *lmax = std::sqrt((1.0 + 100 * TOL) * lam);
+}
+
+}  // extern "C"

@@ -76,6 +76,10 @@ def lib():
                                          ctypes.c_double, ctypes.c_int, ctypes.c_int, c_double_p]
         L.orc_fermion_force.argtypes = [vp, vp, c_double_p, ctypes.c_void_p, c_double_p]
         L.orc_num_threads.restype = ctypes.c_int
+        L.orc_overlap_apply.restype = ctypes.c_int
+        L.orc_overlap_apply.argtypes = [vp, ctypes.c_double, ctypes.c_double, ctypes.c_int, ctypes.c_int,
+                                        ctypes.c_void_p, ctypes.c_void_p, ctypes.c_double]
+        L.orc_lambda_bounds.argtypes = [vp, ctypes.c_double, ctypes.c_int, ctypes.c_double, c_double_p, c_double_p]
         _lib = L
     return _lib
 
@@ -212,6 +216,20 @@ class Dirac:
         F = np.zeros(self.geom.n_links)
         lib().orc_fermion_force(self.h, self.geom.handle, _dp(A), _p(eta), _dp(F))
         return F
+
+    def overlap(self, v: np.ndarray, lmin: float, lmax: float, order: int = 21, op: int = 0,
+                tol_inner: float = 1e-12) -> np.ndarray:
+        """Overlap::mult (op 0) / adj (1) / DHD (2) restated, CG per pole."""
+        v = np.ascontiguousarray(v, dtype=np.complex128)
+        out = np.zeros_like(v)
+        lib().orc_overlap_apply(self.h, lmin, lmax, order, op, _p(out), _p(v), tol_inner)
+        return out
+
+    def lambda_bounds(self, TOL: float = 1e-8, maxiter: int = 500, tol_outer: float = 1e-10):
+        """Overlap::compute_lambda_max restated: (lambda_min, lambda_max) of D."""
+        a, b = ctypes.c_double(), ctypes.c_double()
+        lib().orc_lambda_bounds(self.h, TOL, maxiter, tol_outer, ctypes.byref(a), ctypes.byref(b))
+        return a.value, b.value
 
     def __del__(self):
         if getattr(self, "h", 0) and _lib is not None:

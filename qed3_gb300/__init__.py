@@ -32,6 +32,7 @@ OK, ERR_ARG, ERR_CUDA, ERR_NOCONV, ERR_TIMEOUT, ERR_STATE, ERR_NOMEM = range(7)
 OP_D, OP_DDAG, OP_DDAGD, OP_DDDAG = range(4)
 PREC_F64, PREC_F32, PREC_BF16 = range(3)
 SOLVE_STREAMING = 2
+SOLVE_BCAST_B = 4
 PREC_NAMES = {"f64": PREC_F64, "f32": PREC_F32, "bf16": PREC_BF16}
 BYTES_PER_SITE = {PREC_F64: 32, PREC_F32: 16, PREC_BF16: 8}
 
@@ -90,6 +91,12 @@ SIGNATURES = [
     ("qed3_hmc_pure_gauge", ctypes.c_int, [vp, vp, vp, ctypes.c_double, ctypes.c_int, ctypes.c_int, ctypes.c_double,
                                            ctypes.c_int, ctypes.c_int, c_int_p, c_double_p, vp]),
     ("qed3_zolotarev", ctypes.c_int, [ctypes.c_double, ctypes.c_int, vp, vp, vp, vp, c_int_p]),
+    ("qed3_overlap_create", ctypes.c_int, [vp, ctypes.c_int, ctypes.c_int, ctypes.POINTER(vp)]),
+    ("qed3_overlap_destroy", ctypes.c_int, [vp]),
+    ("qed3_overlap_update", ctypes.c_int, [vp, ctypes.c_double, ctypes.c_double, ctypes.c_double, vp]),
+    ("qed3_overlap_info", ctypes.c_int, [vp, c_double_p, c_double_p, c_double_p, c_double_p, c_int_p]),
+    ("qed3_overlap_apply", ctypes.c_int, [vp, ctypes.c_int, vp, vp, ctypes.c_double, ctypes.POINTER(SolveReport),
+                                          vp]),
     ("qed3_batch_create", ctypes.c_int, [ctypes.c_int, vp, vp, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                          ctypes.POINTER(vp)]),
     ("qed3_batch_destroy", ctypes.c_int, [vp]),
@@ -403,4 +410,39 @@ class Batch:
     def __del__(self):
         if getattr(self, "_h", None) and _lib is not None:
             _lib.qed3_batch_destroy(self._h)
+            self._h = None
+
+
+class Overlap:
+    """Overlap operator on top of a DiracS2Dual (Overlap<WilsonDirac>, src/both_3d/overlap.h:137).
+
+    update(lmin, lmax): Zolotarev range [lmin/lmax, 1]; omit both to estimate
+    them on the device with the reference's power iterations."""
+
+    def __init__(self, dirac: DiracS2Dual, order: int = 21, precision: int = PREC_F32):
+        self.dirac = dirac
+        self.order = order
+        h = vp()
+        _check(lib().qed3_overlap_create(dirac.handle, order, precision, ctypes.byref(h)))
+        self._h = h
+
+    def update(self, lambda_min: float = 0.0, lambda_max: float = 0.0, tol_outer: float = 1e-8, stream=None):
+        _check(lib().qed3_overlap_update(self._h, lambda_min, lambda_max, tol_outer, _stream(stream)))
+        return self.info()
+
+    def info(self) -> dict:
+        a, b, k, dl = (ctypes.c_double() for _ in range(4))
+        np_ = ctypes.c_int()
+        _check(lib().qed3_overlap_info(self._h, *(ctypes.byref(v) for v in (a, b, k, dl, np_))))
+        return dict(lambda_min=a.value, lambda_max=b.value, k=k.value, delta=dl.value, npoles=np_.value)
+
+    def apply(self, out, inp, op: int = OP_D, tol_inner: float = 1e-10, stream=None) -> Report:
+        r = SolveReport()
+        _check(lib().qed3_overlap_apply(self._h, op, _ptr(out), _ptr(inp), tol_inner, ctypes.byref(r),
+                                        _stream(stream)))
+        return Report(r.status, r.iters, r.reliable_updates, r.true_rel_res, r.ms)
+
+    def __del__(self):
+        if getattr(self, "_h", None) and _lib is not None:
+            _lib.qed3_overlap_destroy(self._h)
             self._h = None

@@ -14,6 +14,7 @@
 #include "dirac_impl.h"
 #include "gauge_impl.h"
 #include "handles.h"
+#include "overlap_impl.h"
 #include "qed3_internal.h"
 
 namespace qed3 {
@@ -383,6 +384,43 @@ int qed3_batch_solve(qed3_batch* bt, double* const* x, const double* const* b, c
   for (size_t u = 0; u < bt->user_ops.size(); u++)
     if (!x[u] || !b[u]) return fail(QED3_ERR_ARG, "NULL vector");
   return batch_solve(bt, x, b, shifts, params, reports, ms, (cudaStream_t)stream);
+  QED3_GUARD_END
+}
+
+int qed3_overlap_create(qed3_dirac* dw, int zolo_order, int precision, qed3_overlap** out) {
+  QED3_GUARD_BEGIN
+  if (!dw || !out) return fail(QED3_ERR_ARG, "NULL argument");
+  if (precision < 0 || precision > 2) return fail(QED3_ERR_ARG, "unknown precision");
+  *out = nullptr;
+  return overlap_create(dw, zolo_order, precision, out);
+  QED3_GUARD_END
+}
+
+int qed3_overlap_destroy(qed3_overlap* ov) {
+  overlap_destroy(ov);
+  return QED3_OK;
+}
+
+int qed3_overlap_update(qed3_overlap* ov, double lambda_min, double lambda_max, double tol_outer, void* stream) {
+  QED3_GUARD_BEGIN
+  if (!ov) return fail(QED3_ERR_ARG, "NULL overlap");
+  return overlap_update(ov, lambda_min, lambda_max, tol_outer > 0 ? tol_outer : 1e-8, (cudaStream_t)stream);
+  QED3_GUARD_END
+}
+
+int qed3_overlap_info(const qed3_overlap* ov, double* lambda_min, double* lambda_max, double* k, double* delta,
+                      int* npoles) {
+  if (!ov) return fail(QED3_ERR_ARG, "NULL overlap");
+  return overlap_info(ov, lambda_min, lambda_max, k, delta, npoles);
+}
+
+int qed3_overlap_apply(qed3_overlap* ov, int op, double* out, const double* in, double tol_inner,
+                       qed3_solve_report* report, void* stream) {
+  QED3_GUARD_BEGIN
+  if (!ov || !out || !in) return fail(QED3_ERR_ARG, "NULL argument");
+  if (op < QED3_OP_D || op > QED3_OP_DDDAG) return fail(QED3_ERR_ARG, "unknown operator");
+  if (out == in) return fail(QED3_ERR_ARG, "out must not alias in");
+  return overlap_apply(ov, op, out, in, tol_inner > 0 ? tol_inner : 1e-10, report, (cudaStream_t)stream);
   QED3_GUARD_END
 }
 

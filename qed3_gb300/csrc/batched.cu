@@ -555,14 +555,14 @@ int batch_launch(int prec, int R, BatchArgs& args, int grid, int threads, cudaSt
 }
 
 // import nrhs reference-order vectors into a site-major interleaved field
-__global__ void k_import_interleaved(int Ns, int R, int nrhs, const int* __restrict__ perm, const S64* __restrict__ in,
-                                     S64* __restrict__ out) {
+__global__ void k_import_interleaved(int Ns, int R, int nrhs, long long stride, const int* __restrict__ perm,
+                                     const S64* __restrict__ in, S64* __restrict__ out) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= Ns) return;
   const int x = perm[i];
   for (int r = 0; r < R; r++) {
     Sp64 v{make_double2(0, 0), make_double2(0, 0)};
-    if (r < nrhs) v = ld64(in + size_t(r) * Ns, x);
+    if (r < nrhs) v = ld64(in + size_t(r) * stride, x);
     st64(out, i * R + r, v);
   }
 }
@@ -577,9 +577,10 @@ __global__ void k_export_interleaved(int Ns, int R, int nrhs, const int* __restr
   }
 }
 
-int batch_import(const BatchSys& s, const qed3_dirac_s* d, const double* b_ref, int R, cudaStream_t st) {
-  k_import_interleaved<<<(s.Ns + 255) / 256, 256, 0, st>>>(s.Ns, R, s.nrhs, d->lat->dev.perm,
-                                                         reinterpret_cast<const S64*>(b_ref), const_cast<S64*>(s.b));
+int batch_import(const BatchSys& s, const qed3_dirac_s* d, const double* b_ref, int R, bool bcast, cudaStream_t st) {
+  k_import_interleaved<<<(s.Ns + 255) / 256, 256, 0, st>>>(s.Ns, R, s.nrhs, bcast ? 0LL : (long long)s.Ns,
+                                                         d->lat->dev.perm, reinterpret_cast<const S64*>(b_ref),
+                                                         const_cast<S64*>(s.b));
   QED3_CUDA_TRY(cudaGetLastError());
   return QED3_OK;
 }
@@ -714,7 +715,8 @@ int batch_solve(qed3_batch_s* bt, double* const* x, const double* const* b, cons
     const int u = bt->owner[i], f = bt->first_rhs[i];
     for (int r = 0; r < kMaxTile; r++) s.shift[r] = 0.0;
     for (int r = 0; r < s.nrhs; r++) s.shift[r] = (shifts && shifts[u]) ? shifts[u][f + r] : (prm ? prm->shift : 0.0);
-    const int rc = batch_import(s, bt->user_ops[u], b[u] + size_t(f) * 4 * s.Ns, R, st);
+    const bool bcast = prm && (prm->flags & QED3_SOLVE_BCAST_B);
+    const int rc = batch_import(s, bt->user_ops[u], bcast ? b[u] : b[u] + size_t(f) * 4 * s.Ns, R, bcast, st);
     if (rc) return rc;
   }
   QED3_CUDA_TRY(cudaMemcpyAsync(bt->d_sys, bt->sys.data(), sizeof(BatchSys) * nsys, cudaMemcpyHostToDevice, st));

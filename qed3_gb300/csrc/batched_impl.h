@@ -48,7 +48,7 @@ struct BatchArgs {
 
 int batch_occupancy(int prec, int R, int threads, int* per_sm);
 int batch_launch(int prec, int R, BatchArgs& args, int grid, int threads, cudaStream_t st);
-int batch_import(const BatchSys& s, const qed3_dirac_s* d, const double* b_ref, int R, cudaStream_t st);
+int batch_import(const BatchSys& s, const qed3_dirac_s* d, const double* b_ref, int R, bool bcast, cudaStream_t st);
 int batch_export(const BatchSys& s, const qed3_dirac_s* d, double* x_ref, int R, cudaStream_t st);
 
 }  // namespace qed3

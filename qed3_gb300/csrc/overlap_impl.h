@@ -1,0 +1,15 @@
+// Overlap driver (overlap.cpp).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "handles.h"
+
+namespace qed3 {
+int overlap_create(qed3_dirac_s* d, int order, int prec, qed3_overlap_s** out);
+void overlap_destroy(qed3_overlap_s* ov);
+int overlap_update(qed3_overlap_s* ov, double lmin, double lmax, double tol_outer, cudaStream_t st);
+int overlap_apply(qed3_overlap_s* ov, int op, double* out, const double* in, double tol, qed3_solve_report* rep,
+                  cudaStream_t st);
+int overlap_info(const qed3_overlap_s* ov, double* lmin, double* lmax, double* k, double* delta, int* np);
+}  // namespace qed3

@@ -1,0 +1,102 @@
+"""Overlap operator (Overlap, src/both_3d/overlap.h:137-390) on the GPU.
+
+* against the oracle's restatement (CG per pole) with the same spectral bounds;
+* the device estimate of (lambda_min, lambda_max) against the oracle's
+  restatement of compute_lambda_max (same algorithm);
+* the sign function at n=8 against an FP64 dense eigendecomposition: D_ov - 1
+  = X (X^dag X)^{-1/2} up to the Zolotarev error Delta and the pole tolerance;
+* the Ginsparg-Wilson relation g5 D + D g5 = D g5 D to the same accuracy.
+"""
+import numpy as np
+import pytest
+
+import qed3_gb300 as Q
+from oracle import oracle as O
+from tests.gpu_util import from_dev, rand_spinor, rel, to_dev
+
+pytestmark = pytest.mark.gpu
+
+
+def _setup(n, M5, seed):
+    rng = np.random.default_rng(seed)
+    g = O.geometry(n)
+    lat = Q.S2Trivalent(n)
+    A = rng.normal(size=g.n_links) * 0.4
+    Do = O.Dirac(g, 1.0, M5)
+    Do.update(A)
+    Dq = Q.DiracS2Dual(lat, 1.0, M5)
+    Dq.update(A)
+    return rng, g, lat, Do, Dq
+
+
+@pytest.mark.parametrize("n,order", [(2, 21), (4, 31)])
+def test_overlap_matches_oracle(cuda, n, order):
+    rng, g, lat, Do, Dq = _setup(n, -1.0, 60 + n)
+    lmin, lmax = Do.lambda_bounds()
+    ov = Q.Overlap(Dq, order, Q.PREC_F32)
+    info = ov.update(lmin, lmax)
+    assert info["npoles"] == order // 2
+    v = rand_spinor(rng, g.n_sites)
+    vt = to_dev(v, cuda)
+    for op, oop in ((Q.OP_D, 0), (Q.OP_DDAG, 1), (Q.OP_DDAGD, 2)):
+        out = vt.clone() * 0
+        rep = ov.apply(out, vt, op, tol_inner=1e-11)
+        assert rep.status == Q.OK and rep.true_rel_res <= 1e-11
+        ref = Do.overlap(v, lmin, lmax, order, oop, tol_inner=1e-12)
+        assert rel(from_dev(out), ref) < 1e-8, (op, rel(from_dev(out), ref))
+
+
+def test_lambda_estimate_matches_oracle(cuda):
+    rng, g, lat, Do, Dq = _setup(2, -1.0, 70)
+    lmin, lmax = Do.lambda_bounds(tol_outer=1e-10)
+    ov = Q.Overlap(Dq, 21, Q.PREC_F32)
+    info = ov.update(tol_outer=1e-10)
+    assert abs(info["lambda_max"] / lmax - 1) < 1e-6
+    assert abs(info["lambda_min"] / lmin - 1) < 1e-5
+    assert abs(info["k"] - lmin / lmax) < 1e-5
+
+
+def test_sign_function_against_dense_eigh_n8(cuda):
+    # benchmark spec: sign-function error checked against FP64 dense eigh at n=8
+    rng, g, lat, Do, Dq = _setup(8, -1.0, 71)
+    M = Do.dense()
+    ev = np.linalg.eigvalsh(M.conj().T @ M)
+    lmin, lmax = np.sqrt(ev.min()) * 0.999, np.sqrt(ev.max()) * 1.001
+    order = 41
+    ov = Q.Overlap(Dq, order, Q.PREC_F32)
+    info = ov.update(lmin, lmax)
+    X = M / lmax
+    w, U = np.linalg.eigh(X.conj().T @ X)
+    V = X @ (U @ np.diag(w ** -0.5) @ U.conj().T)  # exact X (X^dag X)^{-1/2}
+    g5 = np.tile([1.0, -1.0], g.n_sites)
+    for _ in range(2):
+        v = rand_spinor(rng, g.n_sites)
+        vt = to_dev(v, cuda)
+        out = vt.clone() * 0
+        rep = ov.apply(out, vt, Q.OP_D, tol_inner=1e-12)
+        assert rep.status == Q.OK
+        Vv = from_dev(out) - v
+        err = np.linalg.norm(Vv - V @ v) / np.linalg.norm(v)
+        assert err < 10 * max(info["delta"], 1e-11), (err, info["delta"])
+        # sign(H_W) = g5 V for H_W = g5 X: g5 V is hermitian and squares to 1
+        sv = g5 * Vv
+        assert abs(np.linalg.norm(sv) / np.linalg.norm(v) - 1) < 1e-8
+
+
+def test_ginsparg_wilson_relation(cuda):
+    rng, g, lat, Do, Dq = _setup(4, -1.0, 72)
+    lmin, lmax = Do.lambda_bounds()
+    ov = Q.Overlap(Dq, 41, Q.PREC_F32)
+    info = ov.update(lmin, lmax)
+    v = rand_spinor(rng, g.n_sites)
+    g5 = np.tile([1.0, -1.0], g.n_sites)
+
+    def D(x):
+        xt = to_dev(x, cuda)
+        out = xt.clone() * 0
+        ov.apply(out, xt, Q.OP_D, tol_inner=1e-12)
+        return from_dev(out)
+
+    lhs = g5 * D(v) + D(g5 * v)
+    rhs = D(g5 * D(v))
+    assert np.linalg.norm(lhs - rhs) / np.linalg.norm(v) < 1e-8 + 10 * info["delta"]
