@@ -48,6 +48,7 @@ extern "C" {
 typedef struct qed3_lattice_s qed3_lattice;
 typedef struct qed3_dirac_s qed3_dirac;
 typedef struct qed3_overlap_s qed3_overlap;
+typedef struct qed3_lpc_s qed3_lpc;
 
 /* Message of the last failure on the calling thread ("" if none). */
 const char* qed3_last_error_string(void);
@@ -232,6 +233,52 @@ int qed3_overlap_apply(qed3_overlap* ov, int op, double* out, const double* in, 
  * Returns the size n/2+1 through *size.
  * ====================================================================== */
 int qed3_zolotarev(double k, int n, double* c, double* cp, double* A, double* scal, int* size);
+
+/* ======================================================================
+ * Learned preconditioner and preconditioned CG  --  no counterpart in the
+ * reference (its solvers are unpreconditioned CG: src/both_3d/cg_cuda.h,
+ * sparse_matrix.h).  N(r) = a^2 r + G^dag G r, G = L_layers o ... o L_1,
+ * each layer a gauge-covariant parallel-transport convolution over complex
+ * channels, L(h)[c] = sum_c' W0[c,c'] h[c'] + W1[c,c'] Hd h[c'] + W2[c,c'] Ho h[c'],
+ * where Hd / Ho are the spin-diagonal / off-diagonal parts of the Dirac hop
+ * restricted to the solver's per-SM site blocks.  N is hermitian positive
+ * definite by construction.  Trained on the GPU (hand-written forward,
+ * backward and Adam kernels) on residual / error pairs taken from the
+ * solver's own iterates, loss 1 - |<z,r>|^2 / (<z,A z> <e,r>) with A = D^dag D.
+ * ====================================================================== */
+/* channels in [1, 64], layers in [1, 2]; the block partition is the one of the
+ * register-resident solvers on the current device. */
+int qed3_lpc_create(qed3_dirac* d, int channels, int layers, unsigned seed, qed3_lpc** out);
+int qed3_lpc_destroy(qed3_lpc* pc);
+/* nparams: complex parameters (layer l: 3 x Cout x Cin, row-major [j][c][c'],
+ * then a as (a, 0)); block_sites: sites per block; npairs: training pairs held. */
+int qed3_lpc_info(const qed3_lpc* pc, int* nparams, int* block_sites, int* npairs);
+/* host arrays of 2*nparams doubles (re, im interleaved); set resets Adam. */
+int qed3_lpc_get_weights(const qed3_lpc* pc, double* w);
+int qed3_lpc_set_weights(qed3_lpc* pc, const double* w);
+/* z = N r with the hop blocks of the operator pc was created on.  r, z: device
+ * complex128, nrhs vectors of 2*n_sites back to back, reference order.
+ * form 0: layer-by-layer (the training network); form 1: the collapsed word
+ * form the solver applies (identical up to rounding). */
+int qed3_lpc_apply(qed3_lpc* pc, int form, double* z, const double* r, int nrhs, void* stream);
+/* loss and its gradient (host grad[2*nparams]) on pairs (r, e) of the creating
+ * operator; device complex128 inputs as in qed3_lpc_apply. */
+int qed3_lpc_loss_grad(qed3_lpc* pc, const double* r, const double* e, int nrhs, double* loss, double* grad,
+                       void* stream);
+/* Adds nsrc * nsnap training pairs from operator d (same lattice): Gaussian
+ * sources (seeded), x* from a full solve, x_k = CG stopped after snapshots[k]
+ * iterations (0: x_k = 0), pair (b - A x_k, x* - x_k) / |b - A x_k|. */
+int qed3_lpc_collect(qed3_lpc* pc, qed3_dirac* d, int nsrc, unsigned seed, const int* snapshots, int nsnap,
+                     int precision);
+/* steps of Adam (learning rate lr), each on `batch` pairs of one operator drawn
+ * at random; loss_history: host [steps] or NULL. */
+int qed3_lpc_train(qed3_lpc* pc, int steps, int batch, double lr, unsigned seed, double* loss_history);
+/* Preconditioned CG on D^dag D + shift with N applied block-locally inside the
+ * persistent kernel.  Same arguments, certificate and report as qed3_cg_solve;
+ * precision QED3_PREC_F32 or QED3_PREC_BF16 (halo copies), FP64 reliable
+ * updates and true residual.  d: any operator on pc's lattice. */
+int qed3_pcg_solve(qed3_dirac* d, qed3_lpc* pc, double* x, const double* b, const qed3_solve_params* params,
+                   qed3_solve_report* report, void* stream);
 
 #ifdef __cplusplus
 }

@@ -103,6 +103,17 @@ SIGNATURES = [
     ("qed3_batch_config", ctypes.c_int, [vp, c_int_p, c_int_p, c_int_p]),
     ("qed3_batch_solve", ctypes.c_int, [vp, vp, vp, vp, ctypes.POINTER(SolveParams), vp,
                                         ctypes.POINTER(ctypes.c_float), vp]),
+    ("qed3_lpc_create", ctypes.c_int, [vp, ctypes.c_int, ctypes.c_int, ctypes.c_uint, ctypes.POINTER(vp)]),
+    ("qed3_lpc_destroy", ctypes.c_int, [vp]),
+    ("qed3_lpc_info", ctypes.c_int, [vp, c_int_p, c_int_p, c_int_p]),
+    ("qed3_lpc_get_weights", ctypes.c_int, [vp, vp]),
+    ("qed3_lpc_set_weights", ctypes.c_int, [vp, vp]),
+    ("qed3_lpc_apply", ctypes.c_int, [vp, ctypes.c_int, vp, vp, ctypes.c_int, vp]),
+    ("qed3_lpc_loss_grad", ctypes.c_int, [vp, vp, vp, ctypes.c_int, c_double_p, vp, vp]),
+    ("qed3_lpc_collect", ctypes.c_int, [vp, vp, ctypes.c_int, ctypes.c_uint, vp, ctypes.c_int, ctypes.c_int]),
+    ("qed3_lpc_train", ctypes.c_int, [vp, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_uint, vp]),
+    ("qed3_pcg_solve", ctypes.c_int, [vp, vp, vp, vp, ctypes.POINTER(SolveParams), ctypes.POINTER(SolveReport),
+                                      vp]),
 ]
 
 
@@ -445,4 +456,71 @@ class Overlap:
     def __del__(self):
         if getattr(self, "_h", None) and _lib is not None:
             _lib.qed3_overlap_destroy(self._h)
+            self._h = None
+
+
+class LearnedPreconditioner:
+    """Gauge-covariant learned preconditioner N = a^2 I + G^dag G (no counterpart
+    in the reference, whose solvers are unpreconditioned CG,
+    src/both_3d/cg_cuda.h).  Trained on the GPU on (residual, error) pairs from
+    the solver's own iterates; applied block-locally inside the persistent
+    preconditioned CG (``solve``)."""
+
+    def __init__(self, dirac: DiracS2Dual, channels: int = 16, layers: int = 2, seed: int = 0):
+        self.dirac = dirac
+        self.channels, self.layers = channels, layers
+        h = vp()
+        _check(lib().qed3_lpc_create(dirac.handle, channels, layers, seed, ctypes.byref(h)))
+        self._h = h
+
+    def info(self) -> dict:
+        a, b, c = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        _check(lib().qed3_lpc_info(self._h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)))
+        return dict(nparams=a.value, block_sites=b.value, npairs=c.value)
+
+    def get_weights(self) -> np.ndarray:
+        w = np.zeros(2 * self.info()["nparams"])
+        _check(lib().qed3_lpc_get_weights(self._h, _ptr(w)))
+        return w.view(np.complex128)
+
+    def set_weights(self, w):
+        w = np.ascontiguousarray(np.asarray(w, dtype=np.complex128))
+        _check(lib().qed3_lpc_set_weights(self._h, _ptr(w)))
+
+    def apply(self, z, r, nrhs: int = 1, form: int = 0, stream=None):
+        """z = N r; device complex128, reference order, nrhs vectors back to back."""
+        _check(lib().qed3_lpc_apply(self._h, form, _ptr(z), _ptr(r), nrhs, _stream(stream)))
+        return z
+
+    def loss_grad(self, r, e, nrhs: int = 1, stream=None):
+        loss = ctypes.c_double()
+        g = np.zeros(2 * self.info()["nparams"])
+        _check(lib().qed3_lpc_loss_grad(self._h, _ptr(r), _ptr(e), nrhs, ctypes.byref(loss), _ptr(g),
+                                        _stream(stream)))
+        return loss.value, g.view(np.complex128)
+
+    def collect(self, dirac: DiracS2Dual, nsrc: int, seed: int, snapshots=(0, 5, 20, 60, 150),
+                precision: int = PREC_F32):
+        snaps = np.ascontiguousarray(snapshots, dtype=np.int32)
+        _check(lib().qed3_lpc_collect(self._h, dirac.handle, nsrc, seed, _ptr(snaps), len(snaps), precision))
+
+    def train(self, steps: int, batch: int = 8, lr: float = 3e-3, seed: int = 0) -> np.ndarray:
+        hist = np.zeros(max(steps, 1))
+        _check(lib().qed3_lpc_train(self._h, steps, batch, lr, seed, _ptr(hist)))
+        return hist[:steps]
+
+    def solve(self, dirac: DiracS2Dual, x, b, tol: float = 1e-10, maxiter: int = 100000,
+              precision: int = PREC_F32, delta: float = 0.1, shift: float = 0.0, stream=None) -> Report:
+        """Preconditioned CG on (D^dag D + shift) x = b; FP64 true-residual certificate."""
+        p = SolveParams(tol, maxiter, precision, delta, shift, 0)
+        r = SolveReport()
+        rc = lib().qed3_pcg_solve(dirac.handle, self._h, _ptr(x), _ptr(b), ctypes.byref(p), ctypes.byref(r),
+                                  _stream(stream))
+        if rc not in (OK, ERR_NOCONV):
+            _check(rc)
+        return Report(r.status, r.iters, r.reliable_updates, r.true_rel_res, r.ms)
+
+    def __del__(self):
+        if getattr(self, "_h", None) and _lib is not None:
+            _lib.qed3_lpc_destroy(self._h)
             self._h = None

@@ -14,7 +14,9 @@
 #include "dirac_impl.h"
 #include "gauge_impl.h"
 #include "handles.h"
+#include "lpc_impl.h"
 #include "overlap_impl.h"
+#include "pcg_impl.h"
 #include "qed3_internal.h"
 
 namespace qed3 {
@@ -442,6 +444,128 @@ int qed3_zolotarev(double k, int n, double* c, double* cp, double* A, double* sc
   }
   if (size) *size = z.size;
   return QED3_OK;
+  QED3_GUARD_END
+}
+
+int qed3_lpc_create(qed3_dirac* d, int channels, int layers, unsigned seed, qed3_lpc** out) {
+  QED3_GUARD_BEGIN
+  if (!d || !out) return fail(QED3_ERR_ARG, "NULL argument");
+  if (!d->coeffs_set) return fail(QED3_ERR_STATE, "operator coefficients not set");
+  *out = nullptr;
+  int dev = 0, smc = 0;
+  QED3_CUDA_TRY(cudaGetDevice(&dev));
+  QED3_CUDA_TRY(cudaDeviceGetAttribute(&smc, cudaDevAttrMultiProcessorCount, dev));
+  return lpc_create(d, channels, layers, pcg_block_sites(d->Ns, smc), seed, out);
+  QED3_GUARD_END
+}
+
+int qed3_lpc_destroy(qed3_lpc* pc) {
+  lpc_destroy(pc);
+  return QED3_OK;
+}
+
+int qed3_lpc_info(const qed3_lpc* pc, int* nparams, int* block_sites, int* npairs) {
+  if (!pc) return fail(QED3_ERR_ARG, "NULL preconditioner");
+  if (nparams) *nparams = pc->nparam;
+  if (block_sites) *block_sites = pc->per;
+  if (npairs) *npairs = pc->npairs;
+  return QED3_OK;
+}
+
+int qed3_lpc_get_weights(const qed3_lpc* pc, double* w) {
+  QED3_GUARD_BEGIN
+  if (!pc || !w) return fail(QED3_ERR_ARG, "NULL argument");
+  return lpc_get_weights(pc, w);
+  QED3_GUARD_END
+}
+
+int qed3_lpc_set_weights(qed3_lpc* pc, const double* w) {
+  QED3_GUARD_BEGIN
+  if (!pc || !w) return fail(QED3_ERR_ARG, "NULL argument");
+  return lpc_set_weights(pc, w);
+  QED3_GUARD_END
+}
+
+int qed3_lpc_apply(qed3_lpc* pc, int form, double* z, const double* r, int nrhs, void* stream) {
+  QED3_GUARD_BEGIN
+  if (!pc || !z || !r) return fail(QED3_ERR_ARG, "NULL argument");
+  if (form != 0 && form != 1) return fail(QED3_ERR_ARG, "form must be 0 (layers) or 1 (words)");
+  if (nrhs < 1) return fail(QED3_ERR_ARG, "nrhs must be positive");
+  if (form == 1 && pc->C < (pc->LG == 2 ? 7 : 3)) return fail(QED3_ERR_ARG, "word form needs >= 7 (3) channels");
+  cudaStream_t st = (cudaStream_t)stream;
+  const size_t n = size_t(nrhs) * pc->Ns * 2;
+  float2 *fr = nullptr, *fz = nullptr;
+  QED3_CUDA_TRY(cudaMalloc(&fr, n * sizeof(float2)));
+  if (cudaMalloc(&fz, n * sizeof(float2)) != cudaSuccess) {
+    cudaFree(fr);
+    return fail(QED3_ERR_NOMEM, "cudaMalloc failed");
+  }
+  int rc = field_import(pc->d, QED3_PREC_F32, fr, r, nrhs, st);
+  if (!rc) rc = form == 0 ? lpc_forward(pc, nrhs, fr, fz, st) : lpc_apply_words(pc, nrhs, fr, fz, st);
+  if (!rc) rc = field_export(pc->d, QED3_PREC_F32, z, fz, nrhs, st);
+  if (!rc && cudaStreamSynchronize(st) != cudaSuccess) rc = fail(QED3_ERR_CUDA, "stream synchronize failed");
+  cudaFree(fr);
+  cudaFree(fz);
+  return rc;
+  QED3_GUARD_END
+}
+
+int qed3_lpc_loss_grad(qed3_lpc* pc, const double* r, const double* e, int nrhs, double* loss, double* grad,
+                       void* stream) {
+  QED3_GUARD_BEGIN
+  if (!pc || !r || !e || !loss) return fail(QED3_ERR_ARG, "NULL argument");
+  if (nrhs < 1) return fail(QED3_ERR_ARG, "nrhs must be positive");
+  cudaStream_t st = (cudaStream_t)stream;
+  const size_t n = size_t(nrhs) * pc->Ns * 2;
+  float2 *fr = nullptr, *fe = nullptr;
+  QED3_CUDA_TRY(cudaMalloc(&fr, n * sizeof(float2)));
+  if (cudaMalloc(&fe, n * sizeof(float2)) != cudaSuccess) {
+    cudaFree(fr);
+    return fail(QED3_ERR_NOMEM, "cudaMalloc failed");
+  }
+  int rc = field_import(pc->d, QED3_PREC_F32, fr, r, nrhs, st);
+  if (!rc) rc = field_import(pc->d, QED3_PREC_F32, fe, e, nrhs, st);
+  if (!rc) rc = lpc_loss_grad(pc, nrhs, fr, fe, loss, st);
+  if (!rc && grad) {
+    std::vector<float2> g(pc->nparam);
+    if (cudaMemcpyAsync(g.data(), pc->G, pc->nparam * sizeof(float2), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+        cudaStreamSynchronize(st) != cudaSuccess)
+      rc = fail(QED3_ERR_CUDA, "gradient read-back failed");
+    for (int i = 0; !rc && i < pc->nparam; i++) {
+      grad[2 * i] = g[i].x;
+      grad[2 * i + 1] = g[i].y;
+    }
+  }
+  cudaFree(fr);
+  cudaFree(fe);
+  return rc;
+  QED3_GUARD_END
+}
+
+int qed3_lpc_collect(qed3_lpc* pc, qed3_dirac* d, int nsrc, unsigned seed, const int* snapshots, int nsnap,
+                     int precision) {
+  QED3_GUARD_BEGIN
+  if (!pc || !d || !snapshots) return fail(QED3_ERR_ARG, "NULL argument");
+  if (nsrc < 1 || nsnap < 1) return fail(QED3_ERR_ARG, "nsrc and nsnap must be positive");
+  if (precision < 0 || precision > 2) return fail(QED3_ERR_ARG, "unknown precision");
+  if (!d->coeffs_set) return fail(QED3_ERR_STATE, "operator coefficients not set");
+  return lpc_collect(pc, d, nsrc, seed, snapshots, nsnap, precision);
+  QED3_GUARD_END
+}
+
+int qed3_lpc_train(qed3_lpc* pc, int steps, int batch, double lr, unsigned seed, double* loss_history) {
+  QED3_GUARD_BEGIN
+  if (!pc) return fail(QED3_ERR_ARG, "NULL preconditioner");
+  if (steps < 0 || batch < 1 || !(lr > 0)) return fail(QED3_ERR_ARG, "need steps >= 0, batch >= 1, lr > 0");
+  return lpc_train(pc, steps, batch, lr, seed, loss_history);
+  QED3_GUARD_END
+}
+
+int qed3_pcg_solve(qed3_dirac* d, qed3_lpc* pc, double* x, const double* b, const qed3_solve_params* params,
+                   qed3_solve_report* report, void* stream) {
+  QED3_GUARD_BEGIN
+  if (!d || !pc || !x || !b) return fail(QED3_ERR_ARG, "NULL argument");
+  return pcg_solve(d, pc, x, b, params, report, (cudaStream_t)stream);
   QED3_GUARD_END
 }
 

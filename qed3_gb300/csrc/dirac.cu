@@ -343,4 +343,12 @@ int dirac_apply_field(qed3_dirac_s* d, int op, int prec, void* out, const void* 
   return QED3_OK;
 }
 
+int dirac_apply32_blocks(qed3_dirac_s* d, const M32* H, void* out, const void* in, int nrhs, cudaStream_t st) {
+  const DeviceLattice& D = d->lat->dev;
+  k_apply32<P32><<<nblk(d->Ns), 256, 0, st>>>(d->Ns, nrhs, D.nbr, H, d->diag32, reinterpret_cast<const float4*>(in),
+                                              reinterpret_cast<float4*>(out));
+  QED3_CUDA_TRY(cudaGetLastError());
+  return QED3_OK;
+}
+
 }  // namespace qed3

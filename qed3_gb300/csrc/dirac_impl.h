@@ -16,12 +16,18 @@ int dirac_set_links(qed3_dirac_s* d, const double* A, int on_device, cudaStream_
 int dirac_set_coefficients(qed3_dirac_s* d, const double* hop, const double* diag);
 int dirac_apply_ref(qed3_dirac_s* d, int op, double* out, const double* in, cudaStream_t st);
 int dirac_apply_field(qed3_dirac_s* d, int op, int prec, void* out, const void* in, int nrhs, cudaStream_t st);
+// fp32 field apply with caller-supplied hop blocks (same lattice and diagonal)
+int dirac_apply32_blocks(qed3_dirac_s* d, const M32* H, void* out, const void* in, int nrhs, cudaStream_t st);
 int field_import(qed3_dirac_s* d, int prec, void* field, const double* in_ref, int nrhs, cudaStream_t st);
 int field_export(qed3_dirac_s* d, int prec, double* out_ref, const void* field, int nrhs, cudaStream_t st);
 
 int cg_solve(qed3_dirac_s* d, double* x, const double* b, const qed3_solve_params* prm, qed3_solve_report* rep,
              cudaStream_t st);
 int solver_free(qed3_dirac_s* d);
+// solver scratch of the operator (allocated on first use) and the common
+// epilogue of the persistent solvers: report, export of the solution
+int ensure_work(qed3_dirac_s* d);
+int cg_finish(qed3_dirac_s* d, double* x, qed3_solve_report* rep, cudaStream_t st);
 int cg_solve_noalloc(qed3_dirac_s* d, double* x, const double* b, const qed3_solve_params* prm,
                      qed3_solve_report* rep, cudaStream_t st);
 

@@ -1,0 +1,531 @@
+// Preconditioned persistent CG with the learned block-local preconditioner.
+//
+// No counterpart in the reference (its solvers are unpreconditioned CG,
+// src/both_3d/sparse_matrix.h / cg_cuda.h).  Same skeleton as the
+// register-resident solver (solver_v2.cu): one block per SM, thread t of block
+// b owns sites b*per + k*T + t, two grid barriers per iteration, FP64
+// reductions riding on them, fp32 state with fp32/bf16 halo copies, FP64
+// reliable updates and an FP64 true-residual certificate.  What changes:
+//
+//   z = N r is applied right after r is updated, inside phase B, entirely in
+//   shared memory: N = a^2 I + sum_{w,w'} O_w^dag M_{ww'} O_w' with words
+//   O_w over {Hd, Ho} (the spin-diagonal / off-diagonal parts of the Dirac hop
+//   restricted to the block) -- it never leaves the SM, so the iteration
+//   keeps its two grid barriers.  N is hermitian positive definite, so the
+//   short PCG recurrence holds:
+//     t = D p = a_z D z + beta t,  p = a_z z + beta p   (phase A, gathers z)
+//     q = D^dag t + s p, x += alpha p, r -= alpha q, z = N r   (phase B, gathers t)
+//   with alpha = <r,z> / (|t|^2 + s|p|^2), beta = <r,z>_new / <r,z>_old.
+//   After a reliable update (r = b - A x in FP64) the direction is
+//   re-conjugated to the new residual: a_z = 1 - beta <r,p> / <r,z>.
+
+#include <cmath>
+#include <string>
+
+#include "device.cuh"
+#include "dirac_impl.h"
+#include "handles.h"
+#include "lpc_impl.h"
+#include "pcg_impl.h"
+#include "v2_common.cuh"
+
+namespace qed3 {
+
+struct PcgArgs {
+  int Ns, per;
+  const int* nbr;
+  const M64* H;
+  const M64* Hd;
+  const double* diag;
+  const M32* H32;
+  const M32* Hd32;
+  const float* diag32;
+  const S64* b;
+  S64* x;
+  S64* t64;
+  void* halo_z;
+  void* halo_t;
+  double* partials;
+  GridBar2* bar;
+  double* scal;
+  double tol2, delta2, shift;
+  int maxiter;
+  long long spin_limit;
+  LpcWordCoef pc;
+};
+
+__device__ __forceinline__ float4 sp2f4(const Sp32& v) { return make_float4(v.s0.x, v.s0.y, v.s1.x, v.s1.y); }
+__device__ __forceinline__ Sp32 f42sp(const float4& v) { return {make_float2(v.x, v.y), make_float2(v.z, v.w)}; }
+__device__ __forceinline__ float2 cm(float2 a, float2 b) { return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x); }
+
+// (Hd F)(i), (Ho F)(i) from the block's shared-memory field F (site j of the
+// block at F[j - blk0]), in-block neighbours only
+template <bool WD, bool WO>
+__device__ __forceinline__ void hop_split(const float4* __restrict__ F, const int (&jj)[3], int blk0, int per, int i,
+                                          int Ns, const M32* __restrict__ H, Sp32& hd, Sp32& ho) {
+  hd = Sp32{make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
+  ho = hd;
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    const int l = jj[k] - blk0;
+    if (unsigned(l) >= unsigned(per)) continue;
+    const float4* m = reinterpret_cast<const float4*>(H + size_t(k) * Ns + i);
+    const float4 r0 = __ldg(m), r1 = __ldg(m + 1);
+    const float4 y = F[l];
+    const float2 y0 = make_float2(y.x, y.y), y1 = make_float2(y.z, y.w);
+    if (WD) {
+      hd.s0 = cfmaf(make_float2(r0.x, r0.y), y0, hd.s0);  // h00 y0
+      hd.s1 = cfmaf(make_float2(r1.z, r1.w), y1, hd.s1);  // h11 y1
+    }
+    if (WO) {
+      ho.s0 = cfmaf(make_float2(r0.z, r0.w), y1, ho.s0);  // h01 y1
+      ho.s1 = cfmaf(make_float2(r1.x, r1.y), y0, ho.s1);  // h10 y0
+    }
+  }
+}
+
+__device__ __forceinline__ void acc_c(Sp32& acc, float2 c, const Sp32& f) {
+  acc.s0 = cfmaf(c, f.s0, acc.s0);
+  acc.s1 = cfmaf(c, f.s1, acc.s1);
+}
+__device__ __forceinline__ Sp32 sp_add(const Sp32& a, const Sp32& b, float sb) {
+  return {make_float2(a.s0.x + sb * b.s0.x, a.s0.y + sb * b.s0.y), make_float2(a.s1.x + sb * b.s1.x, a.s1.y + sb * b.s1.y)};
+}
+
+// z = N r for the block's sites; every thread of the block calls it (sites
+// past Ns carry zeros).  S: NW fields of `per` float4 in shared memory.
+template <int NW, int SPT>
+__device__ __forceinline__ void pc_apply(const PcgArgs& a, float4* S, int blk0, const int (&own)[SPT],
+                                         const int (&loc)[SPT], const bool (&val)[SPT], const int (&jj)[SPT][3],
+                                         const Sp32 (&r)[SPT], Sp32 (&z)[SPT]) {
+  const int per = a.per, Ns = a.Ns;
+  const Sp32 zero{make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
+  float4* S0 = S;
+  float4* S1 = S + per;
+  float4* S2 = S + 2 * per;
+#pragma unroll
+  for (int k = 0; k < SPT; k++) S0[loc[k]] = sp2f4(val[k] ? r[k] : zero);
+  __syncthreads();
+  Sp32 g0[SPT], g1[SPT], g2[SPT];
+#pragma unroll
+  for (int k = 0; k < SPT; k++) {
+    Sp32 f[NW];
+    f[0] = r[k];
+    if (val[k]) hop_split<true, true>(S0, jj[k], blk0, per, own[k], Ns, a.H32, f[1], f[2]);
+    else f[1] = f[2] = zero;
+    if constexpr (NW == 7) {
+      S1[loc[k]] = sp2f4(f[1]);
+      S2[loc[k]] = sp2f4(f[2]);
+    } else {
+#pragma unroll
+      for (int w = 0; w < 3; w++) {
+        Sp32 g = zero;
+#pragma unroll
+        for (int q = 0; q < 3; q++) acc_c(g, a.pc.M[w][q], f[q]);
+        if (w == 0) g0[k] = g;
+        if (w == 1) g1[k] = g;
+        if (w == 2) g2[k] = g;
+      }
+    }
+  }
+  if constexpr (NW == 7) {
+    float4* S3 = S + 3 * per;
+    float4* S4 = S + 4 * per;
+    float4* S5 = S + 5 * per;
+    float4* S6 = S + 6 * per;
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < SPT; k++) {
+      Sp32 f[7];
+      f[0] = r[k];
+      f[1] = f42sp(S1[loc[k]]);
+      f[2] = f42sp(S2[loc[k]]);
+      if (val[k]) {
+        hop_split<true, true>(S1, jj[k], blk0, per, own[k], Ns, a.H32, f[3], f[5]);  // Hd Hd r, Ho Hd r
+        hop_split<true, true>(S2, jj[k], blk0, per, own[k], Ns, a.H32, f[4], f[6]);  // Hd Ho r, Ho Ho r
+      } else {
+        f[3] = f[4] = f[5] = f[6] = zero;
+      }
+#pragma unroll
+      for (int w = 0; w < 7; w++) {
+        Sp32 g = zero;
+#pragma unroll
+        for (int q = 0; q < 7; q++) acc_c(g, a.pc.M[w][q], f[q]);
+        if (w == 0) g0[k] = g;
+        else if (w == 1) g1[k] = g;
+        else if (w == 2) g2[k] = g;
+        else if (w == 3) S3[loc[k]] = sp2f4(g);
+        else if (w == 4) S4[loc[k]] = sp2f4(g);
+        else if (w == 5) S5[loc[k]] = sp2f4(g);
+        else S6[loc[k]] = sp2f4(g);
+      }
+    }
+    __syncthreads();
+    // u = g1 + Hd g3 - Ho g5 -> S1 ; v = -g2 - Hd g4 + Ho g6 -> S2
+#pragma unroll
+    for (int k = 0; k < SPT; k++) {
+      Sp32 u = g1[k], v = sp_add(zero, g2[k], -1.f);
+      if (val[k]) {
+        Sp32 d3, o5, d4, o6, dummy;
+        hop_split<true, false>(S3, jj[k], blk0, per, own[k], Ns, a.H32, d3, dummy);
+        hop_split<false, true>(S5, jj[k], blk0, per, own[k], Ns, a.H32, dummy, o5);
+        hop_split<true, false>(S4, jj[k], blk0, per, own[k], Ns, a.H32, d4, dummy);
+        hop_split<false, true>(S6, jj[k], blk0, per, own[k], Ns, a.H32, dummy, o6);
+        u = sp_add(sp_add(u, d3, 1.f), o5, -1.f);
+        v = sp_add(sp_add(v, d4, -1.f), o6, 1.f);
+      } else {
+        u = v = zero;
+      }
+      S1[loc[k]] = sp2f4(u);
+      S2[loc[k]] = sp2f4(v);
+    }
+  } else {
+#pragma unroll
+    for (int k = 0; k < SPT; k++) {
+      S1[loc[k]] = sp2f4(val[k] ? g1[k] : zero);
+      S2[loc[k]] = sp2f4(val[k] ? sp_add(zero, g2[k], -1.f) : zero);
+    }
+  }
+  __syncthreads();
+  // z = a^2 r + g0 + Hd u + Ho v
+#pragma unroll
+  for (int k = 0; k < SPT; k++) {
+    if (!val[k]) {
+      z[k] = zero;
+      continue;
+    }
+    Sp32 du, ov, dummy;
+    hop_split<true, false>(S1, jj[k], blk0, per, own[k], Ns, a.H32, du, dummy);
+    hop_split<false, true>(S2, jj[k], blk0, per, own[k], Ns, a.H32, dummy, ov);
+    Sp32 o = sp_add(g0[k], r[k], a.pc.a2);
+    o = sp_add(sp_add(o, du, 1.f), ov, 1.f);
+    z[k] = o;
+  }
+}
+
+__device__ __forceinline__ float rdotf(const Sp32& a, const Sp32& b) {  // Re <a, b>
+  return a.s0.x * b.s0.x + a.s0.y * b.s0.y + a.s1.x * b.s1.x + a.s1.y * b.s1.y;
+}
+
+template <int P, int NW, int SPT>
+__global__ void __launch_bounds__(576, 1) k_pcg(PcgArgs a) {
+  extern __shared__ float4 S[];
+  __shared__ double sh[32 * 4 + 64 + 8];
+  const int Ns = a.Ns;
+  const int T = blockDim.x;
+  const int blk0 = blockIdx.x * a.per;
+
+  int own[SPT], loc[SPT];
+  bool val[SPT];
+  int jj[SPT][3];
+  Sp32 r[SPT], p[SPT], t[SPT], z[SPT];
+  Sp64 xh[SPT];
+  Sp32 xl[SPT];
+  const Sp64 z64{make_double2(0, 0), make_double2(0, 0)};
+  const Sp32 z32{make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
+
+  // ---- phase 0: ids, r = b, z = N r, p = t = x = 0 -------------------------------------
+  double v2[2] = {0.0, 0.0};
+#pragma unroll
+  for (int k = 0; k < SPT; k++) {
+    loc[k] = k * T + threadIdx.x;
+    const int i = blk0 + loc[k];
+    own[k] = i;
+    val[k] = i < Ns;
+    xh[k] = z64;
+    xl[k] = z32;
+    p[k] = z32;
+    t[k] = z32;
+    r[k] = z32;
+#pragma unroll
+    for (int q = 0; q < 3; q++) jj[k][q] = 0;
+    if (val[k]) {
+#pragma unroll
+      for (int q = 0; q < 3; q++) jj[k][q] = __ldg(a.nbr + q * Ns + i);
+      const Sp64 bi = ld64(a.b, i);
+      v2[0] += n2(bi);
+      r[k] = Sp32{make_float2(float(bi.s0.x), float(bi.s0.y)), make_float2(float(bi.s1.x), float(bi.s1.y))};
+    }
+  }
+  pc_apply<NW, SPT>(a, S, blk0, own, loc, val, jj, r, z);
+#pragma unroll
+  for (int k = 0; k < SPT; k++) {
+    if (!val[k]) continue;
+    hs32<P>(a.halo_z, own[k], z[k]);
+    v2[1] += double(rdotf(r[k], z[k]));
+  }
+  unsigned int epoch = 0;
+  int parity = 0;
+  v2_publish<2>(v2, a.partials, parity, sh);
+  if (!grid_sync2(a.bar, epoch, a.spin_limit)) goto timeout;
+  {
+    double tot[2];
+    v2_total<2>(a.partials, parity, tot, sh);
+    parity ^= 1;
+    const double bnorm2 = tot[0];
+    double rho = tot[1];
+    double mu = bnorm2, mu_max = bnorm2, beta = 0.0, mu_true = bnorm2;
+    double2 a_z = make_double2(1.0, 0.0);
+    int iter = 0, nru = 0, status = QED3_ERR_NOCONV;
+    const double s = a.shift;
+    if (bnorm2 == 0.0) {
+      status = QED3_OK;
+      mu_true = 0.0;
+      goto finish;
+    }
+    while (true) {
+      // ---- phase A: t = a_z D z + beta t, p = a_z z + beta p ----------------------------
+      {
+        double v[1] = {0.0};
+        const float2 az = make_float2(float(a_z.x), float(a_z.y));
+        const float bt = float(beta);
+#pragma unroll
+        for (int k = 0; k < SPT; k++) {
+          if (!val[k]) continue;
+          const int i = own[k];
+          const Sp32 dz = stencil32<P>(i, Ns, jj[k], a.H32, a.diag32, z[k], a.halo_z);
+          t[k].s0 = cfmaf(az, dz.s0, make_float2(bt * t[k].s0.x, bt * t[k].s0.y));
+          t[k].s1 = cfmaf(az, dz.s1, make_float2(bt * t[k].s1.x, bt * t[k].s1.y));
+          p[k].s0 = cfmaf(az, z[k].s0, make_float2(bt * p[k].s0.x, bt * p[k].s0.y));
+          p[k].s1 = cfmaf(az, z[k].s1, make_float2(bt * p[k].s1.x, bt * p[k].s1.y));
+          hs32<P>(a.halo_t, i, t[k]);
+          v[0] += double(n2f(t[k])) + s * double(n2f(p[k]));
+        }
+        v2_publish<1>(v, a.partials, parity, sh);
+        if (!grid_sync2(a.bar, epoch, a.spin_limit)) goto timeout;
+      }
+      double gam[1];
+      v2_total<1>(a.partials, parity, gam, sh);
+      parity ^= 1;
+      const double alpha = rho / gam[0];
+      // ---- phase B: q = D^dag t + s p, x += alpha p, r -= alpha q, z = N r -------------
+      {
+        double v[2] = {0.0, 0.0};
+        const float al = float(alpha), sf = float(s);
+#pragma unroll
+        for (int k = 0; k < SPT; k++) {
+          if (!val[k]) continue;
+          const Sp32 q = stencil32<P>(own[k], Ns, jj[k], a.Hd32, a.diag32, t[k], a.halo_t);
+          r[k].s0 = make_float2(r[k].s0.x - al * (q.s0.x + sf * p[k].s0.x), r[k].s0.y - al * (q.s0.y + sf * p[k].s0.y));
+          r[k].s1 = make_float2(r[k].s1.x - al * (q.s1.x + sf * p[k].s1.x), r[k].s1.y - al * (q.s1.y + sf * p[k].s1.y));
+          xl[k].s0 = make_float2(xl[k].s0.x + al * p[k].s0.x, xl[k].s0.y + al * p[k].s0.y);
+          xl[k].s1 = make_float2(xl[k].s1.x + al * p[k].s1.x, xl[k].s1.y + al * p[k].s1.y);
+        }
+        pc_apply<NW, SPT>(a, S, blk0, own, loc, val, jj, r, z);
+#pragma unroll
+        for (int k = 0; k < SPT; k++) {
+          if (!val[k]) continue;
+          hs32<P>(a.halo_z, own[k], z[k]);
+          v[0] += double(n2f(r[k]));
+          v[1] += double(rdotf(r[k], z[k]));
+        }
+        v2_publish<2>(v, a.partials, parity, sh);
+        if (!grid_sync2(a.bar, epoch, a.spin_limit)) goto timeout;
+      }
+      double mun[2];
+      v2_total<2>(a.partials, parity, mun, sh);
+      parity ^= 1;
+      iter++;
+      const double mu_new = mun[0], rho_new = mun[1];
+      mu_max = fmax(mu_max, mu_new);
+      const bool want = !isfinite(mu_new) || !isfinite(alpha) || !(rho_new > 0.0) || mu_new < a.tol2 * bnorm2 ||
+                        iter >= a.maxiter || mu_new < a.delta2 * mu_max;
+      if (!want) {
+        beta = rho_new / rho;
+        a_z = make_double2(1.0, 0.0);
+        rho = rho_new;
+        mu = mu_new;
+        continue;
+      }
+      // ---- R0: fold x, publish it ---------------------------------------------------------
+#pragma unroll
+      for (int k = 0; k < SPT; k++) {
+        if (!val[k]) continue;
+        xh[k].s0 = make_double2(xh[k].s0.x + xl[k].s0.x, xh[k].s0.y + xl[k].s0.y);
+        xh[k].s1 = make_double2(xh[k].s1.x + xl[k].s1.x, xh[k].s1.y + xl[k].s1.y);
+        xl[k] = z32;
+        hs64(a.x, own[k], xh[k]);
+      }
+      if (!grid_sync2(a.bar, epoch, a.spin_limit)) goto timeout;
+      // ---- R1: t64 = D x ------------------------------------------------------------------
+#pragma unroll
+      for (int k = 0; k < SPT; k++) {
+        if (!val[k]) continue;
+        const Sp64 o = stencil64(own[k], Ns, jj[k], a.H, a.diag, xh[k], a.x);
+        hs64(a.t64, own[k], o);
+      }
+      if (!grid_sync2(a.bar, epoch, a.spin_limit)) goto timeout;
+      // ---- R2: r = b - D^dag t64 - s x, z = N r;  |r|^2, <r,z>, <r,p> --------------------
+      {
+        double v[4] = {0.0, 0.0, 0.0, 0.0};
+#pragma unroll
+        for (int k = 0; k < SPT; k++) {
+          if (!val[k]) continue;
+          const int i = own[k];
+          const Sp64 self = hl64(a.t64, i);
+          const Sp64 q = stencil64(i, Ns, jj[k], a.Hd, a.diag, self, a.t64);
+          const Sp64 bi = ld64(a.b, i);
+          Sp64 rt;
+          rt.s0 = csub(bi.s0, cadd(q.s0, cscale(s, xh[k].s0)));
+          rt.s1 = csub(bi.s1, cadd(q.s1, cscale(s, xh[k].s1)));
+          v[0] += n2(rt);
+          const double2 pv0 = make_double2(p[k].s0.x, p[k].s0.y), pv1 = make_double2(p[k].s1.x, p[k].s1.y);
+          v[2] += rt.s0.x * pv0.x + rt.s0.y * pv0.y + rt.s1.x * pv1.x + rt.s1.y * pv1.y;
+          v[3] += rt.s0.x * pv0.y - rt.s0.y * pv0.x + rt.s1.x * pv1.y - rt.s1.y * pv1.x;
+          r[k] = Sp32{make_float2(float(rt.s0.x), float(rt.s0.y)), make_float2(float(rt.s1.x), float(rt.s1.y))};
+        }
+        pc_apply<NW, SPT>(a, S, blk0, own, loc, val, jj, r, z);
+#pragma unroll
+        for (int k = 0; k < SPT; k++) {
+          if (!val[k]) continue;
+          hs32<P>(a.halo_z, own[k], z[k]);
+          v[1] += double(rdotf(r[k], z[k]));
+        }
+        v2_publish<4>(v, a.partials, parity, sh);
+        if (!grid_sync2(a.bar, epoch, a.spin_limit)) goto timeout;
+      }
+      double tr[4];
+      v2_total<4>(a.partials, parity, tr, sh);
+      parity ^= 1;
+      nru++;
+      mu_true = tr[0];
+      if (mu_true < a.tol2 * bnorm2) {
+        status = QED3_OK;
+        break;
+      }
+      if (iter >= a.maxiter || !isfinite(mu_true) || !(tr[1] > 0.0)) {
+        status = QED3_ERR_NOCONV;
+        break;
+      }
+      beta = tr[1] / rho;
+      a_z = make_double2(1.0 - beta * tr[2] / tr[1], -beta * tr[3] / tr[1]);
+      rho = tr[1];
+      mu = mu_true;
+      mu_max = mu_true;
+    }
+  finish:
+#pragma unroll
+    for (int k = 0; k < SPT; k++)
+      if (val[k]) hs64(a.x, own[k], xh[k]);
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+      a.scal[0] = mu_true;
+      a.scal[1] = bnorm2;
+      a.scal[2] = iter;
+      a.scal[3] = nru;
+      a.scal[4] = status;
+      a.scal[5] = 0;
+    }
+    (void)mu;
+    return;
+  }
+timeout:
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    a.scal[4] = QED3_ERR_TIMEOUT;
+    a.scal[5] = 0;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------
+template <int P, int NW, int SPT>
+static const void* pcg_fn() {
+  return (const void*)k_pcg<P, NW, SPT>;
+}
+
+static const void* pcg_kernel(int prec, int nw, int spt) {
+  if (prec == QED3_PREC_F32) {
+    if (nw == 7) return spt == 1 ? pcg_fn<P32, 7, 1>() : pcg_fn<P32, 7, 2>();
+    return spt == 1 ? pcg_fn<P32, 3, 1>() : pcg_fn<P32, 3, 2>();
+  }
+  if (nw == 7) return spt == 1 ? pcg_fn<PBF16, 7, 1>() : pcg_fn<PBF16, 7, 2>();
+  return spt == 1 ? pcg_fn<PBF16, 3, 1>() : pcg_fn<PBF16, 3, 2>();
+}
+
+int pcg_block_sites(int Ns, int sm_count) {
+  const long long per_sm = (Ns + sm_count - 1) / sm_count;
+  if (per_sm <= 576) return int((per_sm + 31) / 32 * 32);
+  return int((per_sm + 63) / 64 * 64);
+}
+
+bool pcg_plan(int prec, int nw, int Ns, int per, int sm_count, int* grid, int* threads, int* spt, size_t* smem) {
+  for (int s : {1, 2}) {
+    if (per % (32 * s)) continue;
+    const int T = per / s;
+    if (T > 576) continue;
+    const void* fn = pcg_kernel(prec, nw, s);
+    const size_t sm = size_t(nw) * per * sizeof(float4);
+    if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(sm)) != cudaSuccess) {
+      cudaGetLastError();
+      continue;
+    }
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, T, sm) != cudaSuccess) {
+      cudaGetLastError();
+      continue;
+    }
+    const int G = (Ns + per - 1) / per;
+    if (per_sm < 1 || G > per_sm * sm_count) continue;
+    *grid = G;
+    *threads = T;
+    *spt = s;
+    *smem = sm;
+    return true;
+  }
+  return false;
+}
+
+int pcg_solve(qed3_dirac_s* d, qed3_lpc_s* L, double* x, const double* b, const qed3_solve_params* prm,
+              qed3_solve_report* rep, cudaStream_t st) {
+  if (!d->coeffs_set) return fail(QED3_ERR_STATE, "operator coefficients not set (call qed3_dirac_set_links)");
+  if (L->Ns != d->Ns) return fail(QED3_ERR_ARG, "preconditioner and operator live on different lattices");
+  int rc = ensure_work(d);
+  if (rc) return rc;
+  SolverWork& w = d->work;
+  const int prec = prm ? prm->precision : QED3_PREC_F32;
+  if (prec != QED3_PREC_F32 && prec != QED3_PREC_BF16)
+    return fail(QED3_ERR_ARG, "preconditioned CG runs in mixed precision (QED3_PREC_F32 or QED3_PREC_BF16)");
+  const double tol = prm && prm->tol > 0 ? prm->tol : 1e-10;
+  const double delta = prm && prm->delta > 0 ? prm->delta : 0.1;
+  const int maxiter = prm && prm->maxiter > 0 ? prm->maxiter : 100000;
+  const double shift = prm ? prm->shift : 0.0;
+  LpcWordCoef co;
+  if ((rc = lpc_word_coef_cached(L, &co))) return rc;
+  int grid = 0, threads = 0, spt = 0;
+  size_t smem = 0;
+  if (!pcg_plan(prec, co.nwords, d->Ns, L->per, d->sm_count, &grid, &threads, &spt, &smem))
+    return fail(QED3_ERR_ARG, "lattice too large for the register-resident preconditioned solver");
+  if ((rc = field_import(d, QED3_PREC_F64, w.b, b, 1, st))) return rc;
+  QED3_CUDA_TRY(cudaMemsetAsync(w.bar2, 0, sizeof(GridBar2), st));
+  PcgArgs a{};
+  a.Ns = d->Ns;
+  a.per = L->per;
+  a.nbr = d->lat->dev.nbr;
+  a.H = d->H;
+  a.Hd = d->Hd;
+  a.diag = d->diag;
+  a.H32 = d->H32;
+  a.Hd32 = d->Hd32;
+  a.diag32 = d->diag32;
+  a.b = w.b;
+  a.x = w.xhi;
+  a.t64 = w.t64;
+  a.halo_z = w.r;
+  a.halo_t = w.t;
+  a.partials = w.partials;
+  a.bar = w.bar2;
+  a.scal = w.scal;
+  a.tol2 = tol * tol;
+  a.delta2 = delta * delta;
+  a.shift = shift;
+  a.maxiter = maxiter;
+  a.spin_limit = 4000000LL;
+  a.pc = co;
+  void* kargs[] = {&a};
+  QED3_CUDA_TRY(cudaEventRecord(w.e0, st));
+  QED3_CUDA_TRY(cudaLaunchCooperativeKernel(pcg_kernel(prec, co.nwords, spt), dim3(grid), dim3(threads), kargs, smem, st));
+  QED3_CUDA_TRY(cudaEventRecord(w.e1, st));
+  return cg_finish(d, x, rep, st);
+}
+
+}  // namespace qed3

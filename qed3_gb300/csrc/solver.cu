@@ -368,7 +368,7 @@ timeout:
 // ---------------------------------------------------------------------------
 int cg_finish(qed3_dirac_s* d, double* x, qed3_solve_report* rep, cudaStream_t st);
 
-static int ensure_work(qed3_dirac_s* d) {
+int ensure_work(qed3_dirac_s* d) {
   SolverWork& w = d->work;
   const size_t Ns = size_t(d->Ns);
   if (w.ns == Ns) return QED3_OK;

@@ -1,0 +1,238 @@
+"""Learned preconditioner and preconditioned CG on the GPU.
+
+The network is checked against a plain torch restatement on the CPU
+(complex64): hop blocks taken from the oracle's CSR matrix of D in reference
+order, masked to the solver's site blocks through the lattice permutation.
+Gradients are checked against torch autograd of the same loss; the collapsed
+word form against the layer form; hermiticity and positivity of N directly;
+preconditioned CG against the oracle's CG and the FP64 true residual."""
+import ctypes
+
+import numpy as np
+import pytest
+
+import qed3_gb300 as Q
+from oracle import oracle as O
+from tests.gpu_util import from_dev, rand_spinor, to_dev
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+
+
+def _setup(n, M5=0.05, seed=3):
+    rng = np.random.default_rng(seed)
+    g = O.geometry(n)
+    lat = Q.S2Trivalent(n)
+    A = rng.uniform(-np.pi, np.pi, g.n_links)
+    Do = O.Dirac(g, 1.0, M5)
+    Do.update(A)
+    Dq = Q.DiracS2Dual(lat, 1.0, M5)
+    Dq.update(A)
+    return rng, g, lat, A, Do, Dq
+
+
+def _csr(Do):
+    import scipy.sparse as sp
+    L = O.lib()
+    nnz = L.orc_dirac_nnz(Do.h)
+    rows = np.zeros(Do.N + 1, np.int32)
+    cols = np.zeros(nnz, np.int32)
+    val = np.zeros(nnz, np.complex128)
+    ip = ctypes.POINTER(ctypes.c_int)
+    L.orc_dirac_get_csr(Do.h, rows.ctypes.data_as(ip), cols.ctypes.data_as(ip), val.ctypes.data_as(ctypes.c_void_p))
+    return sp.csr_matrix((val, cols, rows), shape=(Do.N, Do.N))
+
+
+class TorchNet:
+    """N(r) = a^2 r + G^dag G r restated in torch (CPU, complex64)."""
+
+    def __init__(self, g, Do, perm, per, C, LG, w):
+        Ds = _csr(Do)
+        Ns = g.n_sites
+        nns = np.asarray(g.nns).reshape(Ns, 3)
+        iperm = np.argsort(perm)
+        blk = iperm // per
+        Hb = np.zeros((Ns, 3, 2, 2), complex)
+        for x in range(Ns):
+            for k in range(3):
+                y = nns[x, k]
+                Hb[x, k] = Ds[2 * x:2 * x + 2, 2 * y:2 * y + 2].toarray()
+        mask = (blk[nns] == blk[:, None]).astype(float)
+        Hd = np.zeros_like(Hb)
+        Ho = np.zeros_like(Hb)
+        Hd[:, :, 0, 0] = Hb[:, :, 0, 0]
+        Hd[:, :, 1, 1] = Hb[:, :, 1, 1]
+        Ho[:, :, 0, 1] = Hb[:, :, 0, 1]
+        Ho[:, :, 1, 0] = Hb[:, :, 1, 0]
+        Hd *= mask[:, :, None, None]
+        Ho *= mask[:, :, None, None]
+        self.Hd = torch.tensor(Hd, dtype=torch.complex64)
+        self.Ho = torch.tensor(Ho, dtype=torch.complex64)
+        self.nns = torch.tensor(nns, dtype=torch.long)
+        A = (Ds.conj().T @ Ds).tocsr()
+        self.A = torch.sparse_csr_tensor(torch.tensor(A.indptr, dtype=torch.int64),
+                                         torch.tensor(A.indices, dtype=torch.int64),
+                                         torch.tensor(A.data, dtype=torch.complex64), size=A.shape)
+        self.Ns, self.C, self.LG = Ns, C, LG
+        chans = [1] + [C] * LG
+        self.Ws = []
+        off = 0
+        for l in range(LG):
+            k = 3 * chans[l + 1] * chans[l]
+            W = torch.tensor(w[off:off + k].reshape(3, chans[l + 1], chans[l]), dtype=torch.complex64)
+            self.Ws.append(W.requires_grad_(True))
+            off += k
+        self.a = torch.tensor(float(w[off].real), dtype=torch.float32, requires_grad=True)
+
+    def hops(self, h):
+        hn = h[:, self.nns]
+        return (torch.einsum("xkab,nxkcb->nxca", self.Hd, hn), torch.einsum("xkab,nxkcb->nxca", self.Ho, hn))
+
+    def layer(self, W, h, adj):
+        fa, fb = self.hops(h)
+        if adj:
+            Wc = W.conj().transpose(1, 2)
+            return (torch.einsum("oc,nxca->nxoa", Wc[0], h) + torch.einsum("oc,nxca->nxoa", Wc[1], fa)
+                    - torch.einsum("oc,nxca->nxoa", Wc[2], fb))
+        return (torch.einsum("oc,nxca->nxoa", W[0], h) + torch.einsum("oc,nxca->nxoa", W[1], fa)
+                + torch.einsum("oc,nxca->nxoa", W[2], fb))
+
+    def __call__(self, r):  # r: [B, Ns, 2]
+        h = r[:, :, None, :]
+        for W in self.Ws:
+            h = self.layer(W, h, False)
+        for W in reversed(self.Ws):
+            h = self.layer(W, h, True)
+        return self.a * self.a * r + h[:, :, 0, :]
+
+    def loss(self, R, E):
+        Z = self(R)
+        B = R.shape[0]
+        Zf, Rf, Ef = Z.reshape(B, -1), R.reshape(B, -1), E.reshape(B, -1)
+        AZ = (self.A @ Zf.T).T
+        zr = (Zf.conj() * Rf).sum(1)
+        zAz = (Zf.conj() * AZ).sum(1).real
+        er = (Ef.conj() * Rf).sum(1).real
+        return (1 - zr.abs() ** 2 / (zAz * er)).mean()
+
+
+def _net(n, C, LG, seed=5):
+    rng, g, lat, A, Do, Dq = _setup(n)
+    pc = Q.LearnedPreconditioner(Dq, channels=C, layers=LG, seed=seed)
+    info = pc.info()
+    w = pc.get_weights()
+    assert w.shape == (info["nparams"],)
+    tn = TorchNet(g, Do, lat.permutation(), info["block_sites"], C, LG, w)
+    return rng, g, lat, Do, Dq, pc, tn
+
+
+def _crel(a, b):
+    return float(np.abs(a - b).max() / np.abs(b).max())
+
+
+@pytest.mark.parametrize("C,LG", [(8, 1), (8, 2), (16, 2)])
+def test_lpc_forward_matches_torch(cuda, C, LG):
+    rng, g, lat, Do, Dq, pc, tn = _net(8, C, LG)
+    Ns = g.n_sites
+    B = 3
+    r = rand_spinor(rng, Ns, B)
+    rt = to_dev(r.reshape(-1), cuda)
+    z0 = torch.zeros_like(rt)
+    pc.apply(z0, rt, nrhs=B, form=0)
+    with torch.no_grad():
+        zr = tn(torch.tensor(r.reshape(B, Ns, 2), dtype=torch.complex64)).numpy().reshape(-1)
+    assert _crel(from_dev(z0), zr) < 2e-5
+    z1 = torch.zeros_like(rt)
+    pc.apply(z1, rt, nrhs=B, form=1)
+    assert _crel(from_dev(z1), zr) < 2e-5
+
+
+def test_lpc_hermitian_positive(cuda):
+    rng, g, lat, Do, Dq, pc, tn = _net(8, 8, 2)
+    Ns = g.n_sites
+    u = rand_spinor(rng, Ns)
+    v = rand_spinor(rng, Ns)
+    ut, vt = to_dev(u, cuda), to_dev(v, cuda)
+    Nu, Nv = torch.zeros_like(ut), torch.zeros_like(vt)
+    pc.apply(Nu, ut)
+    pc.apply(Nv, vt)
+    Nu, Nv = from_dev(Nu), from_dev(Nv)
+    lhs, rhs = np.vdot(u, Nv), np.vdot(Nu, v)
+    assert abs(lhs - rhs) / abs(lhs) < 1e-5
+    # <u, N u> >= a^2 |u|^2 > 0
+    a2 = pc.get_weights()[-1].real ** 2
+    assert np.vdot(u, Nu).real >= a2 * np.vdot(u, u).real * (1 - 1e-5)
+
+
+@pytest.mark.parametrize("LG", [1, 2])
+def test_lpc_gradient_matches_autograd(cuda, LG):
+    rng, g, lat, Do, Dq, pc, tn = _net(8, 8, LG)
+    Ns = g.n_sites
+    B = 4
+    R = rand_spinor(rng, Ns, B)
+    E = rand_spinor(rng, Ns, B) + 0.5 * R  # <e, r> > 0
+    loss_gpu, grad = pc.loss_grad(to_dev(R.reshape(-1), cuda), to_dev(E.reshape(-1), cuda), nrhs=B)
+    Rt = torch.tensor(R.reshape(B, Ns, 2), dtype=torch.complex64)
+    Et = torch.tensor(E.reshape(B, Ns, 2), dtype=torch.complex64)
+    L = tn.loss(Rt, Et)
+    L.backward()
+    assert abs(loss_gpu - float(L)) < 1e-5 * max(1.0, abs(float(L)))
+    gt = np.concatenate([W.grad.numpy().reshape(-1) for W in tn.Ws] + [np.array([float(tn.a.grad)])])
+    scale = np.abs(gt).max()
+    assert np.abs(grad - gt).max() / scale < 2e-3
+
+
+def test_lpc_training_lowers_loss_and_pcg_converges(cuda):
+    rng, g, lat, A, Do, Dq = _setup(16, M5=0.05, seed=11)
+    pc = Q.LearnedPreconditioner(Dq, channels=8, layers=2, seed=1)
+    pc.collect(Dq, nsrc=4, seed=7, snapshots=(0, 5, 20, 40))
+    assert pc.info()["npairs"] == 16
+    hist = pc.train(300, batch=8, lr=3e-3, seed=2)
+    assert np.all(np.isfinite(hist))
+    assert hist[-30:].mean() < hist[:30].mean() - 0.02
+    b = rand_spinor(rng, g.n_sites)
+    bt = to_dev(b, cuda)
+    x_ref, it_ref, _ = Do.cg(b, tol=1e-10)
+    for prec in (Q.PREC_F32, Q.PREC_BF16):
+        xt = torch.zeros_like(bt)
+        rep = pc.solve(Dq, xt, bt, tol=1e-10, precision=prec)
+        assert rep.status == Q.OK
+        assert rep.true_rel_res <= 1e-10
+        q = torch.zeros_like(bt)
+        Dq.apply(q, xt, Q.OP_DDAGD)
+        assert float((bt - q).norm() / bt.norm()) <= 1.05e-10
+        assert np.linalg.norm(from_dev(xt) - x_ref) / np.linalg.norm(x_ref) < 1e-7
+        assert rep.iters < it_ref
+
+
+def test_pcg_untrained_and_shifted(cuda):
+    rng, g, lat, A, Do, Dq = _setup(8, M5=0.1, seed=12)
+    pc = Q.LearnedPreconditioner(Dq, channels=4, layers=1, seed=3)
+    b = rand_spinor(rng, g.n_sites)
+    bt = to_dev(b, cuda)
+    for shift in (0.0, 0.3):
+        x_ref, _, _ = Do.cg(b, tol=1e-11, shift=shift)
+        xt = torch.zeros_like(bt)
+        rep = pc.solve(Dq, xt, bt, tol=1e-10, precision=Q.PREC_F32, shift=shift)
+        assert rep.status == Q.OK and rep.true_rel_res <= 1e-10
+        assert np.linalg.norm(from_dev(xt) - x_ref) / np.linalg.norm(x_ref) < 1e-7
+    # a zero source returns x = 0 with no iterations
+    xt = torch.ones_like(bt)
+    rep = pc.solve(Dq, xt, torch.zeros_like(bt), precision=Q.PREC_F32)
+    assert rep.status == Q.OK and rep.iters == 0
+    assert float(xt.abs().max()) == 0.0
+
+
+def test_pcg_rejects_fp64_and_other_lattice(cuda):
+    rng, g, lat, A, Do, Dq = _setup(8)
+    pc = Q.LearnedPreconditioner(Dq, channels=4, layers=1)
+    bt = to_dev(rand_spinor(rng, g.n_sites), cuda)
+    with pytest.raises(Q.Qed3Error):
+        pc.solve(Dq, torch.zeros_like(bt), bt, precision=Q.PREC_F64)
+    lat2 = Q.S2Trivalent(4)
+    D2 = Q.DiracS2Dual(lat2, 1.0, 0.1)
+    D2.update(np.zeros(O.geometry(4).n_links))
+    b2 = torch.zeros(2 * lat2.n_sites, dtype=torch.complex128, device=cuda)
+    with pytest.raises(Q.Qed3Error):
+        pc.solve(D2, torch.zeros_like(b2), b2)
