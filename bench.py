@@ -3,14 +3,22 @@
 Workload (the n=64 configuration of the benchmark spec): dual lattice n=64
 (81,920 sites, 122,880 links); links theta ~ U[-pi, pi) (seed 2) smoothed by
 50 pure-gauge HMC trajectories at beta=1.4 (compact action); Wilson r=1,
-M5=0.05; one complex Gaussian source (seed 7).  A step is one full CG solve
+M5=0.05; one complex Gaussian source (seed 7).  A step is one full solve
 of D^dag D x = b certified by the FP64 true residual <= 1e-10.  Inputs are
 synthetic (seeded), no dataset.
 
-`value` = solves/s of the fastest certified solver (device-resident b, x);
-`e2e` = the same through the public C-ABI call with b and x in pinned host
-memory (H2D of b and D2H of x inside every timed step).  L2 (129 MB) is
-flushed between timed steps since the n=64 working set fits in it.
+Before the timed region the learned preconditioner is trained on the GPU
+(the learned-preconditioner configuration of the spec): 2,000 residual/error
+pairs from the plain solver on 40 seeded configurations at beta in
+{1.0, 1.4, 2.0} (seeds 100-139, m = 0.05), then Adam steps.  The timed
+workload's configuration (seed 2) is not among them.
+
+`value` = solves/s of the learned-preconditioned mixed-precision solver
+(device-resident b, x); the plain FP64 / FP32 / BF16 CG solves are timed
+beside it (`solvers`, `speedup_vs_plain_f64`).  `e2e` = the same through the
+public C-ABI call with b and x in pinned host memory (H2D of b and D2H of x
+inside every timed step).  L2 (129 MB) is flushed between timed steps since
+the n=64 working set fits in it.
 
 --impl reference times the reference's algorithm on the host cores: the
 oracle's restatement of MatPoly::solve (src/dual/matpoly.h:204-267) over the
@@ -94,23 +102,69 @@ def make_workload(torch, dev):
     return Q, lat, A, D, b, acc
 
 
+def train_preconditioner(torch, Q, lat, D, dev, n_cfg=40, n_src=10, steps=400):
+    """Pairs from the plain solver on n_cfg seeded configurations, then Adam on the GPU."""
+    t0 = time.perf_counter()
+    pc = Q.LearnedPreconditioner(D, channels=16, layers=2, seed=1)
+    Dt = Q.DiracS2Dual(lat, 1.0, M5)
+    betas = (1.0, 1.4, 2.0)
+    for c in range(n_cfg):
+        Ac, _ = Q.thermalized_links(lat, betas[c % 3], seed=100 + c, ntraj=50, init="uniform", device=dev)
+        Dt.update(Ac)
+        pc.collect(Dt, nsrc=n_src, seed=1000 + c, snapshots=(0, 5, 20, 60, 150))
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    hist = pc.train(steps, batch=8, lr=3e-3, seed=2)
+    torch.cuda.synchronize()
+    t2 = time.perf_counter()
+    info = pc.info()
+    return pc, {"pairs": info["npairs"], "configs": n_cfg, "channels": 16, "layers": 2, "params": info["nparams"],
+                "block_sites": info["block_sites"], "adam_steps": steps, "batch": 8,
+                "loss_first50": float(np.mean(hist[:50])), "loss_last50": float(np.mean(hist[-50:])),
+                "collect_s": t1 - t0, "train_s": t2 - t1}
+
+
+def heldout_iterations(torch, Q, lat, pc, dev, n=6):
+    """Plain vs preconditioned mixed CG on configurations and sources not used in training."""
+    Dt = Q.DiracS2Dual(lat, 1.0, M5)
+    out = []
+    betas = (1.0, 1.4, 2.0)
+    for s in range(n):
+        Ac, _ = Q.thermalized_links(lat, betas[s % 3], seed=5000 + s, ntraj=50, init="uniform", device=dev)
+        Dt.update(Ac)
+        b = torch.from_numpy(Q.ParallelRng(lat, 50 + s).gaussian_spinor()).to(dev)
+        x = torch.zeros_like(b)
+        r0 = Dt.solve(x, b, tol=TOL, precision=Q.PREC_F32)
+        r1 = pc.solve(Dt, x, b, tol=TOL, precision=Q.PREC_F32)
+        out.append({"beta": betas[s % 3], "seed": 5000 + s, "cg_f32_iters": r0.iters, "pcg_f32_iters": r1.iters,
+                    "cg_f32_ms": r0.ms, "pcg_f32_ms": r1.ms,
+                    "certified": r1.status == Q.OK and r1.true_rel_res <= TOL})
+    return out
+
+
 def flush_l2(torch, buf):
     buf.add_(1.0)
 
 
-def time_solver(torch, Q, D, bt, prec, steps, warmup, flush):
+def time_solver(torch, Q, D, bt, prec, steps, warmup, flush, pc=None):
     """Per-step CUDA-event timing of device-resident solves (flush outside the events)."""
     st = torch.cuda.current_stream()
     x = torch.zeros_like(bt)
     reps = []
+
+    def solve():
+        if pc is not None:
+            return pc.solve(D, x, bt, tol=TOL, precision=prec)
+        return D.solve(x, bt, tol=TOL, precision=prec)
+
     for _ in range(warmup):
-        D.solve(x, bt, tol=TOL, precision=prec)
+        solve()
     ms = []
     for _ in range(steps):
         flush_l2(torch, flush)
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(st)
-        rep = D.solve(x, bt, tol=TOL, precision=prec)
+        rep = solve()
         e1.record(st)
         e1.synchronize()
         ms.append(e0.elapsed_time(e1))
@@ -170,7 +224,11 @@ def profile_case(torch, which):
         D.update(A)
         b = torch.from_numpy(Q.ParallelRng(lat, 7).gaussian_spinor()).cuda()
         x = torch.zeros_like(b)
-        rep = D.solve(x, b, tol=TOL, precision=Q.PREC_F32)
+        if which == "pcg":  # untrained network: same per-iteration cost as a trained one
+            pc = Q.LearnedPreconditioner(D, channels=16, layers=2, seed=1)
+            rep = pc.solve(D, x, b, tol=TOL, precision=Q.PREC_F32, maxiter=300)
+        else:
+            rep = D.solve(x, b, tol=TOL, precision=Q.PREC_F32)
         print(json.dumps(rep.__dict__))
     torch.cuda.synchronize()
 
@@ -190,9 +248,10 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--profile", choices=["apply", "cg"], default=None,
+    ap.add_argument("--profile", choices=["apply", "cg", "pcg"], default=None,
                     help="small self-contained case for ncu: 'apply' = D apply at n=512 (f32, bf16, f64; "
-                         "HBM-resident), 'cg' = one n=64 mixed-precision solve")
+                         "HBM-resident), 'cg' = one n=64 mixed-precision solve, 'pcg' = 300 iterations of the "
+                         "n=64 preconditioned solve")
     args = ap.parse_args()
     rank, world, local = env_rank()
     warmup = max(3, args.warmup)
@@ -239,19 +298,24 @@ def main():
         torch.distributed.barrier()
     torch.cuda.synchronize()
 
+    pc, train_info = train_preconditioner(torch, Q, lat, D, dev)
+    torch.cuda.synchronize()
+
     results = {}
-    for name, prec in (("f64", Q.PREC_F64), ("f32", Q.PREC_F32), ("bf16", Q.PREC_BF16)):
-        clocks = Clocks(local) if name == "f32" else None
-        if clocks:
-            clocks.start()
-        ms, reps, x = time_solver(torch, Q, D, bt, prec, args.steps, warmup, flush)
-        if clocks:
-            results["clocks"] = clocks.stop()
+    solvers = (("f64", Q.PREC_F64, None), ("f32", Q.PREC_F32, None), ("bf16", Q.PREC_BF16, None),
+               ("pcg_f32", Q.PREC_F32, pc), ("pcg_bf16", Q.PREC_BF16, pc))
+    clocks = Clocks(local)
+    clocks.start()  # sampled over every timed solver and the e2e loop
+    for name, prec, p in solvers:
+        ms, reps, x = time_solver(torch, Q, D, bt, prec, args.steps, warmup, flush, pc=p)
         ok = all(r.status == Q.OK and r.true_rel_res <= TOL for r in reps)
         results[name] = {"ms": float(np.mean(ms)), "ms_min": float(np.min(ms)), "iters": reps[-1].iters,
                          "reliable_updates": reps[-1].reliable_updates, "true_rel_res": reps[-1].true_rel_res,
                          "certified": ok}
-    best = min((k for k in ("f64", "f32", "bf16") if results[k]["certified"]), key=lambda k: results[k]["ms"])
+    cands = [k for k in ("pcg_f32", "pcg_bf16") if results[k]["certified"]]
+    if not cands:  # the learned solver is judged by plain CG's certificate; fall back to the best plain one
+        cands = [k for k in ("f64", "f32", "bf16") if results[k]["certified"]]
+    best = min(cands, key=lambda k: results[k]["ms"])
     ms_best = results[best]["ms"]
     if world > 1:
         t = torch.tensor([ms_best], device=dev)
@@ -260,7 +324,8 @@ def main():
     value = world * 1e3 / ms_best
 
     # ---- e2e through the public C-ABI call with pinned host buffers ----------------
-    prec_best = {"f64": Q.PREC_F64, "f32": Q.PREC_F32, "bf16": Q.PREC_BF16}[best]
+    prec_best = Q.PREC_BF16 if best.endswith("bf16") else (Q.PREC_F64 if best == "f64" else Q.PREC_F32)
+    use_pc = best.startswith("pcg")
     hb = torch.from_numpy(b).pin_memory()
     hx = torch.zeros_like(hb).pin_memory()
     db = torch.empty_like(bt)
@@ -272,23 +337,30 @@ def main():
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(st)
         db.copy_(hb, non_blocking=True)
-        D.solve(dx, db, tol=TOL, precision=prec_best)
+        if use_pc:
+            pc.solve(D, dx, db, tol=TOL, precision=prec_best)
+        else:
+            D.solve(dx, db, tol=TOL, precision=prec_best)
         hx.copy_(dx, non_blocking=True)
         e1.record(st)
         e1.synchronize()
         if i >= warmup:
             e2e_ms.append(e0.elapsed_time(e1))
     e2e = world * 1e3 / float(np.mean(e2e_ms))
+    clocks_info = clocks.stop()
 
-    # ---- roofline of the dominant kernel (the persistent CG kernel) ----------------
-    # algorithmic bytes per CG iteration per site: phase A reads r (gathered),
-    # t, p and 3 hop blocks + ids + diag, writes t, p; phase B reads t
-    # (gathered), p, r, x, 3 blocks + ids + diag, writes r, x
-    S = {"f64": 32, "f32": 16, "bf16": 8}[best]
-    SP = 32 if best == "f64" else 16
-    M = 64 if best == "f64" else 32
-    dg = 8 if best == "f64" else 4
-    per_site_iter = (S + S + SP + 3 * (M + 4) + dg + S + SP) + (S + SP + S + SP + 3 * (M + 4) + dg + S + SP)
+    heldout = heldout_iterations(torch, Q, lat, pc, dev)
+
+    # ---- roofline of the dominant kernel ----------------------------------------------
+    # algorithmic bytes per site per iteration (fp32 / bf16 halo storage):
+    #   D^dag D = 2 x (2 S_psi + 3 (4 + 32) + 4) with S_psi the stored spinor size,
+    #   7 spinor streams of fp32 state (x, r, p, t, z read / written) = 112,
+    #   preconditioner N: 4 block-local hop passes of 3 (32 + 16) B = 576 (PCG only)
+    S = {"f64": 32, "f32": 16, "bf16": 8, "pcg_f32": 16, "pcg_bf16": 8}[best]
+    if best == "f64":
+        per_site_iter = 2 * (2 * 32 + 3 * (4 + 64) + 8) + 7 * 32
+    else:
+        per_site_iter = 2 * (2 * S + 3 * (4 + 32) + 4) + 7 * 16 + (576 if use_pc else 0)
     iters = results[best]["iters"]
     alg_bytes = per_site_iter * lat.n_sites * iters
     achieved = alg_bytes / (results[best]["ms"] * 1e-3) / 1e9
@@ -296,26 +368,35 @@ def main():
     sweep = []
     for n, p in ((64, Q.PREC_F32), (256, Q.PREC_F32), (512, Q.PREC_F32), (512, Q.PREC_BF16), (256, Q.PREC_F64),
                  (512, Q.PREC_F64)):
-        s = apply_bandwidth(torch, Q, n, p)
-        s["frac_of_" + peak_kind] = s["GB/s"] / peak
-        s["resident"] = "L2" if s["bytes_per_site"] * 20 * n * n < 100e6 else "HBM"
-        sweep.append(s)
+        s_ = apply_bandwidth(torch, Q, n, p)
+        s_["frac_of_" + peak_kind] = s_["GB/s"] / peak
+        s_["resident"] = "L2" if s_["bytes_per_site"] * 20 * n * n < 100e6 else "HBM"
+        sweep.append(s_)
+    kernel = "k_pcg" if use_pc else ("k_cg_v2")
+    dtype = {"f64": "f64", "f32": "f32", "bf16": "f32 (bf16 halo copies)", "pcg_f32": "f32",
+             "pcg_bf16": "f32 (bf16 halo copies)"}[best]
 
     line = {"metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps,
             "warmup": warmup, "ms_per_step": ms_best, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": best, "data": "synthetic",
-            "config": {"workload": WORKLOAD, "solver": f"persistent CG, {best} inner, FP64 reliable updates",
+            "vs_baseline": None, "dtype": dtype, "data": "synthetic",
+            "config": {"workload": WORKLOAD,
+                       "solver": (f"learned-preconditioned persistent CG, {best[4:]} inner, FP64 reliable updates"
+                                  if use_pc else f"persistent CG, {best} inner, FP64 reliable updates"),
                        "l2": "flushed between timed steps (n=64 working set is L2-resident)",
                        "hmc_acceptance": acc, "parallelism": "replicas" if world > 1 else "single GPU"},
             "solvers": results,
-            "speedup_vs_plain_f64": results["f64"]["ms"] / ms_best,
+            "speedup_vs_plain_f64": results["f64"]["ms"] / results[best]["ms"],
+            "preconditioner": train_info,
+            "heldout": heldout,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                         "traffic": None, "kernel": "k_cg_persistent", "note": "n=64 is L2-resident; "
-                         f"{per_site_iter} B/site/iteration x {iters} iterations"},
+                         "traffic": None, "kernel": kernel, "note": "n=64 is L2-resident and the persistent "
+                         "solver is grid-barrier latency bound; "
+                         f"{per_site_iter} B/site/iteration x {iters} iterations; the HBM-bound Dirac apply is "
+                         "in apply_sweep"},
             "apply_sweep": sweep,
             "e2e": {"value": e2e, "unit": "solves/s", "h2d_bytes_per_step": b.nbytes, "d2h_bytes_per_step": b.nbytes},
             "gpu_launches": args.steps * 3,
-            "clocks": results.pop("clocks", None)}
+            "clocks": clocks_info}
     if rank == 0 and not args.no_cpu_baseline:
         dt, it, res, cores = cpu_reference_solve(b, A.cpu().numpy())
         line["cpu_baseline"] = {"value": 1.0 / dt, "unit": "solves/s", "cores": cores, "kind": "port",
