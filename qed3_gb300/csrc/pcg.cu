@@ -56,30 +56,58 @@ struct PcgArgs {
 
 __device__ __forceinline__ float4 sp2f4(const Sp32& v) { return make_float4(v.s0.x, v.s0.y, v.s1.x, v.s1.y); }
 __device__ __forceinline__ Sp32 f42sp(const float4& v) { return {make_float2(v.x, v.y), make_float2(v.z, v.w)}; }
-__device__ __forceinline__ float2 cm(float2 a, float2 b) { return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x); }
 
-// (Hd F)(i), (Ho F)(i) from the block's shared-memory field F (site j of the
-// block at F[j - blk0]), in-block neighbours only
-template <bool WD, bool WO>
-__device__ __forceinline__ void hop_split(const float4* __restrict__ F, const int (&jj)[3], int blk0, int per, int i,
-                                          int Ns, const M32* __restrict__ H, Sp32& hd, Sp32& ho) {
-  hd = Sp32{make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
-  ho = hd;
+// Hop blocks of the owned sites: from shared memory (HS, staged once per
+// solve, SoA Hs[(2k + row) * per + loc]) or through the read-only path.
+template <bool HS>
+__device__ __forceinline__ void ldH(const M32* __restrict__ Hg, const float4* Hs, int per, int Ns, int k, int i,
+                                    int loc, float4& r0, float4& r1) {
+  if constexpr (HS) {
+    r0 = Hs[(2 * k) * per + loc];
+    r1 = Hs[(2 * k + 1) * per + loc];
+  } else {
+    const float4* m = reinterpret_cast<const float4*>(Hg + size_t(k) * Ns + i);
+    r0 = __ldg(m);
+    r1 = __ldg(m + 1);
+  }
+}
+
+__device__ __forceinline__ float2 lo2(const float4& v) { return make_float2(v.x, v.y); }
+__device__ __forceinline__ float2 hi2(const float4& v) { return make_float2(v.z, v.w); }
+// Hd y = (h00 y0, h11 y1), Ho y = (h01 y1, h10 y0) accumulated into d / o
+__device__ __forceinline__ void acc_d(Sp32& d, const float4& r0, const float4& r1, const float4& y) {
+  d.s0 = cfmaf(lo2(r0), lo2(y), d.s0);
+  d.s1 = cfmaf(hi2(r1), hi2(y), d.s1);
+}
+__device__ __forceinline__ void acc_o(Sp32& o, const float4& r0, const float4& r1, const float4& y) {
+  o.s0 = cfmaf(hi2(r0), hi2(y), o.s0);
+  o.s1 = cfmaf(lo2(r1), lo2(y), o.s1);
+}
+
+// One pass over the in-block neighbours of owned site i (block-local index
+// loc): reads every hop block once and applies it to NF shared-memory fields;
+// MODE[f] = 1: Hd F_f -> out[f], 2: Ho F_f -> out[f], 3: both -> out[f], out[f + NF].
+template <bool HS, int NF>
+__device__ __forceinline__ void hop_pass(const float4* const (&F)[NF], const int (&mode)[NF], const int (&jj)[3],
+                                         int blk0, int per, int i, int loc, int Ns, const M32* __restrict__ Hg,
+                                         const float4* Hs, Sp32 (&out)[2 * NF]) {
+#pragma unroll
+  for (int f = 0; f < 2 * NF; f++) out[f] = Sp32{make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
 #pragma unroll
   for (int k = 0; k < 3; k++) {
     const int l = jj[k] - blk0;
     if (unsigned(l) >= unsigned(per)) continue;
-    const float4* m = reinterpret_cast<const float4*>(H + size_t(k) * Ns + i);
-    const float4 r0 = __ldg(m), r1 = __ldg(m + 1);
-    const float4 y = F[l];
-    const float2 y0 = make_float2(y.x, y.y), y1 = make_float2(y.z, y.w);
-    if (WD) {
-      hd.s0 = cfmaf(make_float2(r0.x, r0.y), y0, hd.s0);  // h00 y0
-      hd.s1 = cfmaf(make_float2(r1.z, r1.w), y1, hd.s1);  // h11 y1
-    }
-    if (WO) {
-      ho.s0 = cfmaf(make_float2(r0.z, r0.w), y1, ho.s0);  // h01 y1
-      ho.s1 = cfmaf(make_float2(r1.x, r1.y), y0, ho.s1);  // h10 y0
+    float4 r0, r1;
+    ldH<HS>(Hg, Hs, per, Ns, k, i, loc, r0, r1);
+#pragma unroll
+    for (int f = 0; f < NF; f++) {
+      const float4 y = F[f][l];
+      if (mode[f] == 1) acc_d(out[f], r0, r1, y);
+      else if (mode[f] == 2) acc_o(out[f], r0, r1, y);
+      else {
+        acc_d(out[f], r0, r1, y);
+        acc_o(out[f + NF], r0, r1, y);
+      }
     }
   }
 }
@@ -94,10 +122,13 @@ __device__ __forceinline__ Sp32 sp_add(const Sp32& a, const Sp32& b, float sb) {
 
 // z = N r for the block's sites; every thread of the block calls it (sites
 // past Ns carry zeros).  S: NW fields of `per` float4 in shared memory.
-template <int NW, int SPT>
-__device__ __forceinline__ void pc_apply(const PcgArgs& a, float4* S, int blk0, const int (&own)[SPT],
-                                         const int (&loc)[SPT], const bool (&val)[SPT], const int (&jj)[SPT][3],
-                                         const Sp32 (&r)[SPT], Sp32 (&z)[SPT]) {
+//   f = (r, Hd r, Ho r, Hd Hd r, Hd Ho r, Ho Hd r, Ho Ho r),  g = M f,
+//   z = a^2 r + g0 + Hd u + Ho v,  u = g1 + Hd g3 - Ho g5,  v = -g2 - Hd g4 + Ho g6
+// (the adjoint words, using Hd^dag = Hd and Ho^dag = -Ho): four neighbour passes.
+template <int NW, int SPT, bool HS>
+__device__ __forceinline__ void pc_apply(const PcgArgs& a, float4* S, const float4* Hs, int blk0,
+                                         const int (&own)[SPT], const int (&loc)[SPT], const bool (&val)[SPT],
+                                         const int (&jj)[SPT][3], const Sp32 (&r)[SPT], Sp32 (&z)[SPT]) {
   const int per = a.per, Ns = a.Ns;
   const Sp32 zero{make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
   float4* S0 = S;
@@ -107,32 +138,23 @@ __device__ __forceinline__ void pc_apply(const PcgArgs& a, float4* S, int blk0, 
   for (int k = 0; k < SPT; k++) S0[loc[k]] = sp2f4(val[k] ? r[k] : zero);
   __syncthreads();
   Sp32 g0[SPT], g1[SPT], g2[SPT];
-#pragma unroll
-  for (int k = 0; k < SPT; k++) {
-    Sp32 f[NW];
-    f[0] = r[k];
-    if (val[k]) hop_split<true, true>(S0, jj[k], blk0, per, own[k], Ns, a.H32, f[1], f[2]);
-    else f[1] = f[2] = zero;
-    if constexpr (NW == 7) {
-      S1[loc[k]] = sp2f4(f[1]);
-      S2[loc[k]] = sp2f4(f[2]);
-    } else {
-#pragma unroll
-      for (int w = 0; w < 3; w++) {
-        Sp32 g = zero;
-#pragma unroll
-        for (int q = 0; q < 3; q++) acc_c(g, a.pc.M[w][q], f[q]);
-        if (w == 0) g0[k] = g;
-        if (w == 1) g1[k] = g;
-        if (w == 2) g2[k] = g;
-      }
-    }
-  }
   if constexpr (NW == 7) {
     float4* S3 = S + 3 * per;
     float4* S4 = S + 4 * per;
     float4* S5 = S + 5 * per;
     float4* S6 = S + 6 * per;
+#pragma unroll
+    for (int k = 0; k < SPT; k++) {
+      Sp32 o[2];
+      o[0] = o[1] = zero;
+      if (val[k]) {
+        const float4* const F[1] = {S0};
+        const int md[1] = {3};
+        hop_pass<HS, 1>(F, md, jj[k], blk0, per, own[k], loc[k], Ns, a.H32, Hs, o);
+      }
+      S1[loc[k]] = sp2f4(o[0]);  // Hd r
+      S2[loc[k]] = sp2f4(o[1]);  // Ho r
+    }
     __syncthreads();
 #pragma unroll
     for (int k = 0; k < SPT; k++) {
@@ -140,12 +162,17 @@ __device__ __forceinline__ void pc_apply(const PcgArgs& a, float4* S, int blk0, 
       f[0] = r[k];
       f[1] = f42sp(S1[loc[k]]);
       f[2] = f42sp(S2[loc[k]]);
+      Sp32 o[4];
+      o[0] = o[1] = o[2] = o[3] = zero;
       if (val[k]) {
-        hop_split<true, true>(S1, jj[k], blk0, per, own[k], Ns, a.H32, f[3], f[5]);  // Hd Hd r, Ho Hd r
-        hop_split<true, true>(S2, jj[k], blk0, per, own[k], Ns, a.H32, f[4], f[6]);  // Hd Ho r, Ho Ho r
-      } else {
-        f[3] = f[4] = f[5] = f[6] = zero;
+        const float4* const F[2] = {S1, S2};
+        const int md[2] = {3, 3};
+        hop_pass<HS, 2>(F, md, jj[k], blk0, per, own[k], loc[k], Ns, a.H32, Hs, o);
       }
+      f[3] = o[0];  // Hd Hd r
+      f[4] = o[1];  // Hd Ho r
+      f[5] = o[2];  // Ho Hd r
+      f[6] = o[3];  // Ho Ho r
 #pragma unroll
       for (int w = 0; w < 7; w++) {
         Sp32 g = zero;
@@ -161,20 +188,17 @@ __device__ __forceinline__ void pc_apply(const PcgArgs& a, float4* S, int blk0, 
       }
     }
     __syncthreads();
-    // u = g1 + Hd g3 - Ho g5 -> S1 ; v = -g2 - Hd g4 + Ho g6 -> S2
 #pragma unroll
     for (int k = 0; k < SPT; k++) {
-      Sp32 u = g1[k], v = sp_add(zero, g2[k], -1.f);
+      Sp32 u = zero, v = zero;
       if (val[k]) {
-        Sp32 d3, o5, d4, o6, dummy;
-        hop_split<true, false>(S3, jj[k], blk0, per, own[k], Ns, a.H32, d3, dummy);
-        hop_split<false, true>(S5, jj[k], blk0, per, own[k], Ns, a.H32, dummy, o5);
-        hop_split<true, false>(S4, jj[k], blk0, per, own[k], Ns, a.H32, d4, dummy);
-        hop_split<false, true>(S6, jj[k], blk0, per, own[k], Ns, a.H32, dummy, o6);
-        u = sp_add(sp_add(u, d3, 1.f), o5, -1.f);
-        v = sp_add(sp_add(v, d4, -1.f), o6, 1.f);
-      } else {
-        u = v = zero;
+        Sp32 o[8];
+        const float4* const F[4] = {S3, S4, S5, S6};
+        const int md[4] = {1, 1, 2, 2};
+        hop_pass<HS, 4>(F, md, jj[k], blk0, per, own[k], loc[k], Ns, a.H32, Hs, o);
+        // o[0] = Hd g3, o[1] = Hd g4, o[2] = Ho g5, o[3] = Ho g6
+        u = sp_add(sp_add(g1[k], o[0], 1.f), o[2], -1.f);
+        v = sp_add(sp_add(sp_add(zero, g2[k], -1.f), o[1], -1.f), o[3], 1.f);
       }
       S1[loc[k]] = sp2f4(u);
       S2[loc[k]] = sp2f4(v);
@@ -182,38 +206,85 @@ __device__ __forceinline__ void pc_apply(const PcgArgs& a, float4* S, int blk0, 
   } else {
 #pragma unroll
     for (int k = 0; k < SPT; k++) {
+      Sp32 f[3];
+      f[0] = r[k];
+      Sp32 o[2];
+      o[0] = o[1] = zero;
+      if (val[k]) {
+        const float4* const F[1] = {S0};
+        const int md[1] = {3};
+        hop_pass<HS, 1>(F, md, jj[k], blk0, per, own[k], loc[k], Ns, a.H32, Hs, o);
+      }
+      f[1] = o[0];
+      f[2] = o[1];
+#pragma unroll
+      for (int w = 0; w < 3; w++) {
+        Sp32 g = zero;
+#pragma unroll
+        for (int q = 0; q < 3; q++) acc_c(g, a.pc.M[w][q], f[q]);
+        if (w == 0) g0[k] = g;
+        if (w == 1) g1[k] = g;
+        if (w == 2) g2[k] = g;
+      }
       S1[loc[k]] = sp2f4(val[k] ? g1[k] : zero);
       S2[loc[k]] = sp2f4(val[k] ? sp_add(zero, g2[k], -1.f) : zero);
     }
   }
   __syncthreads();
-  // z = a^2 r + g0 + Hd u + Ho v
 #pragma unroll
   for (int k = 0; k < SPT; k++) {
     if (!val[k]) {
       z[k] = zero;
       continue;
     }
-    Sp32 du, ov, dummy;
-    hop_split<true, false>(S1, jj[k], blk0, per, own[k], Ns, a.H32, du, dummy);
-    hop_split<false, true>(S2, jj[k], blk0, per, own[k], Ns, a.H32, dummy, ov);
-    Sp32 o = sp_add(g0[k], r[k], a.pc.a2);
-    o = sp_add(sp_add(o, du, 1.f), ov, 1.f);
-    z[k] = o;
+    Sp32 o[4];
+    const float4* const F[2] = {S1, S2};
+    const int md[2] = {1, 2};
+    hop_pass<HS, 2>(F, md, jj[k], blk0, per, own[k], loc[k], Ns, a.H32, Hs, o);
+    Sp32 zz = sp_add(g0[k], r[k], a.pc.a2);
+    zz = sp_add(sp_add(zz, o[0], 1.f), o[1], 1.f);
+    z[k] = zz;
   }
+}
+
+// own-site stencil o = diag * self + sum_k H_k halo[nbr_k], hop blocks from
+// shared memory (HS) or the read-only path
+template <int P, bool HS>
+__device__ __forceinline__ Sp32 stencil32h(int i, int loc, int per, int Ns, const int (&jj)[3],
+                                           const M32* __restrict__ Hg, const float4* Hs, float dg, const Sp32& self,
+                                           const void* halo) {
+  Sp32 o{make_float2(dg * self.s0.x, dg * self.s0.y), make_float2(dg * self.s1.x, dg * self.s1.y)};
+  const Sp32 b0 = hl32<P>(halo, jj[0]), b1 = hl32<P>(halo, jj[1]), b2 = hl32<P>(halo, jj[2]);
+  const Sp32 bs[3] = {b0, b1, b2};
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    float4 r0, r1;
+    ldH<HS>(Hg, Hs, per, Ns, k, i, loc, r0, r1);
+    o.s0 = cfmaf(lo2(r0), bs[k].s0, o.s0);
+    o.s0 = cfmaf(hi2(r0), bs[k].s1, o.s0);
+    o.s1 = cfmaf(lo2(r1), bs[k].s0, o.s1);
+    o.s1 = cfmaf(hi2(r1), bs[k].s1, o.s1);
+  }
+  return o;
 }
 
 __device__ __forceinline__ float rdotf(const Sp32& a, const Sp32& b) {  // Re <a, b>
   return a.s0.x * b.s0.x + a.s0.y * b.s0.y + a.s1.x * b.s1.x + a.s1.y * b.s1.y;
 }
 
+// Dynamic shared memory: NW fields of `per` float4 for the preconditioner,
+// then (HS) the owned sites' hop blocks of D and D^dag, 6 x per float4 each.
 template <int P, int NW, int SPT>
 __global__ void __launch_bounds__(576, 1) k_pcg(PcgArgs a) {
+  constexpr bool HS = (SPT == 1);
   extern __shared__ float4 S[];
   __shared__ double sh[32 * 4 + 64 + 8];
   const int Ns = a.Ns;
   const int T = blockDim.x;
   const int blk0 = blockIdx.x * a.per;
+  float4* HsD = S + NW * a.per;       // hop blocks of D (own sites)
+  float4* HsDd = HsD + 6 * a.per;     // hop blocks of D^dag
+  float dg[SPT];
 
   int own[SPT], loc[SPT];
   bool val[SPT];
@@ -239,7 +310,19 @@ __global__ void __launch_bounds__(576, 1) k_pcg(PcgArgs a) {
     r[k] = z32;
 #pragma unroll
     for (int q = 0; q < 3; q++) jj[k][q] = 0;
+    dg[k] = 0.f;
+    if constexpr (HS) {
+#pragma unroll
+      for (int q = 0; q < 6; q++) {
+        const float4 zf = make_float4(0.f, 0.f, 0.f, 0.f);
+        const float4* mh = reinterpret_cast<const float4*>(a.H32 + size_t(q >> 1) * Ns + i) + (q & 1);
+        const float4* md = reinterpret_cast<const float4*>(a.Hd32 + size_t(q >> 1) * Ns + i) + (q & 1);
+        HsD[q * a.per + loc[k]] = val[k] ? __ldg(mh) : zf;
+        HsDd[q * a.per + loc[k]] = val[k] ? __ldg(md) : zf;
+      }
+    }
     if (val[k]) {
+      dg[k] = __ldg(a.diag32 + i);
 #pragma unroll
       for (int q = 0; q < 3; q++) jj[k][q] = __ldg(a.nbr + q * Ns + i);
       const Sp64 bi = ld64(a.b, i);
@@ -247,7 +330,7 @@ __global__ void __launch_bounds__(576, 1) k_pcg(PcgArgs a) {
       r[k] = Sp32{make_float2(float(bi.s0.x), float(bi.s0.y)), make_float2(float(bi.s1.x), float(bi.s1.y))};
     }
   }
-  pc_apply<NW, SPT>(a, S, blk0, own, loc, val, jj, r, z);
+  pc_apply<NW, SPT, HS>(a, S, HsD, blk0, own, loc, val, jj, r, z);
 #pragma unroll
   for (int k = 0; k < SPT; k++) {
     if (!val[k]) continue;
@@ -283,7 +366,7 @@ __global__ void __launch_bounds__(576, 1) k_pcg(PcgArgs a) {
         for (int k = 0; k < SPT; k++) {
           if (!val[k]) continue;
           const int i = own[k];
-          const Sp32 dz = stencil32<P>(i, Ns, jj[k], a.H32, a.diag32, z[k], a.halo_z);
+          const Sp32 dz = stencil32h<P, HS>(i, loc[k], a.per, Ns, jj[k], a.H32, HsD, dg[k], z[k], a.halo_z);
           t[k].s0 = cfmaf(az, dz.s0, make_float2(bt * t[k].s0.x, bt * t[k].s0.y));
           t[k].s1 = cfmaf(az, dz.s1, make_float2(bt * t[k].s1.x, bt * t[k].s1.y));
           p[k].s0 = cfmaf(az, z[k].s0, make_float2(bt * p[k].s0.x, bt * p[k].s0.y));
@@ -305,13 +388,13 @@ __global__ void __launch_bounds__(576, 1) k_pcg(PcgArgs a) {
 #pragma unroll
         for (int k = 0; k < SPT; k++) {
           if (!val[k]) continue;
-          const Sp32 q = stencil32<P>(own[k], Ns, jj[k], a.Hd32, a.diag32, t[k], a.halo_t);
+          const Sp32 q = stencil32h<P, HS>(own[k], loc[k], a.per, Ns, jj[k], a.Hd32, HsDd, dg[k], t[k], a.halo_t);
           r[k].s0 = make_float2(r[k].s0.x - al * (q.s0.x + sf * p[k].s0.x), r[k].s0.y - al * (q.s0.y + sf * p[k].s0.y));
           r[k].s1 = make_float2(r[k].s1.x - al * (q.s1.x + sf * p[k].s1.x), r[k].s1.y - al * (q.s1.y + sf * p[k].s1.y));
           xl[k].s0 = make_float2(xl[k].s0.x + al * p[k].s0.x, xl[k].s0.y + al * p[k].s0.y);
           xl[k].s1 = make_float2(xl[k].s1.x + al * p[k].s1.x, xl[k].s1.y + al * p[k].s1.y);
         }
-        pc_apply<NW, SPT>(a, S, blk0, own, loc, val, jj, r, z);
+        pc_apply<NW, SPT, HS>(a, S, HsD, blk0, own, loc, val, jj, r, z);
 #pragma unroll
         for (int k = 0; k < SPT; k++) {
           if (!val[k]) continue;
@@ -374,7 +457,7 @@ __global__ void __launch_bounds__(576, 1) k_pcg(PcgArgs a) {
           v[3] += rt.s0.x * pv0.y - rt.s0.y * pv0.x + rt.s1.x * pv1.y - rt.s1.y * pv1.x;
           r[k] = Sp32{make_float2(float(rt.s0.x), float(rt.s0.y)), make_float2(float(rt.s1.x), float(rt.s1.y))};
         }
-        pc_apply<NW, SPT>(a, S, blk0, own, loc, val, jj, r, z);
+        pc_apply<NW, SPT, HS>(a, S, HsD, blk0, own, loc, val, jj, r, z);
 #pragma unroll
         for (int k = 0; k < SPT; k++) {
           if (!val[k]) continue;
@@ -454,7 +537,7 @@ bool pcg_plan(int prec, int nw, int Ns, int per, int sm_count, int* grid, int* t
     const int T = per / s;
     if (T > 576) continue;
     const void* fn = pcg_kernel(prec, nw, s);
-    const size_t sm = size_t(nw) * per * sizeof(float4);
+    const size_t sm = size_t(nw + (s == 1 ? 12 : 0)) * per * sizeof(float4);
     if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(sm)) != cudaSuccess) {
       cudaGetLastError();
       continue;
