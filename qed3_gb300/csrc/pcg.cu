@@ -359,7 +359,7 @@ __global__ void __launch_bounds__(576, 1) k_pcg(PcgArgs a) {
     while (true) {
       // ---- phase A: t = a_z D z + beta t, p = a_z z + beta p ----------------------------
       {
-        double v[1] = {0.0};
+        float v[1] = {0.f};
         const float2 az = make_float2(float(a_z.x), float(a_z.y));
         const float bt = float(beta);
 #pragma unroll
@@ -372,9 +372,9 @@ __global__ void __launch_bounds__(576, 1) k_pcg(PcgArgs a) {
           p[k].s0 = cfmaf(az, z[k].s0, make_float2(bt * p[k].s0.x, bt * p[k].s0.y));
           p[k].s1 = cfmaf(az, z[k].s1, make_float2(bt * p[k].s1.x, bt * p[k].s1.y));
           hs32<P>(a.halo_t, i, t[k]);
-          v[0] += double(n2f(t[k])) + s * double(n2f(p[k]));
+          v[0] += n2f(t[k]) + float(s) * n2f(p[k]);
         }
-        v2_publish<1>(v, a.partials, parity, sh);
+        v2_publish_f<1>(v, a.partials, parity, sh);
         if (!grid_sync2(a.bar, epoch, a.spin_limit)) goto timeout;
       }
       double gam[1];
@@ -383,7 +383,7 @@ __global__ void __launch_bounds__(576, 1) k_pcg(PcgArgs a) {
       const double alpha = rho / gam[0];
       // ---- phase B: q = D^dag t + s p, x += alpha p, r -= alpha q, z = N r -------------
       {
-        double v[2] = {0.0, 0.0};
+        float v[2] = {0.f, 0.f};
         const float al = float(alpha), sf = float(s);
 #pragma unroll
         for (int k = 0; k < SPT; k++) {
@@ -399,10 +399,10 @@ __global__ void __launch_bounds__(576, 1) k_pcg(PcgArgs a) {
         for (int k = 0; k < SPT; k++) {
           if (!val[k]) continue;
           hs32<P>(a.halo_z, own[k], z[k]);
-          v[0] += double(n2f(r[k]));
-          v[1] += double(rdotf(r[k], z[k]));
+          v[0] += n2f(r[k]);
+          v[1] += rdotf(r[k], z[k]);
         }
-        v2_publish<2>(v, a.partials, parity, sh);
+        v2_publish_f<2>(v, a.partials, parity, sh);
         if (!grid_sync2(a.bar, epoch, a.spin_limit)) goto timeout;
       }
       double mun[2];

@@ -101,6 +101,7 @@ __global__ void __launch_bounds__(640, 1) k_cg_v2(CgV2Args a) {
       // ---- phase A: t = a_r D r + beta t, p = a_r r + beta p -------------------------
       {
         double v[1] = {0.0};
+        float vf[1] = {0.f};
 #pragma unroll
         for (int k = 0; k < SPT; k++) {
           if (!val[k]) continue;
@@ -114,7 +115,7 @@ __global__ void __launch_bounds__(640, 1) k_cg_v2(CgV2Args a) {
             p[k].s0 = cfmaf(ar, r[k].s0, make_float2(bt * p[k].s0.x, bt * p[k].s0.y));
             p[k].s1 = cfmaf(ar, r[k].s1, make_float2(bt * p[k].s1.x, bt * p[k].s1.y));
             hs32<P>(a.halo_t, i, t[k]);
-            v[0] += double(n2f(t[k])) + s * double(n2f(p[k]));
+            vf[0] += n2f(t[k]) + float(s) * n2f(p[k]);
           } else {
             const Sp64 dr = stencil64(i, Ns, jj[k], a.H, a.diag, r[k], reinterpret_cast<const S64*>(a.halo_r));
             t[k].s0 = cfma(a_r, dr.s0, cscale(beta, t[k].s0));
@@ -125,7 +126,8 @@ __global__ void __launch_bounds__(640, 1) k_cg_v2(CgV2Args a) {
             v[0] += n2(t[k]) + s * n2(p[k]);
           }
         }
-        v2_publish<1>(v, a.partials, parity, sh);
+        if constexpr (mixed) v2_publish_f<1>(vf, a.partials, parity, sh);
+        else v2_publish<1>(v, a.partials, parity, sh);
         if (!grid_sync2(a.bar, epoch, a.spin_limit)) goto timeout;
       }
       double gam[1];
@@ -135,6 +137,7 @@ __global__ void __launch_bounds__(640, 1) k_cg_v2(CgV2Args a) {
       // ---- phase B: q = D^dag t + s p, x += alpha p, r -= alpha q --------------------
       {
         double v[1] = {0.0};
+        float vf[1] = {0.f};
 #pragma unroll
         for (int k = 0; k < SPT; k++) {
           if (!val[k]) continue;
@@ -147,7 +150,7 @@ __global__ void __launch_bounds__(640, 1) k_cg_v2(CgV2Args a) {
             xl[k].s0 = make_float2(xl[k].s0.x + al * p[k].s0.x, xl[k].s0.y + al * p[k].s0.y);
             xl[k].s1 = make_float2(xl[k].s1.x + al * p[k].s1.x, xl[k].s1.y + al * p[k].s1.y);
             hs32<P>(a.halo_r, i, r[k]);
-            v[0] += double(n2f(r[k]));
+            vf[0] += n2f(r[k]);
           } else {
             const Sp64 q = stencil64(i, Ns, jj[k], a.Hd, a.diag, t[k], reinterpret_cast<const S64*>(a.halo_t));
             r[k].s0 = csub(r[k].s0, cscale(alpha, cadd(q.s0, cscale(s, p[k].s0))));
@@ -158,7 +161,8 @@ __global__ void __launch_bounds__(640, 1) k_cg_v2(CgV2Args a) {
             v[0] += n2(r[k]);
           }
         }
-        v2_publish<1>(v, a.partials, parity, sh);
+        if constexpr (mixed) v2_publish_f<1>(vf, a.partials, parity, sh);
+        else v2_publish<1>(v, a.partials, parity, sh);
         if (!grid_sync2(a.bar, epoch, a.spin_limit)) goto timeout;
       }
       double mun[1];

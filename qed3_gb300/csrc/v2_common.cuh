@@ -17,17 +17,29 @@ __device__ __forceinline__ void v2_publish(double (&v)[NV], double* part, int pa
     for (int q = 0; q < NV; q++) __stcg(part + (size_t(parity) * gridDim.x + blockIdx.x) * 4 + q, v[q]);
 }
 
+// Global totals: lane l of warp 0 loads the partials of blocks l, l+32, ...
+// all at once (one L2 round trip instead of one per block stride), then FP64
+// sums in a fixed order (deterministic), broadcast through shared memory.
 template <int NV>
 __device__ __forceinline__ void v2_total(const double* part, int parity, double (&out)[NV], double* sh) {
   if (threadIdx.x < 32) {
+    const int G = gridDim.x;
+    const double* base = part + size_t(parity) * G * 4;
     double acc[NV];
 #pragma unroll
     for (int q = 0; q < NV; q++) acc[q] = 0.0;
-    for (int bI = threadIdx.x; bI < gridDim.x; bI += 32)
+    // fixed trip count: the loads of all strides are independent and issue together
 #pragma unroll
-      for (int q = 0; q < NV; q++) acc[q] += __ldcg(part + (size_t(parity) * gridDim.x + bI) * 4 + q);
+    for (int c = 0; c < 5; c++) {
+      const int bI = threadIdx.x + 32 * c;
 #pragma unroll
-    for (int q = 0; q < NV; q++) acc[q] = warp_sum(acc[q]);
+      for (int q = 0; q < NV; q++) acc[q] += bI < G ? __ldcg(base + size_t(bI) * 4 + q) : 0.0;
+    }
+#pragma unroll
+    for (int q = 0; q < NV; q++) {
+      for (int bI = threadIdx.x + 160; bI < G; bI += 32) acc[q] += __ldcg(base + size_t(bI) * 4 + q);
+      acc[q] = warp_sum(acc[q]);
+    }
     if (threadIdx.x == 0)
 #pragma unroll
       for (int q = 0; q < NV; q++) sh[64 + q] = acc[q];
@@ -36,6 +48,37 @@ __device__ __forceinline__ void v2_total(const double* part, int parity, double 
 #pragma unroll
   for (int q = 0; q < NV; q++) out[q] = sh[64 + q];
   __syncthreads();
+}
+
+__device__ __forceinline__ float warp_sum_f(float v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// Block partial of NV fp32 values (the inner iteration's |t|^2, |r|^2, <r,z>):
+// fp32 warp and cross-warp sums, one conversion, the FP64 partial stored for
+// the global FP64 accumulation in v2_total.  FP64 arithmetic stays off the
+// per-thread path: on GB300 a dependent DADD costs ~2.5x an FADD, a 64-bit
+// shuffle ~2x, and an f32<->f64 conversion ~4x.
+template <int NV>
+__device__ __forceinline__ void v2_publish_f(float (&v)[NV], double* part, int parity, double* sh) {
+  float* shf = reinterpret_cast<float*>(sh);  // 32*NV floats, below the totals' slots
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+#pragma unroll
+  for (int q = 0; q < NV; q++) v[q] = warp_sum_f(v[q]);
+  if (lane == 0)
+#pragma unroll
+    for (int q = 0; q < NV; q++) shf[q * 32 + warp] = v[q];
+  __syncthreads();
+  if (warp == 0) {
+#pragma unroll
+    for (int q = 0; q < NV; q++) {
+      float t = lane < nw ? shf[q * 32 + lane] : 0.f;
+      t = warp_sum_f(t);
+      if (lane == 0) __stcg(part + (size_t(parity) * gridDim.x + blockIdx.x) * 4 + q, double(t));
+    }
+  }
 }
 
 // halo access (L2, bypassing L1: written by other SMs in the previous phase)
