@@ -50,6 +50,7 @@ struct PcgArgs {
   double* scal;
   double tol2, delta2, shift;
   int maxiter;
+  int flexible;  // Polak-Ribiere beta
   long long spin_limit;
   LpcWordCoef pc;
 };
@@ -273,7 +274,8 @@ __device__ __forceinline__ float rdotf(const Sp32& a, const Sp32& b) {  // Re <a
 }
 
 // Dynamic shared memory: NW fields of `per` float4 for the preconditioner,
-// then (HS) the owned sites' hop blocks of D and D^dag, 6 x per float4 each.
+// one for q (flexible mode), then (HS) the owned sites' hop blocks of D and
+// D^dag, 6 x per float4 each.
 template <int P, int NW, int SPT>
 __global__ void __launch_bounds__(576, 1) k_pcg(PcgArgs a) {
   constexpr bool HS = (SPT == 1);
@@ -282,7 +284,8 @@ __global__ void __launch_bounds__(576, 1) k_pcg(PcgArgs a) {
   const int Ns = a.Ns;
   const int T = blockDim.x;
   const int blk0 = blockIdx.x * a.per;
-  float4* HsD = S + NW * a.per;       // hop blocks of D (own sites)
+  float4* Sq = S + NW * a.per;        // q of the owned sites (flexible mode)
+  float4* HsD = Sq + a.per;           // hop blocks of D (own sites)
   float4* HsDd = HsD + 6 * a.per;     // hop blocks of D^dag
   float dg[SPT];
 
@@ -383,16 +386,16 @@ __global__ void __launch_bounds__(576, 1) k_pcg(PcgArgs a) {
       const double alpha = rho / gam[0];
       // ---- phase B: q = D^dag t + s p, x += alpha p, r -= alpha q, z = N r -------------
       {
-        float v[2] = {0.f, 0.f};
+        float v[3] = {0.f, 0.f, 0.f};
         const float al = float(alpha), sf = float(s);
 #pragma unroll
         for (int k = 0; k < SPT; k++) {
           if (!val[k]) continue;
           const Sp32 q = stencil32h<P, HS>(own[k], loc[k], a.per, Ns, jj[k], a.Hd32, HsDd, dg[k], t[k], a.halo_t);
-          r[k].s0 = make_float2(r[k].s0.x - al * (q.s0.x + sf * p[k].s0.x), r[k].s0.y - al * (q.s0.y + sf * p[k].s0.y));
-          r[k].s1 = make_float2(r[k].s1.x - al * (q.s1.x + sf * p[k].s1.x), r[k].s1.y - al * (q.s1.y + sf * p[k].s1.y));
-          xl[k].s0 = make_float2(xl[k].s0.x + al * p[k].s0.x, xl[k].s0.y + al * p[k].s0.y);
-          xl[k].s1 = make_float2(xl[k].s1.x + al * p[k].s1.x, xl[k].s1.y + al * p[k].s1.y);
+          const Sp32 qf = sp_add(q, p[k], sf);
+          if (a.flexible) Sq[loc[k]] = sp2f4(qf);  // kept for <z', q> after the preconditioner
+          r[k] = sp_add(r[k], qf, -al);
+          xl[k] = sp_add(xl[k], p[k], al);
         }
         pc_apply<NW, SPT, HS>(a, S, HsD, blk0, own, loc, val, jj, r, z);
 #pragma unroll
@@ -401,12 +404,23 @@ __global__ void __launch_bounds__(576, 1) k_pcg(PcgArgs a) {
           hs32<P>(a.halo_z, own[k], z[k]);
           v[0] += n2f(r[k]);
           v[1] += rdotf(r[k], z[k]);
+          if (a.flexible) v[2] += rdotf(z[k], f42sp(Sq[loc[k]]));
         }
-        v2_publish_f<2>(v, a.partials, parity, sh);
+        if (a.flexible) v2_publish_f<3>(v, a.partials, parity, sh);
+        else {
+          float v2r[2] = {v[0], v[1]};
+          v2_publish_f<2>(v2r, a.partials, parity, sh);
+        }
         if (!grid_sync2(a.bar, epoch, a.spin_limit)) goto timeout;
       }
-      double mun[2];
-      v2_total<2>(a.partials, parity, mun, sh);
+      double mun[3] = {0.0, 0.0, 0.0};
+      if (a.flexible) v2_total<3>(a.partials, parity, mun, sh);
+      else {
+        double m2[2];
+        v2_total<2>(a.partials, parity, m2, sh);
+        mun[0] = m2[0];
+        mun[1] = m2[1];
+      }
       parity ^= 1;
       iter++;
       const double mu_new = mun[0], rho_new = mun[1];
@@ -414,7 +428,8 @@ __global__ void __launch_bounds__(576, 1) k_pcg(PcgArgs a) {
       const bool want = !isfinite(mu_new) || !isfinite(alpha) || !(rho_new > 0.0) || mu_new < a.tol2 * bnorm2 ||
                         iter >= a.maxiter || mu_new < a.delta2 * mu_max;
       if (!want) {
-        beta = rho_new / rho;
+        // flexible: <z', r' - r> = -alpha <z', q>
+        beta = a.flexible ? -alpha * mun[2] / rho : rho_new / rho;
         a_z = make_double2(1.0, 0.0);
         rho = rho_new;
         mu = mu_new;
@@ -537,7 +552,7 @@ bool pcg_plan(int prec, int nw, int Ns, int per, int sm_count, int* grid, int* t
     const int T = per / s;
     if (T > 576) continue;
     const void* fn = pcg_kernel(prec, nw, s);
-    const size_t sm = size_t(nw + (s == 1 ? 12 : 0)) * per * sizeof(float4);
+    const size_t sm = size_t(nw + 1 + (s == 1 ? 12 : 0)) * per * sizeof(float4);
     if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(sm)) != cudaSuccess) {
       cudaGetLastError();
       continue;
@@ -602,6 +617,7 @@ int pcg_solve(qed3_dirac_s* d, qed3_lpc_s* L, double* x, const double* b, const 
   a.delta2 = delta * delta;
   a.shift = shift;
   a.maxiter = maxiter;
+  a.flexible = (prm && (prm->flags & QED3_SOLVE_FLEXIBLE)) ? 1 : 0;
   a.spin_limit = 4000000LL;
   a.pc = co;
   void* kargs[] = {&a};

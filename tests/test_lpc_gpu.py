@@ -194,9 +194,10 @@ def test_lpc_training_lowers_loss_and_pcg_converges(cuda):
     b = rand_spinor(rng, g.n_sites)
     bt = to_dev(b, cuda)
     x_ref, it_ref, _ = Do.cg(b, tol=1e-10)
-    for prec in (Q.PREC_F32, Q.PREC_BF16):
+    iters = {}
+    for prec, flexible in ((Q.PREC_F32, False), (Q.PREC_BF16, False), (Q.PREC_F32, True)):
         xt = torch.zeros_like(bt)
-        rep = pc.solve(Dq, xt, bt, tol=1e-10, precision=prec)
+        rep = pc.solve(Dq, xt, bt, tol=1e-10, precision=prec, flexible=flexible)
         assert rep.status == Q.OK
         assert rep.true_rel_res <= 1e-10
         q = torch.zeros_like(bt)
@@ -204,6 +205,9 @@ def test_lpc_training_lowers_loss_and_pcg_converges(cuda):
         assert float((bt - q).norm() / bt.norm()) <= 1.05e-10
         assert np.linalg.norm(from_dev(xt) - x_ref) / np.linalg.norm(x_ref) < 1e-7
         assert rep.iters < it_ref
+        iters[(prec, flexible)] = rep.iters
+    # Polak-Ribiere and Fletcher-Reeves beta agree in exact arithmetic
+    assert abs(iters[(Q.PREC_F32, True)] - iters[(Q.PREC_F32, False)]) <= max(3, iters[(Q.PREC_F32, False)] // 10)
 
 
 def test_pcg_untrained_and_shifted(cuda):
