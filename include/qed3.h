@@ -274,6 +274,11 @@ int qed3_lpc_collect(qed3_lpc* pc, qed3_dirac* d, int nsrc, unsigned seed, const
 /* steps of Adam (learning rate lr), each on `batch` pairs of one operator drawn
  * at random; loss_history: host [steps] or NULL. */
 int qed3_lpc_train(qed3_lpc* pc, int steps, int batch, double lr, unsigned seed, double* loss_history);
+/* Channel mixing of the 16 -> 16 layers on the tensor cores (tcgen05, BF16
+ * operands, FP32 accumulation; default on for 16 channels and 2 layers) or in
+ * FP32 on the CUDA cores (enable = 0).  QED3_ERR_ARG if the network has no
+ * 16 -> 16 layer. */
+int qed3_lpc_set_tensor_cores(qed3_lpc* pc, int enable);
 /* Preconditioned CG on D^dag D + shift with N applied block-locally inside the
  * persistent kernel.  Same arguments, certificate and report as qed3_cg_solve;
  * precision QED3_PREC_F32 or QED3_PREC_BF16 (halo copies), FP64 reliable

@@ -113,6 +113,7 @@ SIGNATURES = [
     ("qed3_lpc_loss_grad", ctypes.c_int, [vp, vp, vp, ctypes.c_int, c_double_p, vp, vp]),
     ("qed3_lpc_collect", ctypes.c_int, [vp, vp, ctypes.c_int, ctypes.c_uint, vp, ctypes.c_int, ctypes.c_int]),
     ("qed3_lpc_train", ctypes.c_int, [vp, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_uint, vp]),
+    ("qed3_lpc_set_tensor_cores", ctypes.c_int, [vp, ctypes.c_int]),
     ("qed3_pcg_solve", ctypes.c_int, [vp, vp, vp, vp, ctypes.POINTER(SolveParams), ctypes.POINTER(SolveReport),
                                       vp]),
 ]
@@ -473,6 +474,10 @@ class LearnedPreconditioner:
         h = vp()
         _check(lib().qed3_lpc_create(dirac.handle, channels, layers, seed, ctypes.byref(h)))
         self._h = h
+
+    def set_tensor_cores(self, enable: bool):
+        """16 -> 16 channel mixing on the tensor cores (BF16 operands, FP32 accumulate) or FP32 CUDA cores."""
+        _check(lib().qed3_lpc_set_tensor_cores(self._h, 1 if enable else 0))
 
     def info(self) -> dict:
         a, b, c = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()

@@ -561,6 +561,11 @@ int qed3_lpc_train(qed3_lpc* pc, int steps, int batch, double lr, unsigned seed,
   QED3_GUARD_END
 }
 
+int qed3_lpc_set_tensor_cores(qed3_lpc* pc, int enable) {
+  if (!pc) return fail(QED3_ERR_ARG, "NULL preconditioner");
+  return lpc_set_tensor_cores(pc, enable);
+}
+
 int qed3_pcg_solve(qed3_dirac* d, qed3_lpc* pc, double* x, const double* b, const qed3_solve_params* params,
                    qed3_solve_report* report, void* stream) {
   QED3_GUARD_BEGIN

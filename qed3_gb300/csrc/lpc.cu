@@ -2,7 +2,9 @@
 // backward and Adam kernels) and the collapsed form used by the solver.
 //
 // No counterpart in the reference.  Fields are complex fp32, layout
-// [B][Ns][C][2 spins] in the solver's internal (space-filling-curve) order.
+// [B][Ns][2 spins][C] in the solver's internal (space-filling-curve) order:
+// a (sample, site, spin) row holds its C channels contiguously, the row of
+// the channel-mixing GEMMs.
 // The block mask (hops only between sites of the same `per`-sized block)
 // matches the persistent solver's per-SM ownership, so the preconditioner it
 // learns is applied there with block-local communication only.
@@ -43,18 +45,18 @@ __global__ void k_lpc_hops(int B, int Ns, int C, int per, const int* __restrict_
     const int j = __ldg(nbr + k * Ns + i);
     if (j / per != blk) continue;
     const M32 m = H[k * Ns + i];
-    const float2* hj = h + ((size_t(b) * Ns + j) * C + c) * 2;
-    const float2 y0 = hj[0], y1 = hj[1];
+    const float2* hj = h + (size_t(b) * Ns + j) * 2 * C + c;
+    const float2 y0 = hj[0], y1 = hj[C];
     a0 = caf(a0, cmf(make_float2(m.r0.x, m.r0.y), y0));  // h00 y0
     a1 = caf(a1, cmf(make_float2(m.r1.z, m.r1.w), y1));  // h11 y1
     o0 = caf(o0, cmf(make_float2(m.r0.z, m.r0.w), y1));  // h01 y1
     o1 = caf(o1, cmf(make_float2(m.r1.x, m.r1.y), y0));  // h10 y0
   }
-  const size_t o = size_t(idx) * 2;
+  const size_t o = size_t(bi) * 2 * C + c;
   fa[o] = a0;
-  fa[o + 1] = a1;
+  fa[o + C] = a1;
   fb[o] = o0;
-  fb[o + 1] = o1;
+  fb[o + C] = o1;
 }
 
 // ---- channel mixing of one layer (fp32 SIMT reference form) -------------------
@@ -70,7 +72,7 @@ __global__ void k_lpc_mix(int B, int Ns, int Cin, int Cout, int adj, const float
   const long long bi = idx / Co;
   float2 s0 = make_float2(0.f, 0.f), s1 = s0;
   for (int ci = 0; ci < Ci; ci++) {
-    const size_t f = (size_t(bi) * Ci + ci) * 2;
+    const size_t f = size_t(bi) * 2 * Ci + ci;  // spin 0; spin 1 at f + Ci
     float2 w0, w1, w2;
     if (!adj) {
       w0 = W[(0 * Cout + co) * Cin + ci];
@@ -83,10 +85,10 @@ __global__ void k_lpc_mix(int B, int Ns, int Cin, int Cout, int adj, const float
       w2 = make_float2(-t.x, -t.y);
     }
     s0 = caf(s0, caf(cmf(w0, h[f]), caf(cmf(w1, fa[f]), cmf(w2, fb[f]))));
-    s1 = caf(s1, caf(cmf(w0, h[f + 1]), caf(cmf(w1, fa[f + 1]), cmf(w2, fb[f + 1]))));
+    s1 = caf(s1, caf(cmf(w0, h[f + Ci]), caf(cmf(w1, fa[f + Ci]), cmf(w2, fb[f + Ci]))));
   }
-  out[size_t(idx) * 2] = s0;
-  out[size_t(idx) * 2 + 1] = s1;
+  out[size_t(bi) * 2 * Co + co] = s0;
+  out[size_t(bi) * 2 * Co + Co + co] = s1;
 }
 
 // ---- weight gradient of one layer: partial sums over row chunks --------------
@@ -107,8 +109,8 @@ __global__ void k_lpc_wgrad(int rows, int Cin, int Cout, int adj, const float2* 
   double ax = 0.0, ay = 0.0;
   for (long long r = r0; r < r1; r++) {
     for (int s = 0; s < 2; s++) {
-      const float2 g = G[(size_t(r) * Cg + cg) * 2 + s];
-      const float2 x = f[(size_t(r) * Cf + cf) * 2 + s];
+      const float2 g = G[(size_t(r) * 2 + s) * Cg + cg];
+      const float2 x = f[(size_t(r) * 2 + s) * Cf + cf];
       if (!adj) {  // g conj(x)
         ax += double(g.x) * x.x + double(g.y) * x.y;
         ay += double(g.y) * x.x - double(g.x) * x.y;
@@ -230,6 +232,7 @@ void lpc_destroy(qed3_lpc_s* L) {
     if (p) cudaFree(p);
   for (M32* p : L->cfg_H) cudaFree(p);
   for (M32* p : L->cfg_Hd) cudaFree(p);
+  L->tc.release();
   delete L;
 }
 
@@ -267,13 +270,34 @@ int lpc_create(qed3_dirac_s* d, int channels, int layers, int per, unsigned seed
   QED3_CUDA_TRY(cudaMemcpy(L->W, w.data(), L->nparam * sizeof(float2), cudaMemcpyHostToDevice));
   QED3_CUDA_TRY(cudaMemset(L->m, 0, L->nparam * sizeof(float2)));
   QED3_CUDA_TRY(cudaMemset(L->v, 0, L->nparam * sizeof(float2)));
+  int dev = 0;
+  QED3_CUDA_TRY(cudaGetDevice(&dev));
+  QED3_CUDA_TRY(cudaDeviceGetAttribute(&L->sms, cudaDevAttrMultiProcessorCount, dev));
+  L->use_tc = (channels == 16 && layers == 2);
   *out = L;
   return QED3_OK;
 }
 
+int lpc_set_tensor_cores(qed3_lpc_s* L, int enable) {
+  bool any = false;
+  for (int l = 0; l < L->LG; l++) any = any || (L->cin[l] == 16 && L->cout[l] == 16);
+  if (enable && !any) return fail(QED3_ERR_ARG, "tensor-core mixing needs a 16 -> 16 channel layer");
+  L->use_tc = enable != 0;
+  return QED3_OK;
+}
+
+static bool tc_layer(const qed3_lpc_s* L, int l) { return L->use_tc && L->cin[l] == 16 && L->cout[l] == 16; }
+
 // one layer (or its adjoint) on an input field of c_in_field channels
 static int layer_apply(qed3_lpc_s* L, const M32* H, int B, int l, int adj, const float2* in, float2* out,
                        cudaStream_t st) {
+  if (tc_layer(L, l)) {
+    const long long rows = (long long)B * L->Ns * 2;
+    int rc = L->tc.ensure((long long)L->bmax * L->Ns * 2, L->sms);
+    if (!rc) rc = tc_hops(L->tc, L->d, H, L->per, B, in, st);
+    if (!rc) rc = tc_mix(L->tc, rows, L->W + L->woff[l], adj, reinterpret_cast<float*>(out), st);
+    return rc;
+  }
   const DeviceLattice& D = L->d->lat->dev;
   const int Cin = L->cin[l], Cout = L->cout[l];
   const int Cf = adj ? Cout : Cin;  // channels of the input field
@@ -288,6 +312,13 @@ static int layer_apply(qed3_lpc_s* L, const M32* H, int B, int l, int adj, const
 // weight gradient of layer l given the gradient of its output and its input
 static int layer_wgrad(qed3_lpc_s* L, const M32* H, int B, int l, int adj, const float2* Gout, const float2* in,
                        cudaStream_t st) {
+  if (tc_layer(L, l)) {
+    const long long rows = (long long)B * L->Ns * 2;
+    int rc = L->tc.ensure((long long)L->bmax * L->Ns * 2, L->sms);
+    if (!rc) rc = tc_hops(L->tc, L->d, H, L->per, B, in, st);
+    if (!rc) rc = tc_wgrad(L->tc, rows, reinterpret_cast<const float*>(Gout), adj, L->G + L->woff[l], st);
+    return rc;
+  }
   const DeviceLattice& D = L->d->lat->dev;
   const int Cin = L->cin[l], Cout = L->cout[l];
   const int Cf = adj ? Cout : Cin;
@@ -327,7 +358,9 @@ static int forward_H(qed3_lpc_s* L, const M32* H, int B, const float2* r, float2
 }
 
 int lpc_forward(qed3_lpc_s* L, int B, const float2* r, float2* z, cudaStream_t st) {
-  return forward_H(L, L->d->H32, B, r, z, st);
+  const int rc = forward_H(L, L->d->H32, B, r, z, st);
+  if (rc || !L->use_tc) return rc;
+  return tc_check(L->tc, st);
 }
 
 // loss and parameter gradient (accumulated into L->G after zeroing) for pairs
@@ -416,7 +449,9 @@ static int loss_grad_H(qed3_lpc_s* L, qed3_dirac_s* d, const M32* H, const M32* 
 }
 
 int lpc_loss_grad(qed3_lpc_s* L, int B, const float2* r, const float2* e, double* loss, cudaStream_t st) {
-  return loss_grad_H(L, L->d, L->d->H32, L->d->Hd32, B, r, e, loss, st);
+  const int rc = loss_grad_H(L, L->d, L->d->H32, L->d->Hd32, B, r, e, loss, st);
+  if (rc || !L->use_tc) return rc;
+  return tc_check(L->tc, st);
 }
 
 int lpc_adam(qed3_lpc_s* L, double lr, cudaStream_t st) {
@@ -789,6 +824,7 @@ int lpc_train(qed3_lpc_s* L, int steps, int batch, double lr, unsigned seed, dou
     if (history) history[it] = loss;
   }
   cudaFree(didx);
+  if (!rc && L->use_tc) rc = tc_check(L->tc, 0);
   return rc;
 }
 

@@ -16,6 +16,7 @@
 #include <vector>
 
 #include "handles.h"
+#include "tc_impl.h"
 
 namespace qed3 {
 constexpr int kLpcMaxWords = 7;  // hop words of length <= 2 over {Hd, Ho} (incl. identity)
@@ -55,6 +56,10 @@ struct qed3_lpc_s {
   // collapsed form, cached until the weights change
   bool coef_valid = false;
   qed3::LpcWordCoef coef{};
+  // 16 -> 16 layers on the tensor cores (bf16 operands, fp32 accumulation)
+  bool use_tc = false;
+  int sms = 0;
+  qed3::TcWork tc;
 };
 
 namespace qed3 {
@@ -70,4 +75,5 @@ int lpc_set_weights(qed3_lpc_s* L, const double* w);
 int lpc_apply_words(qed3_lpc_s* L, int B, const float2* r, float2* z, cudaStream_t st);
 int lpc_collect(qed3_lpc_s* L, qed3_dirac_s* d, int nsrc, unsigned seed, const int* snaps, int nsnap, int prec);
 int lpc_train(qed3_lpc_s* L, int steps, int batch, double lr, unsigned seed, double* history);
+int lpc_set_tensor_cores(qed3_lpc_s* L, int enable);
 }  // namespace qed3

@@ -134,6 +134,8 @@ def _crel(a, b):
 @pytest.mark.parametrize("C,LG", [(8, 1), (8, 2), (16, 2)])
 def test_lpc_forward_matches_torch(cuda, C, LG):
     rng, g, lat, Do, Dq, pc, tn = _net(8, C, LG)
+    if C == 16:
+        pc.set_tensor_cores(False)  # FP32 CUDA-core mixing; the tensor-core path is checked below
     Ns = g.n_sites
     B = 3
     r = rand_spinor(rng, Ns, B)
@@ -168,6 +170,8 @@ def test_lpc_hermitian_positive(cuda):
 @pytest.mark.parametrize("LG", [1, 2])
 def test_lpc_gradient_matches_autograd(cuda, LG):
     rng, g, lat, Do, Dq, pc, tn = _net(8, 8, LG)
+    with pytest.raises(Q.Qed3Error):
+        pc.set_tensor_cores(True)  # no 16 -> 16 layer
     Ns = g.n_sites
     B = 4
     R = rand_spinor(rng, Ns, B)
@@ -240,3 +244,46 @@ def test_pcg_rejects_fp64_and_other_lattice(cuda):
     b2 = torch.zeros(2 * lat2.n_sites, dtype=torch.complex128, device=cuda)
     with pytest.raises(Q.Qed3Error):
         pc.solve(D2, torch.zeros_like(b2), b2)
+
+
+@pytest.mark.parametrize("n,B", [(8, 2), (6, 3)])
+def test_lpc_tensor_cores_match_fp32(cuda, n, B):
+    """tcgen05 BF16 channel mixing (forward, adjoint, weight gradients) against
+    the FP32 CUDA-core kernels, including a partial last 128-row tile (n=6, B=3)."""
+    rng, g, lat, Do, Dq, pc, tn = _net(n, 16, 2)
+    Ns = g.n_sites
+    R = rand_spinor(rng, Ns, B)
+    E = rand_spinor(rng, Ns, B) + 0.5 * R
+    Rt, Et = to_dev(R.reshape(-1), cuda), to_dev(E.reshape(-1), cuda)
+    out = {}
+    for tc in (False, True):
+        pc.set_tensor_cores(tc)
+        z = torch.zeros_like(Rt)
+        pc.apply(z, Rt, nrhs=B)
+        loss, grad = pc.loss_grad(Rt, Et, nrhs=B)
+        out[tc] = (from_dev(z), loss, grad)
+    z32, l32, g32 = out[False]
+    ztc, ltc, gtc = out[True]
+    assert _crel(ztc, z32) < 2e-2
+    assert abs(ltc - l32) < 2e-2 * max(1e-3, abs(l32))
+    # the 16 -> 16 layer's weights (the tensor-core GEMM's output) and the rest
+    assert np.abs(gtc - g32).max() / np.abs(g32).max() < 5e-2
+    # layer-2 block (3 x 16 x 16) compared on its own scale
+    s2 = slice(3 * 16, 3 * 16 + 3 * 256)
+    assert np.abs(gtc[s2] - g32[s2]).max() / np.abs(g32[s2]).max() < 5e-2
+
+
+def test_lpc_tensor_core_training_n16(cuda):
+    rng, g, lat, A, Do, Dq = _setup(16, M5=0.05, seed=11)
+    pc = Q.LearnedPreconditioner(Dq, channels=16, layers=2, seed=1)  # tensor cores on by default
+    pc.collect(Dq, nsrc=4, seed=7, snapshots=(0, 5, 20, 40))
+    hist = pc.train(300, batch=8, lr=3e-3, seed=2)
+    assert np.all(np.isfinite(hist))
+    assert hist[-30:].mean() < hist[:30].mean() - 0.02
+    b = rand_spinor(rng, g.n_sites)
+    bt = to_dev(b, cuda)
+    _, it_ref, _ = Do.cg(b, tol=1e-10)
+    xt = torch.zeros_like(bt)
+    rep = pc.solve(Dq, xt, bt, tol=1e-10, precision=Q.PREC_F32)
+    assert rep.status == Q.OK and rep.true_rel_res <= 1e-10
+    assert rep.iters < it_ref
