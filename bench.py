@@ -102,7 +102,7 @@ def make_workload(torch, dev):
     return Q, lat, A, D, b, acc
 
 
-def train_preconditioner(torch, Q, lat, D, dev, n_cfg=40, n_src=10, steps=400):
+def train_preconditioner(torch, Q, lat, D, dev, n_cfg=40, n_src=10, steps=1500):
     """Pairs from the plain solver on n_cfg seeded configurations, then Adam on the GPU."""
     t0 = time.perf_counter()
     pc = Q.LearnedPreconditioner(D, channels=16, layers=2, seed=1)

@@ -247,7 +247,7 @@ int qed3_zolotarev(double k, int n, double* c, double* cp, double* A, double* sc
  * backward and Adam kernels) on residual / error pairs taken from the
  * solver's own iterates, loss 1 - |<z,r>|^2 / (<z,A z> <e,r>) with A = D^dag D.
  * ====================================================================== */
-/* channels in [1, 64], layers in [1, 2]; the block partition is the one of the
+/* channels in [1, 64], layers in [1, 3] (the solver takes 1 or 2); the block partition is the one of the
  * register-resident solvers on the current device. */
 int qed3_lpc_create(qed3_dirac* d, int channels, int layers, unsigned seed, qed3_lpc** out);
 int qed3_lpc_destroy(qed3_lpc* pc);

@@ -123,15 +123,72 @@ __global__ void k_lpc_wgrad(int rows, int Cin, int Cout, int adj, const float2* 
   part[size_t(blockIdx.y) * nent + e] = make_double2(sg * ax, sg * ay);
 }
 
+// Weight gradient of a layer with one 1-channel side (the 1 -> 16 layer and
+// its adjoint): thread (rr, c) of a 16 x 16 block walks rows rr, rr+16, ... of
+// the block's chunk for wide channel c; the 16 row lanes are summed in shared
+// memory.  Entry e = 16 j + c.
+// adj = 0: dW_j[c] += sum G[c] conj(f_j)      (G wide, f narrow)
+// adj = 1: dW_j[c] += s_j sum conj(G) f_j[c]  (G narrow, f wide; s = +, +, -)
+__global__ void __launch_bounds__(256) k_lpc_wgrad_narrow(long long rows, int adj, const float2* __restrict__ G,
+                                                          const float2* __restrict__ h,
+                                                          const float2* __restrict__ fa,
+                                                          const float2* __restrict__ fb, int chunk,
+                                                          double2* __restrict__ part) {
+  __shared__ float2 sh[16][48];
+  const int c = threadIdx.x & 15, rr = threadIdx.x >> 4;
+  const float2* f[3] = {h, fa, fb};
+  float2 acc[3] = {make_float2(0.f, 0.f), make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
+  const long long r0 = (long long)blockIdx.x * chunk, r1 = min(rows, r0 + chunk);
+  for (long long r = r0 + rr; r < r1; r += 16) {
+    if (!adj) {
+      const float2 g = G[r * 16 + c];
+#pragma unroll
+      for (int j = 0; j < 3; j++) {
+        const float2 x = f[j][r];  // g conj(x)
+        acc[j].x += g.x * x.x + g.y * x.y;
+        acc[j].y += g.y * x.x - g.x * x.y;
+      }
+    } else {
+      const float2 g = G[r];
+#pragma unroll
+      for (int j = 0; j < 3; j++) {
+        const float2 x = f[j][r * 16 + c];  // conj(g) x
+        acc[j].x += g.x * x.x + g.y * x.y;
+        acc[j].y += g.x * x.y - g.y * x.x;
+      }
+    }
+  }
+#pragma unroll
+  for (int j = 0; j < 3; j++) sh[rr][16 * j + c] = acc[j];
+  __syncthreads();
+  if (threadIdx.x < 48) {
+    const int e = threadIdx.x, j = e >> 4;
+    double x = 0, y = 0;
+    for (int q = 0; q < 16; q++) {
+      x += sh[q][e].x;
+      y += sh[q][e].y;
+    }
+    const double sg = (adj && j == 2) ? -1.0 : 1.0;
+    part[size_t(blockIdx.x) * 48 + e] = make_double2(sg * x, sg * y);
+  }
+}
+
+// G[e] += sum over chunks of the FP64 partials: one warp per entry, lanes
+// stride over the chunks (fixed order, deterministic)
 __global__ void k_lpc_wgrad_sum(int nent, int nchunks, const double2* __restrict__ part, float2* __restrict__ G) {
-  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  const int e = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), lane = threadIdx.x & 31;
   if (e >= nent) return;
   double x = 0, y = 0;
-  for (int k = 0; k < nchunks; k++) {
+  for (int k = lane; k < nchunks; k += 32) {
     x += part[size_t(k) * nent + e].x;
     y += part[size_t(k) * nent + e].y;
   }
-  G[e] = make_float2(G[e].x + float(x), G[e].y + float(y));
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    x += __shfl_xor_sync(0xffffffffu, x, o);
+    y += __shfl_xor_sync(0xffffffffu, y, o);
+  }
+  if (lane == 0) G[e] = make_float2(G[e].x + float(x), G[e].y + float(y));
 }
 
 // z = a^2 r + g
@@ -237,7 +294,7 @@ void lpc_destroy(qed3_lpc_s* L) {
 }
 
 int lpc_create(qed3_dirac_s* d, int channels, int layers, int per, unsigned seed, qed3_lpc_s** out) {
-  if (channels < 1 || channels > 64 || layers < 1 || layers > 2) return fail(QED3_ERR_ARG, "lpc: channels 1..64, layers 1..2");
+  if (channels < 1 || channels > 64 || layers < 1 || layers > 3) return fail(QED3_ERR_ARG, "lpc: channels 1..64, layers 1..3");
   auto* L = new qed3_lpc_s;
   L->d = d;
   L->C = channels;
@@ -323,6 +380,16 @@ static int layer_wgrad(qed3_lpc_s* L, const M32* H, int B, int l, int adj, const
   const int Cin = L->cin[l], Cout = L->cout[l];
   const int Cf = adj ? Cout : Cin;
   k_lpc_hops<<<nblk((long long)B * L->Ns * Cf), 256, 0, st>>>(B, L->Ns, Cf, L->per, D.nbr, H, in, L->fa, L->fb);
+  if (Cin == 1 && Cout == 16) {
+    const long long rows2 = (long long)B * L->Ns * 2;  // (sample, site, spin) rows
+    const int chunk = int(std::max<long long>(512, (rows2 + 1023) / 1024));
+    const int nch = int((rows2 + chunk - 1) / chunk);
+    k_lpc_wgrad_narrow<<<nch, 256, 0, st>>>(rows2, adj, Gout, in, L->fa, L->fb, chunk,
+                                              reinterpret_cast<double2*>(L->part));
+    k_lpc_wgrad_sum<<<nblk(48 * 32), 256, 0, st>>>(48, nch, reinterpret_cast<double2*>(L->part), L->G + L->woff[l]);
+    QED3_CUDA_TRY(cudaGetLastError());
+    return QED3_OK;
+  }
   const int rows = B * L->Ns;
   const int nent = 3 * Cin * Cout;
   const int nchunks = std::max(1, std::min(65536 / (2 * nent), rows / 256 + 1));
@@ -330,7 +397,8 @@ static int layer_wgrad(qed3_lpc_s* L, const M32* H, int B, int l, int adj, const
   dim3 grid(nblk(nent, 128), nchunks);
   k_lpc_wgrad<<<grid, 128, 0, st>>>(rows, Cin, Cout, adj, Gout, in, L->fa, L->fb, chunk,
                                     reinterpret_cast<double2*>(L->part));
-  k_lpc_wgrad_sum<<<nblk(nent), 256, 0, st>>>(nent, nchunks, reinterpret_cast<double2*>(L->part), L->G + L->woff[l]);
+  k_lpc_wgrad_sum<<<nblk((long long)nent * 32), 256, 0, st>>>(nent, nchunks, reinterpret_cast<double2*>(L->part),
+                                                              L->G + L->woff[l]);
   QED3_CUDA_TRY(cudaGetLastError());
   return QED3_OK;
 }
@@ -470,6 +538,7 @@ int lpc_adam(qed3_lpc_s* L, double lr, cudaStream_t st) {
 // HoHo for LG = 2), word (a b) meaning O_a O_b (O_b applied first).
 // N r = a^2 r + sum_{w w'} M_{w w'} O_w^dag O_w' r with M = K^dag K.
 int lpc_word_coef(const qed3_lpc_s* L, LpcWordCoef* out) {
+  if (L->LG > 2) return fail(QED3_ERR_ARG, "the collapsed (solver) form covers networks of 1 or 2 layers");
   std::vector<float2> w(L->nparam);
   QED3_CUDA_TRY(cudaMemcpy(w.data(), L->W, L->nparam * sizeof(float2), cudaMemcpyDeviceToHost));
   using cd = std::complex<double>;

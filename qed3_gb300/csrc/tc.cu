@@ -399,20 +399,29 @@ __global__ void __launch_bounds__(128) k_tc_wgrad(TcWgArgs a) {
 // forward layer: dW_j[co][c] = sum G[co] conj(f_j[c]);
 // adjoint layer: dW_j[c][c'] = s_j sum conj(G[c']) f_j[c],  s = (+, +, -).
 __global__ void k_tc_wgrad_fin(int nparts, const float* __restrict__ part, int adj, float2* __restrict__ Gw) {
-  const int e = blockIdx.x * blockDim.x + threadIdx.x;  // j * 256 + a * 16 + b  (weight [j][a][b])
+  // one warp per weight entry e = j * 256 + a * 16 + b (weight [j][a][b]); lanes stride over the partials
+  const int e = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), lane = threadIdx.x & 31;
   if (e >= 3 * 256) return;
   const int j = e >> 8, ia = (e >> 4) & 15, ib = e & 15;
   // forward: a = co (G index), b = c (feature index); adjoint: a = c (feature), b = c' (G index)
   const int fc = adj ? ia : ib, gc = adj ? ib : ia;
   const int mr = 32 * j + 2 * fc, mi = mr + 1, nr = 2 * gc, ni = nr + 1;
   double rr = 0, ii = 0, ri = 0, ir = 0;  // P[m_x][n_y] sums
-  for (int k = 0; k < nparts; k++) {
+  for (int k = lane; k < nparts; k += 32) {
     const float* p = part + size_t(k) * 96 * 32;
     rr += p[mr * 32 + nr];
     ii += p[mi * 32 + ni];
     ri += p[mr * 32 + ni];
     ir += p[mi * 32 + nr];
   }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    rr += __shfl_xor_sync(0xffffffffu, rr, o);
+    ii += __shfl_xor_sync(0xffffffffu, ii, o);
+    ri += __shfl_xor_sync(0xffffffffu, ri, o);
+    ir += __shfl_xor_sync(0xffffffffu, ir, o);
+  }
+  if (lane) return;
   double re = rr + ii, im;
   if (!adj) {
     im = ri - ir;  // Gi fr - Gr fi
@@ -504,7 +513,7 @@ int TcWork::ensure(long long rows_needed, int sm_count) {
   QED3_CUDA_TRY(cudaMalloc(&Xh, n * sizeof(__nv_bfloat16)));
   QED3_CUDA_TRY(cudaMalloc(&Xa, n * sizeof(__nv_bfloat16)));
   QED3_CUDA_TRY(cudaMalloc(&Xb, n * sizeof(__nv_bfloat16)));
-  nparts = sm_count;
+  nparts = 4 * sm_count;  // 4 CTAs per SM (41 KB of shared memory each) hide the staging loads
   QED3_CUDA_TRY(cudaMalloc(&part, size_t(nparts) * 96 * 32 * sizeof(float)));
   QED3_CUDA_TRY(cudaMalloc(&err, sizeof(int)));
   QED3_CUDA_TRY(cudaMemset(err, 0, sizeof(int)));
@@ -576,7 +585,7 @@ int tc_wgrad(TcWork& w, long long rows, const float* G, int adj, float2* Gw, cud
   a.err = w.err;
   a.spin = 2000000LL;
   k_tc_wgrad<<<w.nparts, 128, kWgSmem, st>>>(a);
-  k_tc_wgrad_fin<<<3, 256, 0, st>>>(w.nparts, w.part, adj, Gw);
+  k_tc_wgrad_fin<<<3 * 256 / 8, 256, 0, st>>>(w.nparts, w.part, adj, Gw);
   QED3_CUDA_TRY(cudaGetLastError());
   return QED3_OK;
 }

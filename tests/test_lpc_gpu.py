@@ -167,11 +167,14 @@ def test_lpc_hermitian_positive(cuda):
     assert np.vdot(u, Nu).real >= a2 * np.vdot(u, u).real * (1 - 1e-5)
 
 
-@pytest.mark.parametrize("LG", [1, 2])
-def test_lpc_gradient_matches_autograd(cuda, LG):
-    rng, g, lat, Do, Dq, pc, tn = _net(8, 8, LG)
-    with pytest.raises(Q.Qed3Error):
-        pc.set_tensor_cores(True)  # no 16 -> 16 layer
+@pytest.mark.parametrize("C,LG", [(8, 1), (8, 2), (16, 1), (16, 2)])
+def test_lpc_gradient_matches_autograd(cuda, C, LG):
+    rng, g, lat, Do, Dq, pc, tn = _net(8, C, LG)
+    if LG == 1:
+        with pytest.raises(Q.Qed3Error):
+            pc.set_tensor_cores(True)  # no 16 -> 16 layer
+    else:
+        pc.set_tensor_cores(False)  # FP32 kernels against autograd
     Ns = g.n_sites
     B = 4
     R = rand_spinor(rng, Ns, B)
