@@ -202,6 +202,13 @@ int qed3_rng_destroy(qed3_rng* r);
  * (ParallelRngExt::fill_gaussian, src/both_3d/rng.h:122-129) */
 int qed3_rng_gaussian_links(qed3_rng* r, double width, double* links);
 int qed3_rng_gaussian_spinor(qed3_rng* r, double* spinor);
+/* FermionVector::set_random (src/dual/valence.h:54-60): host spinor[2*n_sites]
+ * complex = (z + i z')/sqrt(2 n_sites) with z, z' = z2_site(x), which the
+ * reference draws from uniform_int_distribution(1, 2). */
+int qed3_rng_z2_spinor(qed3_rng* r, double* spinor);
+/* FermionVector::set_pt_source (src/dual/valence.h:47-52): host spinor[2*n_sites]
+ * complex = unit vector at (site x, spin s), reference order. */
+int qed3_point_source(int n_sites, int x, int s, double* spinor);
 int qed3_hmc_pure_gauge(qed3_lattice* lat, qed3_rng* rng, double* A, double beta, int compact, int exact,
                         double tmax, int nsteps, int no_reject, int* accepted, double* dH, void* stream);
 
@@ -218,13 +225,32 @@ int qed3_overlap_destroy(qed3_overlap* ov);
  * <= 0 to estimate them with the reference's power / inverse power iterations
  * (inner CG tolerance tol_outer). */
 int qed3_overlap_update(qed3_overlap* ov, double lambda_min, double lambda_max, double tol_outer, void* stream);
+/* npoles_fp64: leading (smallest-shift) poles whose condition number is too
+ * large for mixed-precision inner iterations; they run in a second, FP64,
+ * batched launch (0 when the overlap was created with QED3_PREC_F64). */
 int qed3_overlap_info(const qed3_overlap* ov, double* lambda_min, double* lambda_max, double* k, double* delta,
-                      int* npoles);
+                      int* npoles, int* npoles_fp64);
 /* mult / adj / DHD / DDH_deviceAsyncLaunch (:309-390): op = QED3_OP_D (D_ov),
  * QED3_OP_DDAG (D_ov^dag), QED3_OP_DDAGD or QED3_OP_DDDAG (D_ov + D_ov^dag,
  * which equals D_ov^dag D_ov for the exact overlap).  tol_inner: pole solves'
  * relative residual.  report: the worst pole (iterations, true residual). */
 int qed3_overlap_apply(qed3_overlap* ov, int op, double* out, const double* in, double tol_inner,
+                       qed3_solve_report* report, void* stream);
+
+/* Overlap pseudofermion force for all links at once -- replaces
+ * Overlap::precalc_grad_deviceAsyncLaunch + grad_deviceAsyncLaunch
+ * (src/both_3d/overlap.h:393-470, one sparse product and dot per pole and
+ * link): F[l] = -2 d/dA_l Re<eta, D_ov eta>.  eta: device complex128,
+ * reference order; F: device [n_links].  report: the worse of the two batched
+ * pole launches. */
+int qed3_overlap_force(qed3_overlap* ov, const double* eta, double* F, double tol_inner, qed3_solve_report* report,
+                       void* stream);
+/* Outer CG on D_ov^dag D_ov (Overlap::DHD) x = b, as MatPoly::solve over the
+ * DHD wrapper (src/both_3d/prop_nontriv.cu:242-260); device complex128 x, b.
+ * report: outer iterations, true_rel_res = ||b - D_ov^dag D_ov x||/||b||
+ * recomputed after convergence, reliable_updates = the largest inner pole
+ * iteration count. */
+int qed3_overlap_solve(qed3_overlap* ov, double* x, const double* b, double tol, double tol_inner, int maxiter,
                        qed3_solve_report* report, void* stream);
 
 /* ======================================================================

@@ -943,6 +943,7 @@ struct SingleRng {
   std::mt19937_64 mt;
   std::normal_distribution<double> g;
   std::uniform_real_distribution<double> u;
+  std::uniform_int_distribution<int> z2{1, 2};  // SingleRng::dist_z2(1,2), src/both/rng.h
 };
 struct OracleRng {
   SingleRng master;
@@ -974,6 +975,20 @@ void orc_rng_gaussian_spinor(OracleRng* r, double* out) {
     }
 }
 double orc_rng_uniform(OracleRng* r) { return r->master.u(r->master.mt); }
+// FermionVector::set_random, src/dual/valence.h:54-60: (z2 + i z2)/sqrt(2 Ns) per
+// entry from the site engine; z2_site draws uniform_int_distribution(1, 2),
+// so the entries are 1 or 2 (over the normalisation) as the reference writes them.
+void orc_rng_z2_spinor(OracleRng* r, double* out) {
+  const double nrm = std::sqrt(2.0 * double(r->sites.size()));
+  for (size_t x = 0; x < r->sites.size(); x++)
+    for (int a = 0; a < 2; a++) {
+      auto& e = r->sites[x];
+      const double re = e.z2(e.mt);
+      const double im = e.z2(e.mt);
+      out[4 * x + 2 * a] = re / nrm;
+      out[4 * x + 2 * a + 1] = im / nrm;
+    }
+}
 
 // HMCPureGauge::run, src/both_3d/hmc.h:212-296: leapfrog (half kick, drift,
 // half kick) nsteps times over tmax; Metropolis with the master uniform.
@@ -1099,6 +1114,84 @@ int orc_overlap_apply(const OracleDirac* d, double lmin, double lmax, int order,
   }
   for (Idx i = 0; i < N; i++)
     out[i] = (op == 0) ? res_mult[i] : (op == 1) ? res_adj[i] : res_mult[i] + res_adj[i];
+  return total_it;
+}
+
+// Overlap pseudofermion force per link, restating Overlap::precalc_grad /
+// grad_deviceAsyncLaunch (src/both_3d/overlap.h:393-470):
+//   Y0 = X^dag eta, Z_m = (X^dag X + s_m)^{-1} eta, Y_m = (X^dag X + s_m)^{-1} Y0,
+//   F_l = -2C/lmax [ sum_m A_m (-Re<X Z_m, dD Y_m> - Re<X Y_m, dD Z_m>)
+//                    + Re<eta, dD (eta + sum_m A_m Z_m)> ]
+// with dD/dA_l = i H_xy at (x,y) and -i H_yx at (y,x) (d_coo_format,
+// src/both_3d/dirac_ext.h:234-269).  F_l = -2 d/dA_l Re<eta, D_ov eta>.
+// Returns the total inner CG iterations.
+int orc_overlap_force(const OracleDirac* d, const OracleGeom* g, const double* A, double lmin, double lmax,
+                      int order, const double* eta_in, double* F, double tol_inner) {
+  const Idx N = d->N;
+  const cplx* eta = reinterpret_cast<const cplx*>(eta_in);
+  const double k = lmin / lmax;
+  const int size = order / 2 + 1;
+  std::vector<double> c(size), cp(size), Am(size), sc(4);
+  orc_zolotarev(k, order, c.data(), cp.data(), Am.data(), sc.data());
+  const double C = sc[3];
+  int total_it = 0;
+  std::vector<cplx> y0(N);
+  csr_mult(d, true, y0.data(), eta);
+  for (Idx i = 0; i < N; i++) y0[i] /= lmax;
+  std::vector<std::vector<cplx>> Z(size), Y(size), XZ(size), XY(size);
+  std::vector<cplx> w(eta, eta + N);
+  for (int m = 1; m < size; m++) {
+    const double sigma = -k * k / cp[m];
+    Z[m].resize(N);
+    Y[m].resize(N);
+    XZ[m].resize(N);
+    XY[m].resize(N);
+    total_it += orc_cg(d, lmax * lmax * sigma, reinterpret_cast<double*>(Z[m].data()),
+                       reinterpret_cast<const double*>(eta), tol_inner, 1000000, nullptr);
+    total_it += orc_cg(d, lmax * lmax * sigma, reinterpret_cast<double*>(Y[m].data()),
+                       reinterpret_cast<const double*>(y0.data()), tol_inner, 1000000, nullptr);
+    for (Idx i = 0; i < N; i++) {  // the reference's operator is (X^dag X + s_m): scale by lmax^2
+      Z[m][i] *= lmax * lmax;
+      Y[m][i] *= lmax * lmax;
+    }
+    csr_mult(d, false, XZ[m].data(), Z[m].data());
+    csr_mult(d, false, XY[m].data(), Y[m].data());
+    for (Idx i = 0; i < N; i++) {
+      XZ[m][i] /= lmax;
+      XY[m][i] /= lmax;
+      w[i] += Am[m] * Z[m][i];
+    }
+  }
+  const cplx I(0.0, 1.0);
+  const Idx Nl = Idx(g->links.size());
+#pragma omp parallel for schedule(static)
+  for (Idx l = 0; l < Nl; l++) {
+    const Idx x = g->links[l][0], y = g->links[l][1];
+    int kx = 0, ky = 0;
+    while (g->nns[x][kx] != y) kx++;
+    while (g->nns[y][ky] != x) ky++;
+    cplx Hxy[4], Hyx[4];
+    hop_matrix(g, d, x, kx, A[l], Hxy);
+    hop_matrix(g, d, y, ky, -A[l], Hyx);
+    // <u, dD v> restricted to the two blocks of link l
+    auto inner = [&](const cplx* u, const cplx* v) {
+      const cplx dx0 = I * (Hxy[0] * v[2 * y] + Hxy[1] * v[2 * y + 1]);
+      const cplx dx1 = I * (Hxy[2] * v[2 * y] + Hxy[3] * v[2 * y + 1]);
+      const cplx dy0 = -I * (Hyx[0] * v[2 * x] + Hyx[1] * v[2 * x + 1]);
+      const cplx dy1 = -I * (Hyx[2] * v[2 * x] + Hyx[3] * v[2 * x + 1]);
+      return std::conj(u[2 * x]) * dx0 + std::conj(u[2 * x + 1]) * dx1 + std::conj(u[2 * y]) * dy0 +
+             std::conj(u[2 * y + 1]) * dy1;
+    };
+    double res = 0.0;
+    for (int m = 1; m < size; m++) {
+      double t = 0.0;
+      t -= inner(XZ[m].data(), Y[m].data()).real();
+      t -= inner(XY[m].data(), Z[m].data()).real();
+      res += Am[m] * t;
+    }
+    res += inner(eta, w.data()).real();
+    F[l] = -2.0 * C / lmax * res;
+  }
   return total_it;
 }
 

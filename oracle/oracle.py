@@ -69,6 +69,7 @@ def lib():
         L.orc_rng_destroy.argtypes = [vp]
         L.orc_rng_gaussian_links.argtypes = [vp, ctypes.c_double, c_double_p]
         L.orc_rng_gaussian_spinor.argtypes = [vp, ctypes.c_void_p]
+        L.orc_rng_z2_spinor.argtypes = [vp, ctypes.c_void_p]
         L.orc_rng_uniform.restype = ctypes.c_double
         L.orc_rng_uniform.argtypes = [vp]
         L.orc_hmc_pure_gauge.restype = ctypes.c_int
@@ -76,6 +77,9 @@ def lib():
                                          ctypes.c_double, ctypes.c_int, ctypes.c_int, c_double_p]
         L.orc_fermion_force.argtypes = [vp, vp, c_double_p, ctypes.c_void_p, c_double_p]
         L.orc_num_threads.restype = ctypes.c_int
+        L.orc_overlap_force.restype = ctypes.c_int
+        L.orc_overlap_force.argtypes = [vp, vp, vp, ctypes.c_double, ctypes.c_double, ctypes.c_int, vp, vp,
+                                        ctypes.c_double]
         L.orc_overlap_apply.restype = ctypes.c_int
         L.orc_overlap_apply.argtypes = [vp, ctypes.c_double, ctypes.c_double, ctypes.c_int, ctypes.c_int,
                                         ctypes.c_void_p, ctypes.c_void_p, ctypes.c_double]
@@ -225,6 +229,15 @@ class Dirac:
         lib().orc_overlap_apply(self.h, lmin, lmax, order, op, _p(out), _p(v), tol_inner)
         return out
 
+    def overlap_force(self, A: np.ndarray, eta: np.ndarray, lmin: float, lmax: float, order: int = 21,
+                      tol_inner: float = 1e-12) -> np.ndarray:
+        """Overlap::precalc_grad + grad_deviceAsyncLaunch restated: F_l = -2 d/dA_l Re<eta, D_ov eta>."""
+        A = np.ascontiguousarray(A, dtype=np.float64)
+        eta = np.ascontiguousarray(eta, dtype=np.complex128)
+        F = np.zeros(self.geom.n_links)
+        lib().orc_overlap_force(self.h, self.geom.handle, _dp(A), lmin, lmax, order, _p(eta), _dp(F), tol_inner)
+        return F
+
     def lambda_bounds(self, TOL: float = 1e-8, maxiter: int = 500, tol_outer: float = 1e-10):
         """Overlap::compute_lambda_max restated: (lambda_min, lambda_max) of D."""
         a, b = ctypes.c_double(), ctypes.c_double()
@@ -287,6 +300,12 @@ class Rng:
     def gaussian_spinor(self):
         out = np.zeros(2 * self.geom.n_sites, np.complex128)
         lib().orc_rng_gaussian_spinor(self.h, _p(out))
+        return out
+
+    def z2_spinor(self):
+        """FermionVector::set_random (src/dual/valence.h:54-60)."""
+        out = np.zeros(2 * self.geom.n_sites, dtype=np.complex128)
+        lib().orc_rng_z2_spinor(self.h, _p(out))
         return out
 
     def uniform(self):

@@ -89,15 +89,20 @@ SIGNATURES = [
     ("qed3_rng_destroy", ctypes.c_int, [vp]),
     ("qed3_rng_gaussian_links", ctypes.c_int, [vp, ctypes.c_double, vp]),
     ("qed3_rng_gaussian_spinor", ctypes.c_int, [vp, vp]),
+    ("qed3_rng_z2_spinor", ctypes.c_int, [vp, vp]),
+    ("qed3_point_source", ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, vp]),
     ("qed3_hmc_pure_gauge", ctypes.c_int, [vp, vp, vp, ctypes.c_double, ctypes.c_int, ctypes.c_int, ctypes.c_double,
                                            ctypes.c_int, ctypes.c_int, c_int_p, c_double_p, vp]),
     ("qed3_zolotarev", ctypes.c_int, [ctypes.c_double, ctypes.c_int, vp, vp, vp, vp, c_int_p]),
     ("qed3_overlap_create", ctypes.c_int, [vp, ctypes.c_int, ctypes.c_int, ctypes.POINTER(vp)]),
     ("qed3_overlap_destroy", ctypes.c_int, [vp]),
     ("qed3_overlap_update", ctypes.c_int, [vp, ctypes.c_double, ctypes.c_double, ctypes.c_double, vp]),
-    ("qed3_overlap_info", ctypes.c_int, [vp, c_double_p, c_double_p, c_double_p, c_double_p, c_int_p]),
+    ("qed3_overlap_info", ctypes.c_int, [vp, c_double_p, c_double_p, c_double_p, c_double_p, c_int_p, c_int_p]),
     ("qed3_overlap_apply", ctypes.c_int, [vp, ctypes.c_int, vp, vp, ctypes.c_double, ctypes.POINTER(SolveReport),
                                           vp]),
+    ("qed3_overlap_force", ctypes.c_int, [vp, vp, vp, ctypes.c_double, ctypes.POINTER(SolveReport), vp]),
+    ("qed3_overlap_solve", ctypes.c_int, [vp, vp, vp, ctypes.c_double, ctypes.c_double, ctypes.c_int,
+                                          ctypes.POINTER(SolveReport), vp]),
     ("qed3_batch_create", ctypes.c_int, [ctypes.c_int, vp, vp, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                          ctypes.POINTER(vp)]),
     ("qed3_batch_destroy", ctypes.c_int, [vp]),
@@ -331,6 +336,12 @@ class ParallelRng:
         _check(lib().qed3_rng_gaussian_spinor(self._h, _ptr(out)))
         return out
 
+    def z2_spinor(self) -> np.ndarray:
+        """FermionVector::set_random: (z + i z')/sqrt(2 Ns), z from the site engines' dist_z2(1, 2)."""
+        out = np.zeros(2 * self.lattice.n_sites, dtype=np.complex128)
+        _check(lib().qed3_rng_z2_spinor(self._h, _ptr(out)))
+        return out
+
     def __del__(self):
         if getattr(self, "_h", None) and _lib is not None:
             _lib.qed3_rng_destroy(self._h)
@@ -365,6 +376,13 @@ def thermalized_links(lattice: S2Trivalent, beta: float, seed: int, ntraj: int, 
         a, _ = hmc_pure_gauge(lattice, rng, A, beta, compact, True, 1.0, nsteps)
         acc += a
     return A, acc / max(1, ntraj)
+
+
+def point_source(lattice: S2Trivalent, x: int, s: int) -> np.ndarray:
+    """FermionVector::set_pt_source (src/dual/valence.h:47-52): unit vector at (site x, spin s)."""
+    out = np.zeros(2 * lattice.n_sites, dtype=np.complex128)
+    _check(lib().qed3_point_source(lattice.n_sites, x, s, _ptr(out)))
+    return out
 
 
 def zolotarev(k: float, n: int) -> dict:
@@ -445,13 +463,27 @@ class Overlap:
 
     def info(self) -> dict:
         a, b, k, dl = (ctypes.c_double() for _ in range(4))
-        np_ = ctypes.c_int()
-        _check(lib().qed3_overlap_info(self._h, *(ctypes.byref(v) for v in (a, b, k, dl, np_))))
-        return dict(lambda_min=a.value, lambda_max=b.value, k=k.value, delta=dl.value, npoles=np_.value)
+        np_, nh = ctypes.c_int(), ctypes.c_int()
+        _check(lib().qed3_overlap_info(self._h, *(ctypes.byref(v) for v in (a, b, k, dl, np_, nh))))
+        return dict(lambda_min=a.value, lambda_max=b.value, k=k.value, delta=dl.value, npoles=np_.value,
+                    npoles_fp64=nh.value)
 
     def apply(self, out, inp, op: int = OP_D, tol_inner: float = 1e-10, stream=None) -> Report:
         r = SolveReport()
         _check(lib().qed3_overlap_apply(self._h, op, _ptr(out), _ptr(inp), tol_inner, ctypes.byref(r),
+                                        _stream(stream)))
+        return Report(r.status, r.iters, r.reliable_updates, r.true_rel_res, r.ms)
+
+    def force(self, F, eta, tol_inner: float = 1e-10, stream=None) -> Report:
+        """F[l] = -2 d/dA_l Re<eta, D_ov eta> for all links (Overlap::grad_deviceAsyncLaunch)."""
+        r = SolveReport()
+        _check(lib().qed3_overlap_force(self._h, _ptr(eta), _ptr(F), tol_inner, ctypes.byref(r), _stream(stream)))
+        return Report(r.status, r.iters, r.reliable_updates, r.true_rel_res, r.ms)
+
+    def solve(self, x, b, tol: float = 1e-10, tol_inner: float = 1e-12, maxiter: int = 10000, stream=None) -> Report:
+        """Outer CG on D_ov^dag D_ov x = b; true_rel_res recomputed after convergence."""
+        r = SolveReport()
+        _check(lib().qed3_overlap_solve(self._h, _ptr(x), _ptr(b), tol, tol_inner, maxiter, ctypes.byref(r),
                                         _stream(stream)))
         return Report(r.status, r.iters, r.reliable_updates, r.true_rel_res, r.ms)
 

@@ -345,6 +345,20 @@ int qed3_rng_gaussian_spinor(qed3_rng* r, double* spinor) {
   return QED3_OK;
 }
 
+int qed3_rng_z2_spinor(qed3_rng* r, double* spinor) {
+  if (!r || !spinor) return fail(QED3_ERR_ARG, "NULL argument");
+  rng_z2_spinor(r, spinor);
+  return QED3_OK;
+}
+
+int qed3_point_source(int n_sites, int x, int s, double* spinor) {
+  if (!spinor || n_sites < 1) return fail(QED3_ERR_ARG, "NULL argument or empty lattice");
+  if (x < 0 || x >= n_sites || s < 0 || s > 1) return fail(QED3_ERR_ARG, "site or spin out of range");
+  std::memset(spinor, 0, size_t(4) * n_sites * sizeof(double));
+  spinor[4 * size_t(x) + 2 * s] = 1.0;
+  return QED3_OK;
+}
+
 int qed3_hmc_pure_gauge(qed3_lattice* lat, qed3_rng* rng, double* A, double beta, int compact, int exact,
                         double tmax, int nsteps, int no_reject, int* accepted, double* dH, void* stream) {
   QED3_GUARD_BEGIN
@@ -411,9 +425,9 @@ int qed3_overlap_update(qed3_overlap* ov, double lambda_min, double lambda_max, 
 }
 
 int qed3_overlap_info(const qed3_overlap* ov, double* lambda_min, double* lambda_max, double* k, double* delta,
-                      int* npoles) {
+                      int* npoles, int* npoles_fp64) {
   if (!ov) return fail(QED3_ERR_ARG, "NULL overlap");
-  return overlap_info(ov, lambda_min, lambda_max, k, delta, npoles);
+  return overlap_info(ov, lambda_min, lambda_max, k, delta, npoles, npoles_fp64);
 }
 
 int qed3_overlap_apply(qed3_overlap* ov, int op, double* out, const double* in, double tol_inner,
@@ -423,6 +437,24 @@ int qed3_overlap_apply(qed3_overlap* ov, int op, double* out, const double* in, 
   if (op < QED3_OP_D || op > QED3_OP_DDDAG) return fail(QED3_ERR_ARG, "unknown operator");
   if (out == in) return fail(QED3_ERR_ARG, "out must not alias in");
   return overlap_apply(ov, op, out, in, tol_inner > 0 ? tol_inner : 1e-10, report, (cudaStream_t)stream);
+  QED3_GUARD_END
+}
+
+int qed3_overlap_force(qed3_overlap* ov, const double* eta, double* F, double tol_inner, qed3_solve_report* report,
+                       void* stream) {
+  QED3_GUARD_BEGIN
+  if (!ov || !eta || !F) return fail(QED3_ERR_ARG, "NULL argument");
+  return overlap_force(ov, eta, F, tol_inner > 0 ? tol_inner : 1e-10, report, (cudaStream_t)stream);
+  QED3_GUARD_END
+}
+
+int qed3_overlap_solve(qed3_overlap* ov, double* x, const double* b, double tol, double tol_inner, int maxiter,
+                       qed3_solve_report* report, void* stream) {
+  QED3_GUARD_BEGIN
+  if (!ov || !x || !b) return fail(QED3_ERR_ARG, "NULL argument");
+  if (x == b) return fail(QED3_ERR_ARG, "x must not alias b");
+  return overlap_solve(ov, x, b, tol > 0 ? tol : 1e-10, tol_inner > 0 ? tol_inner : 1e-12,
+                       maxiter > 0 ? maxiter : 10000, report, (cudaStream_t)stream);
   QED3_GUARD_END
 }
 

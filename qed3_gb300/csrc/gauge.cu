@@ -125,6 +125,59 @@ __global__ void k_fermion_force(int Nl, int Ns, const int32_t* __restrict__ lx, 
   F[l] = -2.0 * inner;
 }
 
+// Re <u, (dD/dA_l) v> over the two blocks of link l = (x, y):
+//   conj(u_x) (i H_xy v_y) + conj(u_y) (-i H_yx v_x)
+__device__ __forceinline__ double link_inner(const M64& hxy, const M64& hyx, const Sp64& ux, const Sp64& uy,
+                                             const Sp64& vx, const Sp64& vy) {
+  const double2 a0 = cfma(hxy.h01, vy.s1, cmul(hxy.h00, vy.s0));
+  const double2 a1 = cfma(hxy.h11, vy.s1, cmul(hxy.h10, vy.s0));
+  const double2 b0 = cfma(hyx.h01, vx.s1, cmul(hyx.h00, vx.s0));
+  const double2 b1 = cfma(hyx.h11, vx.s1, cmul(hyx.h10, vx.s0));
+  // Re[conj(a) (i b)] = a.y b.x - a.x b.y
+  auto re_ci = [](double2 a, double2 b) { return a.y * b.x - a.x * b.y; };
+  return re_ci(ux.s0, a0) + re_ci(ux.s1, a1) - re_ci(uy.s0, b0) - re_ci(uy.s1, b1);
+}
+
+// Overlap force over all links (internal-order fields, np poles back to back):
+//   F_l = sum_m c_m (Re<DZ_m, dD Y_m> + Re<DY_m, dD Z_m>) + c_w Re<eta, dD w>
+struct OvForceCoef {
+  double c[64];
+  double cw;
+  int np;
+};
+__global__ void k_overlap_force(int Nl, int Ns, const int32_t* __restrict__ lx, const int32_t* __restrict__ ly,
+                                const int8_t* __restrict__ kx, const int8_t* __restrict__ ky,
+                                const M64* __restrict__ H, const S64* __restrict__ Z, const S64* __restrict__ Y,
+                                const S64* __restrict__ DZ, const S64* __restrict__ DY, const S64* __restrict__ eta,
+                                const S64* __restrict__ w, OvForceCoef co, double* __restrict__ F) {
+  const int l = blockIdx.x * blockDim.x + threadIdx.x;
+  if (l >= Nl) return;
+  const int x = lx[l], y = ly[l];
+  const M64 hxy = H[size_t(kx[l]) * Ns + x], hyx = H[size_t(ky[l]) * Ns + y];
+  double f = co.cw * link_inner(hxy, hyx, ld64(eta, x), ld64(eta, y), ld64(w, x), ld64(w, y));
+  for (int m = 0; m < co.np; m++) {
+    const size_t o = size_t(m) * Ns;
+    const double t = link_inner(hxy, hyx, ld64(DZ + o, x), ld64(DZ + o, y), ld64(Y + o, x), ld64(Y + o, y)) +
+                     link_inner(hxy, hyx, ld64(DY + o, x), ld64(DY + o, y), ld64(Z + o, x), ld64(Z + o, y));
+    f += co.c[m] * t;
+  }
+  F[l] = f;
+}
+
+int overlap_force_links(qed3_dirac_s* d, int np, const double* c, double cw, const S64* Z, const S64* Y,
+                        const S64* DZ, const S64* DY, const S64* eta, const S64* w, double* F, cudaStream_t st) {
+  if (np > 64) return fail(QED3_ERR_ARG, "at most 64 poles");
+  const DeviceLattice& D = d->lat->dev;
+  OvForceCoef co{};
+  for (int m = 0; m < np; m++) co.c[m] = c[m];
+  co.cw = cw;
+  co.np = np;
+  k_overlap_force<<<nblk(D.Nl), 256, 0, st>>>(D.Nl, d->Ns, D.link_x, D.link_y, D.link_kx, D.link_ky, d->H, Z, Y, DZ,
+                                              DY, eta, w, co, F);
+  QED3_CUDA_TRY(cudaGetLastError());
+  return QED3_OK;
+}
+
 // ---------------------------------------------------------------------------
 // host side
 // ---------------------------------------------------------------------------
@@ -246,6 +299,7 @@ struct RngEngine {
   std::mt19937_64 mt;
   std::normal_distribution<double> g;
   std::uniform_real_distribution<double> u;
+  std::uniform_int_distribution<int> z2{1, 2};  // SingleRng::dist_z2(1,2)
 };
 struct HostRng {
   RngEngine master;
@@ -285,6 +339,18 @@ void rng_gaussian_spinor(qed3_rng_s* r, double* out) {
     }
 }
 double rng_uniform(qed3_rng_s* r) { return r->r.master.u(r->r.master.mt); }
+void rng_z2_spinor(qed3_rng_s* r, double* out) {
+  // FermionVector::set_random, src/dual/valence.h:54-60 (z2_site draws 1 or 2)
+  const double nrm = std::sqrt(2.0 * double(r->r.sites.size()));
+  for (size_t x = 0; x < r->r.sites.size(); x++)
+    for (int a = 0; a < 2; a++) {
+      auto& e = r->r.sites[x];
+      const double re = e.z2(e.mt);
+      const double im = e.z2(e.mt);
+      out[4 * x + 2 * a] = re / nrm;
+      out[4 * x + 2 * a + 1] = im / nrm;
+    }
+}
 
 int hmc_pure_gauge(qed3_lattice_s* lat, qed3_rng_s* rng, double* A, double beta, int compact, int exact, double tmax,
                    int nsteps, int no_reject, int* accepted, double* dH_out, cudaStream_t st) {

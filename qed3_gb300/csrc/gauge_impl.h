@@ -13,11 +13,15 @@ int gauge_plaquette_avg(qed3_lattice_s* lat, const double* A, double* theta, dou
 int gauge_action(qed3_lattice_s* lat, const double* A, double beta, int compact, double* S, cudaStream_t st);
 int gauge_force(qed3_lattice_s* lat, const double* A, double beta, int compact, int exact, double* F, cudaStream_t st);
 int fermion_force(qed3_dirac_s* d, const double* eta_ref, double* F, cudaStream_t st);
+// F_l = sum_m c_m (Re<DZ_m, dD Y_m> + Re<DY_m, dD Z_m>) + cw Re<eta, dD w>, internal-order fields
+int overlap_force_links(qed3_dirac_s* d, int np, const double* c, double cw, const S64* Z, const S64* Y,
+                        const S64* DZ, const S64* DY, const S64* eta, const S64* w, double* F, cudaStream_t st);
 qed3_rng_s* rng_create(int n_links, int n_sites, int seed);
 void rng_destroy(qed3_rng_s* r);
 void rng_gaussian_links(qed3_rng_s* r, double width, double* out);
 void rng_gaussian_spinor(qed3_rng_s* r, double* out);
 double rng_uniform(qed3_rng_s* r);
+void rng_z2_spinor(qed3_rng_s* r, double* out);
 int hmc_pure_gauge(qed3_lattice_s* lat, qed3_rng_s* rng, double* A, double beta, int compact, int exact, double tmax,
                    int nsteps, int no_reject, int* accepted, double* dH, cudaStream_t st);
 }  // namespace qed3

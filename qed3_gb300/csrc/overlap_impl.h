@@ -11,5 +11,10 @@ void overlap_destroy(qed3_overlap_s* ov);
 int overlap_update(qed3_overlap_s* ov, double lmin, double lmax, double tol_outer, cudaStream_t st);
 int overlap_apply(qed3_overlap_s* ov, int op, double* out, const double* in, double tol, qed3_solve_report* rep,
                   cudaStream_t st);
-int overlap_info(const qed3_overlap_s* ov, double* lmin, double* lmax, double* k, double* delta, int* np);
+int overlap_force(qed3_overlap_s* ov, const double* eta, double* F, double tol, qed3_solve_report* rep,
+                  cudaStream_t st);
+int overlap_solve(qed3_overlap_s* ov, double* x, const double* b, double tol, double tol_inner, int maxiter,
+                  qed3_solve_report* rep, cudaStream_t st);
+int overlap_info(const qed3_overlap_s* ov, double* lmin, double* lmax, double* k, double* delta, int* np,
+                 int* np_fp64);
 }  // namespace qed3

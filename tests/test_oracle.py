@@ -174,3 +174,31 @@ def test_rng_streams_are_deterministic():
     c = O.Rng(g, 8).gaussian_spinor()
     assert np.array_equal(a, b) and not np.array_equal(a, c)
     assert abs(np.mean(np.abs(a) ** 2) - 1.0) < 0.5
+
+
+def test_overlap_force_finite_difference():
+    """The oracle's restatement of Overlap::grad_deviceAsyncLaunch equals
+    -2 d/dA_l Re<eta, D_ov eta> (central differences, eps = 1e-5 as in
+    src/dual/grad.cu:143-172)."""
+    n = 2
+    g = O.geometry(n)
+    rng = np.random.default_rng(5)
+    A = rng.uniform(-np.pi, np.pi, g.n_links)
+    D = O.Dirac(g, 1.0, -1.0)
+    D.update(A)
+    lmin, lmax = D.lambda_bounds()
+    eta = rng.normal(size=2 * g.n_sites) + 1j * rng.normal(size=2 * g.n_sites)
+    F = D.overlap_force(A, eta, lmin, lmax, 21)
+
+    def f(Ap):
+        Dp = O.Dirac(g, 1.0, -1.0)
+        Dp.update(Ap)
+        return np.vdot(eta, Dp.overlap(eta, lmin, lmax, 21, 0)).real
+
+    eps = 1e-5
+    for l in (0, 7, 19, 33):
+        Ap, Am = A.copy(), A.copy()
+        Ap[l] += eps
+        Am[l] -= eps
+        fd = -2 * (f(Ap) - f(Am)) / (2 * eps)
+        assert abs(F[l] - fd) <= 1e-6 * max(1.0, abs(fd))
