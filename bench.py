@@ -306,6 +306,7 @@ def main():
                ("pcg_f32", Q.PREC_F32, pc), ("pcg_bf16", Q.PREC_BF16, pc))
     clocks = Clocks(local)
     clocks.start()  # sampled over every timed solver and the e2e loop
+    torch.cuda.nvtx.range_push("timed")  # the launch list of the timed region (ncu --nvtx-include timed/)
     for name, prec, p in solvers:
         ms, reps, x = time_solver(torch, Q, D, bt, prec, args.steps, warmup, flush, pc=p)
         ok = all(r.status == Q.OK and r.true_rel_res <= TOL for r in reps)
@@ -347,6 +348,7 @@ def main():
         if i >= warmup:
             e2e_ms.append(e0.elapsed_time(e1))
     e2e = world * 1e3 / float(np.mean(e2e_ms))
+    torch.cuda.nvtx.range_pop()
     clocks_info = clocks.stop()
 
     heldout = heldout_iterations(torch, Q, lat, pc, dev)
