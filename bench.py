@@ -41,6 +41,10 @@ N_REFINE = 64
 BETA = 1.4
 M5 = 0.05
 TOL = 1e-10
+# DRAM read + write bytes of one k_pcg launch at n=64 from ncu (summary in
+# profiles/k_pcg_n64_f32.md): the operator and vectors are loaded once, the
+# iterations run out of L2.
+PCG_DRAM_BYTES_PER_LAUNCH = 53.06e6
 METRIC = "D†D solves/s to 1e-10 at n=64: learned-PC mixed vs plain FP64 CG; apply GB/s"
 WORKLOAD = ("n=64 dual lattice (81,920 sites), r=1, M5=0.05, links U[-pi,pi) seed 2 + 50 HMC traj beta=1.4, "
             "Gaussian source seed 7, CG on D^dag D to 1e-10 FP64 true residual")
@@ -391,7 +395,7 @@ def main():
             "preconditioner": train_info,
             "heldout": heldout,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                         "traffic": None, "kernel": kernel, "note": "n=64 is L2-resident and the persistent "
+                         "traffic": PCG_DRAM_BYTES_PER_LAUNCH if use_pc else None, "kernel": kernel, "note": "n=64 is L2-resident and the persistent "
                          "solver is grid-barrier latency bound; "
                          f"{per_site_iter} B/site/iteration x {iters} iterations; the HBM-bound Dirac apply is "
                          "in apply_sweep"},
