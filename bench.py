@@ -41,8 +41,8 @@ N_REFINE = 64
 BETA = 1.4
 M5 = 0.05
 TOL = 1e-10
-# DRAM read + write bytes of one k_pcg launch at n=64 from ncu (summary in
-# profiles/k_pcg_n64_f32.md): the operator and vectors are loaded once, the
+# DRAM read + write bytes of one k_pcg launch at n=64 from an ncu capture
+# (--set full, one launch): the operator and vectors are loaded once, the
 # iterations run out of L2.
 PCG_DRAM_BYTES_PER_LAUNCH = 53.06e6
 METRIC = "D†D solves/s to 1e-10 at n=64: learned-PC mixed vs plain FP64 CG; apply GB/s"
