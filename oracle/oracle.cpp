@@ -5,7 +5,7 @@
 // into, called by, or shipped with the product library.  Only tests/,
 // __graft_entry__.smoke() and bench.py's cpu_baseline / reference leg load it.
 //
-// Parity status (see DESIGN.md "Oracle"): the reference cannot be built here
+// Parity status: the reference cannot be built here
 // (Eigen, GSL, the QFE lattice library and its .dat geometry tables are all
 // absent), so geometry parity against the reference's own tables is UNPINNED.
 // The oracle is pinned instead by every invariant the reference asserts
