@@ -53,6 +53,10 @@ struct PcgArgs {
   int flexible;  // Polak-Ribiere beta
   long long spin_limit;
   LpcWordCoef pc;
+  // pipelined kernel: gathered copies of u, p, q at residual replacements
+  void* halo_u;
+  void* halo_p;
+  void* halo_q;
 };
 
 __device__ __forceinline__ float4 sp2f4(const Sp32& v) { return make_float4(v.s0.x, v.s0.y, v.s1.x, v.s1.y); }
@@ -524,6 +528,290 @@ timeout:
 }
 
 // ---------------------------------------------------------------------------
+// Pipelined preconditioned CG: ONE grid barrier per iteration
+// ---------------------------------------------------------------------------
+// Ghysels & Vanroose's pipelined PCG (u = N r, w = A u, s = A p, q = N s,
+// z = A q, A = D^dag D + s):
+//   gam = <r,u>, delta = <w,u>;  m = N w;  n = A m
+//   beta = gam / gam_old, alpha = gam / (delta - beta gam / alpha_old)
+//   z = n + beta z, q = m + beta q, s = w + beta s, p = u + beta p,
+//   x += alpha p, r -= alpha s, u -= alpha q, w -= alpha z.
+// The dots and m = N w (block-local) need no neighbour data, and A m is
+// applied as a two-hop stencil from ONE gathered field,
+//   (D m)_y = diag_y m_y + sum_k H_{y,k} m_{nbr(y,k)}   (y = i and its neighbours),
+//   n_i = diag_i (D m)_i + sum_k Hd_{i,k} (D m)_{nbr(i,k)} + s m_i,
+// so each iteration is [dots, m = N w, publish m | barrier | totals, n = A m,
+// updates].  A residual replacement (FP64 reliable update, three barriers as
+// in the other solvers) recomputes r = b - A x, u, w and s = A p, q = N s,
+// z = A q, m = N w, n = A m exactly (two more barriers) and takes that step
+// with a direct line search along p' = u + beta p: alpha = <r,p'> / <p',A p'>
+// (in a CPU model of this recurrence in FP32 with FP64 replacements the
+// iteration counts equal those of the two-barrier PCG at n = 16, 32, 64).
+
+__device__ __forceinline__ Sp32 blk_mul(const float4& r0, const float4& r1, const Sp32& y) {
+  Sp32 o;
+  o.s0 = cfmaf(lo2(r0), y.s0, make_float2(0.f, 0.f));
+  o.s0 = cfmaf(hi2(r0), y.s1, o.s0);
+  o.s1 = cfmaf(lo2(r1), y.s0, make_float2(0.f, 0.f));
+  o.s1 = cfmaf(hi2(r1), y.s1, o.s1);
+  return o;
+}
+
+// n_i = (D^dag D + sig) m at owned site i from the gathered field `halo`;
+// nb2[(3k+q) * per + lc] = nbr(nbr(i,k), q); own hop blocks of D and D^dag
+// from shared memory, the neighbours' blocks of D through the read-only path.
+template <int P>
+__device__ __forceinline__ Sp32 two_hop(int i, int lc, int per, int Ns, const int (&jj)[3], const int* nb2,
+                                        const M32* __restrict__ H32, const float* __restrict__ diag32,
+                                        const float4* HsD, const float4* HsDd, float dg, float sig, const Sp32& self,
+                                        const void* halo) {
+  Sp32 mn[3], m2[9];
+#pragma unroll
+  for (int k = 0; k < 3; k++) mn[k] = hl32<P>(halo, jj[k]);
+#pragma unroll
+  for (int t = 0; t < 9; t++) m2[t] = hl32<P>(halo, nb2[t * per + lc]);
+  Sp32 di = sp_add(Sp32{make_float2(0.f, 0.f), make_float2(0.f, 0.f)}, self, dg);
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    const Sp32 h = blk_mul(HsD[(2 * k) * per + lc], HsD[(2 * k + 1) * per + lc], mn[k]);
+    di = sp_add(di, h, 1.f);
+  }
+  Sp32 o = sp_add(Sp32{make_float2(0.f, 0.f), make_float2(0.f, 0.f)}, di, dg);
+  o = sp_add(o, self, sig);
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    const int j = jj[k];
+    Sp32 dj = sp_add(Sp32{make_float2(0.f, 0.f), make_float2(0.f, 0.f)}, mn[k], __ldg(diag32 + j));
+#pragma unroll
+    for (int q = 0; q < 3; q++) {
+      const float4* hm = reinterpret_cast<const float4*>(H32 + size_t(q) * Ns + j);
+      dj = sp_add(dj, blk_mul(__ldg(hm), __ldg(hm + 1), m2[3 * k + q]), 1.f);
+    }
+    o = sp_add(o, blk_mul(HsDd[(2 * k) * per + lc], HsDd[(2 * k + 1) * per + lc], dj), 1.f);
+  }
+  return o;
+}
+
+template <int P, int NW>
+__global__ void __launch_bounds__(576, 1) k_ppcg(PcgArgs a) {
+  extern __shared__ float4 S[];
+  __shared__ double sh[32 * 4 + 64 + 8];
+  const int Ns = a.Ns, per = a.per;
+  const int blk0 = blockIdx.x * per;
+  float4* HsD = S + NW * per;
+  float4* HsDd = HsD + 6 * per;
+  int* nb2 = reinterpret_cast<int*>(HsDd + 6 * per);
+  const int lc = threadIdx.x;  // one site per thread
+  const int i = blk0 + lc;
+  const bool ok = i < Ns;
+  const int own[1] = {i}, loc[1] = {lc};
+  const bool val[1] = {ok};
+  int jj[1][3] = {{0, 0, 0}};
+  float dg = 0.f;
+  const Sp32 z32{make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
+  const float4 zf = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+  for (int q = 0; q < 6; q++) {
+    HsD[q * per + lc] = ok ? __ldg(reinterpret_cast<const float4*>(a.H32 + size_t(q >> 1) * Ns + i) + (q & 1)) : zf;
+    HsDd[q * per + lc] = ok ? __ldg(reinterpret_cast<const float4*>(a.Hd32 + size_t(q >> 1) * Ns + i) + (q & 1)) : zf;
+  }
+  if (ok) {
+    dg = __ldg(a.diag32 + i);
+#pragma unroll
+    for (int k = 0; k < 3; k++) jj[0][k] = __ldg(a.nbr + k * Ns + i);
+  }
+#pragma unroll
+  for (int k = 0; k < 3; k++)
+#pragma unroll
+    for (int q = 0; q < 3; q++) nb2[(3 * k + q) * per + lc] = ok ? __ldg(a.nbr + q * Ns + jj[0][k]) : 0;
+  const float sig = float(a.shift);
+  auto A2 = [&](const Sp32& self, const void* halo) {
+    return ok ? two_hop<P>(i, lc, per, Ns, jj[0], nb2, a.H32, a.diag32, HsD, HsDd, dg, sig, self, halo) : z32;
+  };
+
+  Sp32 r[1] = {z32}, u[1] = {z32}, m[1] = {z32};
+  Sp32 w = z32, zz = z32, q = z32, s = z32, p = z32, xl = z32;
+  // ---- phase 0: r = b, u = N r; |b|^2 -----------------------------------------------
+  double v1[1] = {0.0};
+  if (ok) {
+    const Sp64 bi = ld64(a.b, i);
+    v1[0] = n2(bi);
+    r[0] = Sp32{make_float2(float(bi.s0.x), float(bi.s0.y)), make_float2(float(bi.s1.x), float(bi.s1.y))};
+  }
+  pc_apply<NW, 1, true>(a, S, HsD, blk0, own, loc, val, jj, r, u);
+  if (ok) hs32<P>(a.halo_u, i, u[0]);
+  unsigned int epoch = 0;
+  int parity = 0;
+  v2_publish<1>(v1, a.partials, parity, sh);
+  if (!grid_sync2(a.bar, epoch, a.spin_limit)) goto timeout;
+  {
+    double tot[1];
+    v2_total<1>(a.partials, parity, tot, sh);
+    parity ^= 1;
+    const double bnorm2 = tot[0];
+    double mu_true = bnorm2, mu_max = bnorm2, gam_old = 0.0, al_old = 0.0;
+    int iter = 0, nru = 0, status = QED3_ERR_NOCONV;
+    bool first = true;
+    if (bnorm2 == 0.0) {
+      status = QED3_OK;
+      mu_true = 0.0;
+      goto finish;
+    }
+    w = A2(u[0], a.halo_u);
+    while (true) {
+      // ---- dots of (r, u, w), m = N w, publish m | barrier -----------------------------
+      float v[3] = {0.f, 0.f, 0.f};
+      if (ok) {
+        v[0] = rdotf(r[0], u[0]);
+        v[1] = rdotf(w, u[0]);
+        v[2] = n2f(r[0]);
+      }
+      {
+        const Sp32 wv[1] = {w};
+        pc_apply<NW, 1, true>(a, S, HsD, blk0, own, loc, val, jj, wv, m);
+      }
+      if (ok) hs32<P>(a.halo_z, i, m[0]);
+      v2_publish_f<3>(v, a.partials, parity, sh);
+      if (!grid_sync2(a.bar, epoch, a.spin_limit)) goto timeout;
+      double t3[3];
+      v2_total<3>(a.partials, parity, t3, sh);
+      parity ^= 1;
+      double gam = t3[0];
+      const double dl = t3[1], mu = t3[2];
+      mu_max = fmax(mu_max, mu);
+      double alpha, beta;
+      Sp32 n;
+      const bool want = !first && (!isfinite(mu) || !(gam > 0.0) || mu < a.tol2 * bnorm2 || iter >= a.maxiter ||
+                                   mu < a.delta2 * mu_max);
+      if (!want) {
+        if (first) {
+          beta = 0.0;
+          alpha = gam / dl;
+        } else {
+          beta = gam / gam_old;
+          alpha = gam / (dl - beta * gam / al_old);
+        }
+        n = A2(m[0], a.halo_z);
+      } else {
+        // ---- residual replacement: R0 fold and publish x ----------------------------------
+        Sp64 xh{make_double2(0, 0), make_double2(0, 0)};
+        if (ok) {
+          xh = hl64(a.x, i);
+          xh.s0 = make_double2(xh.s0.x + xl.s0.x, xh.s0.y + xl.s0.y);
+          xh.s1 = make_double2(xh.s1.x + xl.s1.x, xh.s1.y + xl.s1.y);
+          hs64(a.x, i, xh);
+        }
+        xl = z32;
+        if (!grid_sync2(a.bar, epoch, a.spin_limit)) goto timeout;
+        // ---- R1: t64 = D x ------------------------------------------------------------------
+        if (ok) hs64(a.t64, i, stencil64(i, Ns, jj[0], a.H, a.diag, xh, a.x));
+        if (!grid_sync2(a.bar, epoch, a.spin_limit)) goto timeout;
+        // ---- R2: r = b - D^dag t64 - s x (FP64), u = N r; publish u, p ---------------------
+        double vv[1] = {0.0};
+        if (ok) {
+          const Sp64 self = hl64(a.t64, i);
+          const Sp64 qd = stencil64(i, Ns, jj[0], a.Hd, a.diag, self, a.t64);
+          const Sp64 bi = ld64(a.b, i);
+          Sp64 rt;
+          rt.s0 = csub(bi.s0, cadd(qd.s0, cscale(a.shift, xh.s0)));
+          rt.s1 = csub(bi.s1, cadd(qd.s1, cscale(a.shift, xh.s1)));
+          vv[0] = n2(rt);
+          r[0] = Sp32{make_float2(float(rt.s0.x), float(rt.s0.y)), make_float2(float(rt.s1.x), float(rt.s1.y))};
+        }
+        pc_apply<NW, 1, true>(a, S, HsD, blk0, own, loc, val, jj, r, u);
+        if (ok) {
+          hs32<P>(a.halo_u, i, u[0]);
+          hs32<P>(a.halo_p, i, p);
+        }
+        v2_publish<1>(vv, a.partials, parity, sh);
+        if (!grid_sync2(a.bar, epoch, a.spin_limit)) goto timeout;
+        double tr[1];
+        v2_total<1>(a.partials, parity, tr, sh);
+        parity ^= 1;
+        nru++;
+        mu_true = tr[0];
+        if (mu_true < a.tol2 * bnorm2) {
+          status = QED3_OK;
+          break;
+        }
+        if (iter >= a.maxiter || !isfinite(mu_true)) {
+          status = QED3_ERR_NOCONV;
+          break;
+        }
+        mu_max = mu_true;
+        // ---- R3: w = A u, s = A p, q = N s, m = N w; publish q, m; line-search dots ------
+        w = A2(u[0], a.halo_u);
+        s = A2(p, a.halo_p);
+        Sp32 qq[1];
+        {
+          const Sp32 sv[1] = {s};
+          pc_apply<NW, 1, true>(a, S, HsD, blk0, own, loc, val, jj, sv, qq);
+        }
+        q = qq[0];
+        {
+          const Sp32 wv[1] = {w};
+          pc_apply<NW, 1, true>(a, S, HsD, blk0, own, loc, val, jj, wv, m);
+        }
+        float v5[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
+        if (ok) {
+          hs32<P>(a.halo_q, i, q);
+          hs32<P>(a.halo_z, i, m[0]);
+          v5[0] = rdotf(r[0], u[0]);
+          v5[1] = rdotf(r[0], p);
+          v5[2] = rdotf(u[0], w);
+          v5[3] = rdotf(u[0], s) + rdotf(p, w);
+          v5[4] = rdotf(p, s);
+        }
+        v2_publish_f<5, 8>(v5, a.partials, parity, sh);
+        if (!grid_sync2(a.bar, epoch, a.spin_limit)) goto timeout;
+        double t5[5];
+        v2_total<5, 8>(a.partials, parity, t5, sh);
+        parity ^= 1;
+        gam = t5[0];
+        beta = gam / gam_old;
+        const double rp = gam + beta * t5[1];
+        const double pap = t5[2] + beta * t5[3] + beta * beta * t5[4];
+        alpha = rp / pap;
+        // ---- R4: z = A q, n = A m -------------------------------------------------------
+        zz = A2(q, a.halo_q);
+        n = A2(m[0], a.halo_z);
+      }
+      // ---- recurrences -------------------------------------------------------------------
+      {
+        const float al = float(alpha), bt = float(beta);
+        zz = sp_add(n, zz, bt);
+        q = sp_add(m[0], q, bt);
+        s = sp_add(w, s, bt);
+        p = sp_add(u[0], p, bt);
+        xl = sp_add(xl, p, al);
+        r[0] = sp_add(r[0], s, -al);
+        u[0] = sp_add(u[0], q, -al);
+        w = sp_add(w, zz, -al);
+      }
+      gam_old = gam;
+      al_old = alpha;
+      first = false;
+      iter++;
+    }
+  finish:
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+      a.scal[0] = mu_true;
+      a.scal[1] = bnorm2;
+      a.scal[2] = iter;
+      a.scal[3] = nru;
+      a.scal[4] = status;
+      a.scal[5] = 0;
+    }
+    return;
+  }
+timeout:
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    a.scal[4] = QED3_ERR_TIMEOUT;
+    a.scal[5] = 0;
+  }
+}
+
+// ---------------------------------------------------------------------------
 // host side
 // ---------------------------------------------------------------------------
 template <int P, int NW, int SPT>
@@ -544,6 +832,33 @@ int pcg_block_sites(int Ns, int sm_count) {
   const long long per_sm = (Ns + sm_count - 1) / sm_count;
   if (per_sm <= 576) return int((per_sm + 31) / 32 * 32);
   return int((per_sm + 63) / 64 * 64);
+}
+
+static const void* ppcg_kernel(int prec, int nw) {
+  if (prec == QED3_PREC_F32) return nw == 7 ? (const void*)k_ppcg<P32, 7> : (const void*)k_ppcg<P32, 3>;
+  return nw == 7 ? (const void*)k_ppcg<PBF16, 7> : (const void*)k_ppcg<PBF16, 3>;
+}
+
+// The pipelined kernel: one site per thread, per <= 576; shared memory holds the
+// preconditioner fields, the owned hop blocks of D and D^dag and the two-hop ids.
+static bool ppcg_plan(int prec, int nw, int Ns, int per, int sm_count, int* grid, size_t* smem) {
+  if (per % 32 || per > 576) return false;
+  const void* fn = ppcg_kernel(prec, nw);
+  const size_t sm = size_t(nw + 12) * per * sizeof(float4) + size_t(9) * per * sizeof(int);
+  if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(sm)) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  int per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, per, sm) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  const int G = (Ns + per - 1) / per;
+  if (per_sm < 1 || G > per_sm * sm_count) return false;
+  *grid = G;
+  *smem = sm;
+  return true;
 }
 
 bool pcg_plan(int prec, int nw, int Ns, int per, int sm_count, int* grid, int* threads, int* spt, size_t* smem) {
@@ -589,11 +904,15 @@ int pcg_solve(qed3_dirac_s* d, qed3_lpc_s* L, double* x, const double* b, const 
   const double shift = prm ? prm->shift : 0.0;
   LpcWordCoef co;
   if ((rc = lpc_word_coef_cached(L, &co))) return rc;
+  const bool flexible = prm && (prm->flags & QED3_SOLVE_FLEXIBLE);
+  const bool two_barrier = flexible || (prm && (prm->flags & QED3_SOLVE_TWO_BARRIER));
   int grid = 0, threads = 0, spt = 0;
   size_t smem = 0;
-  if (!pcg_plan(prec, co.nwords, d->Ns, L->per, d->sm_count, &grid, &threads, &spt, &smem))
+  const bool pipelined = !two_barrier && ppcg_plan(prec, co.nwords, d->Ns, L->per, d->sm_count, &grid, &smem);
+  if (!pipelined && !pcg_plan(prec, co.nwords, d->Ns, L->per, d->sm_count, &grid, &threads, &spt, &smem))
     return fail(QED3_ERR_ARG, "lattice too large for the register-resident preconditioned solver");
   if ((rc = field_import(d, QED3_PREC_F64, w.b, b, 1, st))) return rc;
+  if (pipelined) QED3_CUDA_TRY(cudaMemsetAsync(w.xhi, 0, size_t(d->Ns) * 4 * sizeof(double), st));
   QED3_CUDA_TRY(cudaMemsetAsync(w.bar2, 0, sizeof(GridBar2), st));
   PcgArgs a{};
   a.Ns = d->Ns;
@@ -620,9 +939,16 @@ int pcg_solve(qed3_dirac_s* d, qed3_lpc_s* L, double* x, const double* b, const 
   a.flexible = (prm && (prm->flags & QED3_SOLVE_FLEXIBLE)) ? 1 : 0;
   a.spin_limit = 4000000LL;
   a.pc = co;
+  a.halo_u = w.t;
+  a.halo_p = w.p;
+  a.halo_q = w.xlo;
   void* kargs[] = {&a};
   QED3_CUDA_TRY(cudaEventRecord(w.e0, st));
-  QED3_CUDA_TRY(cudaLaunchCooperativeKernel(pcg_kernel(prec, co.nwords, spt), dim3(grid), dim3(threads), kargs, smem, st));
+  if (pipelined)
+    QED3_CUDA_TRY(cudaLaunchCooperativeKernel(ppcg_kernel(prec, co.nwords), dim3(grid), dim3(L->per), kargs, smem, st));
+  else
+    QED3_CUDA_TRY(
+        cudaLaunchCooperativeKernel(pcg_kernel(prec, co.nwords, spt), dim3(grid), dim3(threads), kargs, smem, st));
   QED3_CUDA_TRY(cudaEventRecord(w.e1, st));
   return cg_finish(d, x, rep, st);
 }

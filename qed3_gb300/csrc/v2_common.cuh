@@ -20,11 +20,13 @@ __device__ __forceinline__ void v2_publish(double (&v)[NV], double* part, int pa
 // Global totals: lane l of warp 0 loads the partials of blocks l, l+32, ...
 // all at once (one L2 round trip instead of one per block stride), then FP64
 // sums in a fixed order (deterministic), broadcast through shared memory.
-template <int NV>
+// W: doubles per block slot in `part` (>= NV)
+template <int NV, int W = 4>
 __device__ __forceinline__ void v2_total(const double* part, int parity, double (&out)[NV], double* sh) {
+  static_assert(NV <= W, "slot too small");
   if (threadIdx.x < 32) {
     const int G = gridDim.x;
-    const double* base = part + size_t(parity) * G * 4;
+    const double* base = part + size_t(parity) * G * W;
     double acc[NV];
 #pragma unroll
     for (int q = 0; q < NV; q++) acc[q] = 0.0;
@@ -33,11 +35,11 @@ __device__ __forceinline__ void v2_total(const double* part, int parity, double 
     for (int c = 0; c < 5; c++) {
       const int bI = threadIdx.x + 32 * c;
 #pragma unroll
-      for (int q = 0; q < NV; q++) acc[q] += bI < G ? __ldcg(base + size_t(bI) * 4 + q) : 0.0;
+      for (int q = 0; q < NV; q++) acc[q] += bI < G ? __ldcg(base + size_t(bI) * W + q) : 0.0;
     }
 #pragma unroll
     for (int q = 0; q < NV; q++) {
-      for (int bI = threadIdx.x + 160; bI < G; bI += 32) acc[q] += __ldcg(base + size_t(bI) * 4 + q);
+      for (int bI = threadIdx.x + 160; bI < G; bI += 32) acc[q] += __ldcg(base + size_t(bI) * W + q);
       acc[q] = warp_sum(acc[q]);
     }
     if (threadIdx.x == 0)
@@ -61,8 +63,9 @@ __device__ __forceinline__ float warp_sum_f(float v) {
 // the global FP64 accumulation in v2_total.  FP64 arithmetic stays off the
 // per-thread path: on GB300 a dependent DADD costs ~2.5x an FADD, a 64-bit
 // shuffle ~2x, and an f32<->f64 conversion ~4x.
-template <int NV>
+template <int NV, int W = 4>
 __device__ __forceinline__ void v2_publish_f(float (&v)[NV], double* part, int parity, double* sh) {
+  static_assert(NV <= W, "slot too small");
   float* shf = reinterpret_cast<float*>(sh);  // 32*NV floats, below the totals' slots
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
 #pragma unroll
@@ -76,7 +79,7 @@ __device__ __forceinline__ void v2_publish_f(float (&v)[NV], double* part, int p
     for (int q = 0; q < NV; q++) {
       float t = lane < nw ? shf[q * 32 + lane] : 0.f;
       t = warp_sum_f(t);
-      if (lane == 0) __stcg(part + (size_t(parity) * gridDim.x + blockIdx.x) * 4 + q, double(t));
+      if (lane == 0) __stcg(part + (size_t(parity) * gridDim.x + blockIdx.x) * W + q, double(t));
     }
   }
 }

@@ -290,3 +290,32 @@ def test_lpc_tensor_core_training_n16(cuda):
     rep = pc.solve(Dq, xt, bt, tol=1e-10, precision=Q.PREC_F32)
     assert rep.status == Q.OK and rep.true_rel_res <= 1e-10
     assert rep.iters < it_ref
+
+
+@pytest.mark.parametrize("prec", [Q.PREC_F32, Q.PREC_BF16])
+def test_pipelined_pcg_matches_two_barrier(cuda, prec):
+    """The one-barrier pipelined recurrence against the two-barrier PCG: same
+    certificate, same solution to the tolerance, iteration counts within a few."""
+    rng, g, lat, A, Do, Dq = _setup(16, M5=0.05, seed=13)
+    pc = Q.LearnedPreconditioner(Dq, channels=8, layers=2, seed=4)
+    pc.collect(Dq, nsrc=2, seed=9, snapshots=(0, 10, 30))
+    pc.train(200, batch=6, lr=3e-3, seed=1)
+    b = rand_spinor(rng, g.n_sites)
+    bt = to_dev(b, cuda)
+    x_ref, it_ref, _ = Do.cg(b, tol=1e-10)
+    reps = {}
+    for pipelined in (False, True):
+        for shift in (0.0, 0.2):
+            xt = torch.zeros_like(bt)
+            rep = pc.solve(Dq, xt, bt, tol=1e-10, precision=prec, shift=shift, pipelined=pipelined)
+            assert rep.status == Q.OK and rep.true_rel_res <= 1e-10
+            q = torch.zeros_like(bt)
+            Dq.apply(q, xt, Q.OP_DDAGD)
+            q = q + shift * xt
+            assert float((bt - q).norm() / bt.norm()) <= 1.05e-10
+            if shift == 0.0:
+                assert np.linalg.norm(from_dev(xt) - x_ref) / np.linalg.norm(x_ref) < 1e-7
+            reps[(pipelined, shift)] = rep.iters
+    for shift in (0.0, 0.2):
+        a, c = reps[(False, shift)], reps[(True, shift)]
+        assert abs(a - c) <= max(4, a // 20)
