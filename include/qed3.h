@@ -112,7 +112,7 @@ int qed3_dirac_apply_field(qed3_dirac* d, int op, int prec, void* out, const voi
 #define QED3_SOLVE_STREAMING 2 /* force the memory-streaming persistent kernel (default: register-resident when it fits) */
 #define QED3_SOLVE_BCAST_B 4   /* batched: every right-hand side of system u is b[u]'s first vector */
 #define QED3_SOLVE_FLEXIBLE 8  /* preconditioned CG: Polak-Ribiere beta = <z', r' - r> / <z, r> (flexible CG) */
-#define QED3_SOLVE_TWO_BARRIER 16 /* preconditioned CG: the two-barrier recurrence (default: pipelined, one barrier) */
+#define QED3_SOLVE_PIPELINED 16 /* preconditioned CG: pipelined one-barrier recurrence (QED3_PREC_F32 only) */
 
 typedef struct {
   double tol;     /* target ||b - A x|| / ||b|| of the FP64 true residual */

@@ -34,7 +34,7 @@ PREC_F64, PREC_F32, PREC_BF16 = range(3)
 SOLVE_STREAMING = 2
 SOLVE_BCAST_B = 4
 SOLVE_FLEXIBLE = 8
-SOLVE_TWO_BARRIER = 16
+SOLVE_PIPELINED = 16
 PREC_NAMES = {"f64": PREC_F64, "f32": PREC_F32, "bf16": PREC_BF16}
 BYTES_PER_SITE = {PREC_F64: 32, PREC_F32: 16, PREC_BF16: 8}
 
@@ -550,11 +550,11 @@ class LearnedPreconditioner:
 
     def solve(self, dirac: DiracS2Dual, x, b, tol: float = 1e-10, maxiter: int = 100000,
               precision: int = PREC_F32, delta: float = 0.1, shift: float = 0.0, flexible: bool = False,
-              pipelined: bool = True, stream=None) -> Report:
+              pipelined: bool = False, stream=None) -> Report:
         """Preconditioned CG on (D^dag D + shift) x = b; FP64 true-residual certificate.
         flexible: Polak-Ribiere beta (flexible CG), robust to a preconditioner that is
         not exactly linear or hermitian."""
-        flags = (SOLVE_FLEXIBLE if flexible else 0) | (0 if pipelined else SOLVE_TWO_BARRIER)
+        flags = (SOLVE_FLEXIBLE if flexible else 0) | (SOLVE_PIPELINED if pipelined else 0)
         p = SolveParams(tol, maxiter, precision, delta, shift, flags)
         r = SolveReport()
         rc = lib().qed3_pcg_solve(dirac.handle, self._h, _ptr(x), _ptr(b), ctypes.byref(p), ctypes.byref(r),

@@ -557,38 +557,53 @@ __device__ __forceinline__ Sp32 blk_mul(const float4& r0, const float4& r1, cons
   return o;
 }
 
-// n_i = (D^dag D + sig) m at owned site i from the gathered field `halo`;
-// nb2[(3k+q) * per + lc] = nbr(nbr(i,k), q); own hop blocks of D and D^dag
-// from shared memory, the neighbours' blocks of D through the read-only path.
+// n_i = (D^dag D + sig) m at owned site i from the gathered field `halo`.
+// Every thread of the block calls it (two __syncthreads): each owned site
+// computes (D m)_i from its own hop blocks (shared memory) and its three
+// gathered neighbours and posts it to SDm; (D m)_j of an in-block neighbour
+// is then read from SDm, that of a neighbour owned by another block is
+// recomputed here from the gathered field (nb2[(3k+q) * per + lc] =
+// nbr(nbr(i,k), q)) and that neighbour's hop blocks.
 template <int P>
-__device__ __forceinline__ Sp32 two_hop(int i, int lc, int per, int Ns, const int (&jj)[3], const int* nb2,
-                                        const M32* __restrict__ H32, const float* __restrict__ diag32,
-                                        const float4* HsD, const float4* HsDd, float dg, float sig, const Sp32& self,
-                                        const void* halo) {
-  Sp32 mn[3], m2[9];
+__device__ __forceinline__ Sp32 two_hop(bool ok, int i, int lc, int blk0, int per, int Ns, const int (&jj)[3],
+                                        const int* nb2, const M32* __restrict__ H32,
+                                        const float* __restrict__ diag32, const float4* HsD, const float4* HsDd,
+                                        float4* SDm, float dg, float sig, const Sp32& self, const void* halo) {
+  const Sp32 zero{make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
+  Sp32 mn[3] = {zero, zero, zero};
+  Sp32 di = zero;
+  if (ok) {
 #pragma unroll
-  for (int k = 0; k < 3; k++) mn[k] = hl32<P>(halo, jj[k]);
+    for (int k = 0; k < 3; k++) mn[k] = hl32<P>(halo, jj[k]);
+    di = sp_add(zero, self, dg);
 #pragma unroll
-  for (int t = 0; t < 9; t++) m2[t] = hl32<P>(halo, nb2[t * per + lc]);
-  Sp32 di = sp_add(Sp32{make_float2(0.f, 0.f), make_float2(0.f, 0.f)}, self, dg);
-#pragma unroll
-  for (int k = 0; k < 3; k++) {
-    const Sp32 h = blk_mul(HsD[(2 * k) * per + lc], HsD[(2 * k + 1) * per + lc], mn[k]);
-    di = sp_add(di, h, 1.f);
+    for (int k = 0; k < 3; k++)
+      di = sp_add(di, blk_mul(HsD[(2 * k) * per + lc], HsD[(2 * k + 1) * per + lc], mn[k]), 1.f);
   }
-  Sp32 o = sp_add(Sp32{make_float2(0.f, 0.f), make_float2(0.f, 0.f)}, di, dg);
-  o = sp_add(o, self, sig);
+  SDm[lc] = sp2f4(di);
+  __syncthreads();
+  Sp32 o = zero;
+  if (ok) {
+    o = sp_add(sp_add(zero, di, dg), self, sig);
 #pragma unroll
-  for (int k = 0; k < 3; k++) {
-    const int j = jj[k];
-    Sp32 dj = sp_add(Sp32{make_float2(0.f, 0.f), make_float2(0.f, 0.f)}, mn[k], __ldg(diag32 + j));
+    for (int k = 0; k < 3; k++) {
+      const int j = jj[k];
+      const int l = j - blk0;
+      Sp32 dj;
+      if (unsigned(l) < unsigned(per)) {
+        dj = f42sp(SDm[l]);
+      } else {
+        dj = sp_add(zero, mn[k], __ldg(diag32 + j));
 #pragma unroll
-    for (int q = 0; q < 3; q++) {
-      const float4* hm = reinterpret_cast<const float4*>(H32 + size_t(q) * Ns + j);
-      dj = sp_add(dj, blk_mul(__ldg(hm), __ldg(hm + 1), m2[3 * k + q]), 1.f);
+        for (int q = 0; q < 3; q++) {
+          const float4* hm = reinterpret_cast<const float4*>(H32 + size_t(q) * Ns + j);
+          dj = sp_add(dj, blk_mul(__ldg(hm), __ldg(hm + 1), hl32<P>(halo, nb2[(3 * k + q) * per + lc])), 1.f);
+        }
+      }
+      o = sp_add(o, blk_mul(HsDd[(2 * k) * per + lc], HsDd[(2 * k + 1) * per + lc], dj), 1.f);
     }
-    o = sp_add(o, blk_mul(HsDd[(2 * k) * per + lc], HsDd[(2 * k + 1) * per + lc], dj), 1.f);
   }
+  __syncthreads();  // SDm is read before the next call overwrites it
   return o;
 }
 
@@ -601,6 +616,14 @@ __global__ void __launch_bounds__(576, 1) k_ppcg(PcgArgs a) {
   float4* HsD = S + NW * per;
   float4* HsDd = HsD + 6 * per;
   int* nb2 = reinterpret_cast<int*>(HsDd + 6 * per);
+  float4* SDm = reinterpret_cast<float4*>(nb2 + 9 * per);  // (D m) of the owned sites
+  // thread-private slots (each thread touches only its own entry): the
+  // recurrence vectors z, q, s and the fp32 solution increment live in shared
+  // memory to keep the registers for the preconditioner
+  float4* SZ = SDm + per;
+  float4* SQ = SZ + per;
+  float4* SS = SQ + per;
+  float4* SX = SS + per;
   const int lc = threadIdx.x;  // one site per thread
   const int i = blk0 + lc;
   const bool ok = i < Ns;
@@ -626,11 +649,15 @@ __global__ void __launch_bounds__(576, 1) k_ppcg(PcgArgs a) {
     for (int q = 0; q < 3; q++) nb2[(3 * k + q) * per + lc] = ok ? __ldg(a.nbr + q * Ns + jj[0][k]) : 0;
   const float sig = float(a.shift);
   auto A2 = [&](const Sp32& self, const void* halo) {
-    return ok ? two_hop<P>(i, lc, per, Ns, jj[0], nb2, a.H32, a.diag32, HsD, HsDd, dg, sig, self, halo) : z32;
+    return two_hop<P>(ok, i, lc, blk0, per, Ns, jj[0], nb2, a.H32, a.diag32, HsD, HsDd, SDm, dg, sig, self, halo);
   };
 
   Sp32 r[1] = {z32}, u[1] = {z32}, m[1] = {z32};
-  Sp32 w = z32, zz = z32, q = z32, s = z32, p = z32, xl = z32;
+  Sp32 w = z32, p = z32;
+  SZ[lc] = zf;
+  SQ[lc] = zf;
+  SS[lc] = zf;
+  SX[lc] = zf;
   // ---- phase 0: r = b, u = N r; |b|^2 -----------------------------------------------
   double v1[1] = {0.0};
   if (ok) {
@@ -696,12 +723,13 @@ __global__ void __launch_bounds__(576, 1) k_ppcg(PcgArgs a) {
         // ---- residual replacement: R0 fold and publish x ----------------------------------
         Sp64 xh{make_double2(0, 0), make_double2(0, 0)};
         if (ok) {
+          const Sp32 xl = f42sp(SX[lc]);
           xh = hl64(a.x, i);
           xh.s0 = make_double2(xh.s0.x + xl.s0.x, xh.s0.y + xl.s0.y);
           xh.s1 = make_double2(xh.s1.x + xl.s1.x, xh.s1.y + xl.s1.y);
           hs64(a.x, i, xh);
         }
-        xl = z32;
+        SX[lc] = zf;
         if (!grid_sync2(a.bar, epoch, a.spin_limit)) goto timeout;
         // ---- R1: t64 = D x ------------------------------------------------------------------
         if (ok) hs64(a.t64, i, stencil64(i, Ns, jj[0], a.H, a.diag, xh, a.x));
@@ -741,13 +769,15 @@ __global__ void __launch_bounds__(576, 1) k_ppcg(PcgArgs a) {
         mu_max = mu_true;
         // ---- R3: w = A u, s = A p, q = N s, m = N w; publish q, m; line-search dots ------
         w = A2(u[0], a.halo_u);
-        s = A2(p, a.halo_p);
+        const Sp32 s = A2(p, a.halo_p);
+        SS[lc] = sp2f4(s);
         Sp32 qq[1];
         {
           const Sp32 sv[1] = {s};
           pc_apply<NW, 1, true>(a, S, HsD, blk0, own, loc, val, jj, sv, qq);
         }
-        q = qq[0];
+        const Sp32 q = qq[0];
+        SQ[lc] = sp2f4(q);
         {
           const Sp32 wv[1] = {w};
           pc_apply<NW, 1, true>(a, S, HsD, blk0, own, loc, val, jj, wv, m);
@@ -773,17 +803,20 @@ __global__ void __launch_bounds__(576, 1) k_ppcg(PcgArgs a) {
         const double pap = t5[2] + beta * t5[3] + beta * beta * t5[4];
         alpha = rp / pap;
         // ---- R4: z = A q, n = A m -------------------------------------------------------
-        zz = A2(q, a.halo_q);
+        SZ[lc] = sp2f4(A2(f42sp(SQ[lc]), a.halo_q));
         n = A2(m[0], a.halo_z);
       }
       // ---- recurrences -------------------------------------------------------------------
       {
         const float al = float(alpha), bt = float(beta);
-        zz = sp_add(n, zz, bt);
-        q = sp_add(m[0], q, bt);
-        s = sp_add(w, s, bt);
+        const Sp32 zz = sp_add(n, f42sp(SZ[lc]), bt);
+        const Sp32 q = sp_add(m[0], f42sp(SQ[lc]), bt);
+        const Sp32 s = sp_add(w, f42sp(SS[lc]), bt);
         p = sp_add(u[0], p, bt);
-        xl = sp_add(xl, p, al);
+        SZ[lc] = sp2f4(zz);
+        SQ[lc] = sp2f4(q);
+        SS[lc] = sp2f4(s);
+        SX[lc] = sp2f4(sp_add(f42sp(SX[lc]), p, al));
         r[0] = sp_add(r[0], s, -al);
         u[0] = sp_add(u[0], q, -al);
         w = sp_add(w, zz, -al);
@@ -844,7 +877,7 @@ static const void* ppcg_kernel(int prec, int nw) {
 static bool ppcg_plan(int prec, int nw, int Ns, int per, int sm_count, int* grid, size_t* smem) {
   if (per % 32 || per > 576) return false;
   const void* fn = ppcg_kernel(prec, nw);
-  const size_t sm = size_t(nw + 12) * per * sizeof(float4) + size_t(9) * per * sizeof(int);
+  const size_t sm = size_t(nw + 17) * per * sizeof(float4) + size_t(9) * per * sizeof(int);
   if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(sm)) != cudaSuccess) {
     cudaGetLastError();
     return false;
@@ -905,10 +938,12 @@ int pcg_solve(qed3_dirac_s* d, qed3_lpc_s* L, double* x, const double* b, const 
   LpcWordCoef co;
   if ((rc = lpc_word_coef_cached(L, &co))) return rc;
   const bool flexible = prm && (prm->flags & QED3_SOLVE_FLEXIBLE);
-  const bool two_barrier = flexible || (prm && (prm->flags & QED3_SOLVE_TWO_BARRIER));
+  // the pipelined recurrence is FP32-only: with BF16 gathered copies its
+  // auxiliary vectors drift apart (measured: 43,000 instead of 240 iterations)
+  const bool want_pipe = prm && (prm->flags & QED3_SOLVE_PIPELINED) && !flexible && prec == QED3_PREC_F32;
   int grid = 0, threads = 0, spt = 0;
   size_t smem = 0;
-  const bool pipelined = !two_barrier && ppcg_plan(prec, co.nwords, d->Ns, L->per, d->sm_count, &grid, &smem);
+  const bool pipelined = want_pipe && ppcg_plan(prec, co.nwords, d->Ns, L->per, d->sm_count, &grid, &smem);
   if (!pipelined && !pcg_plan(prec, co.nwords, d->Ns, L->per, d->sm_count, &grid, &threads, &spt, &smem))
     return fail(QED3_ERR_ARG, "lattice too large for the register-resident preconditioned solver");
   if ((rc = field_import(d, QED3_PREC_F64, w.b, b, 1, st))) return rc;
