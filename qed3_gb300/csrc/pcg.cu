@@ -564,17 +564,33 @@ __device__ __forceinline__ Sp32 blk_mul(const float4& r0, const float4& r1, cons
 // is then read from SDm, that of a neighbour owned by another block is
 // recomputed here from the gathered field (nb2[(3k+q) * per + lc] =
 // nbr(nbr(i,k), q)) and that neighbour's hop blocks.
-template <int P>
+template <int P, bool TRAIL>
 __device__ __forceinline__ Sp32 two_hop(bool ok, int i, int lc, int blk0, int per, int Ns, const int (&jj)[3],
                                         const int* nb2, const M32* __restrict__ H32,
                                         const float* __restrict__ diag32, const float4* HsD, const float4* HsDd,
                                         float4* SDm, float dg, float sig, const Sp32& self, const void* halo) {
   const Sp32 zero{make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
   Sp32 mn[3] = {zero, zero, zero};
+  Sp32 dj[3] = {zero, zero, zero};  // (D m)_j of neighbours owned by other blocks
   Sp32 di = zero;
   if (ok) {
+    // one round of loads: the three neighbours, and for neighbours owned by
+    // another block their neighbours and hop blocks as well
 #pragma unroll
     for (int k = 0; k < 3; k++) mn[k] = hl32<P>(halo, jj[k]);
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+      const int j = jj[k];
+      if (unsigned(j - blk0) >= unsigned(per)) {
+        Sp32 acc = zero;
+#pragma unroll
+        for (int q = 0; q < 3; q++) {
+          const float4* hm = reinterpret_cast<const float4*>(H32 + size_t(q) * Ns + j);
+          acc = sp_add(acc, blk_mul(__ldg(hm), __ldg(hm + 1), hl32<P>(halo, nb2[(3 * k + q) * per + lc])), 1.f);
+        }
+        dj[k] = sp_add(acc, mn[k], __ldg(diag32 + j));
+      }
+    }
     di = sp_add(zero, self, dg);
 #pragma unroll
     for (int k = 0; k < 3; k++)
@@ -587,23 +603,12 @@ __device__ __forceinline__ Sp32 two_hop(bool ok, int i, int lc, int blk0, int pe
     o = sp_add(sp_add(zero, di, dg), self, sig);
 #pragma unroll
     for (int k = 0; k < 3; k++) {
-      const int j = jj[k];
-      const int l = j - blk0;
-      Sp32 dj;
-      if (unsigned(l) < unsigned(per)) {
-        dj = f42sp(SDm[l]);
-      } else {
-        dj = sp_add(zero, mn[k], __ldg(diag32 + j));
-#pragma unroll
-        for (int q = 0; q < 3; q++) {
-          const float4* hm = reinterpret_cast<const float4*>(H32 + size_t(q) * Ns + j);
-          dj = sp_add(dj, blk_mul(__ldg(hm), __ldg(hm + 1), hl32<P>(halo, nb2[(3 * k + q) * per + lc])), 1.f);
-        }
-      }
-      o = sp_add(o, blk_mul(HsDd[(2 * k) * per + lc], HsDd[(2 * k + 1) * per + lc], dj), 1.f);
+      const int l = jj[k] - blk0;
+      const Sp32 d = (unsigned(l) < unsigned(per)) ? f42sp(SDm[l]) : dj[k];
+      o = sp_add(o, blk_mul(HsDd[(2 * k) * per + lc], HsDd[(2 * k + 1) * per + lc], d), 1.f);
     }
   }
-  __syncthreads();  // SDm is read before the next call overwrites it
+  if (TRAIL) __syncthreads();  // SDm is read before a following call overwrites it
   return o;
 }
 
@@ -648,8 +653,14 @@ __global__ void __launch_bounds__(576, 1) k_ppcg(PcgArgs a) {
 #pragma unroll
     for (int q = 0; q < 3; q++) nb2[(3 * k + q) * per + lc] = ok ? __ldg(a.nbr + q * Ns + jj[0][k]) : 0;
   const float sig = float(a.shift);
+  // A2: the next write of SDm is behind a grid barrier; A2t: another A2 follows
   auto A2 = [&](const Sp32& self, const void* halo) {
-    return two_hop<P>(ok, i, lc, blk0, per, Ns, jj[0], nb2, a.H32, a.diag32, HsD, HsDd, SDm, dg, sig, self, halo);
+    return two_hop<P, false>(ok, i, lc, blk0, per, Ns, jj[0], nb2, a.H32, a.diag32, HsD, HsDd, SDm, dg, sig, self,
+                             halo);
+  };
+  auto A2t = [&](const Sp32& self, const void* halo) {
+    return two_hop<P, true>(ok, i, lc, blk0, per, Ns, jj[0], nb2, a.H32, a.diag32, HsD, HsDd, SDm, dg, sig, self,
+                            halo);
   };
 
   Sp32 r[1] = {z32}, u[1] = {z32}, m[1] = {z32};
@@ -768,8 +779,8 @@ __global__ void __launch_bounds__(576, 1) k_ppcg(PcgArgs a) {
         }
         mu_max = mu_true;
         // ---- R3: w = A u, s = A p, q = N s, m = N w; publish q, m; line-search dots ------
-        w = A2(u[0], a.halo_u);
-        const Sp32 s = A2(p, a.halo_p);
+        w = A2t(u[0], a.halo_u);
+        const Sp32 s = A2t(p, a.halo_p);
         SS[lc] = sp2f4(s);
         Sp32 qq[1];
         {
@@ -803,7 +814,7 @@ __global__ void __launch_bounds__(576, 1) k_ppcg(PcgArgs a) {
         const double pap = t5[2] + beta * t5[3] + beta * beta * t5[4];
         alpha = rp / pap;
         // ---- R4: z = A q, n = A m -------------------------------------------------------
-        SZ[lc] = sp2f4(A2(f42sp(SQ[lc]), a.halo_q));
+        SZ[lc] = sp2f4(A2t(f42sp(SQ[lc]), a.halo_q));
         n = A2(m[0], a.halo_z);
       }
       // ---- recurrences -------------------------------------------------------------------
