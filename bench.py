@@ -228,9 +228,9 @@ def profile_case(torch, which):
         D.update(A)
         b = torch.from_numpy(Q.ParallelRng(lat, 7).gaussian_spinor()).cuda()
         x = torch.zeros_like(b)
-        if which == "pcg":  # untrained network: same per-iteration cost as a trained one
+        if which in ("pcg", "ppcg"):  # untrained network: same per-iteration cost as a trained one
             pc = Q.LearnedPreconditioner(D, channels=16, layers=2, seed=1)
-            rep = pc.solve(D, x, b, tol=TOL, precision=Q.PREC_F32, maxiter=300)
+            rep = pc.solve(D, x, b, tol=TOL, precision=Q.PREC_F32, maxiter=300, pipelined=which == "ppcg")
         else:
             rep = D.solve(x, b, tol=TOL, precision=Q.PREC_F32)
         print(json.dumps(rep.__dict__))
@@ -252,10 +252,10 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--profile", choices=["apply", "cg", "pcg"], default=None,
+    ap.add_argument("--profile", choices=["apply", "cg", "pcg", "ppcg"], default=None,
                     help="small self-contained case for ncu: 'apply' = D apply at n=512 (f32, bf16, f64; "
                          "HBM-resident), 'cg' = one n=64 mixed-precision solve, 'pcg' = 300 iterations of the "
-                         "n=64 preconditioned solve")
+                         "n=64 preconditioned solve, 'ppcg' = the same with the pipelined one-barrier kernel")
     args = ap.parse_args()
     rank, world, local = env_rank()
     warmup = max(3, args.warmup)
