@@ -163,10 +163,6 @@ __device__ __forceinline__ void pc_apply(const PcgArgs& a, float4* S, const floa
     __syncthreads();
 #pragma unroll
     for (int k = 0; k < SPT; k++) {
-      Sp32 f[7];
-      f[0] = r[k];
-      f[1] = f42sp(S1[loc[k]]);
-      f[2] = f42sp(S2[loc[k]]);
       Sp32 o[4];
       o[0] = o[1] = o[2] = o[3] = zero;
       if (val[k]) {
@@ -174,23 +170,29 @@ __device__ __forceinline__ void pc_apply(const PcgArgs& a, float4* S, const floa
         const int md[2] = {3, 3};
         hop_pass<HS, 2>(F, md, jj[k], blk0, per, own[k], loc[k], Ns, a.H32, Hs, o);
       }
-      f[3] = o[0];  // Hd Hd r
-      f[4] = o[1];  // Hd Ho r
-      f[5] = o[2];  // Ho Hd r
-      f[6] = o[3];  // Ho Ho r
+      // park the length-2 words in this site's own slots (f3 = Hd Hd r, f4 = Hd Ho r,
+      // f5 = Ho Hd r, f6 = Ho Ho r), then stream the seven words through the 7 x 7
+      // product one at a time; g3..g6 replace them in the same own slots
+      S3[loc[k]] = sp2f4(o[0]);
+      S4[loc[k]] = sp2f4(o[1]);
+      S5[loc[k]] = sp2f4(o[2]);
+      S6[loc[k]] = sp2f4(o[3]);
+      Sp32 g[7];
 #pragma unroll
-      for (int w = 0; w < 7; w++) {
-        Sp32 g = zero;
+      for (int w = 0; w < 7; w++) g[w] = zero;
 #pragma unroll
-        for (int q = 0; q < 7; q++) acc_c(g, a.pc.M[w][q], f[q]);
-        if (w == 0) g0[k] = g;
-        else if (w == 1) g1[k] = g;
-        else if (w == 2) g2[k] = g;
-        else if (w == 3) S3[loc[k]] = sp2f4(g);
-        else if (w == 4) S4[loc[k]] = sp2f4(g);
-        else if (w == 5) S5[loc[k]] = sp2f4(g);
-        else S6[loc[k]] = sp2f4(g);
+      for (int qw = 0; qw < 7; qw++) {
+        const Sp32 f = qw == 0 ? r[k] : f42sp((S + qw * per)[loc[k]]);
+#pragma unroll
+        for (int w = 0; w < 7; w++) acc_c(g[w], a.pc.M[w][qw], f);
       }
+      g0[k] = g[0];
+      g1[k] = g[1];
+      g2[k] = g[2];
+      S3[loc[k]] = sp2f4(g[3]);
+      S4[loc[k]] = sp2f4(g[4]);
+      S5[loc[k]] = sp2f4(g[5]);
+      S6[loc[k]] = sp2f4(g[6]);
     }
     __syncthreads();
 #pragma unroll
@@ -612,6 +614,28 @@ __device__ __forceinline__ Sp32 two_hop(bool ok, int i, int lc, int blk0, int pe
   return o;
 }
 
+// the recurrences of one pipelined step (z, q, s and the solution increment
+// in the thread's shared slots)
+__device__ __forceinline__ void ppcg_step(double alpha, double beta, const Sp32& n, const Sp32& m, Sp32& r, Sp32& u,
+                                          Sp32& w, Sp32& p, float4* SZ, float4* SQ, float4* SS, float4* SX, int lc) {
+  const float al = float(alpha), bt = float(beta);
+  const Sp32 zz = sp_add(n, f42sp(SZ[lc]), bt);
+  const Sp32 q = sp_add(m, f42sp(SQ[lc]), bt);
+  const Sp32 s = sp_add(w, f42sp(SS[lc]), bt);
+  p = sp_add(u, p, bt);
+  SZ[lc] = sp2f4(zz);
+  SQ[lc] = sp2f4(q);
+  SS[lc] = sp2f4(s);
+  SX[lc] = sp2f4(sp_add(f42sp(SX[lc]), p, al));
+  r = sp_add(r, s, -al);
+  u = sp_add(u, q, -al);
+  w = sp_add(w, zz, -al);
+}
+
+// Phases of k_ppcg around its single preconditioner application (one inlined
+// copy: five copies of the 7-word preconditioner spilled to local memory).
+enum PpcgPhase { PH_INIT = 0, PH_MAIN = 1, PH_R2 = 2, PH_R3A = 3, PH_R3B = 4 };
+
 template <int P, int NW>
 __global__ void __launch_bounds__(576, 1) k_ppcg(PcgArgs a) {
   extern __shared__ float4 S[];
@@ -652,208 +676,203 @@ __global__ void __launch_bounds__(576, 1) k_ppcg(PcgArgs a) {
   for (int k = 0; k < 3; k++)
 #pragma unroll
     for (int q = 0; q < 3; q++) nb2[(3 * k + q) * per + lc] = ok ? __ldg(a.nbr + q * Ns + jj[0][k]) : 0;
-  const float sig = float(a.shift);
-  // A2: the next write of SDm is behind a grid barrier; A2t: another A2 follows
-  auto A2 = [&](const Sp32& self, const void* halo) {
-    return two_hop<P, false>(ok, i, lc, blk0, per, Ns, jj[0], nb2, a.H32, a.diag32, HsD, HsDd, SDm, dg, sig, self,
-                             halo);
-  };
-  auto A2t = [&](const Sp32& self, const void* halo) {
-    return two_hop<P, true>(ok, i, lc, blk0, per, Ns, jj[0], nb2, a.H32, a.diag32, HsD, HsDd, SDm, dg, sig, self,
-                            halo);
-  };
-
-  Sp32 r[1] = {z32}, u[1] = {z32}, m[1] = {z32};
-  Sp32 w = z32, p = z32;
   SZ[lc] = zf;
   SQ[lc] = zf;
   SS[lc] = zf;
   SX[lc] = zf;
-  // ---- phase 0: r = b, u = N r; |b|^2 -----------------------------------------------
-  double v1[1] = {0.0};
+  const float sig = float(a.shift);
+  // A2(x, halo): (D^dag D + s) x from the gathered copy; the next write of SDm
+  // is behind a grid barrier.  A2T: another A2 follows directly.
+  const M32* const H32g = a.H32;
+  const float* const dg32g = a.diag32;
+#define A2(x, halo) two_hop<P, false>(ok, i, lc, blk0, per, Ns, jj[0], nb2, H32g, dg32g, HsD, HsDd, SDm, dg, sig, x, halo)
+#define A2T(x, halo) two_hop<P, true>(ok, i, lc, blk0, per, Ns, jj[0], nb2, H32g, dg32g, HsD, HsDd, SDm, dg, sig, x, halo)
+
+  Sp32 r = z32, u = z32, w = z32, p = z32;
   if (ok) {
     const Sp64 bi = ld64(a.b, i);
-    v1[0] = n2(bi);
-    r[0] = Sp32{make_float2(float(bi.s0.x), float(bi.s0.y)), make_float2(float(bi.s1.x), float(bi.s1.y))};
+    r = Sp32{make_float2(float(bi.s0.x), float(bi.s0.y)), make_float2(float(bi.s1.x), float(bi.s1.y))};
   }
-  pc_apply<NW, 1, true>(a, S, HsD, blk0, own, loc, val, jj, r, u);
-  if (ok) hs32<P>(a.halo_u, i, u[0]);
   unsigned int epoch = 0;
   int parity = 0;
-  v2_publish<1>(v1, a.partials, parity, sh);
-  if (!grid_sync2(a.bar, epoch, a.spin_limit)) goto timeout;
-  {
-    double tot[1];
-    v2_total<1>(a.partials, parity, tot, sh);
-    parity ^= 1;
-    const double bnorm2 = tot[0];
-    double mu_true = bnorm2, mu_max = bnorm2, gam_old = 0.0, al_old = 0.0;
-    int iter = 0, nru = 0, status = QED3_ERR_NOCONV;
-    bool first = true;
-    if (bnorm2 == 0.0) {
-      status = QED3_OK;
-      mu_true = 0.0;
-      goto finish;
+  double bnorm2 = 0.0, mu_true = 0.0, mu_max = 0.0, gam_old = 0.0, al_old = 0.0, ru_part = 0.0;
+  int iter = 0, nru = 0, status = QED3_ERR_NOCONV;
+  bool first = true;
+  int phase = PH_INIT;
+  while (true) {
+    // ---- the single preconditioner application: u = N r (INIT, R2), m = N w (MAIN,
+    //      R3B), q = N s (R3A) ----------------------------------------------------------
+    Sp32 pin[1], pout[1];
+    pin[0] = (phase == PH_INIT || phase == PH_R2) ? r : (phase == PH_R3A ? f42sp(SS[lc]) : w);
+    pc_apply<NW, 1, true>(a, S, HsD, blk0, own, loc, val, jj, pin, pout);
+    if (phase == PH_INIT) {
+      u = pout[0];
+      double v1[1] = {0.0};
+      if (ok) {
+        v1[0] = n2(ld64(a.b, i));
+        hs32<P>(a.halo_u, i, u);
+      }
+      v2_publish<1>(v1, a.partials, parity, sh);
+      if (!grid_sync2(a.bar, epoch, a.spin_limit)) goto timeout;
+      double tot[1];
+      v2_total<1>(a.partials, parity, tot, sh);
+      parity ^= 1;
+      bnorm2 = tot[0];
+      mu_true = mu_max = bnorm2;
+      if (bnorm2 == 0.0) {
+        status = QED3_OK;
+        break;
+      }
+      w = A2(u, a.halo_u);
+      phase = PH_MAIN;
+      continue;
     }
-    w = A2(u[0], a.halo_u);
-    while (true) {
-      // ---- dots of (r, u, w), m = N w, publish m | barrier -----------------------------
+    if (phase == PH_MAIN) {
+      // ---- dots of (r, u, w), publish m = N w | barrier | totals ------------------------
+      const Sp32 m = pout[0];
       float v[3] = {0.f, 0.f, 0.f};
       if (ok) {
-        v[0] = rdotf(r[0], u[0]);
-        v[1] = rdotf(w, u[0]);
-        v[2] = n2f(r[0]);
+        v[0] = rdotf(r, u);
+        v[1] = rdotf(w, u);
+        v[2] = n2f(r);
+        hs32<P>(a.halo_z, i, m);
       }
-      {
-        const Sp32 wv[1] = {w};
-        pc_apply<NW, 1, true>(a, S, HsD, blk0, own, loc, val, jj, wv, m);
-      }
-      if (ok) hs32<P>(a.halo_z, i, m[0]);
       v2_publish_f<3>(v, a.partials, parity, sh);
       if (!grid_sync2(a.bar, epoch, a.spin_limit)) goto timeout;
       double t3[3];
       v2_total<3>(a.partials, parity, t3, sh);
       parity ^= 1;
-      double gam = t3[0];
-      const double dl = t3[1], mu = t3[2];
+      const double gam = t3[0], dl = t3[1], mu = t3[2];
       mu_max = fmax(mu_max, mu);
-      double alpha, beta;
-      Sp32 n;
       const bool want = !first && (!isfinite(mu) || !(gam > 0.0) || mu < a.tol2 * bnorm2 || iter >= a.maxiter ||
                                    mu < a.delta2 * mu_max);
       if (!want) {
-        if (first) {
-          beta = 0.0;
-          alpha = gam / dl;
-        } else {
-          beta = gam / gam_old;
-          alpha = gam / (dl - beta * gam / al_old);
-        }
-        n = A2(m[0], a.halo_z);
-      } else {
-        // ---- residual replacement: R0 fold and publish x ----------------------------------
-        Sp64 xh{make_double2(0, 0), make_double2(0, 0)};
-        if (ok) {
-          const Sp32 xl = f42sp(SX[lc]);
-          xh = hl64(a.x, i);
-          xh.s0 = make_double2(xh.s0.x + xl.s0.x, xh.s0.y + xl.s0.y);
-          xh.s1 = make_double2(xh.s1.x + xl.s1.x, xh.s1.y + xl.s1.y);
-          hs64(a.x, i, xh);
-        }
-        SX[lc] = zf;
-        if (!grid_sync2(a.bar, epoch, a.spin_limit)) goto timeout;
-        // ---- R1: t64 = D x ------------------------------------------------------------------
-        if (ok) hs64(a.t64, i, stencil64(i, Ns, jj[0], a.H, a.diag, xh, a.x));
-        if (!grid_sync2(a.bar, epoch, a.spin_limit)) goto timeout;
-        // ---- R2: r = b - D^dag t64 - s x (FP64), u = N r; publish u, p ---------------------
-        double vv[1] = {0.0};
-        if (ok) {
-          const Sp64 self = hl64(a.t64, i);
-          const Sp64 qd = stencil64(i, Ns, jj[0], a.Hd, a.diag, self, a.t64);
-          const Sp64 bi = ld64(a.b, i);
-          Sp64 rt;
-          rt.s0 = csub(bi.s0, cadd(qd.s0, cscale(a.shift, xh.s0)));
-          rt.s1 = csub(bi.s1, cadd(qd.s1, cscale(a.shift, xh.s1)));
-          vv[0] = n2(rt);
-          r[0] = Sp32{make_float2(float(rt.s0.x), float(rt.s0.y)), make_float2(float(rt.s1.x), float(rt.s1.y))};
-        }
-        pc_apply<NW, 1, true>(a, S, HsD, blk0, own, loc, val, jj, r, u);
-        if (ok) {
-          hs32<P>(a.halo_u, i, u[0]);
-          hs32<P>(a.halo_p, i, p);
-        }
-        v2_publish<1>(vv, a.partials, parity, sh);
-        if (!grid_sync2(a.bar, epoch, a.spin_limit)) goto timeout;
-        double tr[1];
-        v2_total<1>(a.partials, parity, tr, sh);
-        parity ^= 1;
-        nru++;
-        mu_true = tr[0];
-        if (mu_true < a.tol2 * bnorm2) {
-          status = QED3_OK;
-          break;
-        }
-        if (iter >= a.maxiter || !isfinite(mu_true)) {
-          status = QED3_ERR_NOCONV;
-          break;
-        }
-        mu_max = mu_true;
-        // ---- R3: w = A u, s = A p, q = N s, m = N w; publish q, m; line-search dots ------
-        w = A2t(u[0], a.halo_u);
-        const Sp32 s = A2t(p, a.halo_p);
-        SS[lc] = sp2f4(s);
-        Sp32 qq[1];
-        {
-          const Sp32 sv[1] = {s};
-          pc_apply<NW, 1, true>(a, S, HsD, blk0, own, loc, val, jj, sv, qq);
-        }
-        const Sp32 q = qq[0];
-        SQ[lc] = sp2f4(q);
-        {
-          const Sp32 wv[1] = {w};
-          pc_apply<NW, 1, true>(a, S, HsD, blk0, own, loc, val, jj, wv, m);
-        }
-        float v5[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
-        if (ok) {
-          hs32<P>(a.halo_q, i, q);
-          hs32<P>(a.halo_z, i, m[0]);
-          v5[0] = rdotf(r[0], u[0]);
-          v5[1] = rdotf(r[0], p);
-          v5[2] = rdotf(u[0], w);
-          v5[3] = rdotf(u[0], s) + rdotf(p, w);
-          v5[4] = rdotf(p, s);
-        }
-        v2_publish_f<5, 8>(v5, a.partials, parity, sh);
-        if (!grid_sync2(a.bar, epoch, a.spin_limit)) goto timeout;
-        double t5[5];
-        v2_total<5, 8>(a.partials, parity, t5, sh);
-        parity ^= 1;
-        gam = t5[0];
-        beta = gam / gam_old;
-        const double rp = gam + beta * t5[1];
-        const double pap = t5[2] + beta * t5[3] + beta * beta * t5[4];
-        alpha = rp / pap;
-        // ---- R4: z = A q, n = A m -------------------------------------------------------
-        SZ[lc] = sp2f4(A2t(f42sp(SQ[lc]), a.halo_q));
-        n = A2(m[0], a.halo_z);
+        const double beta = first ? 0.0 : gam / gam_old;
+        const double alpha = first ? gam / dl : gam / (dl - beta * gam / al_old);
+        const Sp32 n = A2(m, a.halo_z);
+        ppcg_step(alpha, beta, n, m, r, u, w, p, SZ, SQ, SS, SX, lc);
+        gam_old = gam;
+        al_old = alpha;
+        first = false;
+        iter++;
+        continue;
       }
-      // ---- recurrences -------------------------------------------------------------------
-      {
-        const float al = float(alpha), bt = float(beta);
-        const Sp32 zz = sp_add(n, f42sp(SZ[lc]), bt);
-        const Sp32 q = sp_add(m[0], f42sp(SQ[lc]), bt);
-        const Sp32 s = sp_add(w, f42sp(SS[lc]), bt);
-        p = sp_add(u[0], p, bt);
-        SZ[lc] = sp2f4(zz);
-        SQ[lc] = sp2f4(q);
-        SS[lc] = sp2f4(s);
-        SX[lc] = sp2f4(sp_add(f42sp(SX[lc]), p, al));
-        r[0] = sp_add(r[0], s, -al);
-        u[0] = sp_add(u[0], q, -al);
-        w = sp_add(w, zz, -al);
+      // ---- residual replacement: R0 fold and publish x ------------------------------------
+      Sp64 xh{make_double2(0, 0), make_double2(0, 0)};
+      if (ok) {
+        const Sp32 xl = f42sp(SX[lc]);
+        xh = hl64(a.x, i);
+        xh.s0 = make_double2(xh.s0.x + xl.s0.x, xh.s0.y + xl.s0.y);
+        xh.s1 = make_double2(xh.s1.x + xl.s1.x, xh.s1.y + xl.s1.y);
+        hs64(a.x, i, xh);
       }
+      SX[lc] = zf;
+      if (!grid_sync2(a.bar, epoch, a.spin_limit)) goto timeout;
+      // ---- R1: t64 = D x ------------------------------------------------------------------
+      if (ok) hs64(a.t64, i, stencil64(i, Ns, jj[0], a.H, a.diag, xh, a.x));
+      if (!grid_sync2(a.bar, epoch, a.spin_limit)) goto timeout;
+      // ---- R2 (first half): r = b - D^dag t64 - s x in FP64 --------------------------------
+      ru_part = 0.0;
+      if (ok) {
+        const Sp64 self = hl64(a.t64, i);
+        const Sp64 qd = stencil64(i, Ns, jj[0], a.Hd, a.diag, self, a.t64);
+        const Sp64 bi = ld64(a.b, i);
+        Sp64 rt;
+        rt.s0 = csub(bi.s0, cadd(qd.s0, cscale(a.shift, xh.s0)));
+        rt.s1 = csub(bi.s1, cadd(qd.s1, cscale(a.shift, xh.s1)));
+        ru_part = n2(rt);
+        r = Sp32{make_float2(float(rt.s0.x), float(rt.s0.y)), make_float2(float(rt.s1.x), float(rt.s1.y))};
+      }
+      phase = PH_R2;  // u = N r next
+      continue;
+    }
+    if (phase == PH_R2) {
+      // ---- R2 (second half): publish u = N r and p | barrier | certificate ----------------
+      u = pout[0];
+      if (ok) {
+        hs32<P>(a.halo_u, i, u);
+        hs32<P>(a.halo_p, i, p);
+      }
+      double vv[1] = {ru_part};
+      v2_publish<1>(vv, a.partials, parity, sh);
+      if (!grid_sync2(a.bar, epoch, a.spin_limit)) goto timeout;
+      double tr[1];
+      v2_total<1>(a.partials, parity, tr, sh);
+      parity ^= 1;
+      nru++;
+      mu_true = tr[0];
+      if (mu_true < a.tol2 * bnorm2) {
+        status = QED3_OK;
+        break;
+      }
+      if (iter >= a.maxiter || !isfinite(mu_true)) {
+        status = QED3_ERR_NOCONV;
+        break;
+      }
+      mu_max = mu_true;
+      // ---- R3: w = A u, s = A p (q = N s, m = N w follow) --------------------------------
+      w = A2T(u, a.halo_u);
+      SS[lc] = sp2f4(A2T(p, a.halo_p));
+      phase = PH_R3A;
+      continue;
+    }
+    if (phase == PH_R3A) {
+      SQ[lc] = sp2f4(pout[0]);
+      phase = PH_R3B;
+      continue;
+    }
+    // ---- PH_R3B: publish q, m; line-search dots | barrier | z = A q, n = A m, step ------
+    {
+      const Sp32 m = pout[0];
+      const Sp32 q = f42sp(SQ[lc]), sv = f42sp(SS[lc]);
+      float v5[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
+      if (ok) {
+        hs32<P>(a.halo_q, i, q);
+        hs32<P>(a.halo_z, i, m);
+        v5[0] = rdotf(r, u);
+        v5[1] = rdotf(r, p);
+        v5[2] = rdotf(u, w);
+        v5[3] = rdotf(u, sv) + rdotf(p, w);
+        v5[4] = rdotf(p, sv);
+      }
+      v2_publish_f<5, 8>(v5, a.partials, parity, sh);
+      if (!grid_sync2(a.bar, epoch, a.spin_limit)) goto timeout;
+      double t5[5];
+      v2_total<5, 8>(a.partials, parity, t5, sh);
+      parity ^= 1;
+      const double gam = t5[0];
+      const double beta = gam / gam_old;
+      const double rp = gam + beta * t5[1];
+      const double pap = t5[2] + beta * t5[3] + beta * beta * t5[4];
+      const double alpha = rp / pap;
+      SZ[lc] = sp2f4(A2T(q, a.halo_q));
+      const Sp32 n = A2(m, a.halo_z);
+      ppcg_step(alpha, beta, n, m, r, u, w, p, SZ, SQ, SS, SX, lc);
       gam_old = gam;
       al_old = alpha;
       first = false;
       iter++;
+      phase = PH_MAIN;
     }
-  finish:
-    if (blockIdx.x == 0 && threadIdx.x == 0) {
-      a.scal[0] = mu_true;
-      a.scal[1] = bnorm2;
-      a.scal[2] = iter;
-      a.scal[3] = nru;
-      a.scal[4] = status;
-      a.scal[5] = 0;
-    }
-    return;
   }
+  // finish: x was published at the last residual replacement (or is zero)
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    a.scal[0] = mu_true;
+    a.scal[1] = bnorm2;
+    a.scal[2] = iter;
+    a.scal[3] = nru;
+    a.scal[4] = status;
+    a.scal[5] = 0;
+  }
+  return;
 timeout:
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     a.scal[4] = QED3_ERR_TIMEOUT;
     a.scal[5] = 0;
   }
 }
+#undef A2
+#undef A2T
 
 // ---------------------------------------------------------------------------
 // host side
