@@ -254,6 +254,16 @@ int qed3_overlap_force(qed3_overlap* ov, const double* eta, double* F, double to
 int qed3_overlap_solve(qed3_overlap* ov, double* x, const double* b, double tol, double tol_inner, int maxiter,
                        qed3_solve_report* report, void* stream);
 
+/* Multi-shift CG: x[m] = (D^dag D + shifts[m])^{-1} b for m < nshifts (<= 64),
+ * all shifts in one Krylov space (one D^dag D per iteration for all shifts),
+ * FP64 -- replaces the per-pole MatPoly::solve calls of Overlap
+ * (src/both_3d/overlap.h:309-358).  shifts: host, >= 0; x: device complex128,
+ * nshifts vectors back to back; b: device complex128 (reference order).
+ * reports[m] (host, may be NULL): iterations at which shift m stopped, its
+ * FP64 true residual ||b - (D^dag D + shift) x|| / ||b||, status; ms: device time. */
+int qed3_multishift_solve(qed3_dirac* d, int nshifts, const double* shifts, double* x, const double* b, double tol,
+                          int maxiter, qed3_solve_report* reports, float* ms, void* stream);
+
 /* ======================================================================
  * Zolotarev coefficients  --  replaces Zolotarev(k, n) / Zolotarev::update
  * (src/both_3d/overlap.h:7-116): r(x) = C x (1 + sum_m A[m]/(x^2 - k^2/cp[m])).

@@ -104,6 +104,8 @@ SIGNATURES = [
     ("qed3_overlap_force", ctypes.c_int, [vp, vp, vp, ctypes.c_double, ctypes.POINTER(SolveReport), vp]),
     ("qed3_overlap_solve", ctypes.c_int, [vp, vp, vp, ctypes.c_double, ctypes.c_double, ctypes.c_int,
                                           ctypes.POINTER(SolveReport), vp]),
+    ("qed3_multishift_solve", ctypes.c_int, [vp, ctypes.c_int, vp, vp, vp, ctypes.c_double, ctypes.c_int, vp,
+                                             ctypes.POINTER(ctypes.c_float), vp]),
     ("qed3_batch_create", ctypes.c_int, [ctypes.c_int, vp, vp, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                          ctypes.POINTER(vp)]),
     ("qed3_batch_destroy", ctypes.c_int, [vp]),
@@ -377,6 +379,17 @@ def thermalized_links(lattice: S2Trivalent, beta: float, seed: int, ntraj: int, 
         a, _ = hmc_pure_gauge(lattice, rng, A, beta, compact, True, 1.0, nsteps)
         acc += a
     return A, acc / max(1, ntraj)
+
+
+def multishift_solve(dirac: DiracS2Dual, x, b, shifts, tol: float = 1e-10, maxiter: int = 200000, stream=None):
+    """x[m] = (D^dag D + shifts[m])^{-1} b in one Krylov space (FP64 multi-shift CG).
+    x: device complex128 (nshifts, 2*n_sites); returns (reports, ms)."""
+    sh = np.ascontiguousarray(shifts, dtype=np.float64)
+    reps = (SolveReport * len(sh))()
+    ms = ctypes.c_float()
+    _check(lib().qed3_multishift_solve(dirac.handle, len(sh), _ptr(sh), _ptr(x), _ptr(b), tol, maxiter, reps,
+                                       ctypes.byref(ms), _stream(stream)))
+    return [Report(r.status, r.iters, r.reliable_updates, r.true_rel_res, r.ms) for r in reps], ms.value
 
 
 def point_source(lattice: S2Trivalent, x: int, s: int) -> np.ndarray:

@@ -15,6 +15,7 @@
 #include "gauge_impl.h"
 #include "handles.h"
 #include "lpc_impl.h"
+#include "mshift_impl.h"
 #include "overlap_impl.h"
 #include "pcg_impl.h"
 #include "qed3_internal.h"
@@ -455,6 +456,27 @@ int qed3_overlap_solve(qed3_overlap* ov, double* x, const double* b, double tol,
   if (x == b) return fail(QED3_ERR_ARG, "x must not alias b");
   return overlap_solve(ov, x, b, tol > 0 ? tol : 1e-10, tol_inner > 0 ? tol_inner : 1e-12,
                        maxiter > 0 ? maxiter : 10000, report, (cudaStream_t)stream);
+  QED3_GUARD_END
+}
+
+int qed3_multishift_solve(qed3_dirac* d, int nshifts, const double* shifts, double* x, const double* b, double tol,
+                          int maxiter, qed3_solve_report* reports, float* ms, void* stream) {
+  QED3_GUARD_BEGIN
+  if (!d || !shifts || !x || !b) return fail(QED3_ERR_ARG, "NULL argument");
+  if (nshifts < 1 || nshifts > kMsMaxShifts) return fail(QED3_ERR_ARG, "nshifts must be in [1, 64]");
+  const size_t bytes = size_t(nshifts) * d->Ns * 4 * sizeof(double);
+  void *X = nullptr, *P = nullptr;
+  if (cudaMalloc(&X, bytes) != cudaSuccess) return fail(QED3_ERR_NOMEM, "cudaMalloc failed");
+  if (cudaMalloc(&P, bytes) != cudaSuccess) {
+    cudaFree(X);
+    return fail(QED3_ERR_NOMEM, "cudaMalloc failed");
+  }
+  const int rc = mshift_solve(d, nshifts, shifts, b, x, reinterpret_cast<S64*>(X), reinterpret_cast<S64*>(P),
+                              tol > 0 ? tol : 1e-10, maxiter > 0 ? maxiter : 200000, reports, ms,
+                              (cudaStream_t)stream);
+  cudaFree(X);
+  cudaFree(P);
+  return rc;
   QED3_GUARD_END
 }
 

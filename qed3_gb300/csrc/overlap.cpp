@@ -21,6 +21,7 @@
 #include "blas_impl.h"
 #include "dirac_impl.h"
 #include "gauge_impl.h"
+#include "mshift_impl.h"
 #include "handles.h"
 #include "overlap_impl.h"
 #include "qed3_internal.h"
@@ -34,6 +35,7 @@ struct qed3_overlap_s {
   qed3_batch_s* batch = nullptr;     // poles nh..np-1 in the overlap's precision
   qed3_batch_s* batch_hi = nullptr;  // poles 0..nh-1 (ill-conditioned) in FP64
   int nh = 0, nlo = 0;               // current split
+  bool multishift = true;            // nh > 0: all poles through the FP64 multi-shift CG
   double* Z = nullptr;     // [npoles][2 Ns] complex
   double* y = nullptr;     // [2 Ns] complex
   double* w = nullptr;
@@ -44,6 +46,9 @@ struct qed3_overlap_s {
   double* Yp = nullptr;    // [npoles][2 Ns] complex
   double* fi = nullptr;    // [4 npoles + 2][Ns] internal-order two-spinors (4 doubles per site)
   double *sr = nullptr, *sp = nullptr, *sq = nullptr;
+  // multi-shift scratch (internal-order FP64 fields, [npoles][Ns] each)
+  qed3::S64* msX = nullptr;
+  qed3::S64* msP = nullptr;
 };
 
 namespace qed3 {
@@ -106,7 +111,7 @@ void overlap_destroy(qed3_overlap_s* ov) {
   if (!ov) return;
   if (ov->batch) batch_destroy(ov->batch);
   if (ov->batch_hi) batch_destroy(ov->batch_hi);
-  void* p[] = {ov->Z, ov->y, ov->w, ov->y0, ov->q, ov->part, ov->Yp, ov->fi, ov->sr, ov->sp, ov->sq};
+  void* p[] = {ov->Z, ov->y, ov->w, ov->y0, ov->q, ov->part, ov->Yp, ov->fi, ov->sr, ov->sp, ov->sq, ov->msX, ov->msP};
   for (void* x : p)
     if (x) cudaFree(x);
   delete ov;
@@ -182,10 +187,13 @@ int overlap_update(qed3_overlap_s* ov, double lmin, double lmax, double tol_oute
   return QED3_OK;
 }
 
-// All poles with one right-hand side, broadcast to every pole system:
-// out_m = (D^dag D + lmax^2 sigma_m)^{-1} rhs.  Poles nh..np-1 run in one
-// batched persistent launch in the overlap's precision; the ill-conditioned
-// poles 0..nh-1 (if any) in a second, FP64, launch.
+// All poles with one right-hand side: out_m = (D^dag D + lmax^2 sigma_m)^{-1} rhs.
+// When every pole is within reach of the mixed-precision inner iterations
+// (nh = 0), one batched persistent launch in the overlap's precision, the
+// right-hand side broadcast to every pole system.  Otherwise the ill-
+// conditioned poles set the pace and all poles go through one FP64
+// multi-shift CG (one Krylov space, one D^dag D per iteration for all poles;
+// mshift.cu) -- the split into batched launches is kept for comparison.
 static int pole_solves(qed3_overlap_s* ov, const double* rhs, double* out, double tol, qed3_solve_report* worst,
                        cudaStream_t st) {
   const int np = ov->order / 2;
@@ -195,7 +203,17 @@ static int pole_solves(qed3_overlap_s* ov, const double* rhs, double* out, doubl
   std::vector<qed3_solve_report> reps(np);
   qed3_solve_report w{};
   const double* bs[1] = {rhs};
-  for (int part = 0; part < 2; part++) {
+  if (ov->nh > 0 && ov->multishift) {
+    if (!ov->msX) {
+      QED3_CUDA_TRY(cudaMalloc(&ov->msX, size_t(np) * nd * sizeof(double)));
+      QED3_CUDA_TRY(cudaMalloc(&ov->msP, size_t(np) * nd * sizeof(double)));
+    }
+    float ms = 0;
+    const int rc = mshift_solve(ov->d, np, shifts.data(), rhs, out, ov->msX, ov->msP, tol, 200000, reps.data(), &ms, st);
+    if (rc) return rc;
+    w.ms = ms;
+  }
+  for (int part = 0; part < 2 && !(ov->nh > 0 && ov->multishift); part++) {
     const bool hi = part == 0;
     const int m0 = hi ? 0 : ov->nh, cnt = hi ? ov->nh : ov->nlo;
     if (cnt == 0) continue;

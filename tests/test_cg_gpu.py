@@ -91,3 +91,23 @@ def test_cg_zero_rhs_and_noconv(cuda, flags):
     bt = to_dev(b, cuda)
     rep = Dq.solve(x, bt, tol=1e-14, maxiter=3, flags=flags)
     assert rep.status == Q.ERR_NOCONV and rep.iters == 3
+
+
+@pytest.mark.parametrize("n", [4, 8])
+def test_multishift_matches_oracle(cuda, n):
+    """FP64 multi-shift CG (one Krylov space) against the oracle's CG per shift;
+    every shift certified by its own FP64 true residual."""
+    import torch
+    g, lat, Do, Dq, b = _setup(n, 0.1, 40 + n)
+    shifts = [0.0, 1e-3, 0.05, 0.7, 3.0]
+    bt = to_dev(b, cuda)
+    x = torch.zeros(len(shifts), bt.numel(), dtype=torch.complex128, device=cuda)
+    reps, ms = Q.multishift_solve(Dq, x, bt, shifts, tol=1e-10)
+    X = from_dev(x)
+    for m, sg in enumerate(shifts):
+        assert reps[m].status == Q.OK and reps[m].true_rel_res <= 1.05e-10
+        x_ref, _, _ = Do.cg(b, tol=1e-12, shift=sg)
+        assert np.linalg.norm(X[m] - x_ref) / np.linalg.norm(x_ref) < 1e-8
+    # larger shifts converge (and stop) no later than the base shift
+    its = [r.iters for r in reps]
+    assert its == sorted(its, reverse=True)
