@@ -98,7 +98,7 @@ def test_multishift_matches_oracle(cuda, n):
     """FP64 multi-shift CG (one Krylov space) against the oracle's CG per shift;
     every shift certified by its own FP64 true residual."""
     import torch
-    g, lat, Do, Dq, b = _setup(n, 0.1, 40 + n)
+    g, lat, Do, Dq, b = _setup(n, 0.1, 40 + n, cuda)
     shifts = [0.0, 1e-3, 0.05, 0.7, 3.0]
     bt = to_dev(b, cuda)
     x = torch.zeros(len(shifts), bt.numel(), dtype=torch.complex128, device=cuda)
