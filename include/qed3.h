@@ -234,7 +234,9 @@ int qed3_overlap_info(const qed3_overlap* ov, double* lambda_min, double* lambda
 /* mult / adj / DHD / DDH_deviceAsyncLaunch (:309-390): op = QED3_OP_D (D_ov),
  * QED3_OP_DDAG (D_ov^dag), QED3_OP_DDAGD or QED3_OP_DDDAG (D_ov + D_ov^dag,
  * which equals D_ov^dag D_ov for the exact overlap).  tol_inner: pole solves'
- * relative residual.  report: the worst pole (iterations, true residual). */
+ * relative residual.  report: the worst pole (iterations, true residual); a
+ * pole that stalls within 100 x tol_inner sets report->status but does not fail
+ * the call (ill-conditioned poles reach the FP64 floor there). */
 int qed3_overlap_apply(qed3_overlap* ov, int op, double* out, const double* in, double tol_inner,
                        qed3_solve_report* report, void* stream);
 

@@ -232,7 +232,12 @@ static int pole_solves(qed3_overlap_s* ov, const double* rhs, double* out, doubl
     w.true_rel_res = std::max(w.true_rel_res, r.true_rel_res);
   }
   if (worst) *worst = w;
-  return w.status == QED3_OK ? QED3_OK : fail(w.status, "a pole solve did not converge");
+  // A pole that ends within 100 x tol (the FP64 floor of an ill-conditioned
+  // pole with a low-mode right-hand side) does not abort the product: its
+  // status and true residual are in the report, and an outer solve judges the
+  // result by its own certificate.
+  if (w.status == QED3_OK || w.true_rel_res <= 100.0 * tol) return QED3_OK;
+  return fail(w.status, "a pole solve did not converge");
 }
 
 int overlap_apply(qed3_overlap_s* ov, int op, double* out, const double* in, double tol, qed3_solve_report* rep,
