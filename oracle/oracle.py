@@ -77,6 +77,9 @@ def lib():
                                          ctypes.c_double, ctypes.c_int, ctypes.c_int, c_double_p]
         L.orc_fermion_force.argtypes = [vp, vp, c_double_p, ctypes.c_void_p, c_double_p]
         L.orc_num_threads.restype = ctypes.c_int
+        L.orc_hmc_fermion.restype = ctypes.c_int
+        L.orc_hmc_fermion.argtypes = [vp, vp, vp, vp, ctypes.c_double, ctypes.c_int, ctypes.c_int, ctypes.c_double,
+                                      ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_int, vp, vp]
         L.orc_overlap_force.restype = ctypes.c_int
         L.orc_overlap_force.argtypes = [vp, vp, vp, ctypes.c_double, ctypes.c_double, ctypes.c_int, vp, vp,
                                         ctypes.c_double]
@@ -348,3 +351,15 @@ def thermalized_links(geom: Geometry, beta: float, seed: int, ntraj: int, init: 
 
 def num_threads() -> int:
     return lib().orc_num_threads()
+
+
+def hmc_fermion(geom: Geometry, dirac: "Dirac", rng: "Rng", A: np.ndarray, beta: float, compact: bool = True,
+                exact: bool = True, tmax: float = 1.0, nsteps: int = 10, nsteps_inner: int = 10, tol: float = 1e-12,
+                no_reject: bool = False):
+    """HMC::run with one pseudofermion and ExplicitLeapfrogML restated; A updated in place.
+    Returns (accepted, dH, cg_iterations)."""
+    dH = ctypes.c_double()
+    its = ctypes.c_int()
+    acc = lib().orc_hmc_fermion(geom.handle, dirac.h, rng.h, _dp(A), beta, int(compact), 1 if exact else 0, tmax,
+                                nsteps, nsteps_inner, tol, int(no_reject), ctypes.byref(dH), ctypes.byref(its))
+    return bool(acc), dH.value, its.value

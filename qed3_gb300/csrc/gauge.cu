@@ -19,6 +19,7 @@
 #include <vector>
 
 #include "device.cuh"
+#include "blas_impl.h"
 #include "dirac_impl.h"
 #include "gauge_impl.h"
 #include "handles.h"
@@ -390,6 +391,110 @@ int hmc_pure_gauge(qed3_lattice_s* lat, qed3_rng_s* rng, double* A, double beta,
   }
   QED3_CUDA_TRY(cudaStreamSynchronize(st));
   return QED3_OK;
+}
+
+
+// Fermion HMC trajectory (HMC::run, src/both_3d/hmc.h:75-110, one PseudoFermion,
+// src/both_3d/pseudofermion.h:33-60, ExplicitLeapfrogML,
+// src/both_3d/integrator.h:58-115), every field on the device:
+//   pi ~ N(0,1) per link, xi = fill_gaussian (the reference's streams),
+//   phi = D^dag xi, eta = (D^dag D)^{-1} phi (certified CG), H = 1/2|pi|^2 + S_g + Re<phi,eta>;
+//   pi -= tau/2 F_f; nsteps x [gauge leapfrog of nsteps_inner steps tau/nsteps_inner,
+//   D(U) and eta updated, pi -= tau F_f (tau/2 on the last)]; Metropolis on dH
+//   with the master engine's uniform; a rejection restores U and the operator.
+// dH = sum (pi^2 - pi0^2)/2 + beta * sum (action density differences) + Re<phi, eta1 - eta0>,
+// each difference formed term by term.
+int hmc_fermion(qed3_lattice_s* lat, qed3_dirac_s* d, qed3_rng_s* rng, double* A, double beta, int compact, int exact,
+                double tmax, int nsteps, int nsteps_inner, double tol, int prec, int no_reject, int* accepted,
+                double* dH_out, int* cg_iters, cudaStream_t st) {
+  int rc = gauge_prepare(lat);
+  if (rc) return rc;
+  GaugeDev& G = lat->gauge;
+  const DeviceLattice& D = lat->dev;
+  const int Nl = D.Nl, Nf = D.Nf, Ns = D.Ns;
+  const long long nd = 4LL * Ns;
+  std::vector<double> pi(Nl), xi(nd);
+  rng_gaussian_links(rng, 1.0, pi.data());
+  rng_gaussian_spinor(rng, xi.data());
+  double *phi = nullptr, *eta = nullptr, *eta0 = nullptr, *dxi = nullptr, *Ff = nullptr, *part = nullptr;
+  auto cleanup = [&]() {
+    for (double* p : {phi, eta, eta0, dxi, Ff, part})
+      if (p) cudaFree(p);
+  };
+  if (cudaMalloc(&phi, nd * sizeof(double)) != cudaSuccess || cudaMalloc(&eta, nd * sizeof(double)) != cudaSuccess ||
+      cudaMalloc(&eta0, nd * sizeof(double)) != cudaSuccess || cudaMalloc(&dxi, nd * sizeof(double)) != cudaSuccess ||
+      cudaMalloc(&Ff, size_t(Nl) * sizeof(double)) != cudaSuccess ||
+      cudaMalloc(&part, 4096 * sizeof(double)) != cudaSuccess) {
+    cleanup();
+    return fail(QED3_ERR_NOMEM, "cudaMalloc failed");
+  }
+  qed3_solve_params sp{tol, 0, prec, 0.1, 0.0, 0};
+  int its = 0;
+  auto solve_eta = [&]() -> int {
+    qed3_solve_report r{};
+    int e = cg_solve(d, eta, phi, &sp, &r, st);
+    its += r.iters;
+    if (!e && r.status != QED3_OK) e = fail(QED3_ERR_NOCONV, "pseudofermion solve did not converge");
+    return e;
+  };
+  auto run = [&]() -> int {
+    int e;
+    QED3_CUDA_TRY(cudaMemcpyAsync(G.pi, pi.data(), size_t(Nl) * sizeof(double), cudaMemcpyHostToDevice, st));
+    QED3_CUDA_TRY(cudaMemcpyAsync(G.pi0, G.pi, size_t(Nl) * sizeof(double), cudaMemcpyDeviceToDevice, st));
+    QED3_CUDA_TRY(cudaMemcpyAsync(G.A0, A, size_t(Nl) * sizeof(double), cudaMemcpyDeviceToDevice, st));
+    QED3_CUDA_TRY(cudaMemcpyAsync(dxi, xi.data(), nd * sizeof(double), cudaMemcpyHostToDevice, st));
+    if ((e = dirac_set_links(d, A, 1, st))) return e;
+    if ((e = dirac_apply_ref(d, QED3_OP_DDAG, phi, dxi, st))) return e;
+    if ((e = solve_eta())) return e;
+    QED3_CUDA_TRY(cudaMemcpyAsync(eta0, eta, nd * sizeof(double), cudaMemcpyDeviceToDevice, st));
+    if ((e = gauge_plaquettes(lat, A, G.th0, st))) return e;
+    const double tau = tmax / nsteps, tau_in = tau / nsteps_inner;
+    auto fermion_kick = [&](double c) -> int {
+      int f = fermion_force(d, eta, Ff, st);
+      if (!f) k_axpy<<<nblk(Nl), 256, 0, st>>>(Nl, -c, Ff, G.pi);
+      return f;
+    };
+    auto gauge_kick = [&](double c) -> int {
+      int f = gauge_force(lat, A, beta, compact, exact, G.F, st);
+      if (!f) k_axpy<<<nblk(Nl), 256, 0, st>>>(Nl, -c, G.F, G.pi);
+      return f;
+    };
+    if ((e = fermion_kick(0.5 * tau))) return e;
+    for (int n = 0; n < nsteps; n++) {
+      if ((e = gauge_kick(0.5 * tau_in))) return e;
+      for (int m = 0; m < nsteps_inner; m++) {
+        k_axpy<<<nblk(Nl), 256, 0, st>>>(Nl, tau_in, G.pi, A);
+        if ((e = gauge_kick((m != nsteps_inner - 1 ? 1.0 : 0.5) * tau_in))) return e;
+      }
+      if ((e = dirac_set_links(d, A, 1, st))) return e;
+      if ((e = solve_eta())) return e;
+      if ((e = fermion_kick((n != nsteps - 1 ? 1.0 : 0.5) * tau))) return e;
+    }
+    QED3_CUDA_TRY(cudaGetLastError());
+    if ((e = gauge_plaquettes(lat, A, G.th1, st))) return e;
+    double dk, ds, sf0, sf1;
+    if ((e = reduce(Nl, KinDiff{G.pi, G.pi0}, G.part, &dk, st))) return e;
+    if ((e = reduce(Nf, ActionDiff{G.th1, G.th0, D.face_weight, compact}, G.part, &ds, st))) return e;
+    if ((e = vec_zdot(nd / 2, phi, eta, part, &sf1, nullptr, st))) return e;
+    if ((e = vec_zdot(nd / 2, phi, eta0, part, &sf0, nullptr, st))) return e;
+    const double dH = dk + beta * ds + (sf1 - sf0);
+    *dH_out = dH;
+    if (cg_iters) *cg_iters = its;
+    const double r = std::min(1.0, std::exp(-dH));
+    const double a = rng_uniform(rng);
+    if (a < r || no_reject) {
+      *accepted = 1;
+    } else {
+      *accepted = 0;
+      QED3_CUDA_TRY(cudaMemcpyAsync(A, G.A0, size_t(Nl) * sizeof(double), cudaMemcpyDeviceToDevice, st));
+      if ((e = dirac_set_links(d, A, 1, st))) return e;
+    }
+    QED3_CUDA_TRY(cudaStreamSynchronize(st));
+    return QED3_OK;
+  };
+  rc = run();
+  cleanup();
+  return rc;
 }
 
 }  // namespace qed3

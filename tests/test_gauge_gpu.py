@@ -77,3 +77,55 @@ def test_hmc_trajectory_matches_oracle(cuda, compact):
         assert acc_o == acc_q
         assert abs(dh_o - dh_q) < 1e-11
         assert np.abs(from_dev(At) - Ao).max() < 1e-11
+
+
+def test_fermion_hmc_matches_oracle(cuda):
+    """Wilson-fermion HMC trajectories (HMC::run + ExplicitLeapfrogML, one
+    pseudofermion) against the oracle's restatement from the same RNG streams:
+    same Metropolis decisions, dH and links to the pseudofermion-solve tolerance."""
+    n = 4
+    g = O.geometry(n)
+    lat = Q.S2Trivalent(n)
+    ro, rq = O.Rng(g, 7), Q.ParallelRng(lat, 7)
+    A0 = ro.gaussian_links(0.2)
+    assert np.array_equal(A0, rq.gaussian_links(0.2))
+    Ao = np.ascontiguousarray(A0.copy())
+    At = to_dev(A0, cuda)
+    Do = O.Dirac(g, 1.0, 0.1)
+    Dq = Q.DiracS2Dual(lat, 1.0, 0.1)
+    for it in range(3):
+        acc_o, dh_o, _ = O.hmc_fermion(g, Do, ro, Ao, 1.4, tmax=0.5, nsteps=5, nsteps_inner=4, tol=1e-13)
+        acc_q, dh_q, its = Q.hmc_fermion(lat, Dq, rq, At, 1.4, tmax=0.5, nsteps=5, nsteps_inner=4, tol=1e-13,
+                                         precision=Q.PREC_F64)
+        assert acc_o == acc_q and its > 0
+        assert abs(dh_o - dh_q) < 1e-8 * max(1.0, abs(dh_o))
+        assert np.abs(from_dev(At) - Ao).max() < 1e-9
+
+
+def test_fermion_hmc_dH_scales_as_tau_squared(cuda):
+    """Second-order integrator: halving the outer step divides dH by ~4
+    (the reference's dH ~ tau^2 check), in mixed precision with FP64 certificates."""
+    n = 4
+    lat = Q.S2Trivalent(n)
+    A0 = Q.ParallelRng(lat, 11).gaussian_links(0.3)
+    D = Q.DiracS2Dual(lat, 1.0, 0.1)
+    dh = []
+    for ns in (16, 32):
+        At = to_dev(A0, cuda)
+        _, d, _ = Q.hmc_fermion(lat, D, Q.ParallelRng(lat, 12), At, 1.4, tmax=1.0, nsteps=ns, nsteps_inner=4,
+                                tol=1e-12, precision=Q.PREC_F32, no_reject=True)
+        dh.append(abs(d))
+    assert 2.8 < dh[0] / dh[1] < 5.5
+
+
+def test_fermion_hmc_rejection_restores_links(cuda):
+    lat = Q.S2Trivalent(2)
+    A0 = Q.ParallelRng(lat, 13).gaussian_links(0.3)
+    At = to_dev(A0, cuda)
+    D = Q.DiracS2Dual(lat, 1.0, 0.1)
+    # a huge step makes dH large: the trajectory is rejected and A restored
+    acc, d, _ = Q.hmc_fermion(lat, D, Q.ParallelRng(lat, 14), At, 1.4, tmax=4.0, nsteps=1, nsteps_inner=1,
+                              tol=1e-10, precision=Q.PREC_F64)
+    if not acc:
+        assert np.array_equal(from_dev(At), A0)
+    assert np.isfinite(d)

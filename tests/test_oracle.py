@@ -202,3 +202,17 @@ def test_overlap_force_finite_difference():
         Am[l] -= eps
         fd = -2 * (f(Ap) - f(Am)) / (2 * eps)
         assert abs(F[l] - fd) <= 1e-6 * max(1.0, abs(fd))
+
+
+def test_fermion_hmc_second_order():
+    """The oracle's HMC::run + ExplicitLeapfrogML restatement: dH ~ tau^2."""
+    g = O.geometry(2)
+    A = np.random.default_rng(1).normal(size=g.n_links) * 0.3
+    dh = []
+    for ns in (16, 32):
+        D = O.Dirac(g, 1.0, 0.1)
+        rng = O.Rng(g, 5)
+        Ac = A.copy()
+        _, d, _ = O.hmc_fermion(g, D, rng, Ac, 1.4, tmax=1.0, nsteps=ns, nsteps_inner=4, no_reject=True)
+        dh.append(abs(d))
+    assert 3.0 < dh[0] / dh[1] < 5.0
