@@ -172,6 +172,18 @@ int qed3_batch_config(const qed3_batch* bt, int* rhs_tile, int* threads, int* bl
  * [sum nrhs] in system order, may be NULL; ms: device time of the launch. */
 int qed3_batch_solve(qed3_batch* bt, double* const* x, const double* const* b, const double* const* shifts,
                      const qed3_solve_params* params, qed3_solve_report* reports, float* ms, void* stream);
+/* The same solve split for CUDA-graph capture.  qed3_batch_set_shifts stores
+ * the shifts (host [nrhs[u]] per system or NULL, then `shift`) on the device;
+ * it copies only when a shift changed and refuses to copy while `stream` is
+ * capturing.  qed3_batch_launch enqueues the gather of b, the persistent
+ * launch and the scatter of x with no host synchronisation, allocation or
+ * host-to-device copy, so the sequence can be captured and replayed (a replay
+ * reuses the x, b pointers and shifts of the capture).  qed3_batch_reports
+ * waits for `stream` and reports the last completed launch (ms = 0). */
+int qed3_batch_set_shifts(qed3_batch* bt, const double* const* shifts, double shift, void* stream);
+int qed3_batch_launch(qed3_batch* bt, double* const* x, const double* const* b, const qed3_solve_params* params,
+                      void* stream);
+int qed3_batch_reports(qed3_batch* bt, qed3_solve_report* reports, void* stream);
 
 /* ======================================================================
  * Gauge side  --  replaces U1onS2::plaquette_angle/average_plaquette

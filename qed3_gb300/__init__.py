@@ -115,6 +115,9 @@ SIGNATURES = [
     ("qed3_batch_config", ctypes.c_int, [vp, c_int_p, c_int_p, c_int_p]),
     ("qed3_batch_solve", ctypes.c_int, [vp, vp, vp, vp, ctypes.POINTER(SolveParams), vp,
                                         ctypes.POINTER(ctypes.c_float), vp]),
+    ("qed3_batch_set_shifts", ctypes.c_int, [vp, vp, ctypes.c_double, vp]),
+    ("qed3_batch_launch", ctypes.c_int, [vp, vp, vp, ctypes.POINTER(SolveParams), vp]),
+    ("qed3_batch_reports", ctypes.c_int, [vp, vp, vp]),
     ("qed3_lpc_create", ctypes.c_int, [vp, ctypes.c_int, ctypes.c_int, ctypes.c_uint, ctypes.POINTER(vp)]),
     ("qed3_lpc_destroy", ctypes.c_int, [vp]),
     ("qed3_lpc_info", ctypes.c_int, [vp, c_int_p, c_int_p, c_int_p]),
@@ -466,6 +469,34 @@ class Batch:
         if rc not in (OK, ERR_NOCONV):
             _check(rc)
         return [Report(r.status, r.iters, r.reliable_updates, r.true_rel_res, r.ms) for r in reps], ms.value
+
+    # ---- the same solve in three calls, for CUDA-graph capture ----
+    def set_shifts(self, shifts=None, shift: float = 0.0, stream=None):
+        """Store the shifts on the device (only copies when they changed; must
+        precede a capture)."""
+        n = len(self.systems)
+        arrs = [np.ascontiguousarray(s, dtype=np.float64) if s is not None else None for s in (shifts or [None] * n)]
+        S = (vp * n)(*[(a.ctypes.data if a is not None else None) for a in arrs])
+        _check(lib().qed3_batch_set_shifts(self._h, S if shifts is not None else None, shift, _stream(stream)))
+
+    def launch(self, xs, bs, tol: float = 1e-10, maxiter: int = 100000, delta: float = 0.1, broadcast: bool = False,
+               stream=None):
+        """Enqueue one solve with no host synchronisation: capturable with
+        torch.cuda.graph (pass the capturing stream)."""
+        n = len(self.systems)
+        self._X = (vp * n)(*[x.data_ptr() for x in xs])
+        self._B = (vp * n)(*[b.data_ptr() for b in bs])
+        p = SolveParams(tol, maxiter, PREC_F32, delta, 0.0, SOLVE_BCAST_B if broadcast else 0)
+        _check(lib().qed3_batch_launch(self._h, self._X, self._B, ctypes.byref(p), _stream(stream)))
+
+    def reports(self, stream=None):
+        """Wait for the stream and report the last completed launch."""
+        total = sum(int(s[1]) for s in self.systems)
+        reps = (SolveReport * total)()
+        rc = lib().qed3_batch_reports(self._h, reps, _stream(stream))
+        if rc not in (OK, ERR_NOCONV):
+            _check(rc)
+        return [Report(r.status, r.iters, r.reliable_updates, r.true_rel_res, r.ms) for r in reps]
 
     def __del__(self):
         if getattr(self, "_h", None) and _lib is not None:

@@ -417,6 +417,30 @@ int qed3_batch_solve(qed3_batch* bt, double* const* x, const double* const* b, c
   QED3_GUARD_END
 }
 
+int qed3_batch_set_shifts(qed3_batch* bt, const double* const* shifts, double shift, void* stream) {
+  QED3_GUARD_BEGIN
+  if (!bt) return fail(QED3_ERR_ARG, "NULL argument");
+  return batch_set_shifts(bt, shifts, shift, (cudaStream_t)stream);
+  QED3_GUARD_END
+}
+
+int qed3_batch_launch(qed3_batch* bt, double* const* x, const double* const* b, const qed3_solve_params* params,
+                      void* stream) {
+  QED3_GUARD_BEGIN
+  if (!bt || !x || !b) return fail(QED3_ERR_ARG, "NULL argument");
+  for (size_t u = 0; u < bt->user_ops.size(); u++)
+    if (!x[u] || !b[u]) return fail(QED3_ERR_ARG, "NULL vector");
+  return batch_launch_all(bt, x, b, params, (cudaStream_t)stream);
+  QED3_GUARD_END
+}
+
+int qed3_batch_reports(qed3_batch* bt, qed3_solve_report* reports, void* stream) {
+  QED3_GUARD_BEGIN
+  if (!bt) return fail(QED3_ERR_ARG, "NULL argument");
+  return batch_reports(bt, reports, 0.f, (cudaStream_t)stream);
+  QED3_GUARD_END
+}
+
 int qed3_overlap_create(qed3_dirac* dw, int zolo_order, int precision, qed3_overlap** out) {
   QED3_GUARD_BEGIN
   if (!dw || !out) return fail(QED3_ERR_ARG, "NULL argument");

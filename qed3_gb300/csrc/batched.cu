@@ -619,6 +619,7 @@ static void batch_release(qed3_batch_s* bt) {
 
 static int batch_build(qed3_batch_s* bt) {
   const int R = bt->R;
+  bt->sys_uploaded = false;
   bt->sys.clear();
   bt->owner.clear();
   bt->first_rhs.clear();
@@ -707,19 +708,48 @@ static int batch_build(qed3_batch_s* bt) {
   return QED3_OK;
 }
 
-int batch_solve(qed3_batch_s* bt, double* const* x, const double* const* b, const double* const* shifts,
-                const qed3_solve_params* prm, qed3_solve_report* reports, float* ms_out, cudaStream_t st) {
-  const int R = bt->R, nsys = int(bt->sys.size());
+// Writes the per-right-hand-side shifts into the device descriptors.  The copy
+// is made only when a shift changed since the last upload, from pageable host
+// memory (staged by the runtime before the call returns), so it is never part
+// of a captured launch sequence.
+int batch_set_shifts(qed3_batch_s* bt, const double* const* shifts, double shift, cudaStream_t st) {
+  const int nsys = int(bt->sys.size());
+  bool changed = !bt->sys_uploaded;
   for (int i = 0; i < nsys; i++) {
     BatchSys& s = bt->sys[i];
     const int u = bt->owner[i], f = bt->first_rhs[i];
-    for (int r = 0; r < kMaxTile; r++) s.shift[r] = 0.0;
-    for (int r = 0; r < s.nrhs; r++) s.shift[r] = (shifts && shifts[u]) ? shifts[u][f + r] : (prm ? prm->shift : 0.0);
-    const bool bcast = prm && (prm->flags & QED3_SOLVE_BCAST_B);
+    for (int r = 0; r < kMaxTile; r++) {
+      const double v = r < s.nrhs ? ((shifts && shifts[u]) ? shifts[u][f + r] : shift) : 0.0;
+      if (v != s.shift[r]) changed = true;
+      s.shift[r] = v;
+    }
+  }
+  if (!changed) return QED3_OK;
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  QED3_CUDA_TRY(cudaStreamIsCapturing(st, &cs));
+  if (cs != cudaStreamCaptureStatusNone)
+    return fail(QED3_ERR_STATE, "batch shifts changed during stream capture; set them before capturing");
+  QED3_CUDA_TRY(cudaMemcpyAsync(bt->d_sys, bt->sys.data(), sizeof(BatchSys) * nsys, cudaMemcpyHostToDevice, st));
+  bt->sys_uploaded = true;
+  return QED3_OK;
+}
+
+// Enqueues one batched solve on st: gather of the right-hand sides, the
+// persistent cooperative launch and the scatter of the solutions.  No host
+// synchronisation, allocation or host-to-device copy: the sequence can be
+// captured into a CUDA graph and replayed (the graph keeps x, b and the
+// shifts set before capture).
+int batch_launch_all(qed3_batch_s* bt, double* const* x, const double* const* b, const qed3_solve_params* prm,
+                     cudaStream_t st) {
+  if (!bt->sys_uploaded) return fail(QED3_ERR_STATE, "batch shifts not set");
+  const int R = bt->R, nsys = int(bt->sys.size());
+  const bool bcast = prm && (prm->flags & QED3_SOLVE_BCAST_B);
+  for (int i = 0; i < nsys; i++) {
+    const BatchSys& s = bt->sys[i];
+    const int u = bt->owner[i], f = bt->first_rhs[i];
     const int rc = batch_import(s, bt->user_ops[u], bcast ? b[u] : b[u] + size_t(f) * 4 * s.Ns, R, bcast, st);
     if (rc) return rc;
   }
-  QED3_CUDA_TRY(cudaMemcpyAsync(bt->d_sys, bt->sys.data(), sizeof(BatchSys) * nsys, cudaMemcpyHostToDevice, st));
   QED3_CUDA_TRY(cudaMemsetAsync(bt->bar, 0, sizeof(GridBar), st));
   QED3_CUDA_TRY(cudaMemsetAsync(bt->d_status, 0xff, sizeof(int) * nsys, st));
   BatchArgs a{};
@@ -735,29 +765,33 @@ int batch_solve(qed3_batch_s* bt, double* const* x, const double* const* b, cons
   a.delta2 = delta * delta;
   a.maxiter = prm && prm->maxiter > 0 ? prm->maxiter : 100000;
   a.spin_limit = 20000000LL;
-  QED3_CUDA_TRY(cudaEventRecord(bt->e0, st));
+  if (bt->timing) QED3_CUDA_TRY(cudaEventRecord(bt->e0, st));
   int rc = batch_launch(bt->prec, R, a, bt->grid, bt->threads, st);
   if (rc) return rc;
-  QED3_CUDA_TRY(cudaEventRecord(bt->e1, st));
+  if (bt->timing) QED3_CUDA_TRY(cudaEventRecord(bt->e1, st));
   for (int i = 0; i < nsys; i++) {
     const BatchSys& s = bt->sys[i];
     const int u = bt->owner[i], f = bt->first_rhs[i];
     if ((rc = batch_export(s, bt->user_ops[u], x[u] + size_t(f) * 4 * s.Ns, R, st))) return rc;
   }
+  return QED3_OK;
+}
+
+// Waits for st and turns the device-side results of the last launch into
+// reports (user order: system u, right-hand side j -> offset(u) + j).
+int batch_reports(qed3_batch_s* bt, qed3_solve_report* reports, float ms, cudaStream_t st) {
+  const int R = bt->R, nsys = int(bt->sys.size());
   std::vector<double> scal(size_t(6) * R * nsys);
   std::vector<int> status(nsys);
   QED3_CUDA_TRY(cudaMemcpyAsync(scal.data(), bt->d_scal, scal.size() * sizeof(double), cudaMemcpyDeviceToHost, st));
   QED3_CUDA_TRY(cudaMemcpyAsync(status.data(), bt->d_status, status.size() * sizeof(int), cudaMemcpyDeviceToHost, st));
   QED3_CUDA_TRY(cudaStreamSynchronize(st));
-  float ms = 0.f;
-  QED3_CUDA_TRY(cudaEventElapsedTime(&ms, bt->e0, bt->e1));
-  if (ms_out) *ms_out = ms;
-  bool timeout = false;
-  // reports in user order: user system u, rhs j -> offset(u) + j
+  bool timeout = false, missing = false;
   std::vector<int> off(bt->user_ops.size() + 1, 0);
   for (size_t u = 0; u < bt->user_ops.size(); u++) off[u + 1] = off[u] + bt->user_nrhs[u];
   for (int i = 0; i < nsys; i++) {
     if (status[i] == QED3_ERR_TIMEOUT) timeout = true;
+    if (status[i] == -1) missing = true;  // still the launch's 0xff fill: the kernel never finished the system
     const BatchSys& s = bt->sys[i];
     for (int r = 0; r < s.nrhs; r++) {
       const double* o = &scal[size_t(6) * R * i + 6 * r];
@@ -771,7 +805,23 @@ int batch_solve(qed3_batch_s* bt, double* const* x, const double* const* b, cons
     }
   }
   if (timeout) return fail(QED3_ERR_TIMEOUT, "grid barrier timed out inside the batched CG kernel");
+  if (missing) return fail(QED3_ERR_STATE, "no completed batched launch to report on");
   return QED3_OK;
+}
+
+int batch_solve(qed3_batch_s* bt, double* const* x, const double* const* b, const double* const* shifts,
+                const qed3_solve_params* prm, qed3_solve_report* reports, float* ms_out, cudaStream_t st) {
+  int rc = batch_set_shifts(bt, shifts, prm ? prm->shift : 0.0, st);
+  if (rc) return rc;
+  bt->timing = true;
+  rc = batch_launch_all(bt, x, b, prm, st);
+  bt->timing = false;
+  if (rc) return rc;
+  QED3_CUDA_TRY(cudaStreamSynchronize(st));
+  float ms = 0.f;
+  QED3_CUDA_TRY(cudaEventElapsedTime(&ms, bt->e0, bt->e1));
+  if (ms_out) *ms_out = ms;
+  return batch_reports(bt, reports, ms, st);
 }
 
 // ---- autotuner ----------------------------------------------------------------

@@ -70,6 +70,8 @@ struct qed3_batch_s {
   double* d_scal = nullptr;
   std::vector<void*> buffers;
   cudaEvent_t e0 = nullptr, e1 = nullptr;
+  bool sys_uploaded = false;  // d_sys holds the current descriptors and shifts
+  bool timing = false;        // record e0/e1 around the launch (synchronous solves only)
 };
 
 namespace qed3 {
@@ -78,6 +80,10 @@ int batch_create(int nsys, qed3_dirac_s* const* ops, const int* nrhs, int prec, 
 void batch_destroy(qed3_batch_s* bt);
 int batch_solve(qed3_batch_s* bt, double* const* x, const double* const* b, const double* const* shifts,
                 const qed3_solve_params* prm, qed3_solve_report* reports, float* ms_out, cudaStream_t st);
+int batch_set_shifts(qed3_batch_s* bt, const double* const* shifts, double shift, cudaStream_t st);
+int batch_launch_all(qed3_batch_s* bt, double* const* x, const double* const* b, const qed3_solve_params* prm,
+                     cudaStream_t st);
+int batch_reports(qed3_batch_s* bt, qed3_solve_report* reports, float ms, cudaStream_t st);
 int batch_autotune(qed3_batch_s* proto, int* best_R, int* best_threads,
                    std::vector<std::pair<std::pair<int, int>, float>>* log);
 }  // namespace qed3
