@@ -222,16 +222,17 @@ int qed3_rng_z2_spinor(qed3_rng* r, double* spinor);
 /* FermionVector::set_pt_source (src/dual/valence.h:47-52): host spinor[2*n_sites]
  * complex = unit vector at (site x, spin s), reference order. */
 int qed3_point_source(int n_sites, int x, int s, double* spinor);
-/* HMC::run with one PseudoFermion and ExplicitLeapfrogML (src/both_3d/hmc.h:75-110,
- * src/both_3d/pseudofermion.h:33-60, src/both_3d/integrator.h:58-115): one
+/* HMC::run with one PseudoFermion (npf = 1) or HMC2::run with npf of them,
+ * and ExplicitLeapfrogML (src/both_3d/hmc.h:75-110 and :172-200,
+ * src/both_3d/pseudofermion.h:33-60, src/both_3d/integrator.h:58-168): one
  * trajectory of Wilson fermions + gauge action on the device, in place on the
  * device links A[n_links]; d is the operator (its links are set from A and,
  * on rejection, restored).  nsteps outer (fermion) steps of tmax/nsteps, each
  * with nsteps_inner gauge steps; pseudofermion solves to tol in `precision`,
  * certified by the FP64 true residual.  Writes accepted, dH, cg_iters. */
 int qed3_hmc_fermion(qed3_lattice* lat, qed3_dirac* d, qed3_rng* rng, double* A, double beta, int compact, int exact,
-                     double tmax, int nsteps, int nsteps_inner, double tol, int precision, int no_reject, int* accepted,
-                     double* dH, int* cg_iters, void* stream);
+                     double tmax, int nsteps, int nsteps_inner, int npf, double tol, int precision, int no_reject,
+                     int* accepted, double* dH, int* cg_iters, void* stream);
 int qed3_hmc_pure_gauge(qed3_lattice* lat, qed3_rng* rng, double* A, double beta, int compact, int exact,
                         double tmax, int nsteps, int no_reject, int* accepted, double* dH, void* stream);
 

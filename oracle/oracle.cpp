@@ -1023,8 +1023,10 @@ int orc_hmc_pure_gauge(const OracleGeom* g, OracleRng* rng, double* A, double be
 }
 
 // Fermion HMC trajectory, restating HMC::run (src/both_3d/hmc.h:75-110) with
-// one PseudoFermion (src/both_3d/pseudofermion.h:33-60) and the two-level
-// ExplicitLeapfrogML integrator (src/both_3d/integrator.h:58-115):
+// one PseudoFermion (src/both_3d/pseudofermion.h:33-60), or HMC2::run
+// (src/both_3d/hmc.h:172-200) with npf of them, and the two-level
+// ExplicitLeapfrogML integrator (src/both_3d/integrator.h:58-115, and :117-168
+// for several pseudofermions: their forces kick pi one after the other):
 //   pi ~ N(0,1) per link; xi = fill_gaussian; phi = D^dag xi; eta = (D^dag D)^{-1} phi
 //   H = 1/2 |pi|^2 + S_g(U) + Re<phi, eta>
 //   pi -= tau/2 F_f; repeat nsteps: [gauge leapfrog with nsteps_inner inner steps of
@@ -1034,40 +1036,48 @@ int orc_hmc_pure_gauge(const OracleGeom* g, OracleRng* rng, double* A, double be
 // accepted; writes dH and the total CG iterations.
 void orc_fermion_force(const OracleDirac* d, const OracleGeom* g, const double* A, const double* eta_in, double* F);
 int orc_hmc_fermion(const OracleGeom* g, OracleDirac* d, OracleRng* rng, double* A, double beta, int compact,
-                    int force_mode, double tmax, int nsteps, int nsteps_inner, double tol, int no_reject,
+                    int force_mode, double tmax, int nsteps, int nsteps_inner, int npf, double tol, int no_reject,
                     double* dH_out, int* cg_iters) {
   const size_t Nl = g->links.size();
   const Idx N = d->N;
   std::vector<double> pi(Nl), F(Nl), A0(A, A + Nl);
   orc_rng_gaussian_links(rng, 1.0, pi.data());
-  std::vector<cplx> xi(N), phi(N), eta(N);
-  orc_rng_gaussian_spinor(rng, reinterpret_cast<double*>(xi.data()));
+  // HMC2::run: pf->gen(rng) for each pseudofermion in turn (xi, phi = D^dag xi)
+  std::vector<std::vector<cplx>> phi(npf, std::vector<cplx>(N)), eta(npf, std::vector<cplx>(N));
+  std::vector<cplx> xi(N);
   orc_dirac_update(d, g, A);
-  csr_mult(d, true, phi.data(), xi.data());
+  for (int k = 0; k < npf; k++) {
+    orc_rng_gaussian_spinor(rng, reinterpret_cast<double*>(xi.data()));
+    csr_mult(d, true, phi[k].data(), xi.data());
+  }
   int its = 0;
-  auto solve_eta = [&]() {
-    its += orc_cg(d, 0.0, reinterpret_cast<double*>(eta.data()), reinterpret_cast<const double*>(phi.data()), tol,
-                  1000000, nullptr);
+  auto solve_eta = [&](int k) {
+    its += orc_cg(d, 0.0, reinterpret_cast<double*>(eta[k].data()), reinterpret_cast<const double*>(phi[k].data()),
+                  tol, 1000000, nullptr);
   };
-  solve_eta();
+  for (int k = 0; k < npf; k++) solve_eta(k);
   auto H = [&]() {
     double s = 0;
     for (double p : pi) s += p * p;
-    cplx pe = 0;
-    for (Idx i = 0; i < N; i++) pe += std::conj(phi[i]) * eta[i];
-    return 0.5 * s + orc_gauge_action(g, A, beta, compact) + pe.real();
+    double sf = 0;
+    for (int k = 0; k < npf; k++) {
+      cplx pe = 0;
+      for (Idx i = 0; i < N; i++) pe += std::conj(phi[k][i]) * eta[k][i];
+      sf += pe.real();
+    }
+    return 0.5 * s + orc_gauge_action(g, A, beta, compact) + sf;
   };
   const double h0 = H();
   const double tau = tmax / nsteps, tau_in = tau / nsteps_inner;
-  auto fermion_kick = [&](double c) {
-    orc_fermion_force(d, g, A, reinterpret_cast<const double*>(eta.data()), F.data());
+  auto fermion_kick = [&](int k, double c) {
+    orc_fermion_force(d, g, A, reinterpret_cast<const double*>(eta[k].data()), F.data());
     for (size_t l = 0; l < Nl; l++) pi[l] += -c * F[l];
   };
   auto gauge_kick = [&](double c) {
     orc_gauge_force(g, A, beta, compact, force_mode, F.data());
     for (size_t l = 0; l < Nl; l++) pi[l] += -c * F[l];
   };
-  fermion_kick(0.5 * tau);
+  for (int k = 0; k < npf; k++) fermion_kick(k, 0.5 * tau);
   for (int n = 0; n < nsteps; n++) {
     gauge_kick(0.5 * tau_in);
     for (int m = 0; m < nsteps_inner; m++) {
@@ -1075,8 +1085,10 @@ int orc_hmc_fermion(const OracleGeom* g, OracleDirac* d, OracleRng* rng, double*
       gauge_kick((m != nsteps_inner - 1 ? 1.0 : 0.5) * tau_in);
     }
     orc_dirac_update(d, g, A);
-    solve_eta();
-    fermion_kick((n != nsteps - 1 ? 1.0 : 0.5) * tau);
+    for (int k = 0; k < npf; k++) {
+      solve_eta(k);
+      fermion_kick(k, (n != nsteps - 1 ? 1.0 : 0.5) * tau);
+    }
   }
   const double h1 = H();
   const double dH = h1 - h0;

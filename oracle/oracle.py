@@ -79,7 +79,7 @@ def lib():
         L.orc_num_threads.restype = ctypes.c_int
         L.orc_hmc_fermion.restype = ctypes.c_int
         L.orc_hmc_fermion.argtypes = [vp, vp, vp, vp, ctypes.c_double, ctypes.c_int, ctypes.c_int, ctypes.c_double,
-                                      ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_int, vp, vp]
+                                      ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_int, vp, vp]
         L.orc_overlap_force.restype = ctypes.c_int
         L.orc_overlap_force.argtypes = [vp, vp, vp, ctypes.c_double, ctypes.c_double, ctypes.c_int, vp, vp,
                                         ctypes.c_double]
@@ -355,11 +355,11 @@ def num_threads() -> int:
 
 def hmc_fermion(geom: Geometry, dirac: "Dirac", rng: "Rng", A: np.ndarray, beta: float, compact: bool = True,
                 exact: bool = True, tmax: float = 1.0, nsteps: int = 10, nsteps_inner: int = 10, tol: float = 1e-12,
-                no_reject: bool = False):
-    """HMC::run with one pseudofermion and ExplicitLeapfrogML restated; A updated in place.
-    Returns (accepted, dH, cg_iterations)."""
+                no_reject: bool = False, npf: int = 1):
+    """HMC::run (npf = 1) or HMC2::run (npf pseudofermions) with ExplicitLeapfrogML
+    restated; A updated in place.  Returns (accepted, dH, cg_iterations)."""
     dH = ctypes.c_double()
     its = ctypes.c_int()
     acc = lib().orc_hmc_fermion(geom.handle, dirac.h, rng.h, _dp(A), beta, int(compact), 1 if exact else 0, tmax,
-                                nsteps, nsteps_inner, tol, int(no_reject), ctypes.byref(dH), ctypes.byref(its))
+                                nsteps, nsteps_inner, npf, tol, int(no_reject), ctypes.byref(dH), ctypes.byref(its))
     return bool(acc), dH.value, its.value

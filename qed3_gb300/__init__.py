@@ -93,8 +93,8 @@ SIGNATURES = [
     ("qed3_rng_z2_spinor", ctypes.c_int, [vp, vp]),
     ("qed3_point_source", ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, vp]),
     ("qed3_hmc_fermion", ctypes.c_int, [vp, vp, vp, vp, ctypes.c_double, ctypes.c_int, ctypes.c_int, ctypes.c_double,
-                                        ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_int, ctypes.c_int, c_int_p,
-                                        c_double_p, c_int_p, vp]),
+                                        ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_int,
+                                        ctypes.c_int, c_int_p, c_double_p, c_int_p, vp]),
     ("qed3_hmc_pure_gauge", ctypes.c_int, [vp, vp, vp, ctypes.c_double, ctypes.c_int, ctypes.c_int, ctypes.c_double,
                                            ctypes.c_int, ctypes.c_int, c_int_p, c_double_p, vp]),
     ("qed3_zolotarev", ctypes.c_int, [ctypes.c_double, ctypes.c_int, vp, vp, vp, vp, c_int_p]),
@@ -369,12 +369,13 @@ def hmc_pure_gauge(lattice: S2Trivalent, rng: ParallelRng, A, beta: float, compa
 
 def hmc_fermion(lattice: S2Trivalent, dirac: DiracS2Dual, rng: "ParallelRng", A, beta: float, compact: bool = True,
                 exact: bool = True, tmax: float = 1.0, nsteps: int = 10, nsteps_inner: int = 10, tol: float = 1e-10,
-                precision: int = PREC_F32, no_reject: bool = False, stream=None):
-    """One Wilson-fermion HMC trajectory on device links A (in place): HMC::run with one
-    pseudofermion and ExplicitLeapfrogML.  Returns (accepted, dH, cg_iterations)."""
+                precision: int = PREC_F32, no_reject: bool = False, npf: int = 1, stream=None):
+    """One Wilson-fermion HMC trajectory on device links A (in place): HMC::run (npf = 1)
+    or HMC2::run (npf pseudofermions) with ExplicitLeapfrogML.  Returns
+    (accepted, dH, cg_iterations)."""
     acc, dH, its = ctypes.c_int(), ctypes.c_double(), ctypes.c_int()
     _check(lib().qed3_hmc_fermion(lattice.handle, dirac.handle, rng.handle, _ptr(A), beta, int(compact), int(exact),
-                                  tmax, nsteps, nsteps_inner, tol, precision, int(no_reject), ctypes.byref(acc),
+                                  tmax, nsteps, nsteps_inner, npf, tol, precision, int(no_reject), ctypes.byref(acc),
                                   ctypes.byref(dH), ctypes.byref(its), _stream(stream)))
     return bool(acc.value), dH.value, its.value
 

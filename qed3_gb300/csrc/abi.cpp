@@ -361,14 +361,15 @@ int qed3_point_source(int n_sites, int x, int s, double* spinor) {
 }
 
 int qed3_hmc_fermion(qed3_lattice* lat, qed3_dirac* d, qed3_rng* rng, double* A, double beta, int compact, int exact,
-                     double tmax, int nsteps, int nsteps_inner, double tol, int precision, int no_reject, int* accepted,
-                     double* dH, int* cg_iters, void* stream) {
+                     double tmax, int nsteps, int nsteps_inner, int npf, double tol, int precision, int no_reject,
+                     int* accepted, double* dH, int* cg_iters, void* stream) {
   QED3_GUARD_BEGIN
   if (!lat || !d || !rng || !A || !accepted || !dH) return fail(QED3_ERR_ARG, "NULL argument");
   if (d->lat != lat) return fail(QED3_ERR_ARG, "operator belongs to another lattice");
   if (nsteps < 1 || nsteps_inner < 1 || !(tmax > 0)) return fail(QED3_ERR_ARG, "need nsteps, nsteps_inner >= 1, tmax > 0");
   if (precision < 0 || precision > 2) return fail(QED3_ERR_ARG, "unknown precision");
-  return hmc_fermion(lat, d, rng, A, beta, compact, exact, tmax, nsteps, nsteps_inner, tol > 0 ? tol : 1e-10,
+  if (npf < 1 || npf > 64) return fail(QED3_ERR_ARG, "need 1 <= npf <= 64 pseudofermions");
+  return hmc_fermion(lat, d, rng, A, beta, compact, exact, tmax, nsteps, nsteps_inner, npf, tol > 0 ? tol : 1e-10,
                      precision, no_reject, accepted, dH, cg_iters, (cudaStream_t)stream);
   QED3_GUARD_END
 }

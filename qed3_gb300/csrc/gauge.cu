@@ -405,7 +405,7 @@ int hmc_pure_gauge(qed3_lattice_s* lat, qed3_rng_s* rng, double* A, double beta,
 // dH = sum (pi^2 - pi0^2)/2 + beta * sum (action density differences) + Re<phi, eta1 - eta0>,
 // each difference formed term by term.
 int hmc_fermion(qed3_lattice_s* lat, qed3_dirac_s* d, qed3_rng_s* rng, double* A, double beta, int compact, int exact,
-                double tmax, int nsteps, int nsteps_inner, double tol, int prec, int no_reject, int* accepted,
+                double tmax, int nsteps, int nsteps_inner, int npf, double tol, int prec, int no_reject, int* accepted,
                 double* dH_out, int* cg_iters, cudaStream_t st) {
   int rc = gauge_prepare(lat);
   if (rc) return rc;
@@ -413,16 +413,18 @@ int hmc_fermion(qed3_lattice_s* lat, qed3_dirac_s* d, qed3_rng_s* rng, double* A
   const DeviceLattice& D = lat->dev;
   const int Nl = D.Nl, Nf = D.Nf, Ns = D.Ns;
   const long long nd = 4LL * Ns;
-  std::vector<double> pi(Nl), xi(nd);
+  // HMC2::run draws pi, then one xi per pseudofermion, from the same streams
+  std::vector<double> pi(Nl), xi(nd * npf);
   rng_gaussian_links(rng, 1.0, pi.data());
-  rng_gaussian_spinor(rng, xi.data());
+  for (int k = 0; k < npf; k++) rng_gaussian_spinor(rng, xi.data() + nd * k);
   double *phi = nullptr, *eta = nullptr, *eta0 = nullptr, *dxi = nullptr, *Ff = nullptr, *part = nullptr;
   auto cleanup = [&]() {
     for (double* p : {phi, eta, eta0, dxi, Ff, part})
       if (p) cudaFree(p);
   };
-  if (cudaMalloc(&phi, nd * sizeof(double)) != cudaSuccess || cudaMalloc(&eta, nd * sizeof(double)) != cudaSuccess ||
-      cudaMalloc(&eta0, nd * sizeof(double)) != cudaSuccess || cudaMalloc(&dxi, nd * sizeof(double)) != cudaSuccess ||
+  const size_t vbytes = size_t(nd) * npf * sizeof(double);
+  if (cudaMalloc(&phi, vbytes) != cudaSuccess || cudaMalloc(&eta, vbytes) != cudaSuccess ||
+      cudaMalloc(&eta0, vbytes) != cudaSuccess || cudaMalloc(&dxi, vbytes) != cudaSuccess ||
       cudaMalloc(&Ff, size_t(Nl) * sizeof(double)) != cudaSuccess ||
       cudaMalloc(&part, 4096 * sizeof(double)) != cudaSuccess) {
     cleanup();
@@ -430,9 +432,9 @@ int hmc_fermion(qed3_lattice_s* lat, qed3_dirac_s* d, qed3_rng_s* rng, double* A
   }
   qed3_solve_params sp{tol, 0, prec, 0.1, 0.0, 0};
   int its = 0;
-  auto solve_eta = [&]() -> int {
+  auto solve_eta = [&](int k) -> int {
     qed3_solve_report r{};
-    int e = cg_solve(d, eta, phi, &sp, &r, st);
+    int e = cg_solve(d, eta + nd * k, phi + nd * k, &sp, &r, st);
     its += r.iters;
     if (!e && r.status != QED3_OK) e = fail(QED3_ERR_NOCONV, "pseudofermion solve did not converge");
     return e;
@@ -442,15 +444,17 @@ int hmc_fermion(qed3_lattice_s* lat, qed3_dirac_s* d, qed3_rng_s* rng, double* A
     QED3_CUDA_TRY(cudaMemcpyAsync(G.pi, pi.data(), size_t(Nl) * sizeof(double), cudaMemcpyHostToDevice, st));
     QED3_CUDA_TRY(cudaMemcpyAsync(G.pi0, G.pi, size_t(Nl) * sizeof(double), cudaMemcpyDeviceToDevice, st));
     QED3_CUDA_TRY(cudaMemcpyAsync(G.A0, A, size_t(Nl) * sizeof(double), cudaMemcpyDeviceToDevice, st));
-    QED3_CUDA_TRY(cudaMemcpyAsync(dxi, xi.data(), nd * sizeof(double), cudaMemcpyHostToDevice, st));
+    QED3_CUDA_TRY(cudaMemcpyAsync(dxi, xi.data(), vbytes, cudaMemcpyHostToDevice, st));
     if ((e = dirac_set_links(d, A, 1, st))) return e;
-    if ((e = dirac_apply_ref(d, QED3_OP_DDAG, phi, dxi, st))) return e;
-    if ((e = solve_eta())) return e;
-    QED3_CUDA_TRY(cudaMemcpyAsync(eta0, eta, nd * sizeof(double), cudaMemcpyDeviceToDevice, st));
+    for (int k = 0; k < npf; k++)
+      if ((e = dirac_apply_ref(d, QED3_OP_DDAG, phi + nd * k, dxi + nd * k, st))) return e;
+    for (int k = 0; k < npf; k++)
+      if ((e = solve_eta(k))) return e;
+    QED3_CUDA_TRY(cudaMemcpyAsync(eta0, eta, vbytes, cudaMemcpyDeviceToDevice, st));
     if ((e = gauge_plaquettes(lat, A, G.th0, st))) return e;
     const double tau = tmax / nsteps, tau_in = tau / nsteps_inner;
-    auto fermion_kick = [&](double c) -> int {
-      int f = fermion_force(d, eta, Ff, st);
+    auto fermion_kick = [&](int k, double c) -> int {
+      int f = fermion_force(d, eta + nd * k, Ff, st);
       if (!f) k_axpy<<<nblk(Nl), 256, 0, st>>>(Nl, -c, Ff, G.pi);
       return f;
     };
@@ -459,7 +463,8 @@ int hmc_fermion(qed3_lattice_s* lat, qed3_dirac_s* d, qed3_rng_s* rng, double* A
       if (!f) k_axpy<<<nblk(Nl), 256, 0, st>>>(Nl, -c, G.F, G.pi);
       return f;
     };
-    if ((e = fermion_kick(0.5 * tau))) return e;
+    for (int k = 0; k < npf; k++)
+      if ((e = fermion_kick(k, 0.5 * tau))) return e;
     for (int n = 0; n < nsteps; n++) {
       if ((e = gauge_kick(0.5 * tau_in))) return e;
       for (int m = 0; m < nsteps_inner; m++) {
@@ -467,17 +472,23 @@ int hmc_fermion(qed3_lattice_s* lat, qed3_dirac_s* d, qed3_rng_s* rng, double* A
         if ((e = gauge_kick((m != nsteps_inner - 1 ? 1.0 : 0.5) * tau_in))) return e;
       }
       if ((e = dirac_set_links(d, A, 1, st))) return e;
-      if ((e = solve_eta())) return e;
-      if ((e = fermion_kick((n != nsteps - 1 ? 1.0 : 0.5) * tau))) return e;
+      for (int k = 0; k < npf; k++) {
+        if ((e = solve_eta(k))) return e;
+        if ((e = fermion_kick(k, (n != nsteps - 1 ? 1.0 : 0.5) * tau))) return e;
+      }
     }
     QED3_CUDA_TRY(cudaGetLastError());
     if ((e = gauge_plaquettes(lat, A, G.th1, st))) return e;
-    double dk, ds, sf0, sf1;
+    double dk, ds, dsf = 0;
     if ((e = reduce(Nl, KinDiff{G.pi, G.pi0}, G.part, &dk, st))) return e;
     if ((e = reduce(Nf, ActionDiff{G.th1, G.th0, D.face_weight, compact}, G.part, &ds, st))) return e;
-    if ((e = vec_zdot(nd / 2, phi, eta, part, &sf1, nullptr, st))) return e;
-    if ((e = vec_zdot(nd / 2, phi, eta0, part, &sf0, nullptr, st))) return e;
-    const double dH = dk + beta * ds + (sf1 - sf0);
+    for (int k = 0; k < npf; k++) {
+      double sf0, sf1;
+      if ((e = vec_zdot(nd / 2, phi + nd * k, eta + nd * k, part, &sf1, nullptr, st))) return e;
+      if ((e = vec_zdot(nd / 2, phi + nd * k, eta0 + nd * k, part, &sf0, nullptr, st))) return e;
+      dsf += sf1 - sf0;
+    }
+    const double dH = dk + beta * ds + dsf;
     *dH_out = dH;
     if (cg_iters) *cg_iters = its;
     const double r = std::min(1.0, std::exp(-dH));

@@ -129,3 +129,25 @@ def test_fermion_hmc_rejection_restores_links(cuda):
     if not acc:
         assert np.array_equal(from_dev(At), A0)
     assert np.isfinite(d)
+
+
+def test_fermion_hmc_two_pseudofermions_matches_oracle(cuda):
+    """HMC2::run: two pseudofermions drawn one after the other from the same
+    streams, their forces kicking the momenta in turn; GPU = oracle."""
+    n = 2
+    g = O.geometry(n)
+    lat = Q.S2Trivalent(n)
+    ro, rq = O.Rng(g, 17), Q.ParallelRng(lat, 17)
+    A0 = ro.gaussian_links(0.2)
+    assert np.array_equal(A0, rq.gaussian_links(0.2))
+    Ao = np.ascontiguousarray(A0.copy())
+    At = to_dev(A0, cuda)
+    Do = O.Dirac(g, 1.0, 0.1)
+    Dq = Q.DiracS2Dual(lat, 1.0, 0.1)
+    for it in range(3):
+        acc_o, dh_o, its_o = O.hmc_fermion(g, Do, ro, Ao, 1.4, tmax=0.5, nsteps=5, nsteps_inner=4, tol=1e-13, npf=2)
+        acc_q, dh_q, its = Q.hmc_fermion(lat, Dq, rq, At, 1.4, tmax=0.5, nsteps=5, nsteps_inner=4, tol=1e-13,
+                                         precision=Q.PREC_F64, npf=2)
+        assert acc_o == acc_q and its > 0
+        assert abs(dh_o - dh_q) < 1e-8 * max(1.0, abs(dh_o))
+        assert np.abs(from_dev(At) - Ao).max() < 1e-9

@@ -216,3 +216,16 @@ def test_fermion_hmc_second_order():
         _, d, _ = O.hmc_fermion(g, D, rng, Ac, 1.4, tmax=1.0, nsteps=ns, nsteps_inner=4, no_reject=True)
         dh.append(abs(d))
     assert 3.0 < dh[0] / dh[1] < 5.0
+
+
+def test_fermion_hmc_two_pseudofermions_second_order():
+    """HMC2::run restated: with two pseudofermions dH still falls as tau^2."""
+    g = O.geometry(2)
+    A = np.random.default_rng(2).normal(size=g.n_links) * 0.3
+    dh = []
+    for ns in (32, 64):
+        D = O.Dirac(g, 1.0, 0.1)
+        _, d, its = O.hmc_fermion(g, D, O.Rng(g, 6), A.copy(), 1.4, tmax=1.0, nsteps=ns, nsteps_inner=4,
+                                  no_reject=True, npf=2)
+        dh.append(abs(d))
+    assert 3.0 < dh[0] / dh[1] < 5.0
