@@ -233,6 +233,17 @@ int qed3_point_source(int n_sites, int x, int s, double* spinor);
 int qed3_hmc_fermion(qed3_lattice* lat, qed3_dirac* d, qed3_rng* rng, double* A, double beta, int compact, int exact,
                      double tmax, int nsteps, int nsteps_inner, int npf, double tol, int precision, int no_reject,
                      int* accepted, double* dH, int* cg_iters, void* stream);
+/* The same trajectory with overlap fermions (the reference's IS_OVERLAP build
+ * of HMC2, src/both_3d/hmc.cu:155-160,457-467): operator update =
+ * Overlap::update (src/both_3d/overlap.h:207-216: links, lambda bounds by
+ * power iterations, Zolotarev coefficients) when lmin = lmax = 0, or fixed
+ * bounds lmin < lmax; phi = D_ov^dag xi; eta = (D_ov^dag D_ov)^{-1} phi by
+ * the outer CG to tol (pole solves to tol_inner); force = qed3_overlap_force.
+ * ov's Wilson operator must live on lat. */
+int qed3_hmc_overlap(qed3_lattice* lat, qed3_overlap* ov, qed3_rng* rng, double* A, double beta, int compact,
+                     int exact, double tmax, int nsteps, int nsteps_inner, int npf, double lmin, double lmax,
+                     double tol, double tol_inner, int no_reject, int* accepted, double* dH, int* cg_iters,
+                     void* stream);
 int qed3_hmc_pure_gauge(qed3_lattice* lat, qed3_rng* rng, double* A, double beta, int compact, int exact,
                         double tmax, int nsteps, int no_reject, int* accepted, double* dH, void* stream);
 

@@ -363,3 +363,79 @@ def hmc_fermion(geom: Geometry, dirac: "Dirac", rng: "Rng", A: np.ndarray, beta:
     acc = lib().orc_hmc_fermion(geom.handle, dirac.h, rng.h, _dp(A), beta, int(compact), 1 if exact else 0, tmax,
                                 nsteps, nsteps_inner, npf, tol, int(no_reject), ctypes.byref(dH), ctypes.byref(its))
     return bool(acc), dH.value, its.value
+
+
+def hmc_overlap(geom: Geometry, dirac: "Dirac", rng: "Rng", A: np.ndarray, beta: float, compact: bool = True,
+                exact: bool = True, tmax: float = 1.0, nsteps: int = 10, nsteps_inner: int = 10, npf: int = 1,
+                lmin: float = 0.0, lmax: float = 0.0, order: int = 21, tol: float = 1e-10, tol_inner: float = 1e-12,
+                no_reject: bool = False):
+    """HMC2::run with Overlap fermions (src/both_3d/hmc.h:172-200, src/both_3d/hmc.cu:155-160)
+    and ExplicitLeapfrogML (src/both_3d/integrator.h:117-168), composed from the
+    oracle's overlap pieces; A updated in place.  lmin = lmax = 0: every operator
+    update recomputes the bounds (Overlap::update, src/both_3d/overlap.h:207-216).
+    eta = (D_ov^dag D_ov)^{-1} phi by MatPoly::solve's CG (src/dual/matpoly.h:204-267)
+    on Overlap::DHD.  Returns (accepted, dH, outer CG iterations)."""
+    fixed = lmin > 0 or lmax > 0
+    bounds = [lmin, lmax]
+    pi = rng.gaussian_links(1.0)
+    xis = [rng.gaussian_spinor() for _ in range(npf)]
+    A0 = A.copy()
+
+    def update():
+        dirac.update(A)
+        if not fixed:
+            bounds[0], bounds[1] = dirac.lambda_bounds(tol_outer=tol_inner)
+
+    def ov(v, op):
+        return dirac.overlap(v, bounds[0], bounds[1], order, op, tol_inner=tol_inner)
+
+    its = [0]
+
+    def solve(b):
+        x = np.zeros_like(b)
+        r = b.copy()
+        p = r.copy()
+        bb = np.vdot(b, b).real
+        rr = bb
+        while True:
+            q = ov(p, 2)
+            al = rr / np.vdot(p, q).real
+            x += al * p
+            r -= al * q
+            rn = np.vdot(r, r).real
+            its[0] += 1
+            if rn < tol * tol * bb:
+                return x
+            p = r + (rn / rr) * p
+            rr = rn
+
+    update()
+    phis = [ov(xi, 1) for xi in xis]
+    etas = [solve(ph) for ph in phis]
+
+    def H():
+        return (0.5 * float(np.dot(pi, pi)) + gauge_action(geom, A, beta, compact)
+                + sum(np.vdot(ph, et).real for ph, et in zip(phis, etas)))
+
+    h0 = H()
+    tau = tmax / nsteps
+    tau_in = tau / nsteps_inner
+    for k in range(npf):
+        pi -= 0.5 * tau * dirac.overlap_force(A, etas[k], bounds[0], bounds[1], order, tol_inner)
+    for n in range(nsteps):
+        pi -= 0.5 * tau_in * gauge_force(geom, A, beta, compact, exact)
+        for m in range(nsteps_inner):
+            A += tau_in * pi
+            pi -= (1.0 if m != nsteps_inner - 1 else 0.5) * tau_in * gauge_force(geom, A, beta, compact, exact)
+        update()
+        for k in range(npf):
+            etas[k] = solve(phis[k])
+            pi -= (1.0 if n != nsteps - 1 else 0.5) * tau * dirac.overlap_force(A, etas[k], bounds[0], bounds[1],
+                                                                                 order, tol_inner)
+    dH = H() - h0
+    r = min(1.0, np.exp(-dH))
+    if rng.uniform() < r or no_reject:
+        return True, dH, its[0]
+    A[:] = A0
+    update()
+    return False, dH, its[0]

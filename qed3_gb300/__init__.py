@@ -95,6 +95,10 @@ SIGNATURES = [
     ("qed3_hmc_fermion", ctypes.c_int, [vp, vp, vp, vp, ctypes.c_double, ctypes.c_int, ctypes.c_int, ctypes.c_double,
                                         ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_int,
                                         ctypes.c_int, c_int_p, c_double_p, c_int_p, vp]),
+    ("qed3_hmc_overlap", ctypes.c_int, [vp, vp, vp, vp, ctypes.c_double, ctypes.c_int, ctypes.c_int, ctypes.c_double,
+                                        ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double,
+                                        ctypes.c_double, ctypes.c_double, ctypes.c_int, c_int_p, c_double_p, c_int_p,
+                                        vp]),
     ("qed3_hmc_pure_gauge", ctypes.c_int, [vp, vp, vp, ctypes.c_double, ctypes.c_int, ctypes.c_int, ctypes.c_double,
                                            ctypes.c_int, ctypes.c_int, c_int_p, c_double_p, vp]),
     ("qed3_zolotarev", ctypes.c_int, [ctypes.c_double, ctypes.c_int, vp, vp, vp, vp, c_int_p]),
@@ -377,6 +381,22 @@ def hmc_fermion(lattice: S2Trivalent, dirac: DiracS2Dual, rng: "ParallelRng", A,
     _check(lib().qed3_hmc_fermion(lattice.handle, dirac.handle, rng.handle, _ptr(A), beta, int(compact), int(exact),
                                   tmax, nsteps, nsteps_inner, npf, tol, precision, int(no_reject), ctypes.byref(acc),
                                   ctypes.byref(dH), ctypes.byref(its), _stream(stream)))
+    return bool(acc.value), dH.value, its.value
+
+
+def hmc_overlap(lattice: S2Trivalent, overlap: "Overlap", rng: "ParallelRng", A, beta: float, compact: bool = True,
+                exact: bool = True, tmax: float = 1.0, nsteps: int = 10, nsteps_inner: int = 10, npf: int = 1,
+                lambda_min: float = 0.0, lambda_max: float = 0.0, tol: float = 1e-10, tol_inner: float = 1e-12,
+                no_reject: bool = False, stream=None):
+    """One overlap-fermion HMC trajectory (HMC2::run with Overlap fermions) on device
+    links A, in place.  lambda_min = lambda_max = 0: the operator update recomputes
+    the spectral bounds (Overlap::update); otherwise the bounds stay fixed.
+    Returns (accepted, dH, outer_cg_iterations)."""
+    acc, dH, its = ctypes.c_int(), ctypes.c_double(), ctypes.c_int()
+    _check(lib().qed3_hmc_overlap(lattice.handle, overlap._h, rng.handle, _ptr(A), beta, int(compact), int(exact),
+                                  tmax, nsteps, nsteps_inner, npf, lambda_min, lambda_max, tol, tol_inner,
+                                  int(no_reject), ctypes.byref(acc), ctypes.byref(dH), ctypes.byref(its),
+                                  _stream(stream)))
     return bool(acc.value), dH.value, its.value
 
 

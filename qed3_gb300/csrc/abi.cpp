@@ -374,6 +374,23 @@ int qed3_hmc_fermion(qed3_lattice* lat, qed3_dirac* d, qed3_rng* rng, double* A,
   QED3_GUARD_END
 }
 
+int qed3_hmc_overlap(qed3_lattice* lat, qed3_overlap* ov, qed3_rng* rng, double* A, double beta, int compact,
+                     int exact, double tmax, int nsteps, int nsteps_inner, int npf, double lmin, double lmax,
+                     double tol, double tol_inner, int no_reject, int* accepted, double* dH, int* cg_iters,
+                     void* stream) {
+  QED3_GUARD_BEGIN
+  if (!lat || !ov || !rng || !A || !accepted || !dH) return fail(QED3_ERR_ARG, "NULL argument");
+  if (overlap_dirac(ov)->lat != lat) return fail(QED3_ERR_ARG, "overlap operator belongs to another lattice");
+  if (nsteps < 1 || nsteps_inner < 1 || !(tmax > 0)) return fail(QED3_ERR_ARG, "need nsteps, nsteps_inner >= 1, tmax > 0");
+  if (npf < 1 || npf > 64) return fail(QED3_ERR_ARG, "need 1 <= npf <= 64 pseudofermions");
+  const bool fixed = lmin > 0 || lmax > 0;
+  if (fixed && !(lmin > 0 && lmin < lmax)) return fail(QED3_ERR_ARG, "fixed bounds need 0 < lmin < lmax");
+  return hmc_overlap(lat, ov, rng, A, beta, compact, exact, tmax, nsteps, nsteps_inner, npf, fixed ? lmin : 0.0,
+                     fixed ? lmax : 0.0, tol > 0 ? tol : 1e-10, tol_inner > 0 ? tol_inner : 1e-12, no_reject, accepted,
+                     dH, cg_iters, (cudaStream_t)stream);
+  QED3_GUARD_END
+}
+
 int qed3_hmc_pure_gauge(qed3_lattice* lat, qed3_rng* rng, double* A, double beta, int compact, int exact,
                         double tmax, int nsteps, int no_reject, int* accepted, double* dH, void* stream) {
   QED3_GUARD_BEGIN

@@ -15,6 +15,7 @@
 //    dH accumulated as per-term differences in FP64.
 
 #include <cmath>
+#include <functional>
 #include <random>
 #include <vector>
 
@@ -23,6 +24,7 @@
 #include "dirac_impl.h"
 #include "gauge_impl.h"
 #include "handles.h"
+#include "overlap_impl.h"
 
 namespace qed3 {
 
@@ -404,16 +406,31 @@ int hmc_pure_gauge(qed3_lattice_s* lat, qed3_rng_s* rng, double* A, double beta,
 //   with the master engine's uniform; a rejection restores U and the operator.
 // dH = sum (pi^2 - pi0^2)/2 + beta * sum (action density differences) + Re<phi, eta1 - eta0>,
 // each difference formed term by term.
-int hmc_fermion(qed3_lattice_s* lat, qed3_dirac_s* d, qed3_rng_s* rng, double* A, double beta, int compact, int exact,
-                double tmax, int nsteps, int nsteps_inner, int npf, double tol, int prec, int no_reject, int* accepted,
-                double* dH_out, int* cg_iters, cudaStream_t st) {
+// The fermion side of a trajectory: set the operator from the links,
+// phi = D^dag xi, eta = (D^dag D)^{-1} phi, and the force
+// F_l = dS/dA_l = -2 Re <eta, d(D) eta>-type term of the operator.
+struct HmcFermion {
+  std::function<int(const double* A)> update;
+  std::function<int(double* phi, const double* xi)> apply_dag;
+  std::function<int(double* eta, const double* phi, int* iters)> solve;
+  std::function<int(const double* eta, double* F)> force;
+};
+
+// HMC::run (npf = 1) / HMC2::run (src/both_3d/hmc.h:75-110, :172-200) with
+// ExplicitLeapfrogML (src/both_3d/integrator.h:58-168): momenta and one xi per
+// pseudofermion from the RNG streams, phi = D^dag xi, eta solved; half fermion
+// kick per pseudofermion; nsteps of [gauge leapfrog with nsteps_inner steps,
+// operator update, per pseudofermion: solve + kick]; dH from per-term
+// differences; Metropolis with the master engine; links and operator restored
+// on rejection.
+static int hmc_trajectory(qed3_lattice_s* lat, const HmcFermion& fo, long long nd, qed3_rng_s* rng, double* A,
+                          double beta, int compact, int exact, double tmax, int nsteps, int nsteps_inner, int npf,
+                          int no_reject, int* accepted, double* dH_out, int* cg_iters, cudaStream_t st) {
   int rc = gauge_prepare(lat);
   if (rc) return rc;
   GaugeDev& G = lat->gauge;
   const DeviceLattice& D = lat->dev;
-  const int Nl = D.Nl, Nf = D.Nf, Ns = D.Ns;
-  const long long nd = 4LL * Ns;
-  // HMC2::run draws pi, then one xi per pseudofermion, from the same streams
+  const int Nl = D.Nl, Nf = D.Nf;
   std::vector<double> pi(Nl), xi(nd * npf);
   rng_gaussian_links(rng, 1.0, pi.data());
   for (int k = 0; k < npf; k++) rng_gaussian_spinor(rng, xi.data() + nd * k);
@@ -430,31 +447,24 @@ int hmc_fermion(qed3_lattice_s* lat, qed3_dirac_s* d, qed3_rng_s* rng, double* A
     cleanup();
     return fail(QED3_ERR_NOMEM, "cudaMalloc failed");
   }
-  qed3_solve_params sp{tol, 0, prec, 0.1, 0.0, 0};
   int its = 0;
-  auto solve_eta = [&](int k) -> int {
-    qed3_solve_report r{};
-    int e = cg_solve(d, eta + nd * k, phi + nd * k, &sp, &r, st);
-    its += r.iters;
-    if (!e && r.status != QED3_OK) e = fail(QED3_ERR_NOCONV, "pseudofermion solve did not converge");
-    return e;
-  };
+  auto solve_eta = [&](int k) -> int { return fo.solve(eta + nd * k, phi + nd * k, &its); };
   auto run = [&]() -> int {
     int e;
     QED3_CUDA_TRY(cudaMemcpyAsync(G.pi, pi.data(), size_t(Nl) * sizeof(double), cudaMemcpyHostToDevice, st));
     QED3_CUDA_TRY(cudaMemcpyAsync(G.pi0, G.pi, size_t(Nl) * sizeof(double), cudaMemcpyDeviceToDevice, st));
     QED3_CUDA_TRY(cudaMemcpyAsync(G.A0, A, size_t(Nl) * sizeof(double), cudaMemcpyDeviceToDevice, st));
     QED3_CUDA_TRY(cudaMemcpyAsync(dxi, xi.data(), vbytes, cudaMemcpyHostToDevice, st));
-    if ((e = dirac_set_links(d, A, 1, st))) return e;
+    if ((e = fo.update(A))) return e;
     for (int k = 0; k < npf; k++)
-      if ((e = dirac_apply_ref(d, QED3_OP_DDAG, phi + nd * k, dxi + nd * k, st))) return e;
+      if ((e = fo.apply_dag(phi + nd * k, dxi + nd * k))) return e;
     for (int k = 0; k < npf; k++)
       if ((e = solve_eta(k))) return e;
     QED3_CUDA_TRY(cudaMemcpyAsync(eta0, eta, vbytes, cudaMemcpyDeviceToDevice, st));
     if ((e = gauge_plaquettes(lat, A, G.th0, st))) return e;
     const double tau = tmax / nsteps, tau_in = tau / nsteps_inner;
     auto fermion_kick = [&](int k, double c) -> int {
-      int f = fermion_force(d, eta + nd * k, Ff, st);
+      int f = fo.force(eta + nd * k, Ff);
       if (!f) k_axpy<<<nblk(Nl), 256, 0, st>>>(Nl, -c, Ff, G.pi);
       return f;
     };
@@ -471,7 +481,7 @@ int hmc_fermion(qed3_lattice_s* lat, qed3_dirac_s* d, qed3_rng_s* rng, double* A
         k_axpy<<<nblk(Nl), 256, 0, st>>>(Nl, tau_in, G.pi, A);
         if ((e = gauge_kick((m != nsteps_inner - 1 ? 1.0 : 0.5) * tau_in))) return e;
       }
-      if ((e = dirac_set_links(d, A, 1, st))) return e;
+      if ((e = fo.update(A))) return e;
       for (int k = 0; k < npf; k++) {
         if ((e = solve_eta(k))) return e;
         if ((e = fermion_kick(k, (n != nsteps - 1 ? 1.0 : 0.5) * tau))) return e;
@@ -498,7 +508,7 @@ int hmc_fermion(qed3_lattice_s* lat, qed3_dirac_s* d, qed3_rng_s* rng, double* A
     } else {
       *accepted = 0;
       QED3_CUDA_TRY(cudaMemcpyAsync(A, G.A0, size_t(Nl) * sizeof(double), cudaMemcpyDeviceToDevice, st));
-      if ((e = dirac_set_links(d, A, 1, st))) return e;
+      if ((e = fo.update(A))) return e;
     }
     QED3_CUDA_TRY(cudaStreamSynchronize(st));
     return QED3_OK;
@@ -506,6 +516,54 @@ int hmc_fermion(qed3_lattice_s* lat, qed3_dirac_s* d, qed3_rng_s* rng, double* A
   rc = run();
   cleanup();
   return rc;
+}
+
+int hmc_fermion(qed3_lattice_s* lat, qed3_dirac_s* d, qed3_rng_s* rng, double* A, double beta, int compact, int exact,
+                double tmax, int nsteps, int nsteps_inner, int npf, double tol, int prec, int no_reject, int* accepted,
+                double* dH_out, int* cg_iters, cudaStream_t st) {
+  const qed3_solve_params sp{tol, 0, prec, 0.1, 0.0, 0};
+  HmcFermion fo;
+  fo.update = [&](const double* U) { return dirac_set_links(d, U, 1, st); };
+  fo.apply_dag = [&](double* phi, const double* xi) { return dirac_apply_ref(d, QED3_OP_DDAG, phi, xi, st); };
+  fo.solve = [&](double* eta, const double* phi, int* its) {
+    qed3_solve_report r{};
+    int e = cg_solve(d, eta, phi, &sp, &r, st);
+    *its += r.iters;
+    if (!e && r.status != QED3_OK) e = fail(QED3_ERR_NOCONV, "pseudofermion solve did not converge");
+    return e;
+  };
+  fo.force = [&](const double* eta, double* F) { return fermion_force(d, eta, F, st); };
+  return hmc_trajectory(lat, fo, 4LL * d->Ns, rng, A, beta, compact, exact, tmax, nsteps, nsteps_inner, npf,
+                        no_reject, accepted, dH_out, cg_iters, st);
+}
+
+// Overlap fermions (the reference's IS_OVERLAP build of HMC2): the operator
+// update is Overlap::update (src/both_3d/overlap.h:207-216: Wilson links, then
+// lambda bounds by power iterations and new Zolotarev coefficients) unless
+// fixed bounds lmin, lmax > 0 are given; eta = (D_ov^dag D_ov)^{-1} phi by the
+// outer CG; the force is the overlap force (src/both_3d/overlap.h:393-470).
+int hmc_overlap(qed3_lattice_s* lat, qed3_overlap_s* ov, qed3_rng_s* rng, double* A, double beta, int compact,
+                int exact, double tmax, int nsteps, int nsteps_inner, int npf, double lmin, double lmax, double tol,
+                double tol_inner, int no_reject, int* accepted, double* dH_out, int* cg_iters, cudaStream_t st) {
+  qed3_dirac_s* d = overlap_dirac(ov);
+  HmcFermion fo;
+  fo.update = [&](const double* U) {
+    int e = dirac_set_links(d, U, 1, st);
+    return e ? e : overlap_update(ov, lmin, lmax, tol_inner, st);
+  };
+  fo.apply_dag = [&](double* phi, const double* xi) {
+    return overlap_apply(ov, QED3_OP_DDAG, phi, xi, tol_inner, nullptr, st);
+  };
+  fo.solve = [&](double* eta, const double* phi, int* its) {
+    qed3_solve_report r{};
+    int e = overlap_solve(ov, eta, phi, tol, tol_inner, 100000, &r, st);
+    *its += r.iters;
+    if (!e && r.status != QED3_OK) e = fail(QED3_ERR_NOCONV, "overlap pseudofermion solve did not converge");
+    return e;
+  };
+  fo.force = [&](const double* eta, double* F) { return overlap_force(ov, eta, F, tol_inner, nullptr, st); };
+  return hmc_trajectory(lat, fo, 4LL * d->Ns, rng, A, beta, compact, exact, tmax, nsteps, nsteps_inner, npf,
+                        no_reject, accepted, dH_out, cg_iters, st);
 }
 
 }  // namespace qed3

@@ -414,6 +414,8 @@ int overlap_solve(qed3_overlap_s* ov, double* x, const double* b, double tol, do
 }  // namespace qed3
 
 namespace qed3 {
+qed3_dirac_s* overlap_dirac(qed3_overlap_s* ov) { return ov->d; }
+
 int overlap_info(const qed3_overlap_s* ov, double* lmin, double* lmax, double* k, double* delta, int* np,
                  int* np_fp64) {
   if (np_fp64) *np_fp64 = ov->nh;

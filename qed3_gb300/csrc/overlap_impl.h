@@ -15,6 +15,7 @@ int overlap_force(qed3_overlap_s* ov, const double* eta, double* F, double tol, 
                   cudaStream_t st);
 int overlap_solve(qed3_overlap_s* ov, double* x, const double* b, double tol, double tol_inner, int maxiter,
                   qed3_solve_report* rep, cudaStream_t st);
+qed3_dirac_s* overlap_dirac(qed3_overlap_s* ov);
 int overlap_info(const qed3_overlap_s* ov, double* lmin, double* lmax, double* k, double* delta, int* np,
                  int* np_fp64);
 }  // namespace qed3

@@ -166,3 +166,72 @@ def test_ill_conditioned_poles_run_in_fp64(cuda):
     # FP64 overlap: one launch, nothing split off
     ov64 = Q.Overlap(Dq, 41, Q.PREC_F64)
     assert ov64.update(lmin, lmax)["npoles_fp64"] == 0
+
+
+def test_overlap_hmc_matches_oracle(cuda):
+    """Overlap-fermion HMC (HMC2::run with Overlap fermions, fixed spectral
+    bounds) against the oracle's composition of its overlap pieces from the
+    same RNG streams: same Metropolis decisions, dH and links."""
+    n = 2
+    g = O.geometry(n)
+    lat = Q.S2Trivalent(n)
+    ro, rq = O.Rng(g, 21), Q.ParallelRng(lat, 21)
+    A0 = ro.gaussian_links(0.2)
+    assert np.array_equal(A0, rq.gaussian_links(0.2))
+    Do = O.Dirac(g, 1.0, -1.0)
+    Do.update(A0)
+    lmin, lmax = Do.lambda_bounds()
+    Dq = Q.DiracS2Dual(lat, 1.0, -1.0)
+    Dq.update(to_dev(A0, cuda))
+    ov = Q.Overlap(Dq, 21, Q.PREC_F64)
+    ov.update(lmin, lmax)
+    Ao = np.ascontiguousarray(A0.copy())
+    At = to_dev(A0, cuda)
+    for it in range(2):
+        acc_o, dh_o, its_o = O.hmc_overlap(g, Do, ro, Ao, 1.4, tmax=0.5, nsteps=4, nsteps_inner=4, lmin=lmin,
+                                           lmax=lmax, order=21, tol=1e-11, tol_inner=1e-13)
+        acc_q, dh_q, its_q = Q.hmc_overlap(lat, ov, rq, At, 1.4, tmax=0.5, nsteps=4, nsteps_inner=4,
+                                           lambda_min=lmin, lambda_max=lmax, tol=1e-11, tol_inner=1e-13)
+        assert acc_o == acc_q and its_q > 0
+        assert abs(dh_o - dh_q) < 1e-7, (dh_o, dh_q)
+        assert np.abs(from_dev(At) - Ao).max() < 1e-9
+
+
+def test_overlap_hmc_dH_scales_as_tau_squared(cuda):
+    n = 2
+    lat = Q.S2Trivalent(n)
+    A0 = Q.ParallelRng(lat, 22).gaussian_links(0.2)
+    Dq = Q.DiracS2Dual(lat, 1.0, -1.0)
+    Dq.update(to_dev(A0, cuda))
+    ov = Q.Overlap(Dq, 21, Q.PREC_F32)
+    info = ov.update()
+    dh = []
+    for ns in (16, 32):
+        At = to_dev(A0, cuda)
+        _, d, _ = Q.hmc_overlap(lat, ov, Q.ParallelRng(lat, 23), At, 1.4, tmax=0.5, nsteps=ns, nsteps_inner=2,
+                                lambda_min=info["lambda_min"], lambda_max=info["lambda_max"], tol=1e-11,
+                                tol_inner=1e-12, no_reject=True)
+        dh.append(abs(d))
+    assert 2.8 < dh[0] / dh[1] < 5.5, dh
+
+
+def test_overlap_hmc_recomputed_bounds(cuda):
+    """lambda_min = lambda_max = 0: every operator update re-estimates the
+    bounds (Overlap::update); after the trajectory the overlap holds the
+    bounds of the final links."""
+    n = 2
+    lat = Q.S2Trivalent(n)
+    A0 = Q.ParallelRng(lat, 24).gaussian_links(0.2)
+    At = to_dev(A0, cuda)
+    Dq = Q.DiracS2Dual(lat, 1.0, -1.0)
+    Dq.update(At)
+    ov = Q.Overlap(Dq, 21, Q.PREC_F32)
+    ov.update()
+    acc, d, its = Q.hmc_overlap(lat, ov, Q.ParallelRng(lat, 25), At, 1.4, tmax=0.25, nsteps=4, nsteps_inner=2,
+                                tol=1e-10, tol_inner=1e-12, no_reject=True)
+    assert acc and np.isfinite(d) and abs(d) < 0.5 and its > 0
+    before = ov.info()
+    Dq.update(At)
+    after = ov.update(tol_outer=1e-12)
+    assert abs(before["lambda_max"] / after["lambda_max"] - 1) < 1e-6
+    assert abs(before["lambda_min"] / after["lambda_min"] - 1) < 1e-4
