@@ -554,32 +554,63 @@ int batch_launch(int prec, int R, BatchArgs& args, int grid, int threads, cudaSt
   return QED3_DISPATCH_R(PBF16, R, launch, args, grid, threads, st);
 }
 
-// import nrhs reference-order vectors into a site-major interleaved field
+// Right-hand-side norms |b_r| (reference order, one block per right-hand
+// side, fixed summation order).  The solve runs on b / |b| and the solution is
+// scaled back on export, so the reduced-precision iterations see unit-scale
+// vectors whatever the scale of b: an FP32 residual of a tiny right-hand side
+// would otherwise underflow before the tolerance.
+__global__ void k_rhs_norm(int Ns, int nrhs, long long stride, const S64* __restrict__ in, double* __restrict__ nrm) {
+  __shared__ double sh[32];
+  const int r = blockIdx.x;
+  if (r >= nrhs) return;
+  double v[1] = {0.0};
+  for (int x = threadIdx.x; x < Ns; x += blockDim.x) {
+    const Sp64 a = ld64(in + size_t(r) * stride, x);
+    v[0] += a.s0.x * a.s0.x + a.s0.y * a.s0.y + a.s1.x * a.s1.x + a.s1.y * a.s1.y;
+  }
+  block_sum<1>(v, sh);
+  if (threadIdx.x == 0) nrm[r] = sqrt(v[0]);
+}
+
+// import nrhs reference-order vectors, each divided by its norm, into a
+// site-major interleaved field
 __global__ void k_import_interleaved(int Ns, int R, int nrhs, long long stride, const int* __restrict__ perm,
-                                     const S64* __restrict__ in, S64* __restrict__ out) {
+                                     const S64* __restrict__ in, const double* __restrict__ nrm,
+                                     S64* __restrict__ out) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= Ns) return;
   const int x = perm[i];
   for (int r = 0; r < R; r++) {
     Sp64 v{make_double2(0, 0), make_double2(0, 0)};
-    if (r < nrhs) v = ld64(in + size_t(r) * stride, x);
+    if (r < nrhs && nrm[r] > 0.0) {
+      const double inv = 1.0 / nrm[r];
+      v = ld64(in + size_t(r) * stride, x);
+      v.s0 = cscale(inv, v.s0);
+      v.s1 = cscale(inv, v.s1);
+    }
     st64(out, i * R + r, v);
   }
 }
 __global__ void k_export_interleaved(int Ns, int R, int nrhs, const int* __restrict__ perm, const S64* __restrict__ in0,
-                                     const S64* __restrict__ in1, const double* __restrict__ scal, S64* __restrict__ out) {
+                                     const S64* __restrict__ in1, const double* __restrict__ scal,
+                                     const double* __restrict__ nrm, S64* __restrict__ out) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= Ns) return;
   const int x = perm[i];
   for (int r = 0; r < nrhs; r++) {
     const S64* src = (scal[6 * r + 5] != 0.0) ? in1 : in0;
-    st64(out + size_t(r) * Ns, x, ld64(src, i * R + r));
+    Sp64 v = ld64(src, i * R + r);
+    v.s0 = cscale(nrm[r], v.s0);
+    v.s1 = cscale(nrm[r], v.s1);
+    st64(out + size_t(r) * Ns, x, v);
   }
 }
 
 int batch_import(const BatchSys& s, const qed3_dirac_s* d, const double* b_ref, int R, bool bcast, cudaStream_t st) {
-  k_import_interleaved<<<(s.Ns + 255) / 256, 256, 0, st>>>(s.Ns, R, s.nrhs, bcast ? 0LL : (long long)s.Ns,
-                                                         d->lat->dev.perm, reinterpret_cast<const S64*>(b_ref),
+  const long long stride = bcast ? 0LL : (long long)s.Ns;
+  k_rhs_norm<<<s.nrhs, 256, 0, st>>>(s.Ns, s.nrhs, stride, reinterpret_cast<const S64*>(b_ref), s.bnorm);
+  k_import_interleaved<<<(s.Ns + 255) / 256, 256, 0, st>>>(s.Ns, R, s.nrhs, stride, d->lat->dev.perm,
+                                                         reinterpret_cast<const S64*>(b_ref), s.bnorm,
                                                          const_cast<S64*>(s.b));
   QED3_CUDA_TRY(cudaGetLastError());
   return QED3_OK;
@@ -587,7 +618,7 @@ int batch_import(const BatchSys& s, const qed3_dirac_s* d, const double* b_ref, 
 
 int batch_export(const BatchSys& s, const qed3_dirac_s* d, double* x_ref, int R, cudaStream_t st) {
   k_export_interleaved<<<(s.Ns + 255) / 256, 256, 0, st>>>(s.Ns, R, s.nrhs, d->lat->dev.perm, s.xhi, s.xhi2, s.scal,
-                                                         reinterpret_cast<S64*>(x_ref));
+                                                         s.bnorm, reinterpret_cast<S64*>(x_ref));
   QED3_CUDA_TRY(cudaGetLastError());
   return QED3_OK;
 }
@@ -695,8 +726,11 @@ static int batch_build(qed3_batch_s* bt) {
     s.rh = p[8];
     s.th = p[9];
   }
-  QED3_CUDA_TRY(cudaMalloc(&bt->d_scal, sizeof(double) * 6 * R * nsys));
-  for (int i = 0; i < nsys; i++) bt->sys[i].scal = bt->d_scal + size_t(6) * R * i;
+  QED3_CUDA_TRY(cudaMalloc(&bt->d_scal, sizeof(double) * 7 * R * nsys));
+  for (int i = 0; i < nsys; i++) {
+    bt->sys[i].scal = bt->d_scal + size_t(6) * R * i;
+    bt->sys[i].bnorm = bt->d_scal + size_t(6) * R * nsys + size_t(R) * i;
+  }
   QED3_CUDA_TRY(cudaMalloc(&bt->d_sys, sizeof(BatchSys) * nsys));
   QED3_CUDA_TRY(cudaMalloc(&bt->d_sys_of_block, sizeof(int) * sob.size()));
   QED3_CUDA_TRY(cudaMemcpy(bt->d_sys_of_block, sob.data(), sizeof(int) * sob.size(), cudaMemcpyHostToDevice));

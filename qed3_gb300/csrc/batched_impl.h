@@ -32,6 +32,7 @@ struct BatchSys {
   void* rh;      // bf16 copies of r and t for the neighbour gathers (bf16 mode)
   void* th;
   double* scal;  // [nrhs][6]: mu_true, bnorm2, iters, reliable updates, status, x buffer
+  double* bnorm; // [nrhs]: |b| of each right-hand side (the kernel solves for b / |b|)
 };
 
 struct BatchArgs {

@@ -155,3 +155,22 @@ def test_batched_graph_capture_replay(cuda):
             for r in range(bn.shape[0]):
                 res = np.linalg.norm(bn[r] - Do.apply(xh[r], 2) - sh[r] * xh[r]) / np.linalg.norm(bn[r])
                 assert res <= 1.05e-10, (trial, r, res)
+
+
+@pytest.mark.parametrize("scale", [1e-30, 1e30])
+def test_batched_scale_invariance(cuda, scale):
+    """Right-hand sides far from unit scale: the reduced-precision iterations run
+    on b / |b|, so the solution is the unit-scale solution times the scale (to
+    the tolerance) instead of an FP32 underflow or overflow."""
+    sy = _systems(cuda, ns=(4,), nrhs=(3,), seed=55)
+    g, lat, Do, Dq, b = sy[0]
+    batch = Q.Batch([(Dq, 3)], precision=Q.PREC_F32, rhs_tile=4, threads=128)
+    bt = to_dev(b, cuda)
+    x1 = [bt.clone() * 0]
+    reps1, _ = batch.solve(x1, [bt], tol=1e-12, precision=Q.PREC_F32)
+    xs = [bt.clone() * 0]
+    reps, _ = batch.solve(xs, [bt * scale], tol=1e-12, precision=Q.PREC_F32)
+    assert all(r.status == Q.OK and r.true_rel_res <= 1e-12 for r in reps), reps
+    assert [r.iters for r in reps] == [r.iters for r in reps1]
+    x, xr = from_dev(xs[0]), from_dev(x1[0]) * scale
+    assert np.abs(x - xr).max() <= 1e-13 * np.abs(xr).max()
