@@ -401,7 +401,7 @@ def main():
                          "in apply_sweep"},
             "apply_sweep": sweep,
             "e2e": {"value": e2e, "unit": "solves/s", "h2d_bytes_per_step": b.nbytes, "d2h_bytes_per_step": b.nbytes},
-            "gpu_launches": args.steps * 3,
+            "gpu_launches": args.steps * 4,  # |b| partials, unit-norm import, solver, scaled export
             "clocks": clocks_info}
     if rank == 0 and not args.no_cpu_baseline:
         dt, it, res, cores = cpu_reference_solve(b, A.cpu().numpy())

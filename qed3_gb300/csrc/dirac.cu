@@ -9,6 +9,7 @@
 // three 2x2 blocks and its neighbours' two-spinors: 276 B/site in FP64,
 // 144 B in FP32, 128 B with bf16 spinors.
 
+#include <algorithm>
 #include <cmath>
 #include <complex>
 #include <cstring>
@@ -148,6 +149,59 @@ __global__ void k_export(int Ns, int nrhs, const int* __restrict__ perm, const v
 }
 
 static inline int nblk(long long n, int t = 256) { return int((n + t - 1) / t); }
+
+// Unit-norm import for the solvers: block partials of |b|^2, then every block
+// of the import sums the partials in the same fixed order (one warp), divides
+// b by |b| and block 0 stores |b|.  The solvers iterate on b / |b| so their
+// FP32/BF16 vectors stay near unit scale whatever the scale of b (a residual
+// of a right-hand side with |b_i| ~ 1e-20 would underflow in FP32, one with
+// |b_i| ~ 1e20 would overflow); the export multiplies the solution by |b|.
+constexpr int kNormParts = 256;
+
+__global__ void k_norm_part(long long n, const double* __restrict__ in, double* __restrict__ part) {
+  __shared__ double sh[32];
+  double v[1] = {0.0};
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    v[0] += in[i] * in[i];
+  block_sum<1>(v, sh);
+  if (threadIdx.x == 0) part[blockIdx.x] = v[0];
+}
+
+__global__ void k_import_unit(int Ns, const int* __restrict__ perm, const S64* __restrict__ in,
+                              const double* __restrict__ part, int nparts, S64* __restrict__ out,
+                              double* __restrict__ nrm_out) {
+  __shared__ double inv_s;
+  if (threadIdx.x < 32) {
+    double s = 0.0;
+    for (int k = threadIdx.x; k < nparts; k += 32) s += part[k];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (threadIdx.x == 0) {
+      const double nr = sqrt(s);
+      inv_s = nr > 0.0 ? 1.0 / nr : 0.0;
+      if (blockIdx.x == 0) *nrm_out = nr;
+    }
+  }
+  __syncthreads();
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= Ns) return;
+  const double inv = inv_s;
+  Sp64 v = ld64(in, perm[i]);
+  v.s0 = cscale(inv, v.s0);
+  v.s1 = cscale(inv, v.s1);
+  st64(out, i, v);
+}
+
+__global__ void k_export_scaled(int Ns, const int* __restrict__ perm, const S64* __restrict__ in,
+                                const double* __restrict__ nrm, S64* __restrict__ out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= Ns) return;
+  const double s = *nrm;
+  Sp64 v = ld64(in, i);
+  v.s0 = cscale(s, v.s0);
+  v.s1 = cscale(s, v.s1);
+  st64(out, perm[i], v);
+}
 
 // ---------------------------------------------------------------------------
 // Host side
@@ -309,6 +363,22 @@ int field_import(qed3_dirac_s* d, int prec, void* field, const double* in_ref, i
   if (prec == QED3_PREC_F64) k_import<P64><<<g, 256, 0, st>>>(d->Ns, nrhs, D.perm, in, field);
   else if (prec == QED3_PREC_F32) k_import<P32><<<g, 256, 0, st>>>(d->Ns, nrhs, D.perm, in, field);
   else k_import<PBF16><<<g, 256, 0, st>>>(d->Ns, nrhs, D.perm, in, field);
+  QED3_CUDA_TRY(cudaGetLastError());
+  return QED3_OK;
+}
+
+int field_import_unit(qed3_dirac_s* d, S64* field, const double* in_ref, double* part, double* nrm, cudaStream_t st) {
+  const long long n = 4LL * d->Ns;
+  const int parts = std::min(kNormParts, nblk(n));
+  k_norm_part<<<parts, 256, 0, st>>>(n, in_ref, part);
+  k_import_unit<<<nblk(d->Ns), 256, 0, st>>>(d->Ns, d->lat->dev.perm, reinterpret_cast<const S64*>(in_ref), part,
+                                              parts, field, nrm);
+  QED3_CUDA_TRY(cudaGetLastError());
+  return QED3_OK;
+}
+
+int field_export_scaled(qed3_dirac_s* d, double* out_ref, const S64* field, const double* nrm, cudaStream_t st) {
+  k_export_scaled<<<nblk(d->Ns), 256, 0, st>>>(d->Ns, d->lat->dev.perm, field, nrm, reinterpret_cast<S64*>(out_ref));
   QED3_CUDA_TRY(cudaGetLastError());
   return QED3_OK;
 }

@@ -95,7 +95,7 @@ int cg_solve_noalloc(qed3_dirac_s* d, double* x, const double* b, const qed3_sol
   const double shift = prm ? prm->shift : 0.0;
 
   const auto t0 = std::chrono::steady_clock::now();
-  if ((rc = field_import(d, QED3_PREC_F64, f[0], b, 1, st))) return rc;
+  if ((rc = field_import_unit(d, f[0], b, partials, scal + 6, st))) return rc;
   QED3_CUDA_TRY(cudaMemsetAsync(bar, 0, sizeof(GridBar), st));  // the barrier must start at zero
   rc = cg_launch_on_scratch(prec, d, f[0], f[1], f[2], f[3], f[4], f[5], f[6], f[7], f[8], f[9], partials,
                             kNoallocMaxBlocks, bar, scal, tol, delta, maxiter, shift, st);
@@ -104,7 +104,7 @@ int cg_solve_noalloc(qed3_dirac_s* d, double* x, const double* b, const qed3_sol
   QED3_CUDA_TRY(cudaMemcpyAsync(sc, scal, sizeof(sc), cudaMemcpyDeviceToHost, st));
   QED3_CUDA_TRY(cudaStreamSynchronize(st));
   S64* xres = (sc[5] != 0.0) ? f[2] : f[1];
-  if ((rc = field_export(d, QED3_PREC_F64, x, xres, 1, st))) return rc;
+  if ((rc = field_export_scaled(d, x, xres, scal + 6, st))) return rc;
   QED3_CUDA_TRY(cudaStreamSynchronize(st));
   const double ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
   qed3_solve_report r{};

@@ -976,7 +976,7 @@ int pcg_solve(qed3_dirac_s* d, qed3_lpc_s* L, double* x, const double* b, const 
   const bool pipelined = want_pipe && ppcg_plan(prec, co.nwords, d->Ns, L->per, d->sm_count, &grid, &smem);
   if (!pipelined && !pcg_plan(prec, co.nwords, d->Ns, L->per, d->sm_count, &grid, &threads, &spt, &smem))
     return fail(QED3_ERR_ARG, "lattice too large for the register-resident preconditioned solver");
-  if ((rc = field_import(d, QED3_PREC_F64, w.b, b, 1, st))) return rc;
+  if ((rc = field_import_unit(d, w.b, b, w.partials, w.scal + 6, st))) return rc;
   if (pipelined) QED3_CUDA_TRY(cudaMemsetAsync(w.xhi, 0, size_t(d->Ns) * 4 * sizeof(double), st));
   QED3_CUDA_TRY(cudaMemsetAsync(w.bar2, 0, sizeof(GridBar2), st));
   PcgArgs a{};

@@ -488,7 +488,7 @@ int cg_solve(qed3_dirac_s* d, double* x, const double* b, const qed3_solve_param
   const int maxiter = prm && prm->maxiter > 0 ? prm->maxiter : 100000;
   const double shift = prm ? prm->shift : 0.0;
 
-  rc = field_import(d, QED3_PREC_F64, w.b, b, 1, st);
+  rc = field_import_unit(d, w.b, b, w.partials, w.scal + 6, st);
   if (rc) return rc;
   // register-resident kernel when every site can own a thread
   int vgrid = 0, vthreads = 0, vspt = 0;
@@ -569,7 +569,7 @@ int cg_finish(qed3_dirac_s* d, double* x, qed3_solve_report* rep, cudaStream_t s
   QED3_CUDA_TRY(cudaMemcpyAsync(sc, w.scal, 6 * sizeof(double), cudaMemcpyDeviceToHost, st));
   QED3_CUDA_TRY(cudaStreamSynchronize(st));
   S64* xres = (sc[5] != 0.0) ? w.xhi2 : w.xhi;
-  rc = field_export(d, QED3_PREC_F64, x, xres, 1, st);
+  rc = field_export_scaled(d, x, xres, w.scal + 6, st);
   if (rc) return rc;
   qed3_solve_report r{};
   r.status = int(sc[4]);

@@ -111,3 +111,24 @@ def test_multishift_matches_oracle(cuda, n):
     # larger shifts converge (and stop) no later than the base shift
     its = [r.iters for r in reps]
     assert its == sorted(its, reverse=True)
+
+
+@pytest.mark.parametrize("prec", [Q.PREC_F64, Q.PREC_F32, Q.PREC_BF16])
+@pytest.mark.parametrize("streaming", [False, True])
+def test_solve_scale_invariance(cuda, prec, streaming):
+    """Right-hand sides scaled by 1e-30 and 1e30: the solvers iterate on b / |b|
+    (reduced-precision vectors stay near unit scale) and return |b| x, so the
+    iterations and the scaled solution match the unit-scale solve."""
+    import torch
+    g, lat, Do, Dq, b = _setup(8, 0.1, 91, cuda)
+    bt = to_dev(b, cuda)
+    flags = Q.SOLVE_STREAMING if streaming else 0
+    x1 = torch.zeros_like(bt)
+    r1 = Dq.solve(x1, bt, tol=1e-10, precision=prec, flags=flags)
+    assert r1.status == Q.OK
+    for scale in (1e-30, 1e30):
+        xs = torch.zeros_like(bt)
+        rs = Dq.solve(xs, bt * scale, tol=1e-10, precision=prec, flags=flags)
+        assert rs.status == Q.OK and rs.true_rel_res <= 1e-10, (scale, rs)
+        assert abs(rs.iters - r1.iters) <= 2
+        assert float((xs / scale - x1).norm() / x1.norm()) < 1e-8

@@ -319,3 +319,20 @@ def test_pipelined_pcg_matches_two_barrier(cuda, prec):
     for shift in (0.0, 0.2):
         a, c = reps[(False, shift)], reps[(True, shift)]
         assert abs(a - c) <= max(4, a // 20)
+
+
+@pytest.mark.parametrize("flexible", [False, True])
+def test_pcg_scale_invariance(cuda, flexible):
+    """b far from unit scale: the preconditioned solve iterates on b / |b| and
+    rescales the solution, so FP32/BF16 vectors neither underflow nor overflow."""
+    rng, g, lat, A, Do, Dq = _setup(8, M5=0.1, seed=13)
+    pc = Q.LearnedPreconditioner(Dq, channels=4, layers=1, seed=4)
+    bt = to_dev(rand_spinor(rng, g.n_sites), cuda)
+    x1 = torch.zeros_like(bt)
+    r1 = pc.solve(Dq, x1, bt, tol=1e-10, precision=Q.PREC_F32, flexible=flexible)
+    for scale in (1e-30, 1e30):
+        xs = torch.zeros_like(bt)
+        rs = pc.solve(Dq, xs, bt * scale, tol=1e-10, precision=Q.PREC_F32, flexible=flexible)
+        assert rs.status == Q.OK and rs.true_rel_res <= 1e-10, (scale, rs)
+        assert abs(rs.iters - r1.iters) <= 2
+        assert float((xs / scale - x1).norm() / x1.norm()) < 1e-8
