@@ -137,6 +137,17 @@ int qed3_cg_solve(qed3_dirac* d, double* x, const double* b, const qed3_solve_pa
                   qed3_solve_report* report, void* stream);
 int qed3_solver_last_report(qed3_dirac* d, qed3_solve_report* report);
 
+/* BiCGStab with restarts  --  replaces MatPoly::bicgstab
+ * (src/dual/matpoly.h:366-479), which the reference keeps for experiments.
+ * Solves (op + shift) x = b for op = QED3_OP_D, _DDAG or _DDAGD (device
+ * complex128, reference order) in FP64 (params->precision must be
+ * QED3_PREC_F64), with the reference's start x0 = b, its stopping rules
+ * (|r|^2 < tol^2 |r0|^2, or |t|^2 < eps absolute) and restarts
+ * (|<rc,r>| < eps).  eps < 0 selects the reference default 1e-8.  The
+ * report's true_rel_res is ||b - (op + shift) x|| / ||b||. */
+int qed3_bicgstab_solve(qed3_dirac* d, int op, double* x, const double* b, const qed3_solve_params* params,
+                        double eps, qed3_solve_report* report, void* stream);
+
 /* Allocation-free CG solve.  No counterpart in the reference: it exists for
  * callers that cannot allocate device memory at solve time -- code inside
  * CUDA stream capture, hosts whose device memory is owned by another

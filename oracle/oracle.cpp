@@ -818,6 +818,82 @@ int orc_cg(const OracleDirac* d, double shift, double* x_out, const double* b_in
   return k + 1;
 }
 
+// BiCGStab with restarts, restating MatPoly::bicgstab (src/dual/matpoly.h:366-479)
+// on A = op + shift (op 0: D, 1: D^dag, 2: D^dag D): x0 = b, r = rc = b - A x0,
+// stop on |r|^2 < tol^2 |r0|^2 or |t|^2 < eps (before x takes the al p step),
+// restart rc = p = r when |<rc,r>| < eps or |r|^2 > 2 |r_prev|^2.  Returns the
+// iterations (loop passes); *status_out = 0 converged / 1 maxiter or NaN.
+int orc_bicgstab(const OracleDirac* d, int op, double shift, double* x_out, const double* b_in, double tol,
+                 int maxiter, double eps, int* status_out) {
+  const Idx N = d->N;
+  const cplx* b = reinterpret_cast<const cplx*>(b_in);
+  cplx* x = reinterpret_cast<cplx*>(x_out);
+  std::vector<cplx> p(N), t(N), Ap(N), At(N), r(N), rc(N), tmp(N);
+  auto A = [&](cplx* out, const cplx* in) {
+    if (op == 0) {
+      csr_mult(d, false, out, in);
+    } else if (op == 1) {
+      csr_mult(d, true, out, in);
+    } else {
+      csr_mult(d, false, tmp.data(), in);
+      csr_mult(d, true, out, tmp.data());
+    }
+    if (shift != 0.0)
+      for (Idx i = 0; i < N; i++) out[i] += shift * in[i];
+  };
+  for (Idx i = 0; i < N; i++) x[i] = b[i];
+  A(Ap.data(), x);
+  for (Idx i = 0; i < N; i++) r[i] = -1.0 * Ap[i] + b[i];
+  rc = r;
+  p = r;
+  double mu = zdotc(r.data(), r.data(), N).real();
+  double mu_old = mu;
+  const double mu_crit = tol * tol * mu;
+  int n = 0, status = 0;
+  // r0 = 0 (x0 = b already solves the system, e.g. b = 0): nothing to do,
+  // where the reference's assert on <rc,r> would stop the program
+  const bool ran = !(mu < mu_crit) && mu > 0.0;
+  if (ran) {
+    status = 1;
+    for (; n < maxiter; n++) {
+      A(Ap.data(), p.data());
+      cplx g1 = zdotc(rc.data(), r.data(), N), g2 = zdotc(rc.data(), Ap.data(), N);
+      const cplx al = g1 / g2;
+      for (Idx i = 0; i < N; i++) t[i] = -al * Ap[i] + r[i];
+      if (zdotc(t.data(), t.data(), N).real() < eps) {
+        status = 0;
+        break;
+      }
+      A(At.data(), t.data());
+      g1 = zdotc(t.data(), At.data(), N);
+      g2 = zdotc(At.data(), At.data(), N);
+      const cplx om = g1 / g2;
+      for (Idx i = 0; i < N; i++) x[i] = al * p[i] + x[i];
+      for (Idx i = 0; i < N; i++) x[i] = om * t[i] + x[i];
+      g2 = zdotc(rc.data(), r.data(), N);
+      for (Idx i = 0; i < N; i++) r[i] = -om * At[i] + t[i];
+      g1 = zdotc(rc.data(), r.data(), N);
+      const cplx bet = al / om * g1 / g2;
+      mu = zdotc(r.data(), r.data(), N).real();
+      if (mu < mu_crit) {
+        status = 0;
+        break;
+      }
+      if (std::isnan(mu)) break;
+      mu_old = mu;
+      for (Idx i = 0; i < N; i++) p[i] = -om * Ap[i] + p[i];
+      for (Idx i = 0; i < N; i++) p[i] = bet * p[i] + r[i];
+      const cplx gam = zdotc(rc.data(), r.data(), N);
+      if (std::abs(gam) < eps || 2.0 * mu_old < mu) {
+        rc = r;
+        p = r;
+      }
+    }
+  }
+  if (status_out) *status_out = status;
+  return ran ? (n < maxiter ? n + 1 : n) : 0;
+}
+
 // ===========================================================================
 // Zolotarev rational approximation of sign(x) on [k,1], restating
 // src/both_3d/overlap.h:7-134 (A.D. Kennedy, hep-lat/0402038).

@@ -55,6 +55,9 @@ def lib():
         L.orc_dirac_nnz.argtypes = [vp]
         L.orc_dirac_get_csr.argtypes = [vp, c_int_p, c_int_p, ctypes.c_void_p]
         L.orc_dirac_get_kappa.argtypes = [vp, c_double_p]
+        L.orc_bicgstab.restype = ctypes.c_int
+        L.orc_bicgstab.argtypes = [vp, ctypes.c_int, ctypes.c_double, ctypes.c_void_p, ctypes.c_void_p,
+                                   ctypes.c_double, ctypes.c_int, ctypes.c_double, c_int_p]
         L.orc_cg.restype = ctypes.c_int
         L.orc_cg.argtypes = [vp, ctypes.c_double, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_double,
                              ctypes.c_int, c_double_p]
@@ -216,6 +219,15 @@ class Dirac:
         mu = ctypes.c_double()
         it = lib().orc_cg(self.h, shift, _p(x), _p(b), tol, maxiter, ctypes.byref(mu))
         return x, it, mu.value
+
+    def bicgstab(self, b: np.ndarray, op: int = 0, tol: float = 1e-10, maxiter: int = 100000, shift: float = 0.0,
+                 eps: float = 1e-8):
+        """MatPoly::bicgstab restated on (op + shift) x = b; returns (x, iterations, converged)."""
+        b = np.ascontiguousarray(b, dtype=np.complex128)
+        x = np.zeros_like(b)
+        st = ctypes.c_int()
+        it = lib().orc_bicgstab(self.h, op, shift, _p(x), _p(b), tol, maxiter, eps, ctypes.byref(st))
+        return x, it, st.value == 0
 
     def fermion_force(self, A: np.ndarray, eta: np.ndarray) -> np.ndarray:
         A = np.ascontiguousarray(A, dtype=np.float64)

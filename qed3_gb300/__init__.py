@@ -80,6 +80,8 @@ SIGNATURES = [
     ("qed3_dirac_apply_field", ctypes.c_int, [vp, ctypes.c_int, ctypes.c_int, vp, vp, ctypes.c_int, vp]),
     ("qed3_cg_solve", ctypes.c_int, [vp, vp, vp, ctypes.POINTER(SolveParams), ctypes.POINTER(SolveReport), vp]),
     ("qed3_solver_last_report", ctypes.c_int, [vp, ctypes.POINTER(SolveReport)]),
+    ("qed3_bicgstab_solve", ctypes.c_int, [vp, ctypes.c_int, vp, vp, ctypes.POINTER(SolveParams), ctypes.c_double,
+                                           ctypes.POINTER(SolveReport), vp]),
     ("qed3_cg_solve_noalloc", ctypes.c_int, [vp, vp, vp, ctypes.POINTER(SolveParams), ctypes.POINTER(SolveReport),
                                              vp]),
     ("qed3_plaquette", ctypes.c_int, [vp, vp, vp, c_double_p, vp]),
@@ -286,6 +288,16 @@ class DiracS2Dual:
         rc = lib().qed3_cg_solve(self._h, _ptr(x), _ptr(b), ctypes.byref(p), ctypes.byref(r), _stream(stream))
         if rc not in (OK, ERR_NOCONV):
             _check(rc)
+        return Report(r.status, r.iters, r.reliable_updates, r.true_rel_res, r.ms)
+
+    def bicgstab(self, x, b, op: int = OP_D, tol: float = 1e-10, maxiter: int = 100000, shift: float = 0.0,
+                 eps: float = 1e-8, stream=None) -> Report:
+        """BiCGStab with restarts (MatPoly::bicgstab) on (op + shift) x = b, FP64."""
+        p = SolveParams(tol, maxiter, PREC_F64, 0.1, shift, 0)
+        r = SolveReport()
+        rc = lib().qed3_bicgstab_solve(self._h, op, _ptr(x), _ptr(b), ctypes.byref(p), eps, ctypes.byref(r),
+                                       _stream(stream))
+        _check(rc)
         return Report(r.status, r.iters, r.reliable_updates, r.true_rel_res, r.ms)
 
     @staticmethod

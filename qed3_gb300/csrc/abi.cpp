@@ -287,6 +287,14 @@ int qed3_cg_solve_noalloc(qed3_dirac* d, double* x, const double* b, const qed3_
   QED3_GUARD_END
 }
 
+int qed3_bicgstab_solve(qed3_dirac* d, int op, double* x, const double* b, const qed3_solve_params* params,
+                        double eps, qed3_solve_report* report, void* stream) {
+  QED3_GUARD_BEGIN
+  if (!d || !x || !b) return fail(QED3_ERR_ARG, "NULL argument");
+  return bicgstab_solve(d, op, x, b, params, eps, report, (cudaStream_t)stream);
+  QED3_GUARD_END
+}
+
 int qed3_solver_last_report(qed3_dirac* d, qed3_solve_report* report) {
   if (!d || !report) return fail(QED3_ERR_ARG, "NULL argument");
   *report = d->last;

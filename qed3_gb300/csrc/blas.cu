@@ -20,6 +20,14 @@ __global__ void k_axpby(long long n, double a, const double* __restrict__ x, dou
   if (i < n) out[i] = a * x[i] + b * y[i];
 }
 
+// out = a x + y over complex elements (complex a; out may alias x or y)
+__global__ void k_zaxpy(long long nc, double2 a, const double2* x, const double2* y, double2* out) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nc) return;
+  const double2 u = x[i], v = y[i];
+  out[i] = make_double2(fma(a.x, u.x, fma(-a.y, u.y, v.x)), fma(a.x, u.y, fma(a.y, u.x, v.y)));
+}
+
 // y = x0 + sum_m c_m Z_m, Z stored as np consecutive vectors of n doubles
 __global__ void k_pole_sum(long long n, int np, PoleCoef c, const double* __restrict__ Z,
                            const double* __restrict__ x0, double* __restrict__ y) {
@@ -49,6 +57,13 @@ __global__ void k_zdot_part(long long nc, const double2* __restrict__ x, const d
 
 int vec_axpby(long long n, double a, const double* x, double b, const double* y, double* out, cudaStream_t st) {
   k_axpby<<<nblk(n), 256, 0, st>>>(n, a, x, b, y, out);
+  QED3_CUDA_TRY(cudaGetLastError());
+  return QED3_OK;
+}
+
+int vec_zaxpy(long long nc, double are, double aim, const double* x, const double* y, double* out, cudaStream_t st) {
+  k_zaxpy<<<nblk(nc), 256, 0, st>>>(nc, make_double2(are, aim), reinterpret_cast<const double2*>(x),
+                                    reinterpret_cast<const double2*>(y), reinterpret_cast<double2*>(out));
   QED3_CUDA_TRY(cudaGetLastError());
   return QED3_OK;
 }

@@ -9,6 +9,8 @@ struct PoleCoef {
   double c[kMaxPoles];
 };
 int vec_axpby(long long n, double a, const double* x, double b, const double* y, double* out, cudaStream_t st);
+// out = a x + y over nc complex elements, a = are + i aim
+int vec_zaxpy(long long nc, double are, double aim, const double* x, const double* y, double* out, cudaStream_t st);
 int vec_pole_sum(long long n, int np, const double* coef, const double* Z, const double* x0, double* y,
                  cudaStream_t st);
 // conj(x) . y over nc complex elements; part: device scratch of >= 2048 doubles

@@ -132,3 +132,44 @@ def test_solve_scale_invariance(cuda, prec, streaming):
         assert rs.status == Q.OK and rs.true_rel_res <= 1e-10, (scale, rs)
         assert abs(rs.iters - r1.iters) <= 2
         assert float((xs / scale - x1).norm() / x1.norm()) < 1e-8
+
+
+@pytest.mark.parametrize("op", [Q.OP_D, Q.OP_DDAG, Q.OP_DDAGD])
+@pytest.mark.parametrize("n", [4, 8])
+def test_bicgstab_matches_oracle(cuda, op, n):
+    """BiCGStab (MatPoly::bicgstab restated) on the non-hermitian D, on D^dag and
+    on D^dag D, with the reference's absolute eps = 1e-8 stop: same iteration
+    count and solution as the oracle, certificate recomputed from the oracle."""
+    import torch
+    g, lat, Do, Dq, b = _setup(n, 0.1, 95 + n, cuda)
+    x_ref, it_ref, ok = Do.bicgstab(b, op, tol=1e-10)
+    bt = to_dev(b, cuda)
+    xt = torch.zeros_like(bt)
+    rep = Dq.bicgstab(xt, bt, op=op, tol=1e-10)
+    assert ok and rep.status == Q.OK
+    assert abs(rep.iters - it_ref) <= 2, (rep.iters, it_ref)
+    x = from_dev(xt)
+    assert np.linalg.norm(x - x_ref) / np.linalg.norm(x_ref) < 1e-6
+    res = np.linalg.norm(b - Do.apply(x, op)) / np.linalg.norm(b)
+    assert abs(rep.true_rel_res - res) <= 1e-3 * res + 1e-14
+
+
+def test_bicgstab_to_tolerance_and_shift(cuda):
+    """eps = 0 on D^dag D + shift: the relative stop alone ends the solve; the
+    result agrees with the oracle and with CG."""
+    import torch
+    g, lat, Do, Dq, b = _setup(8, 0.1, 99, cuda)
+    bt = to_dev(b, cuda)
+    for shift in (0.0, 0.3):
+        x_ref, it_ref, ok = Do.bicgstab(b, Q.OP_DDAGD, tol=1e-11, shift=shift, eps=0.0)
+        xt = torch.zeros_like(bt)
+        rep = Dq.bicgstab(xt, bt, op=Q.OP_DDAGD, tol=1e-11, shift=shift, eps=0.0)
+        assert ok and rep.status == Q.OK and abs(rep.iters - it_ref) <= 2
+        x = from_dev(xt)
+        assert np.linalg.norm(x - x_ref) / np.linalg.norm(x_ref) < 1e-7
+        x_cg, _, _ = Do.cg(b, tol=1e-12, shift=shift)
+        assert np.linalg.norm(x - x_cg) / np.linalg.norm(x_cg) < 1e-7
+    # x0 = b is already the solution of the identity-like zero source: b = 0
+    xt = torch.ones_like(bt)
+    rep = Dq.bicgstab(xt, torch.zeros_like(bt), op=Q.OP_D)
+    assert rep.status == Q.OK and float(xt.abs().max()) == 0.0

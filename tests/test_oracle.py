@@ -229,3 +229,21 @@ def test_fermion_hmc_two_pseudofermions_second_order():
                                   no_reject=True, npf=2)
         dh.append(abs(d))
     assert 3.0 < dh[0] / dh[1] < 5.0
+
+
+def test_bicgstab_restatement_against_dense():
+    """MatPoly::bicgstab restated: with eps = 0 the relative stop decides and the
+    solution of D^dag D x = b matches a dense solve; with the reference's
+    eps = 1e-8 (absolute) the non-hermitian D stops at |t|^2 < eps."""
+    g = O.geometry(4)
+    A = np.random.default_rng(1).uniform(-np.pi, np.pi, g.n_links)
+    D = O.Dirac(g, 1.0, 0.1)
+    D.update(A)
+    M = D.dense()
+    rng = np.random.default_rng(2)
+    b = rng.normal(size=D.N) + 1j * rng.normal(size=D.N)
+    x, it, ok = D.bicgstab(b, 2, tol=1e-11, eps=0.0)
+    xs = np.linalg.solve(M.conj().T @ M, b)
+    assert ok and np.linalg.norm(x - xs) / np.linalg.norm(xs) < 1e-7
+    x, it, ok = D.bicgstab(b, 0, tol=1e-10)
+    assert ok and np.linalg.norm(b - M @ x) ** 2 < 1e-6
