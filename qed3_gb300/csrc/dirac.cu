@@ -156,7 +156,7 @@ static inline int nblk(long long n, int t = 256) { return int((n + t - 1) / t); 
 // FP32/BF16 vectors stay near unit scale whatever the scale of b (a residual
 // of a right-hand side with |b_i| ~ 1e-20 would underflow in FP32, one with
 // |b_i| ~ 1e20 would overflow); the export multiplies the solution by |b|.
-constexpr int kNormParts = 256;
+constexpr int kNormParts = 64;  // partials read by every import block: keep them few
 
 __global__ void k_norm_part(long long n, const double* __restrict__ in, double* __restrict__ part) {
   __shared__ double sh[32];

@@ -20,7 +20,7 @@ int dirac_apply_field(qed3_dirac_s* d, int op, int prec, void* out, const void* 
 int dirac_apply32_blocks(qed3_dirac_s* d, const M32* H, void* out, const void* in, int nrhs, cudaStream_t st);
 int field_import(qed3_dirac_s* d, int prec, void* field, const double* in_ref, int nrhs, cudaStream_t st);
 int field_export(qed3_dirac_s* d, int prec, double* out_ref, const void* field, int nrhs, cudaStream_t st);
-// solver import of b / |b| (|b| stored at *nrm; part: 256 doubles of scratch)
+// solver import of b / |b| (|b| stored at *nrm; part: 64 doubles of scratch)
 // and export of |b| x
 int field_import_unit(qed3_dirac_s* d, S64* field, const double* in_ref, double* part, double* nrm, cudaStream_t st);
 int field_export_scaled(qed3_dirac_s* d, double* out_ref, const S64* field, const double* nrm, cudaStream_t st);
