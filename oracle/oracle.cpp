@@ -1026,13 +1026,19 @@ struct OracleRng {
   std::vector<SingleRng> links, sites;
 };
 
+// SingleRng::reseed(const int seed) (src/both/rng.h:26) narrows each 64-bit
+// master draw to int; mt19937_64::seed then widens the int with sign extension.
+static std::uint64_t orc_engine_seed(std::uint64_t draw) {
+  return std::uint64_t(std::int64_t(std::int32_t(std::uint32_t(draw & 0xffffffffu))));
+}
+
 OracleRng* orc_rng_create(int n_links, int n_sites, int seed) {
   auto* r = new OracleRng;
   r->links.resize(n_links);
   r->sites.resize(n_sites);
-  r->master.mt.seed(seed);
-  for (auto& e : r->links) e.mt.seed(r->master.mt());
-  for (auto& e : r->sites) e.mt.seed(r->master.mt());
+  r->master.mt.seed(orc_engine_seed(std::uint64_t(std::int64_t(seed))));
+  for (auto& e : r->links) e.mt.seed(orc_engine_seed(r->master.mt()));
+  for (auto& e : r->sites) e.mt.seed(orc_engine_seed(r->master.mt()));
   return r;
 }
 void orc_rng_destroy(OracleRng* r) { delete r; }

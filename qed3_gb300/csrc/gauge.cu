@@ -15,6 +15,7 @@
 //    dH accumulated as per-term differences in FP64.
 
 #include <cmath>
+#include <cstdint>
 #include <functional>
 #include <random>
 #include <vector>
@@ -317,13 +318,20 @@ struct qed3_rng_s {
 
 namespace qed3 {
 
+// The reference seeds every engine through SingleRng::reseed(const int): the
+// master's 64-bit draw is narrowed to a signed 32-bit int and that int is
+// widened again (sign-extended) by mt19937_64::seed.
+static inline std::uint64_t engine_seed(std::uint64_t draw) {
+  return std::uint64_t(std::int64_t(std::int32_t(std::uint32_t(draw & 0xffffffffu))));
+}
+
 qed3_rng_s* rng_create(int n_links, int n_sites, int seed) {
   auto* r = new qed3_rng_s;
   r->r.links.resize(n_links);
   r->r.sites.resize(n_sites);
-  r->r.master.mt.seed(seed);
-  for (auto& e : r->r.links) e.mt.seed(r->r.master.mt());
-  for (auto& e : r->r.sites) e.mt.seed(r->r.master.mt());
+  r->r.master.mt.seed(engine_seed(std::uint64_t(std::int64_t(seed))));
+  for (auto& e : r->r.links) e.mt.seed(engine_seed(r->r.master.mt()));
+  for (auto& e : r->r.sites) e.mt.seed(engine_seed(r->r.master.mt()));
   return r;
 }
 void rng_destroy(qed3_rng_s* r) { delete r; }

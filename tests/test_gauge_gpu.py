@@ -151,3 +151,27 @@ def test_fermion_hmc_two_pseudofermions_matches_oracle(cuda):
         assert acc_o == acc_q and its > 0
         assert abs(dh_o - dh_q) < 1e-8 * max(1.0, abs(dh_o))
         assert np.abs(from_dev(At) - Ao).max() < 1e-9
+
+
+def test_product_rng_matches_reference_build(cuda):
+    """The library's host ParallelRng streams against the reference's own
+    src/both/rng.h (golden fixture made by compiling it in place)."""
+    import json
+    import os
+    data = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "rng_ref.json")))
+    h = lambda v: np.array([float.fromhex(s) for s in v])
+    for c in data["cases"]:
+        nref = {30: 1, 120: 2, 480: 4}[c["n_links"]]
+        lat = Q.S2Trivalent(nref)
+        assert lat.n_links == c["n_links"] and lat.n_sites == c["n_sites"]
+        rng = Q.ParallelRng(lat, c["seed"])
+        links2 = np.concatenate([rng.gaussian_links(1.0), rng.gaussian_links(1.0)])
+        assert np.array_equal(links2, h(c["links2"]))
+        xi = rng.gaussian_spinor()
+        s4 = h(c["sites4"])
+        assert np.array_equal(xi.real, s4[0::2] / np.sqrt(2.0))
+        assert np.array_equal(xi.imag, s4[1::2] / np.sqrt(2.0))
+        z = rng.z2_spinor()
+        z2 = np.array(c["z2"], dtype=np.float64)
+        nrm = np.sqrt(2.0 * c["n_sites"])
+        assert np.array_equal(z.real, z2[0::2] / nrm) and np.array_equal(z.imag, z2[1::2] / nrm)

@@ -247,3 +247,31 @@ def test_bicgstab_restatement_against_dense():
     assert ok and np.linalg.norm(x - xs) / np.linalg.norm(xs) < 1e-7
     x, it, ok = D.bicgstab(b, 0, tol=1e-10)
     assert ok and np.linalg.norm(b - M @ x) ** 2 < 1e-6
+
+
+class _Sizes:
+    def __init__(self, n_links, n_sites):
+        self.n_links, self.n_sites = n_links, n_sites
+
+
+def test_rng_matches_reference_build():
+    """The oracle's ParallelRng2 restatement against the reference's own
+    src/both/rng.h compiled in place (tests/golden/rng_ref.json): per-link
+    Gaussians over two sweeps (the normal distribution's cached spare), the
+    per-site Gaussians in fill_gaussian's order, master uniforms, Z2 draws."""
+    data = json.load(open(os.path.join(HERE, "golden", "rng_ref.json")))
+    h = lambda v: np.array([float.fromhex(s) for s in v])
+    for c in data["cases"]:
+        nl, ns = c["n_links"], c["n_sites"]
+        rng = O.Rng(_Sizes(nl, ns), c["seed"])
+        links2 = np.concatenate([rng.gaussian_links(1.0), rng.gaussian_links(1.0)])
+        assert np.array_equal(links2, h(c["links2"]))
+        xi = rng.gaussian_spinor()
+        s4 = h(c["sites4"])
+        assert np.array_equal(xi.real, s4[0::2] / np.sqrt(2.0))
+        assert np.array_equal(xi.imag, s4[1::2] / np.sqrt(2.0))
+        assert [rng.uniform() for _ in range(5)] == list(h(c["uniform5"]))
+        z = rng.z2_spinor()
+        z2 = np.array(c["z2"], dtype=np.float64)
+        nrm = np.sqrt(2.0 * ns)
+        assert np.array_equal(z.real, z2[0::2] / nrm) and np.array_equal(z.imag, z2[1::2] / nrm)
