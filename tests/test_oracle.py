@@ -205,30 +205,39 @@ def test_overlap_force_finite_difference():
 
 
 def test_fermion_hmc_second_order():
-    """The oracle's HMC::run + ExplicitLeapfrogML restatement: dH ~ tau^2."""
+    """The oracle's HMC::run + ExplicitLeapfrogML restatement: dH ~ tau^2,
+    measured as the RMS over four momentum / pseudofermion draws (a single
+    draw can sit near a zero crossing of dH)."""
     g = O.geometry(2)
     A = np.random.default_rng(1).normal(size=g.n_links) * 0.3
-    dh = []
+    rms = []
     for ns in (16, 32):
-        D = O.Dirac(g, 1.0, 0.1)
-        rng = O.Rng(g, 5)
-        Ac = A.copy()
-        _, d, _ = O.hmc_fermion(g, D, rng, Ac, 1.4, tmax=1.0, nsteps=ns, nsteps_inner=4, no_reject=True)
-        dh.append(abs(d))
-    assert 3.0 < dh[0] / dh[1] < 5.0
+        v = []
+        for seed in range(5, 9):
+            D = O.Dirac(g, 1.0, 0.1)
+            _, d, _ = O.hmc_fermion(g, D, O.Rng(g, seed), A.copy(), 1.4, tmax=1.0, nsteps=ns, nsteps_inner=4,
+                                    no_reject=True)
+            v.append(d)
+        rms.append(np.sqrt(np.mean(np.square(v))))
+    assert 3.0 < rms[0] / rms[1] < 5.0
 
 
 def test_fermion_hmc_two_pseudofermions_second_order():
-    """HMC2::run restated: with two pseudofermions dH still falls as tau^2."""
+    """HMC2::run restated: with two pseudofermions dH still falls as tau^2 (RMS
+    over four draws)."""
     g = O.geometry(2)
     A = np.random.default_rng(2).normal(size=g.n_links) * 0.3
-    dh = []
-    for ns in (32, 64):
-        D = O.Dirac(g, 1.0, 0.1)
-        _, d, its = O.hmc_fermion(g, D, O.Rng(g, 6), A.copy(), 1.4, tmax=1.0, nsteps=ns, nsteps_inner=4,
-                                  no_reject=True, npf=2)
-        dh.append(abs(d))
-    assert 3.0 < dh[0] / dh[1] < 5.0
+    rms = []
+    for ns in (16, 32):
+        v = []
+        for seed in range(5, 9):
+            D = O.Dirac(g, 1.0, 0.1)
+            _, d, _ = O.hmc_fermion(g, D, O.Rng(g, seed), A.copy(), 1.4, tmax=1.0, nsteps=ns, nsteps_inner=4,
+                                    no_reject=True, npf=2)
+            v.append(d)
+        rms.append(np.sqrt(np.mean(np.square(v))))
+    assert 3.0 < rms[0] / rms[1] < 5.0
+
 
 
 def test_bicgstab_restatement_against_dense():
