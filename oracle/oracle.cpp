@@ -985,9 +985,9 @@ double orc_gauge_action(const OracleGeom* g, const double* A, double beta, int c
   orc_plaquettes(g, A, th.data());
   double res = 0;
   for (size_t v = 0; v < th.size(); v++) {
-    const double w = g->mean_vol / g->vols[v];
-    if (compact) res += -w * std::cos(th[v]);
-    else res += 0.5 * w * th[v] * th[v];
+    // the reference's evaluation order (src/both/action.h:24-25)
+    if (compact) res += -g->mean_vol / g->vols[v] * std::cos(th[v]);
+    else res += 0.5 * g->mean_vol / g->vols[v] * (th[v] * th[v]);
   }
   return res * beta;
 }

@@ -10,6 +10,14 @@ compiled in place by the same `make -C oracle ref` into oracle/_ref/librng_ref.s
 per-link Gaussians (two sweeps), the per-site Gaussians in fill_gaussian's
 order, master uniforms and per-site Z2 draws, for two lattice sizes and seeds.
 
+gauge_ref.json: the REFERENCE's own gauge side compiled in place by the same
+`make -C oracle ref` into oracle/_ref/libgauge_ref.so -- U1onS2 plaquette
+angles and average plaquette (src/both/gauge.h), U1Wilson action and force
+(src/both/action.h), and HMCPureGauge trajectories driven by ParallelRng2
+(src/both/hmc.h:115-200, src/both/rng.h) -- on the oracle's lattice tables
+(faces, dual-face areas, link orientation) for n = 2 and 4, compact and
+non-compact.
+
 free_spectrum.json: the known answers of analysis/ev_dual.ipynb (cells 33-34),
 typed in from the notebook's output cells.
 """
@@ -62,6 +70,43 @@ def rng_fixture():
                        cases=out), f, indent=0)
 
 
+GAUGE_CASES = [(2, False, 1.4, 9), (2, True, 1.4, 9), (4, True, 1.4, 5), (4, False, 2.0, 6)]
+
+
+def gauge_fixture():
+    import sys
+    sys.path.insert(0, ROOT)
+    from oracle import oracle as O
+    subprocess.check_call(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "ref"])
+    L = ctypes.CDLL(os.path.join(ROOT, "oracle", "_ref", "libgauge_ref.so"))
+    dp, ip = ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int)
+    hx = lambda a: [float.hex(float(v)) for v in a]
+    out = []
+    for n, compact, beta, seed in GAUGE_CASES:
+        g = O.geometry(n)
+        A = np.random.default_rng(100 + n).normal(size=g.n_links) * 0.5
+        fo = np.ascontiguousarray(g.face_offsets, np.int32)
+        fs = np.ascontiguousarray(g.face_sites, np.int32)
+        links = np.ascontiguousarray(g.links, np.int32).ravel()
+        vols = np.ascontiguousarray(g.vols)
+        ntraj, tmax, nsteps = 3, 1.0, 20
+        th, F, Aout = np.zeros(g.n_faces), np.zeros(g.n_links), np.zeros(g.n_links)
+        dH, acc = np.zeros(ntraj), np.zeros(ntraj, np.int32)
+        avg, S = ctypes.c_double(), ctypes.c_double()
+        L.ref_gauge_run(g.n_sites, g.n_links, g.n_faces, fo.ctypes.data_as(ip), fs.ctypes.data_as(ip),
+                        vols.ctypes.data_as(dp), ctypes.c_double(g.mean_vol), links.ctypes.data_as(ip), int(compact),
+                        ctypes.c_double(beta), A.ctypes.data_as(dp), th.ctypes.data_as(dp), ctypes.byref(avg),
+                        ctypes.byref(S), F.ctypes.data_as(dp), seed, ctypes.c_double(tmax), nsteps, ntraj,
+                        Aout.ctypes.data_as(dp), dH.ctypes.data_as(dp), acc.ctypes.data_as(ip))
+        out.append(dict(n=n, compact=compact, beta=beta, A=hx(A), theta=hx(th), avg_plaquette=float.hex(avg.value),
+                        action=float.hex(S.value), force=hx(F), hmc=dict(seed=seed, tmax=tmax, nsteps=nsteps,
+                        dH=hx(dH), accepted=[int(v) for v in acc], A_final=hx(Aout))))
+    with open(os.path.join(HERE, "gauge_ref.json"), "w") as f:
+        json.dump(dict(source="reference src/both/{gauge,action,hmc,rng}.h compiled by oracle/Makefile `ref` on the "
+                              "oracle's lattice tables; the force is the reference's (theta, not sin theta)",
+                       cases=out), f, indent=0)
+
+
 def spectrum_fixture():
     data = dict(source="analysis/ev_dual.ipynb cells 33-34: [n, |Im lambda| (j=3/2), |Im lambda| (j=1/2)]",
                 rows=[[2, 1.89453, 0.995597], [4, 1.97081, 0.997657], [6, 1.98474, 0.998488],
@@ -73,4 +118,5 @@ def spectrum_fixture():
 if __name__ == "__main__":
     zolotarev_fixture()
     rng_fixture()
+    gauge_fixture()
     spectrum_fixture()

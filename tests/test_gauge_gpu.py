@@ -179,3 +179,36 @@ def test_product_rng_matches_reference_build(cuda):
         z2 = np.array(c["z2"], dtype=np.float64)
         nrm = np.sqrt(2.0 * c["n_sites"])
         assert np.array_equal(z.real, z2[0::2] / nrm) and np.array_equal(z.imag, z2[1::2] / nrm)
+
+
+def test_product_gauge_side_matches_reference_build(cuda):
+    """The library's plaquettes, action, force and pure-gauge HMC against the
+    reference's own gauge code compiled in place (golden fixture): angles and
+    forces to rounding, the same Metropolis decisions, dH and links to the
+    per-term-difference accuracy of the device reductions."""
+    import json
+    import os
+    import torch
+    data = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "gauge_ref.json")))
+    h = lambda v: np.array([float.fromhex(s) for s in v])
+    for c in data["cases"]:
+        lat = Q.S2Trivalent(c["n"])
+        A = h(c["A"])
+        At = to_dev(A, cuda)
+        th = torch.zeros(lat.n_faces, dtype=torch.float64, device=cuda)
+        avg = Q.plaquette(lat, At, th)
+        assert np.abs(from_dev(th) - h(c["theta"])).max() < 1e-14
+        assert abs(avg - float.fromhex(c["avg_plaquette"])) < 1e-14
+        S_ref = float.fromhex(c["action"])
+        assert abs(Q.gauge_action(lat, At, c["beta"], c["compact"]) - S_ref) < 1e-13 * abs(S_ref)
+        F = torch.zeros_like(At)
+        Q.gauge_force(lat, At, F, c["beta"], c["compact"], exact=False)
+        Fr = h(c["force"])
+        assert np.abs(from_dev(F) - Fr).max() < 1e-13 * np.abs(Fr).max()
+        hm = c["hmc"]
+        rng = Q.ParallelRng(lat, hm["seed"])
+        for t in range(len(hm["dH"])):
+            acc, dH = Q.hmc_pure_gauge(lat, rng, At, c["beta"], c["compact"], False, hm["tmax"], hm["nsteps"])
+            assert acc == bool(hm["accepted"][t])
+            assert abs(dH - float.fromhex(hm["dH"][t])) < 1e-10
+        assert np.abs(from_dev(At) - h(hm["A_final"])).max() < 1e-10

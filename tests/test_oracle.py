@@ -284,3 +284,28 @@ def test_rng_matches_reference_build():
         z2 = np.array(c["z2"], dtype=np.float64)
         nrm = np.sqrt(2.0 * ns)
         assert np.array_equal(z.real, z2[0::2] / nrm) and np.array_equal(z.imag, z2[1::2] / nrm)
+
+
+def test_gauge_side_matches_reference_build():
+    """The oracle's plaquette angles, Wilson action and force (the reference's
+    theta form) and pure-gauge HMC trajectories against the reference's own
+    src/both/{gauge,action,hmc,rng}.h compiled in place on the same lattice
+    tables (tests/golden/gauge_ref.json): bit for bit, dH to its rounding."""
+    data = json.load(open(os.path.join(HERE, "golden", "gauge_ref.json")))
+    h = lambda v: np.array([float.fromhex(s) for s in v])
+    for c in data["cases"]:
+        g = O.geometry(c["n"])
+        A = h(c["A"])
+        th = O.plaquettes(g, A)
+        assert np.array_equal(th, h(c["theta"]))
+        assert abs(np.cos(th).mean() - float.fromhex(c["avg_plaquette"])) < 1e-15
+        assert O.gauge_action(g, A, c["beta"], c["compact"]) == float.fromhex(c["action"])
+        assert np.array_equal(O.gauge_force(g, A, c["beta"], c["compact"], False), h(c["force"]))
+        hm = c["hmc"]
+        rng = O.Rng(g, hm["seed"])
+        Ao = np.ascontiguousarray(A.copy())
+        for t in range(len(hm["dH"])):
+            acc, dH = O.hmc_pure_gauge(g, rng, Ao, c["beta"], c["compact"], False, hm["tmax"], hm["nsteps"])
+            # dH = H1 - H0 of totals ~1e2: the last bits depend on the summation order
+            assert acc == bool(hm["accepted"][t]) and abs(dH - float.fromhex(hm["dH"][t])) < 1e-12
+        assert np.array_equal(Ao, h(hm["A_final"]))
