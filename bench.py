@@ -20,6 +20,10 @@ public C-ABI call with b and x in pinned host memory (H2D of b and D2H of x
 inside every timed step).  L2 (129 MB) is flushed between timed steps since
 the n=64 working set fits in it.
 
+`batched_256` (outside the headline): the multi-lattice batched configuration,
+256 right-hand sides (64 on each of n = 16, 32, 48, 64) solved to 1e-10 in one
+persistent launch per batch, beside the same 256 solves run one after another.
+
 --impl reference times the reference's algorithm on the host cores: the
 oracle's restatement of MatPoly::solve (src/dual/matpoly.h:204-267) over the
 reference CSR operator, OpenMP over rows on every host core.
@@ -214,6 +218,47 @@ def cpu_reference_solve(b, A, threads=None):
     return dt, it, float(np.linalg.norm(r) / np.linalg.norm(b)), O.num_threads()
 
 
+def batched_throughput(torch, Q, dev, reps=3):
+    """The multi-lattice batched configuration: 256 right-hand sides, 64 on each
+    of n = 16, 32, 48, 64 (each with its own beta = 1.4 configuration and a mass
+    from U[0.02, 0.2]), solved to 1e-10 in ONE persistent launch per batch, vs
+    the same 256 solves one after another with the single-system solver."""
+    rng = np.random.default_rng(256)
+    systems, bs = [], []
+    for n in (16, 32, 48, 64):
+        lat_n = Q.S2Trivalent(n)
+        A_n, _ = Q.thermalized_links(lat_n, BETA, seed=300 + n, ntraj=10, init="uniform", device=dev)
+        D_n = Q.DiracS2Dual(lat_n, 1.0, float(rng.uniform(0.02, 0.2)))
+        D_n.update(A_n)
+        b_n = rng.normal(size=(64, 2 * lat_n.n_sites)) + 1j * rng.normal(size=(64, 2 * lat_n.n_sites))
+        systems.append((D_n, 64))
+        bs.append(torch.from_numpy(b_n).to(dev))
+    batch = Q.Batch(systems, precision=Q.PREC_F32)
+    xs = [torch.zeros_like(b_) for b_ in bs]
+    ms_b, ok, iters = [], True, 0
+    for i in range(reps + 1):
+        reps_, ms = batch.solve(xs, bs, tol=TOL, precision=Q.PREC_F32)
+        ok = ok and all(r.status == Q.OK and r.true_rel_res <= TOL for r in reps_)
+        iters = max(iters, max(r.iters for r in reps_))
+        if i > 0:
+            ms_b.append(ms)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    seq_ok = True
+    for (D_n, _), b_ in zip(systems, bs):
+        x_ = torch.zeros_like(b_[0])
+        for r in range(64):
+            rep = D_n.solve(x_, b_[r].contiguous(), tol=TOL, precision=Q.PREC_F32)
+            seq_ok = seq_ok and rep.status == Q.OK
+    torch.cuda.synchronize()
+    seq_s = time.perf_counter() - t0
+    ms = float(np.mean(ms_b))
+    return {"rhs": 256, "lattices": [16, 32, 48, 64], "rhs_tile": batch.rhs_tile, "threads": batch.threads,
+            "blocks": batch.blocks, "ms_per_batch": ms, "solves_per_s": 256e3 / ms, "max_iters": iters,
+            "certified": bool(ok), "sequential_single_solves_per_s": 256 / seq_s, "sequential_certified": seq_ok,
+            "speedup_vs_sequential": (256e3 / ms) / (256 / seq_s)}
+
+
 def profile_case(torch, which):
     """Small cases for ncu captures (a few hundred MB on the device)."""
     import qed3_gb300 as Q
@@ -356,6 +401,7 @@ def main():
     clocks_info = clocks.stop()
 
     heldout = heldout_iterations(torch, Q, lat, pc, dev)
+    batched = batched_throughput(torch, Q, dev)
 
     # ---- roofline of the dominant kernel ----------------------------------------------
     # algorithmic bytes per site per iteration (fp32 / bf16 halo storage):
@@ -400,6 +446,7 @@ def main():
                          f"{per_site_iter} B/site/iteration x {iters} iterations; the HBM-bound Dirac apply is "
                          "in apply_sweep"},
             "apply_sweep": sweep,
+            "batched_256": batched,
             "e2e": {"value": e2e, "unit": "solves/s", "h2d_bytes_per_step": b.nbytes, "d2h_bytes_per_step": b.nbytes},
             "gpu_launches": args.steps * 4,  # |b| partials, unit-norm import, solver, scaled export
             "clocks": clocks_info}
