@@ -75,6 +75,20 @@ int qed3_lattice_tables(const qed3_lattice* lat, double* sites, int* nns, int* l
                         double* omega, double* alpha, double* means);
 /* Internal (device) order: perm[i] = reference index of internal site i. */
 int qed3_lattice_permutation(const qed3_lattice* lat, int* perm);
+/* The lattice of a caller's own simplicial mesh, so that sites and links carry
+ * the caller's numbering -- e.g. the reference's S2Simp tables
+ * (src/both_3d/s2n_simp.h:43-269: vertices, triangles) and S2Trivalent link
+ * list (src/both_3d/s2n_dual.h:49-106), whose link angles a saved gauge
+ * configuration is indexed by.  vertices[n_vertices*3] (normalised here),
+ * triangles[n_triangles*3] (vertex ids, any winding); dual site t is the
+ * circumcentre of triangle t.  links: NULL (lexicographic (i<j) order) or
+ * [n_links*2] pairs (i<j) giving the link numbering.  The mesh must be a
+ * closed triangulation of the sphere (every edge in two triangles, one ring
+ * of triangles per vertex, V - E + F = 2); QED3_ERR_ARG otherwise. */
+int qed3_lattice_from_mesh(int n_vertices, const double* vertices, int n_triangles, const int* triangles,
+                           const int* links, qed3_lattice** out);
+/* The simplicial mesh of a lattice: vertices[n_faces*3], triangles[n_sites*3]. */
+int qed3_lattice_mesh(const qed3_lattice* lat, double* vertices, int* triangles);
 
 /* ======================================================================
  * Wilson-Dirac operator  --  replaces DiracS2Dual / DiracExt<.., DiracS2Dual>

@@ -68,6 +68,8 @@ SIGNATURES = [
     ("qed3_lattice_destroy", ctypes.c_int, [vp]),
     ("qed3_lattice_sizes", ctypes.c_int, [vp, c_int_p, c_int_p, c_int_p, c_int_p]),
     ("qed3_lattice_tables", ctypes.c_int, [vp] + [vp] * 12),
+    ("qed3_lattice_from_mesh", ctypes.c_int, [ctypes.c_int, vp, ctypes.c_int, vp, vp, ctypes.POINTER(vp)]),
+    ("qed3_lattice_mesh", ctypes.c_int, [vp, vp, vp]),
     ("qed3_lattice_permutation", ctypes.c_int, [vp, vp]),
     ("qed3_dirac_create", ctypes.c_int, [vp, ctypes.c_double, ctypes.c_double, ctypes.POINTER(vp)]),
     ("qed3_dirac_destroy", ctypes.c_int, [vp]),
@@ -180,15 +182,38 @@ def _stream(stream):
 class S2Trivalent:
     """Dual trivalent lattice of refinement n (S2Trivalent, src/both_3d/s2n_dual.h:49)."""
 
-    def __init__(self, n_refine: int):
+    def __init__(self, n_refine: int, _handle=None):
         self.n_refine = n_refine
-        h = vp()
-        _check(lib().qed3_lattice_create(n_refine, ctypes.byref(h)))
+        if _handle is None:
+            h = vp()
+            _check(lib().qed3_lattice_create(n_refine, ctypes.byref(h)))
+        else:
+            h = _handle
         self._h = h
         ns, nl, nf, ft = (ctypes.c_int() for _ in range(4))
         _check(lib().qed3_lattice_sizes(h, *(ctypes.byref(v) for v in (ns, nl, nf, ft))))
         self.n_sites, self.n_links, self.n_faces, self.face_total = ns.value, nl.value, nf.value, ft.value
         self._tables = None
+
+    @classmethod
+    def from_mesh(cls, vertices, triangles, links=None) -> "S2Trivalent":
+        """The dual lattice of a caller's closed triangulation of the sphere, in the
+        caller's numbering (dual site t = triangle t; links in the given (i<j) order,
+        else lexicographic)."""
+        v = np.ascontiguousarray(vertices, dtype=np.float64).reshape(-1, 3)
+        t = np.ascontiguousarray(triangles, dtype=np.int32).reshape(-1, 3)
+        lk = None if links is None else np.ascontiguousarray(links, dtype=np.int32).reshape(-1, 2)
+        h = vp()
+        _check(lib().qed3_lattice_from_mesh(v.shape[0], _ptr(v), t.shape[0], _ptr(t),
+                                            None if lk is None else _ptr(lk), ctypes.byref(h)))
+        return cls(0, _handle=h)
+
+    def mesh(self):
+        """(vertices [n_faces, 3], triangles [n_sites, 3]) of the simplicial mesh."""
+        v = np.zeros((self.n_faces, 3))
+        t = np.zeros((self.n_sites, 3), np.int32)
+        _check(lib().qed3_lattice_mesh(self._h, _ptr(v), _ptr(t)))
+        return v, t
 
     @property
     def handle(self):

@@ -131,6 +131,30 @@ int qed3_lattice_create(int n_refine, qed3_lattice** out) {
   QED3_GUARD_END
 }
 
+int qed3_lattice_from_mesh(int n_vertices, const double* vertices, int n_triangles, const int* triangles,
+                           const int* links, qed3_lattice** out) {
+  QED3_GUARD_BEGIN
+  if (!out || !vertices || !triangles) return fail(QED3_ERR_ARG, "NULL argument");
+  *out = nullptr;
+  auto* lat = new qed3_lattice_s;
+  int rc = build_lattice_from_mesh(n_vertices, vertices, n_triangles, triangles, links, true, lat->host);
+  if (rc) {
+    delete lat;
+    return rc;
+  }
+  *out = lat;
+  return QED3_OK;
+  QED3_GUARD_END
+}
+
+int qed3_lattice_mesh(const qed3_lattice* lat, double* vertices, int* triangles) {
+  if (!lat) return fail(QED3_ERR_ARG, "lattice is NULL");
+  const HostLattice& L = lat->host;
+  if (vertices) std::memcpy(vertices, L.simp_sites.data(), L.simp_sites.size() * sizeof(double));
+  if (triangles) std::memcpy(triangles, L.simp_faces.data(), L.simp_faces.size() * sizeof(int32_t));
+  return QED3_OK;
+}
+
 int qed3_lattice_destroy(qed3_lattice* lat) {
   if (!lat) return QED3_OK;
   gauge_free(lat);

@@ -128,16 +128,13 @@ inline uint64_t spread3(uint64_t v) {  // 21 bits -> every third bit
 
 }  // namespace
 
-int build_lattice(int n, bool sfc_order, HostLattice& L) {
-  if (n < 1 || n > 2048) return fail(QED3_ERR_ARG, "n_refine must be in [1, 2048]");
-  L = HostLattice{};
-  L.n = n;
+// Simplicial vertices and triangles of the n-fold refined icosahedron.
+static int refine_icosahedron(int n, std::vector<V3>& vert, std::vector<int32_t>& tri) {
   const Icosa ic = icosahedron();
-  const int64_t Nv = 10LL * n * n + 2, Ns = 20LL * n * n, Nl = 30LL * n * n;
-  if (Ns > (1LL << 30)) return fail(QED3_ERR_ARG, "lattice too large for int32 tables");
+  const int64_t Nv = 10LL * n * n + 2, Ns = 20LL * n * n;
 
   // ---- simplicial vertices --------------------------------------------------
-  std::vector<V3> vert;
+  vert.clear();
   vert.reserve(size_t(Nv));
   for (int i = 0; i < 12; i++) vert.push_back(ic.v[i]);
   std::vector<std::array<int, 2>> edges;
@@ -154,7 +151,7 @@ int build_lattice(int n, bool sfc_order, HostLattice& L) {
     edge_base[e[0]][e[1]] = int(vert.size());
     for (int t = 1; t < n; t++) vert.push_back(unit(double(n - t) * ic.v[e[0]] + double(t) * ic.v[e[1]]));
   }
-  std::vector<int32_t> tri;
+  tri.clear();
   tri.reserve(size_t(Ns) * 3);
   for (int f = 0; f < 20; f++) {
     const int A = ic.f[f][0], B = ic.f[f][1], C = ic.f[f][2];
@@ -188,7 +185,22 @@ int build_lattice(int n, bool sfc_order, HostLattice& L) {
       }
   }
   if (int64_t(vert.size()) != Nv || int64_t(tri.size()) != 3 * Ns) return fail(QED3_ERR_STATE, "refinement count mismatch");
+  return QED3_OK;
+}
 
+// The dual trivalent lattice of a closed triangulation of the sphere:
+// dual site t = triangle t, dual links = shared edges, dual faces = vertex
+// rings; lengths, areas, spin connection and the device order.  Checks that
+// the mesh is a closed 2-manifold of genus 0.
+static int build_dual(const std::vector<V3>& vert, const std::vector<int32_t>& tri, bool sfc_order, HostLattice& L) {
+  const int64_t Nv = int64_t(vert.size()), Ns = int64_t(tri.size()) / 3, Nl = 3 * Ns / 2;
+  if (Ns < 4 || 3 * Ns != int64_t(tri.size()) || Ns % 2) return fail(QED3_ERR_ARG, "mesh: bad triangle count");
+  if (Nv - Nl + Ns != 2) return fail(QED3_ERR_ARG, "mesh: not a closed triangulation of the sphere (V - E + F != 2)");
+  for (int64_t t = 0; t < Ns; t++) {
+    const int32_t a = tri[3 * t], b = tri[3 * t + 1], c = tri[3 * t + 2];
+    if (a < 0 || b < 0 || c < 0 || a >= Nv || b >= Nv || c >= Nv || a == b || b == c || a == c)
+      return fail(QED3_ERR_ARG, "mesh: bad vertex index in triangle " + std::to_string(t));
+  }
   L.n_sites = int(Ns);
   L.n_links = int(Nl);
   L.n_faces = int(Nv);
@@ -232,14 +244,17 @@ int build_lattice(int n, bool sfc_order, HostLattice& L) {
     int cnt = 0;
     for (int e = 0; e < 3; e++) {
       const int32_t u = tri[3 * t + e], v = tri[3 * t + (e + 1) % 3];
-      int32_t other = -1;
+      int32_t other = -1, found = 0;
       for (int32_t a = inc_off[u]; a < inc_off[u + 1]; a++) {
         const int32_t s = inc[a];
         if (s == t) continue;
         for (int32_t b = inc_off[v]; b < inc_off[v + 1]; b++)
-          if (inc[b] == s) other = s;
+          if (inc[b] == s) {
+            other = s;
+            found++;
+          }
       }
-      if (other < 0) return fail(QED3_ERR_STATE, "open edge in refinement");
+      if (found != 1) return fail(QED3_ERR_ARG, "mesh: an edge is not shared by exactly two triangles");
       nb[cnt++] = other;
       if (t < other) lk.push_back({int32_t(t), other, std::min(u, v), std::max(u, v)});
     }
@@ -247,7 +262,10 @@ int build_lattice(int n, bool sfc_order, HostLattice& L) {
     for (int k = 0; k < 3; k++) L.nns[3 * t + k] = nb[k];
   }
   std::sort(lk.begin(), lk.end());
-  if (int64_t(lk.size()) != Nl) return fail(QED3_ERR_STATE, "link count mismatch");
+  if (int64_t(lk.size()) != Nl) return fail(QED3_ERR_ARG, "mesh: link count mismatch");
+  for (int64_t x = 0; x < Ns; x++)
+    if (L.nns[3 * x] == L.nns[3 * x + 1] || L.nns[3 * x + 1] == L.nns[3 * x + 2])
+      return fail(QED3_ERR_ARG, "mesh: two triangles share more than one edge");
   L.links.resize(size_t(Nl) * 2);
   L.simp_links.resize(size_t(Nl) * 2);
   for (int64_t l = 0; l < Nl; l++) {
@@ -303,9 +321,16 @@ int build_lattice(int n, bool sfc_order, HostLattice& L) {
       const int32_t first = neg ? e[1] : e[0], next = neg ? e[0] : e[1];
       L.face_sites.push_back(first);
       if (fl.empty()) break;
+      bool more = false;
       for (size_t jl = 0; jl < fl.size(); jl++)
-        if (fl[jl][0] == next || fl[jl][1] == next) il = jl;
+        if (fl[jl][0] == next || fl[jl][1] == next) {
+          il = jl;
+          more = true;
+        }
+      if (!more) return fail(QED3_ERR_ARG, "mesh: the triangles around a vertex do not form one ring");
     }
+    if (int32_t(L.face_sites.size()) - L.face_offsets[v] != m)
+      return fail(QED3_ERR_ARG, "mesh: the triangles around a vertex do not form one ring");
     L.face_offsets[v + 1] = int32_t(L.face_sites.size());
   }
   L.face_links.resize(L.face_sites.size());
@@ -408,6 +433,79 @@ int build_lattice(int n, bool sfc_order, HostLattice& L) {
   }
   for (int64_t i = 0; i < Ns; i++) L.iperm[L.perm[i]] = int32_t(i);
   return QED3_OK;
+}
+
+// Renumbers the links to a caller's order (each (i < j), a permutation of the
+// lattice's links): every link-indexed table follows.
+static int reorder_links(const int32_t* order, HostLattice& L) {
+  const int64_t Nl = L.n_links;
+  std::map<std::pair<int32_t, int32_t>, int32_t> pos;
+  for (int64_t l = 0; l < Nl; l++) pos[{L.links[2 * l], L.links[2 * l + 1]}] = int32_t(l);
+  std::vector<int32_t> old_of(size_t(Nl), -1), new_of(size_t(Nl), -1);
+  for (int64_t u = 0; u < Nl; u++) {
+    const int32_t i = order[2 * u], j = order[2 * u + 1];
+    if (!(i < j)) return fail(QED3_ERR_ARG, "links: each link must be given as (i, j) with i < j");
+    const auto it = pos.find({i, j});
+    if (it == pos.end()) return fail(QED3_ERR_ARG, "links: (" + std::to_string(i) + ", " + std::to_string(j) +
+                                                       ") is not a link of the mesh");
+    if (new_of[it->second] >= 0) return fail(QED3_ERR_ARG, "links: a link is listed twice");
+    old_of[u] = it->second;
+    new_of[it->second] = int32_t(u);
+  }
+  auto permute2 = [&](std::vector<int32_t>& v) {
+    std::vector<int32_t> w(v.size());
+    for (int64_t u = 0; u < Nl; u++) {
+      w[2 * u] = v[2 * size_t(old_of[u])];
+      w[2 * u + 1] = v[2 * size_t(old_of[u]) + 1];
+    }
+    v.swap(w);
+  };
+  auto permute1 = [&](std::vector<double>& v) {
+    std::vector<double> w(v.size());
+    for (int64_t u = 0; u < Nl; u++) w[u] = v[old_of[u]];
+    v.swap(w);
+  };
+  permute2(L.links);
+  permute2(L.simp_links);
+  permute1(L.ell);
+  permute1(L.link_volume);
+  permute1(L.omega);
+  for (auto& h : L.hop_link) h = new_of[h];
+  for (auto& h : L.face_links) h = new_of[h];
+  return QED3_OK;
+}
+
+int build_lattice(int n, bool sfc_order, HostLattice& L) {
+  if (n < 1 || n > 2048) return fail(QED3_ERR_ARG, "n_refine must be in [1, 2048]");
+  if (20LL * n * n > (1LL << 30)) return fail(QED3_ERR_ARG, "lattice too large for int32 tables");
+  L = HostLattice{};
+  std::vector<V3> vert;
+  std::vector<int32_t> tri;
+  int rc = refine_icosahedron(n, vert, tri);
+  if (!rc) rc = build_dual(vert, tri, sfc_order, L);
+  L.n = n;
+  return rc;
+}
+
+int build_lattice_from_mesh(int n_vertices, const double* vertices, int n_triangles, const int32_t* triangles,
+                            const int32_t* links, bool sfc_order, HostLattice& L) {
+  if (n_vertices < 4 || n_triangles < 4 || int64_t(n_triangles) > (1LL << 30))
+    return fail(QED3_ERR_ARG, "mesh: bad vertex or triangle count");
+  L = HostLattice{};
+  std::vector<V3> vert(static_cast<size_t>(n_vertices));
+  for (int v = 0; v < n_vertices; v++) {
+    const V3 p{vertices[3 * v], vertices[3 * v + 1], vertices[3 * v + 2]};
+    const double r = norm(p);
+    if (!(r > 0.0) || !std::isfinite(r)) return fail(QED3_ERR_ARG, "mesh: vertex " + std::to_string(v) + " is zero");
+    // unit vectors (to rounding) are taken as given, so a mesh exported by
+    // qed3_lattice_mesh rebuilds the identical lattice
+    vert[v] = std::abs(r - 1.0) <= 4e-16 ? p : (1.0 / r) * p;
+  }
+  std::vector<int32_t> tri(triangles, triangles + 3 * size_t(n_triangles));
+  int rc = build_dual(vert, tri, sfc_order, L);
+  if (!rc && links) rc = reorder_links(links, L);
+  L.n = 0;
+  return rc;
 }
 
 }  // namespace qed3

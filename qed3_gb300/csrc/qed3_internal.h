@@ -49,6 +49,10 @@ struct HostLattice {
 };
 
 int build_lattice(int n, bool sfc_order, HostLattice& L);
+// the dual lattice of a caller's closed triangulation of the sphere; links:
+// optional [Nl][2] link order (NULL = lexicographic)
+int build_lattice_from_mesh(int n_vertices, const double* vertices, int n_triangles, const int32_t* triangles,
+                            const int32_t* links, bool sfc_order, HostLattice& L);
 
 // Zolotarev optimal rational approximation of sign(x) on [k, 1].
 struct ZoloCoeffs {

@@ -123,3 +123,44 @@ def test_apply_before_links_is_a_state_error(cuda):
     with pytest.raises(Q.Qed3Error) as e:
         Dq.apply(v.clone(), v, Q.OP_D)
     assert e.value.status == Q.ERR_STATE
+
+
+def test_operator_on_a_callers_mesh(cuda):
+    """The same sphere in a caller's numbering (vertices and triangles
+    relabelled, windings reversed, links in a shuffled order): the plaquettes of
+    the correspondingly mapped link field agree face by face and D^dag D has the
+    same spectrum (the spin structures differ at most by a sign per site)."""
+    import torch
+    from tests.test_lattice import _relabelled_mesh
+    lat, v2, t2, pv, pt = _relabelled_mesh(2, 3)
+    links_default = Q.S2Trivalent.from_mesh(v2, t2).tables()["links"]
+    lat2 = Q.S2Trivalent.from_mesh(v2, t2, links=links_default[np.random.default_rng(4).permutation(lat.n_links)])
+    a, b = lat.tables(), lat2.tables()
+    A = np.random.default_rng(5).uniform(-np.pi, np.pi, lat.n_links)
+    old = {tuple(l): i for i, l in enumerate(a["links"])}
+    A2 = np.empty_like(A)
+    for i, (x, y) in enumerate(b["links"]):
+        ox, oy = pt[x], pt[y]
+        A2[i] = (1.0 if ox < oy else -1.0) * A[old[(min(ox, oy), max(ox, oy))]]
+    th = torch.zeros(lat.n_faces, dtype=torch.float64, device=cuda)
+    th2 = torch.zeros_like(th)
+    Q.plaquette(lat, to_dev(A, cuda), th)
+    Q.plaquette(lat2, to_dev(A2, cuda), th2)
+    assert np.abs(from_dev(th2) - from_dev(th)[pv]).max() < 1e-13
+
+    def dense(L, Ah):
+        D = Q.DiracS2Dual(L, 1.0, 0.1)
+        D.update(Ah)
+        N = 2 * L.n_sites
+        M = np.zeros((N, N), np.complex128)
+        e = torch.zeros(N, dtype=torch.complex128, device=cuda)
+        out = torch.zeros_like(e)
+        for j in range(N):
+            e.zero_()
+            e[j] = 1.0
+            D.apply(out, e, Q.OP_DDAGD)
+            M[:, j] = from_dev(out)
+        return M
+    w1 = np.linalg.eigvalsh(dense(lat, A))
+    w2 = np.linalg.eigvalsh(dense(lat2, A2))
+    assert np.abs(w1 - w2).max() < 1e-12 * w1.max()

@@ -78,3 +78,85 @@ def test_zolotarev_against_reference_fixture():
         err_q = np.abs(r(z, x) - 1).max()
         err_ref = np.abs(r(ref, x) - 1).max()
         assert err_q <= max(1.01 * err_ref, 2 * abs(delta), 1e-13), (c["k"], c["n"], err_q, err_ref, delta)
+
+
+def _relabelled_mesh(n, seed):
+    """The n-refined mesh with its vertices and triangles renumbered at random and
+    every other triangle's winding reversed: how another generator (the
+    reference's QFE-based tables) may number the same sphere."""
+    lat = Q.S2Trivalent(n)
+    v, t = lat.mesh()
+    rng = np.random.default_rng(seed)
+    pv = rng.permutation(v.shape[0])          # new vertex k = old vertex pv[k]
+    inv_v = np.argsort(pv)
+    pt = rng.permutation(t.shape[0])          # new triangle (dual site) s = old triangle pt[s]
+    t2 = inv_v[t[pt]]
+    t2[::2] = t2[::2, ::-1]
+    return lat, v[pv], t2, pv, pt
+
+
+def test_mesh_round_trip_is_identical():
+    lat = Q.S2Trivalent(6)
+    v, t = lat.mesh()
+    lat2 = Q.S2Trivalent.from_mesh(v, t)
+    a, b = lat.tables(), lat2.tables()
+    for k in a:
+        assert np.array_equal(a[k], b[k]), k
+    assert np.array_equal(lat.permutation(), lat2.permutation())
+
+
+def test_mesh_in_a_callers_numbering():
+    """Sites, links and faces follow the caller's numbering; lengths and areas
+    are those of the same geometric objects; omega(x, y) and alpha keep the
+    reference's conventions for the new labels (equal up to orientation and 2 pi)."""
+    lat, v2, t2, pv, pt = _relabelled_mesh(4, 1)
+    lat2 = Q.S2Trivalent.from_mesh(v2, t2)
+    a, b = lat.tables(), lat2.tables()
+    assert np.abs(b["sites"] - a["sites"][pt]).max() < 1e-15
+    inv_t = np.argsort(pt)
+    old_links = {tuple(l): i for i, l in enumerate(a["links"])}
+    for i, (x, y) in enumerate(b["links"]):
+        ox, oy = pt[x], pt[y]
+        j = old_links[(min(ox, oy), max(ox, oy))]
+        sgn = 1.0 if ox < oy else -1.0
+        assert abs(b["ell"][i] - a["ell"][j]) < 1e-14
+        assert abs(b["link_volume"][i] - a["link_volume"][j]) < 1e-15
+        assert abs(wrap(b["omega"][i] - sgn * a["omega"][j])) < 1e-13
+    assert np.abs(b["vols"] - a["vols"][pv]).max() < 1e-15
+    for s in range(lat2.n_sites):
+        for k in range(3):
+            o = pt[s]
+            ko = list(a["nns"][o]).index(pt[b["nns"][s][k]])
+            assert abs(wrap(b["alpha"][s][k] - a["alpha"][o][ko])) < 1e-13
+    assert abs(b["means"][2] - a["means"][2]) < 1e-15
+
+
+def test_mesh_with_a_link_order():
+    lat = Q.S2Trivalent(3)
+    v, t = lat.mesh()
+    a = lat.tables()
+    order = np.random.default_rng(2).permutation(lat.n_links)
+    lat2 = Q.S2Trivalent.from_mesh(v, t, links=a["links"][order])
+    b = lat2.tables()
+    assert np.array_equal(b["links"], a["links"][order])
+    for k in ("simp_links", "ell", "link_volume", "omega"):
+        assert np.array_equal(b[k], a[k][order]), k
+    for k in ("sites", "nns", "face_offsets", "face_sites", "vols", "alpha"):
+        assert np.array_equal(b[k], a[k]), k
+
+
+def test_bad_meshes_are_errors():
+    lat = Q.S2Trivalent(2)
+    v, t = lat.mesh()
+    bad = [t[:-2],                                   # open surface (and V - E + F != 2)
+           np.concatenate([t[:-1], t[:1]]),          # a triangle twice, one missing
+           np.where(np.arange(t.size).reshape(t.shape) == 4, t[0, 0], t)]   # repeated vertex
+    for tb in bad:
+        with pytest.raises(Q.Qed3Error) as e:
+            Q.S2Trivalent.from_mesh(v, tb)
+        assert e.value.status == Q.ERR_ARG
+    links = lat.tables()["links"].copy()
+    for lb in (links[:, ::-1], np.concatenate([links[:-1], links[:1]])):
+        with pytest.raises(Q.Qed3Error) as e:
+            Q.S2Trivalent.from_mesh(v, t, links=lb)
+        assert e.value.status == Q.ERR_ARG
