@@ -89,6 +89,13 @@ int qed3_lattice_from_mesh(int n_vertices, const double* vertices, int n_triangl
                            const int* links, qed3_lattice** out);
 /* The simplicial mesh of a lattice: vertices[n_faces*3], triangles[n_sites*3]. */
 int qed3_lattice_mesh(const qed3_lattice* lat, double* vertices, int* triangles);
+/* Replaces the lattice's spin connection by a caller's tables, e.g. the
+ * reference's SpinStructureDual files (src/both_3d/dirac_dual.h:15-60, written
+ * by integrator/test_sorting.cc:430-594): omega[n_links] = omega(links[l][0],
+ * links[l][1]), alpha[n_sites*3] = alpha(x, nns[x][k]) in this lattice's
+ * numbering.  Either pointer may be NULL (that table is kept).  Operators
+ * created afterwards (qed3_dirac_create) use them. */
+int qed3_lattice_set_spin_structure(qed3_lattice* lat, const double* omega, const double* alpha);
 
 /* ======================================================================
  * Wilson-Dirac operator  --  replaces DiracS2Dual / DiracExt<.., DiracS2Dual>

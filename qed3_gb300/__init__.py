@@ -70,6 +70,7 @@ SIGNATURES = [
     ("qed3_lattice_tables", ctypes.c_int, [vp] + [vp] * 12),
     ("qed3_lattice_from_mesh", ctypes.c_int, [ctypes.c_int, vp, ctypes.c_int, vp, vp, ctypes.POINTER(vp)]),
     ("qed3_lattice_mesh", ctypes.c_int, [vp, vp, vp]),
+    ("qed3_lattice_set_spin_structure", ctypes.c_int, [vp, vp, vp]),
     ("qed3_lattice_permutation", ctypes.c_int, [vp, vp]),
     ("qed3_dirac_create", ctypes.c_int, [vp, ctypes.c_double, ctypes.c_double, ctypes.POINTER(vp)]),
     ("qed3_dirac_destroy", ctypes.c_int, [vp]),
@@ -214,6 +215,15 @@ class S2Trivalent:
         t = np.zeros((self.n_sites, 3), np.int32)
         _check(lib().qed3_lattice_mesh(self._h, _ptr(v), _ptr(t)))
         return v, t
+
+    def set_spin_structure(self, omega=None, alpha=None):
+        """Use a caller's spin connection (omega per link, alpha per hop) for the
+        operators created afterwards."""
+        om = None if omega is None else np.ascontiguousarray(omega, dtype=np.float64).reshape(self.n_links)
+        al = None if alpha is None else np.ascontiguousarray(alpha, dtype=np.float64).reshape(self.n_sites * 3)
+        _check(lib().qed3_lattice_set_spin_structure(self._h, None if om is None else _ptr(om),
+                                                     None if al is None else _ptr(al)))
+        self._tables = None
 
     @property
     def handle(self):

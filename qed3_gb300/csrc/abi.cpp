@@ -4,6 +4,7 @@
 
 #include <cuda_runtime.h>
 
+#include <cmath>
 #include <cstring>
 #include <exception>
 #include <new>
@@ -152,6 +153,21 @@ int qed3_lattice_mesh(const qed3_lattice* lat, double* vertices, int* triangles)
   const HostLattice& L = lat->host;
   if (vertices) std::memcpy(vertices, L.simp_sites.data(), L.simp_sites.size() * sizeof(double));
   if (triangles) std::memcpy(triangles, L.simp_faces.data(), L.simp_faces.size() * sizeof(int32_t));
+  return QED3_OK;
+}
+
+int qed3_lattice_set_spin_structure(qed3_lattice* lat, const double* omega, const double* alpha) {
+  if (!lat) return fail(QED3_ERR_ARG, "lattice is NULL");
+  HostLattice& L = lat->host;
+  for (int pass = 0; pass < 2; pass++) {  // check everything before changing anything
+    const double* src = pass == 0 ? omega : alpha;
+    const size_t n = pass == 0 ? L.omega.size() : L.alpha.size();
+    if (!src) continue;
+    for (size_t i = 0; i < n; i++)
+      if (!std::isfinite(src[i])) return fail(QED3_ERR_ARG, "spin structure: non-finite entry");
+  }
+  if (omega) std::memcpy(L.omega.data(), omega, L.omega.size() * sizeof(double));
+  if (alpha) std::memcpy(L.alpha.data(), alpha, L.alpha.size() * sizeof(double));
   return QED3_OK;
 }
 

@@ -164,3 +164,27 @@ def test_operator_on_a_callers_mesh(cuda):
     w1 = np.linalg.eigvalsh(dense(lat, A))
     w2 = np.linalg.eigvalsh(dense(lat2, A2))
     assert np.abs(w1 - w2).max() < 1e-12 * w1.max()
+
+
+def test_caller_spin_structure_enters_the_operator(cuda):
+    """omega(l) + 2 pi flips the sign of both hop blocks of link l (the half-angle
+    Omega), which is the same operator as A_l + pi: the caller's table is used."""
+    import torch
+    n, l = 4, 17
+    A = np.random.default_rng(6).uniform(-np.pi, np.pi, 30 * n * n)
+    lat1 = Q.S2Trivalent(n)
+    om = lat1.tables()["omega"].copy()
+    om[l] += 2 * np.pi
+    lat1.set_spin_structure(om)
+    D1 = Q.DiracS2Dual(lat1, 1.0, 0.1)
+    D1.update(A)
+    lat2 = Q.S2Trivalent(n)
+    D2 = Q.DiracS2Dual(lat2, 1.0, 0.1)
+    A2 = A.copy()
+    A2[l] += np.pi
+    D2.update(A2)
+    v = to_dev(np.random.default_rng(7).normal(size=2 * lat1.n_sites) * (1 + 1j), cuda)
+    o1, o2 = torch.zeros_like(v), torch.zeros_like(v)
+    D1.apply(o1, v, Q.OP_D)
+    D2.apply(o2, v, Q.OP_D)
+    assert float((o1 - o2).abs().max()) < 1e-13 * float(o2.abs().max())

@@ -160,3 +160,19 @@ def test_bad_meshes_are_errors():
         with pytest.raises(Q.Qed3Error) as e:
             Q.S2Trivalent.from_mesh(v, t, links=lb)
         assert e.value.status == Q.ERR_ARG
+
+
+def test_caller_spin_structure_is_used():
+    lat = Q.S2Trivalent(3)
+    t = lat.tables()
+    om = t["omega"] + 0.25
+    al = t["alpha"] - 0.5
+    lat.set_spin_structure(om, al)
+    t2 = lat.tables()
+    assert np.array_equal(t2["omega"], om) and np.array_equal(t2["alpha"], al)
+    lat.set_spin_structure(omega=t["omega"])
+    assert np.array_equal(lat.tables()["omega"], t["omega"]) and np.array_equal(lat.tables()["alpha"], al)
+    bad = t["omega"].copy()
+    bad[3] = np.nan
+    with pytest.raises(Q.Qed3Error):
+        lat.set_spin_structure(bad)
