@@ -262,9 +262,11 @@ int qed3_point_source(int n_sites, int x, int s, double* spinor);
  * on rejection, restored).  nsteps outer (fermion) steps of tmax/nsteps, each
  * with nsteps_inner gauge steps; pseudofermion solves to tol in `precision`,
  * certified by the FP64 true residual.  Writes accepted, dH, cg_iters. */
+#define QED3_INTEGRATOR_LEAPFROG_ML 0 /* ExplicitLeapfrogML, src/both_3d/integrator.h:58-168 */
+#define QED3_INTEGRATOR_LEAPFROG 1    /* ExplicitLeapfrog, src/dual/integrator.h:9-53 (nsteps_inner unused) */
 int qed3_hmc_fermion(qed3_lattice* lat, qed3_dirac* d, qed3_rng* rng, double* A, double beta, int compact, int exact,
-                     double tmax, int nsteps, int nsteps_inner, int npf, double tol, int precision, int no_reject,
-                     int* accepted, double* dH, int* cg_iters, void* stream);
+                     double tmax, int nsteps, int nsteps_inner, int npf, int integrator, double tol, int precision,
+                     int no_reject, int* accepted, double* dH, int* cg_iters, void* stream);
 /* The same trajectory with overlap fermions (the reference's IS_OVERLAP build
  * of HMC2, src/both_3d/hmc.cu:155-160,457-467): operator update =
  * Overlap::update (src/both_3d/overlap.h:207-216: links, lambda bounds by
@@ -273,9 +275,9 @@ int qed3_hmc_fermion(qed3_lattice* lat, qed3_dirac* d, qed3_rng* rng, double* A,
  * the outer CG to tol (pole solves to tol_inner); force = qed3_overlap_force.
  * ov's Wilson operator must live on lat. */
 int qed3_hmc_overlap(qed3_lattice* lat, qed3_overlap* ov, qed3_rng* rng, double* A, double beta, int compact,
-                     int exact, double tmax, int nsteps, int nsteps_inner, int npf, double lmin, double lmax,
-                     double tol, double tol_inner, int no_reject, int* accepted, double* dH, int* cg_iters,
-                     void* stream);
+                     int exact, double tmax, int nsteps, int nsteps_inner, int npf, int integrator, double lmin,
+                     double lmax, double tol, double tol_inner, int no_reject, int* accepted, double* dH,
+                     int* cg_iters, void* stream);
 int qed3_hmc_pure_gauge(qed3_lattice* lat, qed3_rng* rng, double* A, double beta, int compact, int exact,
                         double tmax, int nsteps, int no_reject, int* accepted, double* dH, void* stream);
 

@@ -1114,12 +1114,15 @@ int orc_hmc_pure_gauge(const OracleGeom* g, OracleRng* rng, double* A, double be
 //   pi -= tau/2 F_f; repeat nsteps: [gauge leapfrog with nsteps_inner inner steps of
 //   tau/nsteps_inner], update D and eta, pi -= tau F_f (tau/2 on the last step);
 //   Metropolis with the master engine's uniform.
+// integrator = 1: the single-level ExplicitLeapfrog (src/dual/integrator.h:9-53)
+// instead: nsteps of [pi -= tau/2 (F_g + F_f), U += tau pi, update D and eta,
+// pi -= tau/2 (F_g + F_f)], F_f summed over the pseudofermions.
 // The fermion force is orc_fermion_force (-2 Re <D eta, dD eta>).  Returns 1 if
 // accepted; writes dH and the total CG iterations.
 void orc_fermion_force(const OracleDirac* d, const OracleGeom* g, const double* A, const double* eta_in, double* F);
 int orc_hmc_fermion(const OracleGeom* g, OracleDirac* d, OracleRng* rng, double* A, double beta, int compact,
-                    int force_mode, double tmax, int nsteps, int nsteps_inner, int npf, double tol, int no_reject,
-                    double* dH_out, int* cg_iters) {
+                    int force_mode, double tmax, int nsteps, int nsteps_inner, int npf, int integrator, double tol,
+                    int no_reject, double* dH_out, int* cg_iters) {
   const size_t Nl = g->links.size();
   const Idx N = d->N;
   std::vector<double> pi(Nl), F(Nl), A0(A, A + Nl);
@@ -1159,8 +1162,26 @@ int orc_hmc_fermion(const OracleGeom* g, OracleDirac* d, OracleRng* rng, double*
     orc_gauge_force(g, A, beta, compact, force_mode, F.data());
     for (size_t l = 0; l < Nl; l++) pi[l] += -c * F[l];
   };
-  for (int k = 0; k < npf; k++) fermion_kick(k, 0.5 * tau);
-  for (int n = 0; n < nsteps; n++) {
+  std::vector<double> Fs(Nl);
+  auto full_kick = [&](double c) {  // pi += -c (dSg + dSf)
+    orc_gauge_force(g, A, beta, compact, force_mode, Fs.data());
+    for (int k = 0; k < npf; k++) {
+      orc_fermion_force(d, g, A, reinterpret_cast<const double*>(eta[k].data()), F.data());
+      for (size_t l = 0; l < Nl; l++) Fs[l] += F[l];
+    }
+    for (size_t l = 0; l < Nl; l++) pi[l] += -c * Fs[l];
+  };
+  if (integrator == 1) {
+    for (int n = 0; n < nsteps; n++) {
+      full_kick(0.5 * tau);
+      for (size_t l = 0; l < Nl; l++) A[l] += tau * pi[l];
+      orc_dirac_update(d, g, A);
+      for (int k = 0; k < npf; k++) solve_eta(k);
+      full_kick(0.5 * tau);
+    }
+  }
+  for (int k = 0; k < npf && integrator != 1; k++) fermion_kick(k, 0.5 * tau);
+  for (int n = 0; n < nsteps && integrator != 1; n++) {
     gauge_kick(0.5 * tau_in);
     for (int m = 0; m < nsteps_inner; m++) {
       for (size_t l = 0; l < Nl; l++) A[l] += tau_in * pi[l];

@@ -82,7 +82,8 @@ def lib():
         L.orc_num_threads.restype = ctypes.c_int
         L.orc_hmc_fermion.restype = ctypes.c_int
         L.orc_hmc_fermion.argtypes = [vp, vp, vp, vp, ctypes.c_double, ctypes.c_int, ctypes.c_int, ctypes.c_double,
-                                      ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_int, vp, vp]
+                                      ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double,
+                                      ctypes.c_int, vp, vp]
         L.orc_overlap_force.restype = ctypes.c_int
         L.orc_overlap_force.argtypes = [vp, vp, vp, ctypes.c_double, ctypes.c_double, ctypes.c_int, vp, vp,
                                         ctypes.c_double]
@@ -367,20 +368,22 @@ def num_threads() -> int:
 
 def hmc_fermion(geom: Geometry, dirac: "Dirac", rng: "Rng", A: np.ndarray, beta: float, compact: bool = True,
                 exact: bool = True, tmax: float = 1.0, nsteps: int = 10, nsteps_inner: int = 10, tol: float = 1e-12,
-                no_reject: bool = False, npf: int = 1):
+                no_reject: bool = False, npf: int = 1, integrator: int = 0):
     """HMC::run (npf = 1) or HMC2::run (npf pseudofermions) with ExplicitLeapfrogML
-    restated; A updated in place.  Returns (accepted, dH, cg_iterations)."""
+    (integrator 0) or ExplicitLeapfrog (1) restated; A updated in place.
+    Returns (accepted, dH, cg_iterations)."""
     dH = ctypes.c_double()
     its = ctypes.c_int()
     acc = lib().orc_hmc_fermion(geom.handle, dirac.h, rng.h, _dp(A), beta, int(compact), 1 if exact else 0, tmax,
-                                nsteps, nsteps_inner, npf, tol, int(no_reject), ctypes.byref(dH), ctypes.byref(its))
+                                nsteps, nsteps_inner, npf, integrator, tol, int(no_reject), ctypes.byref(dH),
+                                ctypes.byref(its))
     return bool(acc), dH.value, its.value
 
 
 def hmc_overlap(geom: Geometry, dirac: "Dirac", rng: "Rng", A: np.ndarray, beta: float, compact: bool = True,
                 exact: bool = True, tmax: float = 1.0, nsteps: int = 10, nsteps_inner: int = 10, npf: int = 1,
                 lmin: float = 0.0, lmax: float = 0.0, order: int = 21, tol: float = 1e-10, tol_inner: float = 1e-12,
-                no_reject: bool = False):
+                no_reject: bool = False, integrator: int = 0):
     """HMC2::run with Overlap fermions (src/both_3d/hmc.h:172-200, src/both_3d/hmc.cu:155-160)
     and ExplicitLeapfrogML (src/both_3d/integrator.h:117-168), composed from the
     oracle's overlap pieces; A updated in place.  lmin = lmax = 0: every operator
@@ -432,9 +435,27 @@ def hmc_overlap(geom: Geometry, dirac: "Dirac", rng: "Rng", A: np.ndarray, beta:
     h0 = H()
     tau = tmax / nsteps
     tau_in = tau / nsteps_inner
-    for k in range(npf):
+
+    def full_force():  # dSg + dSf, the single-level ExplicitLeapfrog's kick
+        Fs = gauge_force(geom, A, beta, compact, exact)
+        for k in range(npf):
+            Fs = Fs + dirac.overlap_force(A, etas[k], bounds[0], bounds[1], order, tol_inner)
+        return Fs
+
+    if integrator == 1:
+        for n in range(nsteps):
+            pi += -0.5 * tau * full_force()
+            A += tau * pi
+            update()
+            for k in range(npf):
+                etas[k] = solve(phis[k])
+            pi += -0.5 * tau * full_force()
+        nsteps_ml = 0
+    else:
+        nsteps_ml = nsteps
+    for k in range(npf if integrator != 1 else 0):
         pi -= 0.5 * tau * dirac.overlap_force(A, etas[k], bounds[0], bounds[1], order, tol_inner)
-    for n in range(nsteps):
+    for n in range(nsteps_ml):
         pi -= 0.5 * tau_in * gauge_force(geom, A, beta, compact, exact)
         for m in range(nsteps_inner):
             A += tau_in * pi

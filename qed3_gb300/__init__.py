@@ -31,6 +31,7 @@ LIB_PATH = os.path.join(_HERE, "libqed3.so")
 OK, ERR_ARG, ERR_CUDA, ERR_NOCONV, ERR_TIMEOUT, ERR_STATE, ERR_NOMEM = range(7)
 OP_D, OP_DDAG, OP_DDAGD, OP_DDDAG = range(4)
 PREC_F64, PREC_F32, PREC_BF16 = range(3)
+INTEGRATOR_LEAPFROG_ML, INTEGRATOR_LEAPFROG = 0, 1
 SOLVE_STREAMING = 2
 SOLVE_BCAST_B = 4
 SOLVE_FLEXIBLE = 8
@@ -98,10 +99,11 @@ SIGNATURES = [
     ("qed3_rng_z2_spinor", ctypes.c_int, [vp, vp]),
     ("qed3_point_source", ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, vp]),
     ("qed3_hmc_fermion", ctypes.c_int, [vp, vp, vp, vp, ctypes.c_double, ctypes.c_int, ctypes.c_int, ctypes.c_double,
-                                        ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_int,
-                                        ctypes.c_int, c_int_p, c_double_p, c_int_p, vp]),
+                                        ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double,
+                                        ctypes.c_int, ctypes.c_int, c_int_p, c_double_p, c_int_p, vp]),
     ("qed3_hmc_overlap", ctypes.c_int, [vp, vp, vp, vp, ctypes.c_double, ctypes.c_int, ctypes.c_int, ctypes.c_double,
-                                        ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double,
+                                        ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double,
+                                        ctypes.c_double,
                                         ctypes.c_double, ctypes.c_double, ctypes.c_int, c_int_p, c_double_p, c_int_p,
                                         vp]),
     ("qed3_hmc_pure_gauge", ctypes.c_int, [vp, vp, vp, ctypes.c_double, ctypes.c_int, ctypes.c_int, ctypes.c_double,
@@ -420,13 +422,15 @@ def hmc_pure_gauge(lattice: S2Trivalent, rng: ParallelRng, A, beta: float, compa
 
 def hmc_fermion(lattice: S2Trivalent, dirac: DiracS2Dual, rng: "ParallelRng", A, beta: float, compact: bool = True,
                 exact: bool = True, tmax: float = 1.0, nsteps: int = 10, nsteps_inner: int = 10, tol: float = 1e-10,
-                precision: int = PREC_F32, no_reject: bool = False, npf: int = 1, stream=None):
+                precision: int = PREC_F32, no_reject: bool = False, npf: int = 1,
+                integrator: int = 0, stream=None):
     """One Wilson-fermion HMC trajectory on device links A (in place): HMC::run (npf = 1)
-    or HMC2::run (npf pseudofermions) with ExplicitLeapfrogML.  Returns
+    or HMC2::run (npf pseudofermions) with ExplicitLeapfrogML (integrator
+    INTEGRATOR_LEAPFROG_ML) or ExplicitLeapfrog (INTEGRATOR_LEAPFROG).  Returns
     (accepted, dH, cg_iterations)."""
     acc, dH, its = ctypes.c_int(), ctypes.c_double(), ctypes.c_int()
     _check(lib().qed3_hmc_fermion(lattice.handle, dirac.handle, rng.handle, _ptr(A), beta, int(compact), int(exact),
-                                  tmax, nsteps, nsteps_inner, npf, tol, precision, int(no_reject), ctypes.byref(acc),
+                                  tmax, nsteps, nsteps_inner, npf, integrator, tol, precision, int(no_reject), ctypes.byref(acc),
                                   ctypes.byref(dH), ctypes.byref(its), _stream(stream)))
     return bool(acc.value), dH.value, its.value
 
@@ -434,14 +438,14 @@ def hmc_fermion(lattice: S2Trivalent, dirac: DiracS2Dual, rng: "ParallelRng", A,
 def hmc_overlap(lattice: S2Trivalent, overlap: "Overlap", rng: "ParallelRng", A, beta: float, compact: bool = True,
                 exact: bool = True, tmax: float = 1.0, nsteps: int = 10, nsteps_inner: int = 10, npf: int = 1,
                 lambda_min: float = 0.0, lambda_max: float = 0.0, tol: float = 1e-10, tol_inner: float = 1e-12,
-                no_reject: bool = False, stream=None):
+                no_reject: bool = False, integrator: int = 0, stream=None):
     """One overlap-fermion HMC trajectory (HMC2::run with Overlap fermions) on device
     links A, in place.  lambda_min = lambda_max = 0: the operator update recomputes
     the spectral bounds (Overlap::update); otherwise the bounds stay fixed.
     Returns (accepted, dH, outer_cg_iterations)."""
     acc, dH, its = ctypes.c_int(), ctypes.c_double(), ctypes.c_int()
     _check(lib().qed3_hmc_overlap(lattice.handle, overlap._h, rng.handle, _ptr(A), beta, int(compact), int(exact),
-                                  tmax, nsteps, nsteps_inner, npf, lambda_min, lambda_max, tol, tol_inner,
+                                  tmax, nsteps, nsteps_inner, npf, integrator, lambda_min, lambda_max, tol, tol_inner,
                                   int(no_reject), ctypes.byref(acc), ctypes.byref(dH), ctypes.byref(its),
                                   _stream(stream)))
     return bool(acc.value), dH.value, its.value

@@ -409,23 +409,25 @@ int qed3_point_source(int n_sites, int x, int s, double* spinor) {
 }
 
 int qed3_hmc_fermion(qed3_lattice* lat, qed3_dirac* d, qed3_rng* rng, double* A, double beta, int compact, int exact,
-                     double tmax, int nsteps, int nsteps_inner, int npf, double tol, int precision, int no_reject,
-                     int* accepted, double* dH, int* cg_iters, void* stream) {
+                     double tmax, int nsteps, int nsteps_inner, int npf, int integrator, double tol, int precision,
+                     int no_reject, int* accepted, double* dH, int* cg_iters, void* stream) {
   QED3_GUARD_BEGIN
   if (!lat || !d || !rng || !A || !accepted || !dH) return fail(QED3_ERR_ARG, "NULL argument");
   if (d->lat != lat) return fail(QED3_ERR_ARG, "operator belongs to another lattice");
   if (nsteps < 1 || nsteps_inner < 1 || !(tmax > 0)) return fail(QED3_ERR_ARG, "need nsteps, nsteps_inner >= 1, tmax > 0");
   if (precision < 0 || precision > 2) return fail(QED3_ERR_ARG, "unknown precision");
   if (npf < 1 || npf > 64) return fail(QED3_ERR_ARG, "need 1 <= npf <= 64 pseudofermions");
-  return hmc_fermion(lat, d, rng, A, beta, compact, exact, tmax, nsteps, nsteps_inner, npf, tol > 0 ? tol : 1e-10,
-                     precision, no_reject, accepted, dH, cg_iters, (cudaStream_t)stream);
+  if (integrator != QED3_INTEGRATOR_LEAPFROG_ML && integrator != QED3_INTEGRATOR_LEAPFROG)
+    return fail(QED3_ERR_ARG, "unknown integrator");
+  return hmc_fermion(lat, d, rng, A, beta, compact, exact, tmax, nsteps, nsteps_inner, npf, integrator,
+                     tol > 0 ? tol : 1e-10, precision, no_reject, accepted, dH, cg_iters, (cudaStream_t)stream);
   QED3_GUARD_END
 }
 
 int qed3_hmc_overlap(qed3_lattice* lat, qed3_overlap* ov, qed3_rng* rng, double* A, double beta, int compact,
-                     int exact, double tmax, int nsteps, int nsteps_inner, int npf, double lmin, double lmax,
-                     double tol, double tol_inner, int no_reject, int* accepted, double* dH, int* cg_iters,
-                     void* stream) {
+                     int exact, double tmax, int nsteps, int nsteps_inner, int npf, int integrator, double lmin,
+                     double lmax, double tol, double tol_inner, int no_reject, int* accepted, double* dH,
+                     int* cg_iters, void* stream) {
   QED3_GUARD_BEGIN
   if (!lat || !ov || !rng || !A || !accepted || !dH) return fail(QED3_ERR_ARG, "NULL argument");
   if (overlap_dirac(ov)->lat != lat) return fail(QED3_ERR_ARG, "overlap operator belongs to another lattice");
@@ -433,9 +435,11 @@ int qed3_hmc_overlap(qed3_lattice* lat, qed3_overlap* ov, qed3_rng* rng, double*
   if (npf < 1 || npf > 64) return fail(QED3_ERR_ARG, "need 1 <= npf <= 64 pseudofermions");
   const bool fixed = lmin > 0 || lmax > 0;
   if (fixed && !(lmin > 0 && lmin < lmax)) return fail(QED3_ERR_ARG, "fixed bounds need 0 < lmin < lmax");
-  return hmc_overlap(lat, ov, rng, A, beta, compact, exact, tmax, nsteps, nsteps_inner, npf, fixed ? lmin : 0.0,
-                     fixed ? lmax : 0.0, tol > 0 ? tol : 1e-10, tol_inner > 0 ? tol_inner : 1e-12, no_reject, accepted,
-                     dH, cg_iters, (cudaStream_t)stream);
+  if (integrator != QED3_INTEGRATOR_LEAPFROG_ML && integrator != QED3_INTEGRATOR_LEAPFROG)
+    return fail(QED3_ERR_ARG, "unknown integrator");
+  return hmc_overlap(lat, ov, rng, A, beta, compact, exact, tmax, nsteps, nsteps_inner, npf, integrator,
+                     fixed ? lmin : 0.0, fixed ? lmax : 0.0, tol > 0 ? tol : 1e-10, tol_inner > 0 ? tol_inner : 1e-12,
+                     no_reject, accepted, dH, cg_iters, (cudaStream_t)stream);
   QED3_GUARD_END
 }
 

@@ -404,16 +404,6 @@ int hmc_pure_gauge(qed3_lattice_s* lat, qed3_rng_s* rng, double* A, double beta,
 }
 
 
-// Fermion HMC trajectory (HMC::run, src/both_3d/hmc.h:75-110, one PseudoFermion,
-// src/both_3d/pseudofermion.h:33-60, ExplicitLeapfrogML,
-// src/both_3d/integrator.h:58-115), every field on the device:
-//   pi ~ N(0,1) per link, xi = fill_gaussian (the reference's streams),
-//   phi = D^dag xi, eta = (D^dag D)^{-1} phi (certified CG), H = 1/2|pi|^2 + S_g + Re<phi,eta>;
-//   pi -= tau/2 F_f; nsteps x [gauge leapfrog of nsteps_inner steps tau/nsteps_inner,
-//   D(U) and eta updated, pi -= tau F_f (tau/2 on the last)]; Metropolis on dH
-//   with the master engine's uniform; a rejection restores U and the operator.
-// dH = sum (pi^2 - pi0^2)/2 + beta * sum (action density differences) + Re<phi, eta1 - eta0>,
-// each difference formed term by term.
 // The fermion side of a trajectory: set the operator from the links,
 // phi = D^dag xi, eta = (D^dag D)^{-1} phi, and the force
 // F_l = dS/dA_l = -2 Re <eta, d(D) eta>-type term of the operator.
@@ -424,16 +414,23 @@ struct HmcFermion {
   std::function<int(const double* eta, double* F)> force;
 };
 
-// HMC::run (npf = 1) / HMC2::run (src/both_3d/hmc.h:75-110, :172-200) with
-// ExplicitLeapfrogML (src/both_3d/integrator.h:58-168): momenta and one xi per
-// pseudofermion from the RNG streams, phi = D^dag xi, eta solved; half fermion
-// kick per pseudofermion; nsteps of [gauge leapfrog with nsteps_inner steps,
-// operator update, per pseudofermion: solve + kick]; dH from per-term
-// differences; Metropolis with the master engine; links and operator restored
-// on rejection.
+// HMC::run (npf = 1) / HMC2::run (src/both_3d/hmc.h:75-110, :172-200), every
+// field on the device: momenta and one xi per pseudofermion from the RNG
+// streams (fill_gaussian order), phi = D^dag xi, eta = (D^dag D)^{-1} phi;
+// H = |pi|^2/2 + S_g + sum Re<phi, eta>, dH formed term by term; Metropolis
+// with the master engine's uniform; links and operator restored on rejection.
+// Integrators:
+//  * QED3_INTEGRATOR_LEAPFROG_ML, ExplicitLeapfrogML
+//    (src/both_3d/integrator.h:58-168): half fermion kick per pseudofermion;
+//    nsteps of [gauge leapfrog with nsteps_inner steps of tau/nsteps_inner,
+//    operator update, per pseudofermion: solve + kick (half on the last)];
+//  * QED3_INTEGRATOR_LEAPFROG, ExplicitLeapfrog (src/dual/integrator.h:9-53):
+//    nsteps of [pi -= tau/2 (F_g + F_f), U += tau pi, operator update and
+//    solves, pi -= tau/2 (F_g + F_f)] (F_f summed over the pseudofermions).
 static int hmc_trajectory(qed3_lattice_s* lat, const HmcFermion& fo, long long nd, qed3_rng_s* rng, double* A,
                           double beta, int compact, int exact, double tmax, int nsteps, int nsteps_inner, int npf,
-                          int no_reject, int* accepted, double* dH_out, int* cg_iters, cudaStream_t st) {
+                          int integrator, int no_reject, int* accepted, double* dH_out, int* cg_iters,
+                          cudaStream_t st) {
   int rc = gauge_prepare(lat);
   if (rc) return rc;
   GaugeDev& G = lat->gauge;
@@ -481,9 +478,29 @@ static int hmc_trajectory(qed3_lattice_s* lat, const HmcFermion& fo, long long n
       if (!f) k_axpy<<<nblk(Nl), 256, 0, st>>>(Nl, -c, G.F, G.pi);
       return f;
     };
-    for (int k = 0; k < npf; k++)
+    // pi -= c (F_g + sum_k F_f,k): the forces summed first, as (dSg + dSf)
+    auto full_kick = [&](double c) -> int {
+      int f = gauge_force(lat, A, beta, compact, exact, G.F, st);
+      for (int k = 0; k < npf && !f; k++) {
+        f = fo.force(eta + nd * k, Ff);
+        if (!f) k_axpy<<<nblk(Nl), 256, 0, st>>>(Nl, 1.0, Ff, G.F);
+      }
+      if (!f) k_axpy<<<nblk(Nl), 256, 0, st>>>(Nl, -c, G.F, G.pi);
+      return f;
+    };
+    if (integrator == QED3_INTEGRATOR_LEAPFROG) {
+      for (int n = 0; n < nsteps; n++) {
+        if ((e = full_kick(0.5 * tau))) return e;
+        k_axpy<<<nblk(Nl), 256, 0, st>>>(Nl, tau, G.pi, A);
+        if ((e = fo.update(A))) return e;
+        for (int k = 0; k < npf; k++)
+          if ((e = solve_eta(k))) return e;
+        if ((e = full_kick(0.5 * tau))) return e;
+      }
+    }
+    for (int k = 0; k < npf && integrator != QED3_INTEGRATOR_LEAPFROG; k++)
       if ((e = fermion_kick(k, 0.5 * tau))) return e;
-    for (int n = 0; n < nsteps; n++) {
+    for (int n = 0; n < nsteps && integrator != QED3_INTEGRATOR_LEAPFROG; n++) {
       if ((e = gauge_kick(0.5 * tau_in))) return e;
       for (int m = 0; m < nsteps_inner; m++) {
         k_axpy<<<nblk(Nl), 256, 0, st>>>(Nl, tau_in, G.pi, A);
@@ -527,8 +544,8 @@ static int hmc_trajectory(qed3_lattice_s* lat, const HmcFermion& fo, long long n
 }
 
 int hmc_fermion(qed3_lattice_s* lat, qed3_dirac_s* d, qed3_rng_s* rng, double* A, double beta, int compact, int exact,
-                double tmax, int nsteps, int nsteps_inner, int npf, double tol, int prec, int no_reject, int* accepted,
-                double* dH_out, int* cg_iters, cudaStream_t st) {
+                double tmax, int nsteps, int nsteps_inner, int npf, int integrator, double tol, int prec, int no_reject,
+                int* accepted, double* dH_out, int* cg_iters, cudaStream_t st) {
   const qed3_solve_params sp{tol, 0, prec, 0.1, 0.0, 0};
   HmcFermion fo;
   fo.update = [&](const double* U) { return dirac_set_links(d, U, 1, st); };
@@ -542,7 +559,7 @@ int hmc_fermion(qed3_lattice_s* lat, qed3_dirac_s* d, qed3_rng_s* rng, double* A
   };
   fo.force = [&](const double* eta, double* F) { return fermion_force(d, eta, F, st); };
   return hmc_trajectory(lat, fo, 4LL * d->Ns, rng, A, beta, compact, exact, tmax, nsteps, nsteps_inner, npf,
-                        no_reject, accepted, dH_out, cg_iters, st);
+                        integrator, no_reject, accepted, dH_out, cg_iters, st);
 }
 
 // Overlap fermions (the reference's IS_OVERLAP build of HMC2): the operator
@@ -551,8 +568,9 @@ int hmc_fermion(qed3_lattice_s* lat, qed3_dirac_s* d, qed3_rng_s* rng, double* A
 // fixed bounds lmin, lmax > 0 are given; eta = (D_ov^dag D_ov)^{-1} phi by the
 // outer CG; the force is the overlap force (src/both_3d/overlap.h:393-470).
 int hmc_overlap(qed3_lattice_s* lat, qed3_overlap_s* ov, qed3_rng_s* rng, double* A, double beta, int compact,
-                int exact, double tmax, int nsteps, int nsteps_inner, int npf, double lmin, double lmax, double tol,
-                double tol_inner, int no_reject, int* accepted, double* dH_out, int* cg_iters, cudaStream_t st) {
+                int exact, double tmax, int nsteps, int nsteps_inner, int npf, int integrator, double lmin, double lmax,
+                double tol, double tol_inner, int no_reject, int* accepted, double* dH_out, int* cg_iters,
+                cudaStream_t st) {
   qed3_dirac_s* d = overlap_dirac(ov);
   HmcFermion fo;
   fo.update = [&](const double* U) {
@@ -571,7 +589,7 @@ int hmc_overlap(qed3_lattice_s* lat, qed3_overlap_s* ov, qed3_rng_s* rng, double
   };
   fo.force = [&](const double* eta, double* F) { return overlap_force(ov, eta, F, tol_inner, nullptr, st); };
   return hmc_trajectory(lat, fo, 4LL * d->Ns, rng, A, beta, compact, exact, tmax, nsteps, nsteps_inner, npf,
-                        no_reject, accepted, dH_out, cg_iters, st);
+                        integrator, no_reject, accepted, dH_out, cg_iters, st);
 }
 
 }  // namespace qed3

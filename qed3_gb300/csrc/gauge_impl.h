@@ -23,11 +23,12 @@ void rng_gaussian_spinor(qed3_rng_s* r, double* out);
 double rng_uniform(qed3_rng_s* r);
 void rng_z2_spinor(qed3_rng_s* r, double* out);
 int hmc_fermion(qed3_lattice_s* lat, qed3_dirac_s* d, qed3_rng_s* rng, double* A, double beta, int compact, int exact,
-                double tmax, int nsteps, int nsteps_inner, int npf, double tol, int prec, int no_reject, int* accepted,
-                double* dH_out, int* cg_iters, cudaStream_t st);
+                double tmax, int nsteps, int nsteps_inner, int npf, int integrator, double tol, int prec, int no_reject,
+                int* accepted, double* dH_out, int* cg_iters, cudaStream_t st);
 int hmc_overlap(qed3_lattice_s* lat, qed3_overlap_s* ov, qed3_rng_s* rng, double* A, double beta, int compact,
-                int exact, double tmax, int nsteps, int nsteps_inner, int npf, double lmin, double lmax, double tol,
-                double tol_inner, int no_reject, int* accepted, double* dH_out, int* cg_iters, cudaStream_t st);
+                int exact, double tmax, int nsteps, int nsteps_inner, int npf, int integrator, double lmin, double lmax,
+                double tol, double tol_inner, int no_reject, int* accepted, double* dH_out, int* cg_iters,
+                cudaStream_t st);
 int hmc_pure_gauge(qed3_lattice_s* lat, qed3_rng_s* rng, double* A, double beta, int compact, int exact, double tmax,
                    int nsteps, int no_reject, int* accepted, double* dH, cudaStream_t st);
 }  // namespace qed3

@@ -79,7 +79,8 @@ def test_hmc_trajectory_matches_oracle(cuda, compact):
         assert np.abs(from_dev(At) - Ao).max() < 1e-11
 
 
-def test_fermion_hmc_matches_oracle(cuda):
+@pytest.mark.parametrize("integrator", [Q.INTEGRATOR_LEAPFROG_ML, Q.INTEGRATOR_LEAPFROG])
+def test_fermion_hmc_matches_oracle(cuda, integrator):
     """Wilson-fermion HMC trajectories (HMC::run + ExplicitLeapfrogML, one
     pseudofermion) against the oracle's restatement from the same RNG streams:
     same Metropolis decisions, dH and links to the pseudofermion-solve tolerance."""
@@ -94,9 +95,10 @@ def test_fermion_hmc_matches_oracle(cuda):
     Do = O.Dirac(g, 1.0, 0.1)
     Dq = Q.DiracS2Dual(lat, 1.0, 0.1)
     for it in range(3):
-        acc_o, dh_o, _ = O.hmc_fermion(g, Do, ro, Ao, 1.4, tmax=0.5, nsteps=5, nsteps_inner=4, tol=1e-13)
+        acc_o, dh_o, _ = O.hmc_fermion(g, Do, ro, Ao, 1.4, tmax=0.5, nsteps=5, nsteps_inner=4, tol=1e-13,
+                                       integrator=integrator)
         acc_q, dh_q, its = Q.hmc_fermion(lat, Dq, rq, At, 1.4, tmax=0.5, nsteps=5, nsteps_inner=4, tol=1e-13,
-                                         precision=Q.PREC_F64)
+                                         precision=Q.PREC_F64, integrator=integrator)
         assert acc_o == acc_q and its > 0
         assert abs(dh_o - dh_q) < 1e-8 * max(1.0, abs(dh_o))
         assert np.abs(from_dev(At) - Ao).max() < 1e-9

@@ -309,3 +309,19 @@ def test_gauge_side_matches_reference_build():
             # dH = H1 - H0 of totals ~1e2: the last bits depend on the summation order
             assert acc == bool(hm["accepted"][t]) and abs(dH - float.fromhex(hm["dH"][t])) < 1e-12
         assert np.array_equal(Ao, h(hm["A_final"]))
+
+
+def test_single_level_leapfrog_second_order():
+    """ExplicitLeapfrog (src/dual/integrator.h:9-53) restated: dH ~ tau^2 (RMS)."""
+    g = O.geometry(2)
+    A = np.random.default_rng(3).normal(size=g.n_links) * 0.3
+    rms = []
+    for ns in (16, 32):
+        v = []
+        for seed in range(5, 9):
+            D = O.Dirac(g, 1.0, 0.1)
+            _, d, _ = O.hmc_fermion(g, D, O.Rng(g, seed), A.copy(), 1.4, tmax=1.0, nsteps=ns, no_reject=True,
+                                    integrator=1)
+            v.append(d)
+        rms.append(np.sqrt(np.mean(np.square(v))))
+    assert 3.0 < rms[0] / rms[1] < 5.0, rms

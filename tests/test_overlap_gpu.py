@@ -168,7 +168,8 @@ def test_ill_conditioned_poles_run_in_fp64(cuda):
     assert ov64.update(lmin, lmax)["npoles_fp64"] == 0
 
 
-def test_overlap_hmc_matches_oracle(cuda):
+@pytest.mark.parametrize("integrator", [Q.INTEGRATOR_LEAPFROG_ML, Q.INTEGRATOR_LEAPFROG])
+def test_overlap_hmc_matches_oracle(cuda, integrator):
     """Overlap-fermion HMC (HMC2::run with Overlap fermions, fixed spectral
     bounds) against the oracle's composition of its overlap pieces from the
     same RNG streams: same Metropolis decisions, dH and links."""
@@ -189,9 +190,10 @@ def test_overlap_hmc_matches_oracle(cuda):
     At = to_dev(A0, cuda)
     for it in range(2):
         acc_o, dh_o, its_o = O.hmc_overlap(g, Do, ro, Ao, 1.4, tmax=0.5, nsteps=4, nsteps_inner=4, lmin=lmin,
-                                           lmax=lmax, order=21, tol=1e-11, tol_inner=1e-13)
+                                           lmax=lmax, order=21, tol=1e-11, tol_inner=1e-13, integrator=integrator)
         acc_q, dh_q, its_q = Q.hmc_overlap(lat, ov, rq, At, 1.4, tmax=0.5, nsteps=4, nsteps_inner=4,
-                                           lambda_min=lmin, lambda_max=lmax, tol=1e-11, tol_inner=1e-13)
+                                           lambda_min=lmin, lambda_max=lmax, tol=1e-11, tol_inner=1e-13,
+                                           integrator=integrator)
         assert acc_o == acc_q and its_q > 0
         assert abs(dh_o - dh_q) < 1e-7, (dh_o, dh_q)
         assert np.abs(from_dev(At) - Ao).max() < 1e-9
