@@ -21,6 +21,7 @@
 #include <vector>
 
 #include "device.cuh"
+#include "batched_impl.h"
 #include "blas_impl.h"
 #include "dirac_impl.h"
 #include "gauge_impl.h"
@@ -411,6 +412,8 @@ struct HmcFermion {
   std::function<int(const double* A)> update;
   std::function<int(double* phi, const double* xi)> apply_dag;
   std::function<int(double* eta, const double* phi, int* iters)> solve;
+  // optional: every pseudofermion's solve at once (eta, phi: npf fields back to back)
+  std::function<int(double* eta, const double* phi, int npf, int* iters)> solve_all;
   std::function<int(const double* eta, double* F)> force;
 };
 
@@ -454,6 +457,14 @@ static int hmc_trajectory(qed3_lattice_s* lat, const HmcFermion& fo, long long n
   }
   int its = 0;
   auto solve_eta = [&](int k) -> int { return fo.solve(eta + nd * k, phi + nd * k, &its); };
+  // the npf solves of one operator update: one batched launch when available
+  // (their order does not matter: no solve depends on the momenta)
+  auto solve_all = [&]() -> int {
+    if (fo.solve_all && npf > 1) return fo.solve_all(eta, phi, npf, &its);
+    for (int k = 0; k < npf; k++)
+      if (int e = solve_eta(k)) return e;
+    return QED3_OK;
+  };
   auto run = [&]() -> int {
     int e;
     QED3_CUDA_TRY(cudaMemcpyAsync(G.pi, pi.data(), size_t(Nl) * sizeof(double), cudaMemcpyHostToDevice, st));
@@ -463,8 +474,7 @@ static int hmc_trajectory(qed3_lattice_s* lat, const HmcFermion& fo, long long n
     if ((e = fo.update(A))) return e;
     for (int k = 0; k < npf; k++)
       if ((e = fo.apply_dag(phi + nd * k, dxi + nd * k))) return e;
-    for (int k = 0; k < npf; k++)
-      if ((e = solve_eta(k))) return e;
+    if ((e = solve_all())) return e;
     QED3_CUDA_TRY(cudaMemcpyAsync(eta0, eta, vbytes, cudaMemcpyDeviceToDevice, st));
     if ((e = gauge_plaquettes(lat, A, G.th0, st))) return e;
     const double tau = tmax / nsteps, tau_in = tau / nsteps_inner;
@@ -493,8 +503,7 @@ static int hmc_trajectory(qed3_lattice_s* lat, const HmcFermion& fo, long long n
         if ((e = full_kick(0.5 * tau))) return e;
         k_axpy<<<nblk(Nl), 256, 0, st>>>(Nl, tau, G.pi, A);
         if ((e = fo.update(A))) return e;
-        for (int k = 0; k < npf; k++)
-          if ((e = solve_eta(k))) return e;
+        if ((e = solve_all())) return e;
         if ((e = full_kick(0.5 * tau))) return e;
       }
     }
@@ -507,10 +516,9 @@ static int hmc_trajectory(qed3_lattice_s* lat, const HmcFermion& fo, long long n
         if ((e = gauge_kick((m != nsteps_inner - 1 ? 1.0 : 0.5) * tau_in))) return e;
       }
       if ((e = fo.update(A))) return e;
-      for (int k = 0; k < npf; k++) {
-        if ((e = solve_eta(k))) return e;
+      if ((e = solve_all())) return e;
+      for (int k = 0; k < npf; k++)
         if ((e = fermion_kick(k, (n != nsteps - 1 ? 1.0 : 0.5) * tau))) return e;
-      }
     }
     QED3_CUDA_TRY(cudaGetLastError());
     if ((e = gauge_plaquettes(lat, A, G.th1, st))) return e;
@@ -558,8 +566,30 @@ int hmc_fermion(qed3_lattice_s* lat, qed3_dirac_s* d, qed3_rng_s* rng, double* A
     return e;
   };
   fo.force = [&](const double* eta, double* F) { return fermion_force(d, eta, F, st); };
-  return hmc_trajectory(lat, fo, 4LL * d->Ns, rng, A, beta, compact, exact, tmax, nsteps, nsteps_inner, npf,
-                        integrator, no_reject, accepted, dH_out, cg_iters, st);
+  // several pseudofermions of the one operator: one batched persistent launch
+  // per operator update, the right-hand sides in one tile
+  qed3_batch_s* bt = nullptr;
+  fo.solve_all = [&](double* eta, const double* phi, int n, int* its) -> int {
+    if (!bt) {
+      const int tile = n <= 1 ? 1 : n <= 2 ? 2 : n <= 4 ? 4 : 8;
+      qed3_dirac_s* ops[1] = {d};
+      const int nr[1] = {n};
+      if (int e = batch_create(1, ops, nr, prec, tile, 128, &bt)) return e;
+    }
+    double* xs[1] = {eta};
+    const double* bs[1] = {phi};
+    std::vector<qed3_solve_report> reps(static_cast<size_t>(n));
+    int e = batch_solve(bt, xs, bs, nullptr, &sp, reps.data(), nullptr, st);
+    for (const auto& r : reps) {
+      *its += r.iters;
+      if (!e && r.status != QED3_OK) e = fail(QED3_ERR_NOCONV, "pseudofermion solve did not converge");
+    }
+    return e;
+  };
+  const int rc = hmc_trajectory(lat, fo, 4LL * d->Ns, rng, A, beta, compact, exact, tmax, nsteps, nsteps_inner, npf,
+                                integrator, no_reject, accepted, dH_out, cg_iters, st);
+  if (bt) batch_destroy(bt);
+  return rc;
 }
 
 // Overlap fermions (the reference's IS_OVERLAP build of HMC2): the operator
