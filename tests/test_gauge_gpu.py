@@ -185,9 +185,9 @@ def test_product_rng_matches_reference_build(cuda):
 
 def test_product_gauge_side_matches_reference_build(cuda):
     """The library's plaquettes, action, force and pure-gauge HMC against the
-    reference's own gauge code compiled in place (golden fixture): angles and
-    forces to rounding, the same Metropolis decisions, dH and links to the
-    per-term-difference accuracy of the device reductions."""
+    reference's own gauge code compiled in place (golden fixture): angles bit
+    for bit, forces to rounding, the same Metropolis decisions, dH within 1e-12
+    and the links to rounding after three trajectories."""
     import json
     import os
     import torch
@@ -199,7 +199,7 @@ def test_product_gauge_side_matches_reference_build(cuda):
         At = to_dev(A, cuda)
         th = torch.zeros(lat.n_faces, dtype=torch.float64, device=cuda)
         avg = Q.plaquette(lat, At, th)
-        assert np.abs(from_dev(th) - h(c["theta"])).max() < 1e-14
+        assert np.array_equal(from_dev(th), h(c["theta"]))
         assert abs(avg - float.fromhex(c["avg_plaquette"])) < 1e-14
         S_ref = float.fromhex(c["action"])
         assert abs(Q.gauge_action(lat, At, c["beta"], c["compact"]) - S_ref) < 1e-13 * abs(S_ref)
@@ -212,5 +212,5 @@ def test_product_gauge_side_matches_reference_build(cuda):
         for t in range(len(hm["dH"])):
             acc, dH = Q.hmc_pure_gauge(lat, rng, At, c["beta"], c["compact"], False, hm["tmax"], hm["nsteps"])
             assert acc == bool(hm["accepted"][t])
-            assert abs(dH - float.fromhex(hm["dH"][t])) < 1e-10
-        assert np.abs(from_dev(At) - h(hm["A_final"])).max() < 1e-10
+            assert abs(dH - float.fromhex(hm["dH"][t])) < 1e-12  # measured <= 1.7e-13
+        assert np.abs(from_dev(At) - h(hm["A_final"])).max() < 1e-13
