@@ -188,3 +188,31 @@ def test_bicgstab_to_tolerance_and_shift(cuda):
     xt = torch.ones_like(bt)
     rep = Dq.bicgstab(xt, torch.zeros_like(bt), op=Q.OP_D)
     assert rep.status == Q.OK and float(xt.abs().max()) == 0.0
+
+
+def test_cpu_runnable_configuration_n8_on_the_gpu(cuda):
+    """The plain method's CPU-runnable configuration (n=8; links from the
+    reference's pure-gauge HMC recipe at beta = 1.4, seed 1, 200 trajectories;
+    r = 1, m = 0.1; Gaussian source seed 7): the device FP64 CG takes the
+    oracle's iterations and solution; the mixed solvers reach the same
+    certified 1e-10."""
+    import torch
+    from tests.configs import reference_thermalised_links
+    g = O.geometry(8)
+    lat = Q.S2Trivalent(8)
+    A, _ = reference_thermalised_links(g, 1.4, 1, 200)
+    Do = O.Dirac(g, 1.0, 0.1)
+    Do.update(A)
+    Dq = Q.DiracS2Dual(lat, 1.0, 0.1)
+    Dq.update(A)
+    b = O.Rng(g, 7).gaussian_spinor()
+    xo, it_o, _ = Do.cg(b, tol=1e-10)
+    bt = to_dev(b, cuda)
+    for prec in (Q.PREC_F64, Q.PREC_F32, Q.PREC_BF16):
+        xt = torch.zeros_like(bt)
+        rep = Dq.solve(xt, bt, tol=1e-10, precision=prec)
+        assert rep.status == Q.OK and rep.true_rel_res <= 1e-10
+        x = from_dev(xt)
+        assert np.linalg.norm(x - xo) / np.linalg.norm(xo) < 1e-8
+        if prec == Q.PREC_F64:
+            assert abs(rep.iters - it_o) <= 1, (rep.iters, it_o)

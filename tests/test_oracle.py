@@ -325,3 +325,23 @@ def test_single_level_leapfrog_second_order():
             v.append(d)
         rms.append(np.sqrt(np.mean(np.square(v))))
     assert 3.0 < rms[0] / rms[1] < 5.0, rms
+
+
+def test_cpu_runnable_configuration_n8():
+    """The plain method's CPU-runnable configuration: n=8 (1,280 dual sites,
+    1,920 links), compact links from the reference's pure-gauge HMC recipe at
+    beta = 1.4, seed 1, after 200 thermalisation trajectories; r = 1, m = 0.1;
+    one Gaussian source (seed 7); FP64 CG on D^dag D to 1e-10."""
+    from tests.configs import reference_thermalised_links
+    g = O.geometry(8)
+    assert (g.n_sites, g.n_links) == (1280, 1920)
+    A, acc = reference_thermalised_links(g, 1.4, 1, 200)
+    # the reference's compact force is theta, not sin(theta) (src/dual/action.h:37),
+    # so its compact trajectories conserve H poorly: acceptance ~10 %
+    assert 0.0 < acc <= 1.0
+    D = O.Dirac(g, 1.0, 0.1)
+    D.update(A)
+    b = O.Rng(g, 7).gaussian_spinor()
+    x, it, _ = D.cg(b, tol=1e-10)
+    assert np.linalg.norm(b - D.apply(x, 2)) / np.linalg.norm(b) <= 1e-10
+    assert 20 < it < 2000
