@@ -276,6 +276,25 @@ def profile_case(torch, which):
         for prec in (Q.PREC_F32, Q.PREC_BF16, Q.PREC_F64):
             r = apply_bandwidth(torch, Q, 512, prec, reps=3)
             print(json.dumps(r))
+    elif which == "batched":
+        # a quarter of the 256-RHS configuration (16 right-hand sides on each
+        # of n = 16, 32, 48, 64; ~0.4 GB of fields, above L2) with the tile the
+        # autotuner picks for the full one, so no tuning launches precede it
+        rng = np.random.default_rng(256)
+        systems, bs = [], []
+        for n in (16, 32, 48, 64):
+            lat_n = Q.S2Trivalent(n)
+            D_n = Q.DiracS2Dual(lat_n, 1.0, float(rng.uniform(0.02, 0.2)))
+            D_n.update(torch.from_numpy(rng.uniform(-np.pi, np.pi, lat_n.n_links)).cuda())
+            b_n = rng.normal(size=(16, 2 * lat_n.n_sites)) + 1j * rng.normal(size=(16, 2 * lat_n.n_sites))
+            systems.append((D_n, 16))
+            bs.append(torch.from_numpy(b_n).cuda())
+        batch = Q.Batch(systems, precision=Q.PREC_F32, rhs_tile=2, threads=128)
+        xs = [torch.zeros_like(b_) for b_ in bs]
+        for _ in range(2):
+            reps, ms = batch.solve(xs, bs, tol=TOL, precision=Q.PREC_F32)
+        print(json.dumps({"ms": ms, "max_iters": max(r.iters for r in reps),
+                          "certified": all(r.status == Q.OK and r.true_rel_res <= TOL for r in reps)}))
     else:
         lat = Q.S2Trivalent(N_REFINE)
         D = Q.DiracS2Dual(lat, 1.0, M5)
@@ -307,7 +326,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--profile", choices=["apply", "cg", "pcg", "ppcg"], default=None,
+    ap.add_argument("--profile", choices=["apply", "cg", "pcg", "ppcg", "batched"], default=None,
                     help="small self-contained case for ncu: 'apply' = D apply at n=512 (f32, bf16, f64; "
                          "HBM-resident), 'cg' = one n=64 mixed-precision solve, 'pcg' = 300 iterations of the "
                          "n=64 preconditioned solve, 'ppcg' = the same with the pipelined one-barrier kernel")

@@ -94,8 +94,14 @@ __device__ __forceinline__ double* part_ptr(double* base, int parity, int R3) {
   return base + (size_t(parity) * gridDim.x + blockIdx.x) * R3;
 }
 
-template <int P, int R>
-__global__ void __launch_bounds__(256) k_batched_cg(BatchArgs a) {
+// T threads per block.  The scalar state of a system is held per thread, so
+// without a register cap the kernel takes 128 registers and four 128-thread
+// blocks per SM, and the grid-strided site loops are latency bound.  Capping
+// at 64 registers (1024 / T blocks of T threads per SM) for tiles up to 4
+// doubles the resident warps; measured on the 256-RHS multi-lattice batch:
+// 154 ms (tile 1) vs 188 ms for the best uncapped shape.
+template <int P, int R, int T>
+__global__ void __launch_bounds__(T, (R <= 4 ? 1024 / T : 1)) k_batched_cg(BatchArgs a) {
   __shared__ double sh[32 * 3 * R];
   __shared__ double tot[3 * R];
   // ---- my system ----
@@ -524,15 +530,20 @@ __global__ void __launch_bounds__(256) k_batched_cg(BatchArgs a) {
 // host side
 // ---------------------------------------------------------------------------
 template <int P, int R>
+static const void* batch_kernel(int threads) {
+  return threads == 128 ? (const void*)k_batched_cg<P, R, 128> : (const void*)k_batched_cg<P, R, 256>;
+}
+
+template <int P, int R>
 static int launch(BatchArgs& args, int grid, int threads, cudaStream_t st) {
   void* kargs[] = {&args};
-  QED3_CUDA_TRY(cudaLaunchCooperativeKernel((void*)k_batched_cg<P, R>, dim3(grid), dim3(threads), kargs, 0, st));
+  QED3_CUDA_TRY(cudaLaunchCooperativeKernel(batch_kernel<P, R>(threads), dim3(grid), dim3(threads), kargs, 0, st));
   return QED3_OK;
 }
 
 template <int P, int R>
 static int occupancy(int threads, int* per_sm) {
-  QED3_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, k_batched_cg<P, R>, threads, 0));
+  QED3_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, batch_kernel<P, R>(threads), threads, 0));
   return QED3_OK;
 }
 
