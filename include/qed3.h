@@ -53,6 +53,14 @@ typedef struct qed3_lpc_s qed3_lpc;
 /* Message of the last failure on the calling thread ("" if none). */
 const char* qed3_last_error_string(void);
 int qed3_version(void);
+/* Self-test of the bounded device waits every persistent solver relies on:
+ * a two-block launch in which one block never arrives at the grid barriers,
+ * so the other's waits end only by running out after spin_limit polls (both
+ * barrier forms: the register-resident solvers' and the streaming solver's).
+ * Returns QED3_ERR_TIMEOUT when both waits ran out and raised their abort
+ * flags (the expected outcome), QED3_OK otherwise; the CUDA context stays
+ * usable.  No counterpart in the reference. */
+int qed3_selftest_wait_timeout(long long spin_limit, int* timed_out_resident, int* timed_out_streaming);
 
 /* ======================================================================
  * Lattice  --  replaces S2Trivalent(n_refine) (src/both_3d/s2n_dual.h:49-106)

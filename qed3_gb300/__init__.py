@@ -65,6 +65,7 @@ class Qed3Error(RuntimeError):
 SIGNATURES = [
     ("qed3_last_error_string", ctypes.c_char_p, []),
     ("qed3_version", ctypes.c_int, []),
+    ("qed3_selftest_wait_timeout", ctypes.c_int, [ctypes.c_longlong, c_int_p, c_int_p]),
     ("qed3_lattice_create", ctypes.c_int, [ctypes.c_int, ctypes.POINTER(vp)]),
     ("qed3_lattice_destroy", ctypes.c_int, [vp]),
     ("qed3_lattice_sizes", ctypes.c_int, [vp, c_int_p, c_int_p, c_int_p, c_int_p]),
@@ -487,6 +488,13 @@ def point_source(lattice: S2Trivalent, x: int, s: int) -> np.ndarray:
     out = np.zeros(2 * lattice.n_sites, dtype=np.complex128)
     _check(lib().qed3_point_source(lattice.n_sites, x, s, _ptr(out)))
     return out
+
+
+def selftest_wait_timeout(spin_limit: int = 20000):
+    """Run the bounded-wait self-test; returns (status, resident_timed_out, streaming_timed_out)."""
+    a, b = ctypes.c_int(), ctypes.c_int()
+    rc = lib().qed3_selftest_wait_timeout(spin_limit, ctypes.byref(a), ctypes.byref(b))
+    return rc, bool(a.value), bool(b.value)
 
 
 def zolotarev(k: float, n: int) -> dict:

@@ -115,6 +115,12 @@ extern "C" {
 const char* qed3_last_error_string(void) { return g_last_error.c_str(); }
 int qed3_version(void) { return 100; }
 
+int qed3_selftest_wait_timeout(long long spin_limit, int* timed_out_resident, int* timed_out_streaming) {
+  QED3_GUARD_BEGIN
+  return selftest_wait_timeout(spin_limit, timed_out_resident, timed_out_streaming);
+  QED3_GUARD_END
+}
+
 int qed3_lattice_create(int n_refine, qed3_lattice** out) {
   QED3_GUARD_BEGIN
   if (!out) return fail(QED3_ERR_ARG, "out is NULL");

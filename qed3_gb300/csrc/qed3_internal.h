@@ -16,6 +16,7 @@ namespace qed3 {
 // ---------------------------------------------------------------------------
 void set_error(const std::string& msg);
 int fail(int status, const std::string& msg);
+int selftest_wait_timeout(long long spin_limit, int* timed_out_v2, int* timed_out_streaming);
 
 // ---------------------------------------------------------------------------
 // Host lattice: the dual trivalent lattice S2Trivalent of the reference

@@ -217,3 +217,17 @@ def test_cpu_runnable_configuration_n8_on_the_gpu(cuda):
         assert np.linalg.norm(x - xo) / np.linalg.norm(xo) < 1e-8
         if prec == Q.PREC_F64:
             assert abs(rep.iters - it_o) <= 1, (rep.iters, it_o)
+
+
+def test_bounded_waits_run_out_and_the_context_survives(cuda):
+    """Failure detection without a GPU fault: a grid barrier whose partner
+    block never arrives gives up after its poll limit, raises the abort flag
+    and returns an error status; a solve right after works normally."""
+    import torch
+    rc, resident, streaming = Q.selftest_wait_timeout(20000)
+    assert rc == Q.ERR_TIMEOUT and resident and streaming
+    g, lat, Do, Dq, b = _setup(4, 0.1, 123, cuda)
+    bt = to_dev(b, cuda)
+    x = torch.zeros_like(bt)
+    rep = Dq.solve(x, bt, tol=1e-10, precision=Q.PREC_F32)
+    assert rep.status == Q.OK and rep.true_rel_res <= 1e-10
