@@ -90,7 +90,9 @@ int qed3_lattice_permutation(const qed3_lattice* lat, int* perm);
  * configuration is indexed by.  vertices[n_vertices*3] (normalised here),
  * triangles[n_triangles*3] (vertex ids, any winding); dual site t is the
  * circumcentre of triangle t.  links: NULL (lexicographic (i<j) order) or
- * [n_links*2] pairs (i<j) giving the link numbering.  The mesh must be a
+ * [n_links*2] pairs giving the link numbering and orientation: link l points
+ * links[l][0] -> links[l][1] (its angle enters the hop in that direction with
+ * +A, as the reference's map2sign), in either label order.  The mesh must be a
  * closed triangulation of the sphere (every edge in two triangles, one ring
  * of triangles per vertex, V - E + F = 2); QED3_ERR_ARG otherwise. */
 int qed3_lattice_from_mesh(int n_vertices, const double* vertices, int n_triangles, const int* triangles,

@@ -435,16 +435,21 @@ static int build_dual(const std::vector<V3>& vert, const std::vector<int32_t>& t
   return QED3_OK;
 }
 
-// Renumbers the links to a caller's order (each (i < j), a permutation of the
-// lattice's links): every link-indexed table follows.
+// Renumbers and orients the links as a caller lists them (a permutation of
+// the lattice's links, each (i, j) in either order): links[l][0] -> links[l][1]
+// becomes the positive direction of link l (the reference's map2sign,
+// src/both_3d/s2n_dual.h:94-101), so hop and face signs follow the stored
+// orientation and omega of a reversed link changes sign (the same spin
+// connection per hop).  Every link-indexed table follows.
 static int reorder_links(const int32_t* order, HostLattice& L) {
   const int64_t Nl = L.n_links;
   std::map<std::pair<int32_t, int32_t>, int32_t> pos;
   for (int64_t l = 0; l < Nl; l++) pos[{L.links[2 * l], L.links[2 * l + 1]}] = int32_t(l);
   std::vector<int32_t> old_of(size_t(Nl), -1), new_of(size_t(Nl), -1);
+  std::vector<char> flip(size_t(Nl), 0);
   for (int64_t u = 0; u < Nl; u++) {
-    const int32_t i = order[2 * u], j = order[2 * u + 1];
-    if (!(i < j)) return fail(QED3_ERR_ARG, "links: each link must be given as (i, j) with i < j");
+    const int32_t i = std::min(order[2 * u], order[2 * u + 1]), j = std::max(order[2 * u], order[2 * u + 1]);
+    flip[u] = order[2 * u] > order[2 * u + 1];
     const auto it = pos.find({i, j});
     if (it == pos.end()) return fail(QED3_ERR_ARG, "links: (" + std::to_string(i) + ", " + std::to_string(j) +
                                                        ") is not a link of the mesh");
@@ -470,8 +475,18 @@ static int reorder_links(const int32_t* order, HostLattice& L) {
   permute1(L.ell);
   permute1(L.link_volume);
   permute1(L.omega);
+  for (int64_t u = 0; u < Nl; u++)
+    if (flip[u]) {
+      std::swap(L.links[2 * u], L.links[2 * u + 1]);
+      L.omega[u] = -L.omega[u];
+    }
   for (auto& h : L.hop_link) h = new_of[h];
   for (auto& h : L.face_links) h = new_of[h];
+  const int64_t Ns = L.n_sites;
+  for (int64_t x = 0; x < Ns; x++)
+    for (int k = 0; k < 3; k++) L.hop_sign[3 * x + k] = L.links[2 * size_t(L.hop_link[3 * x + k])] == x ? 1 : -1;
+  for (size_t e = 0; e < L.face_sites.size(); e++)
+    L.face_link_sign[e] = L.links[2 * size_t(L.face_links[e])] == L.face_sites[e] ? 1 : -1;
   return QED3_OK;
 }
 

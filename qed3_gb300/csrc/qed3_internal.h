@@ -31,7 +31,7 @@ struct HostLattice {
   std::vector<int32_t> simp_faces;   // [Ns*3]
   std::vector<double> sites;         // [Ns*3]
   std::vector<int32_t> nns;          // [Ns*3], ascending
-  std::vector<int32_t> links;        // [Nl*2], (i<j), lexicographic
+  std::vector<int32_t> links;        // [Nl*2], oriented links[l][0] -> links[l][1]; (i<j) lexicographic unless a caller's order was given
   std::vector<int32_t> simp_links;   // [Nl*2], (min,max)
   std::vector<int32_t> face_offsets; // [Nf+1]
   std::vector<int32_t> face_sites;   // ring of each dual face
@@ -40,10 +40,10 @@ struct HostLattice {
   std::vector<double> omega;         // [Nl], omega(links[l][0], links[l][1])
   std::vector<double> alpha;         // [Ns*3], alpha(x, nns[x][k])
   std::vector<int32_t> hop_link;     // [Ns*3]
-  std::vector<int8_t> hop_sign;      // [Ns*3], +1 if x < y
+  std::vector<int8_t> hop_sign;      // [Ns*3], +1 if the hop x -> y runs along its link's orientation
   std::vector<int8_t> hop_back;      // [Ns*3], slot of x in nns[y]
   std::vector<int32_t> face_links;   // [face_total], link id of (f[i], f[i+1])
-  std::vector<int8_t> face_link_sign;// [face_total], +1 if f[i] < f[i+1]
+  std::vector<int8_t> face_link_sign;// [face_total], +1 if f[i] -> f[i+1] runs along the link's orientation
   // space-filling-curve order used on the device
   std::vector<int32_t> perm;         // internal -> reference
   std::vector<int32_t> iperm;        // reference -> internal

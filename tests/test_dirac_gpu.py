@@ -188,3 +188,39 @@ def test_caller_spin_structure_enters_the_operator(cuda):
     D1.apply(o1, v, Q.OP_D)
     D2.apply(o2, v, Q.OP_D)
     assert float((o1 - o2).abs().max()) < 1e-13 * float(o2.abs().max())
+
+
+def test_oriented_links_give_the_same_operator(cuda):
+    """Reversing the stored orientation of some links and negating their
+    angles is the same gauge field: identical D apply, plaquettes and fermion
+    force up to the links' signs."""
+    import torch
+    lat = Q.S2Trivalent(4)
+    v, t = lat.mesh()
+    a = lat.tables()
+    flip = np.zeros(lat.n_links, bool)
+    flip[1::4] = True
+    links = a["links"].copy()
+    links[flip] = links[flip][:, ::-1]
+    lat2 = Q.S2Trivalent.from_mesh(v, t, links=links)
+    A = np.random.default_rng(8).uniform(-np.pi, np.pi, lat.n_links)
+    A2 = np.where(flip, -A, A)
+    D1, D2 = Q.DiracS2Dual(lat, 1.0, 0.1), Q.DiracS2Dual(lat2, 1.0, 0.1)
+    D1.update(A)
+    D2.update(A2)
+    vt = to_dev(np.random.default_rng(9).normal(size=2 * lat.n_sites) * (1 - 1j), cuda)
+    o1, o2 = torch.zeros_like(vt), torch.zeros_like(vt)
+    D1.apply(o1, vt, Q.OP_D)
+    D2.apply(o2, vt, Q.OP_D)
+    assert float((o1 - o2).abs().max()) < 1e-14 * float(o1.abs().max())
+    th1 = torch.zeros(lat.n_faces, dtype=torch.float64, device=cuda)
+    th2 = torch.zeros_like(th1)
+    Q.plaquette(lat, to_dev(A, cuda), th1)
+    Q.plaquette(lat2, to_dev(A2, cuda), th2)
+    assert float((th1 - th2).abs().max()) < 1e-14
+    F1, F2 = torch.zeros_like(th1[:0]).new_zeros(lat.n_links), torch.zeros(lat.n_links, dtype=torch.float64, device=cuda)
+    eta = vt.clone()
+    Q.fermion_force(D1, eta, F1)
+    Q.fermion_force(D2, eta, F2)
+    sgn = torch.from_numpy(np.where(flip, -1.0, 1.0)).to(cuda)
+    assert float((F1 - sgn * F2).abs().max()) < 1e-13 * float(F1.abs().max())

@@ -1,5 +1,7 @@
 """Product lattice builder vs the oracle: integer tables, coordinates and areas
 bit-exact; the spin connection (closed form vs quadrature) to 1e-14."""
+import os
+
 import numpy as np
 import pytest
 
@@ -156,7 +158,7 @@ def test_bad_meshes_are_errors():
             Q.S2Trivalent.from_mesh(v, tb)
         assert e.value.status == Q.ERR_ARG
     links = lat.tables()["links"].copy()
-    for lb in (links[:, ::-1], np.concatenate([links[:-1], links[:1]])):
+    for lb in (np.concatenate([links[:-1], links[:1]]), np.concatenate([links[:-1], [[0, 0]]])):
         with pytest.raises(Q.Qed3Error) as e:
             Q.S2Trivalent.from_mesh(v, t, links=lb)
         assert e.value.status == Q.ERR_ARG
@@ -176,3 +178,64 @@ def test_caller_spin_structure_is_used():
     bad[3] = np.nan
     with pytest.raises(Q.Qed3Error):
         lat.set_spin_structure(bad)
+
+
+def test_mesh_with_oriented_links():
+    """Links listed (j, i) point j -> i: the tables keep that orientation, omega
+    changes sign, and the hop signs follow the stored direction."""
+    lat = Q.S2Trivalent(3)
+    v, t = lat.mesh()
+    a = lat.tables()
+    flip = np.zeros(lat.n_links, bool)
+    flip[::3] = True
+    links = a["links"].copy()
+    links[flip] = links[flip][:, ::-1]
+    b = Q.S2Trivalent.from_mesh(v, t, links=links).tables()
+    assert np.array_equal(b["links"], links)
+    assert np.array_equal(b["omega"][flip], -a["omega"][flip])
+    assert np.array_equal(b["omega"][~flip], a["omega"][~flip])
+    for k in ("sites", "nns", "face_sites", "ell", "link_volume", "vols", "alpha"):
+        assert np.array_equal(b[k], a[k]), k
+
+
+def test_reference_dat_files_round_trip(tmp_path):
+    """The reference's .dat layout (get_geometry.cc / test_sorting.cc writers,
+    s2n_simp.h / dirac_dual.h readers): write, read back, same lattice."""
+    from qed3_gb300 import dats
+    lat = Q.S2Trivalent(4)
+    paths = dats.write(lat, str(tmp_path))
+    assert len(paths) == 10
+    names = sorted(os.path.basename(p) for p in paths)
+    assert "face_dual_n4.dat" in names and "pts_dual_n4_singlepatch.dat" in names
+    # row shapes as the reference's readers parse them
+    first = open(os.path.join(str(tmp_path), "nns_dual_n4_singlepatch.dat")).readline().split()
+    assert len(first) == 3 and all(s.lstrip("-").isdigit() for s in first)
+    lat2 = dats.read(str(tmp_path), 4)
+    assert lat2.max_site_deviation == 0.0
+    a, b = lat.tables(), lat2.tables()
+    for k in ("sites", "nns", "links", "simp_links", "face_offsets", "face_sites", "ell", "link_volume", "vols"):
+        assert np.array_equal(a[k], b[k]), k
+    assert np.abs(a["omega"] - b["omega"]).max() < 1e-14
+    assert np.abs(a["alpha"] - b["alpha"]).max() < 1e-14
+
+
+def test_reference_dat_files_in_another_numbering(tmp_path):
+    """Files whose sites, vertices and link orientations differ from this
+    project's numbering (a relabelled mesh, some links listed j -> i): the read
+    lattice follows the files."""
+    from qed3_gb300 import dats
+    lat0, v2, t2, pv, pt = _relabelled_mesh(3, 11)
+    links = Q.S2Trivalent.from_mesh(v2, t2).tables()["links"].copy()
+    links[::5] = links[::5][:, ::-1]
+    lat = Q.S2Trivalent.from_mesh(v2, t2, links=links)
+    dats.write(lat, str(tmp_path), n_refine=3)
+    # shuffle the triangle rows of face_n: the reader re-pairs them with pts_dual
+    fp = os.path.join(str(tmp_path), "face_n3_singlepatch.dat")
+    rows = open(fp).readlines()
+    perm = np.random.default_rng(0).permutation(len(rows))
+    open(fp, "w").writelines([rows[i] for i in perm])
+    lat2 = dats.read(str(tmp_path), 3)
+    a, b = lat.tables(), lat2.tables()
+    assert np.abs(a["sites"] - b["sites"]).max() < 1e-15
+    assert np.array_equal(a["links"], b["links"]) and np.array_equal(a["nns"], b["nns"])
+    assert np.abs(a["omega"] - b["omega"]).max() < 1e-14
