@@ -253,6 +253,20 @@ int qed3_fermion_force(qed3_dirac* d, const double* eta, double* F, void* stream
 typedef struct qed3_rng_s qed3_rng;
 int qed3_rng_create(int n_links, int n_sites, int seed, qed3_rng** out);
 int qed3_rng_destroy(qed3_rng* r);
+/* Random-stream checkpoint in the reference's layout (ParallelRngExt::ckpoint
+ * / read, src/both_3d/rng.h:131-168, at Nt = 1): a run saved by either side
+ * continues with identical streams on the other. */
+int qed3_rng_save(const qed3_rng* r, const char* path);
+/* ParallelRng::uniform: one draw of the master engine (the Metropolis test). */
+int qed3_rng_uniform(qed3_rng* r, double* out);
+int qed3_rng_load(qed3_rng* r, const char* path);
+/* Gauge checkpoint in the reference's layout (GaugeExt::ckpoint / read,
+ * src/both_3d/gauge_ext.h:225-275, at Nt = 1): host A[n_links] in this
+ * lattice's link numbering, then n_sites temporal angles (written as zero;
+ * their largest magnitude is reported on load, since this path has no
+ * temporal links). */
+int qed3_links_save(const qed3_lattice* lat, const double* A, const char* path);
+int qed3_links_load(const qed3_lattice* lat, double* A, double* temporal_max_abs, const char* path);
 /* host outputs: links[n_links] = width * N(0,1); spinor[2*n_sites] complex
  * (ParallelRngExt::fill_gaussian, src/both_3d/rng.h:122-129) */
 int qed3_rng_gaussian_links(qed3_rng* r, double width, double* links);

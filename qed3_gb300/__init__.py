@@ -66,6 +66,11 @@ SIGNATURES = [
     ("qed3_last_error_string", ctypes.c_char_p, []),
     ("qed3_version", ctypes.c_int, []),
     ("qed3_selftest_wait_timeout", ctypes.c_int, [ctypes.c_longlong, c_int_p, c_int_p]),
+    ("qed3_rng_uniform", ctypes.c_int, [vp, c_double_p]),
+    ("qed3_rng_save", ctypes.c_int, [vp, ctypes.c_char_p]),
+    ("qed3_rng_load", ctypes.c_int, [vp, ctypes.c_char_p]),
+    ("qed3_links_save", ctypes.c_int, [vp, vp, ctypes.c_char_p]),
+    ("qed3_links_load", ctypes.c_int, [vp, vp, c_double_p, ctypes.c_char_p]),
     ("qed3_lattice_create", ctypes.c_int, [ctypes.c_int, ctypes.POINTER(vp)]),
     ("qed3_lattice_destroy", ctypes.c_int, [vp]),
     ("qed3_lattice_sizes", ctypes.c_int, [vp, c_int_p, c_int_p, c_int_p, c_int_p]),
@@ -399,6 +404,19 @@ class ParallelRng:
         _check(lib().qed3_rng_gaussian_spinor(self._h, _ptr(out)))
         return out
 
+    def uniform(self) -> float:
+        """One master-engine uniform draw (the Metropolis test's)."""
+        u = ctypes.c_double()
+        _check(lib().qed3_rng_uniform(self._h, ctypes.byref(u)))
+        return u.value
+
+    def save(self, path: str):
+        """Checkpoint the streams (the reference's ParallelRngExt::ckpoint layout)."""
+        _check(lib().qed3_rng_save(self._h, os.fsencode(path)))
+
+    def load(self, path: str):
+        _check(lib().qed3_rng_load(self._h, os.fsencode(path)))
+
     def z2_spinor(self) -> np.ndarray:
         """FermionVector::set_random: (z + i z')/sqrt(2 Ns), z from the site engines' dist_z2(1, 2)."""
         out = np.zeros(2 * self.lattice.n_sites, dtype=np.complex128)
@@ -488,6 +506,20 @@ def point_source(lattice: S2Trivalent, x: int, s: int) -> np.ndarray:
     out = np.zeros(2 * lattice.n_sites, dtype=np.complex128)
     _check(lib().qed3_point_source(lattice.n_sites, x, s, _ptr(out)))
     return out
+
+
+def save_links(lattice: S2Trivalent, A, path: str):
+    """Gauge checkpoint in the reference's GaugeExt::ckpoint layout (Nt = 1)."""
+    h = np.ascontiguousarray(A.detach().cpu().numpy() if hasattr(A, "detach") else A, dtype=np.float64)
+    _check(lib().qed3_links_save(lattice.handle, _ptr(h), os.fsencode(path)))
+
+
+def load_links(lattice: S2Trivalent, path: str) -> np.ndarray:
+    """Reads a GaugeExt checkpoint (Nt = 1); returns the host link angles."""
+    A = np.zeros(lattice.n_links)
+    t = ctypes.c_double()
+    _check(lib().qed3_links_load(lattice.handle, _ptr(A), ctypes.byref(t), os.fsencode(path)))
+    return A
 
 
 def selftest_wait_timeout(spin_limit: int = 20000):

@@ -4,7 +4,9 @@
 
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
+#include <cstdio>
 #include <cstring>
 #include <exception>
 #include <new>
@@ -386,6 +388,60 @@ int qed3_rng_create(int n_links, int n_sites, int seed, qed3_rng** out) {
 int qed3_rng_destroy(qed3_rng* r) {
   rng_destroy(r);
   return QED3_OK;
+}
+
+int qed3_rng_uniform(qed3_rng* r, double* out) {
+  if (!r || !out) return fail(QED3_ERR_ARG, "NULL argument");
+  *out = rng_uniform(r);
+  return QED3_OK;
+}
+
+int qed3_rng_save(const qed3_rng* r, const char* path) {
+  QED3_GUARD_BEGIN
+  if (!r || !path) return fail(QED3_ERR_ARG, "NULL argument");
+  return rng_save(r, path);
+  QED3_GUARD_END
+}
+
+int qed3_rng_load(qed3_rng* r, const char* path) {
+  QED3_GUARD_BEGIN
+  if (!r || !path) return fail(QED3_ERR_ARG, "NULL argument");
+  return rng_load(r, path);
+  QED3_GUARD_END
+}
+
+// GaugeExt::ckpoint / read (src/both_3d/gauge_ext.h:225-275) at Nt = 1: raw
+// native-endian doubles, the spatial links [n_links] then the temporal links
+// [n_sites] (zero here: the dual-lattice path has no temporal direction).
+int qed3_links_save(const qed3_lattice* lat, const double* A, const char* path) {
+  QED3_GUARD_BEGIN
+  if (!lat || !A || !path) return fail(QED3_ERR_ARG, "NULL argument");
+  FILE* f = std::fopen(path, "wb");
+  if (!f) return fail(QED3_ERR_ARG, std::string("cannot write ") + path);
+  const size_t nl = size_t(lat->host.n_links), ns = size_t(lat->host.n_sites);
+  std::vector<double> zeros(ns, 0.0);
+  const bool ok = std::fwrite(A, sizeof(double), nl, f) == nl && std::fwrite(zeros.data(), sizeof(double), ns, f) == ns;
+  std::fclose(f);
+  return ok ? QED3_OK : fail(QED3_ERR_ARG, std::string("write failed: ") + path);
+  QED3_GUARD_END
+}
+
+int qed3_links_load(const qed3_lattice* lat, double* A, double* temporal_max_abs, const char* path) {
+  QED3_GUARD_BEGIN
+  if (!lat || !A || !path) return fail(QED3_ERR_ARG, "NULL argument");
+  FILE* f = std::fopen(path, "rb");
+  if (!f) return fail(QED3_ERR_ARG, std::string("cannot read ") + path);
+  const size_t nl = size_t(lat->host.n_links), ns = size_t(lat->host.n_sites);
+  std::vector<double> buf(nl + ns + 1);
+  const size_t got = std::fread(buf.data(), sizeof(double), nl + ns + 1, f);
+  std::fclose(f);
+  if (got != nl + ns) return fail(QED3_ERR_ARG, "not a gauge checkpoint of this lattice (Nt = 1): " + std::string(path));
+  std::memcpy(A, buf.data(), nl * sizeof(double));
+  double mx = 0.0;
+  for (size_t i = 0; i < ns; i++) mx = std::max(mx, std::abs(buf[nl + i]));
+  if (temporal_max_abs) *temporal_max_abs = mx;
+  return QED3_OK;
+  QED3_GUARD_END
 }
 
 int qed3_rng_gaussian_links(qed3_rng* r, double width, double* links) {

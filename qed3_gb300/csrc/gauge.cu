@@ -16,7 +16,10 @@
 
 #include <cmath>
 #include <cstdint>
+#include <fstream>
 #include <functional>
+#include <sstream>
+#include <string>
 #include <random>
 #include <vector>
 
@@ -336,6 +339,61 @@ qed3_rng_s* rng_create(int n_links, int n_sites, int seed) {
   return r;
 }
 void rng_destroy(qed3_rng_s* r) { delete r; }
+
+// Checkpoint in the layout of ParallelRngExt::ckpoint / read
+// (src/both_3d/rng.h:131-168, Nt = 1): the master engine, then every link
+// engine, then every site engine, each as SingleRng's operator<< writes it
+// (src/both_3d/rng.h:23-30): four lines -- the mt19937_64 state, then the
+// normal, uniform-real and uniform-int distribution states, in the standard
+// library's stream format.
+int rng_save(const qed3_rng_s* r, const char* path) {
+  std::ofstream os(path);
+  if (!os) return fail(QED3_ERR_ARG, std::string("cannot write ") + path);
+  auto put = [&](const RngEngine& e) {
+    os << e.mt << std::endl;
+    os << e.g << std::endl;
+    os << e.u << std::endl;
+    os << e.z2 << std::endl;
+  };
+  put(r->r.master);
+  for (const auto& e : r->r.links) put(e);
+  for (const auto& e : r->r.sites) put(e);
+  if (!os) return fail(QED3_ERR_ARG, std::string("write failed: ") + path);
+  return QED3_OK;
+}
+
+int rng_load(qed3_rng_s* r, const char* path) {
+  std::ifstream is(path);
+  if (!is) return fail(QED3_ERR_ARG, std::string("cannot read ") + path);
+  HostRng tmp;
+  tmp.links.resize(r->r.links.size());
+  tmp.sites.resize(r->r.sites.size());
+  auto get = [&](RngEngine& e) -> bool {
+    std::string line;
+    std::istringstream ss;
+    if (!std::getline(is, line)) return false;
+    ss.str(line);
+    if (!(ss >> e.mt)) return false;
+    if (!std::getline(is, line)) return false;
+    ss.clear();
+    ss.str(line);
+    if (!(ss >> e.g)) return false;
+    if (!std::getline(is, line)) return false;
+    ss.clear();
+    ss.str(line);
+    if (!(ss >> e.u)) return false;
+    if (!std::getline(is, line)) return false;
+    ss.clear();
+    ss.str(line);
+    return bool(ss >> e.z2);
+  };
+  bool ok = get(tmp.master);
+  for (auto& e : tmp.links) ok = ok && get(e);
+  for (auto& e : tmp.sites) ok = ok && get(e);
+  if (!ok) return fail(QED3_ERR_ARG, std::string("not a random-stream checkpoint of this size: ") + path);
+  r->r = std::move(tmp);
+  return QED3_OK;
+}
 void rng_gaussian_links(qed3_rng_s* r, double width, double* out) {
   for (size_t l = 0; l < r->r.links.size(); l++) out[l] = width * r->r.links[l].g(r->r.links[l].mt);
 }

@@ -21,6 +21,8 @@ void rng_destroy(qed3_rng_s* r);
 void rng_gaussian_links(qed3_rng_s* r, double width, double* out);
 void rng_gaussian_spinor(qed3_rng_s* r, double* out);
 double rng_uniform(qed3_rng_s* r);
+int rng_save(const qed3_rng_s* r, const char* path);
+int rng_load(qed3_rng_s* r, const char* path);
 void rng_z2_spinor(qed3_rng_s* r, double* out);
 int hmc_fermion(qed3_lattice_s* lat, qed3_dirac_s* d, qed3_rng_s* rng, double* A, double beta, int compact, int exact,
                 double tmax, int nsteps, int nsteps_inner, int npf, int integrator, double tol, int prec, int no_reject,

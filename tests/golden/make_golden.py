@@ -18,6 +18,12 @@ angles and average plaquette (src/both/gauge.h), U1Wilson action and force
 (faces, dual-face areas, link orientation) for n = 2 and 4, compact and
 non-compact.
 
+rng_ckpoint_ref.txt / rng_ckpoint_ref.json: a checkpoint written by the
+REFERENCE's ParallelRngExt::ckpoint (src/both_3d/rng.h:131-168, Nt = 1; built
+in place by `make -C oracle ref` into oracle/_ref/librng3d_ref.so) after one
+sweep of link and site Gaussians and three master uniforms (3 links, 2 sites,
+seed 5), and the reference's continuation draws after it.
+
 free_spectrum.json: the known answers of analysis/ev_dual.ipynb (cells 33-34),
 typed in from the notebook's output cells.
 """
@@ -107,6 +113,22 @@ def gauge_fixture():
                        cases=out), f, indent=0)
 
 
+def rng_ckpoint_fixture():
+    subprocess.check_call(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "ref"])
+    L = ctypes.CDLL(os.path.join(ROOT, "oracle", "_ref", "librng3d_ref.so"))
+    nl, ns, seed = 3, 2, 5
+    cont = np.zeros(nl + 4 * ns + 2 + 4 * ns)
+    path = os.path.join(HERE, "rng_ckpoint_ref.txt")
+    dp = ctypes.POINTER(ctypes.c_double)
+    L.ref_rng3d_run(nl, ns, seed, path.encode(), None, cont.ctypes.data_as(dp), None)
+    with open(os.path.join(HERE, "rng_ckpoint_ref.json"), "w") as f:
+        json.dump(dict(source="reference src/both_3d/rng.h ParallelRngExt<.,1>::ckpoint compiled by oracle/Makefile "
+                              "`ref`; draws before: links, 4 x sites, 3 uniforms; after: links, 4 x sites, "
+                              "2 uniforms, 4 x sites z2",
+                       n_links=nl, n_sites=ns, seed=seed, continuation=[float.hex(float(v)) for v in cont]), f,
+                  indent=0)
+
+
 def spectrum_fixture():
     data = dict(source="analysis/ev_dual.ipynb cells 33-34: [n, |Im lambda| (j=3/2), |Im lambda| (j=1/2)]",
                 rows=[[2, 1.89453, 0.995597], [4, 1.97081, 0.997657], [6, 1.98474, 0.998488],
@@ -119,4 +141,5 @@ if __name__ == "__main__":
     zolotarev_fixture()
     rng_fixture()
     gauge_fixture()
+    rng_ckpoint_fixture()
     spectrum_fixture()

@@ -3,6 +3,8 @@ import os
 import re
 import subprocess
 
+import pytest
+
 import qed3_gb300 as Q
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
@@ -71,3 +73,80 @@ def test_header_is_plain_c_and_c_plus_plus(tmp_path):
             n_links, n_sites = 3, 1
         assert float(f[8]) == O.Rng(Sizes(), 7).gaussian_links(1.0)[0]
         assert out[1] == "message"
+
+
+def test_rng_checkpoint_is_the_references(tmp_path):
+    """A random-stream checkpoint written by the library after the same draws
+    is byte-identical to the reference's ParallelRngExt::ckpoint file
+    (tests/golden/rng_ckpoint_ref.txt), and loading the reference's file
+    continues with the reference's draws."""
+    import ctypes
+    import json
+
+    import numpy as np
+    L = Q.lib()
+    gold = json.load(open(os.path.join(ROOT, "tests", "golden", "rng_ckpoint_ref.json")))
+    nl, ns, seed = gold["n_links"], gold["n_sites"], gold["seed"]
+    cont = np.array([float.fromhex(s) for s in gold["continuation"]])
+
+    def new(seed_):
+        h = ctypes.c_void_p()
+        assert L.qed3_rng_create(nl, ns, seed_, ctypes.byref(h)) == Q.OK
+        return h
+
+    def draws(h, nu, z2):
+        links = np.zeros(nl)
+        L.qed3_rng_gaussian_links(h, 1.0, links.ctypes.data_as(ctypes.c_void_p))
+        sp = np.zeros(4 * ns)
+        L.qed3_rng_gaussian_spinor(h, sp.ctypes.data_as(ctypes.c_void_p))
+        out = [links, sp * np.sqrt(2.0)]
+        u = ctypes.c_double()
+        us = []
+        for _ in range(nu):
+            L.qed3_rng_uniform(h, ctypes.byref(u))
+            us.append(u.value)
+        out.append(np.array(us))
+        if z2:
+            zz = np.zeros(4 * ns)
+            L.qed3_rng_z2_spinor(h, zz.ctypes.data_as(ctypes.c_void_p))
+            out.append(np.rint(zz * np.sqrt(2.0 * ns)))
+        return np.concatenate(out)
+
+    h = new(seed)
+    draws(h, 3, False)
+    path = str(tmp_path / "ckpoint_rng")
+    assert L.qed3_rng_save(h, path.encode()) == Q.OK
+    assert open(path, "rb").read() == open(os.path.join(ROOT, "tests", "golden", "rng_ckpoint_ref.txt"), "rb").read()
+    mine = draws(h, 2, True)
+    h2 = new(seed + 1)
+    assert L.qed3_rng_load(h2, os.path.join(ROOT, "tests", "golden", "rng_ckpoint_ref.txt").encode()) == Q.OK
+    loaded = draws(h2, 2, True)
+    k = nl + 4 * ns
+    # the spinor draws are compared after undoing the 1/sqrt(2) scaling
+    assert np.array_equal(mine[:nl], cont[:nl]) and np.array_equal(loaded[:nl], cont[:nl])
+    assert np.allclose(mine[nl:k], cont[nl:k], rtol=0, atol=4e-16) and np.allclose(loaded[nl:k], cont[nl:k],
+                                                                                 rtol=0, atol=4e-16)
+    assert np.array_equal(mine[k:], cont[k:]) and np.array_equal(loaded[k:], cont[k:])
+    for hh in (h, h2):
+        L.qed3_rng_destroy(hh)
+    bad = str(tmp_path / "short")
+    open(bad, "w").write("1 2 3\n")
+    h3 = new(1)
+    assert L.qed3_rng_load(h3, bad.encode()) == Q.ERR_ARG
+    L.qed3_rng_destroy(h3)
+
+
+def test_gauge_checkpoint_layout(tmp_path):
+    """GaugeExt::ckpoint layout at Nt = 1: n_links spatial doubles, then
+    n_sites temporal doubles; load returns the spatial angles."""
+    import numpy as np
+    lat = Q.S2Trivalent(3)
+    A = np.random.default_rng(4).uniform(-np.pi, np.pi, lat.n_links)
+    p = str(tmp_path / "ckpoint_lat")
+    Q.save_links(lat, A, p)
+    raw = np.fromfile(p, dtype=np.float64)
+    assert raw.size == lat.n_links + lat.n_sites
+    assert np.array_equal(raw[:lat.n_links], A) and not raw[lat.n_links:].any()
+    assert np.array_equal(Q.load_links(lat, p), A)
+    with pytest.raises(Q.Qed3Error):
+        Q.load_links(Q.S2Trivalent(2), p)
