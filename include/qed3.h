@@ -168,6 +168,16 @@ int qed3_cg_solve(qed3_dirac* d, double* x, const double* b, const qed3_solve_pa
                   qed3_solve_report* report, void* stream);
 int qed3_solver_last_report(qed3_dirac* d, qed3_solve_report* report);
 
+/* Extremal eigenvalues of D^dag D by FP64 Lanczos on the device -- an
+ * alternative to the power / inverse-power iterations of
+ * Overlap::compute_lambda_max (src/both_3d/overlap.h:217-306) that needs no
+ * solves.  Stops when both extremal Ritz values change by less than tol
+ * (relative) over two checks ten steps apart; returns QED3_ERR_NOCONV (with
+ * the last estimates) after maxsteps.  Ritz values lie inside the spectrum:
+ * lambda_min is approached from above, lambda_max from below. */
+int qed3_dirac_spectral_bounds(qed3_dirac* d, double tol, int maxsteps, double* lambda_min, double* lambda_max,
+                               int* steps, void* stream);
+
 /* BiCGStab with restarts  --  replaces MatPoly::bicgstab
  * (src/dual/matpoly.h:366-479), which the reference keeps for experiments.
  * Solves (op + shift) x = b for op = QED3_OP_D, _DDAG or _DDAGD (device

@@ -90,6 +90,8 @@ SIGNATURES = [
     ("qed3_dirac_apply_field", ctypes.c_int, [vp, ctypes.c_int, ctypes.c_int, vp, vp, ctypes.c_int, vp]),
     ("qed3_cg_solve", ctypes.c_int, [vp, vp, vp, ctypes.POINTER(SolveParams), ctypes.POINTER(SolveReport), vp]),
     ("qed3_solver_last_report", ctypes.c_int, [vp, ctypes.POINTER(SolveReport)]),
+    ("qed3_dirac_spectral_bounds", ctypes.c_int, [vp, ctypes.c_double, ctypes.c_int, c_double_p, c_double_p,
+                                                  c_int_p, vp]),
     ("qed3_bicgstab_solve", ctypes.c_int, [vp, ctypes.c_int, vp, vp, ctypes.POINTER(SolveParams), ctypes.c_double,
                                            ctypes.POINTER(SolveReport), vp]),
     ("qed3_cg_solve_noalloc", ctypes.c_int, [vp, vp, vp, ctypes.POINTER(SolveParams), ctypes.POINTER(SolveReport),
@@ -332,6 +334,15 @@ class DiracS2Dual:
         if rc not in (OK, ERR_NOCONV):
             _check(rc)
         return Report(r.status, r.iters, r.reliable_updates, r.true_rel_res, r.ms)
+
+    def spectral_bounds(self, tol: float = 1e-10, maxsteps: int = 20000, stream=None):
+        """Extremal eigenvalues of D^dag D by device Lanczos: (lambda_min, lambda_max, steps, converged)."""
+        lo, hi, st = ctypes.c_double(), ctypes.c_double(), ctypes.c_int()
+        rc = lib().qed3_dirac_spectral_bounds(self._h, tol, maxsteps, ctypes.byref(lo), ctypes.byref(hi),
+                                              ctypes.byref(st), _stream(stream))
+        if rc not in (OK, ERR_NOCONV):
+            _check(rc)
+        return lo.value, hi.value, st.value, rc == OK
 
     def bicgstab(self, x, b, op: int = OP_D, tol: float = 1e-10, maxiter: int = 100000, shift: float = 0.0,
                  eps: float = 1e-8, stream=None) -> Report:
@@ -628,6 +639,14 @@ class Overlap:
         h = vp()
         _check(lib().qed3_overlap_create(dirac.handle, order, precision, ctypes.byref(h)))
         self._h = h
+
+    def update_lanczos(self, tol: float = 1e-10, margin: float = 1e-6, maxsteps: int = 20000, stream=None):
+        """Spectral bounds from device Lanczos on D^dag D (no solves), widened by
+        `margin` (relative) on each side, then the Zolotarev update."""
+        lo, hi, steps, ok = self.dirac.spectral_bounds(tol, maxsteps, stream)
+        if not ok:
+            raise Qed3Error(ERR_NOCONV, f"Lanczos did not converge in {steps} steps")
+        return self.update(np.sqrt(lo) * (1.0 - margin), np.sqrt(hi) * (1.0 + margin), stream=stream)
 
     def update(self, lambda_min: float = 0.0, lambda_max: float = 0.0, tol_outer: float = 1e-8, stream=None):
         _check(lib().qed3_overlap_update(self._h, lambda_min, lambda_max, tol_outer, _stream(stream)))

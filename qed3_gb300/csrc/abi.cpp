@@ -343,6 +343,14 @@ int qed3_bicgstab_solve(qed3_dirac* d, int op, double* x, const double* b, const
   QED3_GUARD_END
 }
 
+int qed3_dirac_spectral_bounds(qed3_dirac* d, double tol, int maxsteps, double* lambda_min, double* lambda_max,
+                               int* steps, void* stream) {
+  QED3_GUARD_BEGIN
+  if (!d || !lambda_min || !lambda_max) return fail(QED3_ERR_ARG, "NULL argument");
+  return spectral_bounds(d, tol, maxsteps, lambda_min, lambda_max, steps, (cudaStream_t)stream);
+  QED3_GUARD_END
+}
+
 int qed3_solver_last_report(qed3_dirac* d, qed3_solve_report* report) {
   if (!d || !report) return fail(QED3_ERR_ARG, "NULL argument");
   *report = d->last;

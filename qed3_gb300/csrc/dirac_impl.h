@@ -32,6 +32,8 @@ int solver_free(qed3_dirac_s* d);
 // epilogue of the persistent solvers: report, export of the solution
 int ensure_work(qed3_dirac_s* d);
 int cg_finish(qed3_dirac_s* d, double* x, qed3_solve_report* rep, cudaStream_t st);
+int spectral_bounds(qed3_dirac_s* d, double tol, int maxsteps, double* lmin, double* lmax, int* steps_used,
+                    cudaStream_t st);
 int bicgstab_solve(qed3_dirac_s* d, int op, double* x, const double* b, const qed3_solve_params* prm, double eps,
                    qed3_solve_report* rep, cudaStream_t st);
 int cg_solve_noalloc(qed3_dirac_s* d, double* x, const double* b, const qed3_solve_params* prm,

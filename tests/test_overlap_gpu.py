@@ -241,3 +241,19 @@ def test_overlap_hmc_recomputed_bounds(cuda):
     after = ov.update(tol_outer=1e-12)
     assert abs(before["lambda_max"] / after["lambda_max"] - 1) < 1e-6
     assert abs(before["lambda_min"] / after["lambda_min"] - 1) < 1e-4
+
+
+@pytest.mark.parametrize("M5", [0.1, -1.0])
+def test_lanczos_spectral_bounds_against_dense(cuda, M5):
+    """Device Lanczos on D^dag D (no solves): the extremal eigenvalues of a
+    dense FP64 eigendecomposition at n=4 to 1e-9, approached from inside, and
+    bounds that enclose the power-iteration estimate's range."""
+    rng, g, lat, Do, Dq = _setup(4, M5, 80)
+    w = np.linalg.eigvalsh((lambda M: M.conj().T @ M)(Do.dense()))
+    lo, hi, steps, ok = Dq.spectral_bounds(tol=1e-12)
+    assert ok and steps < 5000
+    assert lo >= w[0] * (1 - 1e-12) and hi <= w[-1] * (1 + 1e-12)
+    assert abs(lo / w[0] - 1) < 1e-9 and abs(hi / w[-1] - 1) < 1e-9
+    ov = Q.Overlap(Dq, 21, Q.PREC_F32)
+    info = ov.update_lanczos(tol=1e-12)
+    assert info["lambda_min"] <= np.sqrt(w[0]) and info["lambda_max"] >= np.sqrt(w[-1])
