@@ -172,7 +172,8 @@ int qed3_solver_last_report(qed3_dirac* d, qed3_solve_report* report);
  * alternative to the power / inverse-power iterations of
  * Overlap::compute_lambda_max (src/both_3d/overlap.h:217-306) that needs no
  * solves.  Stops when both extremal Ritz values change by less than tol
- * (relative) over two checks ten steps apart; returns QED3_ERR_NOCONV (with
+ * (relative) over two consecutive checks (every max(10, m/16) steps at step
+ * m); returns QED3_ERR_NOCONV (with
  * the last estimates) after maxsteps.  Ritz values lie inside the spectrum:
  * lambda_min is approached from above, lambda_max from below. */
 int qed3_dirac_spectral_bounds(qed3_dirac* d, double tol, int maxsteps, double* lambda_min, double* lambda_max,

@@ -41,7 +41,7 @@ static double tridiag_eig(const std::vector<double>& a, const std::vector<double
     lo = std::min(lo, a[i] - r);
     hi = std::max(hi, a[i] + r);
   }
-  for (int it = 0; it < 200 && hi - lo > 1e-16 * std::max(std::abs(lo), std::abs(hi)); it++) {
+  for (int it = 0; it < 72 && hi - lo > 1e-16 * std::max(std::abs(lo), std::abs(hi)); it++) {
     const double mid = 0.5 * (lo + hi);
     if (sturm_count(a, b, m, mid) > k) hi = mid;
     else lo = mid;
@@ -72,7 +72,7 @@ int spectral_bounds(qed3_dirac_s* d, double tol, int maxsteps, double* lmin, dou
     if ((e = vec_axpby(nd, 1.0 / std::sqrt(re), v1, 0.0, v1, v1, st))) return e;
     std::vector<double> al, be;
     double prev_min = 0, prev_max = 0, beta = 0;
-    int j = 0, conv = 0;
+    int j = 0, conv = 0, next_check = 10;
     for (; j < maxsteps; j++) {
       if ((e = dirac_apply_ref(d, QED3_OP_DDAGD, w, v1, st))) return e;
       if (j > 0 && (e = vec_axpby(nd, -beta, v0, 1.0, w, w, st))) return e;
@@ -83,7 +83,9 @@ int spectral_bounds(qed3_dirac_s* d, double tol, int maxsteps, double* lmin, dou
       al.push_back(alpha);
       beta = std::sqrt(std::max(re, 0.0));
       const int m = int(al.size());
-      if (m >= 4 && (m % 10 == 0 || beta == 0.0)) {
+      // Ritz values every max(10, m/16) steps: the bisections cost O(m) each
+      if (m >= 4 && (m >= next_check || beta == 0.0)) {
+        next_check = m + std::max(10, m / 16);
         const double tmin = tridiag_eig(al, be, m, 0), tmax = tridiag_eig(al, be, m, m - 1);
         if (std::abs(tmin - prev_min) <= tol * std::abs(tmin) && std::abs(tmax - prev_max) <= tol * std::abs(tmax))
           conv++;
