@@ -206,6 +206,26 @@ int qed3_cg_solve_noalloc(qed3_dirac* d, double* x, const double* b, const qed3_
                           qed3_solve_report* report, void* stream);
 
 /* ======================================================================
+ * S^2 x S^1: Nt time slices  --  replaces DiracExt<Lattice, DiracS2Dual>
+ * (src/both_3d/dirac_ext.h:6-334) for Nt > 1: per slice the dual-lattice
+ * hops with that slice's link angles, spin-diagonal temporal hops with
+ * kappa_t = (triangle area) / mean_ell / at and antiperiodic time boundary,
+ * diagonal M5 + sum r kappa / 2 + r kappa_t.  Vectors: complex128
+ * [Nt][Ns][2] (index Nx s + 2 x + spin, Nx = 2 Ns); link angles on the
+ * device: A[Nt][n_links] spatial, then A[Nt][n_sites] temporal (GaugeExt).
+ * At Nt = 1 it is the dual-lattice operator.
+ * ====================================================================== */
+typedef struct qed3_dirac_ext_s qed3_dirac_ext;
+int qed3_dirac_ext_create(qed3_lattice* lat, double r, double M5, int Nt, double at, qed3_dirac_ext** out);
+int qed3_dirac_ext_destroy(qed3_dirac_ext* e);
+int qed3_dirac_ext_set_links(qed3_dirac_ext* e, const double* A, void* stream);
+/* op: QED3_OP_D, _DDAG, _DDAGD, _DDDAG; in may equal out for D and D^dag */
+int qed3_dirac_ext_apply(qed3_dirac_ext* e, int op, double* out, const double* in, void* stream);
+/* MatPoly::solve on D^dag D (+ params->shift) in FP64, certified by the true residual */
+int qed3_dirac_ext_cg_solve(qed3_dirac_ext* e, double* x, const double* b, const qed3_solve_params* params,
+                            qed3_solve_report* report, void* stream);
+
+/* ======================================================================
  * Batched solves in ONE persistent launch  --  replaces the reference's
  * loops of MatPoly::solve over pseudofermions and Zolotarev poles on OpenMP
  * threads and CUDA streams (src/both_3d/overlap.h:309-332,

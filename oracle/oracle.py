@@ -472,3 +472,54 @@ def hmc_overlap(geom: Geometry, dirac: "Dirac", rng: "Rng", A: np.ndarray, beta:
     A[:] = A0
     update()
     return False, dH, its[0]
+
+
+def triangle_areas(geom: Geometry) -> np.ndarray:
+    """S2Simp::vols (src/both_3d/s2n_simp.h:234-253): L'Huilier area of the
+    simplicial triangle of each dual site (the three dual faces containing it)."""
+    tri = [[] for _ in range(geom.n_sites)]
+    for f in range(geom.n_faces):
+        for x in geom.face_sites[geom.face_offsets[f]:geom.face_offsets[f + 1]]:
+            tri[x].append(f)
+    out = np.zeros(geom.n_sites)
+    for t, (i0, i1, i2) in enumerate(tri):
+        x0, x1, x2 = geom.simp_sites[i0], geom.simp_sites[i1], geom.simp_sites[i2]
+        a, b, c = np.arccos(x0 @ x1), np.arccos(x1 @ x2), np.arccos(x2 @ x0)
+        s = 0.5 * (a + b + c)
+        out[t] = 4.0 * np.arctan(np.sqrt(np.tan(0.5 * s) * np.tan(0.5 * (s - a)) * np.tan(0.5 * (s - b))
+                                         * np.tan(0.5 * (s - c))))
+    return out
+
+
+def dirac_ext_apply(geom: Geometry, r: float, M5: float, Nt: int, at: float, A: np.ndarray, v: np.ndarray,
+                    op: int = 0) -> np.ndarray:
+    """DiracExt::coo_format (src/both_3d/dirac_ext.h:121-213) restated as an apply:
+    op 0 = D, 1 = D^dag, 2 = D^dag D on v[Nt][Ns][2]; A = spatial [Nt][Nl] then
+    temporal [Nt][Ns].  The spatial part of each slice is the dual-lattice
+    operator of that slice's links (Dirac.apply); kappa_t = area / mean_ell / at."""
+    if op == 2:
+        return dirac_ext_apply(geom, r, M5, Nt, at, A, dirac_ext_apply(geom, r, M5, Nt, at, A, v, 0), 1)
+    Ns, Nl = geom.n_sites, geom.n_links
+    v = np.asarray(v, np.complex128).reshape(Nt, Ns, 2)
+    As = np.asarray(A[:Nt * Nl]).reshape(Nt, Nl)
+    At = np.asarray(A[Nt * Nl:Nt * (Nl + Ns)]).reshape(Nt, Ns)
+    kt = triangle_areas(geom) / geom.mean_ell / at if Nt != 1 else np.zeros(Ns)
+    D = Dirac(geom, r, M5)
+    out = np.zeros_like(v)
+    for s in range(Nt):
+        D.update(As[s])
+        out[s] = D.apply(v[s].reshape(-1), op).reshape(Ns, 2) + (r * kt)[:, None] * v[s]
+    if Nt > 1:
+        sig3 = np.array([1.0, -1.0])
+        for s in range(Nt):  # the COO entries of column slice s
+            sP = -1.0 if s == Nt - 1 else 1.0
+            sM = -1.0 if s == 0 else 1.0
+            tmpP = 0.5 * sP * kt[:, None] * (-r - sig3)[None, :] * np.exp(-1j * At[s])[:, None]
+            tmpM = 0.5 * sM * kt[:, None] * (-r + sig3)[None, :] * np.exp(1j * At[(s - 1) % Nt])[:, None]
+            up, dn = (s + 1) % Nt, (s - 1) % Nt
+            if op == 0:  # D[(x,s+1),(x,s)] = tmpP(s), D[(x,s-1),(x,s)] = tmpM(s)
+                out[up] += tmpP * v[s]
+                out[dn] += tmpM * v[s]
+            else:  # D^dag[(x,s),(x,s+1)] = conj(tmpP(s)), D^dag[(x,s),(x,s-1)] = conj(tmpM(s))
+                out[s] += np.conj(tmpP) * v[up] + np.conj(tmpM) * v[dn]
+    return out.reshape(-1)

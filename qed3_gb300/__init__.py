@@ -128,6 +128,13 @@ SIGNATURES = [
                                           ctypes.POINTER(SolveReport), vp]),
     ("qed3_multishift_solve", ctypes.c_int, [vp, ctypes.c_int, vp, vp, vp, ctypes.c_double, ctypes.c_int, vp,
                                              ctypes.POINTER(ctypes.c_float), vp]),
+    ("qed3_dirac_ext_create", ctypes.c_int, [vp, ctypes.c_double, ctypes.c_double, ctypes.c_int, ctypes.c_double,
+                                             ctypes.POINTER(vp)]),
+    ("qed3_dirac_ext_destroy", ctypes.c_int, [vp]),
+    ("qed3_dirac_ext_set_links", ctypes.c_int, [vp, vp, vp]),
+    ("qed3_dirac_ext_apply", ctypes.c_int, [vp, ctypes.c_int, vp, vp, vp]),
+    ("qed3_dirac_ext_cg_solve", ctypes.c_int, [vp, vp, vp, ctypes.POINTER(SolveParams), ctypes.POINTER(SolveReport),
+                                               vp]),
     ("qed3_batch_create", ctypes.c_int, [ctypes.c_int, vp, vp, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                          ctypes.POINTER(vp)]),
     ("qed3_batch_destroy", ctypes.c_int, [vp]),
@@ -552,6 +559,39 @@ def zolotarev(k: float, n: int) -> dict:
 # ---------------------------------------------------------------------------
 # batched persistent solver
 # ---------------------------------------------------------------------------
+class DiracExt:
+    """S^2 x S^1 Wilson-Dirac operator with Nt time slices (DiracExt, src/both_3d/dirac_ext.h:6-334).
+
+    Vectors: device complex128 of Nt * 2 * n_sites (slice-major); links: device
+    float64 [Nt * n_links spatial, then Nt * n_sites temporal]."""
+
+    def __init__(self, lattice: S2Trivalent, r: float = 1.0, M5: float = 0.0, Nt: int = 1, at: float = 1.0):
+        self.lattice, self.r, self.M5, self.Nt, self.at = lattice, r, M5, Nt, at
+        self.N = 2 * lattice.n_sites * Nt
+        h = vp()
+        _check(lib().qed3_dirac_ext_create(lattice.handle, r, M5, Nt, at, ctypes.byref(h)))
+        self._h = h
+
+    def update(self, A, stream=None):
+        _check(lib().qed3_dirac_ext_set_links(self._h, _ptr(A), _stream(stream)))
+
+    def apply(self, out, inp, op: int = OP_D, stream=None):
+        _check(lib().qed3_dirac_ext_apply(self._h, op, _ptr(out), _ptr(inp), _stream(stream)))
+        return out
+
+    def solve(self, x, b, tol: float = 1e-10, maxiter: int = 100000, shift: float = 0.0, stream=None) -> Report:
+        p = SolveParams(tol, maxiter, PREC_F64, 0.1, shift, 0)
+        r = SolveReport()
+        _check(lib().qed3_dirac_ext_cg_solve(self._h, _ptr(x), _ptr(b), ctypes.byref(p), ctypes.byref(r),
+                                             _stream(stream)))
+        return Report(r.status, r.iters, r.reliable_updates, r.true_rel_res, r.ms)
+
+    def __del__(self):
+        if getattr(self, "_h", None) and _lib is not None:
+            _lib.qed3_dirac_ext_destroy(self._h)
+            self._h = None
+
+
 class Batch:
     """Several CG systems (lattices, right-hand sides, shifts) in one persistent launch.
 

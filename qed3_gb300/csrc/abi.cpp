@@ -19,6 +19,7 @@
 #include "handles.h"
 #include "lpc_impl.h"
 #include "mshift_impl.h"
+#include "ext_impl.h"
 #include "overlap_impl.h"
 #include "pcg_impl.h"
 #include "qed3_internal.h"
@@ -253,6 +254,60 @@ int qed3_dirac_create(qed3_lattice* lat, double r, double M5, qed3_dirac** out) 
   }
   *out = d;
   return QED3_OK;
+  QED3_GUARD_END
+}
+
+int qed3_dirac_ext_create(qed3_lattice* lat, double r, double M5, int Nt, double at, qed3_dirac_ext** out) {
+  QED3_GUARD_BEGIN
+  if (!lat || !out) return fail(QED3_ERR_ARG, "NULL argument");
+  if (Nt < 1 || Nt > 4096 || !(at > 0)) return fail(QED3_ERR_ARG, "need 1 <= Nt <= 4096 and at > 0");
+  *out = nullptr;
+  qed3_dirac* d2 = nullptr;
+  int rc = qed3_dirac_create(lat, r, M5, &d2);
+  if (rc) return rc;
+  auto* e = new qed3_dirac_ext_s;
+  e->d2 = d2;
+  e->Nt = Nt;
+  e->at = at;
+  e->r = r;
+  if ((rc = ext_init(e))) {
+    ext_free(e);
+    qed3_dirac_destroy(d2);
+    delete e;
+    return rc;
+  }
+  *out = e;
+  return QED3_OK;
+  QED3_GUARD_END
+}
+
+int qed3_dirac_ext_destroy(qed3_dirac_ext* e) {
+  if (!e) return QED3_OK;
+  ext_free(e);
+  qed3_dirac_destroy(e->d2);
+  delete e;
+  return QED3_OK;
+}
+
+int qed3_dirac_ext_set_links(qed3_dirac_ext* e, const double* A, void* stream) {
+  QED3_GUARD_BEGIN
+  if (!e || !A) return fail(QED3_ERR_ARG, "NULL argument");
+  return ext_set_links(e, A, (cudaStream_t)stream);
+  QED3_GUARD_END
+}
+
+int qed3_dirac_ext_apply(qed3_dirac_ext* e, int op, double* out, const double* in, void* stream) {
+  QED3_GUARD_BEGIN
+  if (!e || !out || !in) return fail(QED3_ERR_ARG, "NULL argument");
+  return ext_apply(e, op, out, in, (cudaStream_t)stream);
+  QED3_GUARD_END
+}
+
+int qed3_dirac_ext_cg_solve(qed3_dirac_ext* e, double* x, const double* b, const qed3_solve_params* params,
+                            qed3_solve_report* report, void* stream) {
+  QED3_GUARD_BEGIN
+  if (!e || !x || !b) return fail(QED3_ERR_ARG, "NULL argument");
+  return ext_cg(e, x, b, params, report, (cudaStream_t)stream);
   QED3_GUARD_END
 }
 

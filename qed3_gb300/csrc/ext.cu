@@ -1,0 +1,254 @@
+// The S^2 x S^1 operator: Nt time slices of the dual lattice, DiracExt
+// (src/both_3d/dirac_ext.h:6-334).  Per time slice s the spatial hops are the
+// dual-lattice blocks with that slice's link angles,
+//     0.5 kappa_l (-r + gamma(x,y)) e^{i A_s(x,y)} Omega(x,y)        (:135-150),
+// the temporal hops between (x, s) and (x, s +- 1) are spin-diagonal,
+//     D[(x,s+1),(x,s)] = 0.5 sP kappa_t[x] (-r - sigma3) e^{-i A_t(s,x)},
+//     D[(x,s-1),(x,s)] = 0.5 sM kappa_t[x] (-r + sigma3) e^{+i A_t(s-1,x)}
+// (:156-184) with the antiperiodic signs sP = -1 at s = Nt-1, sM = -1 at s = 0,
+// and the diagonal is M5 + sum_l r kappa_l / 2 + r kappa_t[x] (:188-205) with
+// kappa_t[x] = (area of the triangle of x) / mean_ell / at, zero at Nt = 1
+// (:297-305).  Vectors are the reference's: index Nx s + 2 x + spin, Nx = 2 Ns.
+// Link angles: A[Nt][Nl] spatial then A[Nt][Ns] temporal (GaugeExt's layout).
+//
+// Spatial blocks per slice are formed once per link update; the apply is one
+// kernel per operator (a thread per site and slice).  CG on D^dag D is the
+// reference's MatPoly::solve recurrence in FP64 with device BLAS.
+
+#include <cmath>
+#include <vector>
+
+#include "blas_impl.h"
+#include "device.cuh"
+#include "dirac_impl.h"
+#include "ext_impl.h"
+#include "handles.h"
+
+namespace qed3 {
+
+static inline int nblk(long long n, int t = 256) { return int((n + t - 1) / t); }
+
+// per-slice spatial blocks: H3[s][k][i] = e^{i sgn A_s[l]} G[k][i], Hd3 likewise
+__global__ void k_ext_set_links(int Ns, int Nl, int Nt, const int32_t* __restrict__ hop_link,
+                                const int8_t* __restrict__ hop_sign, const double* __restrict__ A,
+                                const M64* __restrict__ G, const M64* __restrict__ Gd, M64* __restrict__ H3,
+                                M64* __restrict__ Hd3) {
+  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= 3LL * Ns * Nt) return;
+  const int s = int(idx / (3LL * Ns));
+  const int q = int(idx % (3LL * Ns));
+  const double a = double(hop_sign[q]) * A[size_t(s) * Nl + hop_link[q]];
+  double sn, cs;
+  sincos(a, &sn, &cs);
+  const double2 ph = make_double2(cs, sn);
+  const M64 g = G[q], gd = Gd[q];
+  H3[idx] = M64{cmul(ph, g.h00), cmul(ph, g.h01), cmul(ph, g.h10), cmul(ph, g.h11)};
+  Hd3[idx] = M64{cmul(ph, gd.h00), cmul(ph, gd.h01), cmul(ph, gd.h10), cmul(ph, gd.h11)};
+}
+
+// out = op(D) in for op = D (adj = 0) or D^dag (adj = 1), reference order
+__global__ void k_ext_apply(int Ns, int Nt, int adj, const int32_t* __restrict__ nbr_ref,
+                            const int32_t* __restrict__ perm, const M64* __restrict__ H3,
+                            const double* __restrict__ diag3, const double* __restrict__ kt,
+                            const double* __restrict__ At, double r, const S64* __restrict__ in,
+                            S64* __restrict__ out) {
+  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= (long long)Ns * Nt) return;
+  const int s = int(idx / Ns), i = int(idx % Ns);
+  const int x = perm[i];
+  const S64* vs = in + size_t(s) * Ns;
+  const Sp64 self = ld64(vs, x);
+  const double dg = diag3[i];
+  Sp64 o{cscale(dg, self.s0), cscale(dg, self.s1)};
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    const M64 m = H3[(size_t(s) * 3 + k) * Ns + i];
+    const Sp64 b = ld64(vs, nbr_ref[size_t(k) * Ns + i]);
+    o.s0 = cfma(m.h00, b.s0, o.s0);
+    o.s0 = cfma(m.h01, b.s1, o.s0);
+    o.s1 = cfma(m.h10, b.s0, o.s1);
+    o.s1 = cfma(m.h11, b.s1, o.s1);
+  }
+  if (Nt > 1) {
+    const double kh = 0.5 * kt[i];
+    const int sp = (s + 1) % Nt, sm = (s + Nt - 1) % Nt;
+    const Sp64 up = ld64(in + size_t(sp) * Ns, x), dn = ld64(in + size_t(sm) * Ns, x);
+    // spin-diagonal coefficients (upper, lower) and phases of the two hops
+    double cu0, cu1, cd0, cd1, au, ad;
+    if (!adj) {
+      // from (x, s+1): tmpM(s+1) = 0.5 sM(s+1) kt (-r + sigma3) e^{+i A_t(s,x)}
+      const double sgn_u = (sp == 0) ? -1.0 : 1.0;
+      cu0 = sgn_u * kh * (-r + 1.0);
+      cu1 = sgn_u * kh * (-r - 1.0);
+      au = At[size_t(s) * Ns + x];
+      // from (x, s-1): tmpP(s-1) = 0.5 sP(s-1) kt (-r - sigma3) e^{-i A_t(s-1,x)}
+      const double sgn_d = (sm == Nt - 1) ? -1.0 : 1.0;
+      cd0 = sgn_d * kh * (-r - 1.0);
+      cd1 = sgn_d * kh * (-r + 1.0);
+      ad = -At[size_t(sm) * Ns + x];
+    } else {
+      // conj(D[(x,s+1),(x,s)]) = conj(tmpP(s)): sP(s) kt/2 (-r - sigma3) e^{+i A_t(s,x)}
+      const double sgn_u = (s == Nt - 1) ? -1.0 : 1.0;
+      cu0 = sgn_u * kh * (-r - 1.0);
+      cu1 = sgn_u * kh * (-r + 1.0);
+      au = At[size_t(s) * Ns + x];
+      // conj(D[(x,s-1),(x,s)]) = conj(tmpM(s)): sM(s) kt/2 (-r + sigma3) e^{-i A_t(s-1,x)}
+      const double sgn_d = (s == 0) ? -1.0 : 1.0;
+      cd0 = sgn_d * kh * (-r + 1.0);
+      cd1 = sgn_d * kh * (-r - 1.0);
+      ad = -At[size_t(sm) * Ns + x];
+    }
+    double su, cu, sd, cdn;
+    sincos(au, &su, &cu);
+    sincos(ad, &sd, &cdn);
+    const double2 pu = make_double2(cu, su), pd = make_double2(cdn, sd);
+    o.s0 = cadd(o.s0, cadd(cscale(cu0, cmul(pu, up.s0)), cscale(cd0, cmul(pd, dn.s0))));
+    o.s1 = cadd(o.s1, cadd(cscale(cu1, cmul(pu, up.s1)), cscale(cd1, cmul(pd, dn.s1))));
+  }
+  st64(out + size_t(s) * Ns, x, o);
+}
+
+int ext_init(qed3_dirac_ext_s* e) {
+  qed3_dirac_s* d = e->d2;
+  const HostLattice& L = d->lat->host;
+  const int Ns = d->Ns, Nt = e->Nt;
+  std::vector<double> kt(Ns), diag2(Ns), diag3(Ns);
+  QED3_CUDA_TRY(cudaMemcpy(diag2.data(), d->diag, Ns * sizeof(double), cudaMemcpyDeviceToHost));
+  for (int i = 0; i < Ns; i++) {
+    const int x = L.perm[i];
+    kt[i] = Nt != 1 ? L.tri_area[x] / L.mean_ell / e->at : 0.0;
+    diag3[i] = diag2[i] + e->r * kt[i];
+  }
+  const size_t nh = size_t(3) * Ns * Nt;
+  QED3_CUDA_TRY(cudaMalloc(&e->H3, nh * sizeof(M64)));
+  QED3_CUDA_TRY(cudaMalloc(&e->Hd3, nh * sizeof(M64)));
+  QED3_CUDA_TRY(cudaMalloc(&e->kt, Ns * sizeof(double)));
+  QED3_CUDA_TRY(cudaMalloc(&e->diag3, Ns * sizeof(double)));
+  QED3_CUDA_TRY(cudaMalloc(&e->At, size_t(Ns) * Nt * sizeof(double)));
+  QED3_CUDA_TRY(cudaMalloc(&e->tmp, size_t(Ns) * Nt * sizeof(S64)));
+  QED3_CUDA_TRY(cudaMalloc(&e->work, size_t(Ns) * Nt * 3 * sizeof(S64) + 2048 * sizeof(double)));
+  QED3_CUDA_TRY(cudaMemcpy(e->kt, kt.data(), Ns * sizeof(double), cudaMemcpyHostToDevice));
+  QED3_CUDA_TRY(cudaMemcpy(e->diag3, diag3.data(), Ns * sizeof(double), cudaMemcpyHostToDevice));
+  return QED3_OK;
+}
+
+void ext_free(qed3_dirac_ext_s* e) {
+  void* p[] = {e->H3, e->Hd3, e->kt, e->diag3, e->At, e->tmp, e->work};
+  for (void* q : p)
+    if (q) cudaFree(q);
+}
+
+int ext_set_links(qed3_dirac_ext_s* e, const double* A, cudaStream_t st) {
+  qed3_dirac_s* d = e->d2;
+  const DeviceLattice& D = d->lat->dev;
+  const int Ns = d->Ns, Nl = D.Nl, Nt = e->Nt;
+  k_ext_set_links<<<nblk(3LL * Ns * Nt), 256, 0, st>>>(Ns, Nl, Nt, D.hop_link, D.hop_sign, A, d->G, d->Gd, e->H3,
+                                                      e->Hd3);
+  QED3_CUDA_TRY(cudaGetLastError());
+  QED3_CUDA_TRY(cudaMemcpyAsync(e->At, A + size_t(Nt) * Nl, size_t(Ns) * Nt * sizeof(double),
+                                cudaMemcpyDeviceToDevice, st));
+  e->links_set = true;
+  return QED3_OK;
+}
+
+int ext_apply(qed3_dirac_ext_s* e, int op, double* out, const double* in, cudaStream_t st) {
+  if (!e->links_set) return fail(QED3_ERR_STATE, "call qed3_dirac_ext_set_links first");
+  qed3_dirac_s* d = e->d2;
+  const DeviceLattice& D = d->lat->dev;
+  const int Ns = d->Ns, Nt = e->Nt;
+  const long long n = (long long)Ns * Nt;
+  auto run = [&](int adj, S64* o, const S64* v) {
+    k_ext_apply<<<nblk(n), 256, 0, st>>>(Ns, Nt, adj, D.nbr_ref, D.perm, adj ? e->Hd3 : e->H3, e->diag3, e->kt,
+                                        e->At, d->r, v, o);
+  };
+  const S64* v = reinterpret_cast<const S64*>(in);
+  S64* o = reinterpret_cast<S64*>(out);
+  if (op == QED3_OP_D || op == QED3_OP_DDAG) {
+    if (in == out) {
+      QED3_CUDA_TRY(cudaMemcpyAsync(e->tmp, in, n * sizeof(S64), cudaMemcpyDeviceToDevice, st));
+      v = e->tmp;
+    }
+    run(op == QED3_OP_DDAG, o, v);
+  } else if (op == QED3_OP_DDAGD) {
+    run(0, e->tmp, v);
+    run(1, o, e->tmp);
+  } else if (op == QED3_OP_DDDAG) {
+    run(1, e->tmp, v);
+    run(0, o, e->tmp);
+  } else {
+    return fail(QED3_ERR_ARG, "unknown operator");
+  }
+  QED3_CUDA_TRY(cudaGetLastError());
+  return QED3_OK;
+}
+
+// MatPoly::solve (src/dual/matpoly.h:204-267) on D^dag D + shift in FP64:
+// x0 = 0, stop on the recursive residual, certified by the true residual.
+int ext_cg(qed3_dirac_ext_s* e, double* x, const double* b, const qed3_solve_params* prm, qed3_solve_report* rep,
+           cudaStream_t st) {
+  if (!e->links_set) return fail(QED3_ERR_STATE, "call qed3_dirac_ext_set_links first");
+  if (prm && prm->precision != QED3_PREC_F64) return fail(QED3_ERR_ARG, "the S2 x S1 solve runs in FP64");
+  const double tol = prm && prm->tol > 0 ? prm->tol : 1e-10;
+  const int maxiter = prm && prm->maxiter > 0 ? prm->maxiter : 100000;
+  const double shift = prm ? prm->shift : 0.0;
+  const long long nd = 4LL * e->d2->Ns * e->Nt, nc = nd / 2;
+  double* r = reinterpret_cast<double*>(e->work);
+  double* p = r + nd;
+  double* q = p + nd;
+  double* part = q + nd;
+  cudaEvent_t e0, e1;
+  QED3_CUDA_TRY(cudaEventCreate(&e0));
+  QED3_CUDA_TRY(cudaEventCreate(&e1));
+  QED3_CUDA_TRY(cudaEventRecord(e0, st));
+  auto A = [&](double* o, const double* v) -> int {
+    int c = ext_apply(e, QED3_OP_DDAGD, o, v, st);
+    if (!c && shift != 0.0) c = vec_axpby(nd, shift, v, 1.0, o, o, st);
+    return c;
+  };
+  int rc;
+  double bb = 0, im = 0;
+  if ((rc = vec_zdot(nc, b, b, part, &bb, &im, st))) return rc;
+  QED3_CUDA_TRY(cudaMemsetAsync(x, 0, nd * sizeof(double), st));
+  QED3_CUDA_TRY(cudaMemcpyAsync(r, b, nd * sizeof(double), cudaMemcpyDeviceToDevice, st));
+  QED3_CUDA_TRY(cudaMemcpyAsync(p, b, nd * sizeof(double), cudaMemcpyDeviceToDevice, st));
+  double mu = bb;
+  int it = 0, status = bb == 0.0 ? QED3_OK : QED3_ERR_NOCONV;
+  while (status != QED3_OK && it < maxiter) {
+    if ((rc = A(q, p))) return rc;
+    double pq = 0;
+    if ((rc = vec_zdot(nc, p, q, part, &pq, &im, st))) return rc;
+    const double al = mu / pq;
+    if ((rc = vec_axpby(nd, al, p, 1.0, x, x, st)) || (rc = vec_axpby(nd, -al, q, 1.0, r, r, st))) return rc;
+    double mn = 0;
+    if ((rc = vec_zdot(nc, r, r, part, &mn, &im, st))) return rc;
+    it++;
+    if (!std::isfinite(mn)) break;
+    if (mn < tol * tol * bb) {
+      status = QED3_OK;
+      break;
+    }
+    if ((rc = vec_axpby(nd, 1.0, r, mn / mu, p, p, st))) return rc;
+    mu = mn;
+  }
+  double tr = 0;
+  if (bb > 0) {
+    if ((rc = A(q, x)) || (rc = vec_axpby(nd, 1.0, b, -1.0, q, q, st)) || (rc = vec_zdot(nc, q, q, part, &tr, &im, st)))
+      return rc;
+  }
+  QED3_CUDA_TRY(cudaEventRecord(e1, st));
+  QED3_CUDA_TRY(cudaEventSynchronize(e1));
+  float ms = 0;
+  cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (rep) {
+    rep->status = status;
+    rep->iters = it;
+    rep->reliable_updates = 0;
+    rep->true_rel_res = bb > 0 ? std::sqrt(tr / bb) : 0.0;
+    rep->ms = ms;
+  }
+  return QED3_OK;
+}
+
+}  // namespace qed3

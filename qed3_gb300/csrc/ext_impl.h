@@ -1,0 +1,29 @@
+// S^2 x S^1 operator (ext.cu).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "handles.h"
+
+struct qed3_dirac_ext_s {
+  qed3_dirac_s* d2 = nullptr;  // the dual-lattice operator: geometry blocks, kappa, diagonal
+  int Nt = 1;
+  double at = 1.0, r = 1.0;
+  qed3::M64* H3 = nullptr;     // [Nt][3][Ns] spatial blocks of D per slice (internal site order)
+  qed3::M64* Hd3 = nullptr;    // [Nt][3][Ns] the same for D^dagger
+  double* kt = nullptr;        // [Ns] kappa_t (internal order)
+  double* diag3 = nullptr;     // [Ns]
+  double* At = nullptr;        // [Nt][Ns] temporal angles (reference order)
+  qed3::S64* tmp = nullptr;    // [Nt][Ns]
+  void* work = nullptr;        // CG vectors
+  bool links_set = false;
+};
+
+namespace qed3 {
+int ext_init(qed3_dirac_ext_s* e);
+void ext_free(qed3_dirac_ext_s* e);
+int ext_set_links(qed3_dirac_ext_s* e, const double* A, cudaStream_t st);
+int ext_apply(qed3_dirac_ext_s* e, int op, double* out, const double* in, cudaStream_t st);
+int ext_cg(qed3_dirac_ext_s* e, double* x, const double* b, const qed3_solve_params* prm, qed3_solve_report* rep,
+           cudaStream_t st);
+}  // namespace qed3

@@ -359,6 +359,15 @@ static int build_dual(const std::vector<V3>& vert, const std::vector<int32_t>& t
   s = 0;
   for (double e : L.ell) s += e;
   L.mean_ell = s / double(Nl);
+  // area of each triangle = dual site, S2Simp::vols (src/both_3d/s2n_simp.h:234-253)
+  L.tri_area.resize(size_t(Ns));
+  for (int64_t t = 0; t < Ns; t++) {
+    const V3 x0 = vert[tri[3 * t]], x1 = vert[tri[3 * t + 1]], x2 = vert[tri[3 * t + 2]];
+    const double a_ = std::acos(dot(x0, x1)), b_ = std::acos(dot(x1, x2)), c_ = std::acos(dot(x2, x0));
+    const double s_ = 0.5 * (a_ + b_ + c_);
+    const double tt = std::tan(0.5 * s_) * std::tan(0.5 * (s_ - a_)) * std::tan(0.5 * (s_ - b_)) * std::tan(0.5 * (s_ - c_));
+    L.tri_area[t] = 4.0 * std::atan(std::sqrt(tt));
+  }
   L.vols.resize(size_t(Nv));
   for (int64_t v = 0; v < Nv; v++) {
     double area = 0;

@@ -36,6 +36,7 @@ struct HostLattice {
   std::vector<int32_t> face_offsets; // [Nf+1]
   std::vector<int32_t> face_sites;   // ring of each dual face
   std::vector<double> ell, link_volume, vols;
+  std::vector<double> tri_area;      // [Ns] spherical area of the triangle of dual site t (S2Simp::vols)
   double mean_ell = 0, mean_link_volume = 0, mean_vol = 0;
   std::vector<double> omega;         // [Nl], omega(links[l][0], links[l][1])
   std::vector<double> alpha;         // [Ns*3], alpha(x, nns[x][k])

@@ -345,3 +345,25 @@ def test_cpu_runnable_configuration_n8():
     x, it, _ = D.cg(b, tol=1e-10)
     assert np.linalg.norm(b - D.apply(x, 2)) / np.linalg.norm(b) <= 1e-10
     assert 20 < it < 2000
+
+
+def test_ext_operator_restatement():
+    """DiracExt restated: Nt = 1 is the dual-lattice operator; for Nt > 1 the
+    adjoint is the conjugate transpose (dense check) and D^dag D is hermitian
+    positive definite; the triangle areas tile the sphere."""
+    g = O.geometry(2)
+    assert abs(O.triangle_areas(g).sum() - 4 * np.pi) < 1e-12
+    rng = np.random.default_rng(3)
+    A1 = rng.uniform(-np.pi, np.pi, g.n_links + g.n_sites)
+    v = rng.normal(size=2 * g.n_sites) + 1j * rng.normal(size=2 * g.n_sites)
+    D = O.Dirac(g, 1.0, 0.1)
+    D.update(A1[:g.n_links])
+    assert np.abs(O.dirac_ext_apply(g, 1.0, 0.1, 1, 0.5, A1, v) - D.apply(v, 0)).max() < 1e-14
+    for Nt in (2, 3):
+        A = rng.uniform(-np.pi, np.pi, Nt * (g.n_links + g.n_sites))
+        N = 2 * g.n_sites * Nt
+        M = np.stack([O.dirac_ext_apply(g, 1.0, 0.1, Nt, 0.7, A, e) for e in np.eye(N)], axis=1)
+        Md = np.stack([O.dirac_ext_apply(g, 1.0, 0.1, Nt, 0.7, A, e, 1) for e in np.eye(N)], axis=1)
+        assert np.abs(Md - M.conj().T).max() < 1e-13
+        w = np.linalg.eigvalsh(M.conj().T @ M)
+        assert w[0] > 0
