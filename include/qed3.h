@@ -225,6 +225,18 @@ int qed3_dirac_ext_apply(qed3_dirac_ext* e, int op, double* out, const double* i
 int qed3_dirac_ext_cg_solve(qed3_dirac_ext* e, double* x, const double* b, const qed3_solve_params* params,
                             qed3_solve_report* report, void* stream);
 
+/* S^2 x S^1 gauge side: U1WilsonExt (src/both_3d/action_ext.h:4-161) and the
+ * Polyakov loop (src/both_3d/obs.h:4-10).  A: device [Nt][n_links] spatial,
+ * then [Nt][n_sites] temporal.  theta_s [Nt][n_faces] (spatial plaquettes),
+ * theta_t [Nt][n_links] (temporal: A_s + A_t(s,y) - A_{s+1} - A_t(s,x)); the
+ * action sum beta_s theta_s^2/2 + beta_t theta_t^2/2 with beta_s = at / vols / gsq,
+ * beta_t = 2 / at * link_volume / ell^2 / gsq; F has A's layout; P[n_sites]
+ * complex = exp(i sum_s A_t(s,x)), avg[2] its mean (either may be NULL). */
+int qed3_ext_plaquettes(qed3_lattice* lat, int Nt, const double* A, double* theta_s, double* theta_t, void* stream);
+int qed3_ext_gauge_action(qed3_lattice* lat, int Nt, double at, double gsq, const double* A, double* S, void* stream);
+int qed3_ext_gauge_force(qed3_lattice* lat, int Nt, double at, double gsq, const double* A, double* F, void* stream);
+int qed3_ext_polyakov(qed3_lattice* lat, int Nt, const double* A, double* P, double* avg, void* stream);
+
 /* ======================================================================
  * Batched solves in ONE persistent launch  --  replaces the reference's
  * loops of MatPoly::solve over pseudofermions and Zolotarev poles on OpenMP

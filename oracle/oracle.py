@@ -523,3 +523,81 @@ def dirac_ext_apply(geom: Geometry, r: float, M5: float, Nt: int, at: float, A: 
             else:  # D^dag[(x,s),(x,s+1)] = conj(tmpP(s)), D^dag[(x,s),(x,s-1)] = conj(tmpM(s))
                 out[s] += np.conj(tmpP) * v[up] + np.conj(tmpM) * v[dn]
     return out.reshape(-1)
+
+
+def ext_gauge(geom: Geometry, Nt: int, at: float, gsq: float, A: np.ndarray):
+    """U1WilsonExt restated (src/both_3d/action_ext.h:31-161) with GaugeExt's
+    plaquettes (src/both_3d/gauge_ext.h:124-143), loop for loop in the
+    reference's order.  Returns (theta_s [Nt][Nf], theta_t [Nt][Nl], S, F) with F
+    in A's layout (spatial [Nt][Nl], then temporal [Nt][Ns])."""
+    Ns, Nl, Nf = geom.n_sites, geom.n_links, geom.n_faces
+    sp = np.asarray(A[:Nt * Nl]).reshape(Nt, Nl)
+    tp = np.asarray(A[Nt * Nl:Nt * (Nl + Ns)]).reshape(Nt, Ns)
+    il = {(int(i), int(j)): (l, 1) for l, (i, j) in enumerate(geom.links)}
+    il.update({(int(j), int(i)): (l, -1) for l, (i, j) in enumerate(geom.links)})
+    faces = geom.faces()
+    bs = np.array([at / geom.vols[f] / gsq for f in range(Nf)]) if abs(gsq) > 1e-15 else np.zeros(Nf)
+    bt = np.array([2.0 / at * geom.link_volume[l] / geom.ell[l] ** 2 / gsq for l in range(Nl)]) \
+        if abs(gsq) > 1e-15 else np.zeros(Nl)
+
+    def th_s(s, f):
+        t = 0.0
+        face = faces[f]
+        for k in range(len(face)):
+            l, sg = il[(int(face[k]), int(face[(k + 1) % len(face)]))]
+            t += sg * sp[s % Nt][l]
+        return t
+
+    def th_t(s, l):
+        x, y = int(geom.links[l][0]), int(geom.links[l][1])
+        t = 0.0
+        t += sp[s % Nt][l]
+        t += tp[s % Nt][y]
+        t -= sp[(s + 1) % Nt][l]
+        t -= tp[s % Nt][x]
+        return t
+
+    ths = np.array([[th_s(s, f) for f in range(Nf)] for s in range(Nt)])
+    tht = np.array([[th_t(s, l) for l in range(Nl)] for s in range(Nt)])
+    tmp = [0.0] * Nt
+    for s in range(Nt):
+        for f in range(Nf):
+            tmp[s] += 0.5 * bs[f] * ths[s][f] ** 2
+    for s in range(Nt):
+        for l in range(Nl):
+            tmp[s] += 0.5 * bt[l] * tht[s][l] ** 2
+    S = 0.0
+    for s in range(Nt):
+        S += tmp[s]
+    Fs = np.zeros((Nt, Nl))
+    Ft = np.zeros((Nt, Ns))
+    for s in range(Nt):
+        for f in range(Nf):
+            grad = bs[f] * ths[s][f]
+            face = faces[f]
+            for k in range(len(face)):
+                l, sg = il[(int(face[k]), int(face[(k + 1) % len(face)]))]
+                Fs[s][l] += grad * sg
+    for s in range(Nt):
+        for l in range(Nl):
+            x, y = int(geom.links[l][0]), int(geom.links[l][1])
+            grad = bt[l] * tht[s][l]
+            grad2 = bt[l] * tht[(s - 1) % Nt][l]
+            Fs[s][l] += grad
+            Ft[s][y] += grad
+            Fs[s][l] -= grad2
+            Ft[s][x] -= grad
+    return ths, tht, S, np.concatenate([Fs.ravel(), Ft.ravel()])
+
+
+def ext_polyakov(geom: Geometry, Nt: int, A: np.ndarray) -> np.ndarray:
+    """get_polyakov (src/both_3d/obs.h:4-10) at every dual site."""
+    Ns, Nl = geom.n_sites, geom.n_links
+    tp = np.asarray(A[Nt * Nl:Nt * (Nl + Ns)]).reshape(Nt, Ns)
+    out = np.zeros(Ns, np.complex128)
+    for x in range(Ns):
+        a = 0.0
+        for s in range(Nt):
+            a += tp[s][x]
+        out[x] = np.exp(1j * a)
+    return out

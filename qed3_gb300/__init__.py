@@ -135,6 +135,10 @@ SIGNATURES = [
     ("qed3_dirac_ext_apply", ctypes.c_int, [vp, ctypes.c_int, vp, vp, vp]),
     ("qed3_dirac_ext_cg_solve", ctypes.c_int, [vp, vp, vp, ctypes.POINTER(SolveParams), ctypes.POINTER(SolveReport),
                                                vp]),
+    ("qed3_ext_plaquettes", ctypes.c_int, [vp, ctypes.c_int, vp, vp, vp, vp]),
+    ("qed3_ext_gauge_action", ctypes.c_int, [vp, ctypes.c_int, ctypes.c_double, ctypes.c_double, vp, c_double_p, vp]),
+    ("qed3_ext_gauge_force", ctypes.c_int, [vp, ctypes.c_int, ctypes.c_double, ctypes.c_double, vp, vp, vp]),
+    ("qed3_ext_polyakov", ctypes.c_int, [vp, ctypes.c_int, vp, vp, c_double_p, vp]),
     ("qed3_batch_create", ctypes.c_int, [ctypes.c_int, vp, vp, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                          ctypes.POINTER(vp)]),
     ("qed3_batch_destroy", ctypes.c_int, [vp]),
@@ -559,6 +563,29 @@ def zolotarev(k: float, n: int) -> dict:
 # ---------------------------------------------------------------------------
 # batched persistent solver
 # ---------------------------------------------------------------------------
+def ext_plaquettes(lattice: S2Trivalent, Nt: int, A, theta_s, theta_t, stream=None):
+    """S^2 x S^1 spatial [Nt][n_faces] and temporal [Nt][n_links] plaquette angles (device)."""
+    _check(lib().qed3_ext_plaquettes(lattice.handle, Nt, _ptr(A), _ptr(theta_s), _ptr(theta_t), _stream(stream)))
+
+
+def ext_gauge_action(lattice: S2Trivalent, Nt: int, at: float, gsq: float, A, stream=None) -> float:
+    S = ctypes.c_double()
+    _check(lib().qed3_ext_gauge_action(lattice.handle, Nt, at, gsq, _ptr(A), ctypes.byref(S), _stream(stream)))
+    return S.value
+
+
+def ext_gauge_force(lattice: S2Trivalent, Nt: int, at: float, gsq: float, A, F, stream=None):
+    _check(lib().qed3_ext_gauge_force(lattice.handle, Nt, at, gsq, _ptr(A), _ptr(F), _stream(stream)))
+    return F
+
+
+def ext_polyakov(lattice: S2Trivalent, Nt: int, A, P=None, stream=None):
+    """Polyakov loop per site into P (device complex128, optional); returns its mean."""
+    avg = (ctypes.c_double * 2)()
+    _check(lib().qed3_ext_polyakov(lattice.handle, Nt, _ptr(A), _ptr(P), avg, _stream(stream)))
+    return complex(avg[0], avg[1])
+
+
 class DiracExt:
     """S^2 x S^1 Wilson-Dirac operator with Nt time slices (DiracExt, src/both_3d/dirac_ext.h:6-334).
 

@@ -311,6 +311,34 @@ int qed3_dirac_ext_cg_solve(qed3_dirac_ext* e, double* x, const double* b, const
   QED3_GUARD_END
 }
 
+int qed3_ext_plaquettes(qed3_lattice* lat, int Nt, const double* A, double* theta_s, double* theta_t, void* stream) {
+  QED3_GUARD_BEGIN
+  if (!lat || !A || Nt < 1) return fail(QED3_ERR_ARG, "bad argument");
+  return ext_plaquettes(lat, Nt, A, theta_s, theta_t, (cudaStream_t)stream);
+  QED3_GUARD_END
+}
+
+int qed3_ext_gauge_action(qed3_lattice* lat, int Nt, double at, double gsq, const double* A, double* S, void* stream) {
+  QED3_GUARD_BEGIN
+  if (!lat || !A || !S || Nt < 1 || !(at > 0)) return fail(QED3_ERR_ARG, "bad argument");
+  return ext_gauge_action(lat, Nt, at, gsq, A, S, (cudaStream_t)stream);
+  QED3_GUARD_END
+}
+
+int qed3_ext_gauge_force(qed3_lattice* lat, int Nt, double at, double gsq, const double* A, double* F, void* stream) {
+  QED3_GUARD_BEGIN
+  if (!lat || !A || !F || Nt < 1 || !(at > 0)) return fail(QED3_ERR_ARG, "bad argument");
+  return ext_gauge_force(lat, Nt, at, gsq, A, F, (cudaStream_t)stream);
+  QED3_GUARD_END
+}
+
+int qed3_ext_polyakov(qed3_lattice* lat, int Nt, const double* A, double* P, double* avg, void* stream) {
+  QED3_GUARD_BEGIN
+  if (!lat || !A || Nt < 1) return fail(QED3_ERR_ARG, "bad argument");
+  return ext_polyakov(lat, Nt, A, P, avg, (cudaStream_t)stream);
+  QED3_GUARD_END
+}
+
 int qed3_dirac_destroy(qed3_dirac* d) {
   if (!d) return QED3_OK;
   solver_free(d);

@@ -681,3 +681,212 @@ int hmc_overlap(qed3_lattice_s* lat, qed3_overlap_s* ov, qed3_rng_s* rng, double
 }
 
 }  // namespace qed3
+
+// ===========================================================================
+// S^2 x S^1 gauge side: U1WilsonExt (src/both_3d/action_ext.h:4-161) and the
+// Polyakov loop (src/both_3d/obs.h:4-10).  Links A[Nt][Nl] spatial, then
+// A[Nt][Ns] temporal (reference site order).  Plaquettes:
+//   spatial  theta_s(s, f) = sum of the face's oriented slice-s links,
+//   temporal theta_t(s, l) = A_s[l] + A_t(s, y) - A_{s+1}[l] - A_t(s, x), l = (x, y);
+// action sum_s [sum_f beta_s[f] theta_s^2 / 2 + sum_l beta_t[l] theta_t^2 / 2]
+// with beta_s = at / vols[f] / gsq, beta_t = 2 / at * link_volume / ell^2 / gsq.
+// ===========================================================================
+namespace qed3 {
+
+__global__ void k_ext_plaq(int Nt, int Nl, int Ns, int Nf, const int32_t* __restrict__ off,
+                           const int32_t* __restrict__ flink, const int8_t* __restrict__ fsign,
+                           const int32_t* __restrict__ lx, const int32_t* __restrict__ ly,
+                           const int32_t* __restrict__ perm, const double* __restrict__ A, double* __restrict__ ths,
+                           double* __restrict__ tht) {
+  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long nsp = (long long)Nt * Nf;
+  if (idx < nsp) {
+    const int s = int(idx / Nf), f = int(idx % Nf);
+    const double* As = A + size_t(s) * Nl;
+    double t = 0.0;
+    for (int e = off[f]; e < off[f + 1]; e++) t += double(fsign[e]) * As[flink[e]];
+    ths[idx] = t;
+  } else if (idx < nsp + (long long)Nt * Nl) {
+    const long long j = idx - nsp;
+    const int s = int(j / Nl), l = int(j % Nl), s1 = (s + 1) % Nt;
+    const double* At = A + size_t(Nt) * Nl + size_t(s) * Ns;
+    const int x = perm[lx[l]], y = perm[ly[l]];
+    double t = 0.0;
+    t += A[size_t(s) * Nl + l];
+    t += At[y];
+    t -= A[size_t(s1) * Nl + l];
+    t -= At[x];
+    tht[j] = t;
+  }
+}
+
+struct ExtAction {
+  const double *ths, *tht, *bs, *bt;
+  long long nsp;
+  int Nf, Nl;
+  __device__ double operator()(int i) const {
+    if (i < nsp) return 0.5 * bs[i % Nf] * ths[i] * ths[i];
+    const long long j = i - nsp;
+    return 0.5 * bt[j % Nl] * tht[j] * tht[j];
+  }
+};
+
+// spatial force per (s, l): its two faces (ascending face index), then the
+// temporal plaquettes of slices s and s-1, in the reference's order of updates
+__global__ void k_ext_force_s(int Nt, int Nl, int Nf, const int32_t* __restrict__ lf, const int8_t* __restrict__ ls,
+                              const double* __restrict__ ths, const double* __restrict__ tht,
+                              const double* __restrict__ bs, const double* __restrict__ bt, double* __restrict__ F) {
+  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= (long long)Nt * Nl) return;
+  const int s = int(idx / Nl), l = int(idx % Nl), sm = (s + Nt - 1) % Nt;
+  const int f0 = lf[2 * l], f1 = lf[2 * l + 1];
+  double v = 0.0;
+  v += bs[f0] * ths[size_t(s) * Nf + f0] * double(ls[2 * l]);
+  v += bs[f1] * ths[size_t(s) * Nf + f1] * double(ls[2 * l + 1]);
+  v += bt[l] * tht[size_t(s) * Nl + l];
+  v -= bt[l] * tht[size_t(sm) * Nl + l];
+  F[idx] = v;
+}
+
+// temporal force per (s, x): the three incident links in increasing link
+// index (the reference's loop order), +grad at the link's end, -grad at its start
+__global__ void k_ext_force_t(int Nt, int Nl, int Ns, const int32_t* __restrict__ hop_link,
+                              const int8_t* __restrict__ hop_sign, const int32_t* __restrict__ perm,
+                              const double* __restrict__ tht, const double* __restrict__ bt, double* __restrict__ F) {
+  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= (long long)Nt * Ns) return;
+  const int s = int(idx / Ns), i = int(idx % Ns);
+  int lk[3];
+  int sg[3];
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    lk[k] = hop_link[size_t(k) * Ns + i];
+    sg[k] = hop_sign[size_t(k) * Ns + i];  // +1: this site is the link's start
+  }
+#pragma unroll
+  for (int a = 0; a < 2; a++)
+#pragma unroll
+    for (int b = 0; b < 2 - a; b++)
+      if (lk[b] > lk[b + 1]) {
+        const int tl = lk[b], ts = sg[b];
+        lk[b] = lk[b + 1];
+        sg[b] = sg[b + 1];
+        lk[b + 1] = tl;
+        sg[b + 1] = ts;
+      }
+  double v = 0.0;
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    const double g = bt[lk[k]] * tht[size_t(s) * Nl + lk[k]];
+    if (sg[k] < 0) v += g;
+    else v -= g;
+  }
+  F[size_t(Nt) * Nl + size_t(s) * Ns + perm[i]] = v;
+}
+
+__global__ void k_ext_polyakov(int Nt, int Nl, int Ns, const double* __restrict__ A, double* __restrict__ P) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  if (x >= Ns) return;
+  double a = 0.0;
+  for (int s = 0; s < Nt; s++) a += A[size_t(Nt) * Nl + size_t(s) * Ns + x];
+  double sn, cs;
+  sincos(a, &sn, &cs);
+  P[2 * x] = cs;
+  P[2 * x + 1] = sn;
+}
+
+struct ExtBuf {
+  double *ths = nullptr, *tht = nullptr, *bs = nullptr, *bt = nullptr;
+  ~ExtBuf() {
+    for (double* p : {ths, tht, bs, bt})
+      if (p) cudaFree(p);
+  }
+};
+
+static int ext_prepare(qed3_lattice_s* lat, int Nt, double at, double gsq, const double* A, ExtBuf& b,
+                       cudaStream_t st) {
+  int rc = gauge_prepare(lat);
+  if (rc) return rc;
+  const HostLattice& L = lat->host;
+  const DeviceLattice& D = lat->dev;
+  const int Nl = D.Nl, Nf = D.Nf, Ns = D.Ns;
+  std::vector<double> bs(Nf, 0.0), bt(Nl, 0.0);
+  if (std::abs(gsq) > 1.0e-15) {  // U1WilsonExt::set_beta (src/both_3d/action_ext.h:148-158)
+    for (int f = 0; f < Nf; f++) bs[f] = at / L.vols[f] / gsq;
+    for (int l = 0; l < Nl; l++) bt[l] = 2.0 / at * L.link_volume[l] / std::pow(L.ell[l], 2) / gsq;
+  }
+  QED3_CUDA_TRY(cudaMalloc(&b.ths, size_t(Nt) * Nf * sizeof(double)));
+  QED3_CUDA_TRY(cudaMalloc(&b.tht, size_t(Nt) * Nl * sizeof(double)));
+  QED3_CUDA_TRY(cudaMalloc(&b.bs, size_t(Nf) * sizeof(double)));
+  QED3_CUDA_TRY(cudaMalloc(&b.bt, size_t(Nl) * sizeof(double)));
+  QED3_CUDA_TRY(cudaMemcpyAsync(b.bs, bs.data(), Nf * sizeof(double), cudaMemcpyHostToDevice, st));
+  QED3_CUDA_TRY(cudaMemcpyAsync(b.bt, bt.data(), Nl * sizeof(double), cudaMemcpyHostToDevice, st));
+  const long long n = (long long)Nt * (Nf + Nl);
+  k_ext_plaq<<<nblk(n), 256, 0, st>>>(Nt, Nl, Ns, Nf, D.face_off, D.face_link, D.face_sign, D.link_x, D.link_y,
+                                      D.perm, A, b.ths, b.tht);
+  QED3_CUDA_TRY(cudaGetLastError());
+  QED3_CUDA_TRY(cudaStreamSynchronize(st));  // the host staging vectors go out of scope
+  return QED3_OK;
+}
+
+int ext_plaquettes(qed3_lattice_s* lat, int Nt, const double* A, double* ths, double* tht, cudaStream_t st) {
+  ExtBuf b;
+  int rc = ext_prepare(lat, Nt, 1.0, 0.0, A, b, st);
+  if (rc) return rc;
+  const DeviceLattice& D = lat->dev;
+  if (ths) QED3_CUDA_TRY(cudaMemcpyAsync(ths, b.ths, size_t(Nt) * D.Nf * sizeof(double), cudaMemcpyDeviceToDevice, st));
+  if (tht) QED3_CUDA_TRY(cudaMemcpyAsync(tht, b.tht, size_t(Nt) * D.Nl * sizeof(double), cudaMemcpyDeviceToDevice, st));
+  QED3_CUDA_TRY(cudaStreamSynchronize(st));
+  return QED3_OK;
+}
+
+int ext_gauge_action(qed3_lattice_s* lat, int Nt, double at, double gsq, const double* A, double* S, cudaStream_t st) {
+  ExtBuf b;
+  int rc = ext_prepare(lat, Nt, at, gsq, A, b, st);
+  if (rc) return rc;
+  const DeviceLattice& D = lat->dev;
+  const long long nsp = (long long)Nt * D.Nf;
+  return reduce(int(nsp + (long long)Nt * D.Nl), ExtAction{b.ths, b.tht, b.bs, b.bt, nsp, D.Nf, D.Nl},
+                lat->gauge.part, S, st);
+}
+
+int ext_gauge_force(qed3_lattice_s* lat, int Nt, double at, double gsq, const double* A, double* F, cudaStream_t st) {
+  ExtBuf b;
+  int rc = ext_prepare(lat, Nt, at, gsq, A, b, st);
+  if (rc) return rc;
+  const DeviceLattice& D = lat->dev;
+  const GaugeDev& G = lat->gauge;
+  k_ext_force_s<<<nblk((long long)Nt * D.Nl), 256, 0, st>>>(Nt, D.Nl, D.Nf, G.link_face, G.link_fsign, b.ths, b.tht,
+                                                           b.bs, b.bt, F);
+  k_ext_force_t<<<nblk((long long)Nt * D.Ns), 256, 0, st>>>(Nt, D.Nl, D.Ns, D.hop_link, D.hop_sign, D.perm, b.tht,
+                                                           b.bt, F);
+  QED3_CUDA_TRY(cudaGetLastError());
+  QED3_CUDA_TRY(cudaStreamSynchronize(st));
+  return QED3_OK;
+}
+
+int ext_polyakov(qed3_lattice_s* lat, int Nt, const double* A, double* P, double* avg, cudaStream_t st) {
+  int rc = gauge_prepare(lat);
+  if (rc) return rc;
+  const DeviceLattice& D = lat->dev;
+  double* buf = P;
+  if (!buf) QED3_CUDA_TRY(cudaMalloc(&buf, size_t(D.Ns) * 2 * sizeof(double)));
+  k_ext_polyakov<<<nblk(D.Ns), 256, 0, st>>>(Nt, D.Nl, D.Ns, A, buf);
+  QED3_CUDA_TRY(cudaGetLastError());
+  if (avg) {
+    std::vector<double> h(size_t(D.Ns) * 2);
+    QED3_CUDA_TRY(cudaMemcpyAsync(h.data(), buf, h.size() * sizeof(double), cudaMemcpyDeviceToHost, st));
+    QED3_CUDA_TRY(cudaStreamSynchronize(st));
+    double re = 0, im = 0;
+    for (int x = 0; x < D.Ns; x++) {
+      re += h[2 * x];
+      im += h[2 * x + 1];
+    }
+    avg[0] = re / D.Ns;
+    avg[1] = im / D.Ns;
+  }
+  if (!P) cudaFree(buf);
+  return QED3_OK;
+}
+
+}  // namespace qed3

@@ -31,6 +31,10 @@ int hmc_overlap(qed3_lattice_s* lat, qed3_overlap_s* ov, qed3_rng_s* rng, double
                 int exact, double tmax, int nsteps, int nsteps_inner, int npf, int integrator, double lmin, double lmax,
                 double tol, double tol_inner, int no_reject, int* accepted, double* dH_out, int* cg_iters,
                 cudaStream_t st);
+int ext_plaquettes(qed3_lattice_s* lat, int Nt, const double* A, double* ths, double* tht, cudaStream_t st);
+int ext_gauge_action(qed3_lattice_s* lat, int Nt, double at, double gsq, const double* A, double* S, cudaStream_t st);
+int ext_gauge_force(qed3_lattice_s* lat, int Nt, double at, double gsq, const double* A, double* F, cudaStream_t st);
+int ext_polyakov(qed3_lattice_s* lat, int Nt, const double* A, double* P, double* avg, cudaStream_t st);
 int hmc_pure_gauge(qed3_lattice_s* lat, qed3_rng_s* rng, double* A, double beta, int compact, int exact, double tmax,
                    int nsteps, int no_reject, int* accepted, double* dH, cudaStream_t st);
 }  // namespace qed3

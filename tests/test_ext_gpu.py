@@ -69,3 +69,29 @@ def test_ext_cg_solve(cuda, shift):
     x = from_dev(xt)
     r = b - O.dirac_ext_apply(g, 1.0, 0.1, Nt, at, A, x, 2) - shift * x
     assert np.linalg.norm(r) / np.linalg.norm(b) <= 1.05e-10
+
+
+@pytest.mark.parametrize("n,Nt", [(2, 3), (4, 4)])
+def test_ext_gauge_side_matches_oracle(cuda, n, Nt):
+    """Anisotropic action, force (same update order as the reference: the
+    spatial and temporal forces bit for bit) and Polyakov loop."""
+    import torch
+    g = O.geometry(n)
+    lat = Q.S2Trivalent(n)
+    at, gsq = 0.6, 0.4
+    A = np.random.default_rng(n + Nt).normal(size=Nt * (g.n_links + g.n_sites)) * 0.5
+    ths_o, tht_o, S_o, F_o = O.ext_gauge(g, Nt, at, gsq, A)
+    At = to_dev(A, cuda)
+    ths = torch.zeros(Nt * lat.n_faces, dtype=torch.float64, device=cuda)
+    tht = torch.zeros(Nt * lat.n_links, dtype=torch.float64, device=cuda)
+    Q.ext_plaquettes(lat, Nt, At, ths, tht)
+    assert np.array_equal(from_dev(ths), ths_o.ravel()) and np.array_equal(from_dev(tht), tht_o.ravel())
+    S = Q.ext_gauge_action(lat, Nt, at, gsq, At)
+    assert abs(S - S_o) < 1e-13 * abs(S_o)
+    F = torch.zeros_like(At)
+    Q.ext_gauge_force(lat, Nt, at, gsq, At, F)
+    assert np.array_equal(from_dev(F), F_o)
+    P = torch.zeros(lat.n_sites, dtype=torch.complex128, device=cuda)
+    avg = Q.ext_polyakov(lat, Nt, At, P)
+    Po = O.ext_polyakov(g, Nt, A)
+    assert np.abs(from_dev(P) - Po).max() < 1e-15 and abs(avg - Po.mean()) < 1e-14

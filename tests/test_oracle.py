@@ -367,3 +367,21 @@ def test_ext_operator_restatement():
         assert np.abs(Md - M.conj().T).max() < 1e-13
         w = np.linalg.eigvalsh(M.conj().T @ M)
         assert w[0] > 0
+
+
+def test_ext_gauge_force_is_the_action_gradient():
+    """U1WilsonExt restated: the force is the finite-difference gradient of
+    the action in spatial and temporal angles."""
+    g = O.geometry(2)
+    Nt, at, gsq = 3, 0.6, 0.4
+    rng = np.random.default_rng(9)
+    A = rng.normal(size=Nt * (g.n_links + g.n_sites)) * 0.3
+    _, _, S, F = O.ext_gauge(g, Nt, at, gsq, A)
+    h = 1e-6
+    for k in list(rng.choice(Nt * g.n_links, 4, replace=False)) + list(Nt * g.n_links + rng.choice(Nt * g.n_sites, 4,
+                                                                                                       replace=False)):
+        Ap, Am = A.copy(), A.copy()
+        Ap[k] += h
+        Am[k] -= h
+        fd = (O.ext_gauge(g, Nt, at, gsq, Ap)[2] - O.ext_gauge(g, Nt, at, gsq, Am)[2]) / (2 * h)
+        assert abs(fd - F[k]) < 1e-6 * max(1.0, abs(F[k])), (k, fd, F[k])
