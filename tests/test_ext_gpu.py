@@ -73,8 +73,8 @@ def test_ext_cg_solve(cuda, shift):
 
 @pytest.mark.parametrize("n,Nt", [(2, 3), (4, 4)])
 def test_ext_gauge_side_matches_oracle(cuda, n, Nt):
-    """Anisotropic action, force (same update order as the reference: the
-    spatial and temporal forces bit for bit) and Polyakov loop."""
+    """Anisotropic action, force (the reference's update order) and Polyakov
+    loop; plaquette angles bit for bit."""
     import torch
     g = O.geometry(n)
     lat = Q.S2Trivalent(n)
@@ -90,7 +90,8 @@ def test_ext_gauge_side_matches_oracle(cuda, n, Nt):
     assert abs(S - S_o) < 1e-13 * abs(S_o)
     F = torch.zeros_like(At)
     Q.ext_gauge_force(lat, Nt, at, gsq, At, F)
-    assert np.array_equal(from_dev(F), F_o)
+    # same update order as the reference; the device contracts a*b+c into FMAs
+    assert np.abs(from_dev(F) - F_o).max() < 1e-13 * np.abs(F_o).max()
     P = torch.zeros(lat.n_sites, dtype=torch.complex128, device=cuda)
     avg = Q.ext_polyakov(lat, Nt, At, P)
     Po = O.ext_polyakov(g, Nt, A)
