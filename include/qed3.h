@@ -221,6 +221,10 @@ int qed3_dirac_ext_destroy(qed3_dirac_ext* e);
 int qed3_dirac_ext_set_links(qed3_dirac_ext* e, const double* A, void* stream);
 /* op: QED3_OP_D, _DDAG, _DDAGD, _DDDAG; in may equal out for D and D^dag */
 int qed3_dirac_ext_apply(qed3_dirac_ext* e, int op, double* out, const double* in, void* stream);
+/* Fermion force F = -2 Re <D eta, dD/dA eta> for every spatial and temporal
+ * link (DiracExt::d_coo_format, src/both_3d/dirac_ext.h:234-320), F in the
+ * link layout; eta device complex128 [Nt][Ns][2]. */
+int qed3_dirac_ext_fermion_force(qed3_dirac_ext* e, const double* eta, double* F, void* stream);
 /* MatPoly::solve on D^dag D (+ params->shift) in FP64, certified by the true residual */
 int qed3_dirac_ext_cg_solve(qed3_dirac_ext* e, double* x, const double* b, const qed3_solve_params* params,
                             qed3_solve_report* report, void* stream);

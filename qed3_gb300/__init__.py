@@ -133,6 +133,7 @@ SIGNATURES = [
     ("qed3_dirac_ext_destroy", ctypes.c_int, [vp]),
     ("qed3_dirac_ext_set_links", ctypes.c_int, [vp, vp, vp]),
     ("qed3_dirac_ext_apply", ctypes.c_int, [vp, ctypes.c_int, vp, vp, vp]),
+    ("qed3_dirac_ext_fermion_force", ctypes.c_int, [vp, vp, vp, vp]),
     ("qed3_dirac_ext_cg_solve", ctypes.c_int, [vp, vp, vp, ctypes.POINTER(SolveParams), ctypes.POINTER(SolveReport),
                                                vp]),
     ("qed3_ext_plaquettes", ctypes.c_int, [vp, ctypes.c_int, vp, vp, vp, vp]),
@@ -605,6 +606,11 @@ class DiracExt:
     def apply(self, out, inp, op: int = OP_D, stream=None):
         _check(lib().qed3_dirac_ext_apply(self._h, op, _ptr(out), _ptr(inp), _stream(stream)))
         return out
+
+    def fermion_force(self, eta, F, stream=None):
+        """F (device, link layout) = -2 Re <D eta, dD/dA eta>."""
+        _check(lib().qed3_dirac_ext_fermion_force(self._h, _ptr(eta), _ptr(F), _stream(stream)))
+        return F
 
     def solve(self, x, b, tol: float = 1e-10, maxiter: int = 100000, shift: float = 0.0, stream=None) -> Report:
         p = SolveParams(tol, maxiter, PREC_F64, 0.1, shift, 0)

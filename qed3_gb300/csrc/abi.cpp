@@ -303,6 +303,13 @@ int qed3_dirac_ext_apply(qed3_dirac_ext* e, int op, double* out, const double* i
   QED3_GUARD_END
 }
 
+int qed3_dirac_ext_fermion_force(qed3_dirac_ext* e, const double* eta, double* F, void* stream) {
+  QED3_GUARD_BEGIN
+  if (!e || !eta || !F) return fail(QED3_ERR_ARG, "NULL argument");
+  return ext_fermion_force(e, eta, F, (cudaStream_t)stream);
+  QED3_GUARD_END
+}
+
 int qed3_dirac_ext_cg_solve(qed3_dirac_ext* e, double* x, const double* b, const qed3_solve_params* params,
                             qed3_solve_report* report, void* stream) {
   QED3_GUARD_BEGIN

@@ -108,6 +108,58 @@ __global__ void k_ext_apply(int Ns, int Nt, int adj, const int32_t* __restrict__
   st64(out + size_t(s) * Ns, x, o);
 }
 
+// Fermion force F = -2 Re <D eta, dD/dA eta> for every link (DiracExt::
+// d_coo_format, src/both_3d/dirac_ext.h:234-320); eta, D eta in reference order.
+// Spatial link l = (x -> y) of slice s: i H_xy(s) at (x, y) and -i H_yx(s) at (y, x).
+__global__ void k_ext_force_sp(int Ns, int Nl, int Nt, const int32_t* __restrict__ lx,
+                               const int32_t* __restrict__ ly, const int8_t* __restrict__ kx,
+                               const int8_t* __restrict__ ky, const int32_t* __restrict__ perm,
+                               const M64* __restrict__ H3, const S64* __restrict__ eta, const S64* __restrict__ deta,
+                               double* __restrict__ F) {
+  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= (long long)Nl * Nt) return;
+  const int s = int(idx / Nl), l = int(idx % Nl);
+  const int x = lx[l], y = ly[l];
+  const M64 hxy = H3[(size_t(s) * 3 + kx[l]) * Ns + x], hyx = H3[(size_t(s) * 3 + ky[l]) * Ns + y];
+  const S64* es = eta + size_t(s) * Ns;
+  const S64* ds = deta + size_t(s) * Ns;
+  const int xr = perm[x], yr = perm[y];
+  const Sp64 ex = ld64(es, xr), ey = ld64(es, yr), dx = ld64(ds, xr), dy = ld64(ds, yr);
+  const double2 u0 = cfma(hxy.h01, ey.s1, cmul(hxy.h00, ey.s0));
+  const double2 u1 = cfma(hxy.h11, ey.s1, cmul(hxy.h10, ey.s0));
+  const double2 v0 = cfma(hyx.h01, ex.s1, cmul(hyx.h00, ex.s0));
+  const double2 v1 = cfma(hyx.h11, ex.s1, cmul(hyx.h10, ex.s0));
+  // Re[conj(a) (i b)] = a.y b.x - a.x b.y
+  auto re_ci = [](double2 a, double2 b) { return a.y * b.x - a.x * b.y; };
+  F[idx] = -2.0 * (re_ci(dx.s0, u0) + re_ci(dx.s1, u1) - re_ci(dy.s0, v0) - re_ci(dy.s1, v1));
+}
+
+// Temporal link (s, x) from (x, s) to (x, s+1): D[(x,s+1),(x,s)] = tmpP(s) ~ e^{-iA}
+// and D[(x,s),(x,s+1)] = tmpM(s+1) ~ e^{+iA}, both with the sign -1 at s = Nt-1:
+//   F = -2 Re[ (D eta)_{s+1}^dag (-i tmpP eta_s) + (D eta)_s^dag (i tmpM eta_{s+1}) ]
+__global__ void k_ext_force_tp(int Ns, int Nl, int Nt, const int32_t* __restrict__ perm,
+                               const double* __restrict__ kt, const double* __restrict__ At, double r,
+                               const S64* __restrict__ eta, const S64* __restrict__ deta, double* __restrict__ F) {
+  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= (long long)Ns * Nt) return;
+  const int s = int(idx / Ns), i = int(idx % Ns);
+  const int x = perm[i], s1 = (s + 1) % Nt;
+  const double sg = (s == Nt - 1) ? -1.0 : 1.0;
+  const double kh = 0.5 * kt[i] * sg;
+  double sn, cs;
+  sincos(At[size_t(s) * Ns + x], &sn, &cs);
+  const Sp64 e0 = ld64(eta + size_t(s) * Ns, x), e1 = ld64(eta + size_t(s1) * Ns, x);
+  const Sp64 d0 = ld64(deta + size_t(s) * Ns, x), d1 = ld64(deta + size_t(s1) * Ns, x);
+  // tmpP eta_s: spin-diagonal (-r-1, -r+1) kh e^{-iA};  tmpM eta_{s+1}: (-r+1, -r-1) kh e^{+iA}
+  const double2 pm = make_double2(cs, -sn), pp = make_double2(cs, sn);
+  const double2 a0 = cscale(kh * (-r - 1.0), cmul(pm, e0.s0)), a1 = cscale(kh * (-r + 1.0), cmul(pm, e0.s1));
+  const double2 b0 = cscale(kh * (-r + 1.0), cmul(pp, e1.s0)), b1 = cscale(kh * (-r - 1.0), cmul(pp, e1.s1));
+  auto re_ci = [](double2 a, double2 b) { return a.y * b.x - a.x * b.y; };  // Re[conj(a) (i b)]
+  // (D eta)_{s+1}^dag (-i a) = -Re[conj(d1) (i a)];  (D eta)_s^dag (i b)
+  const double inner = -(re_ci(d1.s0, a0) + re_ci(d1.s1, a1)) + re_ci(d0.s0, b0) + re_ci(d0.s1, b1);
+  F[size_t(Nt) * Nl + size_t(s) * Ns + x] = -2.0 * inner;
+}
+
 int ext_init(qed3_dirac_ext_s* e) {
   qed3_dirac_s* d = e->d2;
   const HostLattice& L = d->lat->host;
@@ -178,6 +230,25 @@ int ext_apply(qed3_dirac_ext_s* e, int op, double* out, const double* in, cudaSt
   } else {
     return fail(QED3_ERR_ARG, "unknown operator");
   }
+  QED3_CUDA_TRY(cudaGetLastError());
+  return QED3_OK;
+}
+
+int ext_fermion_force(qed3_dirac_ext_s* e, const double* eta, double* F, cudaStream_t st) {
+  if (!e->links_set) return fail(QED3_ERR_STATE, "call qed3_dirac_ext_set_links first");
+  qed3_dirac_s* d = e->d2;
+  const DeviceLattice& D = d->lat->dev;
+  const int Ns = d->Ns, Nl = D.Nl, Nt = e->Nt;
+  S64* deta = reinterpret_cast<S64*>(e->work);  // D eta (the CG vectors are not in use here)
+  int rc = ext_apply(e, QED3_OP_D, reinterpret_cast<double*>(deta), eta, st);
+  if (rc) return rc;
+  const S64* et = reinterpret_cast<const S64*>(eta);
+  k_ext_force_sp<<<nblk((long long)Nl * Nt), 256, 0, st>>>(Ns, Nl, Nt, D.link_x, D.link_y, D.link_kx, D.link_ky, D.perm,
+                                                          e->H3, et, deta, F);
+  if (Nt > 1)
+    k_ext_force_tp<<<nblk((long long)Ns * Nt), 256, 0, st>>>(Ns, Nl, Nt, D.perm, e->kt, e->At, d->r, et, deta, F);
+  else
+    QED3_CUDA_TRY(cudaMemsetAsync(F + size_t(Nt) * Nl, 0, size_t(Ns) * sizeof(double), st));
   QED3_CUDA_TRY(cudaGetLastError());
   return QED3_OK;
 }

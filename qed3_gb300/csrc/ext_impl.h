@@ -24,6 +24,7 @@ int ext_init(qed3_dirac_ext_s* e);
 void ext_free(qed3_dirac_ext_s* e);
 int ext_set_links(qed3_dirac_ext_s* e, const double* A, cudaStream_t st);
 int ext_apply(qed3_dirac_ext_s* e, int op, double* out, const double* in, cudaStream_t st);
+int ext_fermion_force(qed3_dirac_ext_s* e, const double* eta, double* F, cudaStream_t st);
 int ext_cg(qed3_dirac_ext_s* e, double* x, const double* b, const qed3_solve_params* prm, qed3_solve_report* rep,
            cudaStream_t st);
 }  // namespace qed3

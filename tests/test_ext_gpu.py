@@ -96,3 +96,33 @@ def test_ext_gauge_side_matches_oracle(cuda, n, Nt):
     avg = Q.ext_polyakov(lat, Nt, At, P)
     Po = O.ext_polyakov(g, Nt, A)
     assert np.abs(from_dev(P) - Po).max() < 1e-15 and abs(avg - Po.mean()) < 1e-14
+
+
+@pytest.mark.parametrize("Nt", [1, 2, 3])
+def test_ext_fermion_force_is_the_derivative(cuda, Nt):
+    """F = -2 Re <D eta, dD/dA eta> = -d/dA <eta, D^dag D eta> (eta fixed), for
+    spatial and temporal links, against finite differences of the oracle's
+    restatement of the operator."""
+    import torch
+    n, at = 2, 0.8
+    g = O.geometry(n)
+    lat = Q.S2Trivalent(n)
+    rng = np.random.default_rng(40 + Nt)
+    A = rng.uniform(-np.pi, np.pi, Nt * (g.n_links + g.n_sites))
+    eta = rng.normal(size=2 * g.n_sites * Nt) + 1j * rng.normal(size=2 * g.n_sites * Nt)
+    De = Q.DiracExt(lat, 1.0, 0.1, Nt, at)
+    De.update(to_dev(A, cuda))
+    F = torch.zeros(A.size, dtype=torch.float64, device=cuda)
+    De.fermion_force(to_dev(eta, cuda), F)
+    F = from_dev(F)
+    f = lambda B: np.vdot(eta, O.dirac_ext_apply(g, 1.0, 0.1, Nt, at, B, eta, 2)).real
+    h = 1e-6
+    nsp = Nt * g.n_links
+    picks = list(rng.choice(nsp, 6, replace=False))
+    picks += list(nsp + rng.choice(Nt * g.n_sites, 6, replace=False)) if Nt > 1 else [nsp]
+    for k in picks:
+        Ap, Am = A.copy(), A.copy()
+        Ap[k] += h
+        Am[k] -= h
+        fd = -(f(Ap) - f(Am)) / (2 * h)
+        assert abs(fd - F[k]) < 1e-6 * max(1.0, abs(fd)), (k, fd, F[k])
