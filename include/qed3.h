@@ -351,6 +351,15 @@ int qed3_hmc_overlap(qed3_lattice* lat, qed3_overlap* ov, qed3_rng* rng, double*
                      int* cg_iters, void* stream);
 int qed3_hmc_pure_gauge(qed3_lattice* lat, qed3_rng* rng, double* A, double beta, int compact, int exact,
                         double tmax, int nsteps, int no_reject, int* accepted, double* dH, void* stream);
+/* One S^2 x S^1 HMC trajectory on the device links A (in place): HMC2::run
+ * with the anisotropic gauge action (at, gsq) and npf Wilson pseudofermions
+ * of the S^2 x S^1 operator e, QED3_INTEGRATOR_LEAPFROG_ML or _LEAPFROG; rng must hold
+ * Nt n_links link engines and Nt n_sites site engines (ParallelRngExt's
+ * layout: spatial momenta from the link engines, temporal momenta and the
+ * pseudofermion sources from the site engines); solves in FP64 to tol. */
+int qed3_hmc_ext(qed3_dirac_ext* e, qed3_rng* rng, double* A, double at, double gsq, double tmax, int nsteps,
+                 int nsteps_inner, int npf, int integrator, double tol, int no_reject, int* accepted, double* dH,
+                 int* cg_iters, void* stream);
 
 /* ======================================================================
  * Overlap operator  --  replaces Overlap<WilsonDirac> (src/both_3d/overlap.h:137-390):

@@ -1045,6 +1045,10 @@ void orc_rng_destroy(OracleRng* r) { delete r; }
 void orc_rng_gaussian_links(OracleRng* r, double width, double* out) {
   for (size_t l = 0; l < r->links.size(); l++) out[l] = width * r->links[l].g(r->links[l].mt);
 }
+// GaugeExt::gaussian's temporal part (src/both_3d/gauge_ext.h:145-149)
+void orc_rng_gaussian_sites(OracleRng* r, double width, double* out) {
+  for (size_t x = 0; x < r->sites.size(); x++) out[x] = width * r->sites[x].g(r->sites[x].mt);
+}
 // fill_gaussian, src/both_3d/rng.h:122-129: (g + i g)/sqrt(2) per spin
 void orc_rng_gaussian_spinor(OracleRng* r, double* out) {
   for (size_t x = 0; x < r->sites.size(); x++)
@@ -1211,12 +1215,13 @@ int orc_hmc_fermion(const OracleGeom* g, OracleDirac* d, OracleRng* rng, double*
 // (src/both_3d/dirac_ext.h:234-269): F_l = -2 Re <D eta, (dD/dA_l) eta>,
 // dD/dA_l = i H_xy at (x,y) and -i H_yx at (y,x) for links[l] = (x,y).
 // ===========================================================================
-void orc_fermion_force(const OracleDirac* d, const OracleGeom* g, const double* A, const double* eta_in,
-                       double* F) {
-  const Idx N = d->N;
+// F_l = -2 Re <chi, dD/dA_l eta> for a given chi; chi = D eta is the fermion
+// force of one pseudofermion, another chi the same derivative of a larger
+// operator whose blocks are D (one time slice of DiracExt).
+void orc_fermion_force_chi(const OracleDirac* d, const OracleGeom* g, const double* A, const double* chi_in,
+                           const double* eta_in, double* F) {
   const cplx* eta = reinterpret_cast<const cplx*>(eta_in);
-  std::vector<cplx> Deta(N);
-  csr_mult(d, false, Deta.data(), eta);
+  const cplx* Deta = reinterpret_cast<const cplx*>(chi_in);
   const cplx I(0.0, 1.0);
   const Idx Nl = Idx(g->links.size());
 #pragma omp parallel for schedule(static)
@@ -1236,6 +1241,13 @@ void orc_fermion_force(const OracleDirac* d, const OracleGeom* g, const double* 
                        std::conj(Deta[2 * y]) * dy0 + std::conj(Deta[2 * y + 1]) * dy1;
     F[l] = -2.0 * inner.real();
   }
+}
+
+void orc_fermion_force(const OracleDirac* d, const OracleGeom* g, const double* A, const double* eta_in,
+                       double* F) {
+  std::vector<cplx> Deta(d->N);
+  csr_mult(d, false, Deta.data(), reinterpret_cast<const cplx*>(eta_in));
+  orc_fermion_force_chi(d, g, A, reinterpret_cast<const double*>(Deta.data()), eta_in, F);
 }
 
 int orc_num_threads() {

@@ -72,6 +72,7 @@ def lib():
         L.orc_rng_destroy.argtypes = [vp]
         L.orc_rng_gaussian_links.argtypes = [vp, ctypes.c_double, c_double_p]
         L.orc_rng_gaussian_spinor.argtypes = [vp, ctypes.c_void_p]
+        L.orc_rng_gaussian_sites.argtypes = [vp, ctypes.c_double, c_double_p]
         L.orc_rng_z2_spinor.argtypes = [vp, ctypes.c_void_p]
         L.orc_rng_uniform.restype = ctypes.c_double
         L.orc_rng_uniform.argtypes = [vp]
@@ -79,6 +80,7 @@ def lib():
         L.orc_hmc_pure_gauge.argtypes = [vp, vp, c_double_p, ctypes.c_double, ctypes.c_int, ctypes.c_int,
                                          ctypes.c_double, ctypes.c_int, ctypes.c_int, c_double_p]
         L.orc_fermion_force.argtypes = [vp, vp, c_double_p, ctypes.c_void_p, c_double_p]
+        L.orc_fermion_force_chi.argtypes = [vp, vp, c_double_p, ctypes.c_void_p, ctypes.c_void_p, c_double_p]
         L.orc_num_threads.restype = ctypes.c_int
         L.orc_hmc_fermion.restype = ctypes.c_int
         L.orc_hmc_fermion.argtypes = [vp, vp, vp, vp, ctypes.c_double, ctypes.c_int, ctypes.c_int, ctypes.c_double,
@@ -237,6 +239,15 @@ class Dirac:
         lib().orc_fermion_force(self.h, self.geom.handle, _dp(A), _p(eta), _dp(F))
         return F
 
+    def fermion_force_chi(self, A: np.ndarray, chi: np.ndarray, eta: np.ndarray) -> np.ndarray:
+        """F_l = -2 Re <chi, dD/dA_l eta> (fermion_force with D eta replaced by chi)."""
+        A = np.ascontiguousarray(A, dtype=np.float64)
+        chi = np.ascontiguousarray(chi, dtype=np.complex128)
+        eta = np.ascontiguousarray(eta, dtype=np.complex128)
+        F = np.zeros(self.geom.n_links)
+        lib().orc_fermion_force_chi(self.h, self.geom.handle, _dp(A), _p(chi), _p(eta), _dp(F))
+        return F
+
     def overlap(self, v: np.ndarray, lmin: float, lmax: float, order: int = 21, op: int = 0,
                 tol_inner: float = 1e-12) -> np.ndarray:
         """Overlap::mult (op 0) / adj (1) / DHD (2) restated, CG per pole."""
@@ -304,23 +315,32 @@ def gauge_force(geom: Geometry, A, beta: float, compact: bool = True, exact: boo
 class Rng:
     """ParallelRng2 restated: master mt19937_64 seeds per-link then per-site engines."""
 
-    def __init__(self, geom: Geometry, seed: int):
+    def __init__(self, geom: Geometry, seed: int, n_slices: int = 1):
+        """n_slices > 1: ParallelRngExt (src/both_3d/rng.h:89-121), engines
+        [Nt][n_links] and [Nt][n_sites] seeded in that order (flat order = the
+        layout of one ParallelRng2 with Nt times as many links and sites)."""
         self.geom = geom
-        self.h = lib().orc_rng_create(geom.n_links, geom.n_sites, seed)
+        self.nl, self.ns = geom.n_links * n_slices, geom.n_sites * n_slices
+        self.h = lib().orc_rng_create(self.nl, self.ns, seed)
 
     def gaussian_links(self, width=1.0):
-        out = np.zeros(self.geom.n_links)
+        out = np.zeros(self.nl)
         lib().orc_rng_gaussian_links(self.h, width, _dp(out))
         return out
 
+    def gaussian_sites(self, width=1.0):
+        out = np.zeros(self.ns)
+        lib().orc_rng_gaussian_sites(self.h, width, _dp(out))
+        return out
+
     def gaussian_spinor(self):
-        out = np.zeros(2 * self.geom.n_sites, np.complex128)
+        out = np.zeros(2 * self.ns, np.complex128)
         lib().orc_rng_gaussian_spinor(self.h, _p(out))
         return out
 
     def z2_spinor(self):
         """FermionVector::set_random (src/dual/valence.h:54-60)."""
-        out = np.zeros(2 * self.geom.n_sites, dtype=np.complex128)
+        out = np.zeros(2 * self.ns, dtype=np.complex128)
         lib().orc_rng_z2_spinor(self.h, _p(out))
         return out
 
@@ -601,3 +621,146 @@ def ext_polyakov(geom: Geometry, Nt: int, A: np.ndarray) -> np.ndarray:
             a += tp[s][x]
         out[x] = np.exp(1j * a)
     return out
+
+
+def _ext_temporal(geom: Geometry, r: float, Nt: int, at: float, At: np.ndarray):
+    """The temporal COO entries of DiracExt (src/both_3d/dirac_ext.h:121-213):
+    column slice s couples to row slice s+1 by tmpP[s] and to s-1 by tmpM[s]
+    (spin-diagonal, [Nt][Ns][2]), antiperiodic across the boundary."""
+    kt = triangle_areas(geom) / geom.mean_ell / at
+    sig3 = np.array([1.0, -1.0])
+    tmpP = np.empty((Nt, geom.n_sites, 2), np.complex128)
+    tmpM = np.empty_like(tmpP)
+    for s in range(Nt):
+        sP = -1.0 if s == Nt - 1 else 1.0
+        sM = -1.0 if s == 0 else 1.0
+        tmpP[s] = 0.5 * sP * kt[:, None] * (-r - sig3)[None, :] * np.exp(-1j * At[s])[:, None]
+        tmpM[s] = 0.5 * sM * kt[:, None] * (-r + sig3)[None, :] * np.exp(1j * At[(s - 1) % Nt])[:, None]
+    return kt, tmpP, tmpM
+
+
+def dirac_ext_matrix(geom: Geometry, r: float, M5: float, Nt: int, at: float, A: np.ndarray) -> np.ndarray:
+    """The dense DiracExt matrix, the same entries as dirac_ext_apply (op 0)."""
+    Ns, Nl = geom.n_sites, geom.n_links
+    As = np.asarray(A[:Nt * Nl]).reshape(Nt, Nl)
+    At = np.asarray(A[Nt * Nl:Nt * (Nl + Ns)]).reshape(Nt, Ns)
+    n2 = 2 * Ns
+    M = np.zeros((Nt * n2, Nt * n2), np.complex128)
+    D = Dirac(geom, r, M5)
+    kt, tmpP, tmpM = _ext_temporal(geom, r, Nt, at, At) if Nt > 1 else (np.zeros(Ns), None, None)
+    for s in range(Nt):
+        D.update(As[s])
+        M[s * n2:(s + 1) * n2, s * n2:(s + 1) * n2] = D.dense() + np.diag(np.repeat(r * kt, 2))
+    if Nt > 1:
+        idx = np.arange(n2)
+        for s in range(Nt):
+            up, dn = (s + 1) % Nt, (s - 1) % Nt
+            M[up * n2 + idx, s * n2 + idx] += tmpP[s].reshape(-1)
+            M[dn * n2 + idx, s * n2 + idx] += tmpM[s].reshape(-1)
+    return M
+
+
+def ext_fermion_force(geom: Geometry, r: float, M5: float, Nt: int, at: float, A: np.ndarray, eta: np.ndarray,
+                      M: np.ndarray | None = None) -> np.ndarray:
+    """F = -2 Re <D eta, dD/dA eta> of DiracExt in A's layout: spatial links of
+    slice s by the dual-lattice force with chi = (D eta)_s; temporal link (s, x)
+    from its two entries, tmpP[s] (row s+1, column s, phase e^{-i A_t}) and
+    tmpM[s+1] (row s, column s+1, phase e^{+i A_t})."""
+    Ns, Nl = geom.n_sites, geom.n_links
+    n2 = 2 * Ns
+    M = dirac_ext_matrix(geom, r, M5, Nt, at, A) if M is None else M
+    eta = np.asarray(eta, np.complex128)
+    chi = M @ eta
+    As = np.asarray(A[:Nt * Nl]).reshape(Nt, Nl)
+    At = np.asarray(A[Nt * Nl:Nt * (Nl + Ns)]).reshape(Nt, Ns)
+    D = Dirac(geom, r, M5)
+    Fs = np.zeros((Nt, Nl))
+    for s in range(Nt):
+        D.update(As[s])
+        Fs[s] = D.fermion_force_chi(As[s], chi[s * n2:(s + 1) * n2], eta[s * n2:(s + 1) * n2])
+    Ft = np.zeros((Nt, Ns))
+    if Nt > 1:
+        _, tmpP, tmpM = _ext_temporal(geom, r, Nt, at, At)
+        e3, c3 = eta.reshape(Nt, Ns, 2), chi.reshape(Nt, Ns, 2)
+        for s in range(Nt):
+            up = (s + 1) % Nt
+            t = (np.conj(c3[up]) * (-1j) * tmpP[s] * e3[s]).sum(1) + (np.conj(c3[s]) * 1j * tmpM[up] * e3[up]).sum(1)
+            Ft[s] = -2.0 * t.real
+    return np.concatenate([Fs.ravel(), Ft.ravel()])
+
+
+def hmc_ext(geom: Geometry, rng: Rng, A: np.ndarray, r: float, M5: float, Nt: int, at: float, gsq: float,
+            tmax: float = 1.0, nsteps: int = 4, nsteps_inner: int = 4, npf: int = 1, integrator: int = 0,
+            tol: float = 1e-12, no_reject: bool = False):
+    """HMC2::run (src/both_3d/hmc.h:172-200) on S^2 x S^1 with U1WilsonExt and
+    npf DiracExt pseudofermions; ExplicitLeapfrogML (src/both_3d/integrator.h:117-168)
+    or, integrator = 1, ExplicitLeapfrog.  rng = Rng(geom, seed, Nt): momenta by
+    GaugeExt::gaussian (src/both_3d/gauge_ext.h:146-149), sources by
+    ParallelRngExt::fill_gaussian.  eta = (D^dag D)^{-1} phi by CG on the dense
+    operator.  A updated in place; returns (accepted, dH, CG iterations)."""
+    Ns, Nl = geom.n_sites, geom.n_links
+    pi = np.concatenate([rng.gaussian_links(1.0), rng.gaussian_sites(1.0)])
+    xis = [rng.gaussian_spinor() for _ in range(npf)]
+    A0 = A.copy()
+    st = {"M": dirac_ext_matrix(geom, r, M5, Nt, at, A)}
+    its = [0]
+
+    def solve(b):
+        M = st["M"]
+        x = np.zeros_like(b)
+        rr_ = b.copy()
+        p = rr_.copy()
+        bb = np.vdot(b, b).real
+        rr = bb
+        while rr > tol * tol * bb:
+            q = M.conj().T @ (M @ p)
+            al = rr / np.vdot(p, q).real
+            x += al * p
+            rr_ -= al * q
+            rn = np.vdot(rr_, rr_).real
+            its[0] += 1
+            p = rr_ + (rn / rr) * p
+            rr = rn
+        return x
+
+    phis = [st["M"].conj().T @ xi for xi in xis]
+    etas = [solve(ph) for ph in phis]
+
+    def H():
+        return (0.5 * float(np.dot(pi, pi)) + ext_gauge(geom, Nt, at, gsq, A)[2]
+                + sum(np.vdot(ph, et).real for ph, et in zip(phis, etas)))
+
+    def update():
+        st["M"] = dirac_ext_matrix(geom, r, M5, Nt, at, A)
+        for k in range(npf):
+            etas[k] = solve(phis[k])
+
+    gforce = lambda: ext_gauge(geom, Nt, at, gsq, A)[3]
+    fforce = lambda k: ext_fermion_force(geom, r, M5, Nt, at, A, etas[k], st["M"])
+    h0 = H()
+    tau = tmax / nsteps
+    tau_in = tau / nsteps_inner
+    if integrator == 1:
+        for n in range(nsteps):
+            pi -= 0.5 * tau * (gforce() + sum(fforce(k) for k in range(npf)))
+            A += tau * pi
+            update()
+            pi -= 0.5 * tau * (gforce() + sum(fforce(k) for k in range(npf)))
+    else:
+        for k in range(npf):
+            pi -= 0.5 * tau * fforce(k)
+        for n in range(nsteps):
+            pi -= 0.5 * tau_in * gforce()
+            for m in range(nsteps_inner):
+                A += tau_in * pi
+                pi -= (1.0 if m != nsteps_inner - 1 else 0.5) * tau_in * gforce()
+            update()
+            for k in range(npf):
+                pi -= (1.0 if n != nsteps - 1 else 0.5) * tau * fforce(k)
+    h1 = H()
+    dH = h1 - h0
+    a = rng.uniform()
+    if a < min(1.0, np.exp(-dH)) or no_reject:
+        return True, dH, its[0]
+    A[:] = A0
+    return False, dH, its[0]

@@ -131,6 +131,9 @@ SIGNATURES = [
     ("qed3_dirac_ext_create", ctypes.c_int, [vp, ctypes.c_double, ctypes.c_double, ctypes.c_int, ctypes.c_double,
                                              ctypes.POINTER(vp)]),
     ("qed3_dirac_ext_destroy", ctypes.c_int, [vp]),
+    ("qed3_hmc_ext", ctypes.c_int, [vp, vp, vp, ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_int,
+                                    ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_int, c_int_p,
+                                    c_double_p, c_int_p, vp]),
     ("qed3_dirac_ext_set_links", ctypes.c_int, [vp, vp, vp]),
     ("qed3_dirac_ext_apply", ctypes.c_int, [vp, ctypes.c_int, vp, vp, vp]),
     ("qed3_dirac_ext_fermion_force", ctypes.c_int, [vp, vp, vp, vp]),
@@ -405,12 +408,17 @@ def fermion_force(dirac: DiracS2Dual, eta, F, stream=None):
 
 
 class ParallelRng:
-    """ParallelRng2 (src/both/rng.h:76-125): seeded per-link and per-site engines."""
+    """ParallelRng2 (src/both/rng.h:76-125): seeded per-link and per-site engines.
 
-    def __init__(self, lattice: S2Trivalent, seed: int = 0):
+    n_slices = Nt > 1: ParallelRngExt (src/both_3d/rng.h:89-121), engines
+    [Nt][n_links] and [Nt][n_sites], the streams of S^2 x S^1 HMC."""
+
+    def __init__(self, lattice: S2Trivalent, seed: int = 0, n_slices: int = 1):
         self.lattice = lattice
+        self.n_slices = n_slices
         h = vp()
-        _check(lib().qed3_rng_create(lattice.n_links, lattice.n_sites, seed, ctypes.byref(h)))
+        _check(lib().qed3_rng_create(lattice.n_links * n_slices, lattice.n_sites * n_slices, seed,
+                                     ctypes.byref(h)))
         self._h = h
 
     @property
@@ -418,12 +426,12 @@ class ParallelRng:
         return self._h
 
     def gaussian_links(self, width: float = 1.0) -> np.ndarray:
-        out = np.zeros(self.lattice.n_links)
+        out = np.zeros(self.lattice.n_links * self.n_slices)
         _check(lib().qed3_rng_gaussian_links(self._h, width, _ptr(out)))
         return out
 
     def gaussian_spinor(self) -> np.ndarray:
-        out = np.zeros(2 * self.lattice.n_sites, np.complex128)
+        out = np.zeros(2 * self.lattice.n_sites * self.n_slices, np.complex128)
         _check(lib().qed3_rng_gaussian_spinor(self._h, _ptr(out)))
         return out
 
@@ -442,7 +450,7 @@ class ParallelRng:
 
     def z2_spinor(self) -> np.ndarray:
         """FermionVector::set_random: (z + i z')/sqrt(2 Ns), z from the site engines' dist_z2(1, 2)."""
-        out = np.zeros(2 * self.lattice.n_sites, dtype=np.complex128)
+        out = np.zeros(2 * self.lattice.n_sites * self.n_slices, dtype=np.complex128)
         _check(lib().qed3_rng_z2_spinor(self._h, _ptr(out)))
         return out
 
@@ -623,6 +631,19 @@ class DiracExt:
         if getattr(self, "_h", None) and _lib is not None:
             _lib.qed3_dirac_ext_destroy(self._h)
             self._h = None
+
+
+def hmc_ext(dirac: DiracExt, rng: ParallelRng, A, gsq: float, tmax: float = 1.0, nsteps: int = 10,
+            nsteps_inner: int = 10, npf: int = 1, integrator: int = 0, tol: float = 1e-10, no_reject: bool = False,
+            stream=None):
+    """One S^2 x S^1 HMC trajectory (HMC2::run with U1WilsonExt(at, gsq) and npf
+    DiracExt pseudofermions) on device links A, in place; rng =
+    ParallelRng(lattice, seed, n_slices=Nt).  Returns (accepted, dH, cg_iterations)."""
+    acc, dH, its = ctypes.c_int(), ctypes.c_double(), ctypes.c_int()
+    _check(lib().qed3_hmc_ext(dirac._h, rng.handle, _ptr(A), dirac.at, gsq, tmax, nsteps, nsteps_inner, npf,
+                              integrator, tol, int(no_reject), ctypes.byref(acc), ctypes.byref(dH), ctypes.byref(its),
+                              _stream(stream)))
+    return bool(acc.value), dH.value, its.value
 
 
 class Batch:

@@ -310,6 +310,25 @@ int qed3_dirac_ext_fermion_force(qed3_dirac_ext* e, const double* eta, double* F
   QED3_GUARD_END
 }
 
+int qed3_hmc_ext(qed3_dirac_ext* e, qed3_rng* rng, double* A, double at, double gsq, double tmax, int nsteps,
+                 int nsteps_inner, int npf, int integrator, double tol, int no_reject, int* accepted, double* dH,
+                 int* cg_iters, void* stream) {
+  QED3_GUARD_BEGIN
+  if (!e || !rng || !A || !accepted || !dH) return fail(QED3_ERR_ARG, "NULL argument");
+  if (nsteps < 1 || nsteps_inner < 1 || !(tmax > 0) || npf < 1 || npf > 64 || !(at > 0))
+    return fail(QED3_ERR_ARG, "need nsteps, nsteps_inner, npf >= 1, tmax > 0, at > 0");
+  if (integrator != QED3_INTEGRATOR_LEAPFROG_ML && integrator != QED3_INTEGRATOR_LEAPFROG)
+    return fail(QED3_ERR_ARG, "unknown integrator");
+  const size_t nl = size_t(e->d2->lat->host.n_links) * e->Nt, ns = size_t(e->d2->Ns) * e->Nt;
+  size_t rl = 0, rs = 0;
+  rng_counts(rng, &rl, &rs);
+  if (rl != nl || rs != ns)
+    return fail(QED3_ERR_ARG, "rng must hold Nt n_links link engines and Nt n_sites site engines");
+  return hmc_ext(e, rng, A, at, gsq, tmax, nsteps, nsteps_inner, npf, integrator, tol > 0 ? tol : 1e-10, no_reject,
+                 accepted, dH, cg_iters, (cudaStream_t)stream);
+  QED3_GUARD_END
+}
+
 int qed3_dirac_ext_cg_solve(qed3_dirac_ext* e, double* x, const double* b, const qed3_solve_params* params,
                             qed3_solve_report* report, void* stream) {
   QED3_GUARD_BEGIN

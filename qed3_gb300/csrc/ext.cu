@@ -323,3 +323,128 @@ int ext_cg(qed3_dirac_ext_s* e, double* x, const double* b, const qed3_solve_par
 }
 
 }  // namespace qed3
+
+// ===========================================================================
+// S^2 x S^1 HMC trajectory: HMC2::run (src/both_3d/hmc.h:172-200) with the
+// anisotropic gauge action U1WilsonExt and npf Wilson pseudofermions of the
+// DiracExt operator, ExplicitLeapfrogML (src/both_3d/integrator.h:117-168) or
+// ExplicitLeapfrog.  The random streams are ParallelRngExt's: link engines
+// [Nt][Nl], site engines [Nt][Ns] (qed3_rng_create(Nt Nl, Nt Ns, seed));
+// momenta: spatial from the link engines, temporal one per site engine
+// (GaugeExt::gaussian); xi = fill_gaussian from the site engines.
+// H = |pi|^2 / 2 + S_g + sum Re <phi, eta>, dH = H1 - H0 as the reference.
+// ===========================================================================
+#include "gauge_impl.h"
+
+namespace qed3 {
+
+int hmc_ext(qed3_dirac_ext_s* e, qed3_rng_s* rng, double* A, double at, double gsq, double tmax, int nsteps,
+            int nsteps_inner, int npf, int integrator, double tol, int no_reject, int* accepted, double* dH_out,
+            int* cg_iters, cudaStream_t st) {
+  qed3_dirac_s* d = e->d2;
+  qed3_lattice_s* lat = d->lat;
+  const int Ns = d->Ns, Nl = lat->dev.Nl, Nt = e->Nt;
+  const long long nA = (long long)Nt * (Nl + Ns), nd = 4LL * Ns * Nt;
+  std::vector<double> pi(static_cast<size_t>(nA)), xi(static_cast<size_t>(nd * npf));
+  rng_gaussian_links(rng, 1.0, pi.data());
+  rng_gaussian_sites(rng, 1.0, pi.data() + size_t(Nt) * Nl);
+  for (int k = 0; k < npf; k++) rng_gaussian_spinor(rng, xi.data() + nd * k);
+  double* buf = nullptr;
+  const size_t bytes = (size_t(nA) * 4 + size_t(nd) * npf * 2 + 2048) * sizeof(double);
+  if (cudaMalloc(&buf, bytes) != cudaSuccess) return fail(QED3_ERR_NOMEM, "cudaMalloc failed");
+  double *P = buf, *A0 = P + nA, *F = A0 + nA, *Ff = F + nA, *phi = Ff + nA, *eta = phi + nd * npf,
+         *part = eta + nd * npf;
+  int its = 0;
+  const qed3_solve_params sp{tol, 0, QED3_PREC_F64, 0.1, 0.0, 0};
+  auto body = [&]() -> int {
+    int rc;
+    QED3_CUDA_TRY(cudaMemcpyAsync(P, pi.data(), nA * sizeof(double), cudaMemcpyHostToDevice, st));
+    QED3_CUDA_TRY(cudaMemcpyAsync(A0, A, nA * sizeof(double), cudaMemcpyDeviceToDevice, st));
+    QED3_CUDA_TRY(cudaMemcpyAsync(Ff, xi.data(), nd * npf * sizeof(double), cudaMemcpyHostToDevice, st));
+    if ((rc = ext_set_links(e, A, st))) return rc;
+    for (int k = 0; k < npf; k++)
+      if ((rc = ext_apply(e, QED3_OP_DDAG, phi + nd * k, Ff + nd * k, st))) return rc;
+    auto solve_all = [&]() -> int {
+      for (int k = 0; k < npf; k++) {
+        qed3_solve_report r{};
+        int c = ext_cg(e, eta + nd * k, phi + nd * k, &sp, &r, st);
+        its += r.iters;
+        if (!c && r.status != QED3_OK) c = fail(QED3_ERR_NOCONV, "pseudofermion solve did not converge");
+        if (c) return c;
+      }
+      return QED3_OK;
+    };
+    auto H = [&](double* h) -> int {
+      double kin = 0, im = 0, sg = 0, sf = 0;
+      int c = vec_zdot(nA / 2, P, P, part, &kin, &im, st);  // nA is even: Nt (Nl + Ns) with Nl, Ns even
+      if (c) return c;
+      if ((c = ext_gauge_action(lat, Nt, at, gsq, A, &sg, st))) return c;
+      for (int k = 0; k < npf; k++) {
+        double re = 0;
+        if ((c = vec_zdot(nd / 2, phi + nd * k, eta + nd * k, part, &re, &im, st))) return c;
+        sf += re;
+      }
+      *h = 0.5 * kin + sg + sf;
+      return QED3_OK;
+    };
+    if ((rc = solve_all())) return rc;
+    double h0 = 0, h1 = 0;
+    if ((rc = H(&h0))) return rc;
+    const double tau = tmax / nsteps, tau_in = tau / nsteps_inner;
+    auto gauge_kick = [&](double c) -> int {
+      int q = ext_gauge_force(lat, Nt, at, gsq, A, F, st);
+      return q ? q : vec_axpby(nA, -c, F, 1.0, P, P, st);
+    };
+    auto fermion_kick = [&](int k, double c) -> int {
+      int q = ext_fermion_force(e, eta + nd * k, Ff, st);
+      return q ? q : vec_axpby(nA, -c, Ff, 1.0, P, P, st);
+    };
+    auto full_kick = [&](double c) -> int {  // pi += -c (dSg + dSf)
+      int q = ext_gauge_force(lat, Nt, at, gsq, A, F, st);
+      for (int k = 0; k < npf && !q; k++) {
+        q = ext_fermion_force(e, eta + nd * k, Ff, st);
+        if (!q) q = vec_axpby(nA, 1.0, Ff, 1.0, F, F, st);
+      }
+      return q ? q : vec_axpby(nA, -c, F, 1.0, P, P, st);
+    };
+    auto drift = [&](double c) -> int { return vec_axpby(nA, c, P, 1.0, A, A, st); };
+    if (integrator == QED3_INTEGRATOR_LEAPFROG) {
+      for (int n = 0; n < nsteps; n++) {
+        if ((rc = full_kick(0.5 * tau)) || (rc = drift(tau)) || (rc = ext_set_links(e, A, st)) ||
+            (rc = solve_all()) || (rc = full_kick(0.5 * tau)))
+          return rc;
+      }
+    } else {
+      for (int k = 0; k < npf; k++)
+        if ((rc = fermion_kick(k, 0.5 * tau))) return rc;
+      for (int n = 0; n < nsteps; n++) {
+        if ((rc = gauge_kick(0.5 * tau_in))) return rc;
+        for (int m = 0; m < nsteps_inner; m++)
+          if ((rc = drift(tau_in)) || (rc = gauge_kick((m != nsteps_inner - 1 ? 1.0 : 0.5) * tau_in))) return rc;
+        if ((rc = ext_set_links(e, A, st)) || (rc = solve_all())) return rc;
+        for (int k = 0; k < npf; k++)
+          if ((rc = fermion_kick(k, (n != nsteps - 1 ? 1.0 : 0.5) * tau))) return rc;
+      }
+    }
+    if ((rc = H(&h1))) return rc;
+    const double dH = h1 - h0;
+    *dH_out = dH;
+    if (cg_iters) *cg_iters = its;
+    const double r = std::min(1.0, std::exp(-dH));
+    const double a = rng_uniform(rng);
+    if (a < r || no_reject) {
+      *accepted = 1;
+    } else {
+      *accepted = 0;
+      QED3_CUDA_TRY(cudaMemcpyAsync(A, A0, nA * sizeof(double), cudaMemcpyDeviceToDevice, st));
+      if ((rc = ext_set_links(e, A, st))) return rc;
+    }
+    QED3_CUDA_TRY(cudaStreamSynchronize(st));
+    return QED3_OK;
+  };
+  const int rc = body();
+  cudaFree(buf);
+  return rc;
+}
+
+}  // namespace qed3

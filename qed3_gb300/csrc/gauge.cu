@@ -397,6 +397,16 @@ int rng_load(qed3_rng_s* r, const char* path) {
 void rng_gaussian_links(qed3_rng_s* r, double width, double* out) {
   for (size_t l = 0; l < r->r.links.size(); l++) out[l] = width * r->r.links[l].g(r->r.links[l].mt);
 }
+// GaugeExt::gaussian's temporal part (src/both_3d/gauge_ext.h:145-149): one
+// Gaussian per site engine, in engine order
+void rng_counts(const qed3_rng_s* r, size_t* n_links, size_t* n_sites) {
+  *n_links = r->r.links.size();
+  *n_sites = r->r.sites.size();
+}
+
+void rng_gaussian_sites(qed3_rng_s* r, double width, double* out) {
+  for (size_t x = 0; x < r->r.sites.size(); x++) out[x] = width * r->r.sites[x].g(r->r.sites[x].mt);
+}
 void rng_gaussian_spinor(qed3_rng_s* r, double* out) {
   // ParallelRngExt::fill_gaussian, src/both_3d/rng.h:122-129
   for (size_t x = 0; x < r->r.sites.size(); x++)

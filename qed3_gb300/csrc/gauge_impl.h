@@ -18,8 +18,10 @@ int overlap_force_links(qed3_dirac_s* d, int np, const double* c, double cw, con
                         const S64* DZ, const S64* DY, const S64* eta, const S64* w, double* F, cudaStream_t st);
 qed3_rng_s* rng_create(int n_links, int n_sites, int seed);
 void rng_destroy(qed3_rng_s* r);
+void rng_counts(const qed3_rng_s* r, size_t* n_links, size_t* n_sites);
 void rng_gaussian_links(qed3_rng_s* r, double width, double* out);
 void rng_gaussian_spinor(qed3_rng_s* r, double* out);
+void rng_gaussian_sites(qed3_rng_s* r, double width, double* out);
 double rng_uniform(qed3_rng_s* r);
 int rng_save(const qed3_rng_s* r, const char* path);
 int rng_load(qed3_rng_s* r, const char* path);

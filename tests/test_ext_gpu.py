@@ -126,3 +126,47 @@ def test_ext_fermion_force_is_the_derivative(cuda, Nt):
         Am[k] -= h
         fd = -(f(Ap) - f(Am)) / (2 * h)
         assert abs(fd - F[k]) < 1e-6 * max(1.0, abs(fd)), (k, fd, F[k])
+
+
+@pytest.mark.parametrize("Nt,npf,integrator", [(2, 1, 0), (3, 2, 0), (2, 2, 1), (4, 1, 1)])
+def test_hmc_ext_matches_oracle(cuda, Nt, npf, integrator):
+    """S^2 x S^1 HMC trajectories (HMC2::run, U1WilsonExt + DiracExt
+    pseudofermions) on the GPU against the oracle from the same seeded
+    ParallelRngExt streams: same Metropolis decisions, dH to 1e-8, links to
+    1e-9 after three trajectories, CG iterations within 10%."""
+    import torch
+    n, at, gsq, r, M5 = 2, 0.8, 1.0, 1.0, 0.1
+    g = O.geometry(n)
+    lat = Q.S2Trivalent(n)
+    A = np.random.default_rng(50 + Nt).uniform(-0.3, 0.3, Nt * (g.n_links + g.n_sites))
+    De = Q.DiracExt(lat, r, M5, Nt, at)
+    seed = 90 + 7 * Nt + npf
+    rd, ro = Q.ParallelRng(lat, seed, n_slices=Nt), O.Rng(g, seed, Nt)
+    Ad = to_dev(A, cuda)
+    Ao = A.copy()
+    for t in range(3):
+        acc_d, dH_d, it_d = Q.hmc_ext(De, rd, Ad, gsq, tmax=0.5, nsteps=4, nsteps_inner=2, npf=npf,
+                                      integrator=integrator, tol=1e-12)
+        acc_o, dH_o, it_o = O.hmc_ext(g, ro, Ao, r, M5, Nt, at, gsq, tmax=0.5, nsteps=4, nsteps_inner=2, npf=npf,
+                                      integrator=integrator, tol=1e-12)
+        assert acc_d == acc_o, (t, dH_d, dH_o)
+        assert abs(dH_d - dH_o) < 1e-8 * (1 + abs(dH_o)), (t, dH_d, dH_o)
+        assert abs(it_d - it_o) <= 0.1 * it_o + 2, (it_d, it_o)
+        torch.cuda.synchronize()
+        assert np.abs(from_dev(Ad) - Ao).max() < 1e-9
+    # the streams stayed in step: the next draws agree
+    assert np.array_equal(rd.gaussian_links(), ro.gaussian_links())
+
+
+def test_hmc_ext_rejects_bad_rng(cuda):
+    """The RNG must hold Nt times the lattice's engines (ParallelRngExt)."""
+    lat = Q.S2Trivalent(2)
+    De = Q.DiracExt(lat, 1.0, 0.1, 2, 0.8)
+    A = torch_zeros(2 * (lat.n_links + lat.n_sites), cuda)
+    with pytest.raises(Q.Qed3Error):
+        Q.hmc_ext(De, Q.ParallelRng(lat, 1), A, 1.0)
+
+
+def torch_zeros(n, device):
+    import torch
+    return torch.zeros(n, dtype=torch.float64, device=device)
