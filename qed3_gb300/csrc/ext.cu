@@ -350,20 +350,20 @@ int hmc_ext(qed3_dirac_ext_s* e, qed3_rng_s* rng, double* A, double at, double g
   rng_gaussian_sites(rng, 1.0, pi.data() + size_t(Nt) * Nl);
   for (int k = 0; k < npf; k++) rng_gaussian_spinor(rng, xi.data() + nd * k);
   double* buf = nullptr;
-  const size_t bytes = (size_t(nA) * 4 + size_t(nd) * npf * 2 + 2048) * sizeof(double);
+  const size_t bytes = (size_t(nA) * 4 + size_t(nd) * npf * 3 + 2048) * sizeof(double);
   if (cudaMalloc(&buf, bytes) != cudaSuccess) return fail(QED3_ERR_NOMEM, "cudaMalloc failed");
-  double *P = buf, *A0 = P + nA, *F = A0 + nA, *Ff = F + nA, *phi = Ff + nA, *eta = phi + nd * npf,
-         *part = eta + nd * npf;
+  double *P = buf, *A0 = P + nA, *F = A0 + nA, *Ff = F + nA, *xid = Ff + nA, *phi = xid + nd * npf,
+         *eta = phi + nd * npf, *part = eta + nd * npf;
   int its = 0;
   const qed3_solve_params sp{tol, 0, QED3_PREC_F64, 0.1, 0.0, 0};
   auto body = [&]() -> int {
     int rc;
     QED3_CUDA_TRY(cudaMemcpyAsync(P, pi.data(), nA * sizeof(double), cudaMemcpyHostToDevice, st));
     QED3_CUDA_TRY(cudaMemcpyAsync(A0, A, nA * sizeof(double), cudaMemcpyDeviceToDevice, st));
-    QED3_CUDA_TRY(cudaMemcpyAsync(Ff, xi.data(), nd * npf * sizeof(double), cudaMemcpyHostToDevice, st));
+    QED3_CUDA_TRY(cudaMemcpyAsync(xid, xi.data(), nd * npf * sizeof(double), cudaMemcpyHostToDevice, st));
     if ((rc = ext_set_links(e, A, st))) return rc;
     for (int k = 0; k < npf; k++)
-      if ((rc = ext_apply(e, QED3_OP_DDAG, phi + nd * k, Ff + nd * k, st))) return rc;
+      if ((rc = ext_apply(e, QED3_OP_DDAG, phi + nd * k, xid + nd * k, st))) return rc;
     auto solve_all = [&]() -> int {
       for (int k = 0; k < npf; k++) {
         qed3_solve_report r{};
