@@ -448,3 +448,40 @@ int hmc_ext(qed3_dirac_ext_s* e, qed3_rng_s* rng, double* A, double at, double g
 }
 
 }  // namespace qed3
+
+namespace qed3 {
+
+// Point-source propagator of prop.cu (src/both_3d/prop.cu:243-268):
+// src1 = delta at (slice s, site ix, spin a) (FermionVector::set_pt_source,
+// src/both_3d/valence.h:67-72), src = D^dag src1, sink = (D^dag D)^{-1} src
+// = D^{-1} src1 by the FP64 CG.  Site ix in the reference's numbering.
+int ext_propagator(qed3_dirac_ext_s* e, int s, int ix, int a, double* sink, const qed3_solve_params* prm,
+                   qed3_solve_report* rep, cudaStream_t st) {
+  if (!e->links_set) return fail(QED3_ERR_STATE, "call qed3_dirac_ext_set_links first");
+  const int Ns = e->d2->Ns;
+  if (s < 0 || s >= e->Nt || ix < 0 || ix >= Ns || a < 0 || a > 1)
+    return fail(QED3_ERR_ARG, "source point out of range");
+  const long long nd = 4LL * Ns * e->Nt;
+  double* buf = nullptr;
+  if (cudaMalloc(&buf, size_t(nd) * 2 * sizeof(double)) != cudaSuccess) return fail(QED3_ERR_NOMEM, "cudaMalloc failed");
+  double *src1 = buf, *src = buf + nd;
+  auto body = [&]() -> int {
+    const double one = 1.0;
+    QED3_CUDA_TRY(cudaMemsetAsync(src1, 0, nd * sizeof(double), st));
+    QED3_CUDA_TRY(cudaMemcpyAsync(src1 + 2 * ((size_t(s) * Ns + ix) * 2 + a), &one, sizeof(double),
+                                  cudaMemcpyHostToDevice, st));
+    int rc = ext_apply(e, QED3_OP_DDAG, src, src1, st);
+    if (rc) return rc;
+    qed3_solve_report r{};
+    rc = ext_cg(e, sink, src, prm, &r, st);
+    if (rep) *rep = r;
+    if (!rc && r.status != QED3_OK) rc = fail(QED3_ERR_NOCONV, "propagator solve did not converge");
+    return rc;
+  };
+  const int rc = body();
+  cudaStreamSynchronize(st);
+  cudaFree(buf);
+  return rc;
+}
+
+}  // namespace qed3

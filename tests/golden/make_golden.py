@@ -24,6 +24,12 @@ in place by `make -C oracle ref` into oracle/_ref/librng3d_ref.so) after one
 sweep of link and site Gaussians and three master uniforms (3 links, 2 sites,
 seed 5), and the reference's continuation draws after it.
 
+analyze_corr_ref.json: the REFERENCE's correlator analysis program
+(src/both_3d/analyze_corr.cpp, built in place by `make -C oracle ref` into
+oracle/_ref/analyze_corr) run on seeded synthetic correlator files (stored in
+the fixture): its complete standard output for three argument sets (two
+streams with one cut short, binsize 1 and 3, one stream).
+
 free_spectrum.json: the known answers of analysis/ev_dual.ipynb (cells 33-34),
 typed in from the notebook's output cells.
 """
@@ -137,9 +143,38 @@ def spectrum_fixture():
         json.dump(data, f, indent=1)
 
 
+def analyze_corr_fixture():
+    import tempfile
+    subprocess.check_call(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "ref"])
+    exe = os.path.join(ROOT, "oracle", "_ref", "analyze_corr")
+    rng = np.random.default_rng(17)
+    Nt = 6
+    files = {}
+    # stream 1: confs 10, 12, ..., 48; stream 2 stops at 40
+    for prefix, last in ((1, 48), (2, 40)):
+        for conf in range(10, last + 1, 2):
+            decay = np.exp(-0.4 * np.arange(Nt)) + np.exp(-0.4 * (Nt - np.arange(Nt)))
+            files[f"corr/s{prefix}/C{conf}.dat"] = [float(v) for v in decay * (1 + 0.1 * rng.normal(size=Nt))]
+    cases = [["corr/s", "C", 10, 60, 2, Nt, 2, 2], ["corr/s", "C", 10, 60, 2, Nt, 3, 2],
+             ["corr/s", "C", 12, 44, 2, Nt, 1, 1]]
+    out = []
+    with tempfile.TemporaryDirectory() as d:
+        for rel, vals in files.items():
+            os.makedirs(os.path.join(d, os.path.dirname(rel)), exist_ok=True)
+            with open(os.path.join(d, rel), "w") as f:
+                f.write("".join(f"{v!r} {0.5 * v!r}\n" for v in vals))
+        for c in cases:
+            r = subprocess.run([exe] + [str(a) for a in c], cwd=d, capture_output=True, text=True, check=True)
+            out.append(dict(args=c, stdout=r.stdout.splitlines()))
+    with open(os.path.join(HERE, "analyze_corr_ref.json"), "w") as f:
+        json.dump(dict(source="src/both_3d/analyze_corr.cpp built in place; files: first column read, second ignored",
+                       files=files, runs=out), f, indent=1)
+
+
 if __name__ == "__main__":
     zolotarev_fixture()
     rng_fixture()
     gauge_fixture()
     rng_ckpoint_fixture()
     spectrum_fixture()
+    analyze_corr_fixture()

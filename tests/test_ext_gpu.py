@@ -170,3 +170,34 @@ def test_hmc_ext_rejects_bad_rng(cuda):
 def torch_zeros(n, device):
     import torch
     return torch.zeros(n, dtype=torch.float64, device=device)
+
+
+@pytest.mark.parametrize("Nt,at", [(1, 1.0), (4, 0.5)])
+def test_ext_propagator_matches_oracle(cuda, Nt, at):
+    """prop.cu's point-source propagator: sink = (D^dag D)^{-1} D^dag delta on
+    the GPU = the oracle's dense D^{-1} delta, for a random and the free field;
+    the written profiles carry the sink's values."""
+    import torch
+    from qed3_gb300 import correlators as C
+    n = 2
+    g = O.geometry(n)
+    lat = Q.S2Trivalent(n)
+    De = Q.DiracExt(lat, 1.0, 0.0, Nt, at)
+    for A in (np.random.default_rng(60 + Nt).uniform(-np.pi, np.pi, Nt * (g.n_links + g.n_sites)),
+              np.zeros(Nt * (g.n_links + g.n_sites))):
+        De.update(to_dev(A, cuda))
+        M = O.dirac_ext_matrix(g, 1.0, 0.0, Nt, at, A)
+        for s, ix, a in ((0, 0, 0), (Nt - 1, 7, 1)):
+            sink = torch.zeros(2 * g.n_sites * Nt, dtype=torch.complex128, device=cuda)
+            rep = De.propagator(sink, s, ix, a, tol=1e-12)
+            assert rep.status == Q.OK and rep.true_rel_res <= 1e-12
+            delta = np.zeros(2 * g.n_sites * Nt, np.complex128)
+            delta[(s * g.n_sites + ix) * 2 + a] = 1.0
+            ref = np.linalg.solve(M, delta)
+            got = from_dev(sink)
+            assert rel(got, ref) < 1e-8
+        sp, tp = C.prop_profiles(lat, sink, Nt, at)
+        fac = (at if Nt > 1 else 1.0) * lat.tables()["means"][0]
+        assert np.allclose(tp[0::2, 1], got.reshape(Nt, -1, 2)[:, 0, 0].real / fac)
+    with pytest.raises(Q.Qed3Error):
+        De.propagator(sink, Nt, 0, 0)
