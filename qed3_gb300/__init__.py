@@ -137,7 +137,7 @@ SIGNATURES = [
     ("qed3_dirac_ext_set_links", ctypes.c_int, [vp, vp, vp]),
     ("qed3_dirac_ext_apply", ctypes.c_int, [vp, ctypes.c_int, vp, vp, vp]),
     ("qed3_dirac_ext_fermion_force", ctypes.c_int, [vp, vp, vp, vp]),
-    ("qed3_dirac_ext_propagator", ctypes.c_int, [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, vp,
+    ("qed3_dirac_ext_propagator", ctypes.c_int, [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, vp,
                                                  ctypes.POINTER(SolveParams), ctypes.POINTER(SolveReport), vp]),
     ("qed3_dirac_ext_cg_solve", ctypes.c_int, [vp, vp, vp, ctypes.POINTER(SolveParams), ctypes.POINTER(SolveReport),
                                                vp]),
@@ -629,12 +629,13 @@ class DiracExt:
                                              _stream(stream)))
         return Report(r.status, r.iters, r.reliable_updates, r.true_rel_res, r.ms)
 
-    def propagator(self, sink, s: int = 0, ix: int = 0, spin: int = 0, tol: float = 1e-10, stream=None) -> Report:
+    def propagator(self, sink, s: int = 0, ix: int = 0, spin: int = 0, tol: float = 1e-10, dagger: bool = False,
+                   stream=None) -> Report:
         """sink = D^{-1} (point source at slice s, site ix, spin), prop.cu's
-        (D^dag D)^{-1} D^dag src solve."""
+        (D^dag D)^{-1} D^dag src solve; dagger: D^{-dag} (IS_DAGGER)."""
         p = SolveParams(tol, 0, PREC_F64, 0.1, 0.0, 0)
         r = SolveReport()
-        _check(lib().qed3_dirac_ext_propagator(self._h, s, ix, spin, _ptr(sink), ctypes.byref(p), ctypes.byref(r),
+        _check(lib().qed3_dirac_ext_propagator(self._h, s, ix, spin, int(dagger), _ptr(sink), ctypes.byref(p), ctypes.byref(r),
                                                _stream(stream)))
         return Report(r.status, r.iters, r.reliable_updates, r.true_rel_res, r.ms)
 

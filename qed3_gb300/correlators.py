@@ -108,17 +108,18 @@ def _g(x: float) -> str:
 
 
 def write_prop_files(lattice, sink, Nt: int, at: float, n_refine: int, directory: str = ".", width: float = 0.05,
-                     overlap: bool = False) -> list[str]:
+                     overlap: bool = False, dagger: bool = False) -> list[str]:
     """Writes prop.cu's two files for the dual lattice,
-    dual_[ov_]prop_spacial_L<n>_Nt<Nt>.dat1 and ..._temporal_..., each row
-    three setw(25) columns in the stream's default format."""
+    [dagger_][ov_]dual_prop_spacial_L<n>_Nt<Nt>.dat1 and ..._temporal_..., each
+    row three setw(25) columns in the stream's default format."""
     spatial, temporal = prop_profiles(lattice, sink, Nt, at, width)
     out = []
     for kind, rows in (("spacial", spatial), ("temporal", temporal)):
-        name = f"prop_{kind}_L{n_refine}_Nt{Nt}.dat1"
+        name = "dual_" + f"prop_{kind}_L{n_refine}_Nt{Nt}.dat1"
         if overlap:
             name = "ov_" + name
-        name = "dual_" + name
+        if dagger:
+            name = "dagger_" + name
         path = os.path.join(directory, name)
         with open(path, "w") as f:
             for r in rows:

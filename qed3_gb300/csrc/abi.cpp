@@ -329,12 +329,12 @@ int qed3_hmc_ext(qed3_dirac_ext* e, qed3_rng* rng, double* A, double at, double 
   QED3_GUARD_END
 }
 
-int qed3_dirac_ext_propagator(qed3_dirac_ext* e, int s, int ix, int a, double* sink, const qed3_solve_params* params,
+int qed3_dirac_ext_propagator(qed3_dirac_ext* e, int s, int ix, int a, int dagger, double* sink, const qed3_solve_params* params,
                               qed3_solve_report* report, void* stream) {
   QED3_GUARD_BEGIN
   if (!e || !sink) return fail(QED3_ERR_ARG, "NULL argument");
   qed3_solve_params p{params ? params->tol : 1e-10, params ? params->maxiter : 0, QED3_PREC_F64, 0.1, 0.0, 0};
-  return ext_propagator(e, s, ix, a, sink, &p, report, (cudaStream_t)stream);
+  return ext_propagator(e, s, ix, a, dagger, sink, &p, report, (cudaStream_t)stream);
   QED3_GUARD_END
 }
 

@@ -256,7 +256,8 @@ int ext_fermion_force(qed3_dirac_ext_s* e, const double* eta, double* F, cudaStr
 // MatPoly::solve (src/dual/matpoly.h:204-267) on D^dag D + shift in FP64:
 // x0 = 0, stop on the recursive residual, certified by the true residual.
 int ext_cg(qed3_dirac_ext_s* e, double* x, const double* b, const qed3_solve_params* prm, qed3_solve_report* rep,
-           cudaStream_t st) {
+           cudaStream_t st, int op) {
+  if (op != QED3_OP_DDAGD && op != QED3_OP_DDDAG) return fail(QED3_ERR_ARG, "CG runs on D^dag D or D D^dag");
   if (!e->links_set) return fail(QED3_ERR_STATE, "call qed3_dirac_ext_set_links first");
   if (prm && prm->precision != QED3_PREC_F64) return fail(QED3_ERR_ARG, "the S2 x S1 solve runs in FP64");
   const double tol = prm && prm->tol > 0 ? prm->tol : 1e-10;
@@ -272,7 +273,7 @@ int ext_cg(qed3_dirac_ext_s* e, double* x, const double* b, const qed3_solve_par
   QED3_CUDA_TRY(cudaEventCreate(&e1));
   QED3_CUDA_TRY(cudaEventRecord(e0, st));
   auto A = [&](double* o, const double* v) -> int {
-    int c = ext_apply(e, QED3_OP_DDAGD, o, v, st);
+    int c = ext_apply(e, op, o, v, st);
     if (!c && shift != 0.0) c = vec_axpby(nd, shift, v, 1.0, o, o, st);
     return c;
   };
@@ -454,8 +455,9 @@ namespace qed3 {
 // Point-source propagator of prop.cu (src/both_3d/prop.cu:243-268):
 // src1 = delta at (slice s, site ix, spin a) (FermionVector::set_pt_source,
 // src/both_3d/valence.h:67-72), src = D^dag src1, sink = (D^dag D)^{-1} src
-// = D^{-1} src1 by the FP64 CG.  Site ix in the reference's numbering.
-int ext_propagator(qed3_dirac_ext_s* e, int s, int ix, int a, double* sink, const qed3_solve_params* prm,
+// = D^{-1} src1 by the FP64 CG; dagger (IS_DAGGER): src = D src1, sink =
+// (D D^dag)^{-1} src = D^{-dag} src1.  Site ix in the reference's numbering.
+int ext_propagator(qed3_dirac_ext_s* e, int s, int ix, int a, int dagger, double* sink, const qed3_solve_params* prm,
                    qed3_solve_report* rep, cudaStream_t st) {
   if (!e->links_set) return fail(QED3_ERR_STATE, "call qed3_dirac_ext_set_links first");
   const int Ns = e->d2->Ns;
@@ -470,10 +472,10 @@ int ext_propagator(qed3_dirac_ext_s* e, int s, int ix, int a, double* sink, cons
     QED3_CUDA_TRY(cudaMemsetAsync(src1, 0, nd * sizeof(double), st));
     QED3_CUDA_TRY(cudaMemcpyAsync(src1 + 2 * ((size_t(s) * Ns + ix) * 2 + a), &one, sizeof(double),
                                   cudaMemcpyHostToDevice, st));
-    int rc = ext_apply(e, QED3_OP_DDAG, src, src1, st);
+    int rc = ext_apply(e, dagger ? QED3_OP_D : QED3_OP_DDAG, src, src1, st);
     if (rc) return rc;
     qed3_solve_report r{};
-    rc = ext_cg(e, sink, src, prm, &r, st);
+    rc = ext_cg(e, sink, src, prm, &r, st, dagger ? QED3_OP_DDDAG : QED3_OP_DDAGD);
     if (rep) *rep = r;
     if (!rc && r.status != QED3_OK) rc = fail(QED3_ERR_NOCONV, "propagator solve did not converge");
     return rc;

@@ -66,3 +66,16 @@ def test_prop_profiles_rows():
     assert np.allclose(sp[0::2, 0], th[sel]) and np.allclose(sp[1::2, 1], sink[0, sel, 1].real / fac)
     assert tp.shape == (2 * Nt, 3)
     assert np.allclose(tp[0::2, 0], at * np.arange(Nt)) and np.allclose(tp[1::2, 2], sink[:, 0, 1].imag / fac)
+
+
+def test_write_prop_files_names_and_format(tmp_path):
+    lat = Q.S2Trivalent(2)
+    Nt, at = 2, 0.5
+    sink = np.arange(Nt * lat.n_sites * 2, dtype=np.float64).astype(np.complex128) * (1 - 0.5j)
+    paths = C.write_prop_files(lat, sink, Nt, at, 2, str(tmp_path), width=0.5, overlap=True, dagger=True)
+    assert [os.path.basename(p) for p in paths] == ["dagger_ov_dual_prop_spacial_L2_Nt2.dat1",
+                                                    "dagger_ov_dual_prop_temporal_L2_Nt2.dat1"]
+    rows = open(paths[1]).read().splitlines()
+    assert len(rows) == 2 * Nt and all(len(r) == 3 * 25 + 2 for r in rows)
+    _, tp = C.prop_profiles(lat, sink, Nt, at, width=0.5)
+    assert [float(x) for x in rows[2].split()] == [float(f"{v:.6g}") for v in tp[2]]

@@ -187,15 +187,18 @@ def test_ext_propagator_matches_oracle(cuda, Nt, at):
               np.zeros(Nt * (g.n_links + g.n_sites))):
         De.update(to_dev(A, cuda))
         M = O.dirac_ext_matrix(g, 1.0, 0.0, Nt, at, A)
-        for s, ix, a in ((0, 0, 0), (Nt - 1, 7, 1)):
+        for s, ix, a, dag in ((0, 0, 0, False), (Nt - 1, 7, 1, False), (0, 3, 1, True)):
             sink = torch.zeros(2 * g.n_sites * Nt, dtype=torch.complex128, device=cuda)
-            rep = De.propagator(sink, s, ix, a, tol=1e-12)
+            rep = De.propagator(sink, s, ix, a, tol=1e-12, dagger=dag)
             assert rep.status == Q.OK and rep.true_rel_res <= 1e-12
             delta = np.zeros(2 * g.n_sites * Nt, np.complex128)
             delta[(s * g.n_sites + ix) * 2 + a] = 1.0
-            ref = np.linalg.solve(M, delta)
+            ref = np.linalg.solve(M.conj().T if dag else M, delta)
             got = from_dev(sink)
-            assert rel(got, ref) < 1e-8
+            assert rel(got, ref) < 1e-8, dag
+            if not dag:
+                sink_d, got_d = sink, got
+        sink, got = sink_d, got_d
         sp, tp = C.prop_profiles(lat, sink, Nt, at)
         fac = (at if Nt > 1 else 1.0) * lat.tables()["means"][0]
         assert np.allclose(tp[0::2, 1], got.reshape(Nt, -1, 2)[:, 0, 0].real / fac)
