@@ -228,6 +228,149 @@ def cpu_reference_solve(b, A, threads=None):
     return dt, it, float(np.linalg.norm(r) / np.linalg.norm(b)), O.num_threads()
 
 
+def _wall(torch, fn, reps):
+    """Median wall time of fn() (host-driven paths: trajectories, host-looped CG)."""
+    ts = []
+    for _ in range(reps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        fn()
+        torch.cuda.synchronize()
+        ts.append(time.perf_counter() - t0)
+    return float(np.median(ts))
+
+
+def paths_timings(torch, Q, dev, cpu=True):
+    """The paths around the solver on the GPU, each beside the oracle's CPU
+    restatement of the reference algorithm on the host cores (one bounded
+    sample): Wilson-fermion HMC trajectory (n=16), overlap apply (n=16, order
+    21), the S^2 x S^1 operator apply (n=64, Nt=16; HBM-resident, roofline),
+    its FP64 CG (n=16, Nt=8) and HMC trajectory (n=8, Nt=8)."""
+    from oracle import oracle as O
+    peak, peak_kind = peaks()
+    out = {}
+    cores = O.num_threads()
+    # -- Wilson-fermion HMC trajectory, ExplicitLeapfrogML, one pseudofermion
+    n = 16
+    lat = Q.S2Trivalent(n)
+    A0, _ = Q.thermalized_links(lat, BETA, seed=3, ntraj=20, init="uniform", device=dev)
+    D = Q.DiracS2Dual(lat, 1.0, 0.1)
+    D.update(A0)
+    kw = dict(tmax=1.0, nsteps=5, nsteps_inner=4, tol=1e-10)
+    rng = Q.ParallelRng(lat, 11)
+    A = A0.clone()
+    its = []
+    gpu_s = _wall(torch, lambda: its.append(Q.hmc_fermion(lat, D, rng, A, BETA, **kw)[2]), 4)
+    row = {"gpu_ms": 1e3 * gpu_s, "cg_iters": its[-1], "config": "n=16, beta=1.4, r=1, M5=0.1, tau=1, 5 x 4 steps, "
+           "tol 1e-10 (mixed FP32 solves, FP64 certificate)"}
+    g = O.geometry(n) if cpu else None
+    if cpu:
+        Do = O.Dirac(g, 1.0, 0.1)
+        Ao = A0.cpu().numpy().copy()
+        t0 = time.perf_counter()
+        O.hmc_fermion(g, Do, O.Rng(g, 11), Ao, BETA, **kw)
+        row["cpu_baseline"] = {"ms": 1e3 * (time.perf_counter() - t0), "cores": cores, "kind": "port",
+                               "sample": "one trajectory, same parameters, FP64 CSR CG"}
+        row["gpu_vs_cpu"] = row["cpu_baseline"]["ms"] / row["gpu_ms"]
+    out["hmc_fermion_n16"] = row
+    # -- overlap apply (M5 = -1, Zolotarev order 41 = 20 poles, bounds from the operator update)
+    Dw = Q.DiracS2Dual(lat, 1.0, -1.0)
+    Dw.update(A0)
+    ov = Q.Overlap(Dw, order=41)
+    ov.update()
+    inf = ov.info()
+    v = torch.from_numpy(Q.ParallelRng(lat, 5).gaussian_spinor()).to(dev)
+    w = torch.empty_like(v)
+    gpu_s = _wall(torch, lambda: ov.apply(w, v, tol_inner=1e-10), 5)
+    row = {"gpu_ms": 1e3 * gpu_s, "k": inf["k"], "config": "n=16, M5=-1, order 41 (20 poles), inner tol 1e-10 "
+           "(batched multi-shift pole solves)"}
+    if cpu:
+        Dow = O.Dirac(g, 1.0, -1.0)
+        Dow.update(A0.cpu().numpy())
+        vh = v.cpu().numpy()
+        t0 = time.perf_counter()
+        Dow.overlap(vh, inf["lambda_min"], inf["lambda_max"], 41, 0, 1e-10)
+        row["cpu_baseline"] = {"ms": 1e3 * (time.perf_counter() - t0), "cores": cores, "kind": "port",
+                               "sample": "one apply, one CG per pole"}
+        row["gpu_vs_cpu"] = row["cpu_baseline"]["ms"] / row["gpu_ms"]
+    out["overlap_apply_n16"] = row
+    # -- S^2 x S^1 operator apply: HBM-resident at n=64, Nt=16
+    n, Nt, at = 64, 16, 0.5
+    lat = Q.S2Trivalent(n)
+    De = Q.DiracExt(lat, 1.0, 0.1, Nt, at)
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(4)
+    Ae = (torch.rand(Nt * (lat.n_links + lat.n_sites), dtype=torch.float64, device=dev, generator=gen) * 2 - 1) * np.pi
+    De.update(Ae)
+    ve = torch.randn(Nt * 2 * lat.n_sites, dtype=torch.complex128, device=dev, generator=gen)
+    we = torch.empty_like(ve)
+    st = torch.cuda.current_stream()
+    for _ in range(3):
+        De.apply(we, ve, Q.OP_D)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    reps = 20
+    e0.record(st)
+    for _ in range(reps):
+        De.apply(we, ve, Q.OP_D)
+    e1.record(st)
+    e1.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    # per site and slice: spinor in 32 + out 32 + 3 slice hop blocks 192 + temporal angle 8,
+    # plus the per-site tables (neighbours 12, permutation 4, diagonal 8, kappa_t 8) once per site
+    bps = 32 + 32 + 192 + 8 + 32.0 / Nt
+    gbs = bps * lat.n_sites * Nt / (ms * 1e-3) / 1e9
+    row = {"gpu_ms": ms, "GB/s": gbs, "bytes_per_site_slice": bps, "frac_of_" + peak_kind: gbs / peak,
+           "config": "n=64, Nt=16 (1.31M site-slices, 252 MB of hop blocks: HBM-resident), FP64, D"}
+    if cpu:
+        g = O.geometry(n)
+        Ah, vh = Ae.cpu().numpy(), ve.cpu().numpy()
+        t0 = time.perf_counter()
+        O.dirac_ext_apply(g, 1.0, 0.1, Nt, at, Ah, vh, 0)
+        row["cpu_baseline"] = {"ms": 1e3 * (time.perf_counter() - t0), "cores": cores, "kind": "port",
+                               "sample": "one D apply (per-slice CSR restatement incl. its per-slice link update)"}
+        row["gpu_vs_cpu"] = row["cpu_baseline"]["ms"] / row["gpu_ms"]
+    out["ext_apply_n64_nt16"] = row
+    del De, Ae, ve, we
+    # -- S^2 x S^1 FP64 CG on D^dag D and the S^2 x S^1 HMC trajectory
+    n, Nt, at = 16, 8, 0.5
+    lat = Q.S2Trivalent(n)
+    De = Q.DiracExt(lat, 1.0, 0.1, Nt, at)
+    Ae = (torch.rand(Nt * (lat.n_links + lat.n_sites), dtype=torch.float64, device=dev, generator=gen) - 0.5) * 0.6
+    De.update(Ae)
+    be = torch.randn(Nt * 2 * lat.n_sites, dtype=torch.complex128, device=dev, generator=gen)
+    xe = torch.empty_like(be)
+    reps_ = []
+    gpu_s = _wall(torch, lambda: reps_.append(De.solve(xe, be, tol=1e-10)), 3)
+    row = {"gpu_ms": 1e3 * gpu_s, "iters": reps_[-1].iters, "true_rel_res": reps_[-1].true_rel_res,
+           "config": "n=16, Nt=8, at=0.5, links 0.6 U[-0.5,0.5), tol 1e-10 FP64"}
+    if cpu:
+        g = O.geometry(n)
+        Ah, bh = Ae.cpu().numpy(), be.cpu().numpy()
+        k = 10
+        t0 = time.perf_counter()
+        for _ in range(k):
+            O.dirac_ext_apply(g, 1.0, 0.1, Nt, at, Ah, bh, 2)
+        per = (time.perf_counter() - t0) / k
+        row["cpu_baseline"] = {"ms": 1e3 * per * reps_[-1].iters, "cores": cores, "kind": "port",
+                               "sample": f"{k} D^dag D applications of the restatement, times the GPU's "
+                                         "iteration count (vector updates not counted)"}
+        row["gpu_vs_cpu"] = row["cpu_baseline"]["ms"] / row["gpu_ms"]
+    out["ext_cg_n16_nt8"] = row
+    n, Nt = 8, 8
+    lat = Q.S2Trivalent(n)
+    De = Q.DiracExt(lat, 1.0, 0.1, Nt, at)
+    Ae = (torch.rand(Nt * (lat.n_links + lat.n_sites), dtype=torch.float64, device=dev, generator=gen) - 0.5) * 0.6
+    rng = Q.ParallelRng(lat, 21, n_slices=Nt)
+    res = []
+    gpu_s = _wall(torch, lambda: res.append(Q.hmc_ext(De, rng, Ae, 1.0, tmax=0.5, nsteps=4, nsteps_inner=4,
+                                                       tol=1e-10)), 3)
+    out["hmc_ext_n8_nt8"] = {"gpu_ms": 1e3 * gpu_s, "cg_iters": res[-1][2], "accepted": [r[0] for r in res],
+                             "config": "n=8, Nt=8, at=0.5, g^2=1, tau=0.5, 4 x 4 steps, tol 1e-10 FP64",
+                             "cpu_baseline": None, "cpu_note": "the oracle's S^2 x S^1 HMC runs on a dense "
+                             "operator (checked at n=2); no CPU sample at this size"}
+    return out
+
+
 def batched_throughput(torch, Q, dev, reps=3):
     """The multi-lattice batched configuration: 256 right-hand sides, 64 on each
     of n = 16, 32, 48, 64 (each with its own beta = 1.4 configuration and a mass
@@ -276,6 +419,20 @@ def profile_case(torch, which):
         for prec in (Q.PREC_F32, Q.PREC_BF16, Q.PREC_F64):
             r = apply_bandwidth(torch, Q, 512, prec, reps=3)
             print(json.dumps(r))
+    elif which == "ext":
+        # the S^2 x S^1 operator at n=64, Nt=16 (0.5 GB of hop blocks, above L2): 3 D applies
+        Nt = 16
+        lat = Q.S2Trivalent(64)
+        De = Q.DiracExt(lat, 1.0, 0.1, Nt, 0.5)
+        g = torch.Generator(device="cuda")
+        g.manual_seed(4)
+        De.update((torch.rand(Nt * (lat.n_links + lat.n_sites), dtype=torch.float64, device="cuda", generator=g)
+                   * 2 - 1) * np.pi)
+        v = torch.randn(Nt * 2 * lat.n_sites, dtype=torch.complex128, device="cuda", generator=g)
+        w = torch.empty_like(v)
+        for _ in range(3):
+            De.apply(w, v, Q.OP_D)
+        print(json.dumps({"norm": float(torch.linalg.vector_norm(w))}))
     elif which == "batched":
         # a quarter of the 256-RHS configuration (16 right-hand sides on each
         # of n = 16, 32, 48, 64; ~0.4 GB of fields, above L2) with the tile the
@@ -326,10 +483,12 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--profile", choices=["apply", "cg", "pcg", "ppcg", "batched"], default=None,
+    ap.add_argument("--no-paths", action="store_true", help="skip the timings of the HMC, overlap and S^2 x S^1 paths")
+    ap.add_argument("--profile", choices=["apply", "cg", "pcg", "ppcg", "batched", "ext"], default=None,
                     help="small self-contained case for ncu: 'apply' = D apply at n=512 (f32, bf16, f64; "
                          "HBM-resident), 'cg' = one n=64 mixed-precision solve, 'pcg' = 300 iterations of the "
-                         "n=64 preconditioned solve, 'ppcg' = the same with the pipelined one-barrier kernel")
+                         "n=64 preconditioned solve, 'ppcg' = the same with the pipelined one-barrier kernel, "
+                         "'batched' = 64 RHS over four lattices, 'ext' = S^2 x S^1 D apply at n=64, Nt=16")
     args = ap.parse_args()
     rank, world, local = env_rank()
     warmup = max(3, args.warmup)
@@ -431,6 +590,7 @@ def main():
 
     heldout = heldout_iterations(torch, Q, lat, pc, dev)
     batched = batched_throughput(torch, Q, dev)
+    paths = None if args.no_paths else paths_timings(torch, Q, dev, cpu=rank == 0 and not args.no_cpu_baseline)
 
     # ---- roofline of the dominant kernel ----------------------------------------------
     # algorithmic bytes per site per iteration (fp32 / bf16 halo storage):
@@ -477,6 +637,7 @@ def main():
                          "in apply_sweep"},
             "apply_sweep": sweep,
             "batched_256": batched,
+            "paths": paths,
             "e2e": {"value": e2e, "unit": "solves/s", "h2d_bytes_per_step": b.nbytes, "d2h_bytes_per_step": b.nbytes},
             "gpu_launches": args.steps * 4,  # |b| partials, unit-norm import, solver, scaled export
             "clocks": clocks_info}

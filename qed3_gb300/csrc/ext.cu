@@ -11,9 +11,12 @@
 // (:297-305).  Vectors are the reference's: index Nx s + 2 x + spin, Nx = 2 Ns.
 // Link angles: A[Nt][Nl] spatial then A[Nt][Ns] temporal (GaugeExt's layout).
 //
-// Spatial blocks per slice are formed once per link update; the apply is one
-// kernel per operator (a thread per site and slice).  CG on D^dag D is the
-// reference's MatPoly::solve recurrence in FP64 with device BLAS.
+// Spatial blocks per slice and the temporal phases e^{i A_t} are formed once
+// per link update (GB300's FP64 pipe is narrow: no sincos in the apply); the
+// apply is one kernel per operator, a thread per (slice, site) in the
+// reference's site order, so the spinor, block and phase streams are
+// coalesced and only the three spatial neighbour reads gather.  CG on
+// D^dag D is the reference's MatPoly::solve recurrence in FP64 with device BLAS.
 
 #include <cmath>
 #include <vector>
@@ -28,15 +31,27 @@ namespace qed3 {
 
 static inline int nblk(long long n, int t = 256) { return int((n + t - 1) / t); }
 
-// per-slice spatial blocks: H3[s][k][i] = e^{i sgn A_s[l]} G[k][i], Hd3 likewise
-__global__ void k_ext_set_links(int Ns, int Nl, int Nt, const int32_t* __restrict__ hop_link,
-                                const int8_t* __restrict__ hop_sign, const double* __restrict__ A,
-                                const M64* __restrict__ G, const M64* __restrict__ Gd, M64* __restrict__ H3,
-                                M64* __restrict__ Hd3) {
+// per-slice spatial blocks in reference site order: H3[s][k][x] = e^{i sgn A_s[l]} G[k][i(x)],
+// Hd3 likewise; then the temporal phases Pt[s][x] = e^{i A_t(s, x)}
+__global__ void k_ext_set_links(int Ns, int Nl, int Nt, const int32_t* __restrict__ iperm,
+                                const int32_t* __restrict__ hop_link, const int8_t* __restrict__ hop_sign,
+                                const double* __restrict__ A, const M64* __restrict__ G, const M64* __restrict__ Gd,
+                                M64* __restrict__ H3, M64* __restrict__ Hd3, double2* __restrict__ Pt) {
   const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (idx >= 3LL * Ns * Nt) return;
+  const long long nh = 3LL * Ns * Nt;
+  if (idx >= nh) {
+    const long long t = idx - nh;
+    if (t < (long long)Ns * Nt) {
+      double sn, cs;
+      sincos(A[size_t(Nt) * Nl + t], &sn, &cs);
+      Pt[t] = make_double2(cs, sn);
+    }
+    return;
+  }
   const int s = int(idx / (3LL * Ns));
-  const int q = int(idx % (3LL * Ns));
+  const int kx = int(idx % (3LL * Ns));
+  const int k = kx / Ns, x = kx % Ns;
+  const int q = k * Ns + iperm[x];
   const double a = double(hop_sign[q]) * A[size_t(s) * Nl + hop_link[q]];
   double sn, cs;
   sincos(a, &sn, &cs);
@@ -46,62 +61,56 @@ __global__ void k_ext_set_links(int Ns, int Nl, int Nt, const int32_t* __restric
   Hd3[idx] = M64{cmul(ph, gd.h00), cmul(ph, gd.h01), cmul(ph, gd.h10), cmul(ph, gd.h11)};
 }
 
-// out = op(D) in for op = D (adj = 0) or D^dag (adj = 1), reference order
-__global__ void k_ext_apply(int Ns, int Nt, int adj, const int32_t* __restrict__ nbr_ref,
-                            const int32_t* __restrict__ perm, const M64* __restrict__ H3,
-                            const double* __restrict__ diag3, const double* __restrict__ kt,
-                            const double* __restrict__ At, double r, const S64* __restrict__ in,
-                            S64* __restrict__ out) {
+// out = op(D) in for op = D (adj = 0) or D^dag (adj = 1), reference order;
+// thread (s, x) for reference site x
+__global__ void k_ext_apply(int Ns, int Nt, int adj, const int32_t* __restrict__ nbrR,
+                            const M64* __restrict__ H3, const double* __restrict__ diag3,
+                            const double* __restrict__ kt, const double2* __restrict__ Pt, double r,
+                            const S64* __restrict__ in, S64* __restrict__ out) {
   const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (idx >= (long long)Ns * Nt) return;
-  const int s = int(idx / Ns), i = int(idx % Ns);
-  const int x = perm[i];
+  const int s = int(idx / Ns), x = int(idx % Ns);
   const S64* vs = in + size_t(s) * Ns;
   const Sp64 self = ld64(vs, x);
-  const double dg = diag3[i];
+  const double dg = diag3[x];
   Sp64 o{cscale(dg, self.s0), cscale(dg, self.s1)};
 #pragma unroll
   for (int k = 0; k < 3; k++) {
-    const M64 m = H3[(size_t(s) * 3 + k) * Ns + i];
-    const Sp64 b = ld64(vs, nbr_ref[size_t(k) * Ns + i]);
+    const M64 m = H3[(size_t(s) * 3 + k) * Ns + x];
+    const Sp64 b = ld64(vs, nbrR[size_t(k) * Ns + x]);
     o.s0 = cfma(m.h00, b.s0, o.s0);
     o.s0 = cfma(m.h01, b.s1, o.s0);
     o.s1 = cfma(m.h10, b.s0, o.s1);
     o.s1 = cfma(m.h11, b.s1, o.s1);
   }
   if (Nt > 1) {
-    const double kh = 0.5 * kt[i];
+    const double kh = 0.5 * kt[x];
     const int sp = (s + 1) % Nt, sm = (s + Nt - 1) % Nt;
     const Sp64 up = ld64(in + size_t(sp) * Ns, x), dn = ld64(in + size_t(sm) * Ns, x);
     // spin-diagonal coefficients (upper, lower) and phases of the two hops
-    double cu0, cu1, cd0, cd1, au, ad;
+    double cu0, cu1, cd0, cd1;
     if (!adj) {
       // from (x, s+1): tmpM(s+1) = 0.5 sM(s+1) kt (-r + sigma3) e^{+i A_t(s,x)}
       const double sgn_u = (sp == 0) ? -1.0 : 1.0;
       cu0 = sgn_u * kh * (-r + 1.0);
       cu1 = sgn_u * kh * (-r - 1.0);
-      au = At[size_t(s) * Ns + x];
       // from (x, s-1): tmpP(s-1) = 0.5 sP(s-1) kt (-r - sigma3) e^{-i A_t(s-1,x)}
       const double sgn_d = (sm == Nt - 1) ? -1.0 : 1.0;
       cd0 = sgn_d * kh * (-r - 1.0);
       cd1 = sgn_d * kh * (-r + 1.0);
-      ad = -At[size_t(sm) * Ns + x];
     } else {
       // conj(D[(x,s+1),(x,s)]) = conj(tmpP(s)): sP(s) kt/2 (-r - sigma3) e^{+i A_t(s,x)}
       const double sgn_u = (s == Nt - 1) ? -1.0 : 1.0;
       cu0 = sgn_u * kh * (-r - 1.0);
       cu1 = sgn_u * kh * (-r + 1.0);
-      au = At[size_t(s) * Ns + x];
       // conj(D[(x,s-1),(x,s)]) = conj(tmpM(s)): sM(s) kt/2 (-r + sigma3) e^{-i A_t(s-1,x)}
       const double sgn_d = (s == 0) ? -1.0 : 1.0;
       cd0 = sgn_d * kh * (-r + 1.0);
       cd1 = sgn_d * kh * (-r - 1.0);
-      ad = -At[size_t(sm) * Ns + x];
     }
-    double su, cu, sd, cdn;
-    sincos(au, &su, &cu);
-    sincos(ad, &sd, &cdn);
-    const double2 pu = make_double2(cu, su), pd = make_double2(cdn, sd);
+    // both cases: up hop e^{+i A_t(s,x)}, down hop e^{-i A_t(s-1,x)}
+    const double2 pu = Pt[size_t(s) * Ns + x], pdc = Pt[size_t(sm) * Ns + x];
+    const double2 pd = make_double2(pdc.x, -pdc.y);
     o.s0 = cadd(o.s0, cadd(cscale(cu0, cmul(pu, up.s0)), cscale(cd0, cmul(pd, dn.s0))));
     o.s1 = cadd(o.s1, cadd(cscale(cu1, cmul(pu, up.s1)), cscale(cd1, cmul(pd, dn.s1))));
   }
@@ -119,11 +128,10 @@ __global__ void k_ext_force_sp(int Ns, int Nl, int Nt, const int32_t* __restrict
   const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (idx >= (long long)Nl * Nt) return;
   const int s = int(idx / Nl), l = int(idx % Nl);
-  const int x = lx[l], y = ly[l];
-  const M64 hxy = H3[(size_t(s) * 3 + kx[l]) * Ns + x], hyx = H3[(size_t(s) * 3 + ky[l]) * Ns + y];
+  const int xr = perm[lx[l]], yr = perm[ly[l]];
+  const M64 hxy = H3[(size_t(s) * 3 + kx[l]) * Ns + xr], hyx = H3[(size_t(s) * 3 + ky[l]) * Ns + yr];
   const S64* es = eta + size_t(s) * Ns;
   const S64* ds = deta + size_t(s) * Ns;
-  const int xr = perm[x], yr = perm[y];
   const Sp64 ex = ld64(es, xr), ey = ld64(es, yr), dx = ld64(ds, xr), dy = ld64(ds, yr);
   const double2 u0 = cfma(hxy.h01, ey.s1, cmul(hxy.h00, ey.s0));
   const double2 u1 = cfma(hxy.h11, ey.s1, cmul(hxy.h10, ey.s0));
@@ -137,17 +145,16 @@ __global__ void k_ext_force_sp(int Ns, int Nl, int Nt, const int32_t* __restrict
 // Temporal link (s, x) from (x, s) to (x, s+1): D[(x,s+1),(x,s)] = tmpP(s) ~ e^{-iA}
 // and D[(x,s),(x,s+1)] = tmpM(s+1) ~ e^{+iA}, both with the sign -1 at s = Nt-1:
 //   F = -2 Re[ (D eta)_{s+1}^dag (-i tmpP eta_s) + (D eta)_s^dag (i tmpM eta_{s+1}) ]
-__global__ void k_ext_force_tp(int Ns, int Nl, int Nt, const int32_t* __restrict__ perm,
-                               const double* __restrict__ kt, const double* __restrict__ At, double r,
-                               const S64* __restrict__ eta, const S64* __restrict__ deta, double* __restrict__ F) {
+__global__ void k_ext_force_tp(int Ns, int Nl, int Nt, const double* __restrict__ kt,
+                               const double2* __restrict__ Pt, double r, const S64* __restrict__ eta,
+                               const S64* __restrict__ deta, double* __restrict__ F) {
   const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (idx >= (long long)Ns * Nt) return;
-  const int s = int(idx / Ns), i = int(idx % Ns);
-  const int x = perm[i], s1 = (s + 1) % Nt;
+  const int s = int(idx / Ns), x = int(idx % Ns);
+  const int s1 = (s + 1) % Nt;
   const double sg = (s == Nt - 1) ? -1.0 : 1.0;
-  const double kh = 0.5 * kt[i] * sg;
-  double sn, cs;
-  sincos(At[size_t(s) * Ns + x], &sn, &cs);
+  const double kh = 0.5 * kt[x] * sg;
+  const double cs = Pt[idx].x, sn = Pt[idx].y;
   const Sp64 e0 = ld64(eta + size_t(s) * Ns, x), e1 = ld64(eta + size_t(s1) * Ns, x);
   const Sp64 d0 = ld64(deta + size_t(s) * Ns, x), d1 = ld64(deta + size_t(s1) * Ns, x);
   // tmpP eta_s: spin-diagonal (-r-1, -r+1) kh e^{-iA};  tmpM eta_{s+1}: (-r+1, -r-1) kh e^{+iA}
@@ -164,19 +171,25 @@ int ext_init(qed3_dirac_ext_s* e) {
   qed3_dirac_s* d = e->d2;
   const HostLattice& L = d->lat->host;
   const int Ns = d->Ns, Nt = e->Nt;
+  // per-site tables in reference order (the apply's thread order)
   std::vector<double> kt(Ns), diag2(Ns), diag3(Ns);
+  std::vector<int32_t> nbr(size_t(3) * Ns), nbrR(size_t(3) * Ns);
   QED3_CUDA_TRY(cudaMemcpy(diag2.data(), d->diag, Ns * sizeof(double), cudaMemcpyDeviceToHost));
+  QED3_CUDA_TRY(cudaMemcpy(nbr.data(), d->lat->dev.nbr_ref, nbr.size() * sizeof(int32_t), cudaMemcpyDeviceToHost));
   for (int i = 0; i < Ns; i++) {
     const int x = L.perm[i];
-    kt[i] = Nt != 1 ? L.tri_area[x] / L.mean_ell / e->at : 0.0;
-    diag3[i] = diag2[i] + e->r * kt[i];
+    kt[x] = Nt != 1 ? L.tri_area[x] / L.mean_ell / e->at : 0.0;
+    diag3[x] = diag2[i] + e->r * kt[x];
+    for (int k = 0; k < 3; k++) nbrR[size_t(k) * Ns + x] = nbr[size_t(k) * Ns + i];
   }
   const size_t nh = size_t(3) * Ns * Nt;
   QED3_CUDA_TRY(cudaMalloc(&e->H3, nh * sizeof(M64)));
   QED3_CUDA_TRY(cudaMalloc(&e->Hd3, nh * sizeof(M64)));
   QED3_CUDA_TRY(cudaMalloc(&e->kt, Ns * sizeof(double)));
   QED3_CUDA_TRY(cudaMalloc(&e->diag3, Ns * sizeof(double)));
-  QED3_CUDA_TRY(cudaMalloc(&e->At, size_t(Ns) * Nt * sizeof(double)));
+  QED3_CUDA_TRY(cudaMalloc(&e->Pt, size_t(Ns) * Nt * sizeof(double2)));
+  QED3_CUDA_TRY(cudaMalloc(&e->nbrR, nbrR.size() * sizeof(int32_t)));
+  QED3_CUDA_TRY(cudaMemcpy(e->nbrR, nbrR.data(), nbrR.size() * sizeof(int32_t), cudaMemcpyHostToDevice));
   QED3_CUDA_TRY(cudaMalloc(&e->tmp, size_t(Ns) * Nt * sizeof(S64)));
   QED3_CUDA_TRY(cudaMalloc(&e->work, size_t(Ns) * Nt * 3 * sizeof(S64) + 2048 * sizeof(double)));
   QED3_CUDA_TRY(cudaMemcpy(e->kt, kt.data(), Ns * sizeof(double), cudaMemcpyHostToDevice));
@@ -185,7 +198,7 @@ int ext_init(qed3_dirac_ext_s* e) {
 }
 
 void ext_free(qed3_dirac_ext_s* e) {
-  void* p[] = {e->H3, e->Hd3, e->kt, e->diag3, e->At, e->tmp, e->work};
+  void* p[] = {e->H3, e->Hd3, e->kt, e->diag3, e->Pt, e->nbrR, e->tmp, e->work};
   for (void* q : p)
     if (q) cudaFree(q);
 }
@@ -194,11 +207,9 @@ int ext_set_links(qed3_dirac_ext_s* e, const double* A, cudaStream_t st) {
   qed3_dirac_s* d = e->d2;
   const DeviceLattice& D = d->lat->dev;
   const int Ns = d->Ns, Nl = D.Nl, Nt = e->Nt;
-  k_ext_set_links<<<nblk(3LL * Ns * Nt), 256, 0, st>>>(Ns, Nl, Nt, D.hop_link, D.hop_sign, A, d->G, d->Gd, e->H3,
-                                                      e->Hd3);
+  k_ext_set_links<<<nblk(4LL * Ns * Nt), 256, 0, st>>>(Ns, Nl, Nt, D.iperm, D.hop_link, D.hop_sign, A, d->G, d->Gd,
+                                                      e->H3, e->Hd3, e->Pt);
   QED3_CUDA_TRY(cudaGetLastError());
-  QED3_CUDA_TRY(cudaMemcpyAsync(e->At, A + size_t(Nt) * Nl, size_t(Ns) * Nt * sizeof(double),
-                                cudaMemcpyDeviceToDevice, st));
   e->links_set = true;
   return QED3_OK;
 }
@@ -210,8 +221,8 @@ int ext_apply(qed3_dirac_ext_s* e, int op, double* out, const double* in, cudaSt
   const int Ns = d->Ns, Nt = e->Nt;
   const long long n = (long long)Ns * Nt;
   auto run = [&](int adj, S64* o, const S64* v) {
-    k_ext_apply<<<nblk(n), 256, 0, st>>>(Ns, Nt, adj, D.nbr_ref, D.perm, adj ? e->Hd3 : e->H3, e->diag3, e->kt,
-                                        e->At, d->r, v, o);
+    k_ext_apply<<<nblk(n), 256, 0, st>>>(Ns, Nt, adj, e->nbrR, adj ? e->Hd3 : e->H3, e->diag3, e->kt, e->Pt, d->r,
+                                        v, o);
   };
   const S64* v = reinterpret_cast<const S64*>(in);
   S64* o = reinterpret_cast<S64*>(out);
@@ -246,7 +257,7 @@ int ext_fermion_force(qed3_dirac_ext_s* e, const double* eta, double* F, cudaStr
   k_ext_force_sp<<<nblk((long long)Nl * Nt), 256, 0, st>>>(Ns, Nl, Nt, D.link_x, D.link_y, D.link_kx, D.link_ky, D.perm,
                                                           e->H3, et, deta, F);
   if (Nt > 1)
-    k_ext_force_tp<<<nblk((long long)Ns * Nt), 256, 0, st>>>(Ns, Nl, Nt, D.perm, e->kt, e->At, d->r, et, deta, F);
+    k_ext_force_tp<<<nblk((long long)Ns * Nt), 256, 0, st>>>(Ns, Nl, Nt, e->kt, e->Pt, d->r, et, deta, F);
   else
     QED3_CUDA_TRY(cudaMemsetAsync(F + size_t(Nt) * Nl, 0, size_t(Ns) * sizeof(double), st));
   QED3_CUDA_TRY(cudaGetLastError());

@@ -9,11 +9,12 @@ struct qed3_dirac_ext_s {
   qed3_dirac_s* d2 = nullptr;  // the dual-lattice operator: geometry blocks, kappa, diagonal
   int Nt = 1;
   double at = 1.0, r = 1.0;
-  qed3::M64* H3 = nullptr;     // [Nt][3][Ns] spatial blocks of D per slice (internal site order)
+  qed3::M64* H3 = nullptr;     // [Nt][3][Ns] spatial blocks of D per slice (reference site order)
   qed3::M64* Hd3 = nullptr;    // [Nt][3][Ns] the same for D^dagger
-  double* kt = nullptr;        // [Ns] kappa_t (internal order)
-  double* diag3 = nullptr;     // [Ns]
-  double* At = nullptr;        // [Nt][Ns] temporal angles (reference order)
+  double* kt = nullptr;        // [Ns] kappa_t (reference order)
+  double* diag3 = nullptr;     // [Ns] (reference order)
+  double2* Pt = nullptr;       // [Nt][Ns] temporal phases e^{i A_t} (reference order)
+  int32_t* nbrR = nullptr;     // [3][Ns] reference ids of the neighbours of reference site x
   qed3::S64* tmp = nullptr;    // [Nt][Ns]
   void* work = nullptr;        // CG vectors
   bool links_set = false;
