@@ -18,6 +18,7 @@
 // coalesced and only the three spatial neighbour reads gather.  CG on
 // D^dag D is the reference's MatPoly::solve recurrence in FP64 with device BLAS.
 
+#include <algorithm>
 #include <cmath>
 #include <vector>
 
@@ -264,6 +265,95 @@ int ext_fermion_force(qed3_dirac_ext_s* e, const double* eta, double* F, cudaStr
   return QED3_OK;
 }
 
+// ---- CG with device-resident scalars ------------------------------------------
+// alpha, beta and the residual norm stay on the device: one iteration is the
+// operator and five small kernels, with no host round trip.  Once the
+// recursive residual meets the tolerance (or turns non-finite) the state's
+// `done` flag makes the remaining kernels of the launched chunk return at
+// once, so the iterate and the iteration count are those of the host-driven
+// recurrence; the host reads the state once per chunk.
+struct ExtCgState {
+  double mu, thr, alpha, beta, done, iters;  // done: 0 running, 1 converged, 2 non-finite
+};
+constexpr int kCgParts = 304;  // partial sums: two blocks per SM
+
+__global__ void k_cg_pq(long long nc, const double2* __restrict__ p, const double2* __restrict__ q,
+                        double* __restrict__ part, const ExtCgState* __restrict__ stt) {
+  if (stt->done != 0.0) return;
+  __shared__ double sh[32];
+  double v[1] = {0.0};
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < nc; i += (long long)gridDim.x * blockDim.x) {
+    const double2 a = p[i], b = q[i];
+    v[0] += a.x * b.x + a.y * b.y;
+  }
+  block_sum<1>(v, sh);
+  if (threadIdx.x == 0) part[blockIdx.x] = v[0];
+}
+
+// alpha = mu / Re<p, A p> (one block; fixed summation order)
+__global__ void k_cg_alpha(const double* __restrict__ part, int np, ExtCgState* __restrict__ stt) {
+  if (stt->done != 0.0) return;
+  __shared__ double sh[32];
+  double v[1] = {0.0};
+  for (int i = threadIdx.x; i < np; i += blockDim.x) v[0] += part[i];
+  block_sum<1>(v, sh);
+  if (threadIdx.x == 0) stt->alpha = stt->mu / v[0];
+}
+
+// x += alpha p, r -= alpha q, partial sums of |r|^2
+__global__ void k_cg_xr(long long nc, const double2* __restrict__ p, const double2* __restrict__ q,
+                        double2* __restrict__ x, double2* __restrict__ r, double* __restrict__ part,
+                        const ExtCgState* __restrict__ stt) {
+  if (stt->done != 0.0) return;
+  __shared__ double sh[32];
+  const double al = stt->alpha;
+  double v[1] = {0.0};
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < nc; i += (long long)gridDim.x * blockDim.x) {
+    const double2 pp = p[i], qq = q[i];
+    double2 xx = x[i], rr = r[i];
+    xx.x += al * pp.x;
+    xx.y += al * pp.y;
+    rr.x -= al * qq.x;
+    rr.y -= al * qq.y;
+    x[i] = xx;
+    r[i] = rr;
+    v[0] += rr.x * rr.x + rr.y * rr.y;
+  }
+  block_sum<1>(v, sh);
+  if (threadIdx.x == 0) part[blockIdx.x] = v[0];
+}
+
+// |r|^2, the stopping test, beta = |r|^2 / mu
+__global__ void k_cg_beta(const double* __restrict__ part, int np, ExtCgState* __restrict__ stt) {
+  if (stt->done != 0.0) return;
+  __shared__ double sh[32];
+  double v[1] = {0.0};
+  for (int i = threadIdx.x; i < np; i += blockDim.x) v[0] += part[i];
+  block_sum<1>(v, sh);
+  if (threadIdx.x == 0) {
+    const double mn = v[0];
+    stt->iters += 1.0;
+    if (!isfinite(mn)) {
+      stt->done = 2.0;
+    } else if (mn < stt->thr) {
+      stt->done = 1.0;
+    } else {
+      stt->beta = mn / stt->mu;
+      stt->mu = mn;
+    }
+  }
+}
+
+__global__ void k_cg_p(long long nc, const double2* __restrict__ r, double2* __restrict__ p,
+                       const ExtCgState* __restrict__ stt) {
+  if (stt->done != 0.0) return;
+  const double bt = stt->beta;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < nc; i += (long long)gridDim.x * blockDim.x) {
+    const double2 rr = r[i], pp = p[i];
+    p[i] = make_double2(rr.x + bt * pp.x, rr.y + bt * pp.y);
+  }
+}
+
 // MatPoly::solve (src/dual/matpoly.h:204-267) on D^dag D + shift in FP64:
 // x0 = 0, stop on the recursive residual, certified by the true residual.
 int ext_cg(qed3_dirac_ext_s* e, double* x, const double* b, const qed3_solve_params* prm, qed3_solve_report* rep,
@@ -294,25 +384,32 @@ int ext_cg(qed3_dirac_ext_s* e, double* x, const double* b, const qed3_solve_par
   QED3_CUDA_TRY(cudaMemsetAsync(x, 0, nd * sizeof(double), st));
   QED3_CUDA_TRY(cudaMemcpyAsync(r, b, nd * sizeof(double), cudaMemcpyDeviceToDevice, st));
   QED3_CUDA_TRY(cudaMemcpyAsync(p, b, nd * sizeof(double), cudaMemcpyDeviceToDevice, st));
-  double mu = bb;
-  int it = 0, status = bb == 0.0 ? QED3_OK : QED3_ERR_NOCONV;
-  while (status != QED3_OK && it < maxiter) {
-    if ((rc = A(q, p))) return rc;
-    double pq = 0;
-    if ((rc = vec_zdot(nc, p, q, part, &pq, &im, st))) return rc;
-    const double al = mu / pq;
-    if ((rc = vec_axpby(nd, al, p, 1.0, x, x, st)) || (rc = vec_axpby(nd, -al, q, 1.0, r, r, st))) return rc;
-    double mn = 0;
-    if ((rc = vec_zdot(nc, r, r, part, &mn, &im, st))) return rc;
-    it++;
-    if (!std::isfinite(mn)) break;
-    if (mn < tol * tol * bb) {
-      status = QED3_OK;
-      break;
+  ExtCgState* dst = reinterpret_cast<ExtCgState*>(part + 1024);
+  ExtCgState hst{bb, tol * tol * bb, 0.0, 0.0, bb == 0.0 ? 1.0 : 0.0, 0.0};
+  QED3_CUDA_TRY(cudaMemcpyAsync(dst, &hst, sizeof(hst), cudaMemcpyHostToDevice, st));
+  const double2* p2 = reinterpret_cast<const double2*>(p);
+  const double2* q2 = reinterpret_cast<const double2*>(q);
+  const int gblk = int(std::min<long long>(kCgParts, (nc + 255) / 256));
+  int launched = 0;
+  const int chunk = 16;
+  while (hst.done == 0.0 && launched < maxiter) {
+    const int m = std::min(chunk, maxiter - launched);
+    for (int k = 0; k < m; k++) {
+      if ((rc = A(q, p))) return rc;
+      k_cg_pq<<<gblk, 256, 0, st>>>(nc, p2, q2, part, dst);
+      k_cg_alpha<<<1, 256, 0, st>>>(part, gblk, dst);
+      k_cg_xr<<<gblk, 256, 0, st>>>(nc, p2, q2, reinterpret_cast<double2*>(x), reinterpret_cast<double2*>(r), part,
+                                    dst);
+      k_cg_beta<<<1, 256, 0, st>>>(part, gblk, dst);
+      k_cg_p<<<gblk, 256, 0, st>>>(nc, reinterpret_cast<const double2*>(r), reinterpret_cast<double2*>(p), dst);
     }
-    if ((rc = vec_axpby(nd, 1.0, r, mn / mu, p, p, st))) return rc;
-    mu = mn;
+    QED3_CUDA_TRY(cudaGetLastError());
+    launched += m;
+    QED3_CUDA_TRY(cudaMemcpyAsync(&hst, dst, sizeof(hst), cudaMemcpyDeviceToHost, st));
+    QED3_CUDA_TRY(cudaStreamSynchronize(st));
   }
+  const int it = int(hst.iters);
+  const int status = hst.done == 1.0 ? QED3_OK : QED3_ERR_NOCONV;
   double tr = 0;
   if (bb > 0) {
     if ((rc = A(q, x)) || (rc = vec_axpby(nd, 1.0, b, -1.0, q, q, st)) || (rc = vec_zdot(nc, q, q, part, &tr, &im, st)))
