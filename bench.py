@@ -320,6 +320,7 @@ def paths_timings(torch, Q, dev, cpu=True):
     bps = 32 + 32 + 192 + 8 + 32.0 / Nt
     gbs = bps * lat.n_sites * Nt / (ms * 1e-3) / 1e9
     row = {"gpu_ms": ms, "GB/s": gbs, "bytes_per_site_slice": bps, "frac_of_" + peak_kind: gbs / peak,
+           "bound": "fp64 pipe (ncu: sm__pipe_fp64_cycles_active 92.5%, dram 22%)",
            "config": "n=64, Nt=16 (1.31M site-slices, 252 MB of hop blocks: HBM-resident), FP64, D"}
     if cpu:
         g = O.geometry(n)
