@@ -115,6 +115,13 @@ int qed3_lattice_set_spin_structure(qed3_lattice* lat, const double* omega, cons
  *           + sum_y kappa_l/2 (-r + gamma_xy) e^{i A_xy} Omega_xy psi_y
  * ====================================================================== */
 int qed3_dirac_create(qed3_lattice* lat, double r, double M5, qed3_dirac** out);
+/* Dirac1fonS2 (src/dual/dirac.h:145-220) on the same layout: hop blocks
+ * -(vol_x/vbar)(r u_{x,k} - v_{x,k}.sigma) Omega e^{iU}, diagonal
+ * sum_k (vol_x/vbar)(r u_{x,k} + m/3) + M5, with the u, v tables of
+ * integrator/test_sorting.cc:499-594 computed from the lattice (vol_x: area of
+ * x's triangle).  Every other call (set_links, apply, solvers, force) is the
+ * same as for qed3_dirac_create's operator. */
+int qed3_dirac_create_1f(qed3_lattice* lat, double r, double m, double M5, qed3_dirac** out);
 int qed3_dirac_destroy(qed3_dirac* d);
 /* DWDevice::update(U) (src/both_3d/sparse_dirac.h:144-151): rebuild every hop
  * matrix on the device from link angles A[n_links] (host or device pointer). */

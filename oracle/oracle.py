@@ -764,3 +764,63 @@ def hmc_ext(geom: Geometry, rng: Rng, A: np.ndarray, r: float, M5: float, Nt: in
         return True, dH, its[0]
     A[:] = A0
     return False, dH, its[0]
+
+
+def dirac1f_tables(geom: Geometry):
+    """The u, v tables of integrator/test_sorting.cc:499-594 (us_*, vs_*):
+    per site x, hop vectors ell_k = acos(x . y_k) (cos alpha_k, sin alpha_k);
+    v from [d13 d23] (v1_c, v2_c) = (a/sqrt3) e_c, v3 = -v1 - v2,
+    a = sqrt(4/sqrt3 vbar), vbar the mean triangle area; u = (1, p, q) with
+    [ell2 ell3](p, q) = -ell1, then u *= 3/mean(u).  Returns (u [Ns,3], v [Ns,3,2],
+    vol [Ns], vbar), solving each small system with numpy."""
+    vol = triangle_areas(geom)
+    vbar = float(np.mean(vol))
+    alat = np.sqrt(4.0 / np.sqrt(3.0) * vbar)
+    Ns = geom.n_sites
+    u = np.zeros((Ns, 3))
+    v = np.zeros((Ns, 3, 2))
+    for x in range(Ns):
+        el = []
+        for k in range(3):
+            y = int(geom.nns[x][k])
+            c = float(np.dot(geom.sites[x], geom.sites[y]))
+            ln = np.pi if c < -1 else (0.0 if c > 1 else np.arccos(c))
+            al = geom.alpha[x][k]
+            el.append(ln * np.array([np.cos(al), np.sin(al)]))
+        d13, d23 = el[0] - el[2], el[1] - el[2]
+        mat = np.array([[d13[0], d23[0], 0, 0], [d13[1], d23[1], 0, 0], [0, 0, d13[0], d23[0]],
+                        [0, 0, d13[1], d23[1]]])
+        vv = np.linalg.solve(mat, np.array([1.0, 0.0, 0.0, 1.0]) * alat / np.sqrt(3.0))
+        v[x, 0] = (vv[0], vv[2])
+        v[x, 1] = (vv[1], vv[3])
+        v[x, 2] = -v[x, 0] - v[x, 1]
+        pq = np.linalg.solve(np.array([[el[1][0], el[2][0]], [el[1][1], el[2][1]]]), -el[0])
+        uu = np.array([1.0, pq[0], pq[1]])
+        u[x] = uu * (3.0 / uu.mean())
+    return u, v, vol, vbar
+
+
+def dirac1f_matrix(geom: Geometry, r: float, m: float, M5: float, A: np.ndarray) -> np.ndarray:
+    """Dirac1fonS2::matrix_form(U) (src/dual/dirac.h:170-183) as a dense matrix:
+    block (x, y_k) -= (vol_x/vbar)(r u_k - gamma_k) e^{iU(x,y)} Omega(x,y),
+    block (x, x) += (vol_x/vbar)(r u_k + m/3) + M5/3 for each k."""
+    u, v, vol, vbar = dirac1f_tables(geom)
+    Ns = geom.n_sites
+    s1 = np.array([[0, 1], [1, 0]], complex)
+    s2 = np.array([[0, -1j], [1j, 0]], complex)
+    sgn = {}
+    for l, (i, j) in enumerate(geom.links):
+        sgn[(int(i), int(j))] = (l, 1.0)
+        sgn[(int(j), int(i))] = (l, -1.0)
+    M = np.zeros((2 * Ns, 2 * Ns), complex)
+    for x in range(Ns):
+        for k in range(3):
+            y = int(geom.nns[x][k])
+            l, sg = sgn[(x, y)]
+            om = sg * geom.omega[l]
+            Om = np.diag([np.exp(-0.5j * om), np.exp(0.5j * om)])
+            gam = v[x, k, 0] * s1 + v[x, k, 1] * s2
+            w = vol[x] / vbar
+            M[2 * x:2 * x + 2, 2 * y:2 * y + 2] -= w * (r * u[x, k] * np.eye(2) - gam) * np.exp(1j * sg * A[l]) @ Om
+            M[2 * x:2 * x + 2, 2 * x:2 * x + 2] += (w * (r * u[x, k] + m / 3.0) + M5 / 3.0) * np.eye(2)
+    return M

@@ -80,6 +80,8 @@ SIGNATURES = [
     ("qed3_lattice_set_spin_structure", ctypes.c_int, [vp, vp, vp]),
     ("qed3_lattice_permutation", ctypes.c_int, [vp, vp]),
     ("qed3_dirac_create", ctypes.c_int, [vp, ctypes.c_double, ctypes.c_double, ctypes.POINTER(vp)]),
+    ("qed3_dirac_create_1f", ctypes.c_int, [vp, ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                                            ctypes.POINTER(vp)]),
     ("qed3_dirac_destroy", ctypes.c_int, [vp]),
     ("qed3_dirac_set_links", ctypes.c_int, [vp, vp, ctypes.c_int, vp]),
     ("qed3_dirac_set_coefficients", ctypes.c_int, [vp, vp, vp]),
@@ -297,12 +299,17 @@ class DiracS2Dual:
     enters as M5, as in the reference where DiracS2Dual::m is unused.
     """
 
-    def __init__(self, lattice: S2Trivalent, r: float = 1.0, M5: float = 0.0):
+    def __init__(self, lattice: S2Trivalent, r: float = 1.0, M5: float = 0.0, one_flavor_mass: float | None = None):
+        """one_flavor_mass = m: Dirac1fonS2's coefficients (src/dual/dirac.h:145-220)
+        instead of DiracS2Dual's, with its real mass m."""
         self.lattice = lattice
         self.r, self.M5 = r, M5
         self.N = 2 * lattice.n_sites
         h = vp()
-        _check(lib().qed3_dirac_create(lattice.handle, r, M5, ctypes.byref(h)))
+        if one_flavor_mass is None:
+            _check(lib().qed3_dirac_create(lattice.handle, r, M5, ctypes.byref(h)))
+        else:
+            _check(lib().qed3_dirac_create_1f(lattice.handle, r, one_flavor_mass, M5, ctypes.byref(h)))
         self._h = h
 
     @property

@@ -230,6 +230,20 @@ int qed3_lattice_permutation(const qed3_lattice* lat, int* perm) {
   return QED3_OK;
 }
 
+int qed3_dirac_create_1f(qed3_lattice* lat, double r, double m, double M5, qed3_dirac** out) {
+  QED3_GUARD_BEGIN
+  if (!lat || !out) return fail(QED3_ERR_ARG, "NULL argument");
+  int rc = qed3_dirac_create(lat, r, M5, out);
+  if (rc) return rc;
+  rc = dirac_use_1f(*out, m);
+  if (rc) {
+    qed3_dirac_destroy(*out);
+    *out = nullptr;
+  }
+  return rc;
+  QED3_GUARD_END
+}
+
 int qed3_dirac_create(qed3_lattice* lat, double r, double M5, qed3_dirac** out) {
   QED3_GUARD_BEGIN
   if (!lat || !out) return fail(QED3_ERR_ARG, "NULL argument");

@@ -275,6 +275,111 @@ int dirac_init_device(qed3_dirac_s* d) {
   return QED3_OK;
 }
 
+// ---------------------------------------------------------------------------
+// Dirac1fonS2 (src/dual/dirac.h:145-220) on the same 3-hop layout.  Per site x
+// and hop k to y = nns[x][k]:
+//   D[x,y] = -(vol_x / vbar) (r u_{x,k} - v_{x,k} . (sigma1, sigma2)) Omega(x,y) e^{iU(x,y)},
+//   D[x,x] = sum_k (vol_x / vbar) (r u_{x,k} + m/3) + M5,
+// vol_x the spherical area of x's triangle, vbar their mean.  u and v are the
+// tables integrator/test_sorting.cc:499-594 writes (us_*, vs_*), computed here
+// from the hop vectors ell_k = |x y_k| (cos alpha_k, sin alpha_k):
+//   v: sum_k ell_k v_k^T = (a/sqrt 3) 1 with v_3 = -v_1 - v_2, a = sqrt(4 vbar / sqrt 3);
+//   u: u_1 ell_1 + u_2 ell_2 + u_3 ell_3 = 0 with u_1 = 1, then u *= 3 / mean(u).
+// ---------------------------------------------------------------------------
+static double acos_clamped(double c) { return c < -1.0 ? M_PI : (c > 1.0 ? 0.0 : std::acos(c)); }
+
+static void tables_1f(const HostLattice& L, int x, double alat, double u[3], double v[3][2]) {
+  double el[3][2];
+  for (int k = 0; k < 3; k++) {
+    const int y = L.nns[3 * x + k];
+    const double* a = &L.sites[3 * size_t(x)];
+    const double* b = &L.sites[3 * size_t(y)];
+    const double len = acos_clamped(a[0] * b[0] + a[1] * b[1] + a[2] * b[2]);
+    const double al = L.alpha[3 * x + k];
+    el[k][0] = len * std::cos(al);
+    el[k][1] = len * std::sin(al);
+  }
+  // [d13 d23] (v1_c, v2_c)^T = (a/sqrt3) e_c for c = x, y
+  const double d13[2] = {el[0][0] - el[2][0], el[0][1] - el[2][1]};
+  const double d23[2] = {el[1][0] - el[2][0], el[1][1] - el[2][1]};
+  const double det = d13[0] * d23[1] - d23[0] * d13[1];
+  const double c = alat / std::sqrt(3.0);
+  // inverse of [[d13x, d23x], [d13y, d23y]] = [[d23y, -d23x], [-d13y, d13x]] / det
+  v[0][0] = d23[1] * c / det;
+  v[1][0] = -d13[1] * c / det;
+  v[0][1] = -d23[0] * c / det;
+  v[1][1] = d13[0] * c / det;
+  v[2][0] = -v[0][0] - v[1][0];
+  v[2][1] = -v[0][1] - v[1][1];
+  // [ell2 ell3] (p, q)^T = -ell1
+  const double det2 = el[1][0] * el[2][1] - el[2][0] * el[1][1];
+  const double p = (-el[0][0] * el[2][1] + el[2][0] * el[0][1]) / det2;
+  const double q = (-el[1][0] * el[0][1] + el[0][0] * el[1][1]) / det2;
+  u[0] = 1.0;
+  u[1] = p;
+  u[2] = q;
+  const double mean = (u[0] + u[1] + u[2]) / 3.0;
+  for (int k = 0; k < 3; k++) u[k] *= 3.0 / mean;
+}
+
+static void block_1f(const HostLattice& L, double r, double vbar, double alat, int x, int k, cd G[4]) {
+  double u[3], v[3][2];
+  tables_1f(L, x, alat, u, v);
+  const double w = L.tri_area[x] / vbar;
+  const double om = L.hop_sign[3 * x + k] * L.omega[L.hop_link[3 * x + k]];
+  const cd em(std::cos(0.5 * om), -std::sin(0.5 * om)), ep(std::cos(0.5 * om), std::sin(0.5 * om));
+  const cd gm(v[k][0], -v[k][1]), gp(v[k][0], v[k][1]);  // gamma = [[0, v0 - i v1], [v0 + i v1, 0]]
+  G[0] = -w * (r * u[k]) * em;
+  G[1] = w * gm * ep;
+  G[2] = w * gp * em;
+  G[3] = -w * (r * u[k]) * ep;
+}
+
+int dirac_use_1f(qed3_dirac_s* d, double m) {
+  const HostLattice& L = d->lat->host;
+  const int Ns = L.n_sites;
+  double vbar = 0.0;
+  for (double a : L.tri_area) vbar += a;
+  vbar /= Ns;
+  const double alat = std::sqrt(4.0 / std::sqrt(3.0) * vbar);
+  std::vector<M64> G(size_t(3) * Ns), Gd(size_t(3) * Ns);
+  std::vector<double> diag(Ns);
+  std::vector<float> diag32(Ns);
+  auto put = [](M64& o, const cd g[4], bool adj) {
+    if (!adj) {
+      o = M64{make_double2(g[0].real(), g[0].imag()), make_double2(g[1].real(), g[1].imag()),
+              make_double2(g[2].real(), g[2].imag()), make_double2(g[3].real(), g[3].imag())};
+    } else {  // conjugate transpose
+      o = M64{make_double2(g[0].real(), -g[0].imag()), make_double2(g[2].real(), -g[2].imag()),
+              make_double2(g[1].real(), -g[1].imag()), make_double2(g[3].real(), -g[3].imag())};
+    }
+  };
+  for (int i = 0; i < Ns; i++) {
+    const int x = L.perm[i];
+    double u[3], v[3][2];
+    tables_1f(L, x, alat, u, v);
+    const double w = L.tri_area[x] / vbar;
+    double dg = 0.0;
+    for (int k = 0; k < 3; k++) {
+      dg += w * (d->r * u[k] + m / 3.0);
+      cd g[4], gy[4];
+      block_1f(L, d->r, vbar, alat, x, k, g);
+      block_1f(L, d->r, vbar, alat, L.nns[3 * x + k], L.hop_back[3 * x + k], gy);
+      put(G[size_t(k) * Ns + i], g, false);
+      put(Gd[size_t(k) * Ns + i], gy, true);
+    }
+    diag[i] = dg + d->M5;
+    diag32[i] = float(diag[i]);
+  }
+  const size_t nm = size_t(3) * Ns;
+  QED3_CUDA_TRY(cudaMemcpy(d->G, G.data(), nm * sizeof(M64), cudaMemcpyHostToDevice));
+  QED3_CUDA_TRY(cudaMemcpy(d->Gd, Gd.data(), nm * sizeof(M64), cudaMemcpyHostToDevice));
+  QED3_CUDA_TRY(cudaMemcpy(d->diag, diag.data(), size_t(Ns) * sizeof(double), cudaMemcpyHostToDevice));
+  QED3_CUDA_TRY(cudaMemcpy(d->diag32, diag32.data(), size_t(Ns) * sizeof(float), cudaMemcpyHostToDevice));
+  d->coeffs_set = false;  // the hop blocks take the link phases at the next set_links
+  return QED3_OK;
+}
+
 int dirac_free_device(qed3_dirac_s* d) {
   void* ptrs[] = {d->G, d->Gd, d->H, d->Hd, d->H32, d->Hd32, d->diag, d->diag32, d->A_dev, d->tmp_in, d->tmp_out, d->tmp_mid};
   for (void* p : ptrs)

@@ -14,6 +14,8 @@ int dirac_init_device(qed3_dirac_s* d);
 int dirac_free_device(qed3_dirac_s* d);
 int dirac_set_links(qed3_dirac_s* d, const double* A, int on_device, cudaStream_t st);
 int dirac_set_coefficients(qed3_dirac_s* d, const double* hop, const double* diag);
+// replace the geometry blocks and diagonal by Dirac1fonS2's (mass m)
+int dirac_use_1f(qed3_dirac_s* d, double m);
 int dirac_apply_ref(qed3_dirac_s* d, int op, double* out, const double* in, cudaStream_t st);
 int dirac_apply_field(qed3_dirac_s* d, int op, int prec, void* out, const void* in, int nrhs, cudaStream_t st);
 // fp32 field apply with caller-supplied hop blocks (same lattice and diagonal)

@@ -224,3 +224,28 @@ def test_oriented_links_give_the_same_operator(cuda):
     Q.fermion_force(D2, eta, F2)
     sgn = torch.from_numpy(np.where(flip, -1.0, 1.0)).to(cuda)
     assert float((F1 - sgn * F2).abs().max()) < 1e-13 * float(F1.abs().max())
+
+
+@pytest.mark.parametrize("n", [2, 4])
+def test_dirac1f_matches_oracle(cuda, n):
+    """Dirac1fonS2's coefficients (u, v tables computed from the lattice) in the
+    3-hop kernels: D, D^dag, D^dag D = the oracle's dense matrix_form(U) to
+    1e-12; the FP32 solver on it is certified in FP64."""
+    import torch
+    g = O.geometry(n)
+    lat = Q.S2Trivalent(n)
+    rng = np.random.default_rng(70 + n)
+    A = rng.uniform(-np.pi, np.pi, g.n_links)
+    r, m, M5 = 1.0, 0.3, 0.1
+    D = Q.DiracS2Dual(lat, r, M5, one_flavor_mass=m)
+    D.update(to_dev(A, cuda))
+    M = O.dirac1f_matrix(g, r, m, M5, A)
+    v = rand_spinor(rng, g.n_sites)[0]
+    for op, ref in ((Q.OP_D, M @ v), (Q.OP_DDAG, M.conj().T @ v), (Q.OP_DDAGD, M.conj().T @ (M @ v))):
+        out = torch.zeros(v.size, dtype=torch.complex128, device=cuda)
+        D.apply(out, to_dev(v, cuda), op)
+        assert rel(from_dev(out), ref) < 1e-12, op
+    x = torch.zeros(v.size, dtype=torch.complex128, device=cuda)
+    rep = D.solve(x, to_dev(v, cuda), tol=1e-10, precision=Q.PREC_F32)
+    assert rep.status == Q.OK and rep.true_rel_res <= 1e-10
+    assert rel(from_dev(x), np.linalg.solve(M.conj().T @ M, v)) < 1e-7

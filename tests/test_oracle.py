@@ -429,3 +429,28 @@ def test_hmc_ext_deltaH_scales_as_tau_squared():
                 d.append(dH)
             rms.append(np.sqrt(np.mean(np.square(d))))
         assert 2.8 < rms[0] / rms[1] < 5.5, (integrator, rms)
+
+
+def test_dirac1f_tables_and_matrix():
+    """Dirac1fonS2's u, v tables (integrator/test_sorting.cc:499-594) restated:
+    sum_k ell_k v_k^T = (a/sqrt3) 1, sum_k u_k ell_k = 0, mean(u) = 3; the
+    dense matrix has the 3-hop sparsity and, at A = 0 and m = M5 = 0, rows
+    whose diagonal is sum_k (vol/vbar) r u_k."""
+    g = O.geometry(2)
+    u, v, vol, vbar = O.dirac1f_tables(g)
+    alat = np.sqrt(4.0 / np.sqrt(3.0) * vbar)
+    for x in range(g.n_sites):
+        el = []
+        for k in range(3):
+            y = g.nns[x][k]
+            ln = np.arccos(np.clip(np.dot(g.sites[x], g.sites[y]), -1, 1))
+            el.append(ln * np.array([np.cos(g.alpha[x][k]), np.sin(g.alpha[x][k])]))
+        S = sum(np.outer(el[k], v[x, k]) for k in range(3))
+        assert np.abs(S - alat / np.sqrt(3.0) * np.eye(2)).max() < 1e-12
+        assert np.abs(sum(u[x, k] * el[k] for k in range(3))).max() < 1e-12
+        assert abs(u[x].mean() - 3.0) < 1e-12
+    M = O.dirac1f_matrix(g, 1.0, 0.0, 0.0, np.zeros(g.n_links))
+    nz = (np.abs(M) > 0).reshape(g.n_sites, 2, g.n_sites, 2).any(axis=(1, 3))
+    assert nz.sum(1).max() == 4  # self + three neighbours
+    d = np.real(np.diag(M)[0::2])
+    assert np.allclose(d, vol / vbar * u.sum(1))
