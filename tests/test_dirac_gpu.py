@@ -240,7 +240,7 @@ def test_dirac1f_matches_oracle(cuda, n):
     D = Q.DiracS2Dual(lat, r, M5, one_flavor_mass=m)
     D.update(to_dev(A, cuda))
     M = O.dirac1f_matrix(g, r, m, M5, A)
-    v = rand_spinor(rng, g.n_sites)[0]
+    v = rand_spinor(rng, g.n_sites)
     for op, ref in ((Q.OP_D, M @ v), (Q.OP_DDAG, M.conj().T @ v), (Q.OP_DDAGD, M.conj().T @ (M @ v))):
         out = torch.zeros(v.size, dtype=torch.complex128, device=cuda)
         D.apply(out, to_dev(v, cuda), op)
