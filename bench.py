@@ -331,7 +331,20 @@ def paths_timings(torch, Q, dev, cpu=True):
                                "sample": "one D apply (per-slice CSR restatement incl. its per-slice link update)"}
         row["gpu_vs_cpu"] = row["cpu_baseline"]["ms"] / row["gpu_ms"]
     out["ext_apply_n64_nt16"] = row
-    del De, Ae, ve, we
+    # the same operator's FP64 and mixed-precision solve at the apply's size (FP64-pipe bound)
+    be = torch.randn(Nt * 2 * lat.n_sites, dtype=torch.complex128, device=dev, generator=gen)
+    xe = torch.empty_like(be)
+    Ae.mul_(0.2)  # a smoother field: a few hundred iterations
+    De.update(Ae)
+    solves = {}
+    for name, prec in (("f64", Q.PREC_F64), ("f32_mixed", Q.PREC_F32)):
+        rr = []
+        t_ = _wall(torch, lambda: rr.append(De.solve(xe, be, tol=1e-10, precision=prec)), 2)
+        solves[name] = {"gpu_ms": 1e3 * t_, "iters": rr[-1].iters, "reliable_updates": rr[-1].reliable_updates,
+                        "true_rel_res": rr[-1].true_rel_res}
+    out["ext_cg_n64_nt16"] = dict(solves, config="n=64, Nt=16, at=0.5, links 0.2 U[-pi,pi), tol 1e-10, "
+                                  "certified by the FP64 true residual")
+    del De, Ae, ve, we, be, xe
     # -- S^2 x S^1 FP64 CG on D^dag D and the S^2 x S^1 HMC trajectory
     n, Nt, at = 16, 8, 0.5
     lat = Q.S2Trivalent(n)
@@ -342,8 +355,12 @@ def paths_timings(torch, Q, dev, cpu=True):
     xe = torch.empty_like(be)
     reps_ = []
     gpu_s = _wall(torch, lambda: reps_.append(De.solve(xe, be, tol=1e-10)), 3)
+    rm = []
+    gpu_m = _wall(torch, lambda: rm.append(De.solve(xe, be, tol=1e-10, precision=Q.PREC_F32)), 3)
     row = {"gpu_ms": 1e3 * gpu_s, "iters": reps_[-1].iters, "true_rel_res": reps_[-1].true_rel_res,
-           "config": "n=16, Nt=8, at=0.5, links 0.6 U[-0.5,0.5), tol 1e-10 FP64"}
+           "mixed_f32": {"gpu_ms": 1e3 * gpu_m, "iters": rm[-1].iters, "reliable_updates": rm[-1].reliable_updates,
+                         "true_rel_res": rm[-1].true_rel_res},
+           "config": "n=16, Nt=8, at=0.5, links 0.6 U[-0.5,0.5), tol 1e-10; FP64 and FP32 + FP64 reliable updates"}
     if cpu:
         g = O.geometry(n)
         Ah, bh = Ae.cpu().numpy(), be.cpu().numpy()

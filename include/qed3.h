@@ -234,12 +234,15 @@ int qed3_dirac_ext_apply(qed3_dirac_ext* e, int op, double* out, const double* i
 int qed3_dirac_ext_fermion_force(qed3_dirac_ext* e, const double* eta, double* F, void* stream);
 /* Point-source propagator (src/both_3d/prop.cu:243-268): sink = D^{-1} src1
  * with src1 = 1 at (slice s, site ix of the reference numbering, spin a),
- * solved as (D^dag D)^{-1} D^dag src1 by the FP64 CG (params->tol; shift and
- * precision ignored); dagger != 0 (prop.cu's IS_DAGGER): sink = D^{-dag} src1
+ * solved as (D^dag D)^{-1} D^dag src1 by the CG (params->tol, ->precision
+ * F64 or F32 as for qed3_dirac_ext_cg_solve; shift ignored); dagger != 0 (prop.cu's IS_DAGGER): sink = D^{-dag} src1
  * = (D D^dag)^{-1} D src1.  sink: device complex128 [Nt][n_sites][2]; synchronous. */
 int qed3_dirac_ext_propagator(qed3_dirac_ext* e, int s, int ix, int a, int dagger, double* sink, const qed3_solve_params* params,
                               qed3_solve_report* report, void* stream);
-/* MatPoly::solve on D^dag D (+ params->shift) in FP64, certified by the true residual */
+/* MatPoly::solve on D^dag D (+ params->shift), certified by the FP64 true
+ * residual.  params->precision QED3_PREC_F64: the reference's FP64 recurrence;
+ * QED3_PREC_F32: FP32 iterations (FP32 copy of the operator) with FP64
+ * reliable updates whenever the residual has dropped by params->delta. */
 int qed3_dirac_ext_cg_solve(qed3_dirac_ext* e, double* x, const double* b, const qed3_solve_params* params,
                             qed3_solve_report* report, void* stream);
 

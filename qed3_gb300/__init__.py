@@ -629,18 +629,21 @@ class DiracExt:
         _check(lib().qed3_dirac_ext_fermion_force(self._h, _ptr(eta), _ptr(F), _stream(stream)))
         return F
 
-    def solve(self, x, b, tol: float = 1e-10, maxiter: int = 100000, shift: float = 0.0, stream=None) -> Report:
-        p = SolveParams(tol, maxiter, PREC_F64, 0.1, shift, 0)
+    def solve(self, x, b, tol: float = 1e-10, maxiter: int = 100000, shift: float = 0.0, precision: int = PREC_F64,
+              delta: float = 0.1, stream=None) -> Report:
+        """CG on D^dag D + shift; precision PREC_F32: FP32 iterations with FP64
+        reliable updates (same FP64 certificate)."""
+        p = SolveParams(tol, maxiter, precision, delta, shift, 0)
         r = SolveReport()
         _check(lib().qed3_dirac_ext_cg_solve(self._h, _ptr(x), _ptr(b), ctypes.byref(p), ctypes.byref(r),
                                              _stream(stream)))
         return Report(r.status, r.iters, r.reliable_updates, r.true_rel_res, r.ms)
 
     def propagator(self, sink, s: int = 0, ix: int = 0, spin: int = 0, tol: float = 1e-10, dagger: bool = False,
-                   stream=None) -> Report:
+                   precision: int = PREC_F64, stream=None) -> Report:
         """sink = D^{-1} (point source at slice s, site ix, spin), prop.cu's
         (D^dag D)^{-1} D^dag src solve; dagger: D^{-dag} (IS_DAGGER)."""
-        p = SolveParams(tol, 0, PREC_F64, 0.1, 0.0, 0)
+        p = SolveParams(tol, 0, precision, 0.1, 0.0, 0)
         r = SolveReport()
         _check(lib().qed3_dirac_ext_propagator(self._h, s, ix, spin, int(dagger), _ptr(sink), ctypes.byref(p), ctypes.byref(r),
                                                _stream(stream)))

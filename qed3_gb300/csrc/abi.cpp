@@ -347,7 +347,9 @@ int qed3_dirac_ext_propagator(qed3_dirac_ext* e, int s, int ix, int a, int dagge
                               qed3_solve_report* report, void* stream) {
   QED3_GUARD_BEGIN
   if (!e || !sink) return fail(QED3_ERR_ARG, "NULL argument");
-  qed3_solve_params p{params ? params->tol : 1e-10, params ? params->maxiter : 0, QED3_PREC_F64, 0.1, 0.0, 0};
+  qed3_solve_params p{params ? params->tol : 1e-10, params ? params->maxiter : 0,
+                      params && params->precision == QED3_PREC_F32 ? QED3_PREC_F32 : QED3_PREC_F64,
+                      params && params->delta > 0 ? params->delta : 0.1, 0.0, 0};
   return ext_propagator(e, s, ix, a, dagger, sink, &p, report, (cudaStream_t)stream);
   QED3_GUARD_END
 }

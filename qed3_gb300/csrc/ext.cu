@@ -199,7 +199,8 @@ int ext_init(qed3_dirac_ext_s* e) {
 }
 
 void ext_free(qed3_dirac_ext_s* e) {
-  void* p[] = {e->H3, e->Hd3, e->kt, e->diag3, e->Pt, e->nbrR, e->tmp, e->work};
+  void* p[] = {e->H3, e->Hd3, e->kt, e->diag3, e->Pt, e->nbrR, e->tmp, e->work, e->H3f, e->Hd3f, e->Ptf, e->diag3f,
+               e->ktf, e->fwork};
   for (void* q : p)
     if (q) cudaFree(q);
 }
@@ -212,6 +213,7 @@ int ext_set_links(qed3_dirac_ext_s* e, const double* A, cudaStream_t st) {
                                                       e->H3, e->Hd3, e->Pt);
   QED3_CUDA_TRY(cudaGetLastError());
   e->links_set = true;
+  e->f32_current = false;
   return QED3_OK;
 }
 
@@ -354,13 +356,324 @@ __global__ void k_cg_p(long long nc, const double2* __restrict__ r, double2* __r
   }
 }
 
+// ---- FP32 operator and the mixed-precision CG ------------------------------
+// GB300's FP64 pipe bounds the FP64 apply (it runs at ~92 % of that pipe);
+// the FP32 copy of the operator moves half the bytes through the wide FP32
+// pipe.  The CG iterates in FP32 on the residual scaled to unit norm, and
+// every time that residual has dropped by delta (or meets the tolerance) the
+// FP64 solution and the FP64 true residual b - A x are refreshed (reliable
+// update); the search direction is kept, rescaled to the new residual norm.
+__global__ void k_ext_to32(long long nh, long long np, const M64* __restrict__ H3, const M64* __restrict__ Hd3,
+                           const double2* __restrict__ Pt, M32* __restrict__ H3f, M32* __restrict__ Hd3f,
+                           float2* __restrict__ Ptf) {
+  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  auto cv = [](const M64& h) {
+    return M32{make_float4(float(h.h00.x), float(h.h00.y), float(h.h01.x), float(h.h01.y)),
+               make_float4(float(h.h10.x), float(h.h10.y), float(h.h11.x), float(h.h11.y))};
+  };
+  if (idx < nh) {
+    H3f[idx] = cv(H3[idx]);
+    Hd3f[idx] = cv(Hd3[idx]);
+  } else if (idx - nh < np) {
+    const double2 p = Pt[idx - nh];
+    Ptf[idx - nh] = make_float2(float(p.x), float(p.y));
+  }
+}
+
+__device__ __forceinline__ float2 cmulf(float2 a, float2 b) {
+  return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+
+// k_ext_apply in FP32 (same entries, same thread order)
+__global__ void k_ext_apply32(int Ns, int Nt, int adj, const int32_t* __restrict__ nbrR, const M32* __restrict__ H3,
+                              const float* __restrict__ diag3, const float* __restrict__ kt,
+                              const float2* __restrict__ Pt, float r, const float4* __restrict__ in,
+                              float4* __restrict__ out) {
+  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= (long long)Ns * Nt) return;
+  const int s = int(idx / Ns), x = int(idx % Ns);
+  const float4* vs = in + size_t(s) * Ns;
+  const Sp32 self = ld32(vs, x);
+  const float dg = diag3[x];
+  Sp32 o{make_float2(dg * self.s0.x, dg * self.s0.y), make_float2(dg * self.s1.x, dg * self.s1.y)};
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    const M32 m = H3[(size_t(s) * 3 + k) * Ns + x];
+    const Sp32 b = ld32(vs, nbrR[size_t(k) * Ns + x]);
+    o.s0 = cfmaf(make_float2(m.r0.x, m.r0.y), b.s0, o.s0);
+    o.s0 = cfmaf(make_float2(m.r0.z, m.r0.w), b.s1, o.s0);
+    o.s1 = cfmaf(make_float2(m.r1.x, m.r1.y), b.s0, o.s1);
+    o.s1 = cfmaf(make_float2(m.r1.z, m.r1.w), b.s1, o.s1);
+  }
+  if (Nt > 1) {
+    const float kh = 0.5f * kt[x];
+    const int sp = (s + 1) % Nt, sm = (s + Nt - 1) % Nt;
+    const Sp32 up = ld32(in + size_t(sp) * Ns, x), dn = ld32(in + size_t(sm) * Ns, x);
+    float cu0, cu1, cd0, cd1;
+    if (!adj) {
+      const float sgn_u = (sp == 0) ? -1.f : 1.f, sgn_d = (sm == Nt - 1) ? -1.f : 1.f;
+      cu0 = sgn_u * kh * (-r + 1.f);
+      cu1 = sgn_u * kh * (-r - 1.f);
+      cd0 = sgn_d * kh * (-r - 1.f);
+      cd1 = sgn_d * kh * (-r + 1.f);
+    } else {
+      const float sgn_u = (s == Nt - 1) ? -1.f : 1.f, sgn_d = (s == 0) ? -1.f : 1.f;
+      cu0 = sgn_u * kh * (-r - 1.f);
+      cu1 = sgn_u * kh * (-r + 1.f);
+      cd0 = sgn_d * kh * (-r + 1.f);
+      cd1 = sgn_d * kh * (-r - 1.f);
+    }
+    const float2 pu = Pt[size_t(s) * Ns + x], pdc = Pt[size_t(sm) * Ns + x];
+    const float2 pd = make_float2(pdc.x, -pdc.y);
+    const float2 u0 = cmulf(pu, up.s0), u1 = cmulf(pu, up.s1), d0 = cmulf(pd, dn.s0), d1 = cmulf(pd, dn.s1);
+    o.s0.x += cu0 * u0.x + cd0 * d0.x;
+    o.s0.y += cu0 * u0.y + cd0 * d0.y;
+    o.s1.x += cu1 * u1.x + cd1 * d1.x;
+    o.s1.y += cu1 * u1.y + cd1 * d1.y;
+  }
+  st32(out + size_t(s) * Ns, x, o);
+}
+
+// Re<p, q> partial sums (FP32 vectors, FP64 accumulation)
+__global__ void k_mcg_pq(long long n, const float4* __restrict__ p, const float4* __restrict__ q,
+                         double* __restrict__ part, const ExtCgState* __restrict__ stt) {
+  if (stt->done != 0.0) return;
+  __shared__ double sh[32];
+  double v[1] = {0.0};
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const float4 a = p[i], b = q[i];
+    v[0] += double(a.x) * b.x + double(a.y) * b.y + double(a.z) * b.z + double(a.w) * b.w;
+  }
+  block_sum<1>(v, sh);
+  if (threadIdx.x == 0) part[blockIdx.x] = v[0];
+}
+
+__global__ void k_mcg_xr(long long n, const float4* __restrict__ p, const float4* __restrict__ q,
+                         float4* __restrict__ x, float4* __restrict__ r, double* __restrict__ part,
+                         const ExtCgState* __restrict__ stt) {
+  if (stt->done != 0.0) return;
+  __shared__ double sh[32];
+  const float al = float(stt->alpha);
+  double v[1] = {0.0};
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const float4 pp = p[i], qq = q[i];
+    float4 xx = x[i], rr = r[i];
+    xx.x += al * pp.x; xx.y += al * pp.y; xx.z += al * pp.z; xx.w += al * pp.w;
+    rr.x -= al * qq.x; rr.y -= al * qq.y; rr.z -= al * qq.z; rr.w -= al * qq.w;
+    x[i] = xx;
+    r[i] = rr;
+    v[0] += double(rr.x) * rr.x + double(rr.y) * rr.y + double(rr.z) * rr.z + double(rr.w) * rr.w;
+  }
+  block_sum<1>(v, sh);
+  if (threadIdx.x == 0) part[blockIdx.x] = v[0];
+}
+
+__global__ void k_mcg_p(long long n, const float4* __restrict__ r, float4* __restrict__ p,
+                        const ExtCgState* __restrict__ stt) {
+  if (stt->done != 0.0) return;
+  const float bt = float(stt->beta);
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const float4 rr = r[i], pp = p[i];
+    p[i] = make_float4(rr.x + bt * pp.x, rr.y + bt * pp.y, rr.z + bt * pp.z, rr.w + bt * pp.w);
+  }
+}
+
+__global__ void k_mcg_shift(long long n, float sh, const float4* __restrict__ p, float4* __restrict__ q,
+                            const ExtCgState* __restrict__ stt) {
+  if (stt->done != 0.0) return;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const float4 pp = p[i];
+    float4 qq = q[i];
+    qq.x += sh * pp.x; qq.y += sh * pp.y; qq.z += sh * pp.z; qq.w += sh * pp.w;
+    q[i] = qq;
+  }
+}
+
+// reliable update, part 1: x += sigma xf (FP64), xf = 0
+__global__ void k_mcg_accum(long long n, double sigma, float4* __restrict__ xf, S64* __restrict__ x) {
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const float4 a = xf[i];
+    S64 v = x[i];
+    v.s0.x += sigma * double(a.x);
+    v.s0.y += sigma * double(a.y);
+    v.s1.x += sigma * double(a.z);
+    v.s1.y += sigma * double(a.w);
+    x[i] = v;
+    xf[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+  }
+}
+
+// reliable update, part 2: rf = r / sigma, p *= pscale, partial |rf|^2
+__global__ void k_mcg_restart(long long n, double sinv, float pscale, const S64* __restrict__ r,
+                              float4* __restrict__ rf, float4* __restrict__ pf, double* __restrict__ part) {
+  __shared__ double sh[32];
+  double v[1] = {0.0};
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const S64 a = r[i];
+    const float4 f = make_float4(float(a.s0.x * sinv), float(a.s0.y * sinv), float(a.s1.x * sinv), float(a.s1.y * sinv));
+    rf[i] = f;
+    float4 pp = pf[i];
+    pp.x *= pscale; pp.y *= pscale; pp.z *= pscale; pp.w *= pscale;
+    pf[i] = pp;
+    v[0] += double(f.x) * f.x + double(f.y) * f.y + double(f.z) * f.z + double(f.w) * f.w;
+  }
+  block_sum<1>(v, sh);
+  if (threadIdx.x == 0) part[blockIdx.x] = v[0];
+}
+
+// reliable update, part 3: mu = |rf|^2, new threshold, running again
+__global__ void k_mcg_setmu(const double* __restrict__ part, int np, double thr, ExtCgState* __restrict__ stt) {
+  __shared__ double sh[32];
+  double v[1] = {0.0};
+  for (int i = threadIdx.x; i < np; i += blockDim.x) v[0] += part[i];
+  block_sum<1>(v, sh);
+  if (threadIdx.x == 0) {
+    stt->mu = v[0];
+    stt->thr = thr;
+    stt->done = 0.0;
+  }
+}
+
+static int ext_ensure_f32(qed3_dirac_ext_s* e, cudaStream_t st) {
+  const int Ns = e->d2->Ns, Nt = e->Nt;
+  const size_t nh = size_t(3) * Ns * Nt, np = size_t(Ns) * Nt;
+  if (!e->H3f) {
+    std::vector<double> kt(Ns), dg(Ns);
+    QED3_CUDA_TRY(cudaMemcpy(kt.data(), e->kt, Ns * sizeof(double), cudaMemcpyDeviceToHost));
+    QED3_CUDA_TRY(cudaMemcpy(dg.data(), e->diag3, Ns * sizeof(double), cudaMemcpyDeviceToHost));
+    std::vector<float> ktf(kt.begin(), kt.end()), dgf(dg.begin(), dg.end());
+    QED3_CUDA_TRY(cudaMalloc(&e->H3f, nh * sizeof(M32)));
+    QED3_CUDA_TRY(cudaMalloc(&e->Hd3f, nh * sizeof(M32)));
+    QED3_CUDA_TRY(cudaMalloc(&e->Ptf, np * sizeof(float2)));
+    QED3_CUDA_TRY(cudaMalloc(&e->diag3f, Ns * sizeof(float)));
+    QED3_CUDA_TRY(cudaMalloc(&e->ktf, Ns * sizeof(float)));
+    QED3_CUDA_TRY(cudaMalloc(&e->fwork, 5 * np * sizeof(float4)));
+    QED3_CUDA_TRY(cudaMemcpy(e->ktf, ktf.data(), Ns * sizeof(float), cudaMemcpyHostToDevice));
+    QED3_CUDA_TRY(cudaMemcpy(e->diag3f, dgf.data(), Ns * sizeof(float), cudaMemcpyHostToDevice));
+  }
+  if (!e->f32_current) {
+    k_ext_to32<<<nblk((long long)(nh + np)), 256, 0, st>>>((long long)nh, (long long)np, e->H3, e->Hd3, e->Pt, e->H3f,
+                                                          e->Hd3f, e->Ptf);
+    QED3_CUDA_TRY(cudaGetLastError());
+    e->f32_current = true;
+  }
+  return QED3_OK;
+}
+
+static int ext_cg_mixed(qed3_dirac_ext_s* e, double* x, const double* b, double tol, int maxiter, double shift,
+                        double delta, qed3_solve_report* rep, cudaStream_t st, int op) {
+  int rc = ext_ensure_f32(e, st);
+  if (rc) return rc;
+  const int Ns = e->d2->Ns, Nt = e->Nt;
+  const long long n = (long long)Ns * Nt, nd = 4 * n, nc = 2 * n;
+  double* r = reinterpret_cast<double*>(e->work);
+  double* q = r + 2 * nd;
+  double* part = q + nd;
+  float4 *rf = e->fwork, *pf = rf + n, *qf = pf + n, *tf = qf + n, *xf = tf + n;
+  cudaEvent_t e0, e1;
+  QED3_CUDA_TRY(cudaEventCreate(&e0));
+  QED3_CUDA_TRY(cudaEventCreate(&e1));
+  QED3_CUDA_TRY(cudaEventRecord(e0, st));
+  auto A64 = [&](double* o, const double* v) -> int {
+    int c = ext_apply(e, op, o, v, st);
+    if (!c && shift != 0.0) c = vec_axpby(nd, shift, v, 1.0, o, o, st);
+    return c;
+  };
+  const int gs = nblk(n);
+  const int first = op == QED3_OP_DDAGD ? 0 : 1;  // D^dag D: D then D^dag; D D^dag: the reverse
+  auto A32 = [&](float4* o, const float4* v) {
+    k_ext_apply32<<<gs, 256, 0, st>>>(Ns, Nt, first, e->nbrR, first ? e->Hd3f : e->H3f, e->diag3f, e->ktf, e->Ptf,
+                                      float(e->r), v, tf);
+    k_ext_apply32<<<gs, 256, 0, st>>>(Ns, Nt, 1 - first, e->nbrR, first ? e->H3f : e->Hd3f, e->diag3f, e->ktf,
+                                      e->Ptf, float(e->r), tf, o);
+  };
+  double bb = 0, im = 0;
+  if ((rc = vec_zdot(nc, b, b, part, &bb, &im, st))) return rc;
+  QED3_CUDA_TRY(cudaMemsetAsync(x, 0, nd * sizeof(double), st));
+  QED3_CUDA_TRY(cudaMemsetAsync(xf, 0, n * sizeof(float4), st));
+  QED3_CUDA_TRY(cudaMemsetAsync(pf, 0, n * sizeof(float4), st));
+  ExtCgState* dst = reinterpret_cast<ExtCgState*>(part + 1024);
+  ExtCgState hst{0.0, 0.0, 0.0, 0.0, bb == 0.0 ? 1.0 : 0.0, 0.0};
+  QED3_CUDA_TRY(cudaMemcpyAsync(dst, &hst, sizeof(hst), cudaMemcpyHostToDevice, st));
+  const int gblk = int(std::min<long long>(kCgParts, (n + 255) / 256));
+  int status = bb == 0.0 ? QED3_OK : QED3_ERR_NOCONV, updates = 0, its = 0;
+  double rr = bb, sigma = 0.0;
+  // (re)start the FP32 iteration on r / |r|: p = r / |r| at the start, p rescaled later
+  auto restart = [&](double rr_now, bool first_time) -> int {
+    const double snew = std::sqrt(rr_now);
+    const float pscale = first_time ? 0.f : float(sigma / snew);
+    k_mcg_restart<<<gblk, 256, 0, st>>>(n, 1.0 / snew, pscale, reinterpret_cast<const S64*>(r), rf, pf, part);
+    if (first_time) QED3_CUDA_TRY(cudaMemcpyAsync(pf, rf, n * sizeof(float4), cudaMemcpyDeviceToDevice, st));
+    k_mcg_setmu<<<1, 256, 0, st>>>(part, gblk, tol * tol * bb / rr_now, dst);
+    QED3_CUDA_TRY(cudaGetLastError());
+    sigma = snew;
+    return QED3_OK;
+  };
+  if (bb > 0) {
+    QED3_CUDA_TRY(cudaMemcpyAsync(r, b, nd * sizeof(double), cudaMemcpyDeviceToDevice, st));
+    if ((rc = restart(bb, true))) return rc;
+  }
+  const double d2 = delta * delta;
+  while (status != QED3_OK && its < maxiter) {
+    const int m = std::min(8, maxiter - its);
+    for (int k = 0; k < m; k++) {
+      A32(qf, pf);
+      if (shift != 0.0) k_mcg_shift<<<gblk, 256, 0, st>>>(n, float(shift), pf, qf, dst);
+      k_mcg_pq<<<gblk, 256, 0, st>>>(n, pf, qf, part, dst);
+      k_cg_alpha<<<1, 256, 0, st>>>(part, gblk, dst);
+      k_mcg_xr<<<gblk, 256, 0, st>>>(n, pf, qf, xf, rf, part, dst);
+      k_cg_beta<<<1, 256, 0, st>>>(part, gblk, dst);
+      k_mcg_p<<<gblk, 256, 0, st>>>(n, rf, pf, dst);
+    }
+    QED3_CUDA_TRY(cudaGetLastError());
+    QED3_CUDA_TRY(cudaMemcpyAsync(&hst, dst, sizeof(hst), cudaMemcpyDeviceToHost, st));
+    QED3_CUDA_TRY(cudaStreamSynchronize(st));
+    its = int(hst.iters);
+    if (hst.done == 2.0) break;  // non-finite
+    // the scaled residual norm: |r|^2 / sigma^2 after the last completed step
+    if (hst.done == 1.0 || hst.mu < d2 || its >= maxiter) {
+      k_mcg_accum<<<gblk, 256, 0, st>>>(n, sigma, xf, reinterpret_cast<S64*>(x));
+      QED3_CUDA_TRY(cudaGetLastError());
+      if ((rc = A64(q, x)) || (rc = vec_axpby(nd, 1.0, b, -1.0, q, r, st)) ||
+          (rc = vec_zdot(nc, r, r, part, &rr, &im, st)))
+        return rc;
+      updates++;
+      if (!std::isfinite(rr)) break;
+      if (rr < tol * tol * bb) {
+        status = QED3_OK;
+        break;
+      }
+      if (its >= maxiter) break;
+      if ((rc = restart(rr, false))) return rc;
+    }
+  }
+  QED3_CUDA_TRY(cudaEventRecord(e1, st));
+  QED3_CUDA_TRY(cudaEventSynchronize(e1));
+  float ms = 0;
+  cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (rep) {
+    rep->status = status;
+    rep->iters = its;
+    rep->reliable_updates = updates;
+    rep->true_rel_res = bb > 0 ? std::sqrt(rr / bb) : 0.0;
+    rep->ms = ms;
+  }
+  return QED3_OK;
+}
+
 // MatPoly::solve (src/dual/matpoly.h:204-267) on D^dag D + shift in FP64:
 // x0 = 0, stop on the recursive residual, certified by the true residual.
+// precision QED3_PREC_F32: the mixed-precision CG above (same certificate).
 int ext_cg(qed3_dirac_ext_s* e, double* x, const double* b, const qed3_solve_params* prm, qed3_solve_report* rep,
            cudaStream_t st, int op) {
   if (op != QED3_OP_DDAGD && op != QED3_OP_DDDAG) return fail(QED3_ERR_ARG, "CG runs on D^dag D or D D^dag");
   if (!e->links_set) return fail(QED3_ERR_STATE, "call qed3_dirac_ext_set_links first");
-  if (prm && prm->precision != QED3_PREC_F64) return fail(QED3_ERR_ARG, "the S2 x S1 solve runs in FP64");
+  if (prm && prm->precision == QED3_PREC_F32)
+    return ext_cg_mixed(e, x, b, prm->tol > 0 ? prm->tol : 1e-10, prm->maxiter > 0 ? prm->maxiter : 100000,
+                        prm->shift, prm->delta > 0 && prm->delta < 1 ? prm->delta : 0.1, rep, st, op);
+  if (prm && prm->precision != QED3_PREC_F64) return fail(QED3_ERR_ARG, "the S2 x S1 solve runs in FP64 or FP32");
   const double tol = prm && prm->tol > 0 ? prm->tol : 1e-10;
   const int maxiter = prm && prm->maxiter > 0 ? prm->maxiter : 100000;
   const double shift = prm ? prm->shift : 0.0;

@@ -15,6 +15,14 @@ struct qed3_dirac_ext_s {
   double* diag3 = nullptr;     // [Ns] (reference order)
   double2* Pt = nullptr;       // [Nt][Ns] temporal phases e^{i A_t} (reference order)
   int32_t* nbrR = nullptr;     // [3][Ns] reference ids of the neighbours of reference site x
+  // FP32 copies for the mixed-precision CG (allocated at its first use)
+  qed3::M32* H3f = nullptr;
+  qed3::M32* Hd3f = nullptr;
+  float2* Ptf = nullptr;
+  float* diag3f = nullptr;
+  float* ktf = nullptr;
+  float4* fwork = nullptr;     // [5][Nt][Ns] FP32 CG vectors
+  bool f32_current = false;    // FP32 copies match the current links
   qed3::S64* tmp = nullptr;    // [Nt][Ns]
   void* work = nullptr;        // CG vectors
   bool links_set = false;

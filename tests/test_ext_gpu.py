@@ -204,3 +204,48 @@ def test_ext_propagator_matches_oracle(cuda, Nt, at):
         assert np.allclose(tp[0::2, 1], got.reshape(Nt, -1, 2)[:, 0, 0].real / fac)
     with pytest.raises(Q.Qed3Error):
         De.propagator(sink, Nt, 0, 0)
+
+
+@pytest.mark.parametrize("shift", [0.0, 0.05])
+def test_ext_cg_mixed_precision(cuda, shift):
+    """FP32 iterations with FP64 reliable updates on the S^2 x S^1 operator:
+    the FP64 certificate holds at 1e-10, the solution is the FP64 solve's,
+    iterations stay within 1.5x of FP64, and b scaled by 1e+-30 gives the
+    same iteration count (the FP32 iteration runs on r / |r|)."""
+    import torch
+    n, Nt, at = 4, 4, 0.6
+    lat = Q.S2Trivalent(n)
+    rng = np.random.default_rng(80)
+    De = Q.DiracExt(lat, 1.0, 0.1, Nt, at)
+    De.update(to_dev(rng.uniform(-np.pi, np.pi, Nt * (lat.n_links + lat.n_sites)), cuda))
+    b = rng.normal(size=2 * lat.n_sites * Nt) + 1j * rng.normal(size=2 * lat.n_sites * Nt)
+    x64 = torch.zeros(b.size, dtype=torch.complex128, device=cuda)
+    r64 = De.solve(x64, to_dev(b, cuda), tol=1e-10, shift=shift)
+    assert r64.status == Q.OK
+    its = []
+    for scale in (1.0, 1e-30, 1e30):
+        x = torch.zeros_like(x64)
+        r = De.solve(x, to_dev(b * scale, cuda), tol=1e-10, shift=shift, precision=Q.PREC_F32)
+        assert r.status == Q.OK and r.true_rel_res <= 1e-10 and r.reliable_updates >= 1, (scale, r)
+        assert rel(from_dev(x) / scale, from_dev(x64)) < 1e-8
+        its.append(r.iters)
+    assert its[0] <= 1.5 * r64.iters + 10, (its, r64.iters)
+    assert max(its) - min(its) <= 2, its
+
+
+def test_ext_propagator_mixed_precision(cuda):
+    import torch
+    n, Nt, at = 2, 4, 0.5
+    g = O.geometry(n)
+    lat = Q.S2Trivalent(n)
+    De = Q.DiracExt(lat, 1.0, 0.0, Nt, at)
+    A = np.random.default_rng(81).uniform(-np.pi, np.pi, Nt * (g.n_links + g.n_sites))
+    De.update(to_dev(A, cuda))
+    M = O.dirac_ext_matrix(g, 1.0, 0.0, Nt, at, A)
+    for dag in (False, True):
+        sink = torch.zeros(2 * g.n_sites * Nt, dtype=torch.complex128, device=cuda)
+        rep = De.propagator(sink, 1, 5, 0, tol=1e-11, dagger=dag, precision=Q.PREC_F32)
+        assert rep.status == Q.OK and rep.true_rel_res <= 1e-11
+        delta = np.zeros(2 * g.n_sites * Nt, np.complex128)
+        delta[(1 * g.n_sites + 5) * 2] = 1.0
+        assert rel(from_dev(sink), np.linalg.solve(M.conj().T if dag else M, delta)) < 1e-8
