@@ -192,7 +192,9 @@ int ext_init(qed3_dirac_ext_s* e) {
   QED3_CUDA_TRY(cudaMalloc(&e->nbrR, nbrR.size() * sizeof(int32_t)));
   QED3_CUDA_TRY(cudaMemcpy(e->nbrR, nbrR.data(), nbrR.size() * sizeof(int32_t), cudaMemcpyHostToDevice));
   QED3_CUDA_TRY(cudaMalloc(&e->tmp, size_t(Ns) * Nt * sizeof(S64)));
-  QED3_CUDA_TRY(cudaMalloc(&e->work, size_t(Ns) * Nt * 3 * sizeof(S64) + 2048 * sizeof(double)));
+  // CG vectors, then 2048 doubles of reduction partials (vec_zdot fills all of
+  // them on large fields), then the device-resident CG state
+  QED3_CUDA_TRY(cudaMalloc(&e->work, size_t(Ns) * Nt * 3 * sizeof(S64) + (2048 + 64) * sizeof(double)));
   QED3_CUDA_TRY(cudaMemcpy(e->kt, kt.data(), Ns * sizeof(double), cudaMemcpyHostToDevice));
   QED3_CUDA_TRY(cudaMemcpy(e->diag3, diag3.data(), Ns * sizeof(double), cudaMemcpyHostToDevice));
   return QED3_OK;
@@ -592,7 +594,7 @@ static int ext_cg_mixed(qed3_dirac_ext_s* e, double* x, const double* b, double 
   QED3_CUDA_TRY(cudaMemsetAsync(x, 0, nd * sizeof(double), st));
   QED3_CUDA_TRY(cudaMemsetAsync(xf, 0, n * sizeof(float4), st));
   QED3_CUDA_TRY(cudaMemsetAsync(pf, 0, n * sizeof(float4), st));
-  ExtCgState* dst = reinterpret_cast<ExtCgState*>(part + 1024);
+  ExtCgState* dst = reinterpret_cast<ExtCgState*>(part + 2048);
   ExtCgState hst{0.0, 0.0, 0.0, 0.0, bb == 0.0 ? 1.0 : 0.0, 0.0};
   QED3_CUDA_TRY(cudaMemcpyAsync(dst, &hst, sizeof(hst), cudaMemcpyHostToDevice, st));
   const int gblk = int(std::min<long long>(kCgParts, (n + 255) / 256));
@@ -697,7 +699,7 @@ int ext_cg(qed3_dirac_ext_s* e, double* x, const double* b, const qed3_solve_par
   QED3_CUDA_TRY(cudaMemsetAsync(x, 0, nd * sizeof(double), st));
   QED3_CUDA_TRY(cudaMemcpyAsync(r, b, nd * sizeof(double), cudaMemcpyDeviceToDevice, st));
   QED3_CUDA_TRY(cudaMemcpyAsync(p, b, nd * sizeof(double), cudaMemcpyDeviceToDevice, st));
-  ExtCgState* dst = reinterpret_cast<ExtCgState*>(part + 1024);
+  ExtCgState* dst = reinterpret_cast<ExtCgState*>(part + 2048);
   ExtCgState hst{bb, tol * tol * bb, 0.0, 0.0, bb == 0.0 ? 1.0 : 0.0, 0.0};
   QED3_CUDA_TRY(cudaMemcpyAsync(dst, &hst, sizeof(hst), cudaMemcpyHostToDevice, st));
   const double2* p2 = reinterpret_cast<const double2*>(p);
