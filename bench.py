@@ -382,8 +382,14 @@ def paths_timings(torch, Q, dev, cpu=True):
     res = []
     gpu_s = _wall(torch, lambda: res.append(Q.hmc_ext(De, rng, Ae, 1.0, tmax=0.5, nsteps=4, nsteps_inner=4,
                                                        tol=1e-10)), 3)
+    res32 = []
+    gpu_m = _wall(torch, lambda: res32.append(Q.hmc_ext(De, rng, Ae, 1.0, tmax=0.5, nsteps=4, nsteps_inner=4,
+                                                         tol=1e-10, precision=Q.PREC_F32)), 3)
     out["hmc_ext_n8_nt8"] = {"gpu_ms": 1e3 * gpu_s, "cg_iters": res[-1][2], "accepted": [r[0] for r in res],
-                             "config": "n=8, Nt=8, at=0.5, g^2=1, tau=0.5, 4 x 4 steps, tol 1e-10 FP64",
+                             "mixed_f32": {"gpu_ms": 1e3 * gpu_m, "cg_iters": res32[-1][2],
+                                           "accepted": [r[0] for r in res32]},
+                             "config": "n=8, Nt=8, at=0.5, g^2=1, tau=0.5, 4 x 4 steps, tol 1e-10; FP64 solves, "
+                                       "then FP32 + FP64 reliable updates",
                              "cpu_baseline": None, "cpu_note": "the oracle's S^2 x S^1 HMC runs on a dense "
                              "operator (checked at n=2); no CPU sample at this size"}
     return out

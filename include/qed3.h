@@ -373,10 +373,12 @@ int qed3_hmc_pure_gauge(qed3_lattice* lat, qed3_rng* rng, double* A, double beta
  * of the S^2 x S^1 operator e, QED3_INTEGRATOR_LEAPFROG_ML or _LEAPFROG; rng must hold
  * Nt n_links link engines and Nt n_sites site engines (ParallelRngExt's
  * layout: spatial momenta from the link engines, temporal momenta and the
- * pseudofermion sources from the site engines); solves in FP64 to tol. */
+ * pseudofermion sources from the site engines); solves to tol, precision
+ * QED3_PREC_F64 (the reference's recurrence) or QED3_PREC_F32 (FP32 iterations
+ * with FP64 reliable updates, same certificate). */
 int qed3_hmc_ext(qed3_dirac_ext* e, qed3_rng* rng, double* A, double at, double gsq, double tmax, int nsteps,
-                 int nsteps_inner, int npf, int integrator, double tol, int no_reject, int* accepted, double* dH,
-                 int* cg_iters, void* stream);
+                 int nsteps_inner, int npf, int integrator, double tol, int precision, int no_reject, int* accepted,
+                 double* dH, int* cg_iters, void* stream);
 
 /* ======================================================================
  * Overlap operator  --  replaces Overlap<WilsonDirac> (src/both_3d/overlap.h:137-390):

@@ -134,8 +134,8 @@ SIGNATURES = [
                                              ctypes.POINTER(vp)]),
     ("qed3_dirac_ext_destroy", ctypes.c_int, [vp]),
     ("qed3_hmc_ext", ctypes.c_int, [vp, vp, vp, ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_int,
-                                    ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_int, c_int_p,
-                                    c_double_p, c_int_p, vp]),
+                                    ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_int,
+                                    ctypes.c_int, c_int_p, c_double_p, c_int_p, vp]),
     ("qed3_dirac_ext_set_links", ctypes.c_int, [vp, vp, vp]),
     ("qed3_dirac_ext_apply", ctypes.c_int, [vp, ctypes.c_int, vp, vp, vp]),
     ("qed3_dirac_ext_fermion_force", ctypes.c_int, [vp, vp, vp, vp]),
@@ -657,14 +657,14 @@ class DiracExt:
 
 def hmc_ext(dirac: DiracExt, rng: ParallelRng, A, gsq: float, tmax: float = 1.0, nsteps: int = 10,
             nsteps_inner: int = 10, npf: int = 1, integrator: int = 0, tol: float = 1e-10, no_reject: bool = False,
-            stream=None):
+            precision: int = PREC_F64, stream=None):
     """One S^2 x S^1 HMC trajectory (HMC2::run with U1WilsonExt(at, gsq) and npf
     DiracExt pseudofermions) on device links A, in place; rng =
     ParallelRng(lattice, seed, n_slices=Nt).  Returns (accepted, dH, cg_iterations)."""
     acc, dH, its = ctypes.c_int(), ctypes.c_double(), ctypes.c_int()
     _check(lib().qed3_hmc_ext(dirac._h, rng.handle, _ptr(A), dirac.at, gsq, tmax, nsteps, nsteps_inner, npf,
-                              integrator, tol, int(no_reject), ctypes.byref(acc), ctypes.byref(dH), ctypes.byref(its),
-                              _stream(stream)))
+                              integrator, tol, precision, int(no_reject), ctypes.byref(acc), ctypes.byref(dH),
+                              ctypes.byref(its), _stream(stream)))
     return bool(acc.value), dH.value, its.value
 
 

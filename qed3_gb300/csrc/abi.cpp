@@ -325,8 +325,8 @@ int qed3_dirac_ext_fermion_force(qed3_dirac_ext* e, const double* eta, double* F
 }
 
 int qed3_hmc_ext(qed3_dirac_ext* e, qed3_rng* rng, double* A, double at, double gsq, double tmax, int nsteps,
-                 int nsteps_inner, int npf, int integrator, double tol, int no_reject, int* accepted, double* dH,
-                 int* cg_iters, void* stream) {
+                 int nsteps_inner, int npf, int integrator, double tol, int precision, int no_reject, int* accepted,
+                 double* dH, int* cg_iters, void* stream) {
   QED3_GUARD_BEGIN
   if (!e || !rng || !A || !accepted || !dH) return fail(QED3_ERR_ARG, "NULL argument");
   if (nsteps < 1 || nsteps_inner < 1 || !(tmax > 0) || npf < 1 || npf > 64 || !(at > 0))
@@ -338,8 +338,9 @@ int qed3_hmc_ext(qed3_dirac_ext* e, qed3_rng* rng, double* A, double at, double 
   rng_counts(rng, &rl, &rs);
   if (rl != nl || rs != ns)
     return fail(QED3_ERR_ARG, "rng must hold Nt n_links link engines and Nt n_sites site engines");
-  return hmc_ext(e, rng, A, at, gsq, tmax, nsteps, nsteps_inner, npf, integrator, tol > 0 ? tol : 1e-10, no_reject,
-                 accepted, dH, cg_iters, (cudaStream_t)stream);
+  if (precision != QED3_PREC_F64 && precision != QED3_PREC_F32) return fail(QED3_ERR_ARG, "precision F64 or F32");
+  return hmc_ext(e, rng, A, at, gsq, tmax, nsteps, nsteps_inner, npf, integrator, tol > 0 ? tol : 1e-10, precision,
+                 no_reject, accepted, dH, cg_iters, (cudaStream_t)stream);
   QED3_GUARD_END
 }
 

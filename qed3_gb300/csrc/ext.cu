@@ -763,8 +763,8 @@ int ext_cg(qed3_dirac_ext_s* e, double* x, const double* b, const qed3_solve_par
 namespace qed3 {
 
 int hmc_ext(qed3_dirac_ext_s* e, qed3_rng_s* rng, double* A, double at, double gsq, double tmax, int nsteps,
-            int nsteps_inner, int npf, int integrator, double tol, int no_reject, int* accepted, double* dH_out,
-            int* cg_iters, cudaStream_t st) {
+            int nsteps_inner, int npf, int integrator, double tol, int prec, int no_reject, int* accepted,
+            double* dH_out, int* cg_iters, cudaStream_t st) {
   qed3_dirac_s* d = e->d2;
   qed3_lattice_s* lat = d->lat;
   const int Ns = d->Ns, Nl = lat->dev.Nl, Nt = e->Nt;
@@ -779,7 +779,7 @@ int hmc_ext(qed3_dirac_ext_s* e, qed3_rng_s* rng, double* A, double at, double g
   double *P = buf, *A0 = P + nA, *F = A0 + nA, *Ff = F + nA, *xid = Ff + nA, *phi = xid + nd * npf,
          *eta = phi + nd * npf, *part = eta + nd * npf;
   int its = 0;
-  const qed3_solve_params sp{tol, 0, QED3_PREC_F64, 0.1, 0.0, 0};
+  const qed3_solve_params sp{tol, 0, prec, 0.1, 0.0, 0};
   auto body = [&]() -> int {
     int rc;
     QED3_CUDA_TRY(cudaMemcpyAsync(P, pi.data(), nA * sizeof(double), cudaMemcpyHostToDevice, st));

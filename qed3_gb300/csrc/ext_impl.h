@@ -37,8 +37,8 @@ int ext_fermion_force(qed3_dirac_ext_s* e, const double* eta, double* F, cudaStr
 int ext_propagator(qed3_dirac_ext_s* e, int s, int ix, int a, int dagger, double* sink, const qed3_solve_params* prm,
                    qed3_solve_report* rep, cudaStream_t st);
 int hmc_ext(qed3_dirac_ext_s* e, qed3_rng_s* rng, double* A, double at, double gsq, double tmax, int nsteps,
-            int nsteps_inner, int npf, int integrator, double tol, int no_reject, int* accepted, double* dH_out,
-            int* cg_iters, cudaStream_t st);
+            int nsteps_inner, int npf, int integrator, double tol, int prec, int no_reject, int* accepted,
+            double* dH_out, int* cg_iters, cudaStream_t st);
 // FP64 CG on op + shift, op = QED3_OP_DDAGD (default) or QED3_OP_DDDAG
 int ext_cg(qed3_dirac_ext_s* e, double* x, const double* b, const qed3_solve_params* prm, qed3_solve_report* rep,
            cudaStream_t st, int op = QED3_OP_DDAGD);

@@ -267,3 +267,21 @@ def test_ext_cg_large_field_iteration_counts(cuda):
     r32 = De.solve(x, b, tol=1e-10, precision=Q.PREC_F32)
     assert r64.status == Q.OK and r32.status == Q.OK and r32.true_rel_res <= 1e-10
     assert 0.8 * r64.iters <= r32.iters <= 1.5 * r64.iters + 10, (r64.iters, r32.iters)
+
+
+def test_hmc_ext_mixed_precision_matches_fp64(cuda):
+    """The S^2 x S^1 trajectory with FP32 + reliable-update solves to 1e-12
+    follows the FP64 one: same decisions, dH to 1e-7, links to 1e-8."""
+    import torch
+    n, Nt, at = 2, 3, 0.8
+    lat = Q.S2Trivalent(n)
+    A = torch.from_numpy(np.random.default_rng(83).uniform(-0.3, 0.3, Nt * (lat.n_links + lat.n_sites))).to(cuda)
+    De = Q.DiracExt(lat, 1.0, 0.1, Nt, at)
+    A64, A32 = A.clone(), A.clone()
+    r64, r32 = Q.ParallelRng(lat, 7, n_slices=Nt), Q.ParallelRng(lat, 7, n_slices=Nt)
+    for t in range(2):
+        a64 = Q.hmc_ext(De, r64, A64, 1.0, tmax=0.5, nsteps=4, nsteps_inner=2, npf=2, tol=1e-12)
+        a32 = Q.hmc_ext(De, r32, A32, 1.0, tmax=0.5, nsteps=4, nsteps_inner=2, npf=2, tol=1e-12,
+                        precision=Q.PREC_F32)
+        assert a64[0] == a32[0] and abs(a64[1] - a32[1]) < 1e-7 * (1 + abs(a64[1])), (a64, a32)
+        assert float((A64 - A32).abs().max()) < 1e-8
