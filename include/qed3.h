@@ -239,6 +239,25 @@ int qed3_dirac_ext_fermion_force(qed3_dirac_ext* e, const double* eta, double* F
  * = (D D^dag)^{-1} D src1.  sink: device complex128 [Nt][n_sites][2]; synchronous. */
 int qed3_dirac_ext_propagator(qed3_dirac_ext* e, int s, int ix, int a, int dagger, double* sink, const qed3_solve_params* params,
                               qed3_solve_report* report, void* stream);
+/* Overlap<DiracExt> (src/both_3d/overlap.h:137-390 on this operator, the
+ * reference's IS_OVERLAP builds of hmc.cu / prop.cu): Zolotarev order `order`,
+ * all poles from one FP64 multi-shift CG on D^dag D.  update: lambda_min /
+ * lambda_max given, or (both 0) from Lanczos on D^dag D to tol widened by the
+ * relative margin.  apply: op = QED3_OP_D (D_ov), _DDAG (D_ov^dag), _DDAGD or
+ * _DDDAG (D_ov + D_ov^dag = D_ov^dag D_ov); pole solves to tol_inner.  solve:
+ * CG on D_ov^dag D_ov to tol (certified by the recomputed residual); prop != 0
+ * solves for D_ov^dag b instead of b (prop.cu: sink = D_ov^{-1} b). */
+typedef struct qed3_overlap_ext_s qed3_overlap_ext;
+int qed3_overlap_ext_create(qed3_dirac_ext* e, int order, qed3_overlap_ext** out);
+int qed3_overlap_ext_destroy(qed3_overlap_ext* ov);
+int qed3_overlap_ext_update(qed3_overlap_ext* ov, double lambda_min, double lambda_max, double tol, double margin,
+                            void* stream);
+int qed3_overlap_ext_info(const qed3_overlap_ext* ov, double* lambda_min, double* lambda_max, double* k,
+                          double* delta);
+int qed3_overlap_ext_apply(qed3_overlap_ext* ov, int op, double* out, const double* in, double tol_inner,
+                           int* pole_iters, void* stream);
+int qed3_overlap_ext_solve(qed3_overlap_ext* ov, double* x, const double* b, double tol, double tol_inner,
+                           int maxiter, int prop, qed3_solve_report* report, void* stream);
 /* MatPoly::solve on D^dag D (+ params->shift), certified by the FP64 true
  * residual.  params->precision QED3_PREC_F64: the reference's FP64 recurrence;
  * QED3_PREC_F32: FP32 iterations (FP32 copy of the operator) with FP64

@@ -824,3 +824,19 @@ def dirac1f_matrix(geom: Geometry, r: float, m: float, M5: float, A: np.ndarray)
             M[2 * x:2 * x + 2, 2 * y:2 * y + 2] -= w * (r * u[x, k] * np.eye(2) - gam) * np.exp(1j * sg * A[l]) @ Om
             M[2 * x:2 * x + 2, 2 * x:2 * x + 2] += (w * (r * u[x, k] + m / 3.0) + M5 / 3.0) * np.eye(2)
     return M
+
+
+def overlap_ext_matrix(geom: Geometry, r: float, M5: float, Nt: int, at: float, A: np.ndarray, lmin: float,
+                       lmax: float, order: int) -> np.ndarray:
+    """Overlap<DiracExt>::mult (src/both_3d/overlap.h:309-332) as a dense matrix:
+    D_ov = 1 + C X (1 + sum_m A_m (X^dag X - k^2/cp_m)^{-1}), X = D / lambda_max,
+    with the Zolotarev coefficients of `zolotarev` (k = lambda_min / lambda_max)."""
+    M = dirac_ext_matrix(geom, r, M5, Nt, at, A)
+    z = zolotarev(lmin / lmax, order)
+    X = M / lmax
+    H = X.conj().T @ X
+    I = np.eye(M.shape[0])
+    acc = I.copy()
+    for m in range(1, z["size"]):
+        acc = acc + z["A"][m] * np.linalg.inv(H - z["k"] ** 2 / z["cp"][m] * I)
+    return I + z["C"] * X @ acc

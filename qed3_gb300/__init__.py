@@ -141,6 +141,14 @@ SIGNATURES = [
     ("qed3_dirac_ext_fermion_force", ctypes.c_int, [vp, vp, vp, vp]),
     ("qed3_dirac_ext_propagator", ctypes.c_int, [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, vp,
                                                  ctypes.POINTER(SolveParams), ctypes.POINTER(SolveReport), vp]),
+    ("qed3_overlap_ext_create", ctypes.c_int, [vp, ctypes.c_int, ctypes.POINTER(vp)]),
+    ("qed3_overlap_ext_destroy", ctypes.c_int, [vp]),
+    ("qed3_overlap_ext_update", ctypes.c_int, [vp, ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                                               vp]),
+    ("qed3_overlap_ext_info", ctypes.c_int, [vp, c_double_p, c_double_p, c_double_p, c_double_p]),
+    ("qed3_overlap_ext_apply", ctypes.c_int, [vp, ctypes.c_int, vp, vp, ctypes.c_double, c_int_p, vp]),
+    ("qed3_overlap_ext_solve", ctypes.c_int, [vp, vp, vp, ctypes.c_double, ctypes.c_double, ctypes.c_int,
+                                              ctypes.c_int, ctypes.POINTER(SolveReport), vp]),
     ("qed3_dirac_ext_cg_solve", ctypes.c_int, [vp, vp, vp, ctypes.POINTER(SolveParams), ctypes.POINTER(SolveReport),
                                                vp]),
     ("qed3_ext_plaquettes", ctypes.c_int, [vp, ctypes.c_int, vp, vp, vp, vp]),
@@ -652,6 +660,44 @@ class DiracExt:
     def __del__(self):
         if getattr(self, "_h", None) and _lib is not None:
             _lib.qed3_dirac_ext_destroy(self._h)
+            self._h = None
+
+
+class OverlapExt:
+    """Overlap<DiracExt>: the overlap operator of the S^2 x S^1 Wilson operator
+    (src/both_3d/overlap.h:137-390), all poles in one FP64 multi-shift CG."""
+
+    def __init__(self, dirac: DiracExt, order: int = 21):
+        self.dirac = dirac
+        h = vp()
+        _check(lib().qed3_overlap_ext_create(dirac._h, order, ctypes.byref(h)))
+        self._h = h
+
+    def update(self, lambda_min: float = 0.0, lambda_max: float = 0.0, tol: float = 1e-10, margin: float = 1e-6,
+               stream=None):
+        _check(lib().qed3_overlap_ext_update(self._h, lambda_min, lambda_max, tol, margin, _stream(stream)))
+
+    def info(self) -> dict:
+        a, b, k, dl = (ctypes.c_double() for _ in range(4))
+        _check(lib().qed3_overlap_ext_info(self._h, *(ctypes.byref(v) for v in (a, b, k, dl))))
+        return dict(lambda_min=a.value, lambda_max=b.value, k=k.value, delta=dl.value)
+
+    def apply(self, out, inp, op: int = OP_D, tol_inner: float = 1e-12, stream=None) -> int:
+        it = ctypes.c_int()
+        _check(lib().qed3_overlap_ext_apply(self._h, op, _ptr(out), _ptr(inp), tol_inner, ctypes.byref(it),
+                                            _stream(stream)))
+        return it.value
+
+    def solve(self, x, b, tol: float = 1e-10, tol_inner: float = 1e-12, maxiter: int = 100000,
+              propagator: bool = False, stream=None) -> Report:
+        r = SolveReport()
+        _check(lib().qed3_overlap_ext_solve(self._h, _ptr(x), _ptr(b), tol, tol_inner, maxiter, int(propagator),
+                                            ctypes.byref(r), _stream(stream)))
+        return Report(r.status, r.iters, r.reliable_updates, r.true_rel_res, r.ms)
+
+    def __del__(self):
+        if getattr(self, "_h", None) and _lib is not None:
+            _lib.qed3_overlap_ext_destroy(self._h)
             self._h = None
 
 

@@ -355,6 +355,54 @@ int qed3_dirac_ext_propagator(qed3_dirac_ext* e, int s, int ix, int a, int dagge
   QED3_GUARD_END
 }
 
+int qed3_overlap_ext_create(qed3_dirac_ext* e, int order, qed3_overlap_ext** out) {
+  QED3_GUARD_BEGIN
+  if (!e || !out) return fail(QED3_ERR_ARG, "NULL argument");
+  return ext_overlap_create(e, order, out);
+  QED3_GUARD_END
+}
+
+int qed3_overlap_ext_destroy(qed3_overlap_ext* ov) {
+  QED3_GUARD_BEGIN
+  ext_overlap_destroy(ov);
+  return QED3_OK;
+  QED3_GUARD_END
+}
+
+int qed3_overlap_ext_update(qed3_overlap_ext* ov, double lambda_min, double lambda_max, double tol, double margin,
+                            void* stream) {
+  QED3_GUARD_BEGIN
+  if (!ov || !(margin >= 0 && margin < 0.5)) return fail(QED3_ERR_ARG, "bad argument");
+  return ext_overlap_update(ov, lambda_min, lambda_max, tol, margin, (cudaStream_t)stream);
+  QED3_GUARD_END
+}
+
+int qed3_overlap_ext_info(const qed3_overlap_ext* ov, double* lambda_min, double* lambda_max, double* k,
+                          double* delta) {
+  QED3_GUARD_BEGIN
+  if (!ov || !lambda_min || !lambda_max || !k || !delta) return fail(QED3_ERR_ARG, "NULL argument");
+  ext_overlap_info(ov, lambda_min, lambda_max, k, delta);
+  return QED3_OK;
+  QED3_GUARD_END
+}
+
+int qed3_overlap_ext_apply(qed3_overlap_ext* ov, int op, double* out, const double* in, double tol_inner,
+                           int* pole_iters, void* stream) {
+  QED3_GUARD_BEGIN
+  if (!ov || !out || !in || out == in) return fail(QED3_ERR_ARG, "NULL or aliased argument");
+  return ext_overlap_apply(ov, op, out, in, tol_inner > 0 ? tol_inner : 1e-12, pole_iters, (cudaStream_t)stream);
+  QED3_GUARD_END
+}
+
+int qed3_overlap_ext_solve(qed3_overlap_ext* ov, double* x, const double* b, double tol, double tol_inner,
+                           int maxiter, int prop, qed3_solve_report* report, void* stream) {
+  QED3_GUARD_BEGIN
+  if (!ov || !x || !b || x == b) return fail(QED3_ERR_ARG, "NULL or aliased argument");
+  return ext_overlap_solve(ov, x, b, tol > 0 ? tol : 1e-10, tol_inner > 0 ? tol_inner : 1e-12,
+                           maxiter > 0 ? maxiter : 100000, prop, report, (cudaStream_t)stream);
+  QED3_GUARD_END
+}
+
 int qed3_dirac_ext_cg_solve(qed3_dirac_ext* e, double* x, const double* b, const qed3_solve_params* params,
                             qed3_solve_report* report, void* stream) {
   QED3_GUARD_BEGIN

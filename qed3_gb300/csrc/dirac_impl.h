@@ -1,6 +1,8 @@
 // Host-side functions implemented in the .cu translation units.
 #pragma once
 
+#include <functional>
+
 #include <cuda_runtime.h>
 
 #include "handles.h"
@@ -36,6 +38,9 @@ int ensure_work(qed3_dirac_s* d);
 int cg_finish(qed3_dirac_s* d, double* x, qed3_solve_report* rep, cudaStream_t st);
 int spectral_bounds(qed3_dirac_s* d, double tol, int maxsteps, double* lmin, double* lmax, int* steps_used,
                     cudaStream_t st);
+// extremal eigenvalues of a hermitian positive operator on nd doubles (Lanczos)
+int lanczos_extremal(long long nd, const std::function<int(double*, const double*)>& apply, double tol, int maxsteps,
+                     double* lmin, double* lmax, int* steps_used, cudaStream_t st);
 int bicgstab_solve(qed3_dirac_s* d, int op, double* x, const double* b, const qed3_solve_params* prm, double eps,
                    qed3_solve_report* rep, cudaStream_t st);
 int cg_solve_noalloc(qed3_dirac_s* d, double* x, const double* b, const qed3_solve_params* prm,

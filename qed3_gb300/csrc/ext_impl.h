@@ -28,6 +28,8 @@ struct qed3_dirac_ext_s {
   bool links_set = false;
 };
 
+struct qed3_overlap_ext_s;
+
 namespace qed3 {
 int ext_init(qed3_dirac_ext_s* e);
 void ext_free(qed3_dirac_ext_s* e);
@@ -36,6 +38,14 @@ int ext_apply(qed3_dirac_ext_s* e, int op, double* out, const double* in, cudaSt
 int ext_fermion_force(qed3_dirac_ext_s* e, const double* eta, double* F, cudaStream_t st);
 int ext_propagator(qed3_dirac_ext_s* e, int s, int ix, int a, int dagger, double* sink, const qed3_solve_params* prm,
                    qed3_solve_report* rep, cudaStream_t st);
+int ext_overlap_create(qed3_dirac_ext_s* e, int order, qed3_overlap_ext_s** out);
+void ext_overlap_destroy(qed3_overlap_ext_s* ov);
+int ext_overlap_update(qed3_overlap_ext_s* ov, double lmin, double lmax, double tol, double margin, cudaStream_t st);
+int ext_overlap_apply(qed3_overlap_ext_s* ov, int op, double* out, const double* in, double tol, int* iters,
+                      cudaStream_t st);
+int ext_overlap_solve(qed3_overlap_ext_s* ov, double* x, const double* b, double tol, double tol_inner, int maxiter,
+                      int prop, qed3_solve_report* rep, cudaStream_t st);
+void ext_overlap_info(const qed3_overlap_ext_s* ov, double* lmin, double* lmax, double* k, double* delta);
 int hmc_ext(qed3_dirac_ext_s* e, qed3_rng_s* rng, double* A, double at, double gsq, double tmax, int nsteps,
             int nsteps_inner, int npf, int integrator, double tol, int prec, int no_reject, int* accepted,
             double* dH_out, int* cg_iters, cudaStream_t st);

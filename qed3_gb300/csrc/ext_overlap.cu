@@ -1,0 +1,280 @@
+// Overlap operator of the S^2 x S^1 Wilson operator: Overlap<DiracExt>
+// (src/both_3d/overlap.h:137-390 with WilsonDirac = DiracExt<S2Trivalent,
+// DiracS2Dual>, the operator of the reference's IS_OVERLAP builds of hmc.cu
+// and prop.cu, src/both_3d/hmc.cu:139-160, src/both_3d/prop.cu:190-215).
+//
+//   D_ov xi     = xi + (C/lmax) D (xi + sum_m A_m lmax^2 z_m)
+//   D_ov^dag xi = xi + C (y0 + sum_m A_m lmax^2 y_m),  y0 = D^dag xi / lmax
+//   D_ov^dag D_ov = D_ov + D_ov^dag                     (Overlap::DHD, :363-375)
+// with z_m = (D^dag D + lmax^2 sigma_m)^{-1} xi, sigma_m = -k^2/cp_m, k =
+// lmin/lmax, the Zolotarev coefficients of zolotarev.cpp (pinned to the
+// reference's own build).  All poles come from ONE FP64 multi-shift CG on the
+// S^2 x S^1 D^dag D (the reference solves one CG per pole): the base system is
+// the smallest shift, the others follow with the shifted-CG scalars, and all
+// shifts' x_m, p_m updates are one kernel per iteration.  lmin, lmax are
+// passed in or come from Lanczos on D^dag D (Ritz values lie inside the
+// spectrum; a relative margin widens them).  The outer solve is CG on
+// D_ov + D_ov^dag (MatPoly::solve over Overlap::DHD).
+
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+#include "blas_impl.h"
+#include "device.cuh"
+#include "dirac_impl.h"
+#include "ext_impl.h"
+#include "handles.h"
+#include "qed3_internal.h"
+
+struct qed3_overlap_ext_s {
+  qed3_dirac_ext_s* e = nullptr;
+  int order = 0;
+  double lmin = 0, lmax = 0;
+  qed3::ZoloCoeffs z;
+  bool ready = false;
+  double* buf = nullptr;  // Z [np][nd], P [np][nd], r, p, q, y0, y, w, t, then 2048 partials
+};
+
+namespace qed3 {
+
+static inline int nblk_o(long long n, int t = 256) { return int((n + t - 1) / t); }
+
+// x_m += a_m p_m, p_m = z_m r + b_m p_m for every active shift m (inactive: a_m = 0, z_m = 0, b_m = 1)
+__global__ void k_ms_update(long long nd, int ns, PoleCoef a, PoleCoef z, PoleCoef b, const double* __restrict__ r,
+                            double* __restrict__ X, double* __restrict__ P) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nd) return;
+  const double ri = r[i];
+  for (int m = 0; m < ns; m++) {
+    const size_t o = size_t(m) * nd + i;
+    const double pm = P[o];
+    X[o] += a.c[m] * pm;
+    P[o] = z.c[m] * ri + b.c[m] * pm;
+  }
+}
+
+int ext_overlap_create(qed3_dirac_ext_s* e, int order, qed3_overlap_ext_s** out) {
+  if (order < 3 || order / 2 > kMaxPoles) return fail(QED3_ERR_ARG, "Zolotarev order must be in [3, 129]");
+  auto* ov = new qed3_overlap_ext_s;
+  ov->e = e;
+  ov->order = order;
+  const long long nd = 4LL * e->d2->Ns * e->Nt;
+  const int np = order / 2;
+  if (cudaMalloc(&ov->buf, (size_t(2 * np + 7) * nd + 2048) * sizeof(double)) != cudaSuccess) {
+    delete ov;
+    return fail(QED3_ERR_NOMEM, "cudaMalloc failed");
+  }
+  *out = ov;
+  return QED3_OK;
+}
+
+void ext_overlap_destroy(qed3_overlap_ext_s* ov) {
+  if (!ov) return;
+  if (ov->buf) cudaFree(ov->buf);
+  delete ov;
+}
+
+// lmin = lmax = 0: sqrt of the extremal eigenvalues of D^dag D by Lanczos to
+// rel. tol, widened by margin (lmin (1 - margin), lmax (1 + margin)).
+int ext_overlap_update(qed3_overlap_ext_s* ov, double lmin, double lmax, double tol, double margin,
+                       cudaStream_t st) {
+  qed3_dirac_ext_s* e = ov->e;
+  if (!e->links_set) return fail(QED3_ERR_STATE, "call qed3_dirac_ext_set_links first");
+  if (!(lmin > 0 && lmax > 0)) {
+    const long long nd = 4LL * e->d2->Ns * e->Nt;
+    double a = 0, b = 0;
+    int steps = 0;
+    const int rc = lanczos_extremal(
+        nd, [&](double* o, const double* v) { return ext_apply(e, QED3_OP_DDAGD, o, v, st); }, tol > 0 ? tol : 1e-10,
+        20000, &a, &b, &steps, st);
+    if (rc && rc != QED3_ERR_NOCONV) return rc;
+    if (!(a > 0)) return fail(QED3_ERR_NOCONV, "Lanczos gave a non-positive lower bound");
+    lmin = std::sqrt(a) * (1.0 - margin);
+    lmax = std::sqrt(b) * (1.0 + margin);
+  }
+  if (!(lmin > 0 && lmin < lmax)) return fail(QED3_ERR_ARG, "need 0 < lambda_min < lambda_max");
+  ov->lmin = lmin;
+  ov->lmax = lmax;
+  const int rc = zolotarev_coeffs(lmin / lmax, ov->order, ov->z);
+  if (rc) return rc;
+  ov->ready = true;
+  return QED3_OK;
+}
+
+// (D^dag D + s_m) Z_m = rhs for all poles, s_m = lmax^2 sigma_m: FP64 multi-shift CG
+static int ext_pole_solves(qed3_overlap_ext_s* ov, const double* rhs, double tol, int* iters, cudaStream_t st) {
+  qed3_dirac_ext_s* e = ov->e;
+  const long long nd = 4LL * e->d2->Ns * e->Nt, nc = nd / 2;
+  const int np = ov->order / 2;
+  double *Z = ov->buf, *P = Z + size_t(np) * nd, *r = P + size_t(np) * nd, *p = r + nd, *q = p + nd;
+  double* part = ov->buf + size_t(2 * np + 7) * nd;
+  std::vector<double> s(np);
+  for (int m = 1; m <= np; m++) s[m - 1] = ov->lmax * ov->lmax * (-ov->z.k * ov->z.k / ov->z.cp[m]);
+  const double sb = *std::min_element(s.begin(), s.end());
+  int rc;
+  double bb = 0, im = 0;
+  if ((rc = vec_zdot(nc, rhs, rhs, part, &bb, &im, st))) return rc;
+  QED3_CUDA_TRY(cudaMemsetAsync(Z, 0, size_t(np) * nd * sizeof(double), st));
+  QED3_CUDA_TRY(cudaMemcpyAsync(r, rhs, nd * sizeof(double), cudaMemcpyDeviceToDevice, st));
+  QED3_CUDA_TRY(cudaMemcpyAsync(p, rhs, nd * sizeof(double), cudaMemcpyDeviceToDevice, st));
+  for (int m = 0; m < np; m++)
+    QED3_CUDA_TRY(cudaMemcpyAsync(P + size_t(m) * nd, rhs, nd * sizeof(double), cudaMemcpyDeviceToDevice, st));
+  std::vector<double> zeta(np, 1.0), zold(np, 1.0);
+  std::vector<char> act(np, bb > 0);
+  double rho = bb, a_old = 1.0, b_old = 0.0;
+  int it = 0, nact = bb > 0 ? np : 0;
+  while (nact > 0 && it < 200000) {
+    if ((rc = ext_apply(e, QED3_OP_DDAGD, q, p, st)) || (rc = vec_axpby(nd, sb, p, 1.0, q, q, st))) return rc;
+    double pq = 0;
+    if ((rc = vec_zdot(nc, p, q, part, &pq, &im, st))) return rc;
+    const double alpha = rho / pq;
+    if ((rc = vec_axpby(nd, -alpha, q, 1.0, r, r, st))) return rc;
+    double rn = 0;
+    if ((rc = vec_zdot(nc, r, r, part, &rn, &im, st))) return rc;
+    it++;
+    if (!std::isfinite(rn)) return fail(QED3_ERR_NOCONV, "multi-shift CG: non-finite residual");
+    const double beta = rn / rho;
+    PoleCoef A{}, Zc{}, B{};
+    for (int m = 0; m < np; m++) {
+      if (!act[m]) {
+        B.c[m] = 1.0;
+        continue;
+      }
+      const double zz = zeta[m], zo = zold[m];
+      const double den = alpha * b_old * (zo - zz) + zo * a_old * (1.0 + (s[m] - sb) * alpha);
+      const double zn = zz * zo * a_old / den;
+      A.c[m] = alpha * zn / zz;
+      Zc.c[m] = zn;
+      B.c[m] = beta * (zn / zz) * (zn / zz);
+      zold[m] = zz;
+      zeta[m] = zn;
+    }
+    k_ms_update<<<nblk_o(nd), 256, 0, st>>>(nd, np, A, Zc, B, r, Z, P);
+    QED3_CUDA_TRY(cudaGetLastError());
+    if ((rc = vec_axpby(nd, 1.0, r, beta, p, p, st))) return rc;
+    nact = 0;
+    for (int m = 0; m < np; m++) {
+      if (!act[m]) continue;
+      if (zeta[m] * zeta[m] * rn < tol * tol * bb || !std::isfinite(zeta[m])) act[m] = 0;
+      else nact++;
+    }
+    a_old = alpha;
+    b_old = beta;
+    rho = rn;
+  }
+  if (iters) *iters = it;
+  if (nact > 0) return fail(QED3_ERR_NOCONV, "multi-shift CG did not converge");
+  return QED3_OK;
+}
+
+int ext_overlap_apply(qed3_overlap_ext_s* ov, int op, double* out, const double* in, double tol, int* iters,
+                      cudaStream_t st) {
+  if (!ov->ready) return fail(QED3_ERR_STATE, "call qed3_overlap_ext_update first");
+  qed3_dirac_ext_s* e = ov->e;
+  const long long nd = 4LL * e->d2->Ns * e->Nt;
+  const int np = ov->order / 2;
+  double *Z = ov->buf, *y0 = Z + size_t(2 * np) * nd + 3 * nd, *y = y0 + nd, *w = y + nd, *t = w + nd;
+  const double l2 = ov->lmax * ov->lmax, C = ov->z.C;
+  std::vector<double> coef(np);
+  for (int m = 1; m <= np; m++) coef[m - 1] = ov->z.A[m] * l2;
+  const bool mult = (op == QED3_OP_D || op == QED3_OP_DDAGD || op == QED3_OP_DDDAG);
+  const bool adj = (op == QED3_OP_DDAG || op == QED3_OP_DDAGD || op == QED3_OP_DDDAG);
+  if (op < QED3_OP_D || op > QED3_OP_DDDAG) return fail(QED3_ERR_ARG, "unknown operator");
+  int rc, i1 = 0, i2 = 0;
+  if (mult) {
+    if ((rc = ext_pole_solves(ov, in, tol, &i1, st))) return rc;
+    if ((rc = vec_pole_sum(nd, np, coef.data(), Z, in, t, st))) return rc;  // t = xi + sum A l2 z
+    if ((rc = ext_apply(e, QED3_OP_D, w, t, st))) return rc;               // w = D t
+  }
+  if (adj) {
+    if ((rc = ext_apply(e, QED3_OP_DDAG, y0, in, st))) return rc;
+    if ((rc = vec_axpby(nd, 1.0 / ov->lmax, y0, 0.0, y0, y0, st))) return rc;
+    if ((rc = ext_pole_solves(ov, y0, tol, &i2, st))) return rc;
+    if ((rc = vec_pole_sum(nd, np, coef.data(), Z, y0, y, st))) return rc;  // y = y0 + sum A l2 y_m
+  }
+  if (mult && adj) {
+    if ((rc = vec_axpby(nd, C / ov->lmax, w, C, y, t, st))) return rc;
+    if ((rc = vec_axpby(nd, 1.0, t, 2.0, in, out, st))) return rc;
+  } else if (mult) {
+    if ((rc = vec_axpby(nd, C / ov->lmax, w, 1.0, in, out, st))) return rc;
+  } else {
+    if ((rc = vec_axpby(nd, C, y, 1.0, in, out, st))) return rc;
+  }
+  if (iters) *iters = std::max(i1, i2);
+  return QED3_OK;
+}
+
+// MatPoly::solve over Overlap::DHD: CG on D_ov + D_ov^dag (= D_ov^dag D_ov),
+// certified by the recomputed FP64 residual.  With prop != 0, the propagator
+// of prop.cu's IS_OVERLAP build (src/both_3d/prop.cu:230-268): b is first
+// replaced by D_ov^dag b.
+int ext_overlap_solve(qed3_overlap_ext_s* ov, double* x, const double* b_in, double tol, double tol_inner,
+                      int maxiter, int prop, qed3_solve_report* rep, cudaStream_t st) {
+  if (!ov->ready) return fail(QED3_ERR_STATE, "call qed3_overlap_ext_update first");
+  qed3_dirac_ext_s* e = ov->e;
+  const long long nd = 4LL * e->d2->Ns * e->Nt, nc = nd / 2;
+  double* bufo = nullptr;
+  if (cudaMalloc(&bufo, size_t(5) * nd * sizeof(double)) != cudaSuccess) return fail(QED3_ERR_NOMEM, "cudaMalloc");
+  double *b = bufo, *r = b + nd, *p = r + nd, *q = p + nd, *tt = q + nd;
+  double* part = ov->buf + size_t(2 * (ov->order / 2) + 7) * nd;
+  auto body = [&]() -> int {
+    int rc;
+    if (prop) {
+      if ((rc = ext_overlap_apply(ov, QED3_OP_DDAG, b, b_in, tol_inner, nullptr, st))) return rc;
+    } else {
+      QED3_CUDA_TRY(cudaMemcpyAsync(b, b_in, nd * sizeof(double), cudaMemcpyDeviceToDevice, st));
+    }
+    double bb = 0, im = 0;
+    if ((rc = vec_zdot(nc, b, b, part, &bb, &im, st))) return rc;
+    QED3_CUDA_TRY(cudaMemsetAsync(x, 0, nd * sizeof(double), st));
+    QED3_CUDA_TRY(cudaMemcpyAsync(r, b, nd * sizeof(double), cudaMemcpyDeviceToDevice, st));
+    QED3_CUDA_TRY(cudaMemcpyAsync(p, b, nd * sizeof(double), cudaMemcpyDeviceToDevice, st));
+    double mu = bb;
+    int it = 0, status = bb == 0.0 ? QED3_OK : QED3_ERR_NOCONV;
+    while (status != QED3_OK && it < maxiter) {
+      if ((rc = ext_overlap_apply(ov, QED3_OP_DDAGD, q, p, tol_inner, nullptr, st))) return rc;
+      double pq = 0;
+      if ((rc = vec_zdot(nc, p, q, part, &pq, &im, st))) return rc;
+      const double al = mu / pq;
+      if ((rc = vec_axpby(nd, al, p, 1.0, x, x, st)) || (rc = vec_axpby(nd, -al, q, 1.0, r, r, st))) return rc;
+      double mn = 0;
+      if ((rc = vec_zdot(nc, r, r, part, &mn, &im, st))) return rc;
+      it++;
+      if (!std::isfinite(mn)) break;
+      if (mn < tol * tol * bb) {
+        status = QED3_OK;
+        break;
+      }
+      if ((rc = vec_axpby(nd, 1.0, r, mn / mu, p, p, st))) return rc;
+      mu = mn;
+    }
+    double tr = 0;
+    if (bb > 0) {
+      if ((rc = ext_overlap_apply(ov, QED3_OP_DDAGD, q, x, tol_inner, nullptr, st)) ||
+          (rc = vec_axpby(nd, 1.0, b, -1.0, q, tt, st)) || (rc = vec_zdot(nc, tt, tt, part, &tr, &im, st)))
+        return rc;
+    }
+    if (rep) {
+      rep->status = status;
+      rep->iters = it;
+      rep->reliable_updates = 0;
+      rep->true_rel_res = bb > 0 ? std::sqrt(tr / bb) : 0.0;
+      rep->ms = 0;
+    }
+    return QED3_OK;
+  };
+  const int rc = body();
+  cudaStreamSynchronize(st);
+  cudaFree(bufo);
+  return rc;
+}
+
+void ext_overlap_info(const qed3_overlap_ext_s* ov, double* lmin, double* lmax, double* k, double* delta) {
+  *lmin = ov->lmin;
+  *lmax = ov->lmax;
+  *k = ov->ready ? ov->z.k : 0.0;
+  *delta = ov->ready ? (ov->z.lambda_inv - 1.0) / (ov->z.lambda_inv + 1.0) : 0.0;  // Zolotarev::Delta
+}
+
+}  // namespace qed3

@@ -11,6 +11,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <functional>
 #include <random>
 #include <vector>
 
@@ -52,8 +53,15 @@ static double tridiag_eig(const std::vector<double>& a, const std::vector<double
 int spectral_bounds(qed3_dirac_s* d, double tol, int maxsteps, double* lmin, double* lmax, int* steps_used,
                     cudaStream_t st) {
   if (!d->coeffs_set) return fail(QED3_ERR_STATE, "operator coefficients not set (call qed3_dirac_set_links)");
+  return lanczos_extremal(
+      4LL * d->Ns, [&](double* o, const double* v) { return dirac_apply_ref(d, QED3_OP_DDAGD, o, v, st); }, tol,
+      maxsteps, lmin, lmax, steps_used, st);
+}
+
+int lanczos_extremal(long long nd, const std::function<int(double*, const double*)>& apply, double tol, int maxsteps,
+                     double* lmin, double* lmax, int* steps_used, cudaStream_t st) {
   if (!(tol > 0) || maxsteps < 2) return fail(QED3_ERR_ARG, "need tol > 0 and maxsteps >= 2");
-  const long long nd = 4LL * d->Ns, nc = nd / 2;
+  const long long nc = nd / 2;
   double* buf = nullptr;
   if (cudaMalloc(&buf, size_t(nd) * 3 * sizeof(double) + 2048 * sizeof(double)) != cudaSuccess)
     return fail(QED3_ERR_NOMEM, "cudaMalloc failed");
@@ -74,7 +82,7 @@ int spectral_bounds(qed3_dirac_s* d, double tol, int maxsteps, double* lmin, dou
     double prev_min = 0, prev_max = 0, beta = 0;
     int j = 0, conv = 0, next_check = 10;
     for (; j < maxsteps; j++) {
-      if ((e = dirac_apply_ref(d, QED3_OP_DDAGD, w, v1, st))) return e;
+      if ((e = apply(w, v1))) return e;
       if (j > 0 && (e = vec_axpby(nd, -beta, v0, 1.0, w, w, st))) return e;
       if ((e = vec_zdot(nc, v1, w, part, &re, &im, st))) return e;
       const double alpha = re;  // real: D^dag D is hermitian
