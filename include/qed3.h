@@ -258,6 +258,10 @@ int qed3_overlap_ext_apply(qed3_overlap_ext* ov, int op, double* out, const doub
                            int* pole_iters, void* stream);
 int qed3_overlap_ext_solve(qed3_overlap_ext* ov, double* x, const double* b, double tol, double tol_inner,
                            int maxiter, int prop, qed3_solve_report* report, void* stream);
+/* Overlap pseudofermion force, F = -2 d/dA Re<eta, D_ov eta> for every spatial
+ * and temporal link (Overlap::precalc_grad + grad_deviceAsyncLaunch,
+ * src/both_3d/overlap.h:393-470), pole solves to tol_inner. */
+int qed3_overlap_ext_force(qed3_overlap_ext* ov, const double* eta, double* F, double tol_inner, void* stream);
 /* MatPoly::solve on D^dag D (+ params->shift), certified by the FP64 true
  * residual.  params->precision QED3_PREC_F64: the reference's FP64 recurrence;
  * QED3_PREC_F32: FP32 iterations (FP32 copy of the operator) with FP64
@@ -398,6 +402,15 @@ int qed3_hmc_pure_gauge(qed3_lattice* lat, qed3_rng* rng, double* A, double beta
 int qed3_hmc_ext(qed3_dirac_ext* e, qed3_rng* rng, double* A, double at, double gsq, double tmax, int nsteps,
                  int nsteps_inner, int npf, int integrator, double tol, int precision, int no_reject, int* accepted,
                  double* dH, int* cg_iters, void* stream);
+/* HMC2::run with Overlap<DiracExt> pseudofermions (the reference's IS_OVERLAP
+ * hmc.cu on S^2 x S^1): as qed3_hmc_ext with phi = D_ov^dag xi, eta by the
+ * outer CG on D_ov^dag D_ov (tol; poles to tol_inner), the overlap force, and
+ * the bounds fixed (lambda_min, lambda_max > 0) or recomputed by Lanczos at
+ * every link update (both 0). */
+int qed3_hmc_ext_overlap(qed3_overlap_ext* ov, qed3_rng* rng, double* A, double at, double gsq, double tmax,
+                         int nsteps, int nsteps_inner, int npf, int integrator, double tol, double tol_inner,
+                         double lambda_min, double lambda_max, int no_reject, int* accepted, double* dH,
+                         int* cg_iters, void* stream);
 
 /* ======================================================================
  * Overlap operator  --  replaces Overlap<WilsonDirac> (src/both_3d/overlap.h:137-390):

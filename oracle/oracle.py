@@ -661,16 +661,18 @@ def dirac_ext_matrix(geom: Geometry, r: float, M5: float, Nt: int, at: float, A:
 
 
 def ext_fermion_force(geom: Geometry, r: float, M5: float, Nt: int, at: float, A: np.ndarray, eta: np.ndarray,
-                      M: np.ndarray | None = None) -> np.ndarray:
+                      M: np.ndarray | None = None, chi: np.ndarray | None = None) -> np.ndarray:
     """F = -2 Re <D eta, dD/dA eta> of DiracExt in A's layout: spatial links of
     slice s by the dual-lattice force with chi = (D eta)_s; temporal link (s, x)
     from its two entries, tmpP[s] (row s+1, column s, phase e^{-i A_t}) and
     tmpM[s+1] (row s, column s+1, phase e^{+i A_t})."""
     Ns, Nl = geom.n_sites, geom.n_links
     n2 = 2 * Ns
-    M = dirac_ext_matrix(geom, r, M5, Nt, at, A) if M is None else M
     eta = np.asarray(eta, np.complex128)
-    chi = M @ eta
+    if chi is None:  # -2 Re <chi, dD/dA eta> with chi = D eta; any chi gives the bilinear form
+        M = dirac_ext_matrix(geom, r, M5, Nt, at, A) if M is None else M
+        chi = M @ eta
+    chi = np.asarray(chi, np.complex128)
     As = np.asarray(A[:Nt * Nl]).reshape(Nt, Nl)
     At = np.asarray(A[Nt * Nl:Nt * (Nl + Ns)]).reshape(Nt, Ns)
     D = Dirac(geom, r, M5)
@@ -840,3 +842,92 @@ def overlap_ext_matrix(geom: Geometry, r: float, M5: float, Nt: int, at: float, 
     for m in range(1, z["size"]):
         acc = acc + z["A"][m] * np.linalg.inv(H - z["k"] ** 2 / z["cp"][m] * I)
     return I + z["C"] * X @ acc
+
+
+def overlap_ext_force(geom: Geometry, r: float, M5: float, Nt: int, at: float, A: np.ndarray, eta: np.ndarray,
+                      lmin: float, lmax: float, order: int) -> np.ndarray:
+    """-2 d/dA Re<eta, D_ov eta> of Overlap<DiracExt> (Overlap::precalc_grad +
+    grad_deviceAsyncLaunch, src/both_3d/overlap.h:393-470) by the chain rule on
+    dense matrices: with X = D/lmax, H = X^dag X, z_m = (H + s_m)^{-1} eta,
+    y_m = (H + s_m)^{-1} X^dag eta, w = eta + sum_m A_m z_m,
+      Re<eta, dD_ov eta> = C/lmax Re<eta, dD w>
+                           - C/lmax^2 sum_m A_m (Re<D z_m, dD y_m> + Re<D y_m, dD z_m>),
+    each Re<a, dD b> from the bilinear form of ext_fermion_force."""
+    M = dirac_ext_matrix(geom, r, M5, Nt, at, A)
+    z = zolotarev(lmin / lmax, order)
+    X = M / lmax
+    H = X.conj().T @ X
+    I = np.eye(M.shape[0])
+    eta = np.asarray(eta, np.complex128)
+    form = lambda a, b: -0.5 * ext_fermion_force(geom, r, M5, Nt, at, A, b, chi=a)  # Re<a, dD b>
+    w = eta.copy()
+    acc = 0.0
+    for m in range(1, z["size"]):
+        Hs = H - z["k"] ** 2 / z["cp"][m] * I
+        zm = np.linalg.solve(Hs, eta)
+        ym = np.linalg.solve(Hs, X.conj().T @ eta)
+        w = w + z["A"][m] * zm
+        acc = acc + z["A"][m] * (form(M @ zm, ym) + form(M @ ym, zm))
+    re = z["C"] / lmax * form(eta, w) - z["C"] / lmax ** 2 * acc
+    return -2.0 * re
+
+
+def hmc_ext_overlap(geom: Geometry, rng: Rng, A: np.ndarray, r: float, M5: float, Nt: int, at: float, gsq: float,
+                    lmin: float, lmax: float, order: int, tmax: float = 1.0, nsteps: int = 4, nsteps_inner: int = 4,
+                    npf: int = 1, integrator: int = 0, no_reject: bool = False):
+    """HMC2::run with Overlap<DiracExt> pseudofermions (the IS_OVERLAP build of
+    src/both_3d/hmc.cu) at fixed bounds: hmc_ext with phi = D_ov^dag xi,
+    eta = (D_ov^dag D_ov)^{-1} phi solved densely (D_ov^dag D_ov taken as
+    D_ov + D_ov^dag, Overlap::DHD), and overlap_ext_force.  A updated in place;
+    returns (accepted, dH)."""
+    pi = np.concatenate([rng.gaussian_links(1.0), rng.gaussian_sites(1.0)])
+    xis = [rng.gaussian_spinor() for _ in range(npf)]
+    A0 = A.copy()
+    st = {}
+
+    def update():
+        Dv = overlap_ext_matrix(geom, r, M5, Nt, at, A, lmin, lmax, order)
+        st["D"] = Dv
+        st["H"] = Dv + Dv.conj().T
+
+    update()
+    phis = [st["D"].conj().T @ xi for xi in xis]
+    etas = [np.linalg.solve(st["H"], ph) for ph in phis]
+
+    def H():
+        return (0.5 * float(np.dot(pi, pi)) + ext_gauge(geom, Nt, at, gsq, A)[2]
+                + sum(np.vdot(ph, et).real for ph, et in zip(phis, etas)))
+
+    def resolve():
+        update()
+        for k in range(npf):
+            etas[k] = np.linalg.solve(st["H"], phis[k])
+
+    gforce = lambda: ext_gauge(geom, Nt, at, gsq, A)[3]
+    fforce = lambda k: overlap_ext_force(geom, r, M5, Nt, at, A, etas[k], lmin, lmax, order)
+    h0 = H()
+    tau = tmax / nsteps
+    tau_in = tau / nsteps_inner
+    if integrator == 1:
+        for n in range(nsteps):
+            pi -= 0.5 * tau * (gforce() + sum(fforce(k) for k in range(npf)))
+            A += tau * pi
+            resolve()
+            pi -= 0.5 * tau * (gforce() + sum(fforce(k) for k in range(npf)))
+    else:
+        for k in range(npf):
+            pi -= 0.5 * tau * fforce(k)
+        for n in range(nsteps):
+            pi -= 0.5 * tau_in * gforce()
+            for m in range(nsteps_inner):
+                A += tau_in * pi
+                pi -= (1.0 if m != nsteps_inner - 1 else 0.5) * tau_in * gforce()
+            resolve()
+            for k in range(npf):
+                pi -= (1.0 if n != nsteps - 1 else 0.5) * tau * fforce(k)
+    dH = H() - h0
+    a = rng.uniform()
+    if a < min(1.0, np.exp(-dH)) or no_reject:
+        return True, dH
+    A[:] = A0
+    return False, dH

@@ -149,6 +149,11 @@ SIGNATURES = [
     ("qed3_overlap_ext_apply", ctypes.c_int, [vp, ctypes.c_int, vp, vp, ctypes.c_double, c_int_p, vp]),
     ("qed3_overlap_ext_solve", ctypes.c_int, [vp, vp, vp, ctypes.c_double, ctypes.c_double, ctypes.c_int,
                                               ctypes.c_int, ctypes.POINTER(SolveReport), vp]),
+    ("qed3_overlap_ext_force", ctypes.c_int, [vp, vp, vp, ctypes.c_double, vp]),
+    ("qed3_hmc_ext_overlap", ctypes.c_int, [vp, vp, vp, ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                                            ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double,
+                                            ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_int, c_int_p,
+                                            c_double_p, c_int_p, vp]),
     ("qed3_dirac_ext_cg_solve", ctypes.c_int, [vp, vp, vp, ctypes.POINTER(SolveParams), ctypes.POINTER(SolveReport),
                                                vp]),
     ("qed3_ext_plaquettes", ctypes.c_int, [vp, ctypes.c_int, vp, vp, vp, vp]),
@@ -695,10 +700,29 @@ class OverlapExt:
                                             ctypes.byref(r), _stream(stream)))
         return Report(r.status, r.iters, r.reliable_updates, r.true_rel_res, r.ms)
 
+    def force(self, eta, F, tol_inner: float = 1e-12, stream=None):
+        """F = -2 d/dA Re<eta, D_ov eta> (device, S^2 x S^1 link layout)."""
+        _check(lib().qed3_overlap_ext_force(self._h, _ptr(eta), _ptr(F), tol_inner, _stream(stream)))
+        return F
+
     def __del__(self):
         if getattr(self, "_h", None) and _lib is not None:
             _lib.qed3_overlap_ext_destroy(self._h)
             self._h = None
+
+
+def hmc_ext_overlap(overlap: OverlapExt, rng: ParallelRng, A, gsq: float, tmax: float = 1.0, nsteps: int = 10,
+                    nsteps_inner: int = 10, npf: int = 1, integrator: int = 0, tol: float = 1e-10,
+                    tol_inner: float = 1e-12, lambda_min: float = 0.0, lambda_max: float = 0.0,
+                    no_reject: bool = False, stream=None):
+    """One S^2 x S^1 HMC trajectory with Overlap<DiracExt> pseudofermions (the
+    reference's IS_OVERLAP hmc.cu); bounds fixed or recomputed at every update."""
+    acc, dH, its = ctypes.c_int(), ctypes.c_double(), ctypes.c_int()
+    _check(lib().qed3_hmc_ext_overlap(overlap._h, rng.handle, _ptr(A), overlap.dirac.at, gsq, tmax, nsteps,
+                                      nsteps_inner, npf, integrator, tol, tol_inner, lambda_min, lambda_max,
+                                      int(no_reject), ctypes.byref(acc), ctypes.byref(dH), ctypes.byref(its),
+                                      _stream(stream)))
+    return bool(acc.value), dH.value, its.value
 
 
 def hmc_ext(dirac: DiracExt, rng: ParallelRng, A, gsq: float, tmax: float = 1.0, nsteps: int = 10,

@@ -324,6 +324,36 @@ int qed3_dirac_ext_fermion_force(qed3_dirac_ext* e, const double* eta, double* F
   QED3_GUARD_END
 }
 
+int qed3_overlap_ext_force(qed3_overlap_ext* ov, const double* eta, double* F, double tol_inner, void* stream) {
+  QED3_GUARD_BEGIN
+  if (!ov || !eta || !F) return fail(QED3_ERR_ARG, "NULL argument");
+  return ext_overlap_force(ov, eta, F, tol_inner > 0 ? tol_inner : 1e-12, nullptr, (cudaStream_t)stream);
+  QED3_GUARD_END
+}
+
+int qed3_hmc_ext_overlap(qed3_overlap_ext* ov, qed3_rng* rng, double* A, double at, double gsq, double tmax,
+                         int nsteps, int nsteps_inner, int npf, int integrator, double tol, double tol_inner,
+                         double lambda_min, double lambda_max, int no_reject, int* accepted, double* dH,
+                         int* cg_iters, void* stream) {
+  QED3_GUARD_BEGIN
+  if (!ov || !rng || !A || !accepted || !dH) return fail(QED3_ERR_ARG, "NULL argument");
+  qed3_dirac_ext_s* e = ext_overlap_operator(ov);
+  if (nsteps < 1 || nsteps_inner < 1 || !(tmax > 0) || npf < 1 || npf > 64 || !(at > 0))
+    return fail(QED3_ERR_ARG, "need nsteps, nsteps_inner, npf >= 1, tmax > 0, at > 0");
+  if (integrator != QED3_INTEGRATOR_LEAPFROG_ML && integrator != QED3_INTEGRATOR_LEAPFROG)
+    return fail(QED3_ERR_ARG, "unknown integrator");
+  const size_t nl = size_t(e->d2->lat->host.n_links) * e->Nt, ns = size_t(e->d2->Ns) * e->Nt;
+  size_t rl = 0, rs = 0;
+  rng_counts(rng, &rl, &rs);
+  if (rl != nl || rs != ns)
+    return fail(QED3_ERR_ARG, "rng must hold Nt n_links link engines and Nt n_sites site engines");
+  if ((lambda_min > 0) != (lambda_max > 0)) return fail(QED3_ERR_ARG, "fix both bounds or neither");
+  return hmc_ext(e, rng, A, at, gsq, tmax, nsteps, nsteps_inner, npf, integrator, tol > 0 ? tol : 1e-10,
+                 QED3_PREC_F64, no_reject, accepted, dH, cg_iters, (cudaStream_t)stream, ov,
+                 tol_inner > 0 ? tol_inner : 1e-12, lambda_min, lambda_max);
+  QED3_GUARD_END
+}
+
 int qed3_hmc_ext(qed3_dirac_ext* e, qed3_rng* rng, double* A, double at, double gsq, double tmax, int nsteps,
                  int nsteps_inner, int npf, int integrator, double tol, int precision, int no_reject, int* accepted,
                  double* dH, int* cg_iters, void* stream) {

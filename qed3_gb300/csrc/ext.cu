@@ -125,7 +125,7 @@ __global__ void k_ext_force_sp(int Ns, int Nl, int Nt, const int32_t* __restrict
                                const int32_t* __restrict__ ly, const int8_t* __restrict__ kx,
                                const int8_t* __restrict__ ky, const int32_t* __restrict__ perm,
                                const M64* __restrict__ H3, const S64* __restrict__ eta, const S64* __restrict__ deta,
-                               double* __restrict__ F) {
+                               double c, int acc, double* __restrict__ F) {
   const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (idx >= (long long)Nl * Nt) return;
   const int s = int(idx / Nl), l = int(idx % Nl);
@@ -140,7 +140,8 @@ __global__ void k_ext_force_sp(int Ns, int Nl, int Nt, const int32_t* __restrict
   const double2 v1 = cfma(hyx.h11, ex.s1, cmul(hyx.h10, ex.s0));
   // Re[conj(a) (i b)] = a.y b.x - a.x b.y
   auto re_ci = [](double2 a, double2 b) { return a.y * b.x - a.x * b.y; };
-  F[idx] = -2.0 * (re_ci(dx.s0, u0) + re_ci(dx.s1, u1) - re_ci(dy.s0, v0) - re_ci(dy.s1, v1));
+  const double f = -2.0 * (re_ci(dx.s0, u0) + re_ci(dx.s1, u1) - re_ci(dy.s0, v0) - re_ci(dy.s1, v1));
+  F[idx] = acc ? F[idx] + c * f : c * f;
 }
 
 // Temporal link (s, x) from (x, s) to (x, s+1): D[(x,s+1),(x,s)] = tmpP(s) ~ e^{-iA}
@@ -148,7 +149,7 @@ __global__ void k_ext_force_sp(int Ns, int Nl, int Nt, const int32_t* __restrict
 //   F = -2 Re[ (D eta)_{s+1}^dag (-i tmpP eta_s) + (D eta)_s^dag (i tmpM eta_{s+1}) ]
 __global__ void k_ext_force_tp(int Ns, int Nl, int Nt, const double* __restrict__ kt,
                                const double2* __restrict__ Pt, double r, const S64* __restrict__ eta,
-                               const S64* __restrict__ deta, double* __restrict__ F) {
+                               const S64* __restrict__ deta, double c, int acc, double* __restrict__ F) {
   const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (idx >= (long long)Ns * Nt) return;
   const int s = int(idx / Ns), x = int(idx % Ns);
@@ -165,7 +166,8 @@ __global__ void k_ext_force_tp(int Ns, int Nl, int Nt, const double* __restrict_
   auto re_ci = [](double2 a, double2 b) { return a.y * b.x - a.x * b.y; };  // Re[conj(a) (i b)]
   // (D eta)_{s+1}^dag (-i a) = -Re[conj(d1) (i a)];  (D eta)_s^dag (i b)
   const double inner = -(re_ci(d1.s0, a0) + re_ci(d1.s1, a1)) + re_ci(d0.s0, b0) + re_ci(d0.s1, b1);
-  F[size_t(Nt) * Nl + size_t(s) * Ns + x] = -2.0 * inner;
+  double& o = F[size_t(Nt) * Nl + size_t(s) * Ns + x];
+  o = acc ? o + c * (-2.0 * inner) : c * (-2.0 * inner);
 }
 
 int ext_init(qed3_dirac_ext_s* e) {
@@ -250,23 +252,30 @@ int ext_apply(qed3_dirac_ext_s* e, int op, double* out, const double* in, cudaSt
   return QED3_OK;
 }
 
-int ext_fermion_force(qed3_dirac_ext_s* e, const double* eta, double* F, cudaStream_t st) {
-  if (!e->links_set) return fail(QED3_ERR_STATE, "call qed3_dirac_ext_set_links first");
+// F (+)= c (-2 Re <chi, dD/dA eta>) for every spatial and temporal link
+int ext_force_bilinear(qed3_dirac_ext_s* e, const double* chi, const double* eta, double c, int acc, double* F,
+                       cudaStream_t st) {
   qed3_dirac_s* d = e->d2;
   const DeviceLattice& D = d->lat->dev;
   const int Ns = d->Ns, Nl = D.Nl, Nt = e->Nt;
-  S64* deta = reinterpret_cast<S64*>(e->work);  // D eta (the CG vectors are not in use here)
-  int rc = ext_apply(e, QED3_OP_D, reinterpret_cast<double*>(deta), eta, st);
-  if (rc) return rc;
   const S64* et = reinterpret_cast<const S64*>(eta);
+  const S64* ch = reinterpret_cast<const S64*>(chi);
   k_ext_force_sp<<<nblk((long long)Nl * Nt), 256, 0, st>>>(Ns, Nl, Nt, D.link_x, D.link_y, D.link_kx, D.link_ky, D.perm,
-                                                          e->H3, et, deta, F);
+                                                          e->H3, et, ch, c, acc, F);
   if (Nt > 1)
-    k_ext_force_tp<<<nblk((long long)Ns * Nt), 256, 0, st>>>(Ns, Nl, Nt, e->kt, e->Pt, d->r, et, deta, F);
-  else
+    k_ext_force_tp<<<nblk((long long)Ns * Nt), 256, 0, st>>>(Ns, Nl, Nt, e->kt, e->Pt, d->r, et, ch, c, acc, F);
+  else if (!acc)
     QED3_CUDA_TRY(cudaMemsetAsync(F + size_t(Nt) * Nl, 0, size_t(Ns) * sizeof(double), st));
   QED3_CUDA_TRY(cudaGetLastError());
   return QED3_OK;
+}
+
+int ext_fermion_force(qed3_dirac_ext_s* e, const double* eta, double* F, cudaStream_t st) {
+  if (!e->links_set) return fail(QED3_ERR_STATE, "call qed3_dirac_ext_set_links first");
+  double* deta = reinterpret_cast<double*>(e->work);  // D eta (the CG vectors are not in use here)
+  int rc = ext_apply(e, QED3_OP_D, deta, eta, st);
+  if (rc) return rc;
+  return ext_force_bilinear(e, deta, eta, 1.0, 0, F, st);
 }
 
 // ---- CG with device-resident scalars ------------------------------------------
@@ -764,7 +773,8 @@ namespace qed3 {
 
 int hmc_ext(qed3_dirac_ext_s* e, qed3_rng_s* rng, double* A, double at, double gsq, double tmax, int nsteps,
             int nsteps_inner, int npf, int integrator, double tol, int prec, int no_reject, int* accepted,
-            double* dH_out, int* cg_iters, cudaStream_t st) {
+            double* dH_out, int* cg_iters, cudaStream_t st, qed3_overlap_ext_s* ov, double tol_inner, double lmin_fix,
+            double lmax_fix) {
   qed3_dirac_s* d = e->d2;
   qed3_lattice_s* lat = d->lat;
   const int Ns = d->Ns, Nl = lat->dev.Nl, Nt = e->Nt;
@@ -785,13 +795,23 @@ int hmc_ext(qed3_dirac_ext_s* e, qed3_rng_s* rng, double* A, double at, double g
     QED3_CUDA_TRY(cudaMemcpyAsync(P, pi.data(), nA * sizeof(double), cudaMemcpyHostToDevice, st));
     QED3_CUDA_TRY(cudaMemcpyAsync(A0, A, nA * sizeof(double), cudaMemcpyDeviceToDevice, st));
     QED3_CUDA_TRY(cudaMemcpyAsync(xid, xi.data(), nd * npf * sizeof(double), cudaMemcpyHostToDevice, st));
-    if ((rc = ext_set_links(e, A, st))) return rc;
+    // the fermion operator: the Wilson DiracExt, or its overlap (Overlap::update
+    // recomputes the bounds at every link update unless they are fixed)
+    auto update_op = [&]() -> int {
+      int c = ext_set_links(e, A, st);
+      if (!c && ov) c = ext_overlap_update(ov, lmin_fix, lmax_fix, 1e-10, 1e-6, st);
+      return c;
+    };
+    if ((rc = update_op())) return rc;
     for (int k = 0; k < npf; k++)
-      if ((rc = ext_apply(e, QED3_OP_DDAG, phi + nd * k, xid + nd * k, st))) return rc;
+      if ((rc = ov ? ext_overlap_apply(ov, QED3_OP_DDAG, phi + nd * k, xid + nd * k, tol_inner, nullptr, st)
+                   : ext_apply(e, QED3_OP_DDAG, phi + nd * k, xid + nd * k, st)))
+        return rc;
     auto solve_all = [&]() -> int {
       for (int k = 0; k < npf; k++) {
         qed3_solve_report r{};
-        int c = ext_cg(e, eta + nd * k, phi + nd * k, &sp, &r, st);
+        int c = ov ? ext_overlap_solve(ov, eta + nd * k, phi + nd * k, tol, tol_inner, 100000, 0, &r, st)
+                   : ext_cg(e, eta + nd * k, phi + nd * k, &sp, &r, st);
         its += r.iters;
         if (!c && r.status != QED3_OK) c = fail(QED3_ERR_NOCONV, "pseudofermion solve did not converge");
         if (c) return c;
@@ -819,14 +839,18 @@ int hmc_ext(qed3_dirac_ext_s* e, qed3_rng_s* rng, double* A, double at, double g
       int q = ext_gauge_force(lat, Nt, at, gsq, A, F, st);
       return q ? q : vec_axpby(nA, -c, F, 1.0, P, P, st);
     };
+    auto ferm_force = [&](int k) -> int {
+      return ov ? ext_overlap_force(ov, eta + nd * k, Ff, tol_inner, nullptr, st)
+                : ext_fermion_force(e, eta + nd * k, Ff, st);
+    };
     auto fermion_kick = [&](int k, double c) -> int {
-      int q = ext_fermion_force(e, eta + nd * k, Ff, st);
+      int q = ferm_force(k);
       return q ? q : vec_axpby(nA, -c, Ff, 1.0, P, P, st);
     };
     auto full_kick = [&](double c) -> int {  // pi += -c (dSg + dSf)
       int q = ext_gauge_force(lat, Nt, at, gsq, A, F, st);
       for (int k = 0; k < npf && !q; k++) {
-        q = ext_fermion_force(e, eta + nd * k, Ff, st);
+        q = ferm_force(k);
         if (!q) q = vec_axpby(nA, 1.0, Ff, 1.0, F, F, st);
       }
       return q ? q : vec_axpby(nA, -c, F, 1.0, P, P, st);
@@ -834,7 +858,7 @@ int hmc_ext(qed3_dirac_ext_s* e, qed3_rng_s* rng, double* A, double at, double g
     auto drift = [&](double c) -> int { return vec_axpby(nA, c, P, 1.0, A, A, st); };
     if (integrator == QED3_INTEGRATOR_LEAPFROG) {
       for (int n = 0; n < nsteps; n++) {
-        if ((rc = full_kick(0.5 * tau)) || (rc = drift(tau)) || (rc = ext_set_links(e, A, st)) ||
+        if ((rc = full_kick(0.5 * tau)) || (rc = drift(tau)) || (rc = update_op()) ||
             (rc = solve_all()) || (rc = full_kick(0.5 * tau)))
           return rc;
       }
@@ -845,7 +869,7 @@ int hmc_ext(qed3_dirac_ext_s* e, qed3_rng_s* rng, double* A, double at, double g
         if ((rc = gauge_kick(0.5 * tau_in))) return rc;
         for (int m = 0; m < nsteps_inner; m++)
           if ((rc = drift(tau_in)) || (rc = gauge_kick((m != nsteps_inner - 1 ? 1.0 : 0.5) * tau_in))) return rc;
-        if ((rc = ext_set_links(e, A, st)) || (rc = solve_all())) return rc;
+        if ((rc = update_op()) || (rc = solve_all())) return rc;
         for (int k = 0; k < npf; k++)
           if ((rc = fermion_kick(k, (n != nsteps - 1 ? 1.0 : 0.5) * tau))) return rc;
       }
@@ -861,7 +885,7 @@ int hmc_ext(qed3_dirac_ext_s* e, qed3_rng_s* rng, double* A, double at, double g
     } else {
       *accepted = 0;
       QED3_CUDA_TRY(cudaMemcpyAsync(A, A0, nA * sizeof(double), cudaMemcpyDeviceToDevice, st));
-      if ((rc = ext_set_links(e, A, st))) return rc;
+      if ((rc = update_op())) return rc;
     }
     QED3_CUDA_TRY(cudaStreamSynchronize(st));
     return QED3_OK;

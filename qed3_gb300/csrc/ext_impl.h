@@ -36,6 +36,8 @@ void ext_free(qed3_dirac_ext_s* e);
 int ext_set_links(qed3_dirac_ext_s* e, const double* A, cudaStream_t st);
 int ext_apply(qed3_dirac_ext_s* e, int op, double* out, const double* in, cudaStream_t st);
 int ext_fermion_force(qed3_dirac_ext_s* e, const double* eta, double* F, cudaStream_t st);
+int ext_force_bilinear(qed3_dirac_ext_s* e, const double* chi, const double* eta, double c, int acc, double* F,
+                       cudaStream_t st);
 int ext_propagator(qed3_dirac_ext_s* e, int s, int ix, int a, int dagger, double* sink, const qed3_solve_params* prm,
                    qed3_solve_report* rep, cudaStream_t st);
 int ext_overlap_create(qed3_dirac_ext_s* e, int order, qed3_overlap_ext_s** out);
@@ -46,9 +48,13 @@ int ext_overlap_apply(qed3_overlap_ext_s* ov, int op, double* out, const double*
 int ext_overlap_solve(qed3_overlap_ext_s* ov, double* x, const double* b, double tol, double tol_inner, int maxiter,
                       int prop, qed3_solve_report* rep, cudaStream_t st);
 void ext_overlap_info(const qed3_overlap_ext_s* ov, double* lmin, double* lmax, double* k, double* delta);
+qed3_dirac_ext_s* ext_overlap_operator(qed3_overlap_ext_s* ov);
+int ext_overlap_force(qed3_overlap_ext_s* ov, const double* eta, double* F, double tol, int* iters, cudaStream_t st);
+// ov != NULL: overlap fermions (bounds fixed to lmin_fix, lmax_fix, or recomputed at every update when 0)
 int hmc_ext(qed3_dirac_ext_s* e, qed3_rng_s* rng, double* A, double at, double gsq, double tmax, int nsteps,
             int nsteps_inner, int npf, int integrator, double tol, int prec, int no_reject, int* accepted,
-            double* dH_out, int* cg_iters, cudaStream_t st);
+            double* dH_out, int* cg_iters, cudaStream_t st, qed3_overlap_ext_s* ov = nullptr, double tol_inner = 1e-12,
+            double lmin_fix = 0.0, double lmax_fix = 0.0);
 // FP64 CG on op + shift, op = QED3_OP_DDAGD (default) or QED3_OP_DDDAG
 int ext_cg(qed3_dirac_ext_s* e, double* x, const double* b, const qed3_solve_params* prm, qed3_solve_report* rep,
            cudaStream_t st, int op = QED3_OP_DDAGD);

@@ -34,6 +34,7 @@ struct qed3_overlap_ext_s {
   qed3::ZoloCoeffs z;
   bool ready = false;
   double* buf = nullptr;  // Z [np][nd], P [np][nd], r, p, q, y0, y, w, t, then 2048 partials
+  double* Yb = nullptr;   // [np][nd] second set of pole solutions (force)
 };
 
 namespace qed3 {
@@ -72,6 +73,7 @@ int ext_overlap_create(qed3_dirac_ext_s* e, int order, qed3_overlap_ext_s** out)
 void ext_overlap_destroy(qed3_overlap_ext_s* ov) {
   if (!ov) return;
   if (ov->buf) cudaFree(ov->buf);
+  if (ov->Yb) cudaFree(ov->Yb);
   delete ov;
 }
 
@@ -269,6 +271,46 @@ int ext_overlap_solve(qed3_overlap_ext_s* ov, double* x, const double* b_in, dou
   cudaFree(bufo);
   return rc;
 }
+
+// Overlap pseudofermion force of all links (Overlap::precalc_grad +
+// grad_deviceAsyncLaunch, src/both_3d/overlap.h:393-470), F = -2 d/dA Re<eta, D_ov eta>:
+//   F = sum_m c_m (Re<D Z'_m, dD Y'_m> + Re<D Y'_m, dD Z'_m>) - 2C/lmax Re<eta, dD w>,
+//   c_m = 2 C A_m lmax^2, Z'_m = (D^dag D + lmax^2 s_m)^{-1} eta,
+//   Y'_m = (D^dag D + lmax^2 s_m)^{-1} D^dag eta / lmax, w = eta + sum_m A_m lmax^2 Z'_m;
+// every Re<a, dD b> is one pass of the link kernels (-2 Re<a, dD b> accumulated with weight).
+int ext_overlap_force(qed3_overlap_ext_s* ov, const double* eta, double* F, double tol, int* iters, cudaStream_t st) {
+  if (!ov->ready) return fail(QED3_ERR_STATE, "call qed3_overlap_ext_update first");
+  qed3_dirac_ext_s* e = ov->e;
+  const long long nd = 4LL * e->d2->Ns * e->Nt;
+  const int np = ov->order / 2;
+  double *Z = ov->buf, *y0 = Z + size_t(2 * np) * nd + 3 * nd, *y = y0 + nd, *w = y + nd, *t = w + nd;
+  if (!ov->Yb) QED3_CUDA_TRY(cudaMalloc(&ov->Yb, size_t(np) * nd * sizeof(double)));
+  const double l2 = ov->lmax * ov->lmax, C = ov->z.C;
+  int rc, i1 = 0, i2 = 0;
+  if ((rc = ext_apply(e, QED3_OP_DDAG, y0, eta, st))) return rc;
+  if ((rc = vec_axpby(nd, 1.0 / ov->lmax, y0, 0.0, y0, y0, st))) return rc;
+  if ((rc = ext_pole_solves(ov, y0, tol, &i2, st))) return rc;
+  QED3_CUDA_TRY(cudaMemcpyAsync(ov->Yb, Z, size_t(np) * nd * sizeof(double), cudaMemcpyDeviceToDevice, st));
+  if ((rc = ext_pole_solves(ov, eta, tol, &i1, st))) return rc;
+  std::vector<double> coef(np);
+  for (int m = 1; m <= np; m++) coef[m - 1] = ov->z.A[m] * l2;
+  if ((rc = vec_pole_sum(nd, np, coef.data(), Z, eta, w, st))) return rc;
+  // -2C/lmax Re<eta, dD w> = (C/lmax) (-2 Re<eta, dD w>)
+  if ((rc = ext_force_bilinear(e, eta, w, C / ov->lmax, 0, F, st))) return rc;
+  for (int m = 0; m < np; m++) {
+    const double cm = 2.0 * C * ov->z.A[m + 1] * l2;
+    const double* Zm = Z + size_t(m) * nd;
+    const double* Ym = ov->Yb + size_t(m) * nd;
+    if ((rc = ext_apply(e, QED3_OP_D, t, Zm, st)) || (rc = ext_apply(e, QED3_OP_D, y, Ym, st))) return rc;
+    if ((rc = ext_force_bilinear(e, t, Ym, -0.5 * cm, 1, F, st)) ||
+        (rc = ext_force_bilinear(e, y, Zm, -0.5 * cm, 1, F, st)))
+      return rc;
+  }
+  if (iters) *iters = std::max(i1, i2);
+  return QED3_OK;
+}
+
+qed3_dirac_ext_s* ext_overlap_operator(qed3_overlap_ext_s* ov) { return ov->e; }
 
 void ext_overlap_info(const qed3_overlap_ext_s* ov, double* lmin, double* lmax, double* k, double* delta) {
   *lmin = ov->lmin;

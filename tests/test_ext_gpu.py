@@ -328,3 +328,52 @@ def test_overlap_ext_matches_oracle(cuda):
     ov2.update(tol=1e-12, margin=1e-6)
     inf = ov2.info()
     assert abs(inf["lambda_min"] / sv[0] - 1) < 1e-4 and abs(inf["lambda_max"] / sv[-1] - 1) < 1e-4, (inf, sv[0], sv[-1])
+
+
+def _ext_overlap_case(cuda):
+    n, Nt, at, r, M5, order = 2, 2, 0.7, 1.0, -1.0, 21
+    g = O.geometry(n)
+    lat = Q.S2Trivalent(n)
+    A = np.random.default_rng(90).uniform(-0.5, 0.5, Nt * (g.n_links + g.n_sites))
+    M = O.dirac_ext_matrix(g, r, M5, Nt, at, A)
+    sv = np.sqrt(np.linalg.eigvalsh(M.conj().T @ M))
+    return g, lat, A, (n, Nt, at, r, M5, order), sv[0] * 0.99, sv[-1] * 1.01
+
+
+def test_overlap_ext_force_matches_oracle(cuda):
+    """F = -2 d/dA Re<eta, D_ov eta> for Overlap<DiracExt> on the GPU (one pass
+    of the link kernels per bilinear) = the oracle's chain-rule restatement on
+    dense matrices (itself checked against finite differences)."""
+    import torch
+    g, lat, A, (n, Nt, at, r, M5, order), lmin, lmax = _ext_overlap_case(cuda)
+    De = Q.DiracExt(lat, r, M5, Nt, at)
+    De.update(to_dev(A, cuda))
+    ov = Q.OverlapExt(De, order)
+    ov.update(lmin, lmax)
+    rng = np.random.default_rng(93)
+    eta = rng.normal(size=2 * g.n_sites * Nt) + 1j * rng.normal(size=2 * g.n_sites * Nt)
+    F = torch.zeros(A.size, dtype=torch.float64, device=cuda)
+    ov.force(to_dev(eta, cuda), F, tol_inner=1e-13)
+    ref = O.overlap_ext_force(g, r, M5, Nt, at, A, eta, lmin, lmax, order)
+    assert rel(from_dev(F), ref) < 1e-9
+
+
+def test_hmc_ext_overlap_matches_oracle(cuda):
+    """S^2 x S^1 HMC with overlap pseudofermions (the reference's IS_OVERLAP
+    hmc.cu) at fixed bounds against the oracle's dense restatement from the
+    same ParallelRngExt streams: same decisions, dH to 1e-7, links to 1e-8."""
+    import torch
+    g, lat, A, (n, Nt, at, r, M5, order), lmin, lmax = _ext_overlap_case(cuda)
+    De = Q.DiracExt(lat, r, M5, Nt, at)
+    ov = Q.OverlapExt(De, order)
+    rd, ro = Q.ParallelRng(lat, 5, n_slices=Nt), O.Rng(g, 5, Nt)
+    Ad, Ao = to_dev(A, cuda), A.copy()
+    for t in range(2):
+        acc_d, dH_d, its = Q.hmc_ext_overlap(ov, rd, Ad, 1.0, tmax=0.3, nsteps=3, nsteps_inner=2, tol=1e-11,
+                                             tol_inner=1e-13, lambda_min=lmin, lambda_max=lmax)
+        acc_o, dH_o = O.hmc_ext_overlap(g, ro, Ao, r, M5, Nt, at, 1.0, lmin, lmax, order, tmax=0.3, nsteps=3,
+                                        nsteps_inner=2)
+        assert acc_d == acc_o and its > 0, (t, dH_d, dH_o)
+        assert abs(dH_d - dH_o) < 1e-7 * (1 + abs(dH_o)), (t, dH_d, dH_o)
+        torch.cuda.synchronize()
+        assert np.abs(from_dev(Ad) - Ao).max() < 1e-8
