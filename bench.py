@@ -392,6 +392,20 @@ def paths_timings(torch, Q, dev, cpu=True):
                                        "then FP32 + FP64 reliable updates",
                              "cpu_baseline": None, "cpu_note": "the oracle's S^2 x S^1 HMC runs on a dense "
                              "operator (checked at n=2); no CPU sample at this size"}
+    # -- overlap of the S^2 x S^1 operator (M5 = -1, order 21), Lanczos bounds
+    Dw = Q.DiracExt(lat, 1.0, -1.0, Nt, at)
+    Dw.update(Ae)
+    ovx = Q.OverlapExt(Dw, 21)
+    t_up = _wall(torch, lambda: ovx.update(tol=1e-10), 1)
+    inf = ovx.info()
+    ve = torch.randn(Nt * 2 * lat.n_sites, dtype=torch.complex128, device=dev, generator=gen)
+    we = torch.empty_like(ve)
+    pits = []
+    t_ap = _wall(torch, lambda: pits.append(ovx.apply(we, ve, Q.OP_D, tol_inner=1e-10)), 3)
+    out["overlap_ext_n8_nt8"] = {"gpu_ms": 1e3 * t_ap, "pole_iters": pits[-1], "lanczos_update_ms": 1e3 * t_up,
+                                 "k": inf["k"], "config": "n=8, Nt=8, M5=-1, order 21 (10 poles, one FP64 "
+                                 "multi-shift CG), inner tol 1e-10", "cpu_baseline": None,
+                                 "cpu_note": "the oracle's S^2 x S^1 overlap is dense (checked at n=2)"}
     return out
 
 
