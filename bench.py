@@ -470,7 +470,9 @@ def profile_case(torch, which):
         w = torch.empty_like(v)
         for _ in range(3):
             De.apply(w, v, Q.OP_D)
-        print(json.dumps({"norm": float(torch.linalg.vector_norm(w))}))
+        # eight FP32 iterations of the mixed-precision CG (k_ext_apply32 and its BLAS)
+        rep = De.solve(w, v, tol=1e-10, maxiter=8, precision=Q.PREC_F32)
+        print(json.dumps({"norm": float(torch.linalg.vector_norm(w)), "iters": rep.iters}))
     elif which == "batched":
         # a quarter of the 256-RHS configuration (16 right-hand sides on each
         # of n = 16, 32, 48, 64; ~0.4 GB of fields, above L2) with the tile the
