@@ -647,8 +647,9 @@ def main():
     achieved = alg_bytes / (results[best]["ms"] * 1e-3) / 1e9
     peak, peak_kind = peaks()
     sweep = []
-    for n, p in ((64, Q.PREC_F32), (256, Q.PREC_F32), (512, Q.PREC_F32), (512, Q.PREC_BF16), (256, Q.PREC_F64),
-                 (512, Q.PREC_F64)):
+    # the apply sweep over n = 32 ... 512 in FP32 (L2-resident below n ~ 100), BF16 and FP64 at the large end
+    for n, p in tuple((n_, Q.PREC_F32) for n_ in (32, 48, 64, 96, 128, 192, 256, 384, 512)) + (
+            (512, Q.PREC_BF16), (256, Q.PREC_F64), (512, Q.PREC_F64)):
         s_ = apply_bandwidth(torch, Q, n, p)
         s_["frac_of_" + peak_kind] = s_["GB/s"] / peak
         s_["resident"] = "L2" if s_["bytes_per_site"] * 20 * n * n < 100e6 else "HBM"
