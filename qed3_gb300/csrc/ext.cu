@@ -20,6 +20,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <functional>
 #include <vector>
 
 #include "blas_impl.h"
@@ -289,6 +290,37 @@ struct ExtCgState {
   double mu, thr, alpha, beta, done, iters;  // done: 0 running, 1 converged, 2 non-finite
 };
 constexpr int kCgParts = 304;  // partial sums: two blocks per SM
+
+// A chunk of solver iterations (kernel launches only) captured once per solve
+// as a CUDA graph on a private stream and replayed on the caller's stream: one
+// launch per chunk instead of seven per iteration.  If the capture fails the
+// solver launches the kernels directly.
+struct IterGraph {
+  cudaGraphExec_t exec = nullptr;
+  ~IterGraph() {
+    if (exec) cudaGraphExecDestroy(exec);
+  }
+  bool build(int reps, const std::function<int(cudaStream_t)>& iter) {
+    cudaStream_t cs = nullptr;
+    if (cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking) != cudaSuccess) {
+      cudaGetLastError();
+      return false;
+    }
+    bool ok = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal) == cudaSuccess;
+    int rc = 0;
+    for (int k = 0; ok && k < reps && !rc; k++) rc = iter(cs);
+    cudaGraph_t g = nullptr;
+    if (ok) ok = cudaStreamEndCapture(cs, &g) == cudaSuccess && rc == 0 && g != nullptr;
+    if (ok) ok = cudaGraphInstantiate(&exec, g, 0) == cudaSuccess;
+    if (g) cudaGraphDestroy(g);
+    cudaStreamDestroy(cs);
+    if (!ok) {
+      exec = nullptr;
+      cudaGetLastError();
+    }
+    return ok;
+  }
+};
 
 __global__ void k_cg_pq(long long nc, const double2* __restrict__ p, const double2* __restrict__ q,
                         double* __restrict__ part, const ExtCgState* __restrict__ stt) {
@@ -592,11 +624,11 @@ static int ext_cg_mixed(qed3_dirac_ext_s* e, double* x, const double* b, double 
   };
   const int gs = nblk(n);
   const int first = op == QED3_OP_DDAGD ? 0 : 1;  // D^dag D: D then D^dag; D D^dag: the reverse
-  auto A32 = [&](float4* o, const float4* v) {
-    k_ext_apply32<<<gs, 256, 0, st>>>(Ns, Nt, first, e->nbrR, first ? e->Hd3f : e->H3f, e->diag3f, e->ktf, e->Ptf,
-                                      float(e->r), v, tf);
-    k_ext_apply32<<<gs, 256, 0, st>>>(Ns, Nt, 1 - first, e->nbrR, first ? e->H3f : e->Hd3f, e->diag3f, e->ktf,
-                                      e->Ptf, float(e->r), tf, o);
+  auto A32 = [&](float4* o, const float4* v, cudaStream_t s) {
+    k_ext_apply32<<<gs, 256, 0, s>>>(Ns, Nt, first, e->nbrR, first ? e->Hd3f : e->H3f, e->diag3f, e->ktf, e->Ptf,
+                                     float(e->r), v, tf);
+    k_ext_apply32<<<gs, 256, 0, s>>>(Ns, Nt, 1 - first, e->nbrR, first ? e->H3f : e->Hd3f, e->diag3f, e->ktf,
+                                     e->Ptf, float(e->r), tf, o);
   };
   double bb = 0, im = 0;
   if ((rc = vec_zdot(nc, b, b, part, &bb, &im, st))) return rc;
@@ -625,16 +657,25 @@ static int ext_cg_mixed(qed3_dirac_ext_s* e, double* x, const double* b, double 
     if ((rc = restart(bb, true))) return rc;
   }
   const double d2 = delta * delta;
+  auto iter = [&](cudaStream_t s) -> int {
+    A32(qf, pf, s);
+    if (shift != 0.0) k_mcg_shift<<<gblk, 256, 0, s>>>(n, float(shift), pf, qf, dst);
+    k_mcg_pq<<<gblk, 256, 0, s>>>(n, pf, qf, part, dst);
+    k_cg_alpha<<<1, 256, 0, s>>>(part, gblk, dst);
+    k_mcg_xr<<<gblk, 256, 0, s>>>(n, pf, qf, xf, rf, part, dst);
+    k_cg_beta<<<1, 256, 0, s>>>(part, gblk, dst);
+    k_mcg_p<<<gblk, 256, 0, s>>>(n, rf, pf, dst);
+    return QED3_OK;
+  };
+  const int chunk = 8;
+  IterGraph graph;
+  const bool use_graph = status != QED3_OK && maxiter >= chunk && graph.build(chunk, iter);
   while (status != QED3_OK && its < maxiter) {
-    const int m = std::min(8, maxiter - its);
-    for (int k = 0; k < m; k++) {
-      A32(qf, pf);
-      if (shift != 0.0) k_mcg_shift<<<gblk, 256, 0, st>>>(n, float(shift), pf, qf, dst);
-      k_mcg_pq<<<gblk, 256, 0, st>>>(n, pf, qf, part, dst);
-      k_cg_alpha<<<1, 256, 0, st>>>(part, gblk, dst);
-      k_mcg_xr<<<gblk, 256, 0, st>>>(n, pf, qf, xf, rf, part, dst);
-      k_cg_beta<<<1, 256, 0, st>>>(part, gblk, dst);
-      k_mcg_p<<<gblk, 256, 0, st>>>(n, rf, pf, dst);
+    const int m = std::min(chunk, maxiter - its);
+    if (use_graph && m == chunk) {
+      QED3_CUDA_TRY(cudaGraphLaunch(graph.exec, st));
+    } else {
+      for (int k = 0; k < m; k++) iter(st);
     }
     QED3_CUDA_TRY(cudaGetLastError());
     QED3_CUDA_TRY(cudaMemcpyAsync(&hst, dst, sizeof(hst), cudaMemcpyDeviceToHost, st));
@@ -697,11 +738,12 @@ int ext_cg(qed3_dirac_ext_s* e, double* x, const double* b, const qed3_solve_par
   QED3_CUDA_TRY(cudaEventCreate(&e0));
   QED3_CUDA_TRY(cudaEventCreate(&e1));
   QED3_CUDA_TRY(cudaEventRecord(e0, st));
-  auto A = [&](double* o, const double* v) -> int {
-    int c = ext_apply(e, op, o, v, st);
-    if (!c && shift != 0.0) c = vec_axpby(nd, shift, v, 1.0, o, o, st);
+  auto As = [&](double* o, const double* v, cudaStream_t s) -> int {
+    int c = ext_apply(e, op, o, v, s);
+    if (!c && shift != 0.0) c = vec_axpby(nd, shift, v, 1.0, o, o, s);
     return c;
   };
+  auto A = [&](double* o, const double* v) -> int { return As(o, v, st); };
   int rc;
   double bb = 0, im = 0;
   if ((rc = vec_zdot(nc, b, b, part, &bb, &im, st))) return rc;
@@ -716,16 +758,25 @@ int ext_cg(qed3_dirac_ext_s* e, double* x, const double* b, const qed3_solve_par
   const int gblk = int(std::min<long long>(kCgParts, (nc + 255) / 256));
   int launched = 0;
   const int chunk = 16;
+  auto iter = [&](cudaStream_t s) -> int {
+    const int c = As(q, p, s);
+    if (c) return c;
+    k_cg_pq<<<gblk, 256, 0, s>>>(nc, p2, q2, part, dst);
+    k_cg_alpha<<<1, 256, 0, s>>>(part, gblk, dst);
+    k_cg_xr<<<gblk, 256, 0, s>>>(nc, p2, q2, reinterpret_cast<double2*>(x), reinterpret_cast<double2*>(r), part, dst);
+    k_cg_beta<<<1, 256, 0, s>>>(part, gblk, dst);
+    k_cg_p<<<gblk, 256, 0, s>>>(nc, reinterpret_cast<const double2*>(r), reinterpret_cast<double2*>(p), dst);
+    return QED3_OK;
+  };
+  IterGraph graph;
+  const bool use_graph = hst.done == 0.0 && maxiter >= chunk && graph.build(chunk, iter);
   while (hst.done == 0.0 && launched < maxiter) {
     const int m = std::min(chunk, maxiter - launched);
-    for (int k = 0; k < m; k++) {
-      if ((rc = A(q, p))) return rc;
-      k_cg_pq<<<gblk, 256, 0, st>>>(nc, p2, q2, part, dst);
-      k_cg_alpha<<<1, 256, 0, st>>>(part, gblk, dst);
-      k_cg_xr<<<gblk, 256, 0, st>>>(nc, p2, q2, reinterpret_cast<double2*>(x), reinterpret_cast<double2*>(r), part,
-                                    dst);
-      k_cg_beta<<<1, 256, 0, st>>>(part, gblk, dst);
-      k_cg_p<<<gblk, 256, 0, st>>>(nc, reinterpret_cast<const double2*>(r), reinterpret_cast<double2*>(p), dst);
+    if (use_graph && m == chunk) {
+      QED3_CUDA_TRY(cudaGraphLaunch(graph.exec, st));
+    } else {
+      for (int k = 0; k < m; k++)
+        if ((rc = iter(st))) return rc;
     }
     QED3_CUDA_TRY(cudaGetLastError());
     launched += m;
