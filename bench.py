@@ -283,7 +283,7 @@ def paths_timings(torch, Q, dev, cpu=True):
     w = torch.empty_like(v)
     gpu_s = _wall(torch, lambda: ov.apply(w, v, tol_inner=1e-10), 5)
     row = {"gpu_ms": 1e3 * gpu_s, "k": inf["k"], "config": "n=16, M5=-1, order 41 (20 poles), inner tol 1e-10 "
-           "(batched multi-shift pole solves)"}
+           "(all poles in one FP64 multi-shift CG)"}
     if cpu:
         Dow = O.Dirac(g, 1.0, -1.0)
         Dow.update(A0.cpu().numpy())
