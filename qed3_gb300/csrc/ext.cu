@@ -291,36 +291,6 @@ struct ExtCgState {
 };
 constexpr int kCgParts = 304;  // partial sums: two blocks per SM
 
-// A chunk of solver iterations (kernel launches only) captured once per solve
-// as a CUDA graph on a private stream and replayed on the caller's stream: one
-// launch per chunk instead of seven per iteration.  If the capture fails the
-// solver launches the kernels directly.
-struct IterGraph {
-  cudaGraphExec_t exec = nullptr;
-  ~IterGraph() {
-    if (exec) cudaGraphExecDestroy(exec);
-  }
-  bool build(int reps, const std::function<int(cudaStream_t)>& iter) {
-    cudaStream_t cs = nullptr;
-    if (cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking) != cudaSuccess) {
-      cudaGetLastError();
-      return false;
-    }
-    bool ok = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal) == cudaSuccess;
-    int rc = 0;
-    for (int k = 0; ok && k < reps && !rc; k++) rc = iter(cs);
-    cudaGraph_t g = nullptr;
-    if (ok) ok = cudaStreamEndCapture(cs, &g) == cudaSuccess && rc == 0 && g != nullptr;
-    if (ok) ok = cudaGraphInstantiate(&exec, g, 0) == cudaSuccess;
-    if (g) cudaGraphDestroy(g);
-    cudaStreamDestroy(cs);
-    if (!ok) {
-      exec = nullptr;
-      cudaGetLastError();
-    }
-    return ok;
-  }
-};
 
 __global__ void k_cg_pq(long long nc, const double2* __restrict__ p, const double2* __restrict__ q,
                         double* __restrict__ part, const ExtCgState* __restrict__ stt) {

@@ -3,6 +3,8 @@
 
 #include <cuda_runtime.h>
 
+#include <functional>
+
 #include "handles.h"
 
 struct qed3_dirac_ext_s {
@@ -31,6 +33,37 @@ struct qed3_dirac_ext_s {
 struct qed3_overlap_ext_s;
 
 namespace qed3 {
+// A chunk of solver iterations (kernel launches only) captured once per solve
+// as a CUDA graph on a private stream and replayed on the caller's stream: one
+// launch per chunk instead of seven per iteration.  If the capture fails the
+// solver launches the kernels directly.
+struct IterGraph {
+  cudaGraphExec_t exec = nullptr;
+  ~IterGraph() {
+    if (exec) cudaGraphExecDestroy(exec);
+  }
+  bool build(int reps, const std::function<int(cudaStream_t)>& iter) {
+    cudaStream_t cs = nullptr;
+    if (cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking) != cudaSuccess) {
+      cudaGetLastError();
+      return false;
+    }
+    bool ok = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal) == cudaSuccess;
+    int rc = 0;
+    for (int k = 0; ok && k < reps && !rc; k++) rc = iter(cs);
+    cudaGraph_t g = nullptr;
+    if (ok) ok = cudaStreamEndCapture(cs, &g) == cudaSuccess && rc == 0 && g != nullptr;
+    if (ok) ok = cudaGraphInstantiate(&exec, g, 0) == cudaSuccess;
+    if (g) cudaGraphDestroy(g);
+    cudaStreamDestroy(cs);
+    if (!ok) {
+      exec = nullptr;
+      cudaGetLastError();
+    }
+    return ok;
+  }
+};
+
 int ext_init(qed3_dirac_ext_s* e);
 void ext_free(qed3_dirac_ext_s* e);
 int ext_set_links(qed3_dirac_ext_s* e, const double* A, cudaStream_t st);

@@ -10,8 +10,9 @@
 // lmin/lmax, the Zolotarev coefficients of zolotarev.cpp (pinned to the
 // reference's own build).  All poles come from ONE FP64 multi-shift CG on the
 // S^2 x S^1 D^dag D (the reference solves one CG per pole): the base system is
-// the smallest shift, the others follow with the shifted-CG scalars, and all
-// shifts' x_m, p_m updates are one kernel per iteration.  lmin, lmax are
+// the smallest shift, the others follow with the shifted-CG scalars (computed
+// on the device), all shifts' x_m, p_m updates are one kernel per iteration,
+// and chunks of iterations replay as a CUDA graph.  lmin, lmax are
 // passed in or come from Lanczos on D^dag D (Ritz values lie inside the
 // spectrum; a relative margin widens them).  The outer solve is CG on
 // D_ov + D_ov^dag (MatPoly::solve over Overlap::DHD).
@@ -35,25 +36,12 @@ struct qed3_overlap_ext_s {
   bool ready = false;
   double* buf = nullptr;  // Z [np][nd], P [np][nd], r, p, q, y0, y, w, t, then 2048 partials
   double* Yb = nullptr;   // [np][nd] second set of pole solutions (force)
+  void* ms = nullptr;     // device state of the multi-shift CG
 };
 
 namespace qed3 {
 
 static inline int nblk_o(long long n, int t = 256) { return int((n + t - 1) / t); }
-
-// x_m += a_m p_m, p_m = z_m r + b_m p_m for every active shift m (inactive: a_m = 0, z_m = 0, b_m = 1)
-__global__ void k_ms_update(long long nd, int ns, PoleCoef a, PoleCoef z, PoleCoef b, const double* __restrict__ r,
-                            double* __restrict__ X, double* __restrict__ P) {
-  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= nd) return;
-  const double ri = r[i];
-  for (int m = 0; m < ns; m++) {
-    const size_t o = size_t(m) * nd + i;
-    const double pm = P[o];
-    X[o] += a.c[m] * pm;
-    P[o] = z.c[m] * ri + b.c[m] * pm;
-  }
-}
 
 int ext_overlap_create(qed3_dirac_ext_s* e, int order, qed3_overlap_ext_s** out) {
   if (order < 3 || order / 2 > kMaxPoles) return fail(QED3_ERR_ARG, "Zolotarev order must be in [3, 129]");
@@ -74,6 +62,7 @@ void ext_overlap_destroy(qed3_overlap_ext_s* ov) {
   if (!ov) return;
   if (ov->buf) cudaFree(ov->buf);
   if (ov->Yb) cudaFree(ov->Yb);
+  if (ov->ms) cudaFree(ov->ms);
   delete ov;
 }
 
@@ -104,6 +93,123 @@ int ext_overlap_update(qed3_overlap_ext_s* ov, double lmin, double lmax, double 
   return QED3_OK;
 }
 
+// ---- multi-shift CG with device-resident scalars ---------------------------
+// State: base-system scalars, then per shift zeta, zold, active flag and the
+// step coefficients a_m, z_m, b_m (np <= kMaxPoles).  All kernels return at
+// once when `done` is set, so a replayed chunk past convergence is a no-op.
+struct MsState {
+  double rho, alpha, beta, a_old, b_old, done, iters, thr, pq;
+  double zeta[kMaxPoles], zold[kMaxPoles], act[kMaxPoles], am[kMaxPoles], zm[kMaxPoles], bm[kMaxPoles];
+};
+constexpr int kMsParts = 304;
+
+__global__ void k_ms_pq(long long nc, const double2* __restrict__ p, const double2* __restrict__ q,
+                        double* __restrict__ part, const MsState* __restrict__ S) {
+  if (S->done != 0.0) return;
+  __shared__ double sh[32];
+  double v[1] = {0.0};
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < nc; i += (long long)gridDim.x * blockDim.x) {
+    const double2 a = p[i], b = q[i];
+    v[0] += a.x * b.x + a.y * b.y;
+  }
+  block_sum<1>(v, sh);
+  if (threadIdx.x == 0) part[blockIdx.x] = v[0];
+}
+
+__global__ void k_ms_alpha(const double* __restrict__ part, int np, MsState* __restrict__ S) {
+  if (S->done != 0.0) return;
+  __shared__ double sh[32];
+  double v[1] = {0.0};
+  for (int i = threadIdx.x; i < np; i += blockDim.x) v[0] += part[i];
+  block_sum<1>(v, sh);
+  if (threadIdx.x == 0) S->alpha = S->rho / v[0];
+}
+
+// r -= alpha q, partial sums of |r|^2
+__global__ void k_ms_r(long long nc, const double2* __restrict__ q, double2* __restrict__ r, double* __restrict__ part,
+                       const MsState* __restrict__ S) {
+  if (S->done != 0.0) return;
+  __shared__ double sh[32];
+  const double al = S->alpha;
+  double v[1] = {0.0};
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < nc; i += (long long)gridDim.x * blockDim.x) {
+    double2 rr = r[i];
+    const double2 qq = q[i];
+    rr.x -= al * qq.x;
+    rr.y -= al * qq.y;
+    r[i] = rr;
+    v[0] += rr.x * rr.x + rr.y * rr.y;
+  }
+  block_sum<1>(v, sh);
+  if (threadIdx.x == 0) part[blockIdx.x] = v[0];
+}
+
+// |r|^2, beta and every active shift's zeta recurrence (Frommer; Jegerlehner)
+__global__ void k_ms_scalars(const double* __restrict__ part, int nparts, int ns, const double* __restrict__ dsig,
+                             MsState* __restrict__ S) {
+  if (S->done != 0.0) return;
+  __shared__ double sh[32];
+  __shared__ double rn_s;
+  double v[1] = {0.0};
+  for (int i = threadIdx.x; i < nparts; i += blockDim.x) v[0] += part[i];
+  block_sum<1>(v, sh);
+  if (threadIdx.x == 0) rn_s = v[0];
+  __syncthreads();
+  const double rn = rn_s, alpha = S->alpha, beta = rn / S->rho, a_old = S->a_old, b_old = S->b_old;
+  const int m = threadIdx.x;
+  if (m < ns) {
+    if (S->act[m] != 0.0) {
+      const double z = S->zeta[m], zo = S->zold[m];
+      const double den = alpha * b_old * (zo - z) + zo * a_old * (1.0 + dsig[m] * alpha);
+      const double zn = z * zo * a_old / den;
+      S->am[m] = alpha * zn / z;
+      S->zm[m] = zn;
+      S->bm[m] = beta * (zn / z) * (zn / z);
+      S->zold[m] = z;
+      S->zeta[m] = zn;
+      if (zn * zn * rn < S->thr || !isfinite(zn)) S->act[m] = 0.0;
+    } else {
+      S->am[m] = 0.0;
+      S->zm[m] = 0.0;
+      S->bm[m] = 1.0;
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int nact = 0;
+    for (int k = 0; k < ns; k++) nact += S->act[k] != 0.0;
+    S->beta = beta;
+    S->a_old = alpha;
+    S->b_old = beta;
+    S->rho = rn;
+    S->iters += 1.0;
+    if (!isfinite(rn)) S->done = 2.0;
+    // the step's updates below still run; `done` is read by the next iteration's kernels
+    S->pq = nact;
+  }
+}
+
+// x_m += a_m p_m, p_m = z_m r + b_m p_m for every shift, then p = r + beta p; sets done when no shift is active
+__global__ void k_ms_update_dev(long long nd, int ns, const double* __restrict__ r, double* __restrict__ X,
+                                double* __restrict__ P, double* __restrict__ p, MsState* __restrict__ S) {
+  if (S->done != 0.0) return;
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < nd) {
+    const double ri = r[i];
+    for (int m = 0; m < ns; m++) {
+      const size_t o = size_t(m) * nd + i;
+      const double pm = P[o];
+      X[o] += S->am[m] * pm;
+      P[o] = S->zm[m] * ri + S->bm[m] * pm;
+    }
+    p[i] = ri + S->beta * p[i];
+  }
+}
+
+__global__ void k_ms_finish(MsState* __restrict__ S) {
+  if (S->done == 0.0 && S->pq == 0.0) S->done = 1.0;
+}
+
 // (D^dag D + s_m) Z_m = rhs for all poles, s_m = lmax^2 sigma_m: FP64 multi-shift CG
 static int ext_pole_solves(qed3_overlap_ext_s* ov, const double* rhs, double tol, int* iters, cudaStream_t st) {
   qed3_dirac_ext_s* e = ov->e;
@@ -111,9 +217,14 @@ static int ext_pole_solves(qed3_overlap_ext_s* ov, const double* rhs, double tol
   const int np = ov->order / 2;
   double *Z = ov->buf, *P = Z + size_t(np) * nd, *r = P + size_t(np) * nd, *p = r + nd, *q = p + nd;
   double* part = ov->buf + size_t(2 * np + 7) * nd;
+  if (!ov->ms) QED3_CUDA_TRY(cudaMalloc(&ov->ms, sizeof(MsState) + kMaxPoles * sizeof(double)));
+  MsState* S = reinterpret_cast<MsState*>(ov->ms);
+  double* dsig = reinterpret_cast<double*>(S + 1);
   std::vector<double> s(np);
   for (int m = 1; m <= np; m++) s[m - 1] = ov->lmax * ov->lmax * (-ov->z.k * ov->z.k / ov->z.cp[m]);
   const double sb = *std::min_element(s.begin(), s.end());
+  std::vector<double> ds(np);
+  for (int m = 0; m < np; m++) ds[m] = s[m] - sb;
   int rc;
   double bb = 0, im = 0;
   if ((rc = vec_zdot(nc, rhs, rhs, part, &bb, &im, st))) return rc;
@@ -122,51 +233,50 @@ static int ext_pole_solves(qed3_overlap_ext_s* ov, const double* rhs, double tol
   QED3_CUDA_TRY(cudaMemcpyAsync(p, rhs, nd * sizeof(double), cudaMemcpyDeviceToDevice, st));
   for (int m = 0; m < np; m++)
     QED3_CUDA_TRY(cudaMemcpyAsync(P + size_t(m) * nd, rhs, nd * sizeof(double), cudaMemcpyDeviceToDevice, st));
-  std::vector<double> zeta(np, 1.0), zold(np, 1.0);
-  std::vector<char> act(np, bb > 0);
-  double rho = bb, a_old = 1.0, b_old = 0.0;
-  int it = 0, nact = bb > 0 ? np : 0;
-  while (nact > 0 && it < 200000) {
-    if ((rc = ext_apply(e, QED3_OP_DDAGD, q, p, st)) || (rc = vec_axpby(nd, sb, p, 1.0, q, q, st))) return rc;
-    double pq = 0;
-    if ((rc = vec_zdot(nc, p, q, part, &pq, &im, st))) return rc;
-    const double alpha = rho / pq;
-    if ((rc = vec_axpby(nd, -alpha, q, 1.0, r, r, st))) return rc;
-    double rn = 0;
-    if ((rc = vec_zdot(nc, r, r, part, &rn, &im, st))) return rc;
-    it++;
-    if (!std::isfinite(rn)) return fail(QED3_ERR_NOCONV, "multi-shift CG: non-finite residual");
-    const double beta = rn / rho;
-    PoleCoef A{}, Zc{}, B{};
-    for (int m = 0; m < np; m++) {
-      if (!act[m]) {
-        B.c[m] = 1.0;
-        continue;
-      }
-      const double zz = zeta[m], zo = zold[m];
-      const double den = alpha * b_old * (zo - zz) + zo * a_old * (1.0 + (s[m] - sb) * alpha);
-      const double zn = zz * zo * a_old / den;
-      A.c[m] = alpha * zn / zz;
-      Zc.c[m] = zn;
-      B.c[m] = beta * (zn / zz) * (zn / zz);
-      zold[m] = zz;
-      zeta[m] = zn;
-    }
-    k_ms_update<<<nblk_o(nd), 256, 0, st>>>(nd, np, A, Zc, B, r, Z, P);
-    QED3_CUDA_TRY(cudaGetLastError());
-    if ((rc = vec_axpby(nd, 1.0, r, beta, p, p, st))) return rc;
-    nact = 0;
-    for (int m = 0; m < np; m++) {
-      if (!act[m]) continue;
-      if (zeta[m] * zeta[m] * rn < tol * tol * bb || !std::isfinite(zeta[m])) act[m] = 0;
-      else nact++;
-    }
-    a_old = alpha;
-    b_old = beta;
-    rho = rn;
+  MsState h{};
+  h.rho = bb;
+  h.a_old = 1.0;
+  h.b_old = 0.0;
+  h.done = bb > 0 ? 0.0 : 1.0;
+  h.thr = tol * tol * bb;
+  h.pq = np;
+  for (int m = 0; m < np; m++) {
+    h.zeta[m] = h.zold[m] = 1.0;
+    h.act[m] = 1.0;
   }
-  if (iters) *iters = it;
-  if (nact > 0) return fail(QED3_ERR_NOCONV, "multi-shift CG did not converge");
+  QED3_CUDA_TRY(cudaMemcpyAsync(S, &h, sizeof(h), cudaMemcpyHostToDevice, st));
+  QED3_CUDA_TRY(cudaMemcpyAsync(dsig, ds.data(), np * sizeof(double), cudaMemcpyHostToDevice, st));
+  const int gblk = int(std::min<long long>(kMsParts, (nc + 255) / 256));
+  auto iter = [&](cudaStream_t cs) -> int {
+    int c = ext_apply(e, QED3_OP_DDAGD, q, p, cs);
+    if (!c) c = vec_axpby(nd, sb, p, 1.0, q, q, cs);
+    if (c) return c;
+    k_ms_pq<<<gblk, 256, 0, cs>>>(nc, reinterpret_cast<const double2*>(p), reinterpret_cast<const double2*>(q), part, S);
+    k_ms_alpha<<<1, 256, 0, cs>>>(part, gblk, S);
+    k_ms_r<<<gblk, 256, 0, cs>>>(nc, reinterpret_cast<const double2*>(q), reinterpret_cast<double2*>(r), part, S);
+    k_ms_scalars<<<1, 128, 0, cs>>>(part, gblk, np, dsig, S);
+    k_ms_update_dev<<<nblk_o(nd), 256, 0, cs>>>(nd, np, r, Z, P, p, S);
+    k_ms_finish<<<1, 1, 0, cs>>>(S);
+    return QED3_OK;
+  };
+  const int chunk = 8;
+  IterGraph graph;
+  const bool use_graph = h.done == 0.0 && graph.build(chunk, iter);
+  int launched = 0;
+  while (h.done == 0.0 && launched < 200000) {
+    if (use_graph) {
+      QED3_CUDA_TRY(cudaGraphLaunch(graph.exec, st));
+    } else {
+      for (int k = 0; k < chunk; k++)
+        if ((rc = iter(st))) return rc;
+    }
+    QED3_CUDA_TRY(cudaGetLastError());
+    launched += chunk;
+    QED3_CUDA_TRY(cudaMemcpyAsync(&h, S, sizeof(h), cudaMemcpyDeviceToHost, st));
+    QED3_CUDA_TRY(cudaStreamSynchronize(st));
+  }
+  if (iters) *iters = int(h.iters);
+  if (h.done != 1.0) return fail(QED3_ERR_NOCONV, "multi-shift CG did not converge");
   return QED3_OK;
 }
 
