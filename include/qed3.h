@@ -415,8 +415,9 @@ int qed3_hmc_ext_overlap(qed3_overlap_ext* ov, qed3_rng* rng, double* A, double 
 /* ======================================================================
  * Overlap operator  --  replaces Overlap<WilsonDirac> (src/both_3d/overlap.h:137-390):
  * D_ov = 1 + X r(X^dag X), X = D_W / lambda_max, r = Zolotarev approximation of
- * (.)^{-1/2} of order zolo_order (n/2 poles).  All poles are solved in ONE
- * batched persistent launch (mixed precision, FP64 true residuals).
+ * (.)^{-1/2} of order zolo_order (n/2 poles).  All poles are solved by ONE
+ * FP64 multi-shift CG (one Krylov space; poles that stall just above the
+ * tolerance get a mixed-precision defect correction), FP64 true residuals.
  * ====================================================================== */
 int qed3_overlap_create(qed3_dirac* dw, int zolo_order, int precision, qed3_overlap** out);
 int qed3_overlap_destroy(qed3_overlap* ov);
@@ -426,8 +427,9 @@ int qed3_overlap_destroy(qed3_overlap* ov);
  * (inner CG tolerance tol_outer). */
 int qed3_overlap_update(qed3_overlap* ov, double lambda_min, double lambda_max, double tol_outer, void* stream);
 /* npoles_fp64: leading (smallest-shift) poles whose condition number is too
- * large for mixed-precision inner iterations; they run in a second, FP64,
- * batched launch (0 when the overlap was created with QED3_PREC_F64). */
+ * large for mixed-precision inner iterations (they would need FP64 in the
+ * batched alternative to the multi-shift solve; 0 when the overlap was
+ * created with QED3_PREC_F64). */
 int qed3_overlap_info(const qed3_overlap* ov, double* lambda_min, double* lambda_max, double* k, double* delta,
                       int* npoles, int* npoles_fp64);
 /* mult / adj / DHD / DDH_deviceAsyncLaunch (:309-390): op = QED3_OP_D (D_ov),
@@ -443,8 +445,8 @@ int qed3_overlap_apply(qed3_overlap* ov, int op, double* out, const double* in, 
  * Overlap::precalc_grad_deviceAsyncLaunch + grad_deviceAsyncLaunch
  * (src/both_3d/overlap.h:393-470, one sparse product and dot per pole and
  * link): F[l] = -2 d/dA_l Re<eta, D_ov eta>.  eta: device complex128,
- * reference order; F: device [n_links].  report: the worse of the two batched
- * pole launches. */
+ * reference order; F: device [n_links].  report: the worse of the two
+ * multi-shift pole solves. */
 int qed3_overlap_force(qed3_overlap* ov, const double* eta, double* F, double tol_inner, qed3_solve_report* report,
                        void* stream);
 /* Outer CG on D_ov^dag D_ov (Overlap::DHD) x = b, as MatPoly::solve over the

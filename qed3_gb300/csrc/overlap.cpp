@@ -2,12 +2,13 @@
 // Zolotarev approximation of (.)^{-1/2} (the sign function of gamma5 X).
 //
 // Replaces Overlap (src/both_3d/overlap.h:137-390).  The reference solves one
-// CG per pole on OpenMP threads and CUDA streams (:309-332); here all poles
-// are ONE batched persistent launch of shifted CGs (batched.cu) that share
-// every stencil read: the right-hand side is broadcast to the npoles systems
-// (D^dag D + lambda_max^2 sigma_m) z_m = xi, sigma_m = -k^2/cp_m > 0, in
-// mixed precision with FP64 reliable updates and an FP64 true-residual
-// certificate per pole.  Then
+// CG per pole on OpenMP threads and CUDA streams (:309-332); here the npoles
+// systems (D^dag D + lambda_max^2 sigma_m) z_m = xi, sigma_m = -k^2/cp_m > 0,
+// are ONE FP64 multi-shift CG (mshift.cu: one Krylov space, one stencil pass
+// per iteration for all poles) with an FP64 true-residual certificate per
+// pole; the alternative, one batched persistent launch of shifted mixed-
+// precision CGs with the right-hand side broadcast (batched.cu), is kept for
+// comparison.  Then
 //   D_ov xi     = xi + (C/lambda_max) D (xi + sum_m A_m lambda_max^2 z_m)
 //   D_ov^dag xi = xi + C (y0 + sum_m A_m lambda_max^2 y_m),  y0 = D^dag xi / lambda_max
 // lambda_min/max come from the reference's procedure (power iteration on
