@@ -377,3 +377,25 @@ def test_hmc_ext_overlap_matches_oracle(cuda):
         assert abs(dH_d - dH_o) < 1e-7 * (1 + abs(dH_o)), (t, dH_d, dH_o)
         torch.cuda.synchronize()
         assert np.abs(from_dev(Ad) - Ao).max() < 1e-8
+
+
+@pytest.mark.parametrize("prec", ["f64", "f32"])
+def test_ext_cg_edge_cases(cuda, prec):
+    """maxiter reached: status NOCONV with exactly maxiter iterations (the
+    device counter, graph chunks or not); b = 0: x = 0 at once."""
+    import torch
+    lat = Q.S2Trivalent(4)
+    Nt = 3
+    De = Q.DiracExt(lat, 1.0, 0.1, Nt, 0.6)
+    rng = np.random.default_rng(84)
+    De.update(to_dev(rng.uniform(-np.pi, np.pi, Nt * (lat.n_links + lat.n_sites)), cuda))
+    p = Q.PREC_F64 if prec == "f64" else Q.PREC_F32
+    b = to_dev(rng.normal(size=2 * lat.n_sites * Nt) + 1j * rng.normal(size=2 * lat.n_sites * Nt), cuda)
+    x = torch.zeros_like(b)
+    for maxiter in (5, 21):
+        r = De.solve(x, b, tol=1e-14, maxiter=maxiter, precision=p)
+        assert r.status == Q.ERR_NOCONV and r.iters == maxiter, (maxiter, r)
+        assert 0 < r.true_rel_res < 1
+    z = torch.zeros_like(b)
+    r = De.solve(x, z, tol=1e-10, precision=p)
+    assert r.status == Q.OK and r.iters == 0 and float(x.abs().max()) == 0.0
