@@ -26,7 +26,17 @@ persistent launch per batch, beside the same 256 solves run one after another.
 
 --impl reference times the reference's algorithm on the host cores: the
 oracle's restatement of MatPoly::solve (src/dual/matpoly.h:204-267) over the
-reference CSR operator, OpenMP over rows on every host core.
+reference CSR operator, OpenMP over rows on every host core.  That arm builds
+its workload with the oracle alone (the same seeded recipe: uniform links,
+50 pure-gauge HMC trajectories, Gaussian source); it loads nothing of this
+project's library.
+
+Baseline legs of our arm (outside the timed region, like `cpu_baseline`):
+`ref_gpu_baseline` runs the reference's GPU CG design on the same GPU -- one
+thread per CSR row, separate axpy kernels, cuBLAS dot products read back by
+the host, allocations per operator call (oracle/ref_gpu_cg.cu, restated from
+src/both_3d/gpu_header.h:102-130 and src/both_3d/matpoly.h:62-267) -- over
+the reference's CSR operator of the same configuration.
 """
 import argparse
 import json
@@ -52,6 +62,12 @@ PCG_DRAM_BYTES_PER_LAUNCH = 53.06e6
 METRIC = "D†D solves/s to 1e-10 at n=64: learned-PC mixed vs plain FP64 CG; apply GB/s"
 WORKLOAD = ("n=64 dual lattice (81,920 sites), r=1, M5=0.05, links U[-pi,pi) seed 2 + 50 HMC traj beta=1.4, "
             "Gaussian source seed 7, CG on D^dag D to 1e-10 FP64 true residual")
+
+
+def config(world):
+    """The workload description both arms print (identical dicts)."""
+    return {"workload": WORKLOAD, "l2": "flushed between timed steps (the n=64 working set is L2-resident)",
+            "parallelism": "replicas" if world > 1 else "single GPU"}
 
 
 def env_rank():
@@ -108,6 +124,17 @@ def make_workload(torch, dev):
     D.update(A)
     b = Q.ParallelRng(lat, 7).gaussian_spinor()
     return Q, lat, A, D, b, acc
+
+
+def make_workload_oracle():
+    """The same seeded configuration built by the oracle alone (its pure-gauge
+    HMC and random streams are the product's, pinned to the reference's own
+    HMCPureGauge and ParallelRng2): no part of this project's library loads."""
+    from oracle import oracle as O
+    g = O.geometry(N_REFINE)
+    A, acc = O.thermalized_links(g, BETA, 2, 50, init="uniform")
+    b = O.Rng(g, 7).gaussian_spinor()
+    return g, A, b, acc / 50
 
 
 def train_preconditioner(torch, Q, lat, D, dev, n_cfg=40, n_src=10, steps=1500):
@@ -215,10 +242,10 @@ def apply_bandwidth(torch, Q, n, prec, reps=50):
             "bytes_per_site": per_site}
 
 
-def cpu_reference_solve(b, A, threads=None):
+def cpu_reference_solve(b, A, g=None):
     """The reference's algorithm on the host cores (oracle restatement)."""
     from oracle import oracle as O
-    g = O.geometry(N_REFINE)
+    g = g or O.geometry(N_REFINE)
     D = O.Dirac(g, 1.0, M5)
     D.update(A)
     t = time.perf_counter()
@@ -450,6 +477,48 @@ def batched_throughput(torch, Q, dev, reps=3):
             "speedup_vs_sequential": (256e3 / ms) / (256 / seq_s)}
 
 
+def ref_gpu_baseline(A, b, reps=3):
+    """The reference's GPU CG design on this GPU (oracle/ref_gpu_cg.cu) over
+    the reference CSR operator of the workload; host-vector solves as the
+    reference's MatPoly::solve makes them (b copied in, x copied out)."""
+    import ctypes
+    from oracle import oracle as O
+    g = O.geometry(N_REFINE)
+    D = O.Dirac(g, 1.0, M5)
+    D.update(A)
+    rows, cols, val = D.csr()
+    rowsT, colsT, valH = D.csr(dagger=True)
+    L = ctypes.CDLL(os.path.join(ROOT, "oracle", "_build", "librefgpu.so"))
+    p = lambda a: a.ctypes.data_as(ctypes.c_void_p)
+    x = np.zeros_like(b)
+    ms = np.zeros(reps)
+    it = L.refgpu_cg(ctypes.c_int(D.N), ctypes.c_int(cols.size), p(rows), p(cols), p(val), p(rowsT), p(colsT),
+                     p(valH), p(b), p(x), ctypes.c_double(TOL), ctypes.c_int(100000), ctypes.c_int(1),
+                     ctypes.c_int(reps), p(ms))
+    if it < 0:
+        return {"error": "refgpu_cg failed"}
+    res = float(np.linalg.norm(b - D.apply(x, 2)) / np.linalg.norm(b))
+    return {"ms": float(np.mean(ms)), "ms_min": float(np.min(ms)), "iters": int(it), "true_rel_res": res,
+            "solves_per_s": 1e3 / float(np.mean(ms)), "kind": "reference GPU algorithm restated",
+            "design": "CSR SpMV one thread per row + separate axpy kernels + cuBLAS Zdotc read back by the host "
+                      "+ cudaMalloc/cudaFree per operator call, FP64, sm_103a (oracle/ref_gpu_cg.cu)",
+            "timing": "host wall clock per host-vector solve (H2D of b and D2H of x inside)"}
+
+
+def count_launches(torch, fn):
+    """Kernel launches of one call of fn(), from the CUDA activity trace
+    (torch.profiler / CUPTI): (this library's kernels, all kernels)."""
+    from torch.profiler import ProfilerActivity, profile
+    torch.cuda.synchronize()
+    with profile(activities=[ProfilerActivity.CUDA]) as prof:
+        fn()
+        torch.cuda.synchronize()
+    names = [e.name for e in prof.events() if getattr(e, "device_type", None) is not None
+             and "CUDA" in str(e.device_type) and not e.name.startswith(("Memcpy", "Memset"))]
+    ours = [n for n in names if "qed3::" in n]
+    return len(ours), len(names)
+
+
 def profile_case(torch, which):
     """Small cases for ncu captures (a few hundred MB on the device)."""
     import qed3_gb300 as Q
@@ -547,11 +616,10 @@ def main():
     if args.impl == "reference":
         if rank != 0:
             return
-        Q, lat, A, D, b, acc = make_workload(torch, dev)
-        A_h = A.cpu().numpy()
+        g, A_h, b, acc = make_workload_oracle()
         times, its = [], []
         for i in range(warmup + args.steps):
-            dt, it, res, cores = cpu_reference_solve(b, A_h)
+            dt, it, res, cores = cpu_reference_solve(b, A_h, g)
             if i >= warmup:
                 times.append(dt)
                 its.append(it)
@@ -559,8 +627,9 @@ def main():
         line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "solves/s", "n_gpus": 0,
                 "steps": args.steps, "warmup": warmup, "ms_per_step": 1e3 * sum(times) / len(times),
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-                "data": "synthetic", "config": {"workload": WORKLOAD, "solver": "reference CG (MatPoly::solve) "
-                                                "restated over the reference CSR operator", "iters": int(np.median(its))},
+                "data": "synthetic", "config": config(1),
+                "solver": "reference CG (MatPoly::solve) restated over the reference CSR operator",
+                "iters": int(np.median(its)), "hmc_acceptance": acc,
                 "cpu_baseline": {"value": v, "unit": "solves/s", "cores": cores, "kind": "port",
                                  "sample": "full n=64 solves to 1e-10 on all host cores"},
                 "e2e": {"value": v, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -633,15 +702,16 @@ def main():
     paths = None if args.no_paths else paths_timings(torch, Q, dev, cpu=rank == 0 and not args.no_cpu_baseline)
 
     # ---- roofline of the dominant kernel ----------------------------------------------
-    # algorithmic bytes per site per iteration (fp32 / bf16 halo storage):
-    #   D^dag D = 2 x (2 S_psi + 3 (4 + 32) + 4) with S_psi the stored spinor size,
-    #   7 spinor streams of fp32 state (x, r, p, t, z read / written) = 112,
-    #   preconditioner N: 4 block-local hop passes of 3 (32 + 16) B = 576 (PCG only)
+    # algorithmic HBM bytes per site per iteration (the measurement rule: each array once):
+    #   D^dag D = 2 x (2 S_psi + 3 (4 + S_H) + S_diag) with S_psi the stored spinor size,
+    #   plus 7 spinor streams of the solver state (read x, r, p, q; write x, r, p).
+    # The learned preconditioner's neighbour passes run in shared memory on the
+    # block's own sites and add no HBM bytes.
     S = {"f64": 32, "f32": 16, "bf16": 8, "pcg_f32": 16, "pcg_bf16": 8}[best]
     if best == "f64":
         per_site_iter = 2 * (2 * 32 + 3 * (4 + 64) + 8) + 7 * 32
     else:
-        per_site_iter = 2 * (2 * S + 3 * (4 + 32) + 4) + 7 * 16 + (576 if use_pc else 0)
+        per_site_iter = 2 * (2 * S + 3 * (4 + 32) + 4) + 7 * 16
     iters = results[best]["iters"]
     alg_bytes = per_site_iter * lat.n_sites * iters
     achieved = alg_bytes / (results[best]["ms"] * 1e-3) / 1e9
@@ -654,6 +724,27 @@ def main():
         s_["frac_of_" + peak_kind] = s_["GB/s"] / peak
         s_["resident"] = "L2" if s_["bytes_per_site"] * 20 * n * n < 100e6 else "HBM"
         sweep.append(s_)
+    hbm_apply = next(s_ for s_ in sweep if s_["n"] == 512 and s_["prec"] == "f32")
+
+    # ---- launches of this library's kernels in the timed region ------------------------
+    def one_step():
+        if use_pc:
+            pc.solve(D, dx, db, tol=TOL, precision=prec_best)
+        else:
+            D.solve(dx, db, tol=TOL, precision=prec_best)
+    try:
+        ours1, all1 = count_launches(torch, one_step)
+        launches = {"per_step": ours1, "per_step_all_kernels": all1,
+                    "source": "CUDA activity trace (torch.profiler) of one extra step, times the timed steps"}
+    except Exception as e:  # the profiler is unavailable: the solve's launch sequence, counted by hand
+        ours1 = 4  # |b| partials, unit-norm import, solver, scaled export
+        launches = {"per_step": ours1, "source": f"launch sequence of the solve (trace unavailable: {e})"}
+    n_timed = args.steps  # the headline's timed steps (the e2e loop repeats them through host buffers)
+    ref_gpu = ref_gpu_baseline(A.cpu().numpy(), b) if rank == 0 and not args.no_cpu_baseline else None
+    if ref_gpu and "ms" in ref_gpu:
+        ref_gpu["learned_speedup"] = ref_gpu["ms"] / results[best]["ms"]
+        ref_gpu["learned_e2e_speedup"] = ref_gpu["ms"] / float(np.mean(e2e_ms))
+        ref_gpu["plain_f64_speedup"] = ref_gpu["ms"] / results["f64"]["ms"]
     kernel = "k_pcg" if use_pc else ("k_cg_v2")
     dtype = {"f64": "f64", "f32": "f32", "bf16": "f32 (bf16 halo copies)", "pcg_f32": "f32",
              "pcg_bf16": "f32 (bf16 halo copies)"}[best]
@@ -661,26 +752,31 @@ def main():
     line = {"metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps,
             "warmup": warmup, "ms_per_step": ms_best, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": dtype, "data": "synthetic",
-            "config": {"workload": WORKLOAD,
-                       "solver": (f"learned-preconditioned persistent CG, {best[4:]} inner, FP64 reliable updates"
-                                  if use_pc else f"persistent CG, {best} inner, FP64 reliable updates"),
-                       "l2": "flushed between timed steps (n=64 working set is L2-resident)",
-                       "hmc_acceptance": acc, "parallelism": "replicas" if world > 1 else "single GPU"},
+            "config": config(world),
+            "solver": (f"learned-preconditioned persistent CG, {best[4:]} inner, FP64 reliable updates"
+                       if use_pc else f"persistent CG, {best} inner, FP64 reliable updates"),
+            "hmc_acceptance": acc,
             "solvers": results,
             "speedup_vs_plain_f64": results["f64"]["ms"] / results[best]["ms"],
             "preconditioner": train_info,
             "heldout": heldout,
             "heldout_summary": heldout_summary(heldout),
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                         "traffic": PCG_DRAM_BYTES_PER_LAUNCH if use_pc else None, "kernel": kernel, "note": "n=64 is L2-resident and the persistent "
-                         "solver is grid-barrier latency bound; "
-                         f"{per_site_iter} B/site/iteration x {iters} iterations; the HBM-bound Dirac apply is "
-                         "in apply_sweep"},
+                         "traffic": PCG_DRAM_BYTES_PER_LAUNCH if use_pc else None, "kernel": kernel,
+                         "resident": "L2", "note": "L2-resident effective bandwidth: the n=64 working set stays "
+                         "in the 129 MB L2, so `traffic` (ncu DRAM bytes per launch) is far below the algorithmic "
+                         f"bytes; {per_site_iter} B/site/iteration (D^dag D + 7 solver-state streams) x "
+                         f"{lat.n_sites} sites x {iters} iterations per launch; the solver is grid-barrier "
+                         "latency bound",
+                         "hbm_apply": {"kernel": "k_apply32<F32>", "n": 512, "GB/s": hbm_apply["GB/s"],
+                                       "frac": hbm_apply["frac_of_" + peak_kind]}},
             "apply_sweep": sweep,
             "batched_256": batched,
             "paths": paths,
             "e2e": {"value": e2e, "unit": "solves/s", "h2d_bytes_per_step": b.nbytes, "d2h_bytes_per_step": b.nbytes},
-            "gpu_launches": args.steps * 4,  # |b| partials, unit-norm import, solver, scaled export
+            "gpu_launches": ours1 * n_timed,
+            "gpu_launches_detail": dict(launches, timed_steps=n_timed),
+            "ref_gpu_baseline": ref_gpu,
             "clocks": clocks_info}
     if rank == 0 and not args.no_cpu_baseline:
         dt, it, res, cores = cpu_reference_solve(b, A.cpu().numpy())

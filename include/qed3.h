@@ -198,10 +198,9 @@ int qed3_bicgstab_solve(qed3_dirac* d, int op, double* x, const double* b, const
                         double eps, qed3_solve_report* report, void* stream);
 
 /* Allocation-free CG solve.  No counterpart in the reference: it exists for
- * callers that cannot allocate device memory at solve time -- code inside
- * CUDA stream capture, hosts whose device memory is owned by another
- * allocator or pool, multi-stream drivers that must avoid cudaFree's
- * device-wide synchronisation.  Same algorithm, arguments and report as
+ * callers that cannot allocate device memory at solve time -- hosts whose
+ * device memory is owned by another allocator or pool, multi-stream drivers
+ * that must avoid cudaFree's device-wide synchronisation.  Same algorithm, arguments and report as
  * qed3_cg_solve, but its scratch is a static device array of the library
  * (about 6.6 MB, held by every GPU that loads the library until exit), so
  * lattices are limited to QED3_NOALLOC_MAX_SITES sites (n_refine <= 32);

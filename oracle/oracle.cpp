@@ -762,6 +762,11 @@ void orc_dirac_get_csr(const OracleDirac* d, int* rows, int* cols, double* val) 
   std::memcpy(cols, d->cols.data(), sizeof(Idx) * d->cols.size());
   std::memcpy(val, d->val.data(), sizeof(cplx) * d->val.size());
 }
+void orc_dirac_get_csr_dagger(const OracleDirac* d, int* rows, int* cols, double* val) {
+  std::memcpy(rows, d->rowsT.data(), sizeof(Idx) * d->rowsT.size());
+  std::memcpy(cols, d->colsT.data(), sizeof(Idx) * d->colsT.size());
+  std::memcpy(val, d->valH.data(), sizeof(cplx) * d->valH.size());
+}
 int orc_dirac_nnz(const OracleDirac* d) { return int(d->val.size()); }
 void orc_dirac_get_kappa(const OracleDirac* d, double* kappa) {
   std::memcpy(kappa, d->kappa.data(), sizeof(double) * d->kappa.size());

@@ -54,6 +54,7 @@ def lib():
         L.orc_dirac_nnz.restype = ctypes.c_int
         L.orc_dirac_nnz.argtypes = [vp]
         L.orc_dirac_get_csr.argtypes = [vp, c_int_p, c_int_p, ctypes.c_void_p]
+        L.orc_dirac_get_csr_dagger.argtypes = [vp, c_int_p, c_int_p, ctypes.c_void_p]
         L.orc_dirac_get_kappa.argtypes = [vp, c_double_p]
         L.orc_bicgstab.restype = ctypes.c_int
         L.orc_bicgstab.argtypes = [vp, ctypes.c_int, ctypes.c_double, ctypes.c_void_p, ctypes.c_void_p,
@@ -215,6 +216,16 @@ class Dirac:
             for jj in range(rows[i], rows[i + 1]):
                 M[i, cols[jj]] += val[jj]
         return M
+
+    def csr(self, dagger: bool = False):
+        """DWDevice's CSR arrays (rows, cols, complex values) of D, or of D^dagger."""
+        nnz = lib().orc_dirac_nnz(self.h)
+        rows = np.zeros(self.N + 1, np.int32)
+        cols = np.zeros(nnz, np.int32)
+        val = np.zeros(nnz, np.complex128)
+        f = lib().orc_dirac_get_csr_dagger if dagger else lib().orc_dirac_get_csr
+        f(self.h, rows.ctypes.data_as(c_int_p), cols.ctypes.data_as(c_int_p), _p(val))
+        return rows, cols, val
 
     def cg(self, b: np.ndarray, tol: float = 1e-10, maxiter: int = 100000, shift: float = 0.0):
         b = np.ascontiguousarray(b, dtype=np.complex128)

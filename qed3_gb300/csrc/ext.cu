@@ -583,9 +583,9 @@ static int ext_cg_mixed(qed3_dirac_ext_s* e, double* x, const double* b, double 
   double* q = r + 2 * nd;
   double* part = q + nd;
   float4 *rf = e->fwork, *pf = rf + n, *qf = pf + n, *tf = qf + n, *xf = tf + n;
-  cudaEvent_t e0, e1;
-  QED3_CUDA_TRY(cudaEventCreate(&e0));
-  QED3_CUDA_TRY(cudaEventCreate(&e1));
+  EventPair ev;
+  QED3_CUDA_TRY(ev.create());
+  cudaEvent_t e0 = ev.e0, e1 = ev.e1;
   QED3_CUDA_TRY(cudaEventRecord(e0, st));
   auto A64 = [&](double* o, const double* v) -> int {
     int c = ext_apply(e, op, o, v, st);
@@ -673,8 +673,6 @@ static int ext_cg_mixed(qed3_dirac_ext_s* e, double* x, const double* b, double 
   QED3_CUDA_TRY(cudaEventSynchronize(e1));
   float ms = 0;
   cudaEventElapsedTime(&ms, e0, e1);
-  cudaEventDestroy(e0);
-  cudaEventDestroy(e1);
   if (rep) {
     rep->status = status;
     rep->iters = its;
@@ -704,9 +702,9 @@ int ext_cg(qed3_dirac_ext_s* e, double* x, const double* b, const qed3_solve_par
   double* p = r + nd;
   double* q = p + nd;
   double* part = q + nd;
-  cudaEvent_t e0, e1;
-  QED3_CUDA_TRY(cudaEventCreate(&e0));
-  QED3_CUDA_TRY(cudaEventCreate(&e1));
+  EventPair ev;
+  QED3_CUDA_TRY(ev.create());
+  cudaEvent_t e0 = ev.e0, e1 = ev.e1;
   QED3_CUDA_TRY(cudaEventRecord(e0, st));
   auto As = [&](double* o, const double* v, cudaStream_t s) -> int {
     int c = ext_apply(e, op, o, v, s);
@@ -764,8 +762,6 @@ int ext_cg(qed3_dirac_ext_s* e, double* x, const double* b, const qed3_solve_par
   QED3_CUDA_TRY(cudaEventSynchronize(e1));
   float ms = 0;
   cudaEventElapsedTime(&ms, e0, e1);
-  cudaEventDestroy(e0);
-  cudaEventDestroy(e1);
   if (rep) {
     rep->status = status;
     rep->iters = it;

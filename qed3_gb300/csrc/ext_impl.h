@@ -37,6 +37,19 @@ namespace qed3 {
 // as a CUDA graph on a private stream and replayed on the caller's stream: one
 // launch per chunk instead of seven per iteration.  If the capture fails the
 // solver launches the kernels directly.
+// Two timing events destroyed on every exit path of the solve that owns them.
+struct EventPair {
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  ~EventPair() {
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+  }
+  cudaError_t create() {
+    cudaError_t e = cudaEventCreate(&e0);
+    return e != cudaSuccess ? e : cudaEventCreate(&e1);
+  }
+};
+
 struct IterGraph {
   cudaGraphExec_t exec = nullptr;
   ~IterGraph() {

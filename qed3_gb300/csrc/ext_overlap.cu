@@ -184,7 +184,8 @@ __global__ void k_ms_scalars(const double* __restrict__ part, int nparts, int ns
     S->rho = rn;
     S->iters += 1.0;
     if (!isfinite(rn)) S->done = 2.0;
-    // the step's updates below still run; `done` is read by the next iteration's kernels
+    // once done is set, k_ms_update_dev (next in stream order) and every later kernel of the
+    // iteration return at once, so the step's updates are skipped
     S->pq = nact;
   }
 }

@@ -1,9 +1,9 @@
 // CG solve that allocates nothing: qed3_cg_solve_noalloc.
 //
-// Some callers cannot allocate device memory at solve time: code running
-// inside CUDA stream capture (cudaMalloc is not a capturable operation), hosts
-// whose device memory is entirely owned by another allocator or pool (for
-// example a framework's caching allocator, or a fixed MPS memory limit), and
+// Some callers cannot allocate device memory at solve time: hosts whose device
+// memory is entirely owned by another allocator or pool (for example a
+// framework's caching allocator, or a fixed MPS memory limit), so a
+// cudaMalloc from this library would fail or steal from the pool, and
 // multi-stream drivers for which cudaFree's implicit device-wide
 // synchronisation would serialise every stream.  The regular qed3_cg_solve
 // allocates its workspace on first use; this entry point instead runs the
@@ -23,6 +23,9 @@
 //    (several streams, several threads) race on the array: serialise them.
 //  * No cudaMalloc, cudaFree, event creation or allocating library routine is
 //    called; the solve report's time is host wall-clock.
+//  * The call returns once the solve has finished: it reads the solve's
+//    scalars back from the device to pick the solution buffer and to fill the
+//    report.
 
 #include <chrono>
 #include <cmath>

@@ -438,6 +438,7 @@ int cg_launch_on_scratch(int prec, qed3_dirac_s* d, S64* b, S64* xhi, S64* xhi2,
     QED3_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cg_persistent<P32>, 256, 0));
   else
     QED3_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cg_persistent<PBF16>, 256, 0));
+  if (per_sm < 1) return fail(QED3_ERR_CUDA, "persistent CG kernel cannot be resident");
   long long grid = std::min<long long>((d->Ns + 255) / 256, (long long)per_sm * smc);
   grid = std::max<long long>(1, std::min<long long>(grid, max_blocks));
   CgArgs a{};

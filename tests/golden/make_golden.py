@@ -32,6 +32,18 @@ streams with one cut short, binsize 1 and 3, one stream).
 
 free_spectrum.json: the known answers of analysis/ev_dual.ipynb (cells 33-34),
 typed in from the notebook's output cells.
+
+dirac_ref.npz: the REFERENCE's own operator pipeline compiled in place by
+`make -C oracle ref` into oracle/_ref/libdirac_ref_n<n>_t<Nt>.so
+(oracle/ref_dirac.cu): S2Simp / S2Trivalent reading this project's lattice
+from .dat tables in the reference's layout (qed3_gb300.dats.write), the
+reference's spin-structure tables and check, DiracS2Dual kappa / gamma /
+Omega, DiracExt::coo_format, DWDevice's CSR assembly and the host SpMV
+`matmul`.  Per case (key prefix "n<n>_t<Nt>/"): the link angles A, the source
+v, D v, D^dag v, D^dag D v, D's CSR values (n=2 only), the CG iterates of
+MatPoly::solve's iteration (restated on the host over the reference's matmul)
+after the counts in `iters_at`, and the converged x at tol 1e-10 with its
+iteration count.
 """
 import ctypes
 import json
@@ -171,6 +183,65 @@ def analyze_corr_fixture():
                        files=files, runs=out), f, indent=1)
 
 
+# (n, Nt, r, M5, at, iterates recorded after these CG iteration counts, store D/D^dag outputs)
+DIRAC_CASES = [(2, 1, 1.0, 0.1, 1.0, (1, 2, 5, 20), True), (4, 1, 1.0, 0.05, 1.0, (1, 5, 20), True),
+               (8, 1, 1.0, 0.1, 1.0, (), False), (2, 2, 1.0, 0.1, 0.5, (1, 5, 20), True),
+               (4, 4, 1.0, -0.5, 0.5, (), False)]
+
+
+def dirac_fixture():
+    import sys
+    import tempfile
+    sys.path.insert(0, ROOT)
+    import qed3_gb300 as Q
+    from qed3_gb300 import dats
+    subprocess.check_call(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "ref"])
+    dp, ip = ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int)
+    out = {}
+    for n, Nt, r, M5, at, iters_at, full in DIRAC_CASES:
+        L = ctypes.CDLL(os.path.join(ROOT, "oracle", "_ref", f"libdirac_ref_n{n}_t{Nt}.so"))
+        lat = Q.S2Trivalent(n)
+        Ns, Nl = lat.n_sites, lat.n_links
+        N = 2 * Ns * Nt
+        rng = np.random.default_rng(1000 * n + Nt)
+        A = rng.uniform(-np.pi, np.pi, Nt * (Nl + Ns))
+        v = rng.normal(size=N) + 1j * rng.normal(size=N)
+        Dv, DHv, DHDv, xf = (np.zeros(N, np.complex128) for _ in range(4))
+        rows, cols = np.zeros(N + 1, np.int32), np.zeros(12 * N, np.int32)
+        val = np.zeros(12 * N, np.complex128)
+        kappa = np.zeros(Nl)
+        its = np.array(iters_at, np.int32)
+        x_at = np.zeros((max(1, len(its)), N), np.complex128)
+        with tempfile.TemporaryDirectory() as d:
+            dats.write(lat, d)
+            k = L.ref_dirac_run(d.encode(), ctypes.c_double(r), ctypes.c_double(M5), ctypes.c_double(at),
+                                A.ctypes.data_as(dp), v.ctypes.data_as(dp), Dv.ctypes.data_as(dp),
+                                DHv.ctypes.data_as(dp), DHDv.ctypes.data_as(dp), rows.ctypes.data_as(ip),
+                                cols.ctypes.data_as(ip), val.ctypes.data_as(dp), kappa.ctypes.data_as(dp),
+                                ctypes.c_double(1e-10), 100000, len(its), its.ctypes.data_as(ip),
+                                x_at.ctypes.data_as(dp), xf.ctypes.data_as(dp))
+        assert k > 0, (n, Nt, k)
+        key = f"n{n}_t{Nt}/"
+        out[key + "params"] = np.array([r, M5, at])
+        out[key + "A"] = A
+        out[key + "v"] = v
+        out[key + "DHDv"] = DHDv
+        out[key + "x_final"] = xf
+        out[key + "cg_iters"] = np.array([k], np.int32)
+        out[key + "kappa"] = kappa
+        if full:
+            out[key + "Dv"] = Dv
+            out[key + "DHv"] = DHv
+        if len(its):
+            out[key + "iters_at"] = its
+            out[key + "x_at"] = x_at
+        if n == 2 and Nt == 1:
+            out[key + "csr_rows"] = rows
+            out[key + "csr_cols"] = cols
+            out[key + "csr_val"] = val
+    np.savez_compressed(os.path.join(HERE, "dirac_ref.npz"), **out)
+
+
 if __name__ == "__main__":
     zolotarev_fixture()
     rng_fixture()
@@ -178,3 +249,4 @@ if __name__ == "__main__":
     rng_ckpoint_fixture()
     spectrum_fixture()
     analyze_corr_fixture()
+    dirac_fixture()

@@ -1,8 +1,8 @@
 """The allocation-free CG entry point, qed3_cg_solve_noalloc.
 
-It serves callers that cannot allocate device memory at solve time (stream
-capture, memory owned by another allocator, multi-stream drivers that must not
-trigger cudaFree's device-wide synchronisation).  Its scratch is a static
+It serves callers that cannot allocate device memory at solve time (memory
+owned by another allocator or pool, multi-stream drivers that must not trigger
+cudaFree's device-wide synchronisation).  Its scratch is a static
 device array of the library shared by every call, so this test calls it twice
 in a row through the C ABI -- the second call must not be disturbed by what
 the first left in the array -- and compares each result with the regular
@@ -64,3 +64,25 @@ def test_noalloc_rejects_oversized_lattice(cuda):
     rc, _ = _solve("qed3_cg_solve_noalloc", D, x, b, Q.PREC_F32)
     assert rc == Q.ERR_ARG
     assert b"at most 20480" in Q.lib().qed3_last_error_string()
+
+
+def test_noalloc_allocates_no_device_memory(cuda):
+    """A fresh operator handle that has never run the regular solve: after one
+    warm-up call (which looks up the scratch array's address), a second call
+    leaves the device's free memory unchanged."""
+    import torch
+    rng = np.random.default_rng(78)
+    lat = Q.S2Trivalent(16)
+    D = Q.DiracS2Dual(lat, 1.0, 0.1)
+    D.update(rng.uniform(-np.pi, np.pi, lat.n_links))
+    b = torch.from_numpy(rng.normal(size=2 * lat.n_sites) + 1j * rng.normal(size=2 * lat.n_sites)).to(cuda)
+    x = torch.zeros_like(b)
+    rc, r = _solve("qed3_cg_solve_noalloc", D, x, b, Q.PREC_F32)
+    assert rc == Q.OK and r.status == Q.OK
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    rc, r = _solve("qed3_cg_solve_noalloc", D, x, b, Q.PREC_F32)
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    assert rc == Q.OK and r.status == Q.OK and r.true_rel_res <= 1e-10
+    assert free1 == free0, (free0, free1)
