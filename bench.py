@@ -507,14 +507,22 @@ def ref_gpu_baseline(A, b, reps=3):
 
 def count_launches(torch, fn):
     """Kernel launches of one call of fn(), from the CUDA activity trace
-    (torch.profiler / CUPTI): (this library's kernels, all kernels)."""
+    (torch.profiler / CUPTI, read back from its chrome-trace export):
+    (this library's kernels, all kernels)."""
+    import tempfile
     from torch.profiler import ProfilerActivity, profile
     torch.cuda.synchronize()
-    with profile(activities=[ProfilerActivity.CUDA]) as prof:
+    with profile(activities=[ProfilerActivity.CPU, ProfilerActivity.CUDA]) as prof:
         fn()
         torch.cuda.synchronize()
-    names = [e.name for e in prof.events() if getattr(e, "device_type", None) is not None
-             and "CUDA" in str(e.device_type) and not e.name.startswith(("Memcpy", "Memset"))]
+    with tempfile.TemporaryDirectory() as d:
+        path = os.path.join(d, "trace.json")
+        prof.export_chrome_trace(path)
+        with open(path) as f:
+            events = json.load(f).get("traceEvents", [])
+    names = [e.get("name", "") for e in events if e.get("cat") == "kernel"]
+    if not names:
+        raise RuntimeError("the trace holds no kernel events")
     ours = [n for n in names if "qed3::" in n]
     return len(ours), len(names)
 

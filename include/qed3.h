@@ -455,6 +455,36 @@ int qed3_overlap_force(qed3_overlap* ov, const double* eta, double* F, double to
  * iteration count. */
 int qed3_overlap_solve(qed3_overlap* ov, double* x, const double* b, double tol, double tol_inner, int maxiter,
                        qed3_solve_report* report, void* stream);
+/* The same outer solve with options (no counterpart in the reference, whose
+ * outer CG is qed3_overlap_solve): QED3_OVSOLVE_CHIRAL solves the two
+ * chirality sectors one after the other -- D_ov + D_ov^dag commutes with
+ * gamma5 and is 2 P_c D_ov P_c on sector c, so each iteration needs one pole
+ * solve instead of two; QED3_OVSOLVE_RELAX loosens the pole solves'
+ * tolerance as the outer residual shrinks (tol_inner |b| / |r|, at most
+ * 1e-5).  Every solve is certified by ||b - (D_ov + D_ov^dag) x|| / ||b||
+ * recomputed with pole solves to tol_inner, and restarted on that residual
+ * when it is above tol. */
+#define QED3_OVSOLVE_CHIRAL 1
+#define QED3_OVSOLVE_RELAX 2
+int qed3_overlap_solve2(qed3_overlap* ov, double* x, const double* b, double tol, double tol_inner, int maxiter,
+                        int flags, qed3_solve_report* report, void* stream);
+/* Low-mode projection of the sign function (no counterpart in the reference,
+ * whose Overlap approximates sign(H) on the whole spectrum,
+ * src/both_3d/overlap.h:207-306): the nev eigenvectors h_i of
+ * H = gamma5 D_W / lambda_max nearest zero (Lanczos on D_W^dag D_W with full
+ * reorthogonalisation to residual tol x its largest eigenvalue, at most
+ * maxsteps steps, then Rayleigh-Ritz with H) are treated exactly,
+ * sign(H) = sum_i sign(mu_i) h_i h_i^dag + H r(H^2)(1 - P), and the
+ * Zolotarev range starts at the (nev+1)-th |mu| (times 1 - margin).  That
+ * removes the near-zero modes of H_W at M5 < 0 from every pole solve.  Needs
+ * qed3_overlap_update first (it keeps lambda_max); nev = 0 switches the
+ * projection off; a later qed3_overlap_update drops it.  While it is on,
+ * qed3_overlap_force refuses (the force is for the unprojected sign
+ * function). */
+int qed3_overlap_project_low_modes(qed3_overlap* ov, int nev, double tol, int maxsteps, double margin, void* stream);
+/* nev in use, max ||H h_i - mu_i h_i||, Lanczos steps, mu[nev] (host, may be NULL) */
+int qed3_overlap_low_modes_info(const qed3_overlap* ov, int* nev, double* max_residual, int* lanczos_steps,
+                                double* mu);
 
 /* Multi-shift CG: x[m] = (D^dag D + shifts[m])^{-1} b for m < nshifts (<= 64),
  * all shifts in one Krylov space (one D^dag D per iteration for all shifts),

@@ -36,6 +36,8 @@ SOLVE_STREAMING = 2
 SOLVE_BCAST_B = 4
 SOLVE_FLEXIBLE = 8
 SOLVE_PIPELINED = 16
+OVSOLVE_CHIRAL = 1
+OVSOLVE_RELAX = 2
 PREC_NAMES = {"f64": PREC_F64, "f32": PREC_F32, "bf16": PREC_BF16}
 BYTES_PER_SITE = {PREC_F64: 32, PREC_F32: 16, PREC_BF16: 8}
 
@@ -128,6 +130,11 @@ SIGNATURES = [
     ("qed3_overlap_force", ctypes.c_int, [vp, vp, vp, ctypes.c_double, ctypes.POINTER(SolveReport), vp]),
     ("qed3_overlap_solve", ctypes.c_int, [vp, vp, vp, ctypes.c_double, ctypes.c_double, ctypes.c_int,
                                           ctypes.POINTER(SolveReport), vp]),
+    ("qed3_overlap_solve2", ctypes.c_int, [vp, vp, vp, ctypes.c_double, ctypes.c_double, ctypes.c_int, ctypes.c_int,
+                                           ctypes.POINTER(SolveReport), vp]),
+    ("qed3_overlap_project_low_modes", ctypes.c_int, [vp, ctypes.c_int, ctypes.c_double, ctypes.c_int,
+                                                      ctypes.c_double, vp]),
+    ("qed3_overlap_low_modes_info", ctypes.c_int, [vp, c_int_p, c_double_p, c_int_p, vp]),
     ("qed3_multishift_solve", ctypes.c_int, [vp, ctypes.c_int, vp, vp, vp, ctypes.c_double, ctypes.c_int, vp,
                                              ctypes.POINTER(ctypes.c_float), vp]),
     ("qed3_dirac_ext_create", ctypes.c_int, [vp, ctypes.c_double, ctypes.c_double, ctypes.c_int, ctypes.c_double,
@@ -857,12 +864,35 @@ class Overlap:
         _check(lib().qed3_overlap_force(self._h, _ptr(eta), _ptr(F), tol_inner, ctypes.byref(r), _stream(stream)))
         return Report(r.status, r.iters, r.reliable_updates, r.true_rel_res, r.ms)
 
-    def solve(self, x, b, tol: float = 1e-10, tol_inner: float = 1e-12, maxiter: int = 10000, stream=None) -> Report:
-        """Outer CG on D_ov^dag D_ov x = b; true_rel_res recomputed after convergence."""
+    def solve(self, x, b, tol: float = 1e-10, tol_inner: float = 1e-12, maxiter: int = 10000, flags: int = 0,
+              stream=None) -> Report:
+        """Outer CG on D_ov^dag D_ov x = b; true_rel_res recomputed after convergence.
+        flags: OVSOLVE_CHIRAL (chirality sectors, one pole solve per
+        iteration), OVSOLVE_RELAX (pole tolerance loosened as |r| shrinks)."""
         r = SolveReport()
-        _check(lib().qed3_overlap_solve(self._h, _ptr(x), _ptr(b), tol, tol_inner, maxiter, ctypes.byref(r),
-                                        _stream(stream)))
+        if flags:
+            _check(lib().qed3_overlap_solve2(self._h, _ptr(x), _ptr(b), tol, tol_inner, maxiter, flags,
+                                             ctypes.byref(r), _stream(stream)))
+        else:
+            _check(lib().qed3_overlap_solve(self._h, _ptr(x), _ptr(b), tol, tol_inner, maxiter, ctypes.byref(r),
+                                            _stream(stream)))
         return Report(r.status, r.iters, r.reliable_updates, r.true_rel_res, r.ms)
+
+    def project_low_modes(self, nev: int, tol: float = 1e-13, maxsteps: int = 6000, margin: float = 1e-3,
+                          stream=None) -> dict:
+        """Treat the nev eigenmodes of gamma5 D_W nearest zero exactly in the sign
+        function; the Zolotarev range then starts above them (nev = 0: off)."""
+        _check(lib().qed3_overlap_project_low_modes(self._h, nev, tol, maxsteps, margin, _stream(stream)))
+        return self.low_modes_info()
+
+    def low_modes_info(self) -> dict:
+        n, res, steps = ctypes.c_int(), ctypes.c_double(), ctypes.c_int()
+        _check(lib().qed3_overlap_low_modes_info(self._h, ctypes.byref(n), ctypes.byref(res), ctypes.byref(steps),
+                                                 None))
+        mu = np.zeros(max(1, n.value))
+        _check(lib().qed3_overlap_low_modes_info(self._h, None, None, None, _ptr(mu)))
+        return dict(nev=n.value, max_residual=res.value, lanczos_steps=steps.value, mu=mu[:n.value],
+                    **self.info())
 
     def __del__(self):
         if getattr(self, "_h", None) and _lib is not None:

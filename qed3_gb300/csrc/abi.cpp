@@ -845,7 +845,34 @@ int qed3_overlap_solve(qed3_overlap* ov, double* x, const double* b, double tol,
   if (!ov || !x || !b) return fail(QED3_ERR_ARG, "NULL argument");
   if (x == b) return fail(QED3_ERR_ARG, "x must not alias b");
   return overlap_solve(ov, x, b, tol > 0 ? tol : 1e-10, tol_inner > 0 ? tol_inner : 1e-12,
-                       maxiter > 0 ? maxiter : 10000, report, (cudaStream_t)stream);
+                       maxiter > 0 ? maxiter : 10000, 0, report, (cudaStream_t)stream);
+  QED3_GUARD_END
+}
+
+int qed3_overlap_solve2(qed3_overlap* ov, double* x, const double* b, double tol, double tol_inner, int maxiter,
+                        int flags, qed3_solve_report* report, void* stream) {
+  QED3_GUARD_BEGIN
+  if (!ov || !x || !b) return fail(QED3_ERR_ARG, "NULL argument");
+  if (x == b) return fail(QED3_ERR_ARG, "x must not alias b");
+  if (flags & ~(QED3_OVSOLVE_CHIRAL | QED3_OVSOLVE_RELAX)) return fail(QED3_ERR_ARG, "unknown flags");
+  return overlap_solve(ov, x, b, tol > 0 ? tol : 1e-10, tol_inner > 0 ? tol_inner : 1e-12,
+                       maxiter > 0 ? maxiter : 10000, flags, report, (cudaStream_t)stream);
+  QED3_GUARD_END
+}
+
+int qed3_overlap_project_low_modes(qed3_overlap* ov, int nev, double tol, int maxsteps, double margin, void* stream) {
+  QED3_GUARD_BEGIN
+  if (!ov) return fail(QED3_ERR_ARG, "NULL argument");
+  return overlap_project_low_modes(ov, nev, tol > 0 ? tol : 1e-13, maxsteps > 0 ? maxsteps : 6000,
+                                   margin >= 0 ? margin : 1e-3, (cudaStream_t)stream);
+  QED3_GUARD_END
+}
+
+int qed3_overlap_low_modes_info(const qed3_overlap* ov, int* nev, double* max_residual, int* lanczos_steps,
+                                double* mu) {
+  QED3_GUARD_BEGIN
+  if (!ov) return fail(QED3_ERR_ARG, "NULL argument");
+  return overlap_low_modes_info(ov, nev, max_residual, lanczos_steps, mu);
   QED3_GUARD_END
 }
 

@@ -680,7 +680,7 @@ int hmc_overlap(qed3_lattice_s* lat, qed3_overlap_s* ov, qed3_rng_s* rng, double
   };
   fo.solve = [&](double* eta, const double* phi, int* its) {
     qed3_solve_report r{};
-    int e = overlap_solve(ov, eta, phi, tol, tol_inner, 100000, &r, st);
+    int e = overlap_solve(ov, eta, phi, tol, tol_inner, 100000, 0, &r, st);
     *its += r.iters;
     if (!e && r.status != QED3_OK) e = fail(QED3_ERR_NOCONV, "overlap pseudofermion solve did not converge");
     return e;

@@ -24,6 +24,7 @@
 #include "gauge_impl.h"
 #include "mshift_impl.h"
 #include "handles.h"
+#include "lowmodes_impl.h"
 #include "overlap_impl.h"
 #include "qed3_internal.h"
 
@@ -46,10 +47,19 @@ struct qed3_overlap_s {
   // force: second pole set and internal-order copies; outer solve: CG vectors
   double* Yp = nullptr;    // [npoles][2 Ns] complex
   double* fi = nullptr;    // [4 npoles + 2][Ns] internal-order two-spinors (4 doubles per site)
-  double *sr = nullptr, *sp = nullptr, *sq = nullptr;
+  double *sr = nullptr, *sp = nullptr, *sq = nullptr, *se = nullptr, *sb = nullptr;
   // multi-shift scratch (internal-order FP64 fields, [npoles][Ns] each)
   qed3::S64* msX = nullptr;
   qed3::S64* msP = nullptr;
+  // low-mode projection: nev eigenvectors h_i of H = gamma5 D / lambda_max
+  // (orthonormal, reference order), their eigenvalues mu_i, and the bounds
+  // before the projection
+  int nev = 0;
+  double* lm_h = nullptr;  // [nev][2 Ns] complex
+  double* lm_t = nullptr;  // [2][2 Ns] complex scratch
+  std::vector<double> lm_mu;
+  double lm_res = 0, lm_theta_next = 0, lmin_full = 0;
+  int lm_steps = 0;
 };
 
 namespace qed3 {
@@ -112,7 +122,8 @@ void overlap_destroy(qed3_overlap_s* ov) {
   if (!ov) return;
   if (ov->batch) batch_destroy(ov->batch);
   if (ov->batch_hi) batch_destroy(ov->batch_hi);
-  void* p[] = {ov->Z, ov->y, ov->w, ov->y0, ov->q, ov->part, ov->Yp, ov->fi, ov->sr, ov->sp, ov->sq, ov->msX, ov->msP};
+  void* p[] = {ov->Z,  ov->y,  ov->w,   ov->y0,  ov->q,   ov->part, ov->Yp,
+               ov->fi, ov->sr, ov->sp,  ov->sq,  ov->msX, ov->msP,  ov->lm_h, ov->lm_t, ov->se, ov->sb};
   for (void* x : p)
     if (x) cudaFree(x);
   delete ov;
@@ -179,13 +190,147 @@ int overlap_update(qed3_overlap_s* ov, double lmin, double lmax, double tol_oute
     lmax = std::sqrt((1.0 + 100 * TOL) * lam);
   }
   if (!(lmin < lmax)) return fail(QED3_ERR_ARG, "need 0 < lambda_min < lambda_max");
-  ov->lmin = lmin;
+  ov->lmin = ov->lmin_full = lmin;
   ov->lmax = lmax;
+  ov->nev = 0;  // new bounds (new links): a projection must be recomputed
   int rc = zolotarev_coeffs(lmin / lmax, ov->order, ov->z);
   if (rc) return rc;
   if ((rc = ov_split(ov))) return rc;
   ov->ready = true;
   return QED3_OK;
+}
+
+// Low-mode projection of the sign function.  With h_i the nev eigenvectors
+// of H = gamma5 D / lambda_max nearest zero (eigenvalues mu_i):
+//   sign(H) = sum_i sign(mu_i) h_i h_i^dag + H r(H^2) (1 - P),  P = sum_i h_i h_i^dag,
+// so D_ov = 1 + gamma5 sign(H) becomes
+//   D_ov xi     = xi + gamma5 sum_i s_i h_i <h_i, xi> + X r(X^dag X) (1 - P) xi
+//   D_ov^dag xi = xi + sum_i s_i h_i <h_i, gamma5 xi> + r(X^dag X) (1 - P) X^dag xi
+// (P commutes with X^dag X = H^2), and the Zolotarev range starts at the
+// (nev+1)-th |mu| instead of the lowest.  The h_i come from Lanczos on D^dag D
+// (lowmodes.cu) followed by Rayleigh-Ritz with H in their span.  The
+// reference's Overlap has no projection (src/both_3d/overlap.h:207-306); it
+// is an addition for the near-zero modes of H_W at M5 < 0.
+int overlap_project_low_modes(qed3_overlap_s* ov, int nev, double tol, int maxsteps, double margin,
+                              cudaStream_t st) {
+  if (!ov->ready) return fail(QED3_ERR_STATE, "call qed3_overlap_update first: the projection keeps lambda_max");
+  if (nev < 0 || nev > kMaxLowModes) return fail(QED3_ERR_ARG, "low modes: nev must be in [0, 256]");
+  qed3_dirac_s* d = ov->d;
+  const long long nd = 4LL * d->Ns, nc = nd / 2;
+  if (ov->lm_h) cudaFree(ov->lm_h);
+  ov->lm_h = nullptr;
+  ov->nev = 0;
+  ov->lm_mu.clear();
+  ov->lm_res = ov->lm_theta_next = 0;
+  ov->lm_steps = 0;
+  int rc;
+  if (nev == 0) {
+    ov->lmin = ov->lmin_full;
+    if ((rc = zolotarev_coeffs(ov->lmin / ov->lmax, ov->order, ov->z))) return rc;
+    return ov_split(ov);
+  }
+  if (!ov->lm_t) QED3_CUDA_TRY(cudaMalloc(&ov->lm_t, 2 * size_t(nd) * sizeof(double)));
+  double* Y = nullptr;
+  std::vector<double> th;
+  double thn = 0, thmax = 0, res = 0;
+  int steps = 0;
+  rc = lanczos_lowmodes(
+      nd, [&](double* o, const double* v) { return dirac_apply_ref(d, QED3_OP_DDAGD, o, v, st); }, nev, tol,
+      maxsteps, &Y, th, &thn, &thmax, &res, &steps, st);
+  if (rc) return rc;
+  auto body = [&]() -> int {
+    // Rayleigh-Ritz with H = gamma5 D / lmax in span{y_i}
+    double* t = ov->lm_t;
+    std::vector<double> G(2 * size_t(nev) * nev);
+    int e;
+    for (int j = 0; j < nev; j++) {
+      if ((e = dirac_apply_ref(d, QED3_OP_D, t, Y + size_t(j) * nd, st)) || (e = chiral(nd, 0, t, t, st))) return e;
+      for (int i = 0; i < nev; i++) {
+        double re = 0, im = 0;
+        if ((e = vec_zdot(nc, Y + size_t(i) * nd, t, ov->part, &re, &im, st))) return e;
+        G[2 * (size_t(i) * nev + j)] = re / ov->lmax;
+        G[2 * (size_t(i) * nev + j) + 1] = im / ov->lmax;
+      }
+    }
+    for (int i = 0; i < nev; i++)  // hermitian part (rounding)
+      for (int j = i; j < nev; j++) {
+        const double re = 0.5 * (G[2 * (size_t(i) * nev + j)] + G[2 * (size_t(j) * nev + i)]);
+        const double im = 0.5 * (G[2 * (size_t(i) * nev + j) + 1] - G[2 * (size_t(j) * nev + i) + 1]);
+        G[2 * (size_t(i) * nev + j)] = G[2 * (size_t(j) * nev + i)] = re;
+        G[2 * (size_t(i) * nev + j) + 1] = im;
+        G[2 * (size_t(j) * nev + i) + 1] = -im;
+      }
+    std::vector<double> mu, U;
+    hermitian_eig(nev, G, mu, U);
+    if (int(mu.size()) != nev) return fail(QED3_ERR_NOCONV, "low modes: Rayleigh-Ritz lost a vector");
+    if ((e = modes_rotate(nd, nev, Y, U, st))) return e;
+    double worst = 0;  // ||H h_i - mu_i h_i||
+    for (int i = 0; i < nev; i++) {
+      const double* h = Y + size_t(i) * nd;
+      double r2 = 0, im = 0;
+      if ((e = dirac_apply_ref(d, QED3_OP_D, t, h, st)) || (e = chiral(nd, 0, t, t, st)) ||
+          (e = vec_axpby(nd, 1.0 / ov->lmax, t, -mu[i], h, t, st)) ||
+          (e = vec_zdot(nc, t, t, ov->part, &r2, &im, st)))
+        return e;
+      worst = std::max(worst, std::sqrt(std::max(r2, 0.0)));
+    }
+    const double knew = std::sqrt(thn) * (1.0 - margin) / ov->lmax;
+    if (!(knew > 0 && knew < 1)) return fail(QED3_ERR_NOCONV, "low modes: no spectral gap above the projected modes");
+    ov->lmin = knew * ov->lmax;
+    if ((e = zolotarev_coeffs(knew, ov->order, ov->z))) return e;
+    if ((e = ov_split(ov))) return e;
+    ov->lm_h = Y;
+    Y = nullptr;
+    ov->nev = nev;
+    ov->lm_mu = mu;
+    ov->lm_res = worst;
+    ov->lm_theta_next = thn;
+    ov->lm_steps = steps;
+    return QED3_OK;
+  };
+  rc = body();
+  if (Y) cudaFree(Y);
+  if (rc) {  // back to the unprojected operator
+    ov->lmin = ov->lmin_full;
+    zolotarev_coeffs(ov->lmin / ov->lmax, ov->order, ov->z);
+    ov_split(ov);
+  }
+  return rc;
+}
+
+// The projected-mode part of D_ov (adj = 0) or D_ov^dag (adj = 1) added to out:
+//   adj = 0: out += gamma5 sum_i s_i h_i <h_i, xi>;  adj = 1: out += sum_i s_i h_i <h_i, gamma5 xi>.
+static int lowmode_part(qed3_overlap_s* ov, int adj, const double* xi, double* out, cudaStream_t st) {
+  const long long nd = 4LL * ov->d->Ns;
+  double* t = ov->lm_t;
+  int e;
+  const double* src = xi;
+  if (adj) {
+    if ((e = chiral(nd, 0, xi, t, st))) return e;
+    src = t;
+  }
+  std::vector<double> c;
+  if ((e = modes_coeffs(nd, ov->nev, ov->lm_h, src, ov->part, c, st))) return e;
+  for (int i = 0; i < ov->nev; i++) {
+    const double sg = ov->lm_mu[i] >= 0 ? 1.0 : -1.0;
+    c[2 * i] *= sg;
+    c[2 * i + 1] *= sg;
+  }
+  double* u = ov->lm_t + nd;
+  QED3_CUDA_TRY(cudaMemsetAsync(u, 0, nd * sizeof(double), st));
+  if ((e = modes_axpy(nd, ov->nev, ov->lm_h, c, u, u, st))) return e;
+  if (!adj && (e = chiral(nd, 0, u, u, st))) return e;
+  return vec_axpby(nd, 1.0, u, 1.0, out, out, st);
+}
+
+// v <- (1 - P) v
+static int lowmode_deflate(qed3_overlap_s* ov, double* v, cudaStream_t st) {
+  const long long nd = 4LL * ov->d->Ns;
+  std::vector<double> c;
+  int e = modes_coeffs(nd, ov->nev, ov->lm_h, v, ov->part, c, st);
+  if (e) return e;
+  for (auto& x : c) x = -x;
+  return modes_axpy(nd, ov->nev, ov->lm_h, c, v, v, st);
 }
 
 // All poles with one right-hand side: out_m = (D^dag D + lmax^2 sigma_m)^{-1} rhs,
@@ -256,14 +401,22 @@ int overlap_apply(qed3_overlap_s* ov, int op, double* out, const double* in, dou
   qed3_solve_report r1{}, r2{};
   const bool mult = (op == QED3_OP_D || op == QED3_OP_DDAGD || op == QED3_OP_DDDAG);
   const bool adj = (op == QED3_OP_DDAG || op == QED3_OP_DDAGD || op == QED3_OP_DDDAG);
+  const bool proj = ov->nev > 0;
   if (mult) {
-    if ((rc = pole_solves(ov, in, ov->Z, tol, &r1, st))) return rc;
-    if ((rc = vec_pole_sum(nd, np, coef.data(), ov->Z, in, ov->y, st))) return rc;  // y = xi + sum A l2 z
-    if ((rc = dirac_apply_ref(d, QED3_OP_D, ov->w, ov->y, st))) return rc;          // w = D y
+    const double* src = in;
+    if (proj) {  // the rational part acts on (1 - P) xi
+      QED3_CUDA_TRY(cudaMemcpyAsync(ov->q, in, nd * sizeof(double), cudaMemcpyDeviceToDevice, st));
+      if ((rc = lowmode_deflate(ov, ov->q, st))) return rc;
+      src = ov->q;
+    }
+    if ((rc = pole_solves(ov, src, ov->Z, tol, &r1, st))) return rc;
+    if ((rc = vec_pole_sum(nd, np, coef.data(), ov->Z, src, ov->y, st))) return rc;  // y = xi + sum A l2 z
+    if ((rc = dirac_apply_ref(d, QED3_OP_D, ov->w, ov->y, st))) return rc;           // w = D y
   }
   if (adj) {
     if ((rc = dirac_apply_ref(d, QED3_OP_DDAG, ov->y0, in, st))) return rc;
     if ((rc = vec_axpby(nd, 1.0 / ov->lmax, ov->y0, 0.0, ov->y0, ov->y0, st))) return rc;  // y0 = D^dag xi / lmax
+    if (proj && (rc = lowmode_deflate(ov, ov->y0, st))) return rc;
     if ((rc = pole_solves(ov, ov->y0, ov->Z, tol, &r2, st))) return rc;
     if ((rc = vec_pole_sum(nd, np, coef.data(), ov->Z, ov->y0, ov->y, st))) return rc;  // y = y0 + sum A l2 y_m
   }
@@ -275,6 +428,10 @@ int overlap_apply(qed3_overlap_s* ov, int op, double* out, const double* in, dou
     if ((rc = vec_axpby(nd, C / ov->lmax, ov->w, 1.0, in, out, st))) return rc;
   } else {
     if ((rc = vec_axpby(nd, C, ov->y, 1.0, in, out, st))) return rc;
+  }
+  if (proj) {
+    if (mult && (rc = lowmode_part(ov, 0, in, out, st))) return rc;
+    if (adj && (rc = lowmode_part(ov, 1, in, out, st))) return rc;
   }
   if (rep) {
     qed3_solve_report w = mult ? r1 : r2;
@@ -298,6 +455,9 @@ int overlap_apply(qed3_overlap_s* ov, int op, double* out, const double* in, dou
 int overlap_force(qed3_overlap_s* ov, const double* eta, double* F, double tol, qed3_solve_report* rep,
                   cudaStream_t st) {
   if (!ov->ready) return fail(QED3_ERR_STATE, "call qed3_overlap_update first");
+  if (ov->nev > 0)
+    return fail(QED3_ERR_STATE, "the overlap force is for the unprojected sign function: switch the low-mode "
+                                "projection off (nev = 0) first");
   qed3_dirac_s* d = ov->d;
   const int Ns = d->Ns;
   const long long nd = 4LL * Ns;
@@ -345,64 +505,124 @@ int overlap_force(qed3_overlap_s* ov, const double* eta, double* F, double tol, 
 
 // Outer CG on D_ov^dag D_ov (= D_ov + D_ov^dag for the overlap; Overlap::DHD,
 // src/both_3d/overlap.h:363-375) as the reference's MatPoly::solve over a
-// LinOpWrapper of DHD (src/both_3d/prop_nontriv.cu:242-260); every product is
-// one pair of batched pole launches.  The report's true_rel_res is
-// ||b - D_ov^dag D_ov x|| / ||b|| recomputed after convergence.
+// LinOpWrapper of DHD (src/both_3d/prop_nontriv.cu:242-260): x0 = 0, stop on
+// the recursive residual; every product is one or two multi-shift pole
+// solves.  Options (flags):
+//  * QED3_OVSOLVE_CHIRAL: D_ov + D_ov^dag = 2 + gamma5 eps + eps gamma5
+//    (eps = gamma5 (D_ov - 1)) commutes with gamma5 for any hermitian eps,
+//    and on the chirality-c sector it is 2 P_c D_ov P_c -- one pole solve per
+//    iteration instead of two; the sectors are solved one after the other.
+//  * QED3_OVSOLVE_RELAX: the pole solves' tolerance grows as the outer
+//    residual shrinks, tol_k = tol_inner |b| / |r_k| (at most 1e-5)
+//    (inexact Krylov: later directions need less accuracy).
+// After convergence the true residual ||b - D_ov^dag D_ov x|| is recomputed
+// with pole solves to tol_inner; above tol, the CG restarts on that residual
+// (at most 4 restarts).  The report: total outer iterations, the certificate,
+// reliable_updates = the largest pole iteration count of any product.
 int overlap_solve(qed3_overlap_s* ov, double* x, const double* b, double tol, double tol_inner, int maxiter,
-                  qed3_solve_report* rep, cudaStream_t st) {
+                  int flags, qed3_solve_report* rep, cudaStream_t st) {
   if (!ov->ready) return fail(QED3_ERR_STATE, "call qed3_overlap_update first");
   const long long nd = 4LL * ov->d->Ns, nc = nd / 2;
   if (!ov->sr) {
     QED3_CUDA_TRY(cudaMalloc(&ov->sr, nd * sizeof(double)));
     QED3_CUDA_TRY(cudaMalloc(&ov->sp, nd * sizeof(double)));
     QED3_CUDA_TRY(cudaMalloc(&ov->sq, nd * sizeof(double)));
+    QED3_CUDA_TRY(cudaMalloc(&ov->se, nd * sizeof(double)));
+    QED3_CUDA_TRY(cudaMalloc(&ov->sb, nd * sizeof(double)));
   }
+  const bool chiral_split = (flags & QED3_OVSOLVE_CHIRAL) != 0;
+  const bool relax = (flags & QED3_OVSOLVE_RELAX) != 0;
   cudaEvent_t e0, e1;
   QED3_CUDA_TRY(cudaEventCreate(&e0));
   QED3_CUDA_TRY(cudaEventCreate(&e1));
+  struct Ev {
+    cudaEvent_t a, b;
+    ~Ev() {
+      cudaEventDestroy(a);
+      cudaEventDestroy(b);
+    }
+  } ev{e0, e1};
   QED3_CUDA_TRY(cudaEventRecord(e0, st));
-  int rc;
+  int rc, inner_max = 0, it = 0;
   double bb = 0;
   if ((rc = vec_zdot(nc, b, b, ov->part, &bb, nullptr, st))) return rc;
   QED3_CUDA_TRY(cudaMemsetAsync(x, 0, nd * sizeof(double), st));
-  QED3_CUDA_TRY(cudaMemcpyAsync(ov->sr, b, nd * sizeof(double), cudaMemcpyDeviceToDevice, st));
-  QED3_CUDA_TRY(cudaMemcpyAsync(ov->sp, b, nd * sizeof(double), cudaMemcpyDeviceToDevice, st));
-  double rr = bb;
-  int it = 0, status = QED3_ERR_NOCONV, inner_max = 0;
-  if (bb == 0.0) status = QED3_OK;
-  while (status != QED3_OK && it < maxiter) {
+  // the operator of sector c (0: the full D_ov + D_ov^dag)
+  auto apply = [&](int c, double* out, const double* v, double tin) -> int {
     qed3_solve_report ir{};
-    if ((rc = overlap_apply(ov, QED3_OP_DDAGD, ov->sq, ov->sp, tol_inner, &ir, st))) return rc;
-    inner_max = std::max(inner_max, ir.iters);
-    double pq = 0;
-    if ((rc = vec_zdot(nc, ov->sp, ov->sq, ov->part, &pq, nullptr, st))) return rc;
-    const double al = rr / pq;
-    if ((rc = vec_axpby(nd, al, ov->sp, 1.0, x, x, st))) return rc;
-    if ((rc = vec_axpby(nd, -al, ov->sq, 1.0, ov->sr, ov->sr, st))) return rc;
-    double rn = 0;
-    if ((rc = vec_zdot(nc, ov->sr, ov->sr, ov->part, &rn, nullptr, st))) return rc;
-    it++;
-    if (!(std::isfinite(rn) && std::isfinite(al))) break;
-    if (rn < tol * tol * bb) {
-      status = QED3_OK;
-      break;
+    int e;
+    if (c == 0) {
+      e = overlap_apply(ov, QED3_OP_DDAGD, out, v, tin, &ir, st);
+    } else {
+      e = overlap_apply(ov, QED3_OP_D, out, v, tin, &ir, st);
+      if (!e) e = chiral(nd, c, out, out, st);
+      if (!e) e = vec_axpby(nd, 2.0, out, 0.0, out, out, st);
     }
-    if ((rc = vec_axpby(nd, 1.0, ov->sr, rn / rr, ov->sp, ov->sp, st))) return rc;
-    rr = rn;
-  }
-  // certificate: r = b - A x with the same operator
+    inner_max = std::max(inner_max, ir.iters);
+    return e;
+  };
+  // CG from zero on A_c e = rhs (ov->sb), e in ov->se, to |r| <= trel |rhs|
+  auto cg = [&](int c, double trel, int budget, bool* conv) -> int {
+    double rr = 0;
+    int e;
+    if ((e = vec_zdot(nc, ov->sb, ov->sb, ov->part, &rr, nullptr, st))) return e;
+    const double r0 = rr;
+    QED3_CUDA_TRY(cudaMemsetAsync(ov->se, 0, nd * sizeof(double), st));
+    QED3_CUDA_TRY(cudaMemcpyAsync(ov->sr, ov->sb, nd * sizeof(double), cudaMemcpyDeviceToDevice, st));
+    QED3_CUDA_TRY(cudaMemcpyAsync(ov->sp, ov->sb, nd * sizeof(double), cudaMemcpyDeviceToDevice, st));
+    *conv = rr == 0.0;
+    for (int k = 0; k < budget && !*conv; k++) {
+      const double tin = relax ? std::min(1e-5, std::max(tol_inner, tol_inner * std::sqrt(bb / rr))) : tol_inner;
+      if ((e = apply(c, ov->sq, ov->sp, tin))) return e;
+      double pq = 0;
+      if ((e = vec_zdot(nc, ov->sp, ov->sq, ov->part, &pq, nullptr, st))) return e;
+      const double al = rr / pq;
+      if ((e = vec_axpby(nd, al, ov->sp, 1.0, ov->se, ov->se, st))) return e;
+      if ((e = vec_axpby(nd, -al, ov->sq, 1.0, ov->sr, ov->sr, st))) return e;
+      double rn = 0;
+      if ((e = vec_zdot(nc, ov->sr, ov->sr, ov->part, &rn, nullptr, st))) return e;
+      it++;
+      if (!(std::isfinite(rn) && std::isfinite(al))) break;
+      if (rn <= trel * trel * r0) {
+        *conv = true;
+        break;
+      }
+      if ((e = vec_axpby(nd, 1.0, ov->sr, rn / rr, ov->sp, ov->sp, st))) return e;
+      rr = rn;
+    }
+    return QED3_OK;
+  };
   double tr = 0;
-  if (bb > 0) {
+  int status = bb == 0.0 ? QED3_OK : QED3_ERR_NOCONV;
+  // r = b (x = 0); then restarts on the true residual
+  QED3_CUDA_TRY(cudaMemcpyAsync(ov->y0, b, nd * sizeof(double), cudaMemcpyDeviceToDevice, st));
+  double rt = bb;
+  for (int restart = 0; restart < 5 && status != QED3_OK && it < maxiter; restart++) {
+    const double trel = 0.7 * tol * std::sqrt(bb / rt);  // |r| target relative to this pass's right-hand side
+    bool ok = true;
+    for (int c : chiral_split ? std::vector<int>{1, -1} : std::vector<int>{0}) {
+      if (c == 0) {
+        QED3_CUDA_TRY(cudaMemcpyAsync(ov->sb, ov->y0, nd * sizeof(double), cudaMemcpyDeviceToDevice, st));
+      } else if ((rc = chiral(nd, c, ov->y0, ov->sb, st))) {
+        return rc;
+      }
+      bool conv = false;
+      if ((rc = cg(c, chiral_split ? trel / std::sqrt(2.0) : trel, maxiter - it, &conv))) return rc;
+      ok = ok && conv;
+      if ((rc = vec_axpby(nd, 1.0, ov->se, 1.0, x, x, st))) return rc;
+    }
+    // certificate: r = b - A x with accurate pole solves
     if ((rc = overlap_apply(ov, QED3_OP_DDAGD, ov->sq, x, tol_inner, nullptr, st))) return rc;
-    if ((rc = vec_axpby(nd, 1.0, b, -1.0, ov->sq, ov->sq, st))) return rc;
-    if ((rc = vec_zdot(nc, ov->sq, ov->sq, ov->part, &tr, nullptr, st))) return rc;
+    if ((rc = vec_axpby(nd, 1.0, b, -1.0, ov->sq, ov->y0, st))) return rc;
+    if ((rc = vec_zdot(nc, ov->y0, ov->y0, ov->part, &tr, nullptr, st))) return rc;
+    rt = tr;
+    if (tr <= tol * tol * bb) status = QED3_OK;
+    else if (!ok && it >= maxiter) break;
   }
   QED3_CUDA_TRY(cudaEventRecord(e1, st));
   QED3_CUDA_TRY(cudaEventSynchronize(e1));
   float ms = 0;
   cudaEventElapsedTime(&ms, e0, e1);
-  cudaEventDestroy(e0);
-  cudaEventDestroy(e1);
   if (rep) {
     rep->status = status;
     rep->iters = it;
@@ -417,6 +637,16 @@ int overlap_solve(qed3_overlap_s* ov, double* x, const double* b, double tol, do
 
 namespace qed3 {
 qed3_dirac_s* overlap_dirac(qed3_overlap_s* ov) { return ov->d; }
+
+int overlap_low_modes_info(const qed3_overlap_s* ov, int* nev, double* max_residual, int* lanczos_steps,
+                           double* mu) {
+  if (nev) *nev = ov->nev;
+  if (max_residual) *max_residual = ov->lm_res;
+  if (lanczos_steps) *lanczos_steps = ov->lm_steps;
+  if (mu)
+    for (int i = 0; i < ov->nev; i++) mu[i] = ov->lm_mu[i];
+  return QED3_OK;
+}
 
 int overlap_info(const qed3_overlap_s* ov, double* lmin, double* lmax, double* k, double* delta, int* np,
                  int* np_fp64) {

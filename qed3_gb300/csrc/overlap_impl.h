@@ -14,7 +14,11 @@ int overlap_apply(qed3_overlap_s* ov, int op, double* out, const double* in, dou
 int overlap_force(qed3_overlap_s* ov, const double* eta, double* F, double tol, qed3_solve_report* rep,
                   cudaStream_t st);
 int overlap_solve(qed3_overlap_s* ov, double* x, const double* b, double tol, double tol_inner, int maxiter,
-                  qed3_solve_report* rep, cudaStream_t st);
+                  int flags, qed3_solve_report* rep, cudaStream_t st);
+int overlap_project_low_modes(qed3_overlap_s* ov, int nev, double tol, int maxsteps, double margin,
+                              cudaStream_t st);
+int overlap_low_modes_info(const qed3_overlap_s* ov, int* nev, double* max_residual, int* lanczos_steps,
+                           double* mu);
 qed3_dirac_s* overlap_dirac(qed3_overlap_s* ov);
 int overlap_info(const qed3_overlap_s* ov, double* lmin, double* lmax, double* k, double* delta, int* np,
                  int* np_fp64);
