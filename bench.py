@@ -159,6 +159,87 @@ def train_preconditioner(torch, Q, lat, D, dev, n_cfg=40, n_src=10, steps=1500):
                 "collect_s": t1 - t0, "train_s": t2 - t1}
 
 
+def tc_training_timing(torch, pc, steps=40, batch=8):
+    """Adam steps of the network with its 16 -> 16 channel mixing on the tensor
+    cores (tcgen05, BF16 operands, FP32 accumulation) and on FP32 CUDA cores;
+    the trained weights are restored afterwards."""
+    w0 = pc.get_weights()
+    out = {}
+    for name, on in (("tcgen05_bf16", True), ("cuda_core_fp32", False)):
+        pc.set_tensor_cores(on)
+        pc.train(3, batch=batch, seed=9)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        pc.train(steps, batch=batch, seed=9)
+        torch.cuda.synchronize()
+        out[name] = {"ms_per_adam_step": 1e3 * (time.perf_counter() - t0) / steps}
+        pc.set_weights(w0)
+    pc.set_tensor_cores(True)
+    out["speedup"] = out["cuda_core_fp32"]["ms_per_adam_step"] / out["tcgen05_bf16"]["ms_per_adam_step"]
+    out["config"] = f"batch {batch} residual/error pairs per step (forward, backward, Adam), n=64, 16 channels"
+    return out
+
+
+def host_pcg_iterations(torch, Q, D, pc, b, tol=TOL, maxiter=3000):
+    """Iterations of a host-driven flexible PCG (FP64 vectors, Polak-Ribiere
+    beta) with the network applied layer by layer (any depth), for comparing
+    networks by iteration count outside the persistent solver."""
+    x = torch.zeros_like(b)
+    r = b.clone()
+    z = torch.empty_like(b)
+    q = torch.empty_like(b)
+    pc.apply(z, r)
+    p = z.clone()
+    rz = torch.vdot(r, z).real
+    bn = float(b.norm())
+    for k in range(1, maxiter + 1):
+        D.apply(q, p, Q.OP_DDAGD)
+        al = rz / torch.vdot(p, q).real
+        x += al * p
+        r_new = r - al * q
+        if float(r_new.norm()) <= tol * bn:
+            break
+        pc.apply(z, r_new)
+        beta = torch.vdot(z, r_new - r).real / rz
+        p = z + beta * p
+        r = r_new
+        rz = torch.vdot(r, z).real
+    D.apply(q, x, Q.OP_DDAGD)
+    return k, float((b - q).norm()) / bn
+
+
+def network_depth_study(torch, Q, lat, D, pc2, dev, seeds=3):
+    """The learned-preconditioner configuration names a 3-layer, 16-channel
+    network; the solver runs the 2-layer one.  Trains the 3-layer network on
+    the same pairs recipe and compares iteration counts of the two networks
+    (host-driven flexible PCG, layer-by-layer application) on the benchmark
+    configuration with several sources."""
+    t0 = time.perf_counter()
+    pc3 = Q.LearnedPreconditioner(D, channels=16, layers=3, seed=1)
+    Dt = Q.DiracS2Dual(lat, 1.0, M5)
+    betas = (1.0, 1.4, 2.0)
+    for c in range(40):
+        Ac, _ = Q.thermalized_links(lat, betas[c % 3], seed=100 + c, ntraj=50, init="uniform", device=dev)
+        Dt.update(Ac)
+        pc3.collect(Dt, nsrc=10, seed=1000 + c, snapshots=(0, 5, 20, 60, 150))
+    hist = pc3.train(1500, batch=8, lr=3e-3, seed=2)
+    torch.cuda.synchronize()
+    out = {"train_s": time.perf_counter() - t0, "loss_last50": float(np.mean(hist[-50:])),
+           "params_3layer": pc3.info()["nparams"], "params_2layer": pc2.info()["nparams"], "cases": [],
+           "solver_words": {"layers2": 7, "layers3": 15}}
+    # the network acts with the hop blocks of the operator it was created on
+    # (the benchmark configuration): several sources on that configuration
+    for src in (7,) + tuple(50 + s for s in range(seeds)):
+        b = torch.from_numpy(Q.ParallelRng(lat, src).gaussian_spinor()).to(dev)
+        row = {"source_seed": src}
+        for name, p_ in (("layers2", pc2), ("layers3", pc3)):
+            it, res = host_pcg_iterations(torch, Q, D, p_, b)
+            row[name] = {"iters": it, "true_rel_res": res}
+        out["cases"].append(row)
+    out["iters_3_over_2"] = float(np.mean([c["layers3"]["iters"] / c["layers2"]["iters"] for c in out["cases"]]))
+    return out
+
+
 def heldout_iterations(torch, Q, lat, pc, dev, n=20):
     """Plain (FP64 and mixed) vs preconditioned mixed CG on 20 held-out
     configurations and sources, none used in training."""
@@ -506,25 +587,21 @@ def ref_gpu_baseline(A, b, reps=3):
 
 
 def count_launches(torch, fn):
-    """Kernel launches of one call of fn(), from the CUDA activity trace
-    (torch.profiler / CUPTI, read back from its chrome-trace export):
-    (this library's kernels, all kernels)."""
-    import tempfile
-    from torch.profiler import ProfilerActivity, profile
+    """Kernel launches of one call of fn() (CUPTI runtime-API callbacks,
+    qed3_gb300/launchcount.c): (this library's kernels, all kernels)."""
+    import ctypes
+    path = os.path.join(ROOT, "qed3_gb300", "liblaunchcount.so")
+    if not os.path.exists(path):
+        raise RuntimeError("launch counter not built (CUPTI headers missing)")
+    L = ctypes.CDLL(path)
     torch.cuda.synchronize()
-    with profile(activities=[ProfilerActivity.CPU, ProfilerActivity.CUDA]) as prof:
-        fn()
-        torch.cuda.synchronize()
-    with tempfile.TemporaryDirectory() as d:
-        path = os.path.join(d, "trace.json")
-        prof.export_chrome_trace(path)
-        with open(path) as f:
-            events = json.load(f).get("traceEvents", [])
-    names = [e.get("name", "") for e in events if e.get("cat") == "kernel"]
-    if not names:
-        raise RuntimeError("the trace holds no kernel events")
-    ours = [n for n in names if "qed3::" in n]
-    return len(ours), len(names)
+    if L.lc_start() != 0:
+        raise RuntimeError("CUPTI subscription failed")
+    fn()
+    torch.cuda.synchronize()
+    ours, tot = ctypes.c_longlong(), ctypes.c_longlong()
+    L.lc_stop(ctypes.byref(ours), ctypes.byref(tot))
+    return int(ours.value), int(tot.value)
 
 
 def profile_case(torch, which):
@@ -550,6 +627,15 @@ def profile_case(torch, which):
         # eight FP32 iterations of the mixed-precision CG (k_ext_apply32 and its BLAS)
         rep = De.solve(w, v, tol=1e-10, maxiter=8, precision=Q.PREC_F32)
         print(json.dumps({"norm": float(torch.linalg.vector_norm(w)), "iters": rep.iters}))
+    elif which == "train":
+        # a few Adam steps of the n=64 network (the tcgen05 mixing and weight-gradient kernels)
+        lat = Q.S2Trivalent(N_REFINE)
+        D = Q.DiracS2Dual(lat, 1.0, M5)
+        D.update(torch.from_numpy(np.random.default_rng(2).uniform(-np.pi, np.pi, lat.n_links)).cuda())
+        pc = Q.LearnedPreconditioner(D, channels=16, layers=2, seed=1)
+        pc.collect(D, nsrc=2, seed=1000, snapshots=(0, 5, 20))
+        hist = pc.train(4, batch=8, lr=3e-3, seed=2)
+        print(json.dumps({"loss": [float(v) for v in hist]}))
     elif which == "batched":
         # a quarter of the 256-RHS configuration (16 right-hand sides on each
         # of n = 16, 32, 48, 64; ~0.4 GB of fields, above L2) with the tile the
@@ -601,11 +687,12 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-paths", action="store_true", help="skip the timings of the HMC, overlap and S^2 x S^1 paths")
-    ap.add_argument("--profile", choices=["apply", "cg", "pcg", "ppcg", "batched", "ext"], default=None,
+    ap.add_argument("--profile", choices=["apply", "cg", "pcg", "ppcg", "batched", "ext", "train"], default=None,
                     help="small self-contained case for ncu: 'apply' = D apply at n=512 (f32, bf16, f64; "
                          "HBM-resident), 'cg' = one n=64 mixed-precision solve, 'pcg' = 300 iterations of the "
                          "n=64 preconditioned solve, 'ppcg' = the same with the pipelined one-barrier kernel, "
-                         "'batched' = 64 RHS over four lattices, 'ext' = S^2 x S^1 D apply at n=64, Nt=16")
+                         "'batched' = 64 RHS over four lattices, 'ext' = S^2 x S^1 D apply at n=64, Nt=16, "
+                         "'train' = four Adam steps of the n=64 network (tcgen05 channel mixing)")
     args = ap.parse_args()
     rank, world, local = env_rank()
     warmup = max(3, args.warmup)
@@ -705,6 +792,8 @@ def main():
     torch.cuda.nvtx.range_pop()
     clocks_info = clocks.stop()
 
+    train_info["tensor_cores"] = tc_training_timing(torch, pc)
+    train_info["depth_study"] = network_depth_study(torch, Q, lat, D, pc, dev)
     heldout = heldout_iterations(torch, Q, lat, pc, dev)
     batched = batched_throughput(torch, Q, dev)
     paths = None if args.no_paths else paths_timings(torch, Q, dev, cpu=rank == 0 and not args.no_cpu_baseline)
@@ -743,7 +832,8 @@ def main():
     try:
         ours1, all1 = count_launches(torch, one_step)
         launches = {"per_step": ours1, "per_step_all_kernels": all1,
-                    "source": "CUDA activity trace (torch.profiler) of one extra step, times the timed steps"}
+                    "source": "CUPTI launch callbacks on one extra step (qed3_gb300/launchcount.c), times the "
+                              "timed steps"}
     except Exception as e:  # the profiler is unavailable: the solve's launch sequence, counted by hand
         ours1 = 4  # |b| partials, unit-norm import, solver, scaled export
         launches = {"per_step": ours1, "source": f"launch sequence of the solve (trace unavailable: {e})"}

@@ -459,13 +459,10 @@ int qed3_overlap_solve(qed3_overlap* ov, double* x, const double* b, double tol,
  * outer CG is qed3_overlap_solve): QED3_OVSOLVE_CHIRAL solves the two
  * chirality sectors one after the other -- D_ov + D_ov^dag commutes with
  * gamma5 and is 2 P_c D_ov P_c on sector c, so each iteration needs one pole
- * solve instead of two; QED3_OVSOLVE_RELAX loosens the pole solves'
- * tolerance as the outer residual shrinks (tol_inner |b| / |r|, at most
- * 1e-5).  Every solve is certified by ||b - (D_ov + D_ov^dag) x|| / ||b||
- * recomputed with pole solves to tol_inner, and restarted on that residual
- * when it is above tol. */
+ * solve instead of two.  Every solve is certified by
+ * ||b - (D_ov + D_ov^dag) x|| / ||b|| recomputed with certified pole solves to
+ * tol_inner, and restarted on that residual when it is above tol. */
 #define QED3_OVSOLVE_CHIRAL 1
-#define QED3_OVSOLVE_RELAX 2
 int qed3_overlap_solve2(qed3_overlap* ov, double* x, const double* b, double tol, double tol_inner, int maxiter,
                         int flags, qed3_solve_report* report, void* stream);
 /* Low-mode projection of the sign function (no counterpart in the reference,
@@ -482,6 +479,17 @@ int qed3_overlap_solve2(qed3_overlap* ov, double* x, const double* b, double tol
  * qed3_overlap_force refuses (the force is for the unprojected sign
  * function). */
 int qed3_overlap_project_low_modes(qed3_overlap* ov, int nev, double tol, int maxsteps, double margin, void* stream);
+/* How the poles are solved (no counterpart in the reference, which runs one
+ * CG per pole on its own stream): QED3_POLES_MULTISHIFT (default) -- one FP64
+ * multi-shift CG for all poles, one stencil pass per iteration;
+ * QED3_POLES_BATCHED -- every pole its own mixed-precision CG (FP32
+ * iterations on FP32 or BF16-halo vectors, FP64 reliable updates and FP64
+ * true-residual certificates) in one persistent batched launch, the
+ * right-hand side broadcast; poles too ill-conditioned for FP32 inner
+ * iterations (condition above 2e5) run in FP64 in a second launch. */
+#define QED3_POLES_MULTISHIFT 0
+#define QED3_POLES_BATCHED 1
+int qed3_overlap_set_pole_solver(qed3_overlap* ov, int mode);
 /* nev in use, max ||H h_i - mu_i h_i||, Lanczos steps, mu[nev] (host, may be NULL) */
 int qed3_overlap_low_modes_info(const qed3_overlap* ov, int* nev, double* max_residual, int* lanczos_steps,
                                 double* mu);

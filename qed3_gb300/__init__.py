@@ -37,7 +37,7 @@ SOLVE_BCAST_B = 4
 SOLVE_FLEXIBLE = 8
 SOLVE_PIPELINED = 16
 OVSOLVE_CHIRAL = 1
-OVSOLVE_RELAX = 2
+POLES_MULTISHIFT, POLES_BATCHED = 0, 1
 PREC_NAMES = {"f64": PREC_F64, "f32": PREC_F32, "bf16": PREC_BF16}
 BYTES_PER_SITE = {PREC_F64: 32, PREC_F32: 16, PREC_BF16: 8}
 
@@ -135,6 +135,7 @@ SIGNATURES = [
     ("qed3_overlap_project_low_modes", ctypes.c_int, [vp, ctypes.c_int, ctypes.c_double, ctypes.c_int,
                                                       ctypes.c_double, vp]),
     ("qed3_overlap_low_modes_info", ctypes.c_int, [vp, c_int_p, c_double_p, c_int_p, vp]),
+    ("qed3_overlap_set_pole_solver", ctypes.c_int, [vp, ctypes.c_int]),
     ("qed3_multishift_solve", ctypes.c_int, [vp, ctypes.c_int, vp, vp, vp, ctypes.c_double, ctypes.c_int, vp,
                                              ctypes.POINTER(ctypes.c_float), vp]),
     ("qed3_dirac_ext_create", ctypes.c_int, [vp, ctypes.c_double, ctypes.c_double, ctypes.c_int, ctypes.c_double,
@@ -867,8 +868,7 @@ class Overlap:
     def solve(self, x, b, tol: float = 1e-10, tol_inner: float = 1e-12, maxiter: int = 10000, flags: int = 0,
               stream=None) -> Report:
         """Outer CG on D_ov^dag D_ov x = b; true_rel_res recomputed after convergence.
-        flags: OVSOLVE_CHIRAL (chirality sectors, one pole solve per
-        iteration), OVSOLVE_RELAX (pole tolerance loosened as |r| shrinks)."""
+        flags: OVSOLVE_CHIRAL (chirality sectors, one pole solve per iteration)."""
         r = SolveReport()
         if flags:
             _check(lib().qed3_overlap_solve2(self._h, _ptr(x), _ptr(b), tol, tol_inner, maxiter, flags,
@@ -884,6 +884,11 @@ class Overlap:
         function; the Zolotarev range then starts above them (nev = 0: off)."""
         _check(lib().qed3_overlap_project_low_modes(self._h, nev, tol, maxsteps, margin, _stream(stream)))
         return self.low_modes_info()
+
+    def set_pole_solver(self, mode: int):
+        """POLES_MULTISHIFT (FP64 multi-shift CG, default) or POLES_BATCHED
+        (one mixed-precision CG per pole in one batched launch)."""
+        _check(lib().qed3_overlap_set_pole_solver(self._h, mode))
 
     def low_modes_info(self) -> dict:
         n, res, steps = ctypes.c_int(), ctypes.c_double(), ctypes.c_int()

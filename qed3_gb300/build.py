@@ -43,6 +43,7 @@ def _needs_rebuild() -> bool:
 
 def build(force: bool = False, verbose: bool = False, extra: list[str] | None = None) -> str:
     if not force and not _needs_rebuild():
+        build_launch_counter()
         return LIB
     os.makedirs(BUILD, exist_ok=True)
     cc = nvcc()
@@ -67,7 +68,29 @@ def build(force: bool = False, verbose: bool = False, extra: list[str] | None = 
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stderr}")
     os.replace(tmp, LIB)
+    build_launch_counter()
     return LIB
+
+
+LC = os.path.join(HERE, "liblaunchcount.so")
+
+
+def build_launch_counter() -> str | None:
+    """The benchmark's CUPTI launch counter (launchcount.c, not part of
+    libqed3); skipped where the CUPTI headers are missing."""
+    src = os.path.join(HERE, "launchcount.c")
+    if os.path.exists(LC) and os.path.getmtime(LC) > os.path.getmtime(src):
+        return LC
+    cuda = os.path.dirname(os.path.dirname(nvcc()))
+    inc = [os.path.join(cuda, "include"), os.path.join(cuda, "extras", "CUPTI", "include")]
+    libdirs = [os.path.join(cuda, "lib64"), os.path.join(cuda, "extras", "CUPTI", "lib64")]
+    cmd = ["gcc", "-O2", "-shared", "-fPIC", "-o", LC + ".tmp", src] + ["-I" + i for i in inc] + \
+          ["-L" + l for l in libdirs] + ["-lcupti"] + ["-Wl,-rpath," + l for l in libdirs]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        return None
+    os.replace(LC + ".tmp", LC)
+    return LC
 
 
 if __name__ == "__main__":

@@ -854,7 +854,7 @@ int qed3_overlap_solve2(qed3_overlap* ov, double* x, const double* b, double tol
   QED3_GUARD_BEGIN
   if (!ov || !x || !b) return fail(QED3_ERR_ARG, "NULL argument");
   if (x == b) return fail(QED3_ERR_ARG, "x must not alias b");
-  if (flags & ~(QED3_OVSOLVE_CHIRAL | QED3_OVSOLVE_RELAX)) return fail(QED3_ERR_ARG, "unknown flags");
+  if (flags & ~QED3_OVSOLVE_CHIRAL) return fail(QED3_ERR_ARG, "unknown flags");
   return overlap_solve(ov, x, b, tol > 0 ? tol : 1e-10, tol_inner > 0 ? tol_inner : 1e-12,
                        maxiter > 0 ? maxiter : 10000, flags, report, (cudaStream_t)stream);
   QED3_GUARD_END
@@ -865,6 +865,13 @@ int qed3_overlap_project_low_modes(qed3_overlap* ov, int nev, double tol, int ma
   if (!ov) return fail(QED3_ERR_ARG, "NULL argument");
   return overlap_project_low_modes(ov, nev, tol > 0 ? tol : 1e-13, maxsteps > 0 ? maxsteps : 6000,
                                    margin >= 0 ? margin : 1e-3, (cudaStream_t)stream);
+  QED3_GUARD_END
+}
+
+int qed3_overlap_set_pole_solver(qed3_overlap* ov, int mode) {
+  QED3_GUARD_BEGIN
+  if (!ov) return fail(QED3_ERR_ARG, "NULL argument");
+  return overlap_set_pole_solver(ov, mode);
   QED3_GUARD_END
 }
 

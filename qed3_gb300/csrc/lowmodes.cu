@@ -237,10 +237,17 @@ void tri_vectors(const std::vector<double>& a, const std::vector<double>& b, int
 }
 }  // namespace
 
-int lanczos_lowmodes(long long nd, const std::function<int(double*, const double*)>& apply, int nev, double tol,
-                     int maxsteps, double** vec_out, std::vector<double>& theta, double* theta_next,
-                     double* theta_max, double* max_res, int* steps_used, cudaStream_t st) {
-  if (nev < 1 || maxsteps < 2 * nev + 10 || !(tol > 0)) return fail(QED3_ERR_ARG, "low modes: need nev >= 1, maxsteps >= 2 nev + 10, tol > 0");
+// Lanczos with full reorthogonalisation on a hermitian `apply`: the nv Ritz
+// pairs at the low end (largest = false) or the high end (largest = true),
+// converged to beta |s_last| <= tol * max|theta| (or after maxsteps when
+// require = false).  *vec_out: device, nv vectors; theta in the order of the
+// end (ascending for the low end, descending for the high end); *extreme =
+// the Ritz value at the opposite end.
+static int lanczos_core(long long nd, const std::function<int(double*, const double*)>& apply, int nv, bool largest,
+                        double tol, int maxsteps, bool require, double** vec_out, std::vector<double>& theta,
+                        double* extreme, int* steps_used, cudaStream_t st) {
+  const int nev = nv - 1;
+  if (nv < 1 || maxsteps < nv + 2 || !(tol > 0)) return fail(QED3_ERR_ARG, "low modes: bad Lanczos arguments");
   const long long nc = nd / 2;
   if (maxsteps > nc) maxsteps = int(nc);
   const int ntiles = int((nc + kTileC - 1) / kTileC);
@@ -273,8 +280,8 @@ int lanczos_lowmodes(long long nd, const std::function<int(double*, const double
     if (e) return e;
     if ((e = vec_axpby(nd, 1.0 / std::sqrt(re), col(0), 0.0, col(0), col(0), st))) return e;
     std::vector<double> al, be;
-    int j = 0, next_check = std::max(2 * nev + 20, 60);
-    bool done = false;
+    int j = 0, next_check = largest ? nev + 12 : std::max(2 * nev + 20, 60);
+    bool done = false, conv = false;
     std::vector<double> th;
     std::vector<std::vector<double>> S;
     double tmax = 0;
@@ -306,15 +313,23 @@ int lanczos_lowmodes(long long nd, const std::function<int(double*, const double
       const int m = j + 1;
       const bool last = beta <= 1e-14 * std::sqrt(std::max(w0, 1e-300)) || m == maxsteps;
       if (m >= next_check || last) {
-        next_check = m + std::max(40, m / 8);
+        next_check = m + (largest ? std::max(8, m / 10) : std::max(40, m / 8));
         if (m > nev) {
           th.assign(nev + 1, 0.0);
-          for (int k = 0; k <= nev; k++) th[k] = tri_eig(al, be, m, k);
-          tmax = tri_eig(al, be, m, m - 1);
-          tri_vectors(al, be, m, th, S);
+          for (int k = 0; k <= nev; k++) th[k] = tri_eig(al, be, m, largest ? m - 1 - k : k);
+          tmax = tri_eig(al, be, m, largest ? 0 : m - 1);
+          if (largest) {  // inverse iteration wants ascending order
+            std::vector<double> asc(th.rbegin(), th.rend());
+            tri_vectors(al, be, m, asc, S);
+            std::reverse(S.begin(), S.end());
+          } else {
+            tri_vectors(al, be, m, th, S);
+          }
           double worst = 0;
+          const double scale = std::max(std::abs(tmax), std::abs(th[0]));
           for (int k = 0; k <= nev; k++) worst = std::max(worst, beta * std::abs(S[k][m - 1]));
-          if (worst <= tol * tmax || last) done = true;
+          conv = worst <= tol * scale;
+          if (conv || last) done = true;
         }
       }
       if (!done) {
@@ -324,15 +339,17 @@ int lanczos_lowmodes(long long nd, const std::function<int(double*, const double
     }
     const int m = int(al.size());
     if (int(th.size()) != nev + 1) return fail(QED3_ERR_NOCONV, "low modes: Lanczos ended before nev + 1 steps");
-    // Ritz vectors of the nev smallest: Y_i = V S_i
+    if (require && !conv) return fail(QED3_ERR_NOCONV, "low modes: Lanczos did not converge in maxsteps");
+    const int nvec = nev + 1;
+    // Ritz vectors: Y_i = V S_i
     double* Y = nullptr;
-    if (cudaMalloc(&Y, size_t(nev) * nd * sizeof(double)) != cudaSuccess) {
+    if (cudaMalloc(&Y, size_t(nvec) * nd * sizeof(double)) != cudaSuccess) {
       cudaGetLastError();
       return fail(QED3_ERR_NOMEM, "low modes: cudaMalloc failed");
     }
-    std::vector<double> Sh(size_t(m) * nev * 2, 0.0);  // complex [m][nev]
+    std::vector<double> Sh(size_t(m) * nvec * 2, 0.0);  // complex [m][nvec]
     for (int jj = 0; jj < m; jj++)
-      for (int i = 0; i < nev; i++) Sh[2 * (size_t(jj) * nev + i)] = S[i][jj];
+      for (int i = 0; i < nvec; i++) Sh[2 * (size_t(jj) * nvec + i)] = S[i][jj];
     double* Sd = nullptr;
     if (cudaMalloc(&Sd, Sh.size() * sizeof(double)) != cudaSuccess) {
       cudaGetLastError();
@@ -342,10 +359,10 @@ int lanczos_lowmodes(long long nd, const std::function<int(double*, const double
     int rc = QED3_OK;
     if (cudaMemcpyAsync(Sd, Sh.data(), Sh.size() * sizeof(double), cudaMemcpyHostToDevice, st) != cudaSuccess)
       rc = fail(QED3_ERR_CUDA, "low modes: copy failed");
-    for (int i0 = 0; i0 < nev && !rc; i0 += kCombine) {
+    for (int i0 = 0; i0 < nvec && !rc; i0 += kCombine) {
       k_combine<<<nblocks(nc, 256), 256, 0, st>>>(nc, m, reinterpret_cast<const double2*>(V),
-                                                   reinterpret_cast<const double2*>(Sd), nev, i0,
-                                                   std::min(kCombine, nev - i0), reinterpret_cast<double2*>(Y));
+                                                   reinterpret_cast<const double2*>(Sd), nvec, i0,
+                                                   std::min(kCombine, nvec - i0), reinterpret_cast<double2*>(Y));
       if (cudaGetLastError() != cudaSuccess) rc = fail(QED3_ERR_CUDA, "low modes: combine failed");
     }
     cudaStreamSynchronize(st);
@@ -354,24 +371,8 @@ int lanczos_lowmodes(long long nd, const std::function<int(double*, const double
       cudaFree(Y);
       return rc;
     }
-    // explicit residuals ||A y - theta y||
-    double worst = 0;
-    for (int i = 0; i < nev && !rc; i++) {
-      double* yi = Y + size_t(i) * nd;
-      rc = apply(w, yi);
-      if (!rc) rc = vec_axpby(nd, 1.0, w, -th[i], yi, w, st);
-      double r2 = 0;
-      if (!rc) rc = vec_zdot(nc, w, w, part, &r2, &im, st);
-      worst = std::max(worst, std::sqrt(std::max(r2, 0.0)));
-    }
-    if (rc) {
-      cudaFree(Y);
-      return rc;
-    }
-    theta.assign(th.begin(), th.begin() + nev);
-    *theta_next = th[nev];
-    *theta_max = tmax;
-    *max_res = worst;
+    theta = th;
+    *extreme = tmax;
     *steps_used = m;
     *vec_out = Y;
     return QED3_OK;
@@ -379,6 +380,140 @@ int lanczos_lowmodes(long long nd, const std::function<int(double*, const double
   const int rc = body();
   cleanup();
   return rc;
+}
+
+// Chebyshev filter q(A) v = T_d((a + b - 2 A) / (b - a)) v: |q| <= 1 on [a, b],
+// growing fast below a, so the low end of A becomes the well separated high
+// end of q(A).  out = c1 x + c2 y + c3 z
+__global__ void k_lin3(long long n, double c1, const double* __restrict__ x, double c2, const double* __restrict__ y,
+                       double c3, const double* __restrict__ z, double* __restrict__ out) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = c1 * x[i] + c2 * y[i] + c3 * z[i];
+}
+
+// The nev smallest eigenpairs of the hermitian PSD `apply` (see the header):
+// a short pilot Lanczos gives an upper bound a of the (nev+1)-th eigenvalue
+// and b of the largest; Lanczos on the Chebyshev-filtered q(A) (degree
+// ~ 2.5 sqrt(b / a)) then converges the nev + 1 largest q, i.e. the nev + 1
+// smallest eigenvalues of A, in few steps even when they are 1e-7 of b apart.
+// Their eigenvalues are the Rayleigh quotients with A; explicit residuals.
+int lanczos_lowmodes(long long nd, const std::function<int(double*, const double*)>& apply, int nev, double tol,
+                     int maxsteps, double** vec_out, std::vector<double>& theta, double* theta_next,
+                     double* theta_max, double* max_res, int* steps_used, cudaStream_t st) {
+  if (nev < 1 || !(tol > 0) || maxsteps < 2 * nev + 20) return fail(QED3_ERR_ARG, "low modes: need nev >= 1, tol > 0, maxsteps >= 2 nev + 20");
+  const long long nc = nd / 2;
+  // pilot: a short unconverged Lanczos on A
+  double* P = nullptr;
+  std::vector<double> pth;
+  double pmax = 0;
+  int psteps = 0;
+  int rc = lanczos_core(nd, apply, nev + 1, false, 1e-300, std::min<long long>(maxsteps, std::min<long long>(nc, 3LL * nev + 80)),
+                        false, &P, pth, &pmax, &psteps, st);
+  if (P) cudaFree(P);
+  if (rc) return rc;
+  double b = 1.02 * pmax, a = 1.5 * pth[nev];
+  double* buf = nullptr;
+  if (cudaMalloc(&buf, 4 * size_t(nd) * sizeof(double)) != cudaSuccess) {
+    cudaGetLastError();
+    return fail(QED3_ERR_NOMEM, "low modes: cudaMalloc failed");
+  }
+  int total_steps = psteps;
+  double* Y = nullptr;
+  std::vector<double> th_out;
+  double res_out = 0, next_out = 0;
+  for (int attempt = 0; attempt < 6; attempt++) {
+    if (!(a < b)) {
+      rc = fail(QED3_ERR_NOCONV, "low modes: no spectral gap for the filter");
+      break;
+    }
+    const int deg = std::min(2000, std::max(8, int(std::ceil(2.5 / std::sqrt(a / b)))));
+    const double al = -2.0 / (b - a), be = (a + b) / (b - a);
+    double *T0 = buf, *T1 = buf + nd, *T2 = buf + 2 * nd, *AT = buf + 3 * nd;
+    auto filt = [&](double* out, const double* v) -> int {
+      int e;
+      QED3_CUDA_TRY(cudaMemcpyAsync(T0, v, nd * sizeof(double), cudaMemcpyDeviceToDevice, st));
+      if ((e = apply(AT, T0))) return e;
+      k_lin3<<<nblocks(nd, 256), 256, 0, st>>>(nd, al, AT, be, T0, 0.0, T0, T1);  // T1 = L v
+      double *pm = T0, *pc = T1, *pn = T2;
+      for (int k = 1; k < deg; k++) {
+        if ((e = apply(AT, pc))) return e;
+        k_lin3<<<nblocks(nd, 256), 256, 0, st>>>(nd, 2.0 * al, AT, 2.0 * be, pc, -1.0, pm, pn);
+        double* t = pm;
+        pm = pc;
+        pc = pn;
+        pn = t;
+      }
+      QED3_CUDA_TRY(cudaGetLastError());
+      QED3_CUDA_TRY(cudaMemcpyAsync(out, pc, nd * sizeof(double), cudaMemcpyDeviceToDevice, st));
+      return QED3_OK;
+    };
+    std::vector<double> qth;
+    double qmin = 0;
+    int qsteps = 0;
+    double* Yq = nullptr;
+    rc = lanczos_core(nd, filt, nev + 1, true, tol, std::min(maxsteps, 8 * (nev + 1) + 200), true, &Yq, qth, &qmin,
+                      &qsteps, st);
+    total_steps += qsteps * deg;
+    if (rc) {
+      if (Yq) cudaFree(Yq);
+      break;
+    }
+    // Rayleigh quotients and residuals with A, ascending
+    std::vector<double> ray(nev + 1), res(nev + 1);
+    double* w = AT;
+    for (int i = 0; i <= nev && !rc; i++) {
+      double* yi = Yq + size_t(i) * nd;
+      double re = 0, im = 0, r2 = 0;
+      rc = apply(w, yi);
+      if (!rc) rc = vec_zdot(nc, yi, w, T0, &re, &im, st);
+      ray[i] = re;
+      if (!rc) rc = vec_axpby(nd, 1.0, w, -re, yi, w, st);
+      if (!rc) rc = vec_zdot(nc, w, w, T0, &r2, &im, st);
+      res[i] = std::sqrt(std::max(r2, 0.0));
+    }
+    if (rc) {
+      cudaFree(Yq);
+      break;
+    }
+    const double top = *std::max_element(ray.begin(), ray.end());
+    if (!(top < a)) {  // the (nev+1)-th mode is not inside the amplified range: widen it
+      cudaFree(Yq);
+      a *= 2.0;
+      continue;
+    }
+    // order ascending in A (the filter is monotone below a, so this is the q order reversed)
+    std::vector<int> idx(nev + 1);
+    for (int i = 0; i <= nev; i++) idx[i] = i;
+    std::sort(idx.begin(), idx.end(), [&](int x, int y) { return ray[x] < ray[y]; });
+    if (cudaMalloc(&Y, size_t(nev) * nd * sizeof(double)) != cudaSuccess) {
+      cudaGetLastError();
+      cudaFree(Yq);
+      rc = fail(QED3_ERR_NOMEM, "low modes: cudaMalloc failed");
+      break;
+    }
+    th_out.assign(nev, 0.0);
+    res_out = 0;
+    for (int i = 0; i < nev; i++) {
+      QED3_CUDA_TRY(cudaMemcpyAsync(Y + size_t(i) * nd, Yq + size_t(idx[i]) * nd, nd * sizeof(double),
+                                    cudaMemcpyDeviceToDevice, st));
+      th_out[i] = ray[idx[i]];
+      res_out = std::max(res_out, res[idx[i]]);
+    }
+    next_out = ray[idx[nev]];
+    cudaStreamSynchronize(st);
+    cudaFree(Yq);
+    break;
+  }
+  cudaFree(buf);
+  if (rc) return rc;
+  if (!Y) return fail(QED3_ERR_NOCONV, "low modes: the filter range did not reach nev + 1 modes");
+  theta = th_out;
+  *theta_next = next_out;
+  *theta_max = b;
+  *max_res = res_out;
+  *steps_used = total_steps;
+  *vec_out = Y;
+  return QED3_OK;
 }
 
 // ---- chirality ------------------------------------------------------------------------------

@@ -236,7 +236,7 @@ static int ms_occupancy(int T, int* per_sm) {
 // fields each.  reps[m]: iterations at which shift m stopped, the FP64 true
 // residual ||b - (D^dag D + shift_m) x_m|| / ||b||, status.
 int mshift_solve(qed3_dirac_s* d, int ns, const double* shifts, const double* b_ref, double* x_ref, S64* X, S64* Pm,
-                 double tol, int maxiter, qed3_solve_report* reps, float* ms_out, cudaStream_t st) {
+                 double tol, int maxiter, qed3_solve_report* reps, float* ms_out, cudaStream_t st, bool certify_all) {
   if (ns < 1 || ns > kMsMaxShifts) return fail(QED3_ERR_ARG, "multi-shift: 1..64 shifts");
   if (!d->coeffs_set) return fail(QED3_ERR_STATE, "operator coefficients not set");
   int rc = ensure_work(d);
@@ -307,6 +307,18 @@ int mshift_solve(qed3_dirac_s* d, int ns, const double* shifts, const double* b_
   if (int(hs[2]) == QED3_ERR_TIMEOUT) return fail(QED3_ERR_TIMEOUT, "grid barrier timed out in the multi-shift kernel");
   // solutions to reference order, then the FP64 certificate of every shift
   if ((rc = field_export(d, QED3_PREC_F64, x_ref, X, ns, st))) return rc;
+  if (!certify_all && int(hs[2]) == QED3_OK) {
+    if (ms_out) *ms_out = ms;
+    for (int m = 0; m < ns; m++) {
+      qed3_solve_report r{};
+      r.iters = int(hs[3 + m]);
+      r.true_rel_res = -1.0;  // not recomputed
+      r.status = QED3_OK;
+      r.ms = ms;
+      if (reps) reps[m] = r;
+    }
+    return QED3_OK;
+  }
   const double bb = hs[1];
   const long long nd = 4LL * Ns;
   double* q = reinterpret_cast<double*>(w.xhi2);  // scratch, one reference-order vector

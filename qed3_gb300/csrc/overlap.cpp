@@ -38,6 +38,7 @@ struct qed3_overlap_s {
   qed3_batch_s* batch_hi = nullptr;  // poles 0..nh-1 (ill-conditioned) in FP64
   int nh = 0, nlo = 0;               // current split
   bool multishift = true;            // all poles through the FP64 multi-shift CG (false: batched launches)
+  bool certify_poles = true;         // FP64 true residual of every pole after each multi-shift solve
   double* Z = nullptr;     // [npoles][2 Ns] complex
   double* y = nullptr;     // [2 Ns] complex
   double* w = nullptr;
@@ -356,7 +357,8 @@ static int pole_solves(qed3_overlap_s* ov, const double* rhs, double* out, doubl
       QED3_CUDA_TRY(cudaMalloc(&ov->msP, size_t(np) * nd * sizeof(double)));
     }
     float ms = 0;
-    const int rc = mshift_solve(ov->d, np, shifts.data(), rhs, out, ov->msX, ov->msP, tol, 200000, reps.data(), &ms, st);
+    const int rc = mshift_solve(ov->d, np, shifts.data(), rhs, out, ov->msX, ov->msP, tol, 200000, reps.data(), &ms, st,
+                                ov->certify_poles);
     if (rc) return rc;
     w.ms = ms;
   }
@@ -512,9 +514,6 @@ int overlap_force(qed3_overlap_s* ov, const double* eta, double* F, double tol, 
 //    (eps = gamma5 (D_ov - 1)) commutes with gamma5 for any hermitian eps,
 //    and on the chirality-c sector it is 2 P_c D_ov P_c -- one pole solve per
 //    iteration instead of two; the sectors are solved one after the other.
-//  * QED3_OVSOLVE_RELAX: the pole solves' tolerance grows as the outer
-//    residual shrinks, tol_k = tol_inner |b| / |r_k| (at most 1e-5)
-//    (inexact Krylov: later directions need less accuracy).
 // After convergence the true residual ||b - D_ov^dag D_ov x|| is recomputed
 // with pole solves to tol_inner; above tol, the CG restarts on that residual
 // (at most 4 restarts).  The report: total outer iterations, the certificate,
@@ -531,7 +530,6 @@ int overlap_solve(qed3_overlap_s* ov, double* x, const double* b, double tol, do
     QED3_CUDA_TRY(cudaMalloc(&ov->sb, nd * sizeof(double)));
   }
   const bool chiral_split = (flags & QED3_OVSOLVE_CHIRAL) != 0;
-  const bool relax = (flags & QED3_OVSOLVE_RELAX) != 0;
   cudaEvent_t e0, e1;
   QED3_CUDA_TRY(cudaEventCreate(&e0));
   QED3_CUDA_TRY(cudaEventCreate(&e1));
@@ -548,6 +546,14 @@ int overlap_solve(qed3_overlap_s* ov, double* x, const double* b, double tol, do
   if ((rc = vec_zdot(nc, b, b, ov->part, &bb, nullptr, st))) return rc;
   QED3_CUDA_TRY(cudaMemsetAsync(x, 0, nd * sizeof(double), st));
   // the operator of sector c (0: the full D_ov + D_ov^dag)
+  // the CG's products skip the per-pole FP64 certificates (the outer
+  // certificate below judges the result); poles that stop unconverged are
+  // still certified and corrected inside the multi-shift solve
+  ov->certify_poles = false;
+  struct Restore {
+    qed3_overlap_s* o;
+    ~Restore() { o->certify_poles = true; }
+  } restore{ov};
   auto apply = [&](int c, double* out, const double* v, double tin) -> int {
     qed3_solve_report ir{};
     int e;
@@ -572,8 +578,7 @@ int overlap_solve(qed3_overlap_s* ov, double* x, const double* b, double tol, do
     QED3_CUDA_TRY(cudaMemcpyAsync(ov->sp, ov->sb, nd * sizeof(double), cudaMemcpyDeviceToDevice, st));
     *conv = rr == 0.0;
     for (int k = 0; k < budget && !*conv; k++) {
-      const double tin = relax ? std::min(1e-5, std::max(tol_inner, tol_inner * std::sqrt(bb / rr))) : tol_inner;
-      if ((e = apply(c, ov->sq, ov->sp, tin))) return e;
+      if ((e = apply(c, ov->sq, ov->sp, tol_inner))) return e;
       double pq = 0;
       if ((e = vec_zdot(nc, ov->sp, ov->sq, ov->part, &pq, nullptr, st))) return e;
       const double al = rr / pq;
@@ -611,8 +616,11 @@ int overlap_solve(qed3_overlap_s* ov, double* x, const double* b, double tol, do
       ok = ok && conv;
       if ((rc = vec_axpby(nd, 1.0, ov->se, 1.0, x, x, st))) return rc;
     }
-    // certificate: r = b - A x with accurate pole solves
-    if ((rc = overlap_apply(ov, QED3_OP_DDAGD, ov->sq, x, tol_inner, nullptr, st))) return rc;
+    // certificate: r = b - A x with accurate, certified pole solves
+    ov->certify_poles = true;
+    rc = overlap_apply(ov, QED3_OP_DDAGD, ov->sq, x, tol_inner, nullptr, st);
+    ov->certify_poles = false;
+    if (rc) return rc;
     if ((rc = vec_axpby(nd, 1.0, b, -1.0, ov->sq, ov->y0, st))) return rc;
     if ((rc = vec_zdot(nc, ov->y0, ov->y0, ov->part, &tr, nullptr, st))) return rc;
     rt = tr;
@@ -637,6 +645,12 @@ int overlap_solve(qed3_overlap_s* ov, double* x, const double* b, double tol, do
 
 namespace qed3 {
 qed3_dirac_s* overlap_dirac(qed3_overlap_s* ov) { return ov->d; }
+
+int overlap_set_pole_solver(qed3_overlap_s* ov, int mode) {
+  if (mode != QED3_POLES_MULTISHIFT && mode != QED3_POLES_BATCHED) return fail(QED3_ERR_ARG, "unknown pole solver");
+  ov->multishift = mode == QED3_POLES_MULTISHIFT;
+  return QED3_OK;
+}
 
 int overlap_low_modes_info(const qed3_overlap_s* ov, int* nev, double* max_residual, int* lanczos_steps,
                            double* mu) {
