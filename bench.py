@@ -517,6 +517,95 @@ def paths_timings(torch, Q, dev, cpu=True):
     return out
 
 
+def topological_charge(torch, Q, lat, A):
+    """Q = sum over dual faces of the plaquette angle wrapped to (-pi, pi], / 2 pi."""
+    th = torch.empty(lat.n_faces, dtype=torch.float64, device=A.device)
+    Q.plaquette(lat, A, th)
+    return float(torch.remainder(th + np.pi, 2 * np.pi).sub(np.pi).sum()) / (2 * np.pi)
+
+
+def dense_sign_error(torch, Q, dev, nev=16):
+    """Sign-function check of the overlap configuration at n=8: D_ov from the
+    dense FP64 eigendecomposition of H = gamma5 D_W (numpy eigh; D_W taken
+    column by column from this library's apply) against the GPU D_ov (20
+    poles), with and without the low-mode projection."""
+    n = 8
+    lat = Q.S2Trivalent(n)
+    A, _ = Q.thermalized_links(lat, BETA, seed=2, ntraj=50, init="uniform", device=dev)
+    D = Q.DiracS2Dual(lat, 1.0, -1.0)
+    D.update(A)
+    N = 2 * lat.n_sites
+    E = torch.eye(N, dtype=torch.complex128, device=dev)
+    M = torch.empty_like(E)
+    for j in range(N):
+        D.apply(M[j], E[j], Q.OP_D)  # row j of M = D e_j, i.e. column j of D
+    Mh = M.T.cpu().numpy()
+    g5 = np.tile([1.0, -1.0], N // 2)
+    w, V = np.linalg.eigh(g5[:, None] * Mh)
+    Dex = np.eye(N) + g5[:, None] * ((V * np.sign(w)) @ V.conj().T)
+    ov = Q.Overlap(D, order=41)
+    ov.update_lanczos()
+    xi = np.random.default_rng(3).normal(size=N) + 1j * np.random.default_rng(4).normal(size=N)
+    xt = torch.from_numpy(xi).to(dev)
+    y = torch.empty_like(xt)
+    ref = Dex @ xi
+    out = {"n": n, "charge": topological_charge(torch, Q, lat, A), "dense": "numpy eigh of gamma5 D_W, FP64"}
+    for nev_ in (0, nev):
+        info = ov.project_low_modes(nev_)
+        ov.apply(y, xt, Q.OP_D, tol_inner=1e-12)
+        out[f"nev{nev_}"] = {"k": info["k"], "delta": info["delta"],
+                             "rel_err_D_ov": float(np.abs(y.cpu().numpy() - ref).max() / np.abs(ref).max())}
+    return out
+
+
+def overlap_config(torch, Q, dev, nev=48):
+    """The overlap configuration: n=32 (20,480 sites), links U[-pi,pi) seed 2 +
+    50 pure-gauge HMC trajectories at beta=1.4, M5=-1, Zolotarev order 41 (20
+    poles), outer D_ov^dag D_ov solve of the propagator right-hand side
+    b = D_ov^dag xi to 1e-10 (certified with certified pole solves).  The
+    configuration carries topological charge, so the massless overlap has
+    exact zero modes; the nev eigenmodes of gamma5 D_W nearest zero are
+    treated exactly in the sign function (qed3_overlap_project_low_modes) and
+    the outer CG runs per chirality sector."""
+    n = 32
+    lat = Q.S2Trivalent(n)
+    A, _ = Q.thermalized_links(lat, BETA, seed=2, ntraj=50, init="uniform", device=dev)
+    D = Q.DiracS2Dual(lat, 1.0, -1.0)
+    D.update(A)
+    ov = Q.Overlap(D, order=41)
+    out = {"config": "n=32, beta=1.4 seed 2 (50 HMC trajectories from U[-pi,pi)), M5=-1, order 41 (20 poles), "
+                     "outer CG on D_ov^dag D_ov to 1e-10, pole solves to 1e-12",
+           "charge": topological_charge(torch, Q, lat, A)}
+    out["bounds_s"] = _wall(torch, lambda: ov.update_lanczos(), 1)
+    i0 = ov.info()
+    out["unprojected"] = {"k": i0["k"], "delta": i0["delta"]}
+    xi = torch.from_numpy(Q.ParallelRng(lat, 5).gaussian_spinor()).to(dev)
+    y = torch.empty_like(xi)
+    reps = []
+    out["unprojected"]["apply_D_ms"] = 1e3 * _wall(torch, lambda: reps.append(ov.apply(y, xi, Q.OP_D,
+                                                                                     tol_inner=1e-12)), 2)
+    out["unprojected"]["pole_iters"] = reps[-1].iters
+    info = {}
+    out["project_s"] = _wall(torch, lambda: info.update(ov.project_low_modes(nev)), 1)
+    out["projected"] = {"nev": nev, "k": info["k"], "delta": info["delta"], "max_residual": info["max_residual"],
+                        "lanczos_applies": info["lanczos_steps"]}
+    reps = []
+    out["projected"]["apply_D_ms"] = 1e3 * _wall(torch, lambda: reps.append(ov.apply(y, xi, Q.OP_D,
+                                                                                   tol_inner=1e-12)), 3)
+    out["projected"]["pole_iters"] = reps[-1].iters
+    b = torch.empty_like(xi)
+    ov.apply(b, xi, Q.OP_DDAG, tol_inner=1e-12)
+    x = torch.zeros_like(b)
+    rr = []
+    t = _wall(torch, lambda: rr.append(ov.solve(x, b, tol=TOL, tol_inner=1e-12, maxiter=20000,
+                                                 flags=Q.OVSOLVE_CHIRAL)), 1)
+    out["outer_solve"] = {"s": t, "iters": rr[-1].iters, "true_rel_res": rr[-1].true_rel_res,
+                          "certified": rr[-1].status == Q.OK and rr[-1].true_rel_res <= TOL,
+                          "max_pole_iters": rr[-1].reliable_updates, "mode": "chirality sectors"}
+    out["sign_check_n8"] = dense_sign_error(torch, Q, dev)
+    return out
+
+
 def batched_throughput(torch, Q, dev, reps=3):
     """The multi-lattice batched configuration: 256 right-hand sides, 64 on each
     of n = 16, 32, 48, 64 (each with its own beta = 1.4 configuration and a mass
@@ -797,6 +886,7 @@ def main():
     heldout = heldout_iterations(torch, Q, lat, pc, dev)
     batched = batched_throughput(torch, Q, dev)
     paths = None if args.no_paths else paths_timings(torch, Q, dev, cpu=rank == 0 and not args.no_cpu_baseline)
+    overlap32 = None if args.no_paths else overlap_config(torch, Q, dev)
 
     # ---- roofline of the dominant kernel ----------------------------------------------
     # algorithmic HBM bytes per site per iteration (the measurement rule: each array once):
@@ -870,6 +960,7 @@ def main():
                                        "frac": hbm_apply["frac_of_" + peak_kind]}},
             "apply_sweep": sweep,
             "batched_256": batched,
+            "overlap_n32": overlap32,
             "paths": paths,
             "e2e": {"value": e2e, "unit": "solves/s", "h2d_bytes_per_step": b.nbytes, "d2h_bytes_per_step": b.nbytes},
             "gpu_launches": ours1 * n_timed,
