@@ -517,6 +517,55 @@ def paths_timings(torch, Q, dev, cpu=True):
     return out
 
 
+def learned_hbm(torch, Q, dev, n=256, reps=3):
+    """The learned preconditioner on an HBM-resident lattice: n=256 (1,310,720
+    sites; ~0.4 GB of FP32 operator and state), where the preconditioned
+    solver streams its state through HBM tile by tile (k_pcgs).  Links
+    U[-pi,pi) seed 2 + 10 pure-gauge HMC trajectories at beta=1.4, M5=0.05,
+    Gaussian source seed 7; the network (16 channels, 2 layers) is trained on
+    pairs from this lattice (4 configurations x 4 sources, 400 Adam steps).
+    Plain FP64 CG, plain mixed CG and the learned solver, each certified."""
+    t0 = time.perf_counter()
+    lat = Q.S2Trivalent(n)
+    A, _ = Q.thermalized_links(lat, BETA, seed=2, ntraj=10, init="uniform", device=dev)
+    D = Q.DiracS2Dual(lat, 1.0, M5)
+    D.update(A)
+    pc = Q.LearnedPreconditioner(D, channels=16, layers=2, seed=1)
+    Dt = Q.DiracS2Dual(lat, 1.0, M5)
+    for c in range(4):
+        Ac, _ = Q.thermalized_links(lat, (1.0, 1.4, 2.0, 1.4)[c], seed=700 + c, ntraj=10, init="uniform", device=dev)
+        Dt.update(Ac)
+        pc.collect(Dt, nsrc=4, seed=900 + c, snapshots=(0, 5, 20, 60, 150))
+    pc.train(400, batch=8, lr=3e-3, seed=2)
+    torch.cuda.synchronize()
+    out = {"n": n, "sites": lat.n_sites, "block_sites": pc.info()["block_sites"], "setup_s": time.perf_counter() - t0}
+    b = torch.from_numpy(Q.ParallelRng(lat, 7).gaussian_spinor()).to(dev)
+    x = torch.zeros_like(b)
+    st = torch.cuda.current_stream()
+    for name, fn in (("cg_f64", lambda: D.solve(x, b, tol=TOL, precision=Q.PREC_F64)),
+                     ("cg_f32", lambda: D.solve(x, b, tol=TOL, precision=Q.PREC_F32)),
+                     ("pcg_f32", lambda: pc.solve(D, x, b, tol=TOL, precision=Q.PREC_F32))):
+        fn()
+        ms, rep = [], None
+        for _ in range(reps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(st)
+            rep = fn()
+            e1.record(st)
+            e1.synchronize()
+            ms.append(e0.elapsed_time(e1))
+        out[name] = {"ms": float(np.mean(ms)), "iters": rep.iters, "true_rel_res": rep.true_rel_res,
+                     "certified": rep.status == Q.OK and rep.true_rel_res <= TOL}
+    out["speedup_vs_cg_f64"] = out["cg_f64"]["ms"] / out["pcg_f32"]["ms"]
+    out["speedup_vs_cg_f32"] = out["cg_f32"]["ms"] / out["pcg_f32"]["ms"]
+    # the streaming kernel's HBM bytes: D^dag D at 288 B/site + 7 FP32 state streams at 16 B
+    gbs = 400 * lat.n_sites * out["pcg_f32"]["iters"] / (out["pcg_f32"]["ms"] * 1e-3) / 1e9
+    peak, kind = peaks()
+    out["pcg_roofline"] = {"kernel": "k_pcgs<F32,7>", "GB/s": gbs, "frac_of_" + kind: gbs / peak,
+                           "bytes_per_site_iter": 400, "resident": "HBM"}
+    return out
+
+
 def topological_charge(torch, Q, lat, A):
     """Q = sum over dual faces of the plaquette angle wrapped to (-pi, pi], / 2 pi."""
     th = torch.empty(lat.n_faces, dtype=torch.float64, device=A.device)
@@ -887,6 +936,7 @@ def main():
     batched = batched_throughput(torch, Q, dev)
     paths = None if args.no_paths else paths_timings(torch, Q, dev, cpu=rank == 0 and not args.no_cpu_baseline)
     overlap32 = None if args.no_paths else overlap_config(torch, Q, dev)
+    hbm_pcg = None if args.no_paths else learned_hbm(torch, Q, dev)
 
     # ---- roofline of the dominant kernel ----------------------------------------------
     # algorithmic HBM bytes per site per iteration (the measurement rule: each array once):
@@ -961,6 +1011,7 @@ def main():
             "apply_sweep": sweep,
             "batched_256": batched,
             "overlap_n32": overlap32,
+            "learned_pc_n256": hbm_pcg,
             "paths": paths,
             "e2e": {"value": e2e, "unit": "solves/s", "h2d_bytes_per_step": b.nbytes, "d2h_bytes_per_step": b.nbytes},
             "gpu_launches": ours1 * n_timed,

@@ -530,6 +530,260 @@ timeout:
 }
 
 // ---------------------------------------------------------------------------
+// Streaming preconditioned CG for lattices that do not fit the registers
+// ---------------------------------------------------------------------------
+// Same recurrence, reliable updates and certificate as k_pcg, for lattices
+// whose per-SM share exceeds what one block can hold in registers (about
+// n >= 94): the preconditioner's blocks become tiles of `per` <= 576 sites,
+// every block of a persistent one-block-per-SM grid walks its tiles inside
+// each phase, and the solver state lives in global memory (read and written
+// once per site and phase; the operator's hop blocks come through the
+// read-only path).  z = N r is applied tile by tile in shared memory right
+// after the tile's residual update, so an iteration keeps its two grid
+// barriers.  State arrays (internal order): r, p, t and z in FP32 (float4 per
+// site), the gathered copies of z and t in the halo precision, x as an FP32
+// increment folded into FP64 at reliable updates.
+struct PcgsState {
+  float4* r;
+  float4* p;
+  float4* t;  // own FP32 copy of t (halo_t holds the gathered copy)
+  float4* z;  // own FP32 copy of z
+  float4* xl;
+};
+
+__device__ __forceinline__ Sp32 ldf4(const float4* f, int i) { return f42sp(f[i]); }
+__device__ __forceinline__ void stf4(float4* f, int i, const Sp32& v) { f[i] = sp2f4(v); }
+
+template <int P, int NW>
+__global__ void __launch_bounds__(576, 1) k_pcgs(PcgArgs a, PcgsState st) {
+  extern __shared__ float4 S[];
+  __shared__ double sh[32 * 4 + 64 + 8];
+  const int Ns = a.Ns, per = a.per;
+  const int ntiles = (Ns + per - 1) / per;
+  const Sp64 z64{make_double2(0, 0), make_double2(0, 0)};
+  const Sp32 z32{make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
+  // per-tile site data of this thread
+  auto site = [&](int tile, int (&own)[1], int (&loc)[1], bool (&val)[1], int (&jj)[1][3]) {
+    loc[0] = threadIdx.x;
+    own[0] = tile * per + threadIdx.x;
+    val[0] = own[0] < Ns;
+#pragma unroll
+    for (int q = 0; q < 3; q++) jj[0][q] = val[0] ? __ldg(a.nbr + q * Ns + own[0]) : 0;
+  };
+  // ---- phase 0: r = b, z = N r, p = t = x = 0 ---------------------------------------------
+  double v2[2] = {0.0, 0.0};
+  for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    int own[1], loc[1], jj[1][3];
+    bool val[1];
+    site(tile, own, loc, val, jj);
+    Sp32 r[1] = {z32}, z[1];
+    const int i = own[0];
+    if (val[0]) {
+      const Sp64 bi = ld64(a.b, i);
+      v2[0] += n2(bi);
+      r[0] = Sp32{make_float2(float(bi.s0.x), float(bi.s0.y)), make_float2(float(bi.s1.x), float(bi.s1.y))};
+    }
+    pc_apply<NW, 1, false>(a, S, nullptr, tile * per, own, loc, val, jj, r, z);
+    if (val[0]) {
+      stf4(st.r, i, r[0]);
+      stf4(st.z, i, z[0]);
+      hs32<P>(a.halo_z, i, z[0]);
+      stf4(st.p, i, z32);
+      stf4(st.t, i, z32);
+      stf4(st.xl, i, z32);
+      hs64(a.x, i, z64);
+      v2[1] += double(rdotf(r[0], z[0]));
+    }
+    __syncthreads();  // the tile's shared fields are reused by the next tile
+  }
+  unsigned int epoch = 0;
+  int parity = 0;
+  v2_publish<2>(v2, a.partials, parity, sh);
+  if (!grid_sync2(a.bar, epoch, a.spin_limit)) goto timeout;
+  {
+    double tot[2];
+    v2_total<2>(a.partials, parity, tot, sh);
+    parity ^= 1;
+    const double bnorm2 = tot[0];
+    double rho = tot[1];
+    double mu_max = bnorm2, beta = 0.0, mu_true = bnorm2;
+    double2 a_z = make_double2(1.0, 0.0);
+    int iter = 0, nru = 0, status = QED3_ERR_NOCONV;
+    const double s = a.shift;
+    if (bnorm2 == 0.0) {
+      status = QED3_OK;
+      mu_true = 0.0;
+      goto finish;
+    }
+    while (true) {
+      // ---- phase A: t = a_z D z + beta t, p = a_z z + beta p ----------------------------
+      {
+        float v[1] = {0.f};
+        const float2 az = make_float2(float(a_z.x), float(a_z.y));
+        const float bt = float(beta);
+        for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+          const int i = tile * per + threadIdx.x;
+          if (i >= Ns) continue;
+          int jj[3];
+#pragma unroll
+          for (int q = 0; q < 3; q++) jj[q] = __ldg(a.nbr + q * Ns + i);
+          const Sp32 zi = ldf4(st.z, i);
+          Sp32 ti = ldf4(st.t, i), pi = ldf4(st.p, i);
+          const Sp32 dz = stencil32h<P, false>(i, 0, per, Ns, jj, a.H32, nullptr, __ldg(a.diag32 + i), zi, a.halo_z);
+          ti.s0 = cfmaf(az, dz.s0, make_float2(bt * ti.s0.x, bt * ti.s0.y));
+          ti.s1 = cfmaf(az, dz.s1, make_float2(bt * ti.s1.x, bt * ti.s1.y));
+          pi.s0 = cfmaf(az, zi.s0, make_float2(bt * pi.s0.x, bt * pi.s0.y));
+          pi.s1 = cfmaf(az, zi.s1, make_float2(bt * pi.s1.x, bt * pi.s1.y));
+          stf4(st.t, i, ti);
+          stf4(st.p, i, pi);
+          hs32<P>(a.halo_t, i, ti);
+          v[0] += n2f(ti) + float(s) * n2f(pi);
+        }
+        v2_publish_f<1>(v, a.partials, parity, sh);
+        if (!grid_sync2(a.bar, epoch, a.spin_limit)) goto timeout;
+      }
+      double gam[1];
+      v2_total<1>(a.partials, parity, gam, sh);
+      parity ^= 1;
+      const double alpha = rho / gam[0];
+      // ---- phase B: q = D^dag t + s p, x += alpha p, r -= alpha q, z = N r -------------
+      {
+        float v[2] = {0.f, 0.f};
+        const float al = float(alpha), sf = float(s);
+        for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+          int own[1], loc[1], jj[1][3];
+          bool val[1];
+          site(tile, own, loc, val, jj);
+          const int i = own[0];
+          Sp32 r[1] = {z32}, z[1];
+          if (val[0]) {
+            const Sp32 ti = ldf4(st.t, i), pi = ldf4(st.p, i);
+            const Sp32 q = stencil32h<P, false>(i, 0, per, Ns, jj[0], a.Hd32, nullptr, __ldg(a.diag32 + i), ti,
+                                                a.halo_t);
+            r[0] = sp_add(ldf4(st.r, i), sp_add(q, pi, sf), -al);
+            stf4(st.xl, i, sp_add(ldf4(st.xl, i), pi, al));
+          }
+          pc_apply<NW, 1, false>(a, S, nullptr, tile * per, own, loc, val, jj, r, z);
+          if (val[0]) {
+            stf4(st.r, i, r[0]);
+            stf4(st.z, i, z[0]);
+            hs32<P>(a.halo_z, i, z[0]);
+            v[0] += n2f(r[0]);
+            v[1] += rdotf(r[0], z[0]);
+          }
+          __syncthreads();
+        }
+        v2_publish_f<2>(v, a.partials, parity, sh);
+        if (!grid_sync2(a.bar, epoch, a.spin_limit)) goto timeout;
+      }
+      double mun[2];
+      v2_total<2>(a.partials, parity, mun, sh);
+      parity ^= 1;
+      iter++;
+      const double mu_new = mun[0], rho_new = mun[1];
+      mu_max = fmax(mu_max, mu_new);
+      const bool want = !isfinite(mu_new) || !isfinite(alpha) || !(rho_new > 0.0) || mu_new < a.tol2 * bnorm2 ||
+                        iter >= a.maxiter || mu_new < a.delta2 * mu_max;
+      if (!want) {
+        beta = rho_new / rho;
+        a_z = make_double2(1.0, 0.0);
+        rho = rho_new;
+        continue;
+      }
+      // ---- R0: fold x ---------------------------------------------------------------------
+      for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const int i = tile * per + threadIdx.x;
+        if (i >= Ns) continue;
+        Sp64 xh = hl64(a.x, i);
+        const Sp32 xl = ldf4(st.xl, i);
+        xh.s0 = make_double2(xh.s0.x + xl.s0.x, xh.s0.y + xl.s0.y);
+        xh.s1 = make_double2(xh.s1.x + xl.s1.x, xh.s1.y + xl.s1.y);
+        hs64(a.x, i, xh);
+        stf4(st.xl, i, z32);
+      }
+      if (!grid_sync2(a.bar, epoch, a.spin_limit)) goto timeout;
+      // ---- R1: t64 = D x ------------------------------------------------------------------
+      for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const int i = tile * per + threadIdx.x;
+        if (i >= Ns) continue;
+        int jj[3];
+#pragma unroll
+        for (int q = 0; q < 3; q++) jj[q] = __ldg(a.nbr + q * Ns + i);
+        hs64(a.t64, i, stencil64(i, Ns, jj, a.H, a.diag, hl64(a.x, i), a.x));
+      }
+      if (!grid_sync2(a.bar, epoch, a.spin_limit)) goto timeout;
+      // ---- R2: r = b - D^dag t64 - s x, z = N r;  |r|^2, <r,z>, <r,p> --------------------
+      {
+        double v[4] = {0.0, 0.0, 0.0, 0.0};
+        for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+          int own[1], loc[1], jj[1][3];
+          bool val[1];
+          site(tile, own, loc, val, jj);
+          const int i = own[0];
+          Sp32 r[1] = {z32}, z[1];
+          if (val[0]) {
+            const Sp64 self = hl64(a.t64, i), xh = hl64(a.x, i);
+            const Sp64 q = stencil64(i, Ns, jj[0], a.Hd, a.diag, self, a.t64);
+            const Sp64 bi = ld64(a.b, i);
+            Sp64 rt;
+            rt.s0 = csub(bi.s0, cadd(q.s0, cscale(s, xh.s0)));
+            rt.s1 = csub(bi.s1, cadd(q.s1, cscale(s, xh.s1)));
+            v[0] += n2(rt);
+            const Sp32 pf = ldf4(st.p, i);
+            const double2 pv0 = make_double2(pf.s0.x, pf.s0.y), pv1 = make_double2(pf.s1.x, pf.s1.y);
+            v[2] += rt.s0.x * pv0.x + rt.s0.y * pv0.y + rt.s1.x * pv1.x + rt.s1.y * pv1.y;
+            v[3] += rt.s0.x * pv0.y - rt.s0.y * pv0.x + rt.s1.x * pv1.y - rt.s1.y * pv1.x;
+            r[0] = Sp32{make_float2(float(rt.s0.x), float(rt.s0.y)), make_float2(float(rt.s1.x), float(rt.s1.y))};
+          }
+          pc_apply<NW, 1, false>(a, S, nullptr, tile * per, own, loc, val, jj, r, z);
+          if (val[0]) {
+            stf4(st.r, i, r[0]);
+            stf4(st.z, i, z[0]);
+            hs32<P>(a.halo_z, i, z[0]);
+            v[1] += double(rdotf(r[0], z[0]));
+          }
+          __syncthreads();
+        }
+        v2_publish<4>(v, a.partials, parity, sh);
+        if (!grid_sync2(a.bar, epoch, a.spin_limit)) goto timeout;
+      }
+      double tr[4];
+      v2_total<4>(a.partials, parity, tr, sh);
+      parity ^= 1;
+      nru++;
+      mu_true = tr[0];
+      if (mu_true < a.tol2 * bnorm2) {
+        status = QED3_OK;
+        break;
+      }
+      if (iter >= a.maxiter || !isfinite(mu_true) || !(tr[1] > 0.0)) {
+        status = QED3_ERR_NOCONV;
+        break;
+      }
+      beta = tr[1] / rho;
+      a_z = make_double2(1.0 - beta * tr[2] / tr[1], -beta * tr[3] / tr[1]);
+      rho = tr[1];
+      mu_max = mu_true;
+    }
+  finish:
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+      a.scal[0] = mu_true;
+      a.scal[1] = bnorm2;
+      a.scal[2] = iter;
+      a.scal[3] = nru;
+      a.scal[4] = status;
+      a.scal[5] = 0;
+    }
+    return;
+  }
+timeout:
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    a.scal[4] = QED3_ERR_TIMEOUT;
+    a.scal[5] = 0;
+  }
+}
+
+// ---------------------------------------------------------------------------
 // Pipelined preconditioned CG: ONE grid barrier per iteration
 // ---------------------------------------------------------------------------
 // Ghysels & Vanroose's pipelined PCG (u = N r, w = A u, s = A p, q = N s,
@@ -891,10 +1145,16 @@ static const void* pcg_kernel(int prec, int nw, int spt) {
   return spt == 1 ? pcg_fn<PBF16, 3, 1>() : pcg_fn<PBF16, 3, 2>();
 }
 
+// The preconditioner's block partition: one block per SM while a block fits
+// the register-resident solver (<= 1152 sites), else tiles of <= 576 sites,
+// k per SM, for the streaming solver.  Training and solver share it.
 int pcg_block_sites(int Ns, int sm_count) {
   const long long per_sm = (Ns + sm_count - 1) / sm_count;
   if (per_sm <= 576) return int((per_sm + 31) / 32 * 32);
-  return int((per_sm + 63) / 64 * 64);
+  if (per_sm <= 1152) return int((per_sm + 63) / 64 * 64);
+  const long long k = (per_sm + 575) / 576;
+  const long long per = (Ns + k * sm_count - 1) / (k * sm_count);
+  return int((per + 31) / 32 * 32);
 }
 
 static const void* ppcg_kernel(int prec, int nw) {
@@ -951,6 +1211,33 @@ bool pcg_plan(int prec, int nw, int Ns, int per, int sm_count, int* grid, int* t
   return false;
 }
 
+static const void* pcgs_kernel(int prec, int nw) {
+  if (prec == QED3_PREC_F32) return nw == 7 ? (const void*)k_pcgs<P32, 7> : (const void*)k_pcgs<P32, 3>;
+  return nw == 7 ? (const void*)k_pcgs<PBF16, 7> : (const void*)k_pcgs<PBF16, 3>;
+}
+
+// The streaming kernel: per threads (one site of the current tile each), the
+// preconditioner fields in shared memory, one block per SM.
+static bool pcgs_plan(int prec, int nw, int Ns, int per, int sm_count, int* grid, size_t* smem) {
+  if (per % 32 || per > 576) return false;
+  const void* fn = pcgs_kernel(prec, nw);
+  const size_t sm = size_t(nw) * per * sizeof(float4);
+  if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(sm)) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  int per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, per, sm) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  if (per_sm < 1) return false;
+  const int tiles = (Ns + per - 1) / per;
+  *grid = std::min(tiles, sm_count);
+  *smem = sm;
+  return true;
+}
+
 int pcg_solve(qed3_dirac_s* d, qed3_lpc_s* L, double* x, const double* b, const qed3_solve_params* prm,
               qed3_solve_report* rep, cudaStream_t st) {
   if (!d->coeffs_set) return fail(QED3_ERR_STATE, "operator coefficients not set (call qed3_dirac_set_links)");
@@ -974,8 +1261,13 @@ int pcg_solve(qed3_dirac_s* d, qed3_lpc_s* L, double* x, const double* b, const 
   int grid = 0, threads = 0, spt = 0;
   size_t smem = 0;
   const bool pipelined = want_pipe && ppcg_plan(prec, co.nwords, d->Ns, L->per, d->sm_count, &grid, &smem);
-  if (!pipelined && !pcg_plan(prec, co.nwords, d->Ns, L->per, d->sm_count, &grid, &threads, &spt, &smem))
-    return fail(QED3_ERR_ARG, "lattice too large for the register-resident preconditioned solver");
+  bool streaming = false;
+  if (!pipelined && !pcg_plan(prec, co.nwords, d->Ns, L->per, d->sm_count, &grid, &threads, &spt, &smem)) {
+    if (flexible) return fail(QED3_ERR_ARG, "flexible preconditioned CG needs the register-resident solver (n <= ~93)");
+    if (!pcgs_plan(prec, co.nwords, d->Ns, L->per, d->sm_count, &grid, &smem))
+      return fail(QED3_ERR_ARG, "no preconditioned solver layout for this lattice and block size");
+    streaming = true;
+  }
   if ((rc = field_import_unit(d, w.b, b, w.partials, w.scal + 6, st))) return rc;
   if (pipelined) QED3_CUDA_TRY(cudaMemsetAsync(w.xhi, 0, size_t(d->Ns) * 4 * sizeof(double), st));
   QED3_CUDA_TRY(cudaMemsetAsync(w.bar2, 0, sizeof(GridBar2), st));
@@ -1009,8 +1301,13 @@ int pcg_solve(qed3_dirac_s* d, qed3_lpc_s* L, double* x, const double* b, const 
   a.halo_q = w.xlo;
   void* kargs[] = {&a};
   QED3_CUDA_TRY(cudaEventRecord(w.e0, st));
+  PcgsState ss{reinterpret_cast<float4*>(w.tg), reinterpret_cast<float4*>(w.p), reinterpret_cast<float4*>(w.rhi),
+               reinterpret_cast<float4*>(w.rg), reinterpret_cast<float4*>(w.xlo)};
+  void* sargs[] = {&a, &ss};
   if (pipelined)
     QED3_CUDA_TRY(cudaLaunchCooperativeKernel(ppcg_kernel(prec, co.nwords), dim3(grid), dim3(L->per), kargs, smem, st));
+  else if (streaming)
+    QED3_CUDA_TRY(cudaLaunchCooperativeKernel(pcgs_kernel(prec, co.nwords), dim3(grid), dim3(L->per), sargs, smem, st));
   else
     QED3_CUDA_TRY(
         cudaLaunchCooperativeKernel(pcg_kernel(prec, co.nwords, spt), dim3(grid), dim3(threads), kargs, smem, st));
