@@ -487,6 +487,14 @@ int qed3_overlap_project_low_modes(qed3_overlap* ov, int nev, double tol, int ma
  * true-residual certificates) in one persistent batched launch, the
  * right-hand side broadcast; poles too ill-conditioned for FP32 inner
  * iterations (condition above 2e5) run in FP64 in a second launch. */
+/* Massive overlap D(m) = (1 - m/2) D_ov + m, m in [0, 2) (no counterpart in
+ * the reference, whose Overlap is massless): qed3_overlap_apply returns
+ * D(m), D(m)^dag and D(m)^dag D(m) = (1 - m^2/4)(D_ov + D_ov^dag) + m^2, and
+ * the outer solves invert the latter.  The massless D_ov^dag D_ov is
+ * singular on configurations with topological charge (|Q| exact zero modes)
+ * and has near-zero modes at strong coupling; the mass bounds its spectrum
+ * below by m^2.  qed3_overlap_force refuses a nonzero mass. */
+int qed3_overlap_set_mass(qed3_overlap* ov, double mass);
 #define QED3_POLES_MULTISHIFT 0
 #define QED3_POLES_BATCHED 1
 int qed3_overlap_set_pole_solver(qed3_overlap* ov, int mode);

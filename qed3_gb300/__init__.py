@@ -136,6 +136,7 @@ SIGNATURES = [
                                                       ctypes.c_double, vp]),
     ("qed3_overlap_low_modes_info", ctypes.c_int, [vp, c_int_p, c_double_p, c_int_p, vp]),
     ("qed3_overlap_set_pole_solver", ctypes.c_int, [vp, ctypes.c_int]),
+    ("qed3_overlap_set_mass", ctypes.c_int, [vp, ctypes.c_double]),
     ("qed3_multishift_solve", ctypes.c_int, [vp, ctypes.c_int, vp, vp, vp, ctypes.c_double, ctypes.c_int, vp,
                                              ctypes.POINTER(ctypes.c_float), vp]),
     ("qed3_dirac_ext_create", ctypes.c_int, [vp, ctypes.c_double, ctypes.c_double, ctypes.c_int, ctypes.c_double,
@@ -884,6 +885,10 @@ class Overlap:
         function; the Zolotarev range then starts above them (nev = 0: off)."""
         _check(lib().qed3_overlap_project_low_modes(self._h, nev, tol, maxsteps, margin, _stream(stream)))
         return self.low_modes_info()
+
+    def set_mass(self, mass: float):
+        """D(m) = (1 - m/2) D_ov + m for apply and the outer solves (0: massless)."""
+        _check(lib().qed3_overlap_set_mass(self._h, mass))
 
     def set_pole_solver(self, mode: int):
         """POLES_MULTISHIFT (FP64 multi-shift CG, default) or POLES_BATCHED

@@ -868,6 +868,13 @@ int qed3_overlap_project_low_modes(qed3_overlap* ov, int nev, double tol, int ma
   QED3_GUARD_END
 }
 
+int qed3_overlap_set_mass(qed3_overlap* ov, double mass) {
+  QED3_GUARD_BEGIN
+  if (!ov) return fail(QED3_ERR_ARG, "NULL argument");
+  return overlap_set_mass(ov, mass);
+  QED3_GUARD_END
+}
+
 int qed3_overlap_set_pole_solver(qed3_overlap* ov, int mode) {
   QED3_GUARD_BEGIN
   if (!ov) return fail(QED3_ERR_ARG, "NULL argument");

@@ -245,7 +245,7 @@ void tri_vectors(const std::vector<double>& a, const std::vector<double>& b, int
 // the Ritz value at the opposite end.
 static int lanczos_core(long long nd, const std::function<int(double*, const double*)>& apply, int nv, bool largest,
                         double tol, int maxsteps, bool require, double** vec_out, std::vector<double>& theta,
-                        double* extreme, int* steps_used, cudaStream_t st) {
+                        double* extreme, int* steps_used, cudaStream_t st, bool* conv_out = nullptr) {
   const int nev = nv - 1;
   if (nv < 1 || maxsteps < nv + 2 || !(tol > 0)) return fail(QED3_ERR_ARG, "low modes: bad Lanczos arguments");
   const long long nc = nd / 2;
@@ -375,6 +375,7 @@ static int lanczos_core(long long nd, const std::function<int(double*, const dou
     *extreme = tmax;
     *steps_used = m;
     *vec_out = Y;
+    if (conv_out) *conv_out = conv;
     return QED3_OK;
   };
   const int rc = body();
@@ -421,8 +422,8 @@ int lanczos_lowmodes(long long nd, const std::function<int(double*, const double
   double* Y = nullptr;
   std::vector<double> th_out;
   double res_out = 0, next_out = 0;
-  for (int attempt = 0; attempt < 6; attempt++) {
-    if (!(a < b)) {
+  for (int attempt = 0; attempt < 10; attempt++) {
+    if (!(a > 0 && a < b)) {
       rc = fail(QED3_ERR_NOCONV, "low modes: no spectral gap for the filter");
       break;
     }
@@ -451,12 +452,29 @@ int lanczos_lowmodes(long long nd, const std::function<int(double*, const double
     double qmin = 0;
     int qsteps = 0;
     double* Yq = nullptr;
-    rc = lanczos_core(nd, filt, nev + 1, true, tol, std::min(maxsteps, 8 * (nev + 1) + 200), true, &Yq, qth, &qmin,
-                      &qsteps, st);
+    bool conv = false;
+    rc = lanczos_core(nd, filt, nev + 1, true, tol, std::min(maxsteps, 8 * (nev + 1) + 200), false, &Yq, qth, &qmin,
+                      &qsteps, st, &conv);
     total_steps += qsteps * deg;
     if (rc) {
       if (Yq) cudaFree(Yq);
       break;
+    }
+    if (!conv) {
+      // Too many modes amplified for the step budget: move the cut down to an
+      // upper bound of the (nev+1)-th eigenvalue read off the filtered Ritz
+      // values (a Ritz value of q(A) is a lower bound of its eigenvalue, so the
+      // inverse map x = (a + b - L (b - a)) / 2, L = cosh(acosh(q) / deg), bounds
+      // the eigenvalue of A from above), at least halving it.
+      cudaFree(Yq);
+      double anew = 0.5 * a;
+      if (qth[nev] > 1.0) {
+        const double L = std::cosh(std::acosh(qth[nev]) / deg);
+        anew = std::min(anew, 1.5 * 0.5 * (a + b - L * (b - a)));
+      }
+      a = anew;
+      rc = QED3_OK;
+      continue;
     }
     // Rayleigh quotients and residuals with A, ascending
     std::vector<double> ray(nev + 1), res(nev + 1);

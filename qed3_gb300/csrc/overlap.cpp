@@ -39,6 +39,7 @@ struct qed3_overlap_s {
   int nh = 0, nlo = 0;               // current split
   bool multishift = true;            // all poles through the FP64 multi-shift CG (false: batched launches)
   bool certify_poles = true;         // FP64 true residual of every pole after each multi-shift solve
+  double mass = 0.0;                 // D(m) = (1 - m/2) D_ov + m
   double* Z = nullptr;     // [npoles][2 Ns] complex
   double* y = nullptr;     // [2 Ns] complex
   double* w = nullptr;
@@ -389,8 +390,9 @@ static int pole_solves(qed3_overlap_s* ov, const double* rhs, double* out, doubl
   return fail(w.status, "a pole solve did not converge");
 }
 
-int overlap_apply(qed3_overlap_s* ov, int op, double* out, const double* in, double tol, qed3_solve_report* rep,
-                  cudaStream_t st) {
+// The massless products (D_ov, D_ov^dag, D_ov + D_ov^dag).
+static int overlap_apply_massless(qed3_overlap_s* ov, int op, double* out, const double* in, double tol,
+                                  qed3_solve_report* rep, cudaStream_t st) {
   if (!ov->ready) return fail(QED3_ERR_STATE, "call qed3_overlap_update first");
   qed3_dirac_s* d = ov->d;
   const long long nd = 4LL * d->Ns;
@@ -447,6 +449,25 @@ int overlap_apply(qed3_overlap_s* ov, int op, double* out, const double* in, dou
   return QED3_OK;
 }
 
+// With a mass m: D(m) = (1 - m/2) D_ov + m, and by the Ginsparg-Wilson
+// relation D_ov^dag D_ov = D_ov + D_ov^dag,
+//   D(m)^dag D(m) = (1 - m^2/4) (D_ov + D_ov^dag) + m^2.
+int overlap_apply(qed3_overlap_s* ov, int op, double* out, const double* in, double tol, qed3_solve_report* rep,
+                  cudaStream_t st) {
+  int rc = overlap_apply_massless(ov, op, out, in, tol, rep, st);
+  if (rc || ov->mass == 0.0) return rc;
+  const long long nd = 4LL * ov->d->Ns;
+  const double m = ov->mass;
+  if (op == QED3_OP_D || op == QED3_OP_DDAG) return vec_axpby(nd, 1.0 - 0.5 * m, out, m, in, out, st);
+  return vec_axpby(nd, 1.0 - 0.25 * m * m, out, m * m, in, out, st);
+}
+
+int overlap_set_mass(qed3_overlap_s* ov, double m) {
+  if (!(m >= 0.0 && m < 2.0)) return fail(QED3_ERR_ARG, "overlap mass must be in [0, 2)");
+  ov->mass = m;
+  return QED3_OK;
+}
+
 // Overlap pseudofermion force for all links at once (Overlap::precalc_grad +
 // grad_deviceAsyncLaunch, src/both_3d/overlap.h:393-470, which loops over
 // links with one sparse product and dot per pole and link):
@@ -460,6 +481,7 @@ int overlap_force(qed3_overlap_s* ov, const double* eta, double* F, double tol, 
   if (ov->nev > 0)
     return fail(QED3_ERR_STATE, "the overlap force is for the unprojected sign function: switch the low-mode "
                                 "projection off (nev = 0) first");
+  if (ov->mass != 0.0) return fail(QED3_ERR_STATE, "the overlap force is for the massless operator (mass 0)");
   qed3_dirac_s* d = ov->d;
   const int Ns = d->Ns;
   const long long nd = 4LL * Ns;
@@ -559,10 +581,11 @@ int overlap_solve(qed3_overlap_s* ov, double* x, const double* b, double tol, do
     int e;
     if (c == 0) {
       e = overlap_apply(ov, QED3_OP_DDAGD, out, v, tin, &ir, st);
-    } else {
-      e = overlap_apply(ov, QED3_OP_D, out, v, tin, &ir, st);
+    } else {  // (1 - m^2/4) 2 P_c D_ov P_c + m^2 on sector c
+      const double m = ov->mass;
+      e = overlap_apply_massless(ov, QED3_OP_D, out, v, tin, &ir, st);
       if (!e) e = chiral(nd, c, out, out, st);
-      if (!e) e = vec_axpby(nd, 2.0, out, 0.0, out, out, st);
+      if (!e) e = vec_axpby(nd, 2.0 * (1.0 - 0.25 * m * m), out, m * m, v, out, st);
     }
     inner_max = std::max(inner_max, ir.iters);
     return e;

@@ -18,6 +18,7 @@ int overlap_solve(qed3_overlap_s* ov, double* x, const double* b, double tol, do
 int overlap_project_low_modes(qed3_overlap_s* ov, int nev, double tol, int maxsteps, double margin,
                               cudaStream_t st);
 int overlap_set_pole_solver(qed3_overlap_s* ov, int mode);
+int overlap_set_mass(qed3_overlap_s* ov, double m);
 int overlap_low_modes_info(const qed3_overlap_s* ov, int* nev, double* max_residual, int* lanczos_steps,
                            double* mu);
 qed3_dirac_s* overlap_dirac(qed3_overlap_s* ov);
