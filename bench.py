@@ -646,6 +646,14 @@ def overlap_config(torch, Q, dev, nev=48):
     out["projected"]["apply_D_ms"] = 1e3 * _wall(torch, lambda: reps.append(ov.apply(y, xi, Q.OP_D,
                                                                                    tol_inner=1e-12)), 3)
     out["projected"]["pole_iters"] = reps[-1].iters
+    # the same product with every pole its own mixed-precision CG (FP32 iterations,
+    # FP64 reliable updates and certificates) in one batched launch
+    ov.set_pole_solver(Q.POLES_BATCHED)
+    reps = []
+    out["projected"]["apply_D_ms_batched_mixed"] = 1e3 * _wall(
+        torch, lambda: reps.append(ov.apply(y, xi, Q.OP_D, tol_inner=1e-12)), 3)
+    out["projected"]["batched_mixed_worst_true_res"] = reps[-1].true_rel_res
+    ov.set_pole_solver(Q.POLES_MULTISHIFT)
     b = torch.empty_like(xi)
     x = torch.zeros_like(b)
     # the massless outer solve within a fixed budget: singular (|Q| zero modes) and ill-conditioned
@@ -812,7 +820,15 @@ def profile_case(torch, which):
         D.update(A)
         b = torch.from_numpy(Q.ParallelRng(lat, 7).gaussian_spinor()).cuda()
         x = torch.zeros_like(b)
-        if which in ("pcg", "ppcg"):  # untrained network: same per-iteration cost as a trained one
+        if which == "pcgs":  # the streaming kernel on an HBM-resident lattice, 200 iterations
+            lat = Q.S2Trivalent(256)
+            D = Q.DiracS2Dual(lat, 1.0, M5)
+            D.update(torch.from_numpy(np.random.default_rng(2).uniform(-np.pi, np.pi, lat.n_links)).cuda())
+            b = torch.from_numpy(Q.ParallelRng(lat, 7).gaussian_spinor()).cuda()
+            x = torch.zeros_like(b)
+            pc = Q.LearnedPreconditioner(D, channels=16, layers=2, seed=1)
+            rep = pc.solve(D, x, b, tol=TOL, precision=Q.PREC_F32, maxiter=200)
+        elif which in ("pcg", "ppcg"):  # untrained network: same per-iteration cost as a trained one
             pc = Q.LearnedPreconditioner(D, channels=16, layers=2, seed=1)
             rep = pc.solve(D, x, b, tol=TOL, precision=Q.PREC_F32, maxiter=300, pipelined=which == "ppcg")
         else:
@@ -837,12 +853,13 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-paths", action="store_true", help="skip the timings of the HMC, overlap and S^2 x S^1 paths")
-    ap.add_argument("--profile", choices=["apply", "cg", "pcg", "ppcg", "batched", "ext", "train"], default=None,
+    ap.add_argument("--profile", choices=["apply", "cg", "pcg", "ppcg", "pcgs", "batched", "ext", "train"], default=None,
                     help="small self-contained case for ncu: 'apply' = D apply at n=512 (f32, bf16, f64; "
                          "HBM-resident), 'cg' = one n=64 mixed-precision solve, 'pcg' = 300 iterations of the "
                          "n=64 preconditioned solve, 'ppcg' = the same with the pipelined one-barrier kernel, "
                          "'batched' = 64 RHS over four lattices, 'ext' = S^2 x S^1 D apply at n=64, Nt=16, "
-                         "'train' = four Adam steps of the n=64 network (tcgen05 channel mixing)")
+                         "'train' = four Adam steps of the n=64 network (tcgen05 channel mixing), 'pcgs' = 200 iterations "
+                         "of the streaming preconditioned solver at n=256")
     args = ap.parse_args()
     rank, world, local = env_rank()
     warmup = max(3, args.warmup)

@@ -540,9 +540,10 @@ timeout:
 // once per site and phase; the operator's hop blocks come through the
 // read-only path).  z = N r is applied tile by tile in shared memory right
 // after the tile's residual update, so an iteration keeps its two grid
-// barriers.  State arrays (internal order): r, p, t and z in FP32 (float4 per
-// site), the gathered copies of z and t in the halo precision, x as an FP32
-// increment folded into FP64 at reliable updates.
+// barriers; the tile's hop blocks are staged in shared memory for the four
+// neighbour passes of N.  State arrays (internal order): r, p, t and z in
+// FP32 (float4 per site), the gathered copies of z and t in the halo
+// precision, x as an FP32 increment folded into FP64 at reliable updates.
 struct PcgsState {
   float4* r;
   float4* p;
@@ -559,6 +560,7 @@ __global__ void __launch_bounds__(576, 1) k_pcgs(PcgArgs a, PcgsState st) {
   extern __shared__ float4 S[];
   __shared__ double sh[32 * 4 + 64 + 8];
   const int Ns = a.Ns, per = a.per;
+  float4* Hs = S + NW * per;  // the tile's own hop blocks of D, read by the preconditioner's passes
   const int ntiles = (Ns + per - 1) / per;
   const Sp64 z64{make_double2(0, 0), make_double2(0, 0)};
   const Sp32 z32{make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
@@ -569,6 +571,12 @@ __global__ void __launch_bounds__(576, 1) k_pcgs(PcgArgs a, PcgsState st) {
     val[0] = own[0] < Ns;
 #pragma unroll
     for (int q = 0; q < 3; q++) jj[0][q] = val[0] ? __ldg(a.nbr + q * Ns + own[0]) : 0;
+    // stage this site's hop blocks for the preconditioner (visible after its first __syncthreads)
+#pragma unroll
+    for (int q = 0; q < 6; q++) {
+      const float4* mh = reinterpret_cast<const float4*>(a.H32 + size_t(q >> 1) * Ns + own[0]) + (q & 1);
+      Hs[q * per + loc[0]] = val[0] ? __ldg(mh) : make_float4(0.f, 0.f, 0.f, 0.f);
+    }
   };
   // ---- phase 0: r = b, z = N r, p = t = x = 0 ---------------------------------------------
   double v2[2] = {0.0, 0.0};
@@ -583,7 +591,7 @@ __global__ void __launch_bounds__(576, 1) k_pcgs(PcgArgs a, PcgsState st) {
       v2[0] += n2(bi);
       r[0] = Sp32{make_float2(float(bi.s0.x), float(bi.s0.y)), make_float2(float(bi.s1.x), float(bi.s1.y))};
     }
-    pc_apply<NW, 1, false>(a, S, nullptr, tile * per, own, loc, val, jj, r, z);
+    pc_apply<NW, 1, true>(a, S, Hs, tile * per, own, loc, val, jj, r, z);
     if (val[0]) {
       stf4(st.r, i, r[0]);
       stf4(st.z, i, z[0]);
@@ -663,7 +671,7 @@ __global__ void __launch_bounds__(576, 1) k_pcgs(PcgArgs a, PcgsState st) {
             r[0] = sp_add(ldf4(st.r, i), sp_add(q, pi, sf), -al);
             stf4(st.xl, i, sp_add(ldf4(st.xl, i), pi, al));
           }
-          pc_apply<NW, 1, false>(a, S, nullptr, tile * per, own, loc, val, jj, r, z);
+          pc_apply<NW, 1, true>(a, S, Hs, tile * per, own, loc, val, jj, r, z);
           if (val[0]) {
             stf4(st.r, i, r[0]);
             stf4(st.z, i, z[0]);
@@ -735,7 +743,7 @@ __global__ void __launch_bounds__(576, 1) k_pcgs(PcgArgs a, PcgsState st) {
             v[3] += rt.s0.x * pv0.y - rt.s0.y * pv0.x + rt.s1.x * pv1.y - rt.s1.y * pv1.x;
             r[0] = Sp32{make_float2(float(rt.s0.x), float(rt.s0.y)), make_float2(float(rt.s1.x), float(rt.s1.y))};
           }
-          pc_apply<NW, 1, false>(a, S, nullptr, tile * per, own, loc, val, jj, r, z);
+          pc_apply<NW, 1, true>(a, S, Hs, tile * per, own, loc, val, jj, r, z);
           if (val[0]) {
             stf4(st.r, i, r[0]);
             stf4(st.z, i, z[0]);
@@ -1217,11 +1225,12 @@ static const void* pcgs_kernel(int prec, int nw) {
 }
 
 // The streaming kernel: per threads (one site of the current tile each), the
-// preconditioner fields in shared memory, one block per SM.
+// preconditioner fields and the tile's hop blocks in shared memory, one block
+// per SM.
 static bool pcgs_plan(int prec, int nw, int Ns, int per, int sm_count, int* grid, size_t* smem) {
   if (per % 32 || per > 576) return false;
   const void* fn = pcgs_kernel(prec, nw);
-  const size_t sm = size_t(nw) * per * sizeof(float4);
+  const size_t sm = size_t(nw + 6) * per * sizeof(float4);
   if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(sm)) != cudaSuccess) {
     cudaGetLastError();
     return false;
