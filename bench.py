@@ -217,6 +217,7 @@ def network_depth_study(torch, Q, lat, D, pc2, dev, seeds=3):
     configuration with several sources."""
     t0 = time.perf_counter()
     pc3 = Q.LearnedPreconditioner(D, channels=16, layers=3, seed=1)
+    pc3.set_tensor_cores(True)  # its 16 -> 16 layers on tcgen05, as the 2-layer network's
     Dt = Q.DiracS2Dual(lat, 1.0, M5)
     betas = (1.0, 1.4, 2.0)
     for c in range(40):

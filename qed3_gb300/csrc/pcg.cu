@@ -534,7 +534,7 @@ timeout:
 // ---------------------------------------------------------------------------
 // Same recurrence, reliable updates and certificate as k_pcg, for lattices
 // whose per-SM share exceeds what one block can hold in registers (about
-// n >= 94): the preconditioner's blocks become tiles of `per` <= 576 sites,
+// n >= 94): the preconditioner's blocks become tiles of `per` <= 512 sites,
 // every block of a persistent one-block-per-SM grid walks its tiles inside
 // each phase, and the solver state lives in global memory (read and written
 // once per site and phase; the operator's hop blocks come through the
@@ -552,11 +552,23 @@ struct PcgsState {
   float4* xl;
 };
 
-__device__ __forceinline__ Sp32 ldf4(const float4* f, int i) { return f42sp(f[i]); }
-__device__ __forceinline__ void stf4(float4* f, int i, const Sp32& v) { f[i] = sp2f4(v); }
+__device__ __forceinline__ Sp32 ldf4(const float4* f, int i) { return f42sp(__ldcg(f + i)); }
+__device__ __forceinline__ void stf4(float4* f, int i, const Sp32& v) { __stcg(f + i, sp2f4(v)); }
+// z and t: with FP32 halos the gathered copy is the FP32 value itself, so the
+// own copy is not stored twice
+template <int P>
+__device__ __forceinline__ Sp32 own_ld(const float4* own, const void* halo, int i) {
+  if constexpr (P == P32) return hl32<P>(halo, i);
+  else return ldf4(own, i);
+}
+template <int P>
+__device__ __forceinline__ void own_st(float4* own, void* halo, int i, const Sp32& v) {
+  hs32<P>(halo, i, v);
+  if constexpr (P != P32) stf4(own, i, v);
+}
 
 template <int P, int NW>
-__global__ void __launch_bounds__(576, 1) k_pcgs(PcgArgs a, PcgsState st) {
+__global__ void __launch_bounds__(512, 1) k_pcgs(PcgArgs a, PcgsState st) {
   extern __shared__ float4 S[];
   __shared__ double sh[32 * 4 + 64 + 8];
   const int Ns = a.Ns, per = a.per;
@@ -594,10 +606,9 @@ __global__ void __launch_bounds__(576, 1) k_pcgs(PcgArgs a, PcgsState st) {
     pc_apply<NW, 1, true>(a, S, Hs, tile * per, own, loc, val, jj, r, z);
     if (val[0]) {
       stf4(st.r, i, r[0]);
-      stf4(st.z, i, z[0]);
-      hs32<P>(a.halo_z, i, z[0]);
+      own_st<P>(st.z, a.halo_z, i, z[0]);
       stf4(st.p, i, z32);
-      stf4(st.t, i, z32);
+      own_st<P>(st.t, a.halo_t, i, z32);
       stf4(st.xl, i, z32);
       hs64(a.x, i, z64);
       v2[1] += double(rdotf(r[0], z[0]));
@@ -625,27 +636,45 @@ __global__ void __launch_bounds__(576, 1) k_pcgs(PcgArgs a, PcgsState st) {
     }
     while (true) {
       // ---- phase A: t = a_z D z + beta t, p = a_z z + beta p ----------------------------
+      // two sites per thread in flight (this tile's and the next one's): all
+      // their loads issue before the first dependent use
       {
         float v[1] = {0.f};
         const float2 az = make_float2(float(a_z.x), float(a_z.y));
         const float bt = float(beta);
-        for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-          const int i = tile * per + threadIdx.x;
-          if (i >= Ns) continue;
-          int jj[3];
+        for (int tile = blockIdx.x; tile < ntiles; tile += 2 * gridDim.x) {
+          int ii[2];
+          bool ok[2];
+          ii[0] = tile * per + threadIdx.x;
+          ii[1] = (tile + gridDim.x) * per + threadIdx.x;
+          ok[0] = ii[0] < Ns;
+          ok[1] = tile + gridDim.x < ntiles && ii[1] < Ns;
+          Sp32 dz[2], zi[2], ti[2], pi[2];
 #pragma unroll
-          for (int q = 0; q < 3; q++) jj[q] = __ldg(a.nbr + q * Ns + i);
-          const Sp32 zi = ldf4(st.z, i);
-          Sp32 ti = ldf4(st.t, i), pi = ldf4(st.p, i);
-          const Sp32 dz = stencil32h<P, false>(i, 0, per, Ns, jj, a.H32, nullptr, __ldg(a.diag32 + i), zi, a.halo_z);
-          ti.s0 = cfmaf(az, dz.s0, make_float2(bt * ti.s0.x, bt * ti.s0.y));
-          ti.s1 = cfmaf(az, dz.s1, make_float2(bt * ti.s1.x, bt * ti.s1.y));
-          pi.s0 = cfmaf(az, zi.s0, make_float2(bt * pi.s0.x, bt * pi.s0.y));
-          pi.s1 = cfmaf(az, zi.s1, make_float2(bt * pi.s1.x, bt * pi.s1.y));
-          stf4(st.t, i, ti);
-          stf4(st.p, i, pi);
-          hs32<P>(a.halo_t, i, ti);
-          v[0] += n2f(ti) + float(s) * n2f(pi);
+          for (int u = 0; u < 2; u++) {
+            if (!ok[u]) continue;
+            const int i = ii[u];
+            int jj[3];
+#pragma unroll
+            for (int q = 0; q < 3; q++) jj[q] = __ldg(a.nbr + q * Ns + i);
+            zi[u] = own_ld<P>(st.z, a.halo_z, i);
+            ti[u] = own_ld<P>(st.t, a.halo_t, i);
+            pi[u] = ldf4(st.p, i);
+            dz[u] = stencil32h<P, false>(i, 0, per, Ns, jj, a.H32, nullptr, __ldg(a.diag32 + i), zi[u], a.halo_z);
+          }
+#pragma unroll
+          for (int u = 0; u < 2; u++) {
+            if (!ok[u]) continue;
+            const int i = ii[u];
+            Sp32 t = ti[u], pp = pi[u];
+            t.s0 = cfmaf(az, dz[u].s0, make_float2(bt * t.s0.x, bt * t.s0.y));
+            t.s1 = cfmaf(az, dz[u].s1, make_float2(bt * t.s1.x, bt * t.s1.y));
+            pp.s0 = cfmaf(az, zi[u].s0, make_float2(bt * pp.s0.x, bt * pp.s0.y));
+            pp.s1 = cfmaf(az, zi[u].s1, make_float2(bt * pp.s1.x, bt * pp.s1.y));
+            own_st<P>(st.t, a.halo_t, i, t);
+            stf4(st.p, i, pp);
+            v[0] += n2f(t) + float(s) * n2f(pp);
+          }
         }
         v2_publish_f<1>(v, a.partials, parity, sh);
         if (!grid_sync2(a.bar, epoch, a.spin_limit)) goto timeout;
@@ -654,28 +683,51 @@ __global__ void __launch_bounds__(576, 1) k_pcgs(PcgArgs a, PcgsState st) {
       v2_total<1>(a.partials, parity, gam, sh);
       parity ^= 1;
       const double alpha = rho / gam[0];
-      // ---- phase B: q = D^dag t + s p, x += alpha p, r -= alpha q, z = N r -------------
+      // ---- phase B1: q = D^dag t + s p, x += alpha p, r -= alpha q (two sites in flight) ------
+      {
+        const float al = float(alpha), sf = float(s);
+        for (int tile = blockIdx.x; tile < ntiles; tile += 2 * gridDim.x) {
+          int ii[2];
+          bool ok[2];
+          ii[0] = tile * per + threadIdx.x;
+          ii[1] = (tile + gridDim.x) * per + threadIdx.x;
+          ok[0] = ii[0] < Ns;
+          ok[1] = tile + gridDim.x < ntiles && ii[1] < Ns;
+          Sp32 q[2], pi[2], ri[2], xl[2];
+#pragma unroll
+          for (int u = 0; u < 2; u++) {
+            if (!ok[u]) continue;
+            const int i = ii[u];
+            int jj[3];
+#pragma unroll
+            for (int k = 0; k < 3; k++) jj[k] = __ldg(a.nbr + k * Ns + i);
+            const Sp32 ti = own_ld<P>(st.t, a.halo_t, i);
+            pi[u] = ldf4(st.p, i);
+            ri[u] = ldf4(st.r, i);
+            xl[u] = ldf4(st.xl, i);
+            q[u] = stencil32h<P, false>(i, 0, per, Ns, jj, a.Hd32, nullptr, __ldg(a.diag32 + i), ti, a.halo_t);
+          }
+#pragma unroll
+          for (int u = 0; u < 2; u++) {
+            if (!ok[u]) continue;
+            stf4(st.r, ii[u], sp_add(ri[u], sp_add(q[u], pi[u], sf), -al));
+            stf4(st.xl, ii[u], sp_add(xl[u], pi[u], al));
+          }
+        }
+      }
+      // ---- phase B2: z = N r tile by tile (each thread reads back its own r) -------------
       {
         float v[2] = {0.f, 0.f};
-        const float al = float(alpha), sf = float(s);
         for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
           int own[1], loc[1], jj[1][3];
           bool val[1];
           site(tile, own, loc, val, jj);
           const int i = own[0];
           Sp32 r[1] = {z32}, z[1];
-          if (val[0]) {
-            const Sp32 ti = ldf4(st.t, i), pi = ldf4(st.p, i);
-            const Sp32 q = stencil32h<P, false>(i, 0, per, Ns, jj[0], a.Hd32, nullptr, __ldg(a.diag32 + i), ti,
-                                                a.halo_t);
-            r[0] = sp_add(ldf4(st.r, i), sp_add(q, pi, sf), -al);
-            stf4(st.xl, i, sp_add(ldf4(st.xl, i), pi, al));
-          }
+          if (val[0]) r[0] = ldf4(st.r, i);
           pc_apply<NW, 1, true>(a, S, Hs, tile * per, own, loc, val, jj, r, z);
           if (val[0]) {
-            stf4(st.r, i, r[0]);
-            stf4(st.z, i, z[0]);
-            hs32<P>(a.halo_z, i, z[0]);
+            own_st<P>(st.z, a.halo_z, i, z[0]);
             v[0] += n2f(r[0]);
             v[1] += rdotf(r[0], z[0]);
           }
@@ -746,8 +798,7 @@ __global__ void __launch_bounds__(576, 1) k_pcgs(PcgArgs a, PcgsState st) {
           pc_apply<NW, 1, true>(a, S, Hs, tile * per, own, loc, val, jj, r, z);
           if (val[0]) {
             stf4(st.r, i, r[0]);
-            stf4(st.z, i, z[0]);
-            hs32<P>(a.halo_z, i, z[0]);
+            own_st<P>(st.z, a.halo_z, i, z[0]);
             v[1] += double(rdotf(r[0], z[0]));
           }
           __syncthreads();
@@ -1154,13 +1205,14 @@ static const void* pcg_kernel(int prec, int nw, int spt) {
 }
 
 // The preconditioner's block partition: one block per SM while a block fits
-// the register-resident solver (<= 1152 sites), else tiles of <= 576 sites,
-// k per SM, for the streaming solver.  Training and solver share it.
+// the register-resident solver (<= 1152 sites), else tiles of <= 512 sites,
+// k per SM, for the streaming solver (512 threads: four warps per SM
+// sub-partition, so 128 registers per thread).  Training and solver share it.
 int pcg_block_sites(int Ns, int sm_count) {
   const long long per_sm = (Ns + sm_count - 1) / sm_count;
   if (per_sm <= 576) return int((per_sm + 31) / 32 * 32);
   if (per_sm <= 1152) return int((per_sm + 63) / 64 * 64);
-  const long long k = (per_sm + 575) / 576;
+  const long long k = (per_sm + 511) / 512;
   const long long per = (Ns + k * sm_count - 1) / (k * sm_count);
   return int((per + 31) / 32 * 32);
 }
@@ -1228,7 +1280,7 @@ static const void* pcgs_kernel(int prec, int nw) {
 // preconditioner fields and the tile's hop blocks in shared memory, one block
 // per SM.
 static bool pcgs_plan(int prec, int nw, int Ns, int per, int sm_count, int* grid, size_t* smem) {
-  if (per % 32 || per > 576) return false;
+  if (per % 32 || per > 512) return false;
   const void* fn = pcgs_kernel(prec, nw);
   const size_t sm = size_t(nw + 6) * per * sizeof(float4);
   if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(sm)) != cudaSuccess) {

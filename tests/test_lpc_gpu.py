@@ -341,7 +341,7 @@ def test_pcg_scale_invariance(cuda, flexible):
 @pytest.mark.parametrize("prec", [Q.PREC_F32, Q.PREC_BF16])
 def test_streaming_pcg_n128_certified(cuda, prec):
     """n=128 (327,680 sites): above what the register-resident solver holds,
-    so the preconditioner's blocks become tiles of <= 576 sites walked by a
+    so the preconditioner's blocks become tiles of <= 512 sites walked by a
     persistent grid (k_pcgs).  Trained briefly on pairs of the same lattice;
     certified at 1e-10 and fewer iterations than plain mixed-precision CG."""
     rng = np.random.default_rng(128)
@@ -350,7 +350,7 @@ def test_streaming_pcg_n128_certified(cuda, prec):
     D = Q.DiracS2Dual(lat, 1.0, 0.05)
     D.update(A)
     pc = Q.LearnedPreconditioner(D, channels=16, layers=2, seed=1)
-    assert pc.info()["block_sites"] <= 576
+    assert pc.info()["block_sites"] <= 512
     pc.collect(D, nsrc=4, seed=3, snapshots=(0, 5, 20, 60))
     pc.train(300, batch=8, lr=3e-3, seed=2)
     b = to_dev(rand_spinor(rng, lat.n_sites), cuda)
