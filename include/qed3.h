@@ -286,8 +286,9 @@ int qed3_ext_polyakov(qed3_lattice* lat, int Nt, const double* A, double* P, dou
  * threads and CUDA streams (src/both_3d/overlap.h:309-332,
  * src/both_3d/hmc.h:172-200).  System u solves (D_u^dag D_u + shift) x = b
  * for nrhs[u] right-hand sides; systems may live on different lattices.
- * rhs_tile (1, 2, 4, 8: right-hand sides sharing each stencil read) and
- * threads (128, 256) are chosen by the built-in autotuner when passed as 0.
+ * rhs_tile (right-hand sides sharing each stencil read: 1, 2, 4, 8 held in
+ * one thread's registers; 16, 32 spread over consecutive threads of a warp)
+ * and threads (128, 256) are chosen by the built-in autotuner when passed as 0.
  * ====================================================================== */
 typedef struct qed3_batch_s qed3_batch;
 int qed3_batch_create(int nsys, qed3_dirac* const* ops, const int* nrhs, int precision, int rhs_tile, int threads,

@@ -750,8 +750,9 @@ def hmc_ext(dirac: DiracExt, rng: ParallelRng, A, gsq: float, tmax: float = 1.0,
 class Batch:
     """Several CG systems (lattices, right-hand sides, shifts) in one persistent launch.
 
-    systems: list of (DiracS2Dual, nrhs).  rhs_tile / threads = 0 lets the
-    built-in autotuner choose."""
+    systems: list of (DiracS2Dual, nrhs).  rhs_tile (1, 2, 4, 8: right-hand
+    sides in one thread's registers; 16, 32: spread over the threads of a
+    warp) and threads (128, 256) = 0 let the built-in autotuner choose."""
 
     def __init__(self, systems, precision: int = PREC_F32, rhs_tile: int = 0, threads: int = 0):
         self.systems = list(systems)

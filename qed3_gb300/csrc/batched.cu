@@ -32,6 +32,7 @@
 #include "device.cuh"
 #include "dirac_impl.h"
 #include "handles.h"
+#include "v2_common.cuh"
 
 namespace qed3 {
 
@@ -98,8 +99,8 @@ __device__ __forceinline__ double* part_ptr(double* base, int parity, int R3) {
 // without a register cap the kernel takes 128 registers and four 128-thread
 // blocks per SM, and the grid-strided site loops are latency bound.  Capping
 // at 64 registers (1024 / T blocks of T threads per SM) for tiles up to 4
-// doubles the resident warps; measured on the 256-RHS multi-lattice batch:
-// 154 ms (tile 1) vs 188 ms for the best uncapped shape.
+// doubles the resident warps (measured the faster shape on the 256-RHS
+// multi-lattice batch).
 template <int P, int R, int T>
 __global__ void __launch_bounds__(T, (R <= 4 ? 1024 / T : 1)) k_batched_cg(BatchArgs a) {
   __shared__ double sh[32 * 3 * R];
@@ -527,11 +528,390 @@ __global__ void __launch_bounds__(T, (R <= 4 ? 1024 / T : 1)) k_batched_cg(Batch
 }
 
 // ---------------------------------------------------------------------------
+// Wide variant: right-hand sides across threads
+// ---------------------------------------------------------------------------
+// Same phases, reliable updates, reductions and state machine as
+// k_batched_cg, with the R (8, 16 or 32) right-hand sides of a system spread
+// over R consecutive threads instead of a register loop: thread t owns
+// right-hand side r = t % R of the sites slot, slot + T/R, ...  Each hop block
+// is then read once for R right-hand sides (a broadcast within the R threads)
+// and a neighbour's R spinors are one contiguous gather, while every thread
+// keeps the scalar state of one right-hand side only.  Per-right-hand-side
+// decisions that steer the whole system (start, reliable update, done) are
+// OR-ed across the block; all blocks of a system see the same totals, so they
+// take the same transitions.
+template <int P, int R, int T>
+__global__ void __launch_bounds__(T, 512 / T) k_batched_wide(BatchArgs a) {
+  static_assert(32 % R == 0 && T % 32 == 0, "R divides the warp");
+  constexpr int SL = T / R;  // site slots per block
+  __shared__ double red[T / 32][3 * R];
+  __shared__ double tot[3 * R];
+  const int sidx = a.sys_of_block[blockIdx.x];
+  const BatchSys& S = a.sys[sidx];
+  const int Ns = S.Ns, nr = S.nrhs;
+  const int lb = blockIdx.x - S.blk0, nb = S.blk1 - S.blk0;
+  const int r = threadIdx.x % R, slot = threadIdx.x / R;
+  const int i0 = lb * SL + slot, istep = nb * SL;
+  const bool mine = r < nr;  // this thread's right-hand side exists
+  constexpr bool mixed = (P != P64);
+  using Lo = typename LoField<P == P64 ? P32 : P>::T;
+
+  S64* r64 = reinterpret_cast<S64*>(S.r);
+  S64* p64 = reinterpret_cast<S64*>(S.p);
+  S64* t64w = reinterpret_cast<S64*>(S.t);
+  float4* r32 = reinterpret_cast<float4*>(S.r);
+  float4* t32 = reinterpret_cast<float4*>(S.t);
+  Lo* rh = reinterpret_cast<Lo*>(P == PBF16 ? S.rh : S.r);
+  Lo* th = reinterpret_cast<Lo*>(P == PBF16 ? S.th : S.t);
+  float4* p32 = reinterpret_cast<float4*>(S.p);
+  float4* xlo = reinterpret_cast<float4*>(S.xlo);
+  S64* xa = S.xhi;
+  S64* xb = S.xhi2;
+
+  double mu = 0, mu_max = 0, beta = 0, bnorm2 = 0, alpha = 0, mu_true = 0;
+  double2 a_r = make_double2(1.0, 0.0);
+  int active = mine, status = QED3_ERR_NOCONV, it_done = 0;
+  int iter = 0, nru = 0, state = ST_INIT, xsel = 0;
+  unsigned int gen = 0;
+  int parity = 0;
+  const double tol2 = a.tol2, delta2 = a.delta2, shift = mine ? S.shift[r] : 0.0;
+
+  while (true) {
+    double v[3] = {0.0, 0.0, 0.0};
+    const int st = state;
+    // ======================= phase work (site i, right-hand side r) ==========
+    if (st == ST_INIT) {
+      if (mine)
+        for (int i = i0; i < Ns; i += istep) {
+          const int e = i * R + r;
+          const Sp64 bi = ld64(S.b, e);
+          v[0] += n2(bi);
+          const Sp64 z{make_double2(0, 0), make_double2(0, 0)};
+          st64(xa, e, z);
+          if constexpr (!mixed) {
+            st64(r64, e, bi);
+            st64(p64, e, z);
+            st64(t64w, e, z);
+          } else {
+            const Sp32 bl{make_float2(float(bi.s0.x), float(bi.s0.y)), make_float2(float(bi.s1.x), float(bi.s1.y))};
+            const Sp32 zl{make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
+            st32(r32, e, bl);
+            st32(t32, e, zl);
+            if constexpr (P == PBF16) {
+              stbf(reinterpret_cast<uint2*>(rh), e, bl);
+              stbf(reinterpret_cast<uint2*>(th), e, zl);
+            }
+            st32(p32, e, zl);
+            st32(xlo, e, zl);
+          }
+        }
+    } else if (st == ST_A) {
+      if (active)
+        for (int i = i0; i < Ns; i += istep) {
+          const int jj[3] = {__ldg(S.nbr + i), __ldg(S.nbr + Ns + i), __ldg(S.nbr + 2 * Ns + i)};
+          const int e = i * R + r;
+          if constexpr (!mixed) {
+            const M64 m[3] = {S.H[i], S.H[Ns + i], S.H[2 * Ns + i]};
+            const double dg = __ldg(S.diag + i);
+            const Sp64 self = ld64(r64, e);
+            Sp64 o{cscale(dg, self.s0), cscale(dg, self.s1)};
+#pragma unroll
+            for (int k = 0; k < 3; k++) {
+              const Sp64 bk = ld64(r64, jj[k] * R + r);
+              o.s0 = cfma(m[k].h00, bk.s0, o.s0);
+              o.s0 = cfma(m[k].h01, bk.s1, o.s0);
+              o.s1 = cfma(m[k].h10, bk.s0, o.s1);
+              o.s1 = cfma(m[k].h11, bk.s1, o.s1);
+            }
+            const Sp64 ti = ld64(t64w, e), pi = ld64(p64, e);
+            Sp64 tn, pn;
+            tn.s0 = cfma(a_r, o.s0, cscale(beta, ti.s0));
+            tn.s1 = cfma(a_r, o.s1, cscale(beta, ti.s1));
+            pn.s0 = cfma(a_r, self.s0, cscale(beta, pi.s0));
+            pn.s1 = cfma(a_r, self.s1, cscale(beta, pi.s1));
+            st64(t64w, e, tn);
+            st64(p64, e, pn);
+            v[0] += n2(tn) + shift * n2(pn);
+          } else {
+            const M32 m[3] = {S.H32[i], S.H32[Ns + i], S.H32[2 * Ns + i]};
+            const float dg = __ldg(S.diag32 + i);
+            const Sp32 self = ld32(r32, e);
+            Sp32 o{make_float2(dg * self.s0.x, dg * self.s0.y), make_float2(dg * self.s1.x, dg * self.s1.y)};
+#pragma unroll
+            for (int k = 0; k < 3; k++) {
+              const Sp32 bk = LoField<P>::ld(rh, jj[k] * R + r);
+              o.s0 = cfmaf(make_float2(m[k].r0.x, m[k].r0.y), bk.s0, o.s0);
+              o.s0 = cfmaf(make_float2(m[k].r0.z, m[k].r0.w), bk.s1, o.s0);
+              o.s1 = cfmaf(make_float2(m[k].r1.x, m[k].r1.y), bk.s0, o.s1);
+              o.s1 = cfmaf(make_float2(m[k].r1.z, m[k].r1.w), bk.s1, o.s1);
+            }
+            const Sp32 ti = ld32(t32, e), pi = ld32(p32, e);
+            const float2 ar = make_float2(float(a_r.x), float(a_r.y));
+            const float bt = float(beta);
+            Sp32 tn, pn;
+            tn.s0 = cfmaf(ar, o.s0, make_float2(bt * ti.s0.x, bt * ti.s0.y));
+            tn.s1 = cfmaf(ar, o.s1, make_float2(bt * ti.s1.x, bt * ti.s1.y));
+            pn.s0 = cfmaf(ar, self.s0, make_float2(bt * pi.s0.x, bt * pi.s0.y));
+            pn.s1 = cfmaf(ar, self.s1, make_float2(bt * pi.s1.x, bt * pi.s1.y));
+            st32(t32, e, tn);
+            if constexpr (P == PBF16) stbf(reinterpret_cast<uint2*>(th), e, tn);
+            st32(p32, e, pn);
+            v[0] += double(n2f(tn)) + shift * double(n2f(pn));
+          }
+        }
+    } else if (st == ST_B) {
+      if (active)
+        for (int i = i0; i < Ns; i += istep) {
+          const int jj[3] = {__ldg(S.nbr + i), __ldg(S.nbr + Ns + i), __ldg(S.nbr + 2 * Ns + i)};
+          const int e = i * R + r;
+          if constexpr (!mixed) {
+            const M64 m[3] = {S.Hd[i], S.Hd[Ns + i], S.Hd[2 * Ns + i]};
+            const double dg = __ldg(S.diag + i);
+            const Sp64 self = ld64(t64w, e);
+            Sp64 q{cscale(dg, self.s0), cscale(dg, self.s1)};
+#pragma unroll
+            for (int k = 0; k < 3; k++) {
+              const Sp64 bk = ld64(t64w, jj[k] * R + r);
+              q.s0 = cfma(m[k].h00, bk.s0, q.s0);
+              q.s0 = cfma(m[k].h01, bk.s1, q.s0);
+              q.s1 = cfma(m[k].h10, bk.s0, q.s1);
+              q.s1 = cfma(m[k].h11, bk.s1, q.s1);
+            }
+            const Sp64 pi = ld64(p64, e), ri = ld64(r64, e), xi = ld64(xa, e);
+            Sp64 rn, xn;
+            rn.s0 = csub(ri.s0, cscale(alpha, cadd(q.s0, cscale(shift, pi.s0))));
+            rn.s1 = csub(ri.s1, cscale(alpha, cadd(q.s1, cscale(shift, pi.s1))));
+            xn.s0 = cadd(xi.s0, cscale(alpha, pi.s0));
+            xn.s1 = cadd(xi.s1, cscale(alpha, pi.s1));
+            st64(r64, e, rn);
+            st64(xa, e, xn);
+            v[0] += n2(rn);
+          } else {
+            const M32 m[3] = {S.Hd32[i], S.Hd32[Ns + i], S.Hd32[2 * Ns + i]};
+            const float dg = __ldg(S.diag32 + i);
+            const Sp32 self = ld32(t32, e);
+            Sp32 q{make_float2(dg * self.s0.x, dg * self.s0.y), make_float2(dg * self.s1.x, dg * self.s1.y)};
+#pragma unroll
+            for (int k = 0; k < 3; k++) {
+              const Sp32 bk = LoField<P>::ld(th, jj[k] * R + r);
+              q.s0 = cfmaf(make_float2(m[k].r0.x, m[k].r0.y), bk.s0, q.s0);
+              q.s0 = cfmaf(make_float2(m[k].r0.z, m[k].r0.w), bk.s1, q.s0);
+              q.s1 = cfmaf(make_float2(m[k].r1.x, m[k].r1.y), bk.s0, q.s1);
+              q.s1 = cfmaf(make_float2(m[k].r1.z, m[k].r1.w), bk.s1, q.s1);
+            }
+            const Sp32 pi = ld32(p32, e), ri = ld32(r32, e), xi = ld32(xlo, e);
+            const float al = float(alpha), sf = float(shift);
+            Sp32 rn, xn;
+            rn.s0 = make_float2(ri.s0.x - al * (q.s0.x + sf * pi.s0.x), ri.s0.y - al * (q.s0.y + sf * pi.s0.y));
+            rn.s1 = make_float2(ri.s1.x - al * (q.s1.x + sf * pi.s1.x), ri.s1.y - al * (q.s1.y + sf * pi.s1.y));
+            xn.s0 = make_float2(xi.s0.x + al * pi.s0.x, xi.s0.y + al * pi.s0.y);
+            xn.s1 = make_float2(xi.s1.x + al * pi.s1.x, xi.s1.y + al * pi.s1.y);
+            st32(r32, e, rn);
+            if constexpr (P == PBF16) stbf(reinterpret_cast<uint2*>(rh), e, rn);
+            st32(xlo, e, xn);
+            v[0] += double(n2f(rn));
+          }
+        }
+    } else if (st == ST_R1) {
+      // t64 = D (x_hi + x_lo);  x_hi2 = x_hi + x_lo
+      if (mine)
+        for (int i = i0; i < Ns; i += istep) {
+          if (!active) {  // a finished right-hand side keeps its solution across the buffer swap
+            if constexpr (mixed) st64(xb, i * R + r, ld64(xa, i * R + r));
+            continue;
+          }
+          const int jj[3] = {__ldg(S.nbr + i), __ldg(S.nbr + Ns + i), __ldg(S.nbr + 2 * Ns + i)};
+          const M64 m[3] = {S.H[i], S.H[Ns + i], S.H[2 * Ns + i]};
+          const double dg = __ldg(S.diag + i);
+          auto xs = [&](int site) {
+            const int e = site * R + r;
+            const Sp64 h = ld64(xa, e);
+            if constexpr (!mixed) {
+              return h;
+            } else {
+              const Sp32 l = ld32(xlo, e);
+              return Sp64{make_double2(h.s0.x + l.s0.x, h.s0.y + l.s0.y), make_double2(h.s1.x + l.s1.x, h.s1.y + l.s1.y)};
+            }
+          };
+          const Sp64 self = xs(i);
+          st64(xb, i * R + r, self);
+          Sp64 o{cscale(dg, self.s0), cscale(dg, self.s1)};
+#pragma unroll
+          for (int k = 0; k < 3; k++) {
+            const Sp64 bj = xs(jj[k]);
+            o.s0 = cfma(m[k].h00, bj.s0, o.s0);
+            o.s0 = cfma(m[k].h01, bj.s1, o.s0);
+            o.s1 = cfma(m[k].h10, bj.s0, o.s1);
+            o.s1 = cfma(m[k].h11, bj.s1, o.s1);
+          }
+          st64(S.t64, i * R + r, o);
+        }
+    } else if (st == ST_R2) {
+      if (active)
+        for (int i = i0; i < Ns; i += istep) {
+          const int jj[3] = {__ldg(S.nbr + i), __ldg(S.nbr + Ns + i), __ldg(S.nbr + 2 * Ns + i)};
+          const M64 m[3] = {S.Hd[i], S.Hd[Ns + i], S.Hd[2 * Ns + i]};
+          const double dg = __ldg(S.diag + i);
+          const int e = i * R + r;
+          const Sp64 self = ld64(S.t64, e);
+          Sp64 q{cscale(dg, self.s0), cscale(dg, self.s1)};
+#pragma unroll
+          for (int k = 0; k < 3; k++) {
+            const Sp64 bj = ld64(S.t64, jj[k] * R + r);
+            q.s0 = cfma(m[k].h00, bj.s0, q.s0);
+            q.s0 = cfma(m[k].h01, bj.s1, q.s0);
+            q.s1 = cfma(m[k].h10, bj.s0, q.s1);
+            q.s1 = cfma(m[k].h11, bj.s1, q.s1);
+          }
+          const Sp64 bi = ld64(S.b, e), xi = ld64(xa, e);
+          Sp64 rt;
+          rt.s0 = csub(bi.s0, cadd(q.s0, cscale(shift, xi.s0)));
+          rt.s1 = csub(bi.s1, cadd(q.s1, cscale(shift, xi.s1)));
+          v[0] += n2(rt);
+          double2 pv0, pv1;
+          if constexpr (!mixed) {
+            const Sp64 pi = ld64(p64, e);
+            pv0 = pi.s0;
+            pv1 = pi.s1;
+            st64(r64, e, rt);
+          } else {
+            const Sp32 pi = ld32(p32, e);
+            pv0 = make_double2(pi.s0.x, pi.s0.y);
+            pv1 = make_double2(pi.s1.x, pi.s1.y);
+            const Sp32 rl{make_float2(float(rt.s0.x), float(rt.s0.y)), make_float2(float(rt.s1.x), float(rt.s1.y))};
+            st32(r32, e, rl);
+            if constexpr (P == PBF16) stbf(reinterpret_cast<uint2*>(rh), e, rl);
+            st32(xlo, e, Sp32{make_float2(0.f, 0.f), make_float2(0.f, 0.f)});
+          }
+          v[1] += rt.s0.x * pv0.x + rt.s0.y * pv0.y + rt.s1.x * pv1.x + rt.s1.y * pv1.y;
+          v[2] += rt.s0.x * pv0.y - rt.s0.y * pv0.x + rt.s1.x * pv1.y - rt.s1.y * pv1.x;
+        }
+    }
+    // ======================= block partials per right-hand side ===============
+    {
+#pragma unroll
+      for (int q = 0; q < 3; q++)
+#pragma unroll
+        for (int o = R; o < 32; o <<= 1) v[q] += __shfl_xor_sync(0xffffffffu, v[q], o);
+      const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+      if (lane < R)
+#pragma unroll
+        for (int q = 0; q < 3; q++) red[warp][3 * lane + q] = v[q];
+      __syncthreads();
+      if (threadIdx.x < 3 * R) {
+        double acc = 0.0;
+        for (int w = 0; w < T / 32; w++) acc += red[w][threadIdx.x];
+        __stcg(part_ptr(a.partials, parity, 3 * R) + threadIdx.x, acc);
+      }
+    }
+    int all_done = 0;
+    if (!grid_sync_vote(a.bar, gen, a.spin_limit, st == ST_DONE, all_done)) {
+      if (blockIdx.x == S.blk0 && threadIdx.x == 0) a.status[sidx] = QED3_ERR_TIMEOUT;
+      return;
+    }
+    if (all_done) break;
+    if (st == ST_DONE) {
+      parity ^= 1;
+      continue;
+    }
+    // ======================= system totals (fixed order over the system's blocks) ==
+    if (threadIdx.x < 3 * R) {
+      double acc = 0.0;
+      for (int bI = S.blk0; bI < S.blk1; bI++)
+        acc += __ldcg(a.partials + (size_t(parity) * gridDim.x + bI) * (3 * R) + threadIdx.x);
+      tot[threadIdx.x] = acc;
+    }
+    __syncthreads();
+    parity ^= 1;
+    const double t0 = tot[3 * r], t1 = tot[3 * r + 1], t2 = tot[3 * r + 2];
+    // ======================= state transition (identical in all blocks of S) ==
+    if (st == ST_INIT) {
+      int any = 0;
+      if (mine) {
+        bnorm2 = t0;
+        mu = mu_max = mu_true = bnorm2;
+        if (bnorm2 == 0.0) {
+          active = 0;
+          status = QED3_OK;
+        } else {
+          any = 1;
+        }
+      }
+      state = __syncthreads_or(any) ? ST_A : ST_DONE;
+    } else if (st == ST_A) {
+      if (active) alpha = mu / t0;
+      state = ST_B;
+    } else if (st == ST_B) {
+      iter++;
+      int want = iter >= a.maxiter;
+      if (active) {
+        mu_max = fmax(mu_max, t0);
+        if (!isfinite(t0) || !isfinite(alpha) || t0 < tol2 * bnorm2 || (mixed && t0 < delta2 * mu_max)) want = 1;
+      }
+      if (__syncthreads_or(want)) {
+        state = ST_R1;  // reliable update of every right-hand side; mu keeps the norm before this step
+      } else {
+        if (active) {
+          beta = t0 / mu;
+          a_r = make_double2(1.0, 0.0);
+          mu = t0;
+        }
+        state = ST_A;
+      }
+    } else if (st == ST_R1) {
+      if constexpr (mixed) {
+        S64* tmp = xa;
+        xa = xb;
+        xb = tmp;
+        xsel ^= 1;
+      }
+      state = ST_R2;
+    } else if (st == ST_R2) {
+      nru++;
+      int any = 0;
+      if (active) {
+        mu_true = t0;
+        if (t0 < tol2 * bnorm2) {
+          active = 0;
+          status = QED3_OK;
+          it_done = iter;
+        } else if (iter >= a.maxiter || !isfinite(t0)) {
+          active = 0;
+          status = QED3_ERR_NOCONV;
+          it_done = iter;
+        } else {
+          any = 1;
+          const double bt = t0 / mu;
+          beta = bt;
+          a_r = make_double2(1.0 - bt * t1 / t0, -bt * t2 / t0);
+          mu = t0;
+          mu_max = t0;
+        }
+      }
+      state = __syncthreads_or(any) ? ST_A : ST_DONE;
+    }
+    if (state == ST_DONE && blockIdx.x == S.blk0 && slot == 0 && mine) {
+      double* o = S.scal + 6 * r;
+      o[0] = mu_true;
+      o[1] = bnorm2;
+      o[2] = it_done;
+      o[3] = nru;
+      o[4] = status;
+      o[5] = xsel;
+      if (r == 0) a.status[sidx] = QED3_OK;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
 // host side
 // ---------------------------------------------------------------------------
 template <int P, int R>
 static const void* batch_kernel(int threads) {
-  return threads == 128 ? (const void*)k_batched_cg<P, R, 128> : (const void*)k_batched_cg<P, R, 256>;
+  if constexpr (R >= 16)
+    return threads == 128 ? (const void*)k_batched_wide<P, R, 128> : (const void*)k_batched_wide<P, R, 256>;
+  else
+    return threads == 128 ? (const void*)k_batched_cg<P, R, 128> : (const void*)k_batched_cg<P, R, 256>;
 }
 
 template <int P, int R>
@@ -551,7 +931,9 @@ static int occupancy(int threads, int* per_sm) {
   (R == 1 ? fn<P, 1>(__VA_ARGS__)                            \
    : R == 2 ? fn<P, 2>(__VA_ARGS__)                          \
    : R == 4 ? fn<P, 4>(__VA_ARGS__)                          \
-            : fn<P, 8>(__VA_ARGS__))
+   : R == 8 ? fn<P, 8>(__VA_ARGS__)                          \
+   : R == 16 ? fn<P, 16>(__VA_ARGS__)                        \
+             : fn<P, 32>(__VA_ARGS__))
 
 int batch_occupancy(int prec, int R, int threads, int* per_sm) {
   if (prec == QED3_PREC_F64) return QED3_DISPATCH_R(P64, R, occupancy, threads, per_sm);
@@ -659,6 +1041,84 @@ static void batch_release(qed3_batch_s* bt) {
   bt->e0 = bt->e1 = nullptr;
 }
 
+// Splits the launch's blocks over the internal systems in proportion to their
+// expected work: sites x right-hand sides x iterations per right-hand side,
+// the last taken from the previous synchronous solve (1 before the first).
+// All systems advance through the same grid barriers, so a system that needs
+// twice the iterations of the others gets twice their blocks per site and
+// finishes with them instead of running on alone.  At least one block per
+// system and no more blocks than site slots (T sites per block pass, T / R in
+// the wide kernel).  The total is fixed when the batch is built, so a launch
+// captured in a CUDA graph stays valid after a re-split: only the contents of
+// the block-to-system table and the descriptors change.
+static void batch_partition(qed3_batch_s* bt) {
+  const int nsys = int(bt->sys.size());
+  const int slots = bt->R >= 16 ? bt->threads / bt->R : bt->threads;
+  std::vector<long long> maxb(nsys);
+  long long room = 0;
+  for (int i = 0; i < nsys; i++) {
+    maxb[i] = (bt->sys[i].Ns + slots - 1) / slots;
+    room += maxb[i];
+  }
+  if (bt->grid <= 0) bt->grid = int(std::min(bt->cap, room));
+  const long long G = bt->grid;
+  double wsum = 0;
+  for (int i = 0; i < nsys; i++) wsum += double(bt->sys[i].Ns) * bt->sys[i].nrhs * bt->work[i];
+  std::vector<double> ideal(nsys);
+  std::vector<long long> nb(nsys);
+  long long tot = 0;
+  for (int i = 0; i < nsys; i++) {
+    const BatchSys& s = bt->sys[i];
+    ideal[i] = double(G) * double(s.Ns) * s.nrhs * bt->work[i] / wsum;
+    nb[i] = std::max(1LL, std::min((long long)std::floor(ideal[i]), maxb[i]));
+    tot += nb[i];
+  }
+  while (tot > G) {  // trim the allocation furthest above its share
+    int imax = -1;
+    for (int i = 0; i < nsys; i++)
+      if (nb[i] > 1 && (imax < 0 || nb[i] - ideal[i] > nb[imax] - ideal[imax])) imax = i;
+    if (imax < 0) break;
+    nb[imax]--;
+    tot--;
+  }
+  while (tot < G) {  // hand out the rest to the allocation furthest below its share
+    int imin = -1;
+    for (int i = 0; i < nsys; i++)
+      if (nb[i] < maxb[i] && (imin < 0 || nb[i] - ideal[i] < nb[imin] - ideal[imin])) imin = i;
+    if (imin < 0) break;
+    nb[imin]++;
+    tot++;
+  }
+  bt->sob.clear();
+  for (int i = 0; i < nsys; i++) {
+    bt->sys[i].blk0 = int(bt->sob.size());
+    for (long long k = 0; k < nb[i]; k++) bt->sob.push_back(i);
+    bt->sys[i].blk1 = int(bt->sob.size());
+  }
+}
+
+// Re-splits the blocks from the iteration counts of the solve just reported
+// (the scalars already copied to the host) and uploads the new table and
+// descriptors on st.  Called only from the synchronous solve, never while a
+// stream is being captured.
+static int batch_rebalance(qed3_batch_s* bt, const std::vector<double>& scal, cudaStream_t st) {
+  const int R = bt->R, nsys = int(bt->sys.size());
+  std::vector<double> w(nsys);
+  for (int i = 0; i < nsys; i++) {
+    double s = 0;
+    for (int r = 0; r < bt->sys[i].nrhs; r++) s += scal[size_t(6) * R * i + 6 * r + 2];
+    w[i] = 1.0 + s / bt->sys[i].nrhs;
+  }
+  const std::vector<int> old = bt->sob;
+  bt->work = w;
+  batch_partition(bt);
+  if (bt->sob == old) return QED3_OK;
+  QED3_CUDA_TRY(cudaMemcpyAsync(bt->d_sys_of_block, bt->sob.data(), sizeof(int) * bt->sob.size(),
+                                cudaMemcpyHostToDevice, st));
+  QED3_CUDA_TRY(cudaMemcpyAsync(bt->d_sys, bt->sys.data(), sizeof(BatchSys) * nsys, cudaMemcpyHostToDevice, st));
+  return QED3_OK;
+}
+
 static int batch_build(qed3_batch_s* bt) {
   const int R = bt->R;
   bt->sys_uploaded = false;
@@ -690,34 +1150,11 @@ static int batch_build(qed3_batch_s* bt) {
   QED3_CUDA_TRY(cudaDeviceGetAttribute(&smc, cudaDevAttrMultiProcessorCount, dev));
   int rc = batch_occupancy(bt->prec, R, bt->threads, &per_sm);
   if (rc) return rc;
-  const long long cap = (long long)per_sm * smc;
-  if (cap < nsys) return fail(QED3_ERR_ARG, "more systems than co-resident blocks; use a larger right-hand-side tile");
-  // blocks in proportion to work, at least one, at most one thread per site
-  double wsum = 0;
-  for (auto& s : bt->sys) wsum += double(s.Ns) * s.nrhs;
-  std::vector<long long> nb(nsys);
-  long long tot = 0;
-  for (int i = 0; i < nsys; i++) {
-    const long long maxb = (bt->sys[i].Ns + bt->threads - 1) / bt->threads;
-    long long b = (long long)std::floor(double(cap) * double(bt->sys[i].Ns) * bt->sys[i].nrhs / wsum);
-    nb[i] = std::max(1LL, std::min(b, maxb));
-    tot += nb[i];
-  }
-  while (tot > cap) {  // trim the largest allocations
-    int imax = 0;
-    for (int i = 1; i < nsys; i++)
-      if (nb[i] > nb[imax]) imax = i;
-    if (nb[imax] <= 1) break;
-    nb[imax]--;
-    tot--;
-  }
-  std::vector<int> sob;
-  for (int i = 0; i < nsys; i++) {
-    bt->sys[i].blk0 = int(sob.size());
-    for (long long k = 0; k < nb[i]; k++) sob.push_back(i);
-    bt->sys[i].blk1 = int(sob.size());
-  }
-  bt->grid = int(sob.size());
+  bt->cap = (long long)per_sm * smc;
+  if (bt->cap < nsys) return fail(QED3_ERR_ARG, "more systems than co-resident blocks; use a larger right-hand-side tile");
+  bt->work.assign(nsys, 1.0);
+  bt->grid = 0;
+  batch_partition(bt);
   // workspaces
   for (auto& s : bt->sys) {
     const size_t bytes = size_t(s.Ns) * R * sizeof(S64);
@@ -743,9 +1180,9 @@ static int batch_build(qed3_batch_s* bt) {
     bt->sys[i].bnorm = bt->d_scal + size_t(6) * R * nsys + size_t(R) * i;
   }
   QED3_CUDA_TRY(cudaMalloc(&bt->d_sys, sizeof(BatchSys) * nsys));
-  QED3_CUDA_TRY(cudaMalloc(&bt->d_sys_of_block, sizeof(int) * sob.size()));
-  QED3_CUDA_TRY(cudaMemcpy(bt->d_sys_of_block, sob.data(), sizeof(int) * sob.size(), cudaMemcpyHostToDevice));
-  QED3_CUDA_TRY(cudaMalloc(&bt->partials, sizeof(double) * 2 * bt->grid * 3 * R));
+  QED3_CUDA_TRY(cudaMalloc(&bt->d_sys_of_block, sizeof(int) * bt->cap));
+  QED3_CUDA_TRY(cudaMemcpy(bt->d_sys_of_block, bt->sob.data(), sizeof(int) * bt->sob.size(), cudaMemcpyHostToDevice));
+  QED3_CUDA_TRY(cudaMalloc(&bt->partials, sizeof(double) * 2 * bt->cap * 3 * R));
   QED3_CUDA_TRY(cudaMalloc(&bt->bar, sizeof(GridBar)));
   QED3_CUDA_TRY(cudaMalloc(&bt->d_status, sizeof(int) * nsys));
   QED3_CUDA_TRY(cudaEventCreate(&bt->e0));
@@ -851,6 +1288,7 @@ int batch_reports(qed3_batch_s* bt, qed3_solve_report* reports, float ms, cudaSt
   }
   if (timeout) return fail(QED3_ERR_TIMEOUT, "grid barrier timed out inside the batched CG kernel");
   if (missing) return fail(QED3_ERR_STATE, "no completed batched launch to report on");
+  bt->last_scal.swap(scal);
   return QED3_OK;
 }
 
@@ -866,7 +1304,9 @@ int batch_solve(qed3_batch_s* bt, double* const* x, const double* const* b, cons
   float ms = 0.f;
   QED3_CUDA_TRY(cudaEventElapsedTime(&ms, bt->e0, bt->e1));
   if (ms_out) *ms_out = ms;
-  return batch_reports(bt, reports, ms, st);
+  rc = batch_reports(bt, reports, ms, st);
+  if (rc) return rc;
+  return batch_rebalance(bt, bt->last_scal, st);
 }
 
 // ---- autotuner ----------------------------------------------------------------
@@ -922,7 +1362,7 @@ int batch_autotune(qed3_batch_s* proto, int* best_R, int* best_threads, std::vec
   float best = 1e30f;
   int bR = 1, bT = 256;
   qed3_solve_params p{1e-30, 24, proto->prec, 0.1, 0.0, 0};
-  for (int R : {1, 2, 4, 8}) {
+  for (int R : {1, 2, 4, 8, 16, 32}) {
     if (R > 1 && R / 2 >= maxn) break;
     for (int T : {128, 256}) {
       qed3_batch_s trial;
@@ -977,9 +1417,9 @@ int batch_create(int nsys, qed3_dirac_s* const* ops, const int* nrhs, int prec, 
     if (R <= 0) R = aR;
     if (T <= 0) T = aT;
   }
-  if (!(R == 1 || R == 2 || R == 4 || R == 8)) {
+  if (!(R == 1 || R == 2 || R == 4 || R == 8 || R == 16 || R == 32)) {
     delete bt;
-    return fail(QED3_ERR_ARG, "rhs_tile must be 1, 2, 4 or 8");
+    return fail(QED3_ERR_ARG, "rhs_tile must be 1, 2, 4, 8, 16 or 32");
   }
   if (T != 128 && T != 256) {
     delete bt;

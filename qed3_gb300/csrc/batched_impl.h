@@ -9,7 +9,7 @@
 
 namespace qed3 {
 
-constexpr int kMaxTile = 8;  // right-hand sides per system (compile-time tile)
+constexpr int kMaxTile = 32;  // right-hand sides per system (compile-time tile; 16 and 32: the wide kernel)
 
 struct BatchSys {
   int Ns, nrhs, blk0, blk1;
@@ -58,11 +58,15 @@ int batch_export(const BatchSys& s, const qed3_dirac_s* d, double* x_ref, int R,
 // sides, with their workspaces and the block partition of the launch.
 struct qed3_batch_s {
   int prec = 0, R = 1, threads = 256, grid = 0;
+  long long cap = 0;                  // co-resident blocks of the kernel (the partials' size)
   std::vector<qed3_dirac_s*> user_ops;
   std::vector<int> user_nrhs;
   // internal systems
   std::vector<int> owner, first_rhs;  // user system and its first rhs
   std::vector<qed3::BatchSys> sys;
+  std::vector<double> work;           // expected iterations per right-hand side of each system
+  std::vector<int> sob;               // block -> system (host copy of d_sys_of_block)
+  std::vector<double> last_scal;      // per-right-hand-side scalars of the last reported launch
   qed3::BatchSys* d_sys = nullptr;
   int* d_sys_of_block = nullptr;
   double* partials = nullptr;

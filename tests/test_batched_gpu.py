@@ -29,7 +29,7 @@ def _systems(cuda, ns=(2, 4, 8), nrhs=(3, 2, 5), seed=50):
 
 
 @pytest.mark.parametrize("prec", [Q.PREC_F64, Q.PREC_F32, Q.PREC_BF16])
-@pytest.mark.parametrize("tile,threads", [(1, 256), (2, 128), (4, 256), (8, 128)])
+@pytest.mark.parametrize("tile,threads", [(1, 256), (2, 128), (4, 256), (8, 128), (16, 128), (32, 256)])
 def test_batched_multi_lattice(cuda, prec, tile, threads):
     sy = _systems(cuda)
     batch = Q.Batch([(s[3], s[4].shape[0]) for s in sy], precision=prec, rhs_tile=tile, threads=threads)
@@ -54,7 +54,7 @@ def test_batched_multi_lattice(cuda, prec, tile, threads):
 def test_batched_shifts_and_autotune(cuda):
     sy = _systems(cuda, ns=(4, 8), nrhs=(4, 3), seed=51)
     batch = Q.Batch([(s[3], s[4].shape[0]) for s in sy], precision=Q.PREC_F32)  # autotuned
-    assert batch.rhs_tile in (1, 2, 4, 8) and batch.threads in (128, 256)
+    assert batch.rhs_tile in (1, 2, 4, 8, 16, 32) and batch.threads in (128, 256)
     shifts = [np.array([0.0, 0.1, 0.5, 2.0]), np.array([0.03, 0.3, 1.0])]
     bs = [to_dev(s[4], cuda) for s in sy]
     xs = [b.clone() * 0 for b in bs]
