@@ -293,6 +293,17 @@ int qed3_ext_polyakov(qed3_lattice* lat, int Nt, const double* A, double* P, dou
 typedef struct qed3_batch_s qed3_batch;
 int qed3_batch_create(int nsys, qed3_dirac* const* ops, const int* nrhs, int precision, int rhs_tile, int threads,
                       qed3_batch** out);
+/* schedule of the persistent launch: QED3_BATCH_STATIC gives each system a
+ * fixed range of blocks (re-split after every synchronous solve in proportion
+ * to the iterations it took); QED3_BATCH_DYNAMIC cuts every system into tiles
+ * of `threads` sites and hands the tiles of each CG step to whichever block is
+ * free.  0: chosen by the autotuner with the tile and threads (static when
+ * both of those are given). */
+#define QED3_BATCH_STATIC 1
+#define QED3_BATCH_DYNAMIC 2
+int qed3_batch_create2(int nsys, qed3_dirac* const* ops, const int* nrhs, int precision, int rhs_tile, int threads,
+                       int schedule, qed3_batch** out);
+int qed3_batch_schedule(const qed3_batch* bt, int* schedule);
 int qed3_batch_destroy(qed3_batch* bt);
 /* tile and threads the batch runs with */
 int qed3_batch_config(const qed3_batch* bt, int* rhs_tile, int* threads, int* blocks);

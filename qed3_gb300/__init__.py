@@ -38,6 +38,7 @@ SOLVE_FLEXIBLE = 8
 SOLVE_PIPELINED = 16
 OVSOLVE_CHIRAL = 1
 POLES_MULTISHIFT, POLES_BATCHED = 0, 1
+BATCH_STATIC, BATCH_DYNAMIC = 1, 2
 PREC_NAMES = {"f64": PREC_F64, "f32": PREC_F32, "bf16": PREC_BF16}
 BYTES_PER_SITE = {PREC_F64: 32, PREC_F32: 16, PREC_BF16: 8}
 
@@ -171,8 +172,11 @@ SIGNATURES = [
     ("qed3_ext_polyakov", ctypes.c_int, [vp, ctypes.c_int, vp, vp, c_double_p, vp]),
     ("qed3_batch_create", ctypes.c_int, [ctypes.c_int, vp, vp, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                          ctypes.POINTER(vp)]),
+    ("qed3_batch_create2", ctypes.c_int, [ctypes.c_int, vp, vp, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                          ctypes.c_int, ctypes.POINTER(vp)]),
     ("qed3_batch_destroy", ctypes.c_int, [vp]),
     ("qed3_batch_config", ctypes.c_int, [vp, c_int_p, c_int_p, c_int_p]),
+    ("qed3_batch_schedule", ctypes.c_int, [vp, c_int_p]),
     ("qed3_batch_solve", ctypes.c_int, [vp, vp, vp, vp, ctypes.POINTER(SolveParams), vp,
                                         ctypes.POINTER(ctypes.c_float), vp]),
     ("qed3_batch_set_shifts", ctypes.c_int, [vp, vp, ctypes.c_double, vp]),
@@ -751,20 +755,23 @@ class Batch:
     """Several CG systems (lattices, right-hand sides, shifts) in one persistent launch.
 
     systems: list of (DiracS2Dual, nrhs).  rhs_tile (1, 2, 4, 8: right-hand
-    sides in one thread's registers; 16, 32: spread over the threads of a
-    warp) and threads (128, 256) = 0 let the built-in autotuner choose."""
+    sides sharing each stencil read), threads (128, 256) and schedule
+    (BATCH_STATIC: a fixed range of blocks per system; BATCH_DYNAMIC: tiles of
+    `threads` sites handed to free blocks at every CG step) = 0 let the built-in
+    autotuner choose."""
 
-    def __init__(self, systems, precision: int = PREC_F32, rhs_tile: int = 0, threads: int = 0):
+    def __init__(self, systems, precision: int = PREC_F32, rhs_tile: int = 0, threads: int = 0, schedule: int = 0):
         self.systems = list(systems)
         n = len(self.systems)
         ops = (vp * n)(*[s[0].handle for s in self.systems])
         nr = (ctypes.c_int * n)(*[int(s[1]) for s in self.systems])
         h = vp()
-        _check(lib().qed3_batch_create(n, ops, nr, precision, rhs_tile, threads, ctypes.byref(h)))
+        _check(lib().qed3_batch_create2(n, ops, nr, precision, rhs_tile, threads, schedule, ctypes.byref(h)))
         self._h = h
-        R, T, B = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        R, T, B, S = ctypes.c_int(), ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
         _check(lib().qed3_batch_config(h, ctypes.byref(R), ctypes.byref(T), ctypes.byref(B)))
-        self.rhs_tile, self.threads, self.blocks = R.value, T.value, B.value
+        _check(lib().qed3_batch_schedule(h, ctypes.byref(S)))
+        self.rhs_tile, self.threads, self.blocks, self.schedule = R.value, T.value, B.value, S.value
 
     def solve(self, xs, bs, shifts=None, tol: float = 1e-10, maxiter: int = 100000, precision: int = PREC_F32,
               delta: float = 0.1, stream=None):

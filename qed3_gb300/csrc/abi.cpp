@@ -747,6 +747,24 @@ int qed3_batch_create(int nsys, qed3_dirac* const* ops, const int* nrhs, int pre
   QED3_GUARD_END
 }
 
+int qed3_batch_create2(int nsys, qed3_dirac* const* ops, const int* nrhs, int precision, int rhs_tile, int threads,
+                       int schedule, qed3_batch** out) {
+  QED3_GUARD_BEGIN
+  if (!out || !ops || !nrhs || nsys < 1) return fail(QED3_ERR_ARG, "bad argument");
+  if (precision < 0 || precision > 2) return fail(QED3_ERR_ARG, "unknown precision");
+  for (int u = 0; u < nsys; u++)
+    if (!ops[u] || nrhs[u] < 1) return fail(QED3_ERR_ARG, "each system needs an operator and >= 1 rhs");
+  *out = nullptr;
+  return batch_create(nsys, ops, nrhs, precision, rhs_tile, threads, out, schedule);
+  QED3_GUARD_END
+}
+
+int qed3_batch_schedule(const qed3_batch* bt, int* schedule) {
+  if (!bt || !schedule) return fail(QED3_ERR_ARG, "NULL argument");
+  *schedule = bt->sched;
+  return QED3_OK;
+}
+
 int qed3_batch_destroy(qed3_batch* bt) {
   batch_destroy(bt);
   return QED3_OK;

@@ -32,7 +32,6 @@
 #include "device.cuh"
 #include "dirac_impl.h"
 #include "handles.h"
-#include "v2_common.cuh"
 
 namespace qed3 {
 
@@ -528,390 +527,11 @@ __global__ void __launch_bounds__(T, (R <= 4 ? 1024 / T : 1)) k_batched_cg(Batch
 }
 
 // ---------------------------------------------------------------------------
-// Wide variant: right-hand sides across threads
-// ---------------------------------------------------------------------------
-// Same phases, reliable updates, reductions and state machine as
-// k_batched_cg, with the R (8, 16 or 32) right-hand sides of a system spread
-// over R consecutive threads instead of a register loop: thread t owns
-// right-hand side r = t % R of the sites slot, slot + T/R, ...  Each hop block
-// is then read once for R right-hand sides (a broadcast within the R threads)
-// and a neighbour's R spinors are one contiguous gather, while every thread
-// keeps the scalar state of one right-hand side only.  Per-right-hand-side
-// decisions that steer the whole system (start, reliable update, done) are
-// OR-ed across the block; all blocks of a system see the same totals, so they
-// take the same transitions.
-template <int P, int R, int T>
-__global__ void __launch_bounds__(T, 512 / T) k_batched_wide(BatchArgs a) {
-  static_assert(32 % R == 0 && T % 32 == 0, "R divides the warp");
-  constexpr int SL = T / R;  // site slots per block
-  __shared__ double red[T / 32][3 * R];
-  __shared__ double tot[3 * R];
-  const int sidx = a.sys_of_block[blockIdx.x];
-  const BatchSys& S = a.sys[sidx];
-  const int Ns = S.Ns, nr = S.nrhs;
-  const int lb = blockIdx.x - S.blk0, nb = S.blk1 - S.blk0;
-  const int r = threadIdx.x % R, slot = threadIdx.x / R;
-  const int i0 = lb * SL + slot, istep = nb * SL;
-  const bool mine = r < nr;  // this thread's right-hand side exists
-  constexpr bool mixed = (P != P64);
-  using Lo = typename LoField<P == P64 ? P32 : P>::T;
-
-  S64* r64 = reinterpret_cast<S64*>(S.r);
-  S64* p64 = reinterpret_cast<S64*>(S.p);
-  S64* t64w = reinterpret_cast<S64*>(S.t);
-  float4* r32 = reinterpret_cast<float4*>(S.r);
-  float4* t32 = reinterpret_cast<float4*>(S.t);
-  Lo* rh = reinterpret_cast<Lo*>(P == PBF16 ? S.rh : S.r);
-  Lo* th = reinterpret_cast<Lo*>(P == PBF16 ? S.th : S.t);
-  float4* p32 = reinterpret_cast<float4*>(S.p);
-  float4* xlo = reinterpret_cast<float4*>(S.xlo);
-  S64* xa = S.xhi;
-  S64* xb = S.xhi2;
-
-  double mu = 0, mu_max = 0, beta = 0, bnorm2 = 0, alpha = 0, mu_true = 0;
-  double2 a_r = make_double2(1.0, 0.0);
-  int active = mine, status = QED3_ERR_NOCONV, it_done = 0;
-  int iter = 0, nru = 0, state = ST_INIT, xsel = 0;
-  unsigned int gen = 0;
-  int parity = 0;
-  const double tol2 = a.tol2, delta2 = a.delta2, shift = mine ? S.shift[r] : 0.0;
-
-  while (true) {
-    double v[3] = {0.0, 0.0, 0.0};
-    const int st = state;
-    // ======================= phase work (site i, right-hand side r) ==========
-    if (st == ST_INIT) {
-      if (mine)
-        for (int i = i0; i < Ns; i += istep) {
-          const int e = i * R + r;
-          const Sp64 bi = ld64(S.b, e);
-          v[0] += n2(bi);
-          const Sp64 z{make_double2(0, 0), make_double2(0, 0)};
-          st64(xa, e, z);
-          if constexpr (!mixed) {
-            st64(r64, e, bi);
-            st64(p64, e, z);
-            st64(t64w, e, z);
-          } else {
-            const Sp32 bl{make_float2(float(bi.s0.x), float(bi.s0.y)), make_float2(float(bi.s1.x), float(bi.s1.y))};
-            const Sp32 zl{make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
-            st32(r32, e, bl);
-            st32(t32, e, zl);
-            if constexpr (P == PBF16) {
-              stbf(reinterpret_cast<uint2*>(rh), e, bl);
-              stbf(reinterpret_cast<uint2*>(th), e, zl);
-            }
-            st32(p32, e, zl);
-            st32(xlo, e, zl);
-          }
-        }
-    } else if (st == ST_A) {
-      if (active)
-        for (int i = i0; i < Ns; i += istep) {
-          const int jj[3] = {__ldg(S.nbr + i), __ldg(S.nbr + Ns + i), __ldg(S.nbr + 2 * Ns + i)};
-          const int e = i * R + r;
-          if constexpr (!mixed) {
-            const M64 m[3] = {S.H[i], S.H[Ns + i], S.H[2 * Ns + i]};
-            const double dg = __ldg(S.diag + i);
-            const Sp64 self = ld64(r64, e);
-            Sp64 o{cscale(dg, self.s0), cscale(dg, self.s1)};
-#pragma unroll
-            for (int k = 0; k < 3; k++) {
-              const Sp64 bk = ld64(r64, jj[k] * R + r);
-              o.s0 = cfma(m[k].h00, bk.s0, o.s0);
-              o.s0 = cfma(m[k].h01, bk.s1, o.s0);
-              o.s1 = cfma(m[k].h10, bk.s0, o.s1);
-              o.s1 = cfma(m[k].h11, bk.s1, o.s1);
-            }
-            const Sp64 ti = ld64(t64w, e), pi = ld64(p64, e);
-            Sp64 tn, pn;
-            tn.s0 = cfma(a_r, o.s0, cscale(beta, ti.s0));
-            tn.s1 = cfma(a_r, o.s1, cscale(beta, ti.s1));
-            pn.s0 = cfma(a_r, self.s0, cscale(beta, pi.s0));
-            pn.s1 = cfma(a_r, self.s1, cscale(beta, pi.s1));
-            st64(t64w, e, tn);
-            st64(p64, e, pn);
-            v[0] += n2(tn) + shift * n2(pn);
-          } else {
-            const M32 m[3] = {S.H32[i], S.H32[Ns + i], S.H32[2 * Ns + i]};
-            const float dg = __ldg(S.diag32 + i);
-            const Sp32 self = ld32(r32, e);
-            Sp32 o{make_float2(dg * self.s0.x, dg * self.s0.y), make_float2(dg * self.s1.x, dg * self.s1.y)};
-#pragma unroll
-            for (int k = 0; k < 3; k++) {
-              const Sp32 bk = LoField<P>::ld(rh, jj[k] * R + r);
-              o.s0 = cfmaf(make_float2(m[k].r0.x, m[k].r0.y), bk.s0, o.s0);
-              o.s0 = cfmaf(make_float2(m[k].r0.z, m[k].r0.w), bk.s1, o.s0);
-              o.s1 = cfmaf(make_float2(m[k].r1.x, m[k].r1.y), bk.s0, o.s1);
-              o.s1 = cfmaf(make_float2(m[k].r1.z, m[k].r1.w), bk.s1, o.s1);
-            }
-            const Sp32 ti = ld32(t32, e), pi = ld32(p32, e);
-            const float2 ar = make_float2(float(a_r.x), float(a_r.y));
-            const float bt = float(beta);
-            Sp32 tn, pn;
-            tn.s0 = cfmaf(ar, o.s0, make_float2(bt * ti.s0.x, bt * ti.s0.y));
-            tn.s1 = cfmaf(ar, o.s1, make_float2(bt * ti.s1.x, bt * ti.s1.y));
-            pn.s0 = cfmaf(ar, self.s0, make_float2(bt * pi.s0.x, bt * pi.s0.y));
-            pn.s1 = cfmaf(ar, self.s1, make_float2(bt * pi.s1.x, bt * pi.s1.y));
-            st32(t32, e, tn);
-            if constexpr (P == PBF16) stbf(reinterpret_cast<uint2*>(th), e, tn);
-            st32(p32, e, pn);
-            v[0] += double(n2f(tn)) + shift * double(n2f(pn));
-          }
-        }
-    } else if (st == ST_B) {
-      if (active)
-        for (int i = i0; i < Ns; i += istep) {
-          const int jj[3] = {__ldg(S.nbr + i), __ldg(S.nbr + Ns + i), __ldg(S.nbr + 2 * Ns + i)};
-          const int e = i * R + r;
-          if constexpr (!mixed) {
-            const M64 m[3] = {S.Hd[i], S.Hd[Ns + i], S.Hd[2 * Ns + i]};
-            const double dg = __ldg(S.diag + i);
-            const Sp64 self = ld64(t64w, e);
-            Sp64 q{cscale(dg, self.s0), cscale(dg, self.s1)};
-#pragma unroll
-            for (int k = 0; k < 3; k++) {
-              const Sp64 bk = ld64(t64w, jj[k] * R + r);
-              q.s0 = cfma(m[k].h00, bk.s0, q.s0);
-              q.s0 = cfma(m[k].h01, bk.s1, q.s0);
-              q.s1 = cfma(m[k].h10, bk.s0, q.s1);
-              q.s1 = cfma(m[k].h11, bk.s1, q.s1);
-            }
-            const Sp64 pi = ld64(p64, e), ri = ld64(r64, e), xi = ld64(xa, e);
-            Sp64 rn, xn;
-            rn.s0 = csub(ri.s0, cscale(alpha, cadd(q.s0, cscale(shift, pi.s0))));
-            rn.s1 = csub(ri.s1, cscale(alpha, cadd(q.s1, cscale(shift, pi.s1))));
-            xn.s0 = cadd(xi.s0, cscale(alpha, pi.s0));
-            xn.s1 = cadd(xi.s1, cscale(alpha, pi.s1));
-            st64(r64, e, rn);
-            st64(xa, e, xn);
-            v[0] += n2(rn);
-          } else {
-            const M32 m[3] = {S.Hd32[i], S.Hd32[Ns + i], S.Hd32[2 * Ns + i]};
-            const float dg = __ldg(S.diag32 + i);
-            const Sp32 self = ld32(t32, e);
-            Sp32 q{make_float2(dg * self.s0.x, dg * self.s0.y), make_float2(dg * self.s1.x, dg * self.s1.y)};
-#pragma unroll
-            for (int k = 0; k < 3; k++) {
-              const Sp32 bk = LoField<P>::ld(th, jj[k] * R + r);
-              q.s0 = cfmaf(make_float2(m[k].r0.x, m[k].r0.y), bk.s0, q.s0);
-              q.s0 = cfmaf(make_float2(m[k].r0.z, m[k].r0.w), bk.s1, q.s0);
-              q.s1 = cfmaf(make_float2(m[k].r1.x, m[k].r1.y), bk.s0, q.s1);
-              q.s1 = cfmaf(make_float2(m[k].r1.z, m[k].r1.w), bk.s1, q.s1);
-            }
-            const Sp32 pi = ld32(p32, e), ri = ld32(r32, e), xi = ld32(xlo, e);
-            const float al = float(alpha), sf = float(shift);
-            Sp32 rn, xn;
-            rn.s0 = make_float2(ri.s0.x - al * (q.s0.x + sf * pi.s0.x), ri.s0.y - al * (q.s0.y + sf * pi.s0.y));
-            rn.s1 = make_float2(ri.s1.x - al * (q.s1.x + sf * pi.s1.x), ri.s1.y - al * (q.s1.y + sf * pi.s1.y));
-            xn.s0 = make_float2(xi.s0.x + al * pi.s0.x, xi.s0.y + al * pi.s0.y);
-            xn.s1 = make_float2(xi.s1.x + al * pi.s1.x, xi.s1.y + al * pi.s1.y);
-            st32(r32, e, rn);
-            if constexpr (P == PBF16) stbf(reinterpret_cast<uint2*>(rh), e, rn);
-            st32(xlo, e, xn);
-            v[0] += double(n2f(rn));
-          }
-        }
-    } else if (st == ST_R1) {
-      // t64 = D (x_hi + x_lo);  x_hi2 = x_hi + x_lo
-      if (mine)
-        for (int i = i0; i < Ns; i += istep) {
-          if (!active) {  // a finished right-hand side keeps its solution across the buffer swap
-            if constexpr (mixed) st64(xb, i * R + r, ld64(xa, i * R + r));
-            continue;
-          }
-          const int jj[3] = {__ldg(S.nbr + i), __ldg(S.nbr + Ns + i), __ldg(S.nbr + 2 * Ns + i)};
-          const M64 m[3] = {S.H[i], S.H[Ns + i], S.H[2 * Ns + i]};
-          const double dg = __ldg(S.diag + i);
-          auto xs = [&](int site) {
-            const int e = site * R + r;
-            const Sp64 h = ld64(xa, e);
-            if constexpr (!mixed) {
-              return h;
-            } else {
-              const Sp32 l = ld32(xlo, e);
-              return Sp64{make_double2(h.s0.x + l.s0.x, h.s0.y + l.s0.y), make_double2(h.s1.x + l.s1.x, h.s1.y + l.s1.y)};
-            }
-          };
-          const Sp64 self = xs(i);
-          st64(xb, i * R + r, self);
-          Sp64 o{cscale(dg, self.s0), cscale(dg, self.s1)};
-#pragma unroll
-          for (int k = 0; k < 3; k++) {
-            const Sp64 bj = xs(jj[k]);
-            o.s0 = cfma(m[k].h00, bj.s0, o.s0);
-            o.s0 = cfma(m[k].h01, bj.s1, o.s0);
-            o.s1 = cfma(m[k].h10, bj.s0, o.s1);
-            o.s1 = cfma(m[k].h11, bj.s1, o.s1);
-          }
-          st64(S.t64, i * R + r, o);
-        }
-    } else if (st == ST_R2) {
-      if (active)
-        for (int i = i0; i < Ns; i += istep) {
-          const int jj[3] = {__ldg(S.nbr + i), __ldg(S.nbr + Ns + i), __ldg(S.nbr + 2 * Ns + i)};
-          const M64 m[3] = {S.Hd[i], S.Hd[Ns + i], S.Hd[2 * Ns + i]};
-          const double dg = __ldg(S.diag + i);
-          const int e = i * R + r;
-          const Sp64 self = ld64(S.t64, e);
-          Sp64 q{cscale(dg, self.s0), cscale(dg, self.s1)};
-#pragma unroll
-          for (int k = 0; k < 3; k++) {
-            const Sp64 bj = ld64(S.t64, jj[k] * R + r);
-            q.s0 = cfma(m[k].h00, bj.s0, q.s0);
-            q.s0 = cfma(m[k].h01, bj.s1, q.s0);
-            q.s1 = cfma(m[k].h10, bj.s0, q.s1);
-            q.s1 = cfma(m[k].h11, bj.s1, q.s1);
-          }
-          const Sp64 bi = ld64(S.b, e), xi = ld64(xa, e);
-          Sp64 rt;
-          rt.s0 = csub(bi.s0, cadd(q.s0, cscale(shift, xi.s0)));
-          rt.s1 = csub(bi.s1, cadd(q.s1, cscale(shift, xi.s1)));
-          v[0] += n2(rt);
-          double2 pv0, pv1;
-          if constexpr (!mixed) {
-            const Sp64 pi = ld64(p64, e);
-            pv0 = pi.s0;
-            pv1 = pi.s1;
-            st64(r64, e, rt);
-          } else {
-            const Sp32 pi = ld32(p32, e);
-            pv0 = make_double2(pi.s0.x, pi.s0.y);
-            pv1 = make_double2(pi.s1.x, pi.s1.y);
-            const Sp32 rl{make_float2(float(rt.s0.x), float(rt.s0.y)), make_float2(float(rt.s1.x), float(rt.s1.y))};
-            st32(r32, e, rl);
-            if constexpr (P == PBF16) stbf(reinterpret_cast<uint2*>(rh), e, rl);
-            st32(xlo, e, Sp32{make_float2(0.f, 0.f), make_float2(0.f, 0.f)});
-          }
-          v[1] += rt.s0.x * pv0.x + rt.s0.y * pv0.y + rt.s1.x * pv1.x + rt.s1.y * pv1.y;
-          v[2] += rt.s0.x * pv0.y - rt.s0.y * pv0.x + rt.s1.x * pv1.y - rt.s1.y * pv1.x;
-        }
-    }
-    // ======================= block partials per right-hand side ===============
-    {
-#pragma unroll
-      for (int q = 0; q < 3; q++)
-#pragma unroll
-        for (int o = R; o < 32; o <<= 1) v[q] += __shfl_xor_sync(0xffffffffu, v[q], o);
-      const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-      if (lane < R)
-#pragma unroll
-        for (int q = 0; q < 3; q++) red[warp][3 * lane + q] = v[q];
-      __syncthreads();
-      if (threadIdx.x < 3 * R) {
-        double acc = 0.0;
-        for (int w = 0; w < T / 32; w++) acc += red[w][threadIdx.x];
-        __stcg(part_ptr(a.partials, parity, 3 * R) + threadIdx.x, acc);
-      }
-    }
-    int all_done = 0;
-    if (!grid_sync_vote(a.bar, gen, a.spin_limit, st == ST_DONE, all_done)) {
-      if (blockIdx.x == S.blk0 && threadIdx.x == 0) a.status[sidx] = QED3_ERR_TIMEOUT;
-      return;
-    }
-    if (all_done) break;
-    if (st == ST_DONE) {
-      parity ^= 1;
-      continue;
-    }
-    // ======================= system totals (fixed order over the system's blocks) ==
-    if (threadIdx.x < 3 * R) {
-      double acc = 0.0;
-      for (int bI = S.blk0; bI < S.blk1; bI++)
-        acc += __ldcg(a.partials + (size_t(parity) * gridDim.x + bI) * (3 * R) + threadIdx.x);
-      tot[threadIdx.x] = acc;
-    }
-    __syncthreads();
-    parity ^= 1;
-    const double t0 = tot[3 * r], t1 = tot[3 * r + 1], t2 = tot[3 * r + 2];
-    // ======================= state transition (identical in all blocks of S) ==
-    if (st == ST_INIT) {
-      int any = 0;
-      if (mine) {
-        bnorm2 = t0;
-        mu = mu_max = mu_true = bnorm2;
-        if (bnorm2 == 0.0) {
-          active = 0;
-          status = QED3_OK;
-        } else {
-          any = 1;
-        }
-      }
-      state = __syncthreads_or(any) ? ST_A : ST_DONE;
-    } else if (st == ST_A) {
-      if (active) alpha = mu / t0;
-      state = ST_B;
-    } else if (st == ST_B) {
-      iter++;
-      int want = iter >= a.maxiter;
-      if (active) {
-        mu_max = fmax(mu_max, t0);
-        if (!isfinite(t0) || !isfinite(alpha) || t0 < tol2 * bnorm2 || (mixed && t0 < delta2 * mu_max)) want = 1;
-      }
-      if (__syncthreads_or(want)) {
-        state = ST_R1;  // reliable update of every right-hand side; mu keeps the norm before this step
-      } else {
-        if (active) {
-          beta = t0 / mu;
-          a_r = make_double2(1.0, 0.0);
-          mu = t0;
-        }
-        state = ST_A;
-      }
-    } else if (st == ST_R1) {
-      if constexpr (mixed) {
-        S64* tmp = xa;
-        xa = xb;
-        xb = tmp;
-        xsel ^= 1;
-      }
-      state = ST_R2;
-    } else if (st == ST_R2) {
-      nru++;
-      int any = 0;
-      if (active) {
-        mu_true = t0;
-        if (t0 < tol2 * bnorm2) {
-          active = 0;
-          status = QED3_OK;
-          it_done = iter;
-        } else if (iter >= a.maxiter || !isfinite(t0)) {
-          active = 0;
-          status = QED3_ERR_NOCONV;
-          it_done = iter;
-        } else {
-          any = 1;
-          const double bt = t0 / mu;
-          beta = bt;
-          a_r = make_double2(1.0 - bt * t1 / t0, -bt * t2 / t0);
-          mu = t0;
-          mu_max = t0;
-        }
-      }
-      state = __syncthreads_or(any) ? ST_A : ST_DONE;
-    }
-    if (state == ST_DONE && blockIdx.x == S.blk0 && slot == 0 && mine) {
-      double* o = S.scal + 6 * r;
-      o[0] = mu_true;
-      o[1] = bnorm2;
-      o[2] = it_done;
-      o[3] = nru;
-      o[4] = status;
-      o[5] = xsel;
-      if (r == 0) a.status[sidx] = QED3_OK;
-    }
-  }
-}
-
-// ---------------------------------------------------------------------------
 // host side
 // ---------------------------------------------------------------------------
 template <int P, int R>
 static const void* batch_kernel(int threads) {
-  if constexpr (R >= 16)
-    return threads == 128 ? (const void*)k_batched_wide<P, R, 128> : (const void*)k_batched_wide<P, R, 256>;
-  else
-    return threads == 128 ? (const void*)k_batched_cg<P, R, 128> : (const void*)k_batched_cg<P, R, 256>;
+  return threads == 128 ? (const void*)k_batched_cg<P, R, 128> : (const void*)k_batched_cg<P, R, 256>;
 }
 
 template <int P, int R>
@@ -931,9 +551,7 @@ static int occupancy(int threads, int* per_sm) {
   (R == 1 ? fn<P, 1>(__VA_ARGS__)                            \
    : R == 2 ? fn<P, 2>(__VA_ARGS__)                          \
    : R == 4 ? fn<P, 4>(__VA_ARGS__)                          \
-   : R == 8 ? fn<P, 8>(__VA_ARGS__)                          \
-   : R == 16 ? fn<P, 16>(__VA_ARGS__)                        \
-             : fn<P, 32>(__VA_ARGS__))
+            : fn<P, 8>(__VA_ARGS__))
 
 int batch_occupancy(int prec, int R, int threads, int* per_sm) {
   if (prec == QED3_PREC_F64) return QED3_DISPATCH_R(P64, R, occupancy, threads, per_sm);
@@ -1027,9 +645,14 @@ static void batch_release(qed3_batch_s* bt) {
   for (void* p : bt->buffers)
     if (p) cudaFree(p);
   bt->buffers.clear();
-  void* ptrs[] = {bt->d_sys, bt->d_sys_of_block, bt->partials, bt->bar, bt->d_status, bt->d_scal};
+  void* ptrs[] = {bt->d_sys,         bt->d_sys_of_block, bt->partials, bt->bar,        bt->d_status,
+                  bt->d_scal,        bt->d_sys_of_tile,  bt->d_dyn,    bt->d_counters, bt->d_tile_part};
   for (void* p : ptrs)
     if (p) cudaFree(p);
+  bt->d_sys_of_tile = nullptr;
+  bt->d_dyn = nullptr;
+  bt->d_counters = nullptr;
+  bt->d_tile_part = nullptr;
   bt->d_sys = nullptr;
   bt->d_sys_of_block = nullptr;
   bt->partials = nullptr;
@@ -1047,13 +670,12 @@ static void batch_release(qed3_batch_s* bt) {
 // All systems advance through the same grid barriers, so a system that needs
 // twice the iterations of the others gets twice their blocks per site and
 // finishes with them instead of running on alone.  At least one block per
-// system and no more blocks than site slots (T sites per block pass, T / R in
-// the wide kernel).  The total is fixed when the batch is built, so a launch
+// system and no more blocks than site slots (T sites per block pass).  The total is fixed when the batch is built, so a launch
 // captured in a CUDA graph stays valid after a re-split: only the contents of
 // the block-to-system table and the descriptors change.
 static void batch_partition(qed3_batch_s* bt) {
   const int nsys = int(bt->sys.size());
-  const int slots = bt->R >= 16 ? bt->threads / bt->R : bt->threads;
+  const int slots = bt->threads;
   std::vector<long long> maxb(nsys);
   long long room = 0;
   for (int i = 0; i < nsys; i++) {
@@ -1145,16 +767,37 @@ static int batch_build(qed3_batch_s* bt) {
     }
   }
   const int nsys = int(bt->sys.size());
+  const bool dyn = bt->sched == QED3_BATCH_DYNAMIC;
   int dev = 0, smc = 0, per_sm = 0;
   QED3_CUDA_TRY(cudaGetDevice(&dev));
   QED3_CUDA_TRY(cudaDeviceGetAttribute(&smc, cudaDevAttrMultiProcessorCount, dev));
-  int rc = batch_occupancy(bt->prec, R, bt->threads, &per_sm);
+  int rc = dyn ? batch_dyn_occupancy(bt->prec, R, bt->threads, &per_sm) : batch_occupancy(bt->prec, R, bt->threads, &per_sm);
   if (rc) return rc;
+  if (per_sm < 1) return fail(QED3_ERR_CUDA, "batched CG kernel cannot be resident");
   bt->cap = (long long)per_sm * smc;
-  if (bt->cap < nsys) return fail(QED3_ERR_ARG, "more systems than co-resident blocks; use a larger right-hand-side tile");
-  bt->work.assign(nsys, 1.0);
-  bt->grid = 0;
-  batch_partition(bt);
+  std::vector<int> sot;
+  if (dyn) {
+    // warp tiles of 32 x spt consecutive sites, system after system: about
+    // eight tiles per co-resident warp and step while every system is active
+    double work = 0;  // site x right-hand-side pairs
+    for (const auto& s : bt->sys) work += double(s.Ns) * s.nrhs;
+    bt->spt = int(std::max(1.0, std::min(32.0, std::floor(work / (8.0 * bt->cap * bt->threads * bt->R)))));
+    const int tile = 32 * bt->spt;
+    for (int i = 0; i < nsys; i++) {
+      BatchSys& s = bt->sys[i];
+      s.ch0 = int(sot.size());
+      for (int c = 0; c < (s.Ns + tile - 1) / tile; c++) sot.push_back(i);
+      s.ch1 = int(sot.size());
+      s.blk0 = s.blk1 = 0;
+    }
+    bt->ntiles = int(sot.size());
+    bt->grid = int(bt->cap);
+  } else {
+    if (bt->cap < nsys) return fail(QED3_ERR_ARG, "more systems than co-resident blocks; use a larger right-hand-side tile");
+    bt->work.assign(nsys, 1.0);
+    bt->grid = 0;
+    batch_partition(bt);
+  }
   // workspaces
   for (auto& s : bt->sys) {
     const size_t bytes = size_t(s.Ns) * R * sizeof(S64);
@@ -1180,9 +823,17 @@ static int batch_build(qed3_batch_s* bt) {
     bt->sys[i].bnorm = bt->d_scal + size_t(6) * R * nsys + size_t(R) * i;
   }
   QED3_CUDA_TRY(cudaMalloc(&bt->d_sys, sizeof(BatchSys) * nsys));
-  QED3_CUDA_TRY(cudaMalloc(&bt->d_sys_of_block, sizeof(int) * bt->cap));
-  QED3_CUDA_TRY(cudaMemcpy(bt->d_sys_of_block, bt->sob.data(), sizeof(int) * bt->sob.size(), cudaMemcpyHostToDevice));
-  QED3_CUDA_TRY(cudaMalloc(&bt->partials, sizeof(double) * 2 * bt->cap * 3 * R));
+  if (dyn) {
+    QED3_CUDA_TRY(cudaMalloc(&bt->d_sys_of_tile, sizeof(int) * sot.size()));
+    QED3_CUDA_TRY(cudaMemcpy(bt->d_sys_of_tile, sot.data(), sizeof(int) * sot.size(), cudaMemcpyHostToDevice));
+    QED3_CUDA_TRY(cudaMalloc(&bt->d_dyn, sizeof(DynState<kMaxTile>) * nsys));
+    QED3_CUDA_TRY(cudaMalloc(&bt->d_counters, sizeof(int) * (nsys + 3)));
+    QED3_CUDA_TRY(cudaMalloc(&bt->d_tile_part, sizeof(double) * 3 * R * sot.size()));
+  } else {
+    QED3_CUDA_TRY(cudaMalloc(&bt->d_sys_of_block, sizeof(int) * bt->cap));
+    QED3_CUDA_TRY(cudaMemcpy(bt->d_sys_of_block, bt->sob.data(), sizeof(int) * bt->sob.size(), cudaMemcpyHostToDevice));
+    QED3_CUDA_TRY(cudaMalloc(&bt->partials, sizeof(double) * 2 * bt->cap * 3 * R));
+  }
   QED3_CUDA_TRY(cudaMalloc(&bt->bar, sizeof(GridBar)));
   QED3_CUDA_TRY(cudaMalloc(&bt->d_status, sizeof(int) * nsys));
   QED3_CUDA_TRY(cudaEventCreate(&bt->e0));
@@ -1234,21 +885,45 @@ int batch_launch_all(qed3_batch_s* bt, double* const* x, const double* const* b,
   }
   QED3_CUDA_TRY(cudaMemsetAsync(bt->bar, 0, sizeof(GridBar), st));
   QED3_CUDA_TRY(cudaMemsetAsync(bt->d_status, 0xff, sizeof(int) * nsys, st));
-  BatchArgs a{};
-  a.sys = bt->d_sys;
-  a.sys_of_block = bt->d_sys_of_block;
-  a.nsys = nsys;
-  a.partials = bt->partials;
-  a.bar = bt->bar;
-  a.status = bt->d_status;
   const double tol = prm && prm->tol > 0 ? prm->tol : 1e-10;
   const double delta = prm && prm->delta > 0 ? prm->delta : 0.1;
-  a.tol2 = tol * tol;
-  a.delta2 = delta * delta;
-  a.maxiter = prm && prm->maxiter > 0 ? prm->maxiter : 100000;
-  a.spin_limit = 20000000LL;
-  if (bt->timing) QED3_CUDA_TRY(cudaEventRecord(bt->e0, st));
-  int rc = batch_launch(bt->prec, R, a, bt->grid, bt->threads, st);
+  const int maxiter = prm && prm->maxiter > 0 ? prm->maxiter : 100000;
+  int rc = QED3_OK;
+  if (bt->sched == QED3_BATCH_DYNAMIC) {
+    QED3_CUDA_TRY(cudaMemsetAsync(bt->d_dyn, 0, sizeof(DynState<kMaxTile>) * nsys, st));
+    QED3_CUDA_TRY(cudaMemsetAsync(bt->d_counters, 0, sizeof(int) * (nsys + 3), st));
+    DynArgs a{};
+    a.sys = bt->d_sys;
+    a.nsys = nsys;
+    a.sys_of_tile = bt->d_sys_of_tile;
+    a.ntiles = bt->ntiles;
+    a.spt = bt->spt;
+    a.state = bt->d_dyn;
+    a.counters = bt->d_counters;
+    a.part = bt->d_tile_part;
+    a.bar = bt->bar;
+    a.status = bt->d_status;
+    a.tol2 = tol * tol;
+    a.delta2 = delta * delta;
+    a.maxiter = maxiter;
+    a.spin_limit = 20000000LL;
+    if (bt->timing) QED3_CUDA_TRY(cudaEventRecord(bt->e0, st));
+    rc = batch_dyn_launch(bt->prec, R, a, bt->grid, bt->threads, st);
+  } else {
+    BatchArgs a{};
+    a.sys = bt->d_sys;
+    a.sys_of_block = bt->d_sys_of_block;
+    a.nsys = nsys;
+    a.partials = bt->partials;
+    a.bar = bt->bar;
+    a.status = bt->d_status;
+    a.tol2 = tol * tol;
+    a.delta2 = delta * delta;
+    a.maxiter = maxiter;
+    a.spin_limit = 20000000LL;
+    if (bt->timing) QED3_CUDA_TRY(cudaEventRecord(bt->e0, st));
+    rc = batch_launch(bt->prec, R, a, bt->grid, bt->threads, st);
+  }
   if (rc) return rc;
   if (bt->timing) QED3_CUDA_TRY(cudaEventRecord(bt->e1, st));
   for (int i = 0; i < nsys; i++) {
@@ -1306,7 +981,7 @@ int batch_solve(qed3_batch_s* bt, double* const* x, const double* const* b, cons
   if (ms_out) *ms_out = ms;
   rc = batch_reports(bt, reports, ms, st);
   if (rc) return rc;
-  return batch_rebalance(bt, bt->last_scal, st);
+  return bt->sched == QED3_BATCH_DYNAMIC ? QED3_OK : batch_rebalance(bt, bt->last_scal, st);
 }
 
 // ---- autotuner ----------------------------------------------------------------
@@ -1318,8 +993,11 @@ struct TuneKey {
   std::vector<long long> sig;
   bool operator<(const TuneKey& o) const { return sig < o.sig; }
 };
-static std::map<TuneKey, std::pair<int, int>>& tune_cache() {
-  static std::map<TuneKey, std::pair<int, int>> c;
+struct TuneBest {
+  int R, T, sched;
+};
+static std::map<TuneKey, TuneBest>& tune_cache() {
+  static std::map<TuneKey, TuneBest> c;
   return c;
 }
 
@@ -1333,9 +1011,12 @@ __global__ void k_fill_synthetic(int n, double* v, unsigned seed) {
   v[i] = double(h & 0xffffff) / double(0x1000000) - 0.5;
 }
 
-int batch_autotune(qed3_batch_s* proto, int* best_R, int* best_threads, std::vector<std::pair<std::pair<int, int>, float>>* log) {
+int batch_autotune(qed3_batch_s* proto, int* best_R, int* best_threads, int* best_sched, std::vector<BatchTrial>* log) {
   TuneKey key;
   key.sig.push_back(proto->prec);
+  key.sig.push_back(proto->R);
+  key.sig.push_back(proto->threads);
+  key.sig.push_back(proto->sched);
   int maxn = 1;
   for (size_t u = 0; u < proto->user_ops.size(); u++) {
     key.sig.push_back(proto->user_ops[u]->Ns);
@@ -1344,8 +1025,9 @@ int batch_autotune(qed3_batch_s* proto, int* best_R, int* best_threads, std::vec
   }
   auto it = tune_cache().find(key);
   if (it != tune_cache().end() && !log) {
-    *best_R = it->second.first;
-    *best_threads = it->second.second;
+    *best_R = it->second.R;
+    *best_threads = it->second.T;
+    *best_sched = it->second.sched;
     return QED3_OK;
   }
   // synthetic right-hand sides
@@ -1360,31 +1042,39 @@ int batch_autotune(qed3_batch_s* proto, int* best_R, int* best_threads, std::vec
     bs.push_back(bb);
   }
   float best = 1e30f;
-  int bR = 1, bT = 256;
+  int bR = 1, bT = 256, bS = QED3_BATCH_STATIC;
   qed3_solve_params p{1e-30, 24, proto->prec, 0.1, 0.0, 0};
-  for (int R : {1, 2, 4, 8, 16, 32}) {
-    if (R > 1 && R / 2 >= maxn) break;
-    for (int T : {128, 256}) {
-      qed3_batch_s trial;
-      trial.prec = proto->prec;
-      trial.R = R;
-      trial.threads = T;
-      trial.user_ops = proto->user_ops;
-      trial.user_nrhs = proto->user_nrhs;
-      int rc = batch_build(&trial);
-      float ms = 1e30f;
-      if (rc == QED3_OK) {
-        float m0 = 0.f, m1 = 0.f;
-        rc = batch_solve(&trial, xs.data(), bs.data(), nullptr, &p, nullptr, &m0, 0);
-        if (rc == QED3_OK || rc == QED3_ERR_NOCONV) rc = batch_solve(&trial, xs.data(), bs.data(), nullptr, &p, nullptr, &m1, 0);
-        if (rc == QED3_OK || rc == QED3_ERR_NOCONV) ms = m1;
-      }
-      batch_release(&trial);
-      if (log) log->push_back({{R, T}, ms});
-      if (ms < best) {
-        best = ms;
-        bR = R;
-        bT = T;
+  for (int sched : {QED3_BATCH_STATIC, QED3_BATCH_DYNAMIC}) {
+    if (proto->sched > 0 && sched != proto->sched) continue;
+    for (int R : {1, 2, 4, 8}) {
+      if (R > 1 && R / 2 >= maxn) break;
+      if (proto->R > 0 && R != proto->R) continue;
+      for (int T : {128, 256}) {
+        if (proto->threads > 0 && T != proto->threads) continue;
+        qed3_batch_s trial;
+        trial.prec = proto->prec;
+        trial.R = R;
+        trial.threads = T;
+        trial.sched = sched;
+        trial.user_ops = proto->user_ops;
+        trial.user_nrhs = proto->user_nrhs;
+        int rc = batch_build(&trial);
+        float ms = 1e30f;
+        if (rc == QED3_OK) {
+          float m0 = 0.f, m1 = 0.f;
+          rc = batch_solve(&trial, xs.data(), bs.data(), nullptr, &p, nullptr, &m0, 0);
+          if (rc == QED3_OK || rc == QED3_ERR_NOCONV)
+            rc = batch_solve(&trial, xs.data(), bs.data(), nullptr, &p, nullptr, &m1, 0);
+          if (rc == QED3_OK || rc == QED3_ERR_NOCONV) ms = m1;
+        }
+        batch_release(&trial);
+        if (log) log->push_back({R, T, sched, ms});
+        if (ms < best) {
+          best = ms;
+          bR = R;
+          bT = T;
+          bS = sched;
+        }
       }
     }
   }
@@ -1392,34 +1082,45 @@ int batch_autotune(qed3_batch_s* proto, int* best_R, int* best_threads, std::vec
   for (double* p2 : bs) cudaFree(p2);
   set_error("");
   if (best >= 1e29f) return fail(QED3_ERR_CUDA, "autotuner found no runnable configuration");
-  tune_cache()[key] = {bR, bT};
+  tune_cache()[key] = {bR, bT, bS};
   *best_R = bR;
   *best_threads = bT;
+  *best_sched = bS;
   return QED3_OK;
 }
 
 int batch_create(int nsys, qed3_dirac_s* const* ops, const int* nrhs, int prec, int rhs_tile, int threads,
-                 qed3_batch_s** out) {
+                 qed3_batch_s** out, int sched) {
   auto* bt = new qed3_batch_s;
   bt->prec = prec;
   for (int u = 0; u < nsys; u++) {
     bt->user_ops.push_back(ops[u]);
     bt->user_nrhs.push_back(nrhs[u]);
   }
-  int R = rhs_tile, T = threads;
+  int R = rhs_tile, T = threads, S = sched;
+  if (S != 0 && S != QED3_BATCH_STATIC && S != QED3_BATCH_DYNAMIC) {
+    delete bt;
+    return fail(QED3_ERR_ARG, "schedule must be 0, QED3_BATCH_STATIC or QED3_BATCH_DYNAMIC");
+  }
   if (R <= 0 || T <= 0) {
-    int aR = 1, aT = 256;
-    const int rc = batch_autotune(bt, &aR, &aT, nullptr);
+    // the autotuner picks what was left open (the schedule too, when 0)
+    int aR = 1, aT = 256, aS = QED3_BATCH_STATIC;
+    bt->R = R;
+    bt->threads = T;
+    bt->sched = S;
+    const int rc = batch_autotune(bt, &aR, &aT, &aS, nullptr);
     if (rc) {
       delete bt;
       return rc;
     }
     if (R <= 0) R = aR;
     if (T <= 0) T = aT;
+    if (S <= 0) S = aS;
   }
-  if (!(R == 1 || R == 2 || R == 4 || R == 8 || R == 16 || R == 32)) {
+  if (S <= 0) S = QED3_BATCH_STATIC;
+  if (!(R == 1 || R == 2 || R == 4 || R == 8)) {
     delete bt;
-    return fail(QED3_ERR_ARG, "rhs_tile must be 1, 2, 4, 8, 16 or 32");
+    return fail(QED3_ERR_ARG, "rhs_tile must be 1, 2, 4 or 8");
   }
   if (T != 128 && T != 256) {
     delete bt;
@@ -1427,6 +1128,7 @@ int batch_create(int nsys, qed3_dirac_s* const* ops, const int* nrhs, int prec, 
   }
   bt->R = R;
   bt->threads = T;
+  bt->sched = S;
   const int rc = batch_build(bt);
   if (rc) {
     batch_release(bt);

@@ -9,10 +9,11 @@
 
 namespace qed3 {
 
-constexpr int kMaxTile = 32;  // right-hand sides per system (compile-time tile; 16 and 32: the wide kernel)
+constexpr int kMaxTile = 8;  // right-hand sides per system (compile-time tile)
 
 struct BatchSys {
   int Ns, nrhs, blk0, blk1;
+  int ch0, ch1;  // site tiles of this system in the dynamic schedule's tile list
   const int* nbr;
   const M64* H;
   const M64* Hd;
@@ -47,7 +48,37 @@ struct BatchArgs {
   long long spin_limit;
 };
 
+// Dynamic schedule: the CG state of each system lives in device memory and
+// blocks take site tiles (T consecutive sites of one system, all its right-hand
+// sides) from a per-step counter; the block that completes a system's last
+// tile of the step reduces its tile partials and advances its state.
+template <int R>
+struct DynState {
+  int state, iter, nru, xsel;
+  int active[R], status[R], it_done[R];
+  double mu[R], mu_max[R], beta[R], bnorm2[R], alpha[R], mu_true[R];
+  double2 a_r[R];
+};
+
+struct DynArgs {
+  const BatchSys* sys;
+  int nsys;
+  const int* sys_of_tile;
+  int ntiles;
+  int spt;        // sites per thread in a tile (a tile is threads x spt consecutive sites)
+  void* state;    // DynState<R>[nsys]
+  int* counters;  // [nsys] tiles done this step, then [2] step tile counters, then [1] systems done
+  double* part;   // [ntiles][3 R]
+  GridBar* bar;
+  int* status;
+  double tol2, delta2;
+  int maxiter;
+  long long spin_limit;
+};
+
 int batch_occupancy(int prec, int R, int threads, int* per_sm);
+int batch_dyn_occupancy(int prec, int R, int threads, int* per_sm);
+int batch_dyn_launch(int prec, int R, DynArgs& args, int grid, int threads, cudaStream_t st);
 int batch_launch(int prec, int R, BatchArgs& args, int grid, int threads, cudaStream_t st);
 int batch_import(const BatchSys& s, const qed3_dirac_s* d, const double* b_ref, int R, bool bcast, cudaStream_t st);
 int batch_export(const BatchSys& s, const qed3_dirac_s* d, double* x_ref, int R, cudaStream_t st);
@@ -58,7 +89,14 @@ int batch_export(const BatchSys& s, const qed3_dirac_s* d, double* x_ref, int R,
 // sides, with their workspaces and the block partition of the launch.
 struct qed3_batch_s {
   int prec = 0, R = 1, threads = 256, grid = 0;
+  int sched = 0;                      // QED3_BATCH_STATIC (fixed block split) or QED3_BATCH_DYNAMIC (tiles per step)
   long long cap = 0;                  // co-resident blocks of the kernel (the partials' size)
+  int ntiles = 0;                     // dynamic schedule: site tiles over all systems
+  int spt = 1;                        // dynamic schedule: sites per thread in a tile
+  int* d_sys_of_tile = nullptr;
+  void* d_dyn = nullptr;              // DynState per system
+  int* d_counters = nullptr;
+  double* d_tile_part = nullptr;
   std::vector<qed3_dirac_s*> user_ops;
   std::vector<int> user_nrhs;
   // internal systems
@@ -81,7 +119,7 @@ struct qed3_batch_s {
 
 namespace qed3 {
 int batch_create(int nsys, qed3_dirac_s* const* ops, const int* nrhs, int prec, int rhs_tile, int threads,
-                 qed3_batch_s** out);
+                 qed3_batch_s** out, int sched = 0);
 void batch_destroy(qed3_batch_s* bt);
 int batch_solve(qed3_batch_s* bt, double* const* x, const double* const* b, const double* const* shifts,
                 const qed3_solve_params* prm, qed3_solve_report* reports, float* ms_out, cudaStream_t st);
@@ -89,6 +127,9 @@ int batch_set_shifts(qed3_batch_s* bt, const double* const* shifts, double shift
 int batch_launch_all(qed3_batch_s* bt, double* const* x, const double* const* b, const qed3_solve_params* prm,
                      cudaStream_t st);
 int batch_reports(qed3_batch_s* bt, qed3_solve_report* reports, float ms, cudaStream_t st);
-int batch_autotune(qed3_batch_s* proto, int* best_R, int* best_threads,
-                   std::vector<std::pair<std::pair<int, int>, float>>* log);
+struct BatchTrial {
+  int R, threads, sched;
+  float ms;
+};
+int batch_autotune(qed3_batch_s* proto, int* best_R, int* best_threads, int* best_sched, std::vector<BatchTrial>* log);
 }  // namespace qed3
