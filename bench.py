@@ -56,7 +56,10 @@ BETA = 1.4
 OV_MASS = 0.05  # overlap outer solve: D(m) = (1 - m/2) D_ov + m
 M5 = 0.05
 TOL = 1e-10
-BATCH_DELTA = 0.01  # batched leg: FP64 reliable update when |r| fell 100x (each costs two FP64 stencil passes)
+# mixed-precision solves: an FP64 reliable update when |r| fell 100x since the last
+# one (delta = 0.01; each costs two FP64 stencil passes, the slow pipe on this
+# GPU); measured: the same iterations as delta = 0.1 with half the updates
+RU_DELTA = 0.01
 # DRAM read + write bytes of one k_pcg launch at n=64 from an ncu capture
 # (--set full, one launch): the operator and vectors are loaded once, the
 # iterations run out of L2.
@@ -255,8 +258,8 @@ def heldout_iterations(torch, Q, lat, pc, dev, n=20):
         b = torch.from_numpy(Q.ParallelRng(lat, 50 + s).gaussian_spinor()).to(dev)
         x = torch.zeros_like(b)
         r64 = Dt.solve(x, b, tol=TOL, precision=Q.PREC_F64)
-        r0 = Dt.solve(x, b, tol=TOL, precision=Q.PREC_F32)
-        r1 = pc.solve(Dt, x, b, tol=TOL, precision=Q.PREC_F32)
+        r0 = Dt.solve(x, b, tol=TOL, precision=Q.PREC_F32, delta=RU_DELTA)
+        r1 = pc.solve(Dt, x, b, tol=TOL, precision=Q.PREC_F32, delta=RU_DELTA)
         out.append({"beta": betas[s % 3], "seed": 5000 + s, "cg_f64_iters": r64.iters, "cg_f32_iters": r0.iters,
                     "pcg_f32_iters": r1.iters, "cg_f64_ms": r64.ms, "cg_f32_ms": r0.ms, "pcg_f32_ms": r1.ms,
                     "certified": r1.status == Q.OK and r1.true_rel_res <= TOL})
@@ -283,8 +286,8 @@ def time_solver(torch, Q, D, bt, prec, steps, warmup, flush, pc=None):
 
     def solve():
         if pc is not None:
-            return pc.solve(D, x, bt, tol=TOL, precision=prec)
-        return D.solve(x, bt, tol=TOL, precision=prec)
+            return pc.solve(D, x, bt, tol=TOL, precision=prec, delta=RU_DELTA)
+        return D.solve(x, bt, tol=TOL, precision=prec, delta=RU_DELTA)
 
     for _ in range(warmup):
         solve()
@@ -546,8 +549,8 @@ def learned_hbm(torch, Q, dev, n=256, reps=3):
     x = torch.zeros_like(b)
     st = torch.cuda.current_stream()
     for name, fn in (("cg_f64", lambda: D.solve(x, b, tol=TOL, precision=Q.PREC_F64)),
-                     ("cg_f32", lambda: D.solve(x, b, tol=TOL, precision=Q.PREC_F32)),
-                     ("pcg_f32", lambda: pc.solve(D, x, b, tol=TOL, precision=Q.PREC_F32))):
+                     ("cg_f32", lambda: D.solve(x, b, tol=TOL, precision=Q.PREC_F32, delta=RU_DELTA)),
+                     ("pcg_f32", lambda: pc.solve(D, x, b, tol=TOL, precision=Q.PREC_F32, delta=RU_DELTA))):
         fn()
         ms, rep = [], None
         for _ in range(reps):
@@ -696,7 +699,7 @@ def batched_throughput(torch, Q, dev, reps=3):
     xs = [torch.zeros_like(b_) for b_ in bs]
     ms_b, ok, iters, rus = [], True, 0, 0
     for i in range(reps + 1):
-        reps_, ms = batch.solve(xs, bs, tol=TOL, precision=Q.PREC_F32, delta=BATCH_DELTA)
+        reps_, ms = batch.solve(xs, bs, tol=TOL, precision=Q.PREC_F32, delta=RU_DELTA)
         ok = ok and all(r.status == Q.OK and r.true_rel_res <= TOL for r in reps_)
         iters = max(iters, max(r.iters for r in reps_))
         rus = max(rus, max(r.reliable_updates for r in reps_))
@@ -708,14 +711,14 @@ def batched_throughput(torch, Q, dev, reps=3):
     for (D_n, _), b_ in zip(systems, bs):
         x_ = torch.zeros_like(b_[0])
         for r in range(64):
-            rep = D_n.solve(x_, b_[r].contiguous(), tol=TOL, precision=Q.PREC_F32)
+            rep = D_n.solve(x_, b_[r].contiguous(), tol=TOL, precision=Q.PREC_F32, delta=RU_DELTA)
             seq_ok = seq_ok and rep.status == Q.OK
     torch.cuda.synchronize()
     seq_s = time.perf_counter() - t0
     ms = float(np.mean(ms_b))
     return {"rhs": 256, "lattices": [16, 32, 48, 64], "rhs_tile": batch.rhs_tile, "threads": batch.threads,
             "blocks": batch.blocks, "schedule": {Q.BATCH_STATIC: "static", Q.BATCH_DYNAMIC: "dynamic"}[batch.schedule],
-            "reliable_update_delta": BATCH_DELTA, "max_reliable_updates": rus,
+            "reliable_update_delta": RU_DELTA, "max_reliable_updates": rus,
             "ms_per_batch": ms, "solves_per_s": 256e3 / ms, "max_iters": iters,
             "certified": bool(ok), "sequential_single_solves_per_s": 256 / seq_s, "sequential_certified": seq_ok,
             "speedup_vs_sequential": (256e3 / ms) / (256 / seq_s)}
@@ -799,10 +802,11 @@ def profile_case(torch, which):
         pc.collect(D, nsrc=2, seed=1000, snapshots=(0, 5, 20))
         hist = pc.train(4, batch=8, lr=3e-3, seed=2)
         print(json.dumps({"loss": [float(v) for v in hist]}))
-    elif which == "batched":
+    elif which in ("batched", "batched_static"):
         # a quarter of the 256-RHS configuration (16 right-hand sides on each
-        # of n = 16, 32, 48, 64; ~0.4 GB of fields, above L2) with the tile the
-        # autotuner picks for the full one, so no tuning launches precede it
+        # of n = 16, 32, 48, 64; ~0.4 GB of fields, above L2) with the tile,
+        # threads and schedule the autotuner picks for the full one (or the
+        # static schedule), so no tuning launches precede it
         rng = np.random.default_rng(256)
         systems, bs = [], []
         for n in (16, 32, 48, 64):
@@ -812,10 +816,13 @@ def profile_case(torch, which):
             b_n = rng.normal(size=(16, 2 * lat_n.n_sites)) + 1j * rng.normal(size=(16, 2 * lat_n.n_sites))
             systems.append((D_n, 16))
             bs.append(torch.from_numpy(b_n).cuda())
-        batch = Q.Batch(systems, precision=Q.PREC_F32, rhs_tile=2, threads=128)
+        if which == "batched":
+            batch = Q.Batch(systems, precision=Q.PREC_F32, rhs_tile=1, threads=256, schedule=Q.BATCH_DYNAMIC)
+        else:
+            batch = Q.Batch(systems, precision=Q.PREC_F32, rhs_tile=1, threads=128, schedule=Q.BATCH_STATIC)
         xs = [torch.zeros_like(b_) for b_ in bs]
         for _ in range(2):
-            reps, ms = batch.solve(xs, bs, tol=TOL, precision=Q.PREC_F32)
+            reps, ms = batch.solve(xs, bs, tol=TOL, precision=Q.PREC_F32, delta=RU_DELTA)
         print(json.dumps({"ms": ms, "max_iters": max(r.iters for r in reps),
                           "certified": all(r.status == Q.OK and r.true_rel_res <= TOL for r in reps)}))
     else:
@@ -858,11 +865,13 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-paths", action="store_true", help="skip the timings of the HMC, overlap and S^2 x S^1 paths")
-    ap.add_argument("--profile", choices=["apply", "cg", "pcg", "ppcg", "pcgs", "batched", "ext", "train"], default=None,
+    ap.add_argument("--profile", choices=["apply", "cg", "pcg", "ppcg", "pcgs", "batched", "batched_static", "ext", "train"],
+                    default=None,
                     help="small self-contained case for ncu: 'apply' = D apply at n=512 (f32, bf16, f64; "
                          "HBM-resident), 'cg' = one n=64 mixed-precision solve, 'pcg' = 300 iterations of the "
                          "n=64 preconditioned solve, 'ppcg' = the same with the pipelined one-barrier kernel, "
-                         "'batched' = 64 RHS over four lattices, 'ext' = S^2 x S^1 D apply at n=64, Nt=16, "
+                         "'batched' / 'batched_static' = 64 RHS over four lattices (dynamic / static schedule), "
+                         "'ext' = S^2 x S^1 D apply at n=64, Nt=16, "
                          "'train' = four Adam steps of the n=64 network (tcgen05 channel mixing), 'pcgs' = 200 iterations "
                          "of the streaming preconditioned solver at n=256")
     args = ap.parse_args()
@@ -952,9 +961,9 @@ def main():
         e0.record(st)
         db.copy_(hb, non_blocking=True)
         if use_pc:
-            pc.solve(D, dx, db, tol=TOL, precision=prec_best)
+            pc.solve(D, dx, db, tol=TOL, precision=prec_best, delta=RU_DELTA)
         else:
-            D.solve(dx, db, tol=TOL, precision=prec_best)
+            D.solve(dx, db, tol=TOL, precision=prec_best, delta=RU_DELTA)
         hx.copy_(dx, non_blocking=True)
         e1.record(st)
         e1.synchronize()
@@ -1000,9 +1009,9 @@ def main():
     # ---- launches of this library's kernels in the timed region ------------------------
     def one_step():
         if use_pc:
-            pc.solve(D, dx, db, tol=TOL, precision=prec_best)
+            pc.solve(D, dx, db, tol=TOL, precision=prec_best, delta=RU_DELTA)
         else:
-            D.solve(dx, db, tol=TOL, precision=prec_best)
+            D.solve(dx, db, tol=TOL, precision=prec_best, delta=RU_DELTA)
     try:
         ours1, all1 = count_launches(torch, one_step)
         launches = {"per_step": ours1, "per_step_all_kernels": all1,
@@ -1028,7 +1037,7 @@ def main():
             "solver": (f"learned-preconditioned persistent CG, {best[4:]} inner, FP64 reliable updates"
                        if use_pc else f"persistent CG, {best} inner, FP64 reliable updates"),
             "hmc_acceptance": acc,
-            "solvers": results,
+            "solvers": results, "reliable_update_delta": RU_DELTA,
             "speedup_vs_plain_f64": results["f64"]["ms"] / results[best]["ms"],
             "preconditioner": train_info,
             "heldout": heldout,
