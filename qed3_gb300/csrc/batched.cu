@@ -641,6 +641,11 @@ int batch_export(const BatchSys& s, const qed3_dirac_s* d, double* x_ref, int R,
 // ===========================================================================
 namespace qed3 {
 
+// Dynamic-schedule counters in one int buffer: tiles done [nsys], steps
+// completed [nsys], the 64-bit work counter (8-byte aligned), systems done.
+static int dyn_work_offset(int nsys) { return (2 * nsys + 1) & ~1; }
+static int dyn_counter_ints(int nsys) { return dyn_work_offset(nsys) + 4; }
+
 static void batch_release(qed3_batch_s* bt) {
   for (void* p : bt->buffers)
     if (p) cudaFree(p);
@@ -830,7 +835,7 @@ static int batch_build(qed3_batch_s* bt) {
     QED3_CUDA_TRY(cudaMalloc(&bt->d_sys_of_tile, sizeof(int) * sot.size()));
     QED3_CUDA_TRY(cudaMemcpy(bt->d_sys_of_tile, sot.data(), sizeof(int) * sot.size(), cudaMemcpyHostToDevice));
     QED3_CUDA_TRY(cudaMalloc(&bt->d_dyn, sizeof(DynState<kMaxTile>) * nsys));
-    QED3_CUDA_TRY(cudaMalloc(&bt->d_counters, sizeof(int) * (nsys + 3)));
+    QED3_CUDA_TRY(cudaMalloc(&bt->d_counters, sizeof(int) * dyn_counter_ints(nsys)));
     QED3_CUDA_TRY(cudaMalloc(&bt->d_tile_part, sizeof(double) * 3 * R * sot.size()));
   } else {
     QED3_CUDA_TRY(cudaMalloc(&bt->d_sys_of_block, sizeof(int) * bt->cap));
@@ -894,7 +899,7 @@ int batch_launch_all(qed3_batch_s* bt, double* const* x, const double* const* b,
   int rc = QED3_OK;
   if (bt->sched == QED3_BATCH_DYNAMIC) {
     QED3_CUDA_TRY(cudaMemsetAsync(bt->d_dyn, 0, sizeof(DynState<kMaxTile>) * nsys, st));
-    QED3_CUDA_TRY(cudaMemsetAsync(bt->d_counters, 0, sizeof(int) * (nsys + 3), st));
+    QED3_CUDA_TRY(cudaMemsetAsync(bt->d_counters, 0, sizeof(int) * dyn_counter_ints(nsys), st));
     DynArgs a{};
     a.sys = bt->d_sys;
     a.nsys = nsys;
@@ -902,7 +907,10 @@ int batch_launch_all(qed3_batch_s* bt, double* const* x, const double* const* b,
     a.ntiles = bt->ntiles;
     a.spt = bt->spt;
     a.state = bt->d_dyn;
-    a.counters = bt->d_counters;
+    a.sys_cnt = bt->d_counters;
+    a.epoch = bt->d_counters + nsys;
+    a.work = reinterpret_cast<unsigned long long*>(bt->d_counters + dyn_work_offset(nsys));
+    a.ndone = bt->d_counters + dyn_work_offset(nsys) + 2;
     a.part = bt->d_tile_part;
     a.bar = bt->bar;
     a.status = bt->d_status;

@@ -1,29 +1,32 @@
 // Batched CG, dynamic schedule: the systems of a batch (see batched.cu) run the
 // same per-system CG state machine
 //     INIT -> (A -> B)* -> [R1 -> R2] -> ... -> DONE
-// but no block is tied to a system.  Every system is cut into warp tiles of
-// 32 x spt consecutive sites (all R right-hand sides of a site together, so a
-// tile reads each hop block once for R spinors), and one step of the machine
-// -- one phase of every unfinished system -- is a single pass over the list of
-// all tiles.  Each warp works on its own: it takes the next tile from the
-// step's counter (prefetching the one after it while it works), does the
-// tile's phase work for its system and publishes the tile's partial sums in
-// the tile's own slot.  The warp that completes a system's last tile of the
-// step sums that system's tile slots in a fixed order and advances the
-// system's state, which lives in device memory.  No block-wide barrier runs
-// inside a step; one grid barrier ends it, and its last arriving block reads
-// how many systems are done and publishes "all done" with the new generation.
+// but no block is tied to a system and no grid barrier separates the steps.
+// Every system is cut into warp tiles of 32 x spt consecutive sites (all R
+// right-hand sides of a site together, so a tile reads each hop block once for
+// R spinors).  A work item is one step of one tile, numbered
+// step * ntiles + tile, and each warp takes items in increasing order from one
+// counter (prefetching the next while it works).  A step of a system only
+// depends on that system's previous step, so before working on an item the
+// warp waits until its system has completed the previous step (a per-system
+// epoch, release/acquire); systems in different steps overlap freely.  The
+// warp publishes the tile's partial sums in the tile's own slot; the warp that
+// completes a system's last tile of a step sums the slots in a fixed order,
+// advances the system's state (in device memory) and releases the next step.
+// Tiles of finished systems are skipped; every warp leaves when all systems
+// are done.
 //
-// Against the static schedule (each system owns a fixed range of blocks for
-// the whole solve) this keeps every warp busy until the step's tile list is
-// empty: a system that needs more iterations than the others is worked on by
-// the whole GPU once the others finish, uneven tiles even out within a step,
-// and the per-system scalars leave the registers.  Sums are over fixed tile
-// slots in a fixed order, so results do not depend on which warp took which
-// tile: a replay gives bit-identical iterates.
+// No deadlock: items are taken in order, so every item of step k was taken
+// before any of step k + 1, and the lowest step held by any warp can always
+// proceed.  Against the static schedule (each system owns a fixed range of
+// blocks for the whole solve) the whole GPU works on whatever systems are
+// still running, and a slow tile delays only its own system.  Sums are over
+// fixed tile slots in a fixed order, so results do not depend on which warp
+// took which tile: a replay gives bit-identical iterates.
 //
 // Counters and states are zeroed before each launch (stream-ordered memsets),
-// and every wait is bounded as in the other persistent kernels.
+// and every wait is bounded: on expiry the warp sets the abort flag, every
+// warp leaves, and the unfinished systems report a timeout.
 
 #include <cuda_runtime.h>
 
@@ -36,51 +39,6 @@ namespace qed3 {
 namespace {
 
 enum DynPhase { D_INIT = 0, D_A = 1, D_B = 2, D_R1 = 3, D_R2 = 4, D_DONE = 5 };
-
-// Grid barrier ending a step.  The last arriving block reads the number of
-// finished systems (every finisher of the step incremented it before its block
-// arrived) and publishes all-done in the top bit of the new generation, so all
-// blocks leave at the same barrier.  Bounded: on expiry it sets `abort`.
-__device__ __forceinline__ bool step_barrier(GridBar* bar, unsigned int& gen, long long spin_limit,
-                                             const int* ndone, int nsys, int& all_done) {
-  __syncthreads();
-  __shared__ int s_ok, s_all;
-  if (threadIdx.x == 0) {
-    int ok = 1, all = 0;
-    __threadfence();
-    const unsigned int prev = atomicAdd(&bar->count, 1u);
-    if (prev == gridDim.x - 1) {
-      __threadfence();
-      all = ld_volatile_int(ndone) >= nsys ? 1 : 0;
-      atomicExch(&bar->count, 0u);
-      __threadfence();
-      st_release(&bar->gen, ((gen + 1u) & 0x7fffffffu) | (unsigned(all) << 31));
-    } else {
-      long long spins = 0;
-      unsigned int g;
-      while (((g = ld_acquire(&bar->gen)) & 0x7fffffffu) == (gen & 0x7fffffffu)) {
-        if (ld_volatile_int(&bar->abort)) {
-          ok = 0;
-          break;
-        }
-        if (++spins > spin_limit) {
-          atomicExch(&bar->abort, 1);
-          ok = 0;
-          break;
-        }
-        __nanosleep(40);
-      }
-      all = int(g >> 31);
-    }
-    if (ld_volatile_int(&bar->abort)) ok = 0;
-    gen = (gen + 1u) & 0x7fffffffu;
-    s_ok = ok;
-    s_all = all;
-  }
-  __syncthreads();
-  all_done = s_all;
-  return s_ok != 0;
-}
 
 // The state transition of one system after a step, from its totals
 // tot[3 r + q] (q = 0: the phase's squared norm, 1/2: Re/Im <r, p> after a
@@ -558,6 +516,15 @@ __device__ __forceinline__ void tile_R2(const BatchSys& S, int i0, int spt, cons
   }
 }
 
+__device__ __forceinline__ int ld_acquire_s32(const int* p) {
+  int v;
+  asm volatile("ld.acquire.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_release_s32(int* p, int v) {
+  asm volatile("st.release.gpu.global.s32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
 // Register budgets: one right-hand side per system runs at 64 registers (1024
 // threads per SM, a few bytes spilled); tiles of 2 and 4 take 128 (measured
 // faster than 64 with their spills on the 256-right-hand-side batch); 8 up to 255.
@@ -565,7 +532,6 @@ template <int P, int R, int T>
 __global__ void __launch_bounds__(T, (R == 1 ? 1024 / T : R <= 4 ? 512 / T : 256 / T)) k_batched_dyn(DynArgs a) {
   constexpr int NQ = 3 * R;
   constexpr int NW = T / 32;
-  constexpr int TT = (32 / NQ) * NQ;  // lanes of the finisher's strided sum
   constexpr bool mixed = (P != P64);
   static_assert(NQ <= 32, "one warp finishes a system");
   // per-warp coefficients of the tile's system and the finisher's scratch
@@ -575,112 +541,151 @@ __global__ void __launch_bounds__(T, (R == 1 ? 1024 / T : R <= 4 ? 512 / T : 256
   __shared__ double s_tot[NW][NQ];
 
   DynState<R>* ds = reinterpret_cast<DynState<R>*>(a.state);
-  int* sys_cnt = a.counters;
-  int* step_cnt = a.counters + a.nsys;
-  int* ndone = a.counters + a.nsys + 2;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const unsigned full = 0xffffffffu;
-  unsigned int gen = 0;
-  int par = 0;
+  const unsigned long long NT = (unsigned long long)a.ntiles;
+  bool aborted = false;
 
+  // work item = step * ntiles + tile, taken in increasing order; the next one
+  // is fetched while the current one is worked on
+  unsigned long long next = 0;
+  if (lane == 0) next = atomicAdd(a.work, 1ull);
   while (true) {
-    int* cnt = step_cnt + par;
-    int next = 0;
+    const unsigned long long item = __shfl_sync(full, next, 0);
+    const int step = int(item / NT);
+    const int g = int(item - (unsigned long long)step * NT);
+    const int sidx = __ldg(a.sys_of_tile + g);
+    const BatchSys& S = a.sys[sidx];
+    volatile DynState<R>* d = ds + sidx;
+    int st = D_DONE, xsel = 0, quit = 0;
     if (lane == 0) {
-      next = atomicAdd(cnt, 1);
-      // the other counter served the previous step, which every block has left
-      if (blockIdx.x == 0 && w == 0) step_cnt[par ^ 1] = 0;
+      next = atomicAdd(a.work, 1ull);
+      // wait until this system has finished step - 1: then its state is the
+      // one of this step (a finished system's tiles are skipped)
+      long long spins = 0;
+      while (true) {
+        if (d->state == D_DONE) break;
+        if (ld_acquire_s32(a.epoch + sidx) >= step) {
+          st = d->state;
+          break;
+        }
+        if (ld_volatile_int(&a.bar->abort)) {
+          quit = 2;
+          break;
+        }
+        if (++spins > a.spin_limit) {
+          atomicExch(&a.bar->abort, 1);
+          quit = 2;
+          break;
+        }
+        __nanosleep(32);
+      }
+      if (!quit) {
+        if (st == D_DONE) {
+          atomicMax(a.work, (unsigned long long)step * NT + (unsigned long long)S.ch1);  // skip its other tiles
+          if (ld_volatile_int(a.ndone) >= a.nsys) quit = 1;  // every system finished: leave
+        } else {
+          xsel = d->xsel;
+        }
+      }
     }
-    while (true) {
-      const int g = __shfl_sync(full, next, 0);
-      if (g >= a.ntiles) break;
-      const int sidx = __ldg(a.sys_of_tile + g);
-      const BatchSys& S = a.sys[sidx];
-      volatile DynState<R>* d = ds + sidx;
-      int st = 0, xsel = 0;
-      if (lane == 0) {
-        next = atomicAdd(cnt, 1);  // the next tile, fetched while this one is worked on
-        st = d->state;
-        xsel = d->xsel;
-        if (st == D_DONE) atomicMax(cnt, S.ch1);  // skip the rest of a finished system
-      }
-      if (lane < R) {
-        s_act[w][lane] = d->active[lane];
-        s_beta[w][lane] = d->beta[lane];
-        s_arx[w][lane] = d->a_r[lane].x;
-        s_ary[w][lane] = d->a_r[lane].y;
-        s_alpha[w][lane] = d->alpha[lane];
-      }
-      st = __shfl_sync(full, st, 0);
-      xsel = __shfl_sync(full, xsel, 0);
-      __syncwarp();
-      if (st == D_DONE) continue;
+    quit = __shfl_sync(full, quit, 0);
+    if (quit) {
+      aborted = quit == 2;
+      break;
+    }
+    st = __shfl_sync(full, st, 0);
+    xsel = __shfl_sync(full, xsel, 0);
+    __syncwarp();  // orders lane 0's acquire before the other lanes' loads
+    if (st == D_DONE) continue;
+    if (lane < R) {
+      s_act[w][lane] = d->active[lane];
+      s_beta[w][lane] = d->beta[lane];
+      s_arx[w][lane] = d->a_r[lane].x;
+      s_ary[w][lane] = d->a_r[lane].y;
+      s_alpha[w][lane] = d->alpha[lane];
+    }
+    __syncwarp();
 
-      S64* xa = xsel ? S.xhi2 : S.xhi;
-      double v[NQ];
+    S64* xa = xsel ? S.xhi2 : S.xhi;
+    double v[NQ];
 #pragma unroll
-      for (int q = 0; q < NQ; q++) v[q] = 0.0;
-      const int i0 = (g - S.ch0) * 32 * a.spt + lane;
-      if (st == D_A) {
-        tile_A<P, R, 32>(S, i0, a.spt, s_act[w], s_beta[w], s_arx[w], s_ary[w], v);
-      } else if (st == D_B) {
-        tile_B<P, R, 32>(S, i0, a.spt, s_act[w], s_alpha[w], xa, v);
-      } else if (st == D_INIT) {
-        tile_init<P, R, 32>(S, i0, a.spt, xa, v);
-      } else if (st == D_R1) {
-        tile_R1<P, R, 32>(S, i0, a.spt, s_act[w], xa, xsel ? S.xhi : S.xhi2);
-      } else if (st == D_R2) {
-        tile_R2<P, R, 32>(S, i0, a.spt, s_act[w], xa, v);
+    for (int q = 0; q < NQ; q++) v[q] = 0.0;
+    const int i0 = (g - S.ch0) * 32 * a.spt + lane;
+    if (st == D_A) {
+      tile_A<P, R, 32>(S, i0, a.spt, s_act[w], s_beta[w], s_arx[w], s_ary[w], v);
+    } else if (st == D_B) {
+      tile_B<P, R, 32>(S, i0, a.spt, s_act[w], s_alpha[w], xa, v);
+    } else if (st == D_INIT) {
+      tile_init<P, R, 32>(S, i0, a.spt, xa, v);
+    } else if (st == D_R1) {
+      tile_R1<P, R, 32>(S, i0, a.spt, s_act[w], xa, xsel ? S.xhi : S.xhi2);
+    } else if (st == D_R2) {
+      tile_R2<P, R, 32>(S, i0, a.spt, s_act[w], xa, v);
+    }
+    // ---- the tile's partial sums into its slot; the last tile of the system finishes the step
+    if (st == D_R2) {
+#pragma unroll
+      for (int q = 0; q < NQ; q++) v[q] = warp_sum(v[q]);
+    } else {  // the other phases sum one norm per right-hand side
+#pragma unroll
+      for (int r = 0; r < R; r++) v[3 * r] = warp_sum(v[3 * r]);
+    }
+    int fin = 0;
+    if (lane == 0) {
+      double* pp = a.part + size_t(g) * NQ;
+#pragma unroll
+      for (int q = 0; q < NQ; q++) __stcg(pp + q, v[q]);
+      __threadfence();
+      const int prev = atomicAdd(a.sys_cnt + sidx, 1);
+      fin = (prev == S.ch1 - S.ch0 - 1);
+    }
+    fin = __shfl_sync(full, fin, 0);
+    if (fin) {
+      __threadfence();
+      // the system's totals from its tile slots, in a fixed order: lane l sums
+      // value l % nq of tiles l / nq, l / nq + 32 / nq, ... (four loads in
+      // flight), then lane q adds the lanes of value q in lane order.  Only
+      // the R2 step has three values per right-hand side; the others one.
+      const int nt = S.ch1 - S.ch0;
+      const int nq = st == D_R2 ? NQ : R, stride = st == D_R2 ? 1 : 3;
+      const int tl = 32 / nq, used = tl * nq;
+      double acc = 0.0;
+      if (lane < used) {
+        const double* base = a.part + size_t(S.ch0) * NQ + (lane % nq) * stride;
+        int t = lane / nq;
+        for (; t + 3 * tl < nt; t += 4 * tl) {
+          const double x0 = __ldcg(base + size_t(t) * NQ), x1 = __ldcg(base + size_t(t + tl) * NQ),
+                       x2 = __ldcg(base + size_t(t + 2 * tl) * NQ), x3 = __ldcg(base + size_t(t + 3 * tl) * NQ);
+          acc += x0;
+          acc += x1;
+          acc += x2;
+          acc += x3;
+        }
+        for (; t < nt; t += tl) acc += __ldcg(base + size_t(t) * NQ);
       }
-      // ---- the tile's partial sums into its slot; the last tile of the system finishes it
-      if (st == D_R2) {
-#pragma unroll
-        for (int q = 0; q < NQ; q++) v[q] = warp_sum(v[q]);
-      } else {  // the other phases sum one norm per right-hand side
-#pragma unroll
-        for (int r = 0; r < R; r++) v[3 * r] = warp_sum(v[3 * r]);
+      s_red[w][lane] = acc;
+      __syncwarp();
+      if (lane < NQ) s_tot[w][lane] = 0.0;
+      __syncwarp();
+      if (lane < nq) {
+        double t = 0.0;
+        for (int j = lane; j < used; j += nq) t += s_red[w][j];
+        s_tot[w][lane * stride] = t;
       }
-      int fin = 0;
+      __syncwarp();
       if (lane == 0) {
-        double* pp = a.part + size_t(g) * NQ;
-#pragma unroll
-        for (int q = 0; q < NQ; q++) __stcg(pp + q, v[q]);
+        a.sys_cnt[sidx] = 0;
+        dyn_transition<R>(a, S, sidx, d, s_tot[w], mixed, a.ndone);
         __threadfence();
-        const int prev = atomicAdd(sys_cnt + sidx, 1);
-        fin = (prev == S.ch1 - S.ch0 - 1);
+        st_release_s32(a.epoch + sidx, step + 1);  // the system's next step may start
       }
-      fin = __shfl_sync(full, fin, 0);
-      if (fin) {
-        __threadfence();
-        const int nt = S.ch1 - S.ch0;
-        double acc = 0.0;
-        if (lane < TT) {
-          const double* base = a.part + size_t(S.ch0) * NQ;
-          for (int e = lane; e < nt * NQ; e += TT) acc += __ldcg(base + e);
-        }
-        s_red[w][lane] = acc;
-        __syncwarp();
-        if (lane < NQ) {
-          double t = 0.0;
-          for (int j = lane; j < TT; j += NQ) t += s_red[w][j];
-          s_tot[w][lane] = t;
-        }
-        __syncwarp();
-        if (lane == 0) {
-          sys_cnt[sidx] = 0;
-          dyn_transition<R>(a, S, sidx, d, s_tot[w], mixed, ndone);
-        }
-        __syncwarp();
-      }
+      __syncwarp();
     }
-    int all = 0;
-    if (!step_barrier(a.bar, gen, a.spin_limit, ndone, a.nsys, all)) {
-      if (threadIdx.x == 0)
-        for (int s2 = blockIdx.x; s2 < a.nsys; s2 += gridDim.x) atomicCAS(a.status + s2, -1, QED3_ERR_TIMEOUT);
-      return;
-    }
-    if (all) break;
-    par ^= 1;
+  }
+  if (aborted && lane == 0) {
+    const int gw = blockIdx.x * NW + w, nw = gridDim.x * NW;
+    for (int s2 = gw; s2 < a.nsys; s2 += nw) atomicCAS(a.status + s2, -1, QED3_ERR_TIMEOUT);
   }
 }
 

@@ -49,9 +49,9 @@ struct BatchArgs {
 };
 
 // Dynamic schedule: the CG state of each system lives in device memory and
-// blocks take site tiles (T consecutive sites of one system, all its right-hand
-// sides) from a per-step counter; the block that completes a system's last
-// tile of the step reduces its tile partials and advances its state.
+// warps take work items (a step of one system's site tile) in order from one
+// counter; the warp that completes a system's last tile of a step reduces its
+// tile partials, advances its state and releases the system's next step.
 template <int R>
 struct DynState {
   int state, iter, nru, xsel;
@@ -66,8 +66,11 @@ struct DynArgs {
   const int* sys_of_tile;
   int ntiles;
   int spt;        // sites per thread in a tile (a tile is threads x spt consecutive sites)
-  void* state;    // DynState<R>[nsys]
-  int* counters;  // [nsys] tiles done this step, then [2] step tile counters, then [1] systems done
+  void* state;              // DynState<R>[nsys]
+  int* sys_cnt;              // [nsys] tiles of the current step done
+  int* epoch;                // [nsys] steps completed
+  unsigned long long* work;  // next work item (step * ntiles + tile)
+  int* ndone;                // systems finished
   double* part;   // [ntiles][3 R]
   GridBar* bar;
   int* status;
