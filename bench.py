@@ -23,6 +23,8 @@ the n=64 working set fits in it.
 `batched_256` (outside the headline): the multi-lattice batched configuration,
 256 right-hand sides (64 on each of n = 16, 32, 48, 64) solved to 1e-10 in one
 persistent launch per batch, beside the same 256 solves run one after another.
+`multi_rhs_n64`: 64 right-hand sides of the headline operator in one batched
+launch, beside the single-right-hand-side learned solver.
 
 --impl reference times the reference's algorithm on the host cores: the
 oracle's restatement of MatPoly::solve (src/dual/matpoly.h:204-267) over the
@@ -724,6 +726,29 @@ def batched_throughput(torch, Q, dev, reps=3):
             "speedup_vs_sequential": (256e3 / ms) / (256 / seq_s)}
 
 
+def multi_rhs_n64(torch, Q, dev, D, lat, single_ms, reps=3):
+    """64 right-hand sides of the headline operator (n=64, m=0.05) in one
+    batched persistent launch (autotuned tile, threads and schedule; plain CG,
+    FP32 iterations with FP64 reliable updates, each solution certified by its
+    FP64 true residual), against the single-right-hand-side learned solver."""
+    rng = np.random.default_rng(64)
+    b = torch.from_numpy(rng.normal(size=(64, 2 * lat.n_sites)) + 1j * rng.normal(size=(64, 2 * lat.n_sites))).to(dev)
+    batch = Q.Batch([(D, 64)], precision=Q.PREC_F32)
+    xs = [torch.zeros_like(b)]
+    ms_l, ok, iters = [], True, 0
+    for i in range(reps + 1):
+        reps_, ms = batch.solve(xs, [b], tol=TOL, precision=Q.PREC_F32, delta=RU_DELTA)
+        ok = ok and all(r.status == Q.OK and r.true_rel_res <= TOL for r in reps_)
+        iters = max(iters, max(r.iters for r in reps_))
+        if i > 0:
+            ms_l.append(ms)
+    ms = float(np.mean(ms_l))
+    return {"rhs": 64, "n": N_REFINE, "rhs_tile": batch.rhs_tile, "threads": batch.threads,
+            "schedule": {Q.BATCH_STATIC: "static", Q.BATCH_DYNAMIC: "dynamic"}[batch.schedule],
+            "ms_per_batch": ms, "solves_per_s": 64e3 / ms, "max_iters": iters, "certified": bool(ok),
+            "single_rhs_learned_solves_per_s": 1e3 / single_ms, "throughput_per_rhs_vs_single": (64e3 / ms) / (1e3 / single_ms)}
+
+
 def ref_gpu_baseline(A, b, reps=3):
     """The reference's GPU CG design on this GPU (oracle/ref_gpu_cg.cu) over
     the reference CSR operator of the workload; host-vector solves as the
@@ -817,7 +842,7 @@ def profile_case(torch, which):
             systems.append((D_n, 16))
             bs.append(torch.from_numpy(b_n).cuda())
         if which == "batched":
-            batch = Q.Batch(systems, precision=Q.PREC_F32, rhs_tile=1, threads=256, schedule=Q.BATCH_DYNAMIC)
+            batch = Q.Batch(systems, precision=Q.PREC_F32, rhs_tile=2, threads=256, schedule=Q.BATCH_DYNAMIC)
         else:
             batch = Q.Batch(systems, precision=Q.PREC_F32, rhs_tile=1, threads=128, schedule=Q.BATCH_STATIC)
         xs = [torch.zeros_like(b_) for b_ in bs]
@@ -977,6 +1002,7 @@ def main():
     train_info["depth_study"] = network_depth_study(torch, Q, lat, D, pc, dev)
     heldout = heldout_iterations(torch, Q, lat, pc, dev)
     batched = batched_throughput(torch, Q, dev)
+    multi64 = multi_rhs_n64(torch, Q, dev, D, lat, results[best]["ms"])
     paths = None if args.no_paths else paths_timings(torch, Q, dev, cpu=rank == 0 and not args.no_cpu_baseline)
     overlap32 = None if args.no_paths else overlap_config(torch, Q, dev)
     hbm_pcg = None if args.no_paths else learned_hbm(torch, Q, dev)
@@ -1053,6 +1079,7 @@ def main():
                                        "frac": hbm_apply["frac_of_" + peak_kind]}},
             "apply_sweep": sweep,
             "batched_256": batched,
+            "multi_rhs_n64": multi64,
             "overlap_n32": overlap32,
             "learned_pc_n256": hbm_pcg,
             "paths": paths,
