@@ -58,10 +58,16 @@ BETA = 1.4
 OV_MASS = 0.05  # overlap outer solve: D(m) = (1 - m/2) D_ov + m
 M5 = 0.05
 TOL = 1e-10
-# mixed-precision solves: an FP64 reliable update when |r| fell 100x since the last
-# one (delta = 0.01; each costs two FP64 stencil passes, the slow pipe on this
-# GPU); measured: the same iterations as delta = 0.1 with half the updates
+# FP32 solves: an FP64 reliable update when |r| fell 100x since the last one
+# (delta = 0.01; each costs two FP64 stencil passes, the slow pipe on this
+# GPU); measured: the same iterations as delta = 0.1 with half the updates.
+# BF16 halo copies keep delta = 0.1: their rounding (~4e-3) needs the more
+# frequent updates (at 0.01 the BF16 solvers stagnate).
 RU_DELTA = 0.01
+
+
+def ru_delta(Q, prec):
+    return RU_DELTA if prec == Q.PREC_F32 else 0.1
 # DRAM read + write bytes of one k_pcg launch at n=64 from an ncu capture
 # (--set full, one launch): the operator and vectors are loaded once, the
 # iterations run out of L2.
@@ -288,8 +294,8 @@ def time_solver(torch, Q, D, bt, prec, steps, warmup, flush, pc=None):
 
     def solve():
         if pc is not None:
-            return pc.solve(D, x, bt, tol=TOL, precision=prec, delta=RU_DELTA)
-        return D.solve(x, bt, tol=TOL, precision=prec, delta=RU_DELTA)
+            return pc.solve(D, x, bt, tol=TOL, precision=prec, delta=ru_delta(Q, prec))
+        return D.solve(x, bt, tol=TOL, precision=prec, delta=ru_delta(Q, prec))
 
     for _ in range(warmup):
         solve()
@@ -986,9 +992,9 @@ def main():
         e0.record(st)
         db.copy_(hb, non_blocking=True)
         if use_pc:
-            pc.solve(D, dx, db, tol=TOL, precision=prec_best, delta=RU_DELTA)
+            pc.solve(D, dx, db, tol=TOL, precision=prec_best, delta=ru_delta(Q, prec_best))
         else:
-            D.solve(dx, db, tol=TOL, precision=prec_best, delta=RU_DELTA)
+            D.solve(dx, db, tol=TOL, precision=prec_best, delta=ru_delta(Q, prec_best))
         hx.copy_(dx, non_blocking=True)
         e1.record(st)
         e1.synchronize()
@@ -1035,9 +1041,9 @@ def main():
     # ---- launches of this library's kernels in the timed region ------------------------
     def one_step():
         if use_pc:
-            pc.solve(D, dx, db, tol=TOL, precision=prec_best, delta=RU_DELTA)
+            pc.solve(D, dx, db, tol=TOL, precision=prec_best, delta=ru_delta(Q, prec_best))
         else:
-            D.solve(dx, db, tol=TOL, precision=prec_best, delta=RU_DELTA)
+            D.solve(dx, db, tol=TOL, precision=prec_best, delta=ru_delta(Q, prec_best))
     try:
         ours1, all1 = count_launches(torch, one_step)
         launches = {"per_step": ours1, "per_step_all_kernels": all1,
@@ -1063,7 +1069,7 @@ def main():
             "solver": (f"learned-preconditioned persistent CG, {best[4:]} inner, FP64 reliable updates"
                        if use_pc else f"persistent CG, {best} inner, FP64 reliable updates"),
             "hmc_acceptance": acc,
-            "solvers": results, "reliable_update_delta": RU_DELTA,
+            "solvers": results, "reliable_update_delta": {"f32": RU_DELTA, "bf16": 0.1},
             "speedup_vs_plain_f64": results["f64"]["ms"] / results[best]["ms"],
             "preconditioner": train_info,
             "heldout": heldout,

@@ -772,13 +772,29 @@ void orc_dirac_get_kappa(const OracleDirac* d, double* kappa) {
   std::memcpy(kappa, d->kappa.data(), sizeof(double) * d->kappa.size());
 }
 
+// <x, y> summed in fixed chunks (each chunk in index order, then the chunk
+// sums in order), so the result does not depend on the number of threads:
+// BiCGStab on the non-normal D amplifies rounding differences, and a
+// thread-count-dependent sum made its convergence depend on the machine.
 static cplx zdotc(const cplx* x, const cplx* y, Idx n) {
+  constexpr Idx C = 4096;
+  const Idx nc = (n + C - 1) / C;
+  std::vector<cplx> part(nc);
+#pragma omp parallel for schedule(static)
+  for (Idx c = 0; c < nc; c++) {
+    double re = 0, im = 0;
+    const Idx e = std::min(n, (c + 1) * C);
+    for (Idx i = c * C; i < e; i++) {
+      const cplx t = std::conj(x[i]) * y[i];
+      re += t.real();
+      im += t.imag();
+    }
+    part[c] = {re, im};
+  }
   double re = 0, im = 0;
-#pragma omp parallel for reduction(+ : re, im) schedule(static)
-  for (Idx i = 0; i < n; i++) {
-    const cplx t = std::conj(x[i]) * y[i];
-    re += t.real();
-    im += t.imag();
+  for (Idx c = 0; c < nc; c++) {
+    re += part[c].real();
+    im += part[c].imag();
   }
   return {re, im};
 }

@@ -516,15 +516,6 @@ __device__ __forceinline__ void tile_R2(const BatchSys& S, int i0, int spt, cons
   }
 }
 
-__device__ __forceinline__ int ld_acquire_s32(const int* p) {
-  int v;
-  asm volatile("ld.acquire.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
-  return v;
-}
-__device__ __forceinline__ void st_release_s32(int* p, int v) {
-  asm volatile("st.release.gpu.global.s32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
-}
-
 // Register budgets: one right-hand side per system runs at 64 registers (1024
 // threads per SM, a few bytes spilled); tiles of 2 and 4 take 128 (measured
 // faster than 64 with their spills on the 256-right-hand-side batch); 8 up to 255.
@@ -562,24 +553,9 @@ __global__ void __launch_bounds__(T, (R == 1 ? 1024 / T : R <= 4 ? 512 / T : 256
       next = atomicAdd(a.work, 1ull);
       // wait until this system has finished step - 1: then its state is the
       // one of this step (a finished system's tiles are skipped)
-      long long spins = 0;
-      while (true) {
-        if (d->state == D_DONE) break;
-        if (ld_acquire_s32(a.epoch + sidx) >= step) {
-          st = d->state;
-          break;
-        }
-        if (ld_volatile_int(&a.bar->abort)) {
-          quit = 2;
-          break;
-        }
-        if (++spins > a.spin_limit) {
-          atomicExch(&a.bar->abort, 1);
-          quit = 2;
-          break;
-        }
-        __nanosleep(32);
-      }
+      const int wr = wait_step(a.epoch + sidx, step, &d->state, D_DONE, &a.bar->abort, a.spin_limit);
+      if (wr == 0) st = d->state;
+      if (wr == 2) quit = 2;
       if (!quit) {
         if (st == D_DONE) {
           atomicMax(a.work, (unsigned long long)step * NT + (unsigned long long)S.ch1);  // skip its other tiles

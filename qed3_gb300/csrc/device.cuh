@@ -252,6 +252,35 @@ __device__ __forceinline__ bool grid_sync(GridBar* bar, unsigned int& gen, long 
   return s_ok != 0;
 }
 
+// ---- per-system step wait (dynamic batched schedule) ---------------------------
+__device__ __forceinline__ int ld_acquire_s32(const int* p) {
+  int v;
+  asm volatile("ld.acquire.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_release_s32(int* p, int v) {
+  asm volatile("st.release.gpu.global.s32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// Waits (one thread) until *epoch >= step, i.e. the system has completed the
+// step before `step`, or until its state reads `done_state`.  Returns 0 when
+// the step may start, 1 when the system is done, 2 when the wait ran out
+// (after spin_limit polls it raises *abort) or another wait raised *abort.
+__device__ __forceinline__ int wait_step(const int* epoch, int step, const volatile int* state, int done_state,
+                                         int* abort, long long spin_limit) {
+  long long spins = 0;
+  while (true) {
+    if (*state == done_state) return 1;
+    if (ld_acquire_s32(epoch) >= step) return 0;
+    if (ld_volatile_int(abort)) return 2;
+    if (++spins > spin_limit) {
+      atomicExch(abort, 1);
+      return 2;
+    }
+    __nanosleep(32);
+  }
+}
+
 // ---- grid barrier, monotonic form -------------------------------------------
 // The arrival counter and the generation only grow within a launch (both are
 // zeroed before it), so no reset sits on the critical path: the block whose
