@@ -131,8 +131,11 @@ def _crel(a, b):
     return float(np.abs(a - b).max() / np.abs(b).max())
 
 
-@pytest.mark.parametrize("C,LG", [(8, 1), (8, 2), (16, 2)])
+@pytest.mark.parametrize("C,LG", [(8, 1), (8, 2), (16, 2), (16, 3)])
 def test_lpc_forward_matches_torch(cuda, C, LG):
+    """Layer by layer (form 0) and in the solver's collapsed form (form 1,
+    up to two layers; the 3-layer 16-channel network of the learned-
+    preconditioner configuration runs layer by layer)."""
     rng, g, lat, Do, Dq, pc, tn = _net(8, C, LG)
     if C == 16:
         pc.set_tensor_cores(False)  # FP32 CUDA-core mixing; the tensor-core path is checked below
@@ -146,6 +149,10 @@ def test_lpc_forward_matches_torch(cuda, C, LG):
         zr = tn(torch.tensor(r.reshape(B, Ns, 2), dtype=torch.complex64)).numpy().reshape(-1)
     assert _crel(from_dev(z0), zr) < 2e-5
     z1 = torch.zeros_like(rt)
+    if LG > 2:
+        with pytest.raises(Q.Qed3Error):
+            pc.apply(z1, rt, nrhs=B, form=1)
+        return
     pc.apply(z1, rt, nrhs=B, form=1)
     assert _crel(from_dev(z1), zr) < 2e-5
 
@@ -167,7 +174,7 @@ def test_lpc_hermitian_positive(cuda):
     assert np.vdot(u, Nu).real >= a2 * np.vdot(u, u).real * (1 - 1e-5)
 
 
-@pytest.mark.parametrize("C,LG", [(8, 1), (8, 2), (16, 1), (16, 2)])
+@pytest.mark.parametrize("C,LG", [(8, 1), (8, 2), (16, 1), (16, 2), (16, 3)])
 def test_lpc_gradient_matches_autograd(cuda, C, LG):
     rng, g, lat, Do, Dq, pc, tn = _net(8, C, LG)
     if LG == 1:
