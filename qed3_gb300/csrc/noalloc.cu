@@ -15,8 +15,7 @@
 //    every GPU that loads the library until the process exits
 //    (QED3_NOALLOC_MAX_SITES x 10 fields x 32 B + ~5 KB = about 6.6 MB).
 //  * The first call on each device looks up the array's device address
-//    (cudaGetSymbolAddress) with that device current; make that first call
-//    before any stream capture begins.
+//    (cudaGetSymbolAddress) with that device current.
 //  * All calls share the one array, which keeps the previous call's contents;
 //    the barrier state is cleared by every call and every field is
 //    initialised by the kernel.  Calls whose executions overlap on the GPU
