@@ -205,8 +205,8 @@ int qed3_bicgstab_solve(qed3_dirac* d, int op, double* x, const double* b, const
  * (about 6.6 MB, held by every GPU that loads the library until exit), so
  * lattices are limited to QED3_NOALLOC_MAX_SITES sites (n_refine <= 32);
  * larger ones return QED3_ERR_ARG.  The first call on a device looks up the
- * array's address and should precede any stream capture.  All calls share
- * the array: calls that overlap on the GPU race and must be serialised. */
+ * array's address.  All calls share the array: calls that overlap on the GPU
+ * race and must be serialised. */
 #define QED3_NOALLOC_MAX_SITES 20480
 int qed3_cg_solve_noalloc(qed3_dirac* d, double* x, const double* b, const qed3_solve_params* params,
                           qed3_solve_report* report, void* stream);
