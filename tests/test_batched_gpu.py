@@ -166,14 +166,15 @@ def test_batched_graph_capture_replay(cuda, sched):
                 assert res <= 1.05e-10, (trial, r, res)
 
 
+@pytest.mark.parametrize("sched", [Q.BATCH_STATIC, Q.BATCH_DYNAMIC])
 @pytest.mark.parametrize("scale", [1e-30, 1e30])
-def test_batched_scale_invariance(cuda, scale):
+def test_batched_scale_invariance(cuda, scale, sched):
     """Right-hand sides far from unit scale: the reduced-precision iterations run
     on b / |b|, so the solution is the unit-scale solution times the scale (to
     the tolerance) instead of an FP32 underflow or overflow."""
     sy = _systems(cuda, ns=(4,), nrhs=(3,), seed=55)
     g, lat, Do, Dq, b = sy[0]
-    batch = Q.Batch([(Dq, 3)], precision=Q.PREC_F32, rhs_tile=4, threads=128)
+    batch = Q.Batch([(Dq, 3)], precision=Q.PREC_F32, rhs_tile=4, threads=128, schedule=sched)
     bt = to_dev(b, cuda)
     x1 = [bt.clone() * 0]
     reps1, _ = batch.solve(x1, [bt], tol=1e-12, precision=Q.PREC_F32)
