@@ -945,7 +945,7 @@ def main():
         line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "solves/s", "n_gpus": 0,
                 "steps": args.steps, "warmup": warmup, "ms_per_step": 1e3 * sum(times) / len(times),
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-                "data": "synthetic", "config": config(1),
+                "data": "synthetic", "config": config(world),
                 "solver": "reference CG (MatPoly::solve) restated over the reference CSR operator",
                 "iters": int(np.median(its)), "hmc_acceptance": acc,
                 "cpu_baseline": {"value": v, "unit": "solves/s", "cores": cores, "kind": "port",
