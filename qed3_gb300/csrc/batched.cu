@@ -21,6 +21,11 @@
 // This replaces, for a batch, what the reference does with one MatPoly::solve
 // per right-hand side and per pole on OpenMP threads driving CUDA streams
 // (src/both_3d/overlap.h:309-332, src/dual/matpoly.h:204-267).
+//
+// This file holds the static schedule (each system owns a range of blocks,
+// re-split after every synchronous solve by the iterations each system took),
+// the host side of both schedules and the autotuner; batched_dyn.cu holds the
+// dynamic schedule's kernel (warp tiles, no grid barrier).
 
 #include <algorithm>
 #include <cmath>
