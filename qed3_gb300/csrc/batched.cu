@@ -185,6 +185,10 @@ __global__ void __launch_bounds__(T, (R <= 4 ? 1024 / T : 1)) k_batched_cg(Batch
         }
       }
     } else if (st == ST_A) {
+      // mixed: FP32 sums over the thread's sites, FP64 from the block sum on
+      float vf[R];
+#pragma unroll
+      for (int r = 0; r < R; r++) vf[r] = 0.f;
       for (int i = tid; i < Ns; i += nth) {
         const int j0 = __ldg(S.nbr + i), j1 = __ldg(S.nbr + Ns + i), j2 = __ldg(S.nbr + 2 * Ns + i);
         if constexpr (!mixed) {
@@ -250,11 +254,17 @@ __global__ void __launch_bounds__(T, (R <= 4 ? 1024 / T : 1)) k_batched_cg(Batch
             st32(p32, e, pn);
             const float tt = tn.s0.x * tn.s0.x + tn.s0.y * tn.s0.y + tn.s1.x * tn.s1.x + tn.s1.y * tn.s1.y;
             const float pp = pn.s0.x * pn.s0.x + pn.s0.y * pn.s0.y + pn.s1.x * pn.s1.x + pn.s1.y * pn.s1.y;
-            v[3 * r] += double(tt) + S.shift[r] * double(pp);
+            vf[r] += tt + float(S.shift[r]) * pp;
           }
         }
       }
+      if constexpr (mixed)
+#pragma unroll
+        for (int r = 0; r < R; r++) v[3 * r] += double(vf[r]);
     } else if (st == ST_B) {
+      float vf[R];
+#pragma unroll
+      for (int r = 0; r < R; r++) vf[r] = 0.f;
       for (int i = tid; i < Ns; i += nth) {
         const int j0 = __ldg(S.nbr + i), j1 = __ldg(S.nbr + Ns + i), j2 = __ldg(S.nbr + 2 * Ns + i);
         if constexpr (!mixed) {
@@ -315,10 +325,13 @@ __global__ void __launch_bounds__(T, (R <= 4 ? 1024 / T : 1)) k_batched_cg(Batch
             st32(r32, e, rn);
             if constexpr (P == PBF16) stbf(reinterpret_cast<uint2*>(rh), e, rn);
             st32(xlo, e, xn);
-            v[3 * r] += double(rn.s0.x * rn.s0.x + rn.s0.y * rn.s0.y + rn.s1.x * rn.s1.x + rn.s1.y * rn.s1.y);
+            vf[r] += rn.s0.x * rn.s0.x + rn.s0.y * rn.s0.y + rn.s1.x * rn.s1.x + rn.s1.y * rn.s1.y;
           }
         }
       }
+      if constexpr (mixed)
+#pragma unroll
+        for (int r = 0; r < R; r++) v[3 * r] += double(vf[r]);
     } else if (st == ST_R1) {
       // t64 = D (x_hi + x_lo);  x_hi2 = x_hi + x_lo
       for (int i = tid; i < Ns; i += nth) {
