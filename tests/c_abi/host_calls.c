@@ -27,7 +27,14 @@ int main(void) {
   qed3_rng* rng = NULL;
   double g[3];
   if (qed3_rng_create(3, 1, 7, &rng) != QED3_OK || qed3_rng_gaussian_links(rng, 1.0, g) != QED3_OK) return 7;
-  printf("%d %d %d %d %.17g %d %d %.17g %.17g\n", ns, nl, nf, ft, ell[0], rc_bad, size, scal[3], g[0]);
+  /* argument checks of the batched solver (no device work): no systems, unknown schedule */
+  qed3_batch* bt = NULL;
+  const int nr1 = 1;
+  const int rc_b0 = qed3_batch_create2(0, NULL, &nr1, QED3_PREC_F32, 0, 0, 0, &bt);
+  int sched = 0;
+  const int rc_b1 = qed3_batch_schedule(NULL, &sched);
+  printf("%d %d %d %d %.17g %d %d %.17g %.17g %d %d\n", ns, nl, nf, ft, ell[0], rc_bad, size, scal[3], g[0], rc_b0,
+         rc_b1);
   printf("%s\n", qed3_last_error_string() ? "message" : "none");
   qed3_rng_destroy(rng);
   qed3_lattice_destroy(lat2);

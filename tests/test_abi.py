@@ -72,6 +72,7 @@ def test_header_is_plain_c_and_c_plus_plus(tmp_path):
         class Sizes:
             n_links, n_sites = 3, 1
         assert float(f[8]) == O.Rng(Sizes(), 7).gaussian_links(1.0)[0]
+        assert int(f[9]) == Q.ERR_ARG and int(f[10]) == Q.ERR_ARG  # batch argument checks
         assert out[1] == "message"
 
 
