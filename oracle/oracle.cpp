@@ -236,6 +236,7 @@ struct OracleGeom {
   std::vector<std::array<Idx, 3>> hop_link;   // link id of hop (x, nns[x][k])
   std::vector<std::array<int, 3>> hop_sign;   // +1 if x<y
   std::map<std::pair<Idx, Idx>, Idx> map2il;
+  std::vector<Idx> face_link;  // link of each face edge in ring order, faces in order (face_links)
 };
 
 static void build_vertices(OracleGeom& g, const Icosa& ic) {
@@ -988,14 +989,28 @@ int orc_zolotarev(double k, int n, double* c, double* cp, double* A, double* sca
 // compact: S = -beta sum w_p cos(theta_p); force_mode 0 = the reference's
 // (theta_p, src/dual/action.h:37), 1 = exact (sin theta_p).
 // ===========================================================================
+// The link of every edge of every dual face (faces in order, edges in ring
+// order), looked up in map2il once per geometry: the plaquette and gauge-force
+// loops below visit the same links in the same order as with a lookup per edge
+// (the reference's U(Link) map access), without its O(log Nl) cost per edge.
+static const std::vector<Idx>& face_links(const OracleGeom* g) {
+  if (g->face_link.empty()) {
+    std::vector<Idx>& fl = const_cast<OracleGeom*>(g)->face_link;
+    for (const auto& f : g->faces)
+      for (size_t i = 0; i < f.size(); i++) fl.push_back(g->map2il.at({f[i], f[(i + 1) % f.size()]}));
+  }
+  return g->face_link;
+}
+
 void orc_plaquettes(const OracleGeom* g, const double* A, double* theta) {
+  const std::vector<Idx>& fl = face_links(g);
+  size_t e = 0;
   for (size_t v = 0; v < g->faces.size(); v++) {
     const auto& f = g->faces[v];
     double s = 0;
-    for (size_t i = 0; i < f.size(); i++) {
+    for (size_t i = 0; i < f.size(); i++, e++) {
       const Idx a = f[i], b = f[(i + 1) % f.size()];
-      const Idx l = g->map2il.at({a, b});
-      s += (a < b ? 1.0 : -1.0) * A[l];
+      s += (a < b ? 1.0 : -1.0) * A[fl[e]];
     }
     theta[v] = s;
   }
@@ -1019,13 +1034,15 @@ void orc_gauge_force(const OracleGeom* g, const double* A, double beta, int comp
   for (size_t l = 0; l < Nl; l++) F[l] = 0.0;
   std::vector<double> th(g->faces.size());
   orc_plaquettes(g, A, th.data());
+  const std::vector<Idx>& fl = face_links(g);
+  size_t e = 0;
   for (size_t v = 0; v < g->faces.size(); v++) {
     const auto& f = g->faces[v];
     const double w = g->mean_vol / g->vols[v];
     const double gr = w * ((compact && force_mode == 1) ? std::sin(th[v]) : th[v]);
-    for (size_t i = 0; i < f.size(); i++) {
+    for (size_t i = 0; i < f.size(); i++, e++) {
       const Idx a = f[i], b = f[(i + 1) % f.size()];
-      F[g->map2il.at({a, b})] += gr * (a < b ? 1.0 : -1.0);
+      F[fl[e]] += gr * (a < b ? 1.0 : -1.0);
     }
   }
   for (size_t l = 0; l < Nl; l++) F[l] *= beta;
